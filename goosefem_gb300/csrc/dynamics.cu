@@ -1,0 +1,443 @@
+// Fused explicit velocity-Verlet increment (element kernel + node kernel) and the FP64 probe.
+//
+// Element kernels (one thread per element) turn the nodal displacement into element forces
+// fe [nelem, nne, ndim]:
+//  * general path: gather ue through conn, then per Gauss point symGradN (stored dNx), linear
+//    elastic stress and the int_gradN_dot_tensor2_dV accumulation, in the operation order of
+//    ElementQuad4.h:407-491 / Element.h:991-1022 + ElementHex8.h:355-383;
+//  * uniform Quad4 path: for meshes of congruent axis-aligned rectangles with the 2x2 Gauss rule
+//    the same integral is evaluated from the four "Walsh" combinations of the nodal values
+//    (mean gradient + hourglass mode); the Gauss sums are done in closed form, which needs about
+//    a quarter of the FP64 instructions (FP64 issue rate, not HBM, bounds this kernel on GB300).
+// The node kernel (one thread per node-dof) gathers fe through the dof CSR in ascending
+// (e, m, i) order (the serial order of Vector.h:724-741, deterministic), then performs the three
+// velocity estimates of docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:129-157 and the
+// displacement predictor of the next increment (main.cpp:119).
+#include <cmath>
+
+#include "common.cuh"
+
+namespace gfgpu {
+
+// ------------------------------------------------------------------ element kernels
+
+template <bool S, int NNE, int ND>
+__global__ void __launch_bounds__(128)
+k_elem_force_general(const int32_t* __restrict__ conn, const double* __restrict__ u,
+                     const double* __restrict__ dNx, const double* __restrict__ vol,
+                     const double* __restrict__ Km, const double* __restrict__ Gm, int64_t nelem,
+                     int nip, double* __restrict__ fe)
+{
+    GF_FOR(e, nelem)
+    {
+        double ue[NNE * ND];
+#pragma unroll
+        for (int m = 0; m < NNE; ++m) {
+            int64_t n = __ldg(conn + e * NNE + m);
+#pragma unroll
+            for (int i = 0; i < ND; ++i) ue[m * ND + i] = __ldg(u + n * ND + i);
+        }
+        double K = __ldg(Km + e), G = __ldg(Gm + e);
+        double g2 = mul<S>(2.0, G);
+        double f[NNE * ND];
+#pragma unroll
+        for (int k = 0; k < NNE * ND; ++k) f[k] = 0.0;
+        for (int q = 0; q < nip; ++q) {
+            int64_t t = e * nip + q;
+            double g[NNE * ND];
+            const double2* gp = reinterpret_cast<const double2*>(dNx + t * NNE * ND);
+#pragma unroll
+            for (int k = 0; k < NNE * ND / 2; ++k) {
+                double2 v2 = __ldg(gp + k);
+                g[2 * k] = v2.x;
+                g[2 * k + 1] = v2.y;
+            }
+            double v = __ldg(vol + t);
+            double eps[ND * ND];
+            if constexpr (ND == 2) {
+                // ElementQuad4.h:407-434
+                double e00 = mul<S>(g[0], ue[0]);
+                e00 = madd<S>(g[2], ue[2], e00);
+                e00 = madd<S>(g[4], ue[4], e00);
+                e00 = madd<S>(g[6], ue[6], e00);
+                double e11 = mul<S>(g[1], ue[1]);
+                e11 = madd<S>(g[3], ue[3], e11);
+                e11 = madd<S>(g[5], ue[5], e11);
+                e11 = madd<S>(g[7], ue[7], e11);
+                double s = mul<S>(g[0], ue[1]);
+                s = madd<S>(g[2], ue[3], s);
+                s = madd<S>(g[4], ue[5], s);
+                s = madd<S>(g[6], ue[7], s);
+                s = madd<S>(g[1], ue[0], s);
+                s = madd<S>(g[3], ue[2], s);
+                s = madd<S>(g[5], ue[4], s);
+                s = madd<S>(g[7], ue[6], s);
+                s = mul<S>(0.5, s);
+                eps[0] = e00; eps[1] = s; eps[2] = s; eps[3] = e11;
+            }
+            else {
+                // Element.h:991-1022
+#pragma unroll
+                for (int k = 0; k < 9; ++k) eps[k] = 0.0;
+#pragma unroll
+                for (int m = 0; m < NNE; ++m)
+#pragma unroll
+                    for (int i = 0; i < 3; ++i)
+#pragma unroll
+                        for (int j = 0; j < 3; ++j) {
+                            double h = mul<S>(0.5, g[m * 3 + i]);
+                            eps[i * 3 + j] = madd<S>(h, ue[m * 3 + j], eps[i * 3 + j]);
+                            eps[j * 3 + i] = madd<S>(h, ue[m * 3 + j], eps[j * 3 + i]);
+                        }
+            }
+            // sigma = K tr I + 2G (eps - tr/3 I)
+            double tr = 0.0;
+#pragma unroll
+            for (int i = 0; i < ND; ++i) tr = add<S>(tr, eps[i * ND + i]);
+            double Kt = mul<S>(K, tr);
+            double mth = __ddiv_rn(tr, 3.0);
+            double sig[ND * ND];
+#pragma unroll
+            for (int i = 0; i < ND; ++i)
+#pragma unroll
+                for (int j = 0; j < ND; ++j)
+                    sig[i * ND + j] = (i == j) ? madd<S>(g2, sub<S>(eps[i * ND + j], mth), Kt)
+                                               : mul<S>(g2, eps[i * ND + j]);
+            // ElementQuad4.h:467-491 / ElementHex8.h:355-383
+#pragma unroll
+            for (int m = 0; m < NNE; ++m)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) {
+                    double acc = mul<S>(g[m * ND + 0], sig[0 * ND + j]);
+#pragma unroll
+                    for (int i = 1; i < ND; ++i) acc = madd<S>(g[m * ND + i], sig[i * ND + j], acc);
+                    f[m * ND + j] = madd<S>(acc, v, f[m * ND + j]);
+                }
+        }
+        double2* fo = reinterpret_cast<double2*>(fe + e * NNE * ND);
+#pragma unroll
+        for (int k = 0; k < NNE * ND / 2; ++k) fo[k] = make_double2(f[2 * k], f[2 * k + 1]);
+    }
+}
+
+// Constants of the uniform Quad4 path (see k_elem_force_quad4_uniform).
+struct Quad4Uniform {
+    double ax, ay;  // 1 / (2 hx), 1 / (2 hy): dNx(m,0) = ax s_xi(m) (1 + s_eta(m) eta), ...
+    double cx, cy;  // 4 vol ax, 4 vol ay (vol = hx hy / 4 per Gauss point)
+    double hx2, hy2; // (4/3) g^2-weighted hourglass factors: 4 g^2 vol ax^2, 4 g^2 vol ay^2
+};
+
+// Uniform Quad4: with A1 = -u0+u1+u2-u3, A2 = -u0-u1+u2+u3, A3 = u0-u1+u2-u3 (per component),
+// the gradient at Gauss point (xi, eta) is du_j/dx = ax (A1_j + eta A3_j),
+// du_j/dy = ay (A2_j + xi A3_j). With the 2x2 rule (sum 1 = 4, sum xi = sum eta = sum xi eta = 0,
+// sum xi^2 = sum eta^2 = 4 g^2) the force splits into the mean-stress part and the hourglass
+// part:  f(m,j) = s_xi(m) P_j + s_eta(m) Q_j + s_xi(m) s_eta(m) H_j  with
+//   P = cx [sigma_bar(0,0), sigma_bar(0,1)],  Q = cy [sigma_bar(1,0), sigma_bar(1,1)],
+//   H_0 = (hx2 (lam + 2G) + hy2 G) A3_x,  H_1 = (hx2 G + hy2 (lam + 2G)) A3_y,
+// sigma_bar the plane-strain stress of the mean strain, lam = K - 2G/3.
+__global__ void __launch_bounds__(256)
+k_elem_force_quad4_uniform(const int32_t* __restrict__ conn, const double* __restrict__ u,
+                           const double* __restrict__ Km, const double* __restrict__ Gm,
+                           int64_t nelem, Quad4Uniform c, double* __restrict__ fe)
+{
+    GF_FOR(e, nelem)
+    {
+        int4 cn = __ldg(reinterpret_cast<const int4*>(conn) + e);
+        double2 u0 = __ldg(reinterpret_cast<const double2*>(u) + cn.x);
+        double2 u1 = __ldg(reinterpret_cast<const double2*>(u) + cn.y);
+        double2 u2 = __ldg(reinterpret_cast<const double2*>(u) + cn.z);
+        double2 u3 = __ldg(reinterpret_cast<const double2*>(u) + cn.w);
+        double K = __ldg(Km + e), G = __ldg(Gm + e);
+        // Walsh combinations
+        double px = u2.x - u0.x, qx = u1.x - u3.x;
+        double py = u2.y - u0.y, qy = u1.y - u3.y;
+        double A1x = px + qx, A2x = px - qx, A3x = (u0.x + u2.x) - (u1.x + u3.x);
+        double A1y = py + qy, A2y = py - qy, A3y = (u0.y + u2.y) - (u1.y + u3.y);
+        // moduli
+        double lam = fma(-2.0 / 3.0, G, K);
+        double l2g = fma(2.0, G, lam);
+        // mean strain and stress
+        double e00 = c.ax * A1x, e11 = c.ay * A2y;
+        double lt = lam * (e00 + e11);
+        double s00 = fma(2.0 * G, e00, lt);
+        double s11 = fma(2.0 * G, e11, lt);
+        double s01 = G * fma(c.ax, A1y, c.ay * A2x);
+        double P0 = c.cx * s00, P1 = c.cx * s01;
+        double Q0 = c.cy * s01, Q1 = c.cy * s11;
+        double H0 = fma(c.hx2, l2g, c.hy2 * G) * A3x;
+        double H1 = fma(c.hx2, G, c.hy2 * l2g) * A3y;
+        // f(m,j) = s_xi P + s_eta Q + s_h H with s_xi = (-,+,+,-), s_eta = (-,-,+,+), s_h = (+,-,+,-)
+        double Sx = P0 + Q0, Dx = P0 - Q0, Sy = P1 + Q1, Dy = P1 - Q1;
+        double2* fo = reinterpret_cast<double2*>(fe) + e * 4;
+        fo[0] = make_double2(H0 - Sx, H1 - Sy);
+        fo[1] = make_double2(Dx - H0, Dy - H1);
+        fo[2] = make_double2(Sx + H0, Sy + H1);
+        fo[3] = make_double2(-(Dx + H0), -(Dy + H1));
+    }
+}
+
+// ------------------------------------------------------------------ node kernels
+
+struct VerletCoef {
+    double dt, h, c, eta; // h = 0.5 dt, c = 0.5 dt^2
+};
+
+__global__ void k_predict(double* __restrict__ u, const double* __restrict__ v,
+                          const double* __restrict__ a, int64_t n, VerletCoef k)
+{
+    // u = u + dt v + 0.5 dt^2 a  (main.cpp:119)
+    GF_FOR(t, n) u[t] = __dadd_rn(__dadd_rn(u[t], __dmul_rn(k.dt, v[t])), __dmul_rn(k.c, a[t]));
+}
+
+template <bool S>
+__global__ void __launch_bounds__(256)
+k_verlet_node(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
+              const int32_t* __restrict__ idx, const int32_t* __restrict__ part, int64_t nnu,
+              const double* __restrict__ inv, const double* __restrict__ fe,
+              const double* __restrict__ fext, int64_t n, VerletCoef k, int advance,
+              double* __restrict__ u, double* __restrict__ v, double* __restrict__ a)
+{
+    GF_FOR(t, n)
+    {
+        int32_t d = __ldg(dofs + t);
+        int32_t b = __ldg(ptr + d), en = __ldg(ptr + d + 1);
+        double fint = 0.0;
+        for (int32_t j = b; j < en; ++j) fint = __dadd_rn(fint, __ldg(fe + __ldg(idx + j)));
+        double R = sub<S>(fext ? __ldg(fext + t) : 0.0, fint);
+        int32_t p = __ldg(part + t);
+        bool fr = p < nnu;
+        double mi = fr ? __ldg(inv + p) : 0.0;
+        double vn = v[t], an = a[t];
+        // estimate 1 (main.cpp:129-137)
+        double vv = madd<S>(k.dt, an, vn);
+        double aa = fr ? mul<S>(mi, sub<S>(R, mul<S>(k.eta, vv))) : an;
+        // estimate 2 (main.cpp:139-147)
+        vv = madd<S>(k.h, add<S>(an, aa), vn);
+        aa = fr ? mul<S>(mi, sub<S>(R, mul<S>(k.eta, vv))) : aa;
+        // final (main.cpp:149-157)
+        vv = madd<S>(k.h, add<S>(an, aa), vn);
+        aa = fr ? mul<S>(mi, sub<S>(R, mul<S>(k.eta, vv))) : aa;
+        v[t] = vv;
+        a[t] = aa;
+        if (advance) u[t] = madd<S>(k.c, aa, madd<S>(k.dt, vv, u[t]));
+    }
+}
+
+__global__ void k_detect_quad4_uniform(const double* __restrict__ dNx, const double* __restrict__ vol,
+                                       int64_t nelem, const double* __restrict__ ref, double vref,
+                                       double tol_g, double tol_v, int* __restrict__ bad)
+{
+    GF_FOR(t, nelem * 4)
+    {
+        int q = static_cast<int>(t & 3);
+        const double* g = dNx + t * 8;
+        bool ok = fabs(vol[t] - vref) <= tol_v;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) ok = ok && fabs(g[k] - ref[q * 8 + k]) <= tol_g;
+        if (!ok) *bad = 1;
+    }
+}
+
+// FP64 probe: 8 independent DFMA chains per thread.
+__global__ void k_probe_fp64(int64_t iters, double* out)
+{
+    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4,
+           a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    const double m = 0.999999999, c = 1e-7;
+    for (int64_t i = 0; i < iters; ++i) {
+        a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+        a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+    }
+    double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    if (s == 123.456) out[0] = s; // practically never taken; keeps the chains alive
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[1] = s;
+}
+
+} // namespace gfgpu
+
+using namespace gfgpu;
+
+static int check_desc(const gfgpu_verlet_desc* d)
+{
+    GF_REQUIRE(d, "null descriptor");
+    GF_REQUIRE((d->nne == 4 && d->ndim == 2) || (d->nne == 8 && d->ndim == 3),
+               "only Quad4 and Hex8");
+    GF_REQUIRE(d->conn && d->dofs && d->csr_ptr && d->csr_idx && d->part && d->inv && d->K && d->G,
+               "null table");
+    GF_REQUIRE(d->uniform || (d->dNx && d->vol && d->nip > 0), "general path needs dNx and vol");
+    GF_REQUIRE(!too_big(d->nelem * d->nne * d->ndim) && !too_big(d->nnode * d->ndim), "too large");
+    GF_REQUIRE(d->dt > 0.0, "dt must be positive");
+    return GFGPU_OK;
+}
+
+static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, cudaStream_t s)
+{
+    if (d->nelem == 0) return GFGPU_OK;
+    if (d->uniform && d->nne == 4) {
+        Quad4Uniform c;
+        double g = 1.0 / std::sqrt(3.0);
+        double vq = d->hx * d->hy / 4.0;
+        c.ax = 1.0 / (2.0 * d->hx);
+        c.ay = 1.0 / (2.0 * d->hy);
+        c.cx = 4.0 * vq * c.ax;
+        c.cy = 4.0 * vq * c.ay;
+        c.hx2 = 4.0 * (g * g) * vq * c.ax * c.ax;
+        c.hy2 = 4.0 * (g * g) * vq * c.ay * c.ay;
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int64_t blocks = (d->nelem + 255) / 256;
+        int64_t cap = static_cast<int64_t>(sms) * 8 * 16;
+        if (blocks > cap) blocks = cap;
+        k_elem_force_quad4_uniform<<<static_cast<unsigned>(blocks), 256, 0, s>>>(
+            d->conn, u, d->K, d->G, d->nelem, c, fe);
+    }
+    else if (d->uniform) {
+        return fail(GFGPU_ERR_UNSUPPORTED, "uniform path: Quad4 only in the explicit step");
+    }
+    else {
+        unsigned g = grid_for(d->nelem, 128);
+        if (d->nne == 4) {
+            if (strict_mode())
+                k_elem_force_general<true, 4, 2><<<g, 128, 0, s>>>(d->conn, u, d->dNx, d->vol, d->K,
+                                                                   d->G, d->nelem, d->nip, fe);
+            else
+                k_elem_force_general<false, 4, 2><<<g, 128, 0, s>>>(d->conn, u, d->dNx, d->vol, d->K,
+                                                                    d->G, d->nelem, d->nip, fe);
+        }
+        else {
+            if (strict_mode())
+                k_elem_force_general<true, 8, 3><<<g, 128, 0, s>>>(d->conn, u, d->dNx, d->vol, d->K,
+                                                                   d->G, d->nelem, d->nip, fe);
+            else
+                k_elem_force_general<false, 8, 3><<<g, 128, 0, s>>>(d->conn, u, d->dNx, d->vol, d->K,
+                                                                    d->G, d->nelem, d->nip, fe);
+        }
+    }
+    return check_launch("verlet element kernel");
+}
+
+extern "C" {
+
+int64_t gfgpu_verlet_workspace_bytes(const gfgpu_verlet_desc* d)
+{
+    if (!d) return 0;
+    int64_t b = d->nelem * d->nne * d->ndim * static_cast<int64_t>(sizeof(double));
+    return (b + 255) / 256 * 256;
+}
+
+int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
+                                const double* vol_host, double rtol)
+{
+    // dNx_host / vol_host: the first element's dNx [nip,4,2] and vol [nip] (host copies); the
+    // device arrays d->dNx / d->vol are scanned on the GPU against the rectangle they imply.
+    GF_REQUIRE(d && dNx_host && vol_host, "bad argument");
+    d->uniform = 0;
+    if (!(d->nne == 4 && d->ndim == 2 && d->nip == 4) || !d->dNx || !d->vol) return GFGPU_OK;
+    double g = 1.0 / std::sqrt(3.0);
+    const double xi[4][2] = {{-g, -g}, {+g, -g}, {+g, +g}, {-g, +g}};
+    const double sx[4] = {-1, +1, +1, -1}, se[4] = {-1, -1, +1, +1};
+    // edge lengths from the first Gauss point: dNx(m=1,0) = ax (1 - eta_0), dNx(m=3,1) = ay (1 - xi_0)
+    double ax = dNx_host[1 * 2 + 0] / (1.0 - xi[0][1]);
+    double ay = dNx_host[3 * 2 + 1] / (1.0 - xi[0][0]);
+    if (!(ax > 0.0) || !(ay > 0.0)) return GFGPU_OK;
+    double hx = 1.0 / (2.0 * ax), hy = 1.0 / (2.0 * ay);
+    double ref[32];
+    double gmax = 0.0;
+    for (int q = 0; q < 4; ++q)
+        for (int m = 0; m < 4; ++m) {
+            ref[q * 8 + m * 2 + 0] = ax * sx[m] * (1.0 + se[m] * xi[q][1]);
+            ref[q * 8 + m * 2 + 1] = ay * se[m] * (1.0 + sx[m] * xi[q][0]);
+            gmax = std::fmax(gmax, std::fabs(ref[q * 8 + m * 2 + 0]));
+            gmax = std::fmax(gmax, std::fabs(ref[q * 8 + m * 2 + 1]));
+        }
+    double vref = hx * hy / 4.0;
+    for (int q = 0; q < 4; ++q) {
+        if (std::fabs(vol_host[q] - vref) > rtol * vref) return GFGPU_OK;
+        for (int k = 0; k < 8; ++k)
+            if (std::fabs(dNx_host[q * 8 + k] - ref[q * 8 + k]) > rtol * gmax) return GFGPU_OK;
+    }
+    double* dref = nullptr;
+    int* bad = nullptr;
+    GF_TRY(check_cuda(cudaMalloc(&dref, sizeof(ref)), "cudaMalloc"));
+    GF_TRY(check_cuda(cudaMalloc(&bad, sizeof(int)), "cudaMalloc"));
+    cudaMemcpy(dref, ref, sizeof(ref), cudaMemcpyHostToDevice);
+    cudaMemset(bad, 0, sizeof(int));
+    k_detect_quad4_uniform<<<grid_for(d->nelem * 4), kBlock>>>(d->dNx, d->vol, d->nelem, dref, vref,
+                                                               rtol * gmax, rtol * vref, bad);
+    int hbad = 1;
+    int rc = check_launch("detect_uniform");
+    if (rc == GFGPU_OK)
+        rc = check_cuda(cudaMemcpy(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
+    cudaFree(dref);
+    cudaFree(bad);
+    GF_TRY(rc);
+    if (!hbad) {
+        d->uniform = 1;
+        d->hx = hx;
+        d->hy = hy;
+        d->hz = 0.0;
+    }
+    return GFGPU_OK;
+}
+
+int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                      int64_t nsteps, void* workspace, gfgpu_stream_t stream)
+{
+    GF_TRY(check_desc(d));
+    GF_REQUIRE(u && v && a && workspace && nsteps >= 0, "bad argument");
+    GF_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 15u) == 0, "workspace must be 16-byte aligned");
+    if (nsteps == 0) return GFGPU_OK;
+    cudaStream_t s = S(stream);
+    double* fe = static_cast<double*>(workspace);
+    VerletCoef k;
+    k.dt = d->dt;
+    k.h = 0.5 * d->dt;
+    k.c = 0.5 * std::pow(d->dt, 2.0);
+    k.eta = d->eta;
+    int64_t n = d->nnode * d->ndim;
+    unsigned gn = grid_for(n);
+    k_predict<<<gn, kBlock, 0, s>>>(u, v, a, n, k);
+    GF_TRY(check_launch("verlet predict"));
+    bool st = strict_mode();
+    for (int64_t it = 0; it < nsteps; ++it) {
+        GF_TRY(launch_elem(d, u, fe, s));
+        int adv = it + 1 < nsteps ? 1 : 0;
+        if (st)
+            k_verlet_node<true><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
+                                                      d->inv, fe, d->fext, n, k, adv, u, v, a);
+        else
+            k_verlet_node<false><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
+                                                       d->inv, fe, d->fext, n, k, adv, u, v, a);
+        GF_TRY(check_launch("verlet node kernel"));
+    }
+    return GFGPU_OK;
+}
+
+int gfgpu_internal_force(const gfgpu_verlet_desc* d, const double* u, double* fint,
+                         void* workspace, gfgpu_stream_t stream)
+{
+    GF_TRY(check_desc(d));
+    GF_REQUIRE(u && fint && workspace, "bad argument");
+    double* fe = static_cast<double*>(workspace);
+    GF_TRY(launch_elem(d, u, fe, S(stream)));
+    return gfgpu_assemble_node(d->csr_ptr, d->csr_idx, d->dofs, d->nnode, d->ndim, fe, fint, stream);
+}
+
+int gfgpu_verlet_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
+                                gfgpu_stream_t stream)
+{
+    GF_TRY(check_desc(d));
+    GF_REQUIRE(u && fe, "bad argument");
+    GF_REQUIRE((reinterpret_cast<uintptr_t>(fe) & 15u) == 0, "fe must be 16-byte aligned");
+    return launch_elem(d, u, fe, S(stream));
+}
+
+int gfgpu_probe_fp64(int64_t blocks, int64_t iters, double* out, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(blocks > 0 && iters > 0 && out, "bad argument");
+    k_probe_fp64<<<static_cast<unsigned>(blocks), 256, 0, S(stream)>>>(iters, out);
+    return check_launch("probe_fp64");
+}
+
+} // extern "C"

@@ -1,0 +1,144 @@
+"""Linear elastic stress and the fused explicit velocity-Verlet integrator on the GPU.
+
+The integrator runs the loop of docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:110-157
+(scheme: docs/examples/dynamics_inertia-damping.rst:6-66) with a nodal viscous damping force
+-eta * v in the residual, a lumped mass from Int_N_scalar_NT_dV with nodal quadrature, and
+fixed DOFs handled as MatrixDiagonalPartitioned does (the solve leaves them untouched).
+"""
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+from . import mesh as _mesh
+from .element import Quad4, Hex8
+
+
+def elastic_stress(eps, K, G, sig=None):
+    """sigma = K tr(eps) I + 2 G dev(eps) per Gauss point, K and G per element [nelem]
+    (plane strain for 2-d tensors; convention of docs/theory/examples/
+    cartesian_linear-elasticity.py:146-186)."""
+    eps = _dev.dev_f64(eps)
+    K = _dev.dev_f64(K)
+    G = _dev.dev_f64(G)
+    nelem, nip, nd, _ = eps.shape
+    if sig is None:
+        sig = torch.empty_like(eps)
+    _lib.call("gfgpu_elastic_stress", eps.data_ptr(), K.data_ptr(), G.data_ptr(), nelem, nip, nd,
+              sig.data_ptr(), _dev.stream())
+    return sig
+
+
+class VelocityVerlet:
+    """Explicit dynamics of a linear elastic Quad4/Hex8 mesh, fully device resident.
+
+    Parameters
+    ----------
+    coor, conn, dofs : mesh tables (host or device)
+    K, G : per-element bulk and shear moduli [nelem]
+    rho : density (scalar) used for the lumped mass
+    dt, eta : time step and nodal viscous damping coefficient
+    iip : prescribed (fixed) dofs, or None
+    fext : external force nodevec, or None
+    uniform : "auto" (detect congruent axis-aligned elements), True or False
+    """
+
+    def __init__(self, coor, conn, dofs, K, G, rho=1.0, dt=None, eta=0.0, iip=None, fext=None,
+                 uniform="auto"):
+        from .vector import Vector
+        from .matrix import MatrixDiagonal, MatrixDiagonalPartitioned
+
+        conn_h = _dev.host_i32(conn)
+        dofs_h = _dev.host_i32(dofs)
+        nelem, nne = conn_h.shape
+        nnode, nd = dofs_h.shape
+        self.nelem, self.nnode, self.nne, self.ndim = nelem, nnode, nne, nd
+        E = Quad4 if nne == 4 else Hex8
+        self.vector = Vector(conn_h, dofs_h)
+        x = self.vector.AsElement(_dev.dev_f64(coor))
+        self.quad = E.Quadrature(x)
+        nodal = E.Quadrature(x, E.Nodal.xi(), E.Nodal.w())
+        rho_q = torch.full((nelem, nodal.nip()), float(rho), dtype=torch.float64,
+                           device=_dev.device())
+        Me = nodal.Int_N_scalar_NT_dV(rho_q)
+        if iip is None or len(iip) == 0:
+            self.mass = MatrixDiagonal(conn_h, dofs_h)
+            self.mass.assemble(Me)
+            part = dofs_h
+            nnu = self.mass.ndof()
+            inv = self.mass.inverse()
+        else:
+            self.mass = MatrixDiagonalPartitioned(conn_h, dofs_h, iip)
+            self.mass.assemble(Me)
+            part = self.mass.part()
+            nnu = self.mass.nnu()
+            inv = self.mass.inverse()
+        del Me, nodal
+        self.part_d = _dev.dev_i32(part)
+        self.inv = inv
+        self.K = _dev.dev_f64(K)
+        self.G = _dev.dev_f64(G)
+        self.fext = None if fext is None else _dev.dev_f64(fext)
+        self.dt = float(dt)
+        self.eta = float(eta)
+
+        d = _lib.VerletDesc()
+        d.nelem, d.nnode, d.nne, d.ndim, d.nip = nelem, nnode, nne, nd, self.quad.nip()
+        d.conn = self.vector.conn_d.data_ptr()
+        d.dofs = self.vector.dofs_d.data_ptr()
+        d.csr_ptr = self.vector.csr_ptr.data_ptr()
+        d.csr_idx = self.vector.csr_idx.data_ptr()
+        d.part = self.part_d.data_ptr()
+        d.nnu = nnu
+        d.inv = self.inv.data_ptr()
+        d.dNx = self.quad.GradN().data_ptr()
+        d.vol = self.quad.dV().data_ptr()
+        d.K = self.K.data_ptr()
+        d.G = self.G.data_ptr()
+        d.fext = None if self.fext is None else self.fext.data_ptr()
+        d.dt, d.eta = self.dt, self.eta
+        d.uniform = 0
+        self.desc = d
+        if uniform is True or uniform == "auto":
+            g0 = self.quad.GradN()[0].detach().cpu().numpy().copy()
+            v0 = self.quad.dV()[0].detach().cpu().numpy().copy()
+            _lib.call("gfgpu_verlet_detect_uniform", C.addressof(d), g0.ctypes.data,
+                      v0.ctypes.data, 1e-12)
+            if uniform is True and not d.uniform:
+                raise RuntimeError("mesh is not a uniform axis-aligned Quad4 mesh")
+        self.ws = torch.empty(int(_lib.lib().gfgpu_verlet_workspace_bytes(C.addressof(d))) // 8,
+                              dtype=torch.float64, device=_dev.device())
+
+    @property
+    def uniform(self):
+        return bool(self.desc.uniform)
+
+    def use_general_path(self):
+        self.desc.uniform = 0
+
+    def step(self, u, v, a, nsteps=1):
+        """Advance nsteps increments in place (u, v, a: device nodevec float64)."""
+        for t in (u, v, a):
+            _dev.check_shape(t, (self.nnode, self.ndim), "VelocityVerlet.step")
+            if t.dtype != torch.float64 or not t.is_contiguous() or not t.is_cuda:
+                raise ValueError("u, v, a must be contiguous float64 CUDA tensors")
+        _lib.call("gfgpu_verlet_step", C.addressof(self.desc), u.data_ptr(), v.data_ptr(),
+                  a.data_ptr(), int(nsteps), self.ws.data_ptr(), _dev.stream())
+
+    def internal_force(self, u, fint=None):
+        u = _dev.dev_f64(u)
+        if fint is None:
+            fint = torch.empty_like(u)
+        _lib.call("gfgpu_internal_force", C.addressof(self.desc), u.data_ptr(), fint.data_ptr(),
+                  self.ws.data_ptr(), _dev.stream())
+        return fint
+
+
+def critical_dt(K, G, rho=1.0, h=1.0):
+    """h / c_max with c = sqrt((K + 4G/3) / rho) (plane-strain P-wave speed)."""
+    K = np.asarray(K, dtype=np.float64)
+    G = np.asarray(G, dtype=np.float64)
+    return h / math.sqrt(float(np.max(K + 4.0 * G / 3.0)) / rho)

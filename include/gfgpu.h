@@ -1,0 +1,266 @@
+/*
+ * gfgpu — GB300-native (sm_103a) element hot path of GooseFEM behind a plain C ABI.
+ *
+ * Conventions (every entry point):
+ *  - returns GFGPU_OK (0) or a negative GFGPU_ERR_* code; gfgpu_last_error() has the message;
+ *  - arrays are row-major, FP64 values, int32 indices (the reference's size_t tables are
+ *    narrowed once at set-up; sizes above 2^31-1 entries are rejected with GFGPU_ERR_ARG);
+ *  - functions named gfgpu_host_* take HOST pointers and run on the CPU (set-up / bookkeeping);
+ *    every other function takes DEVICE pointers and enqueues work on `stream`
+ *    (a cudaStream_t; NULL = legacy default stream) and returns without synchronising,
+ *    unless its comment says otherwise;
+ *  - storage names follow GooseFEM: "dofval" [ndof], "nodevec" [nnode, ndim],
+ *    "elemvec" [nelem, nne, ndim], "elemmat" [nelem, nne*ndim, nne*ndim],
+ *    "qscalar" [nelem, nip], "qvector" [nelem, nip, n], "qtensor" [nelem, nip, ndim, ndim].
+ *
+ * Reference paths cited below are relative to the GooseFEM source tree.
+ */
+#ifndef GFGPU_H
+#define GFGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void* gfgpu_stream_t;
+
+enum {
+    GFGPU_OK = 0,
+    GFGPU_ERR_ARG = -1,          /* bad size / shape / null pointer (GOOSEFEM_ASSERT) */
+    GFGPU_ERR_INDEX = -2,        /* index table out of range */
+    GFGPU_ERR_CUDA = -3,         /* CUDA runtime error */
+    GFGPU_ERR_TIMEOUT = -4,      /* bounded device wait gave up */
+    GFGPU_ERR_NAN = -5,          /* non-finite value detected */
+    GFGPU_ERR_NOT_DIAGONAL = -6, /* MatrixDiagonal::assemble on a non-diagonal elemmat */
+    GFGPU_ERR_UNSUPPORTED = -7,  /* element type / quadrature not supported by this entry */
+    GFGPU_ERR_DIVERGED = -8      /* iterative solver did not converge */
+};
+
+/* Message of the last failing call on this host thread. */
+const char* gfgpu_last_error(void);
+/* Library version string. */
+const char* gfgpu_version(void);
+
+/* Arithmetic mode of the operator kernels (not of the fused explicit step):
+ * 0 = fast (FMA contraction allowed; agreement with the reference ~1e-16 relative),
+ * 1 = strict (every product and sum rounded separately in the reference's order, which
+ *     reproduces the reference's FP64 results bit for bit). Default 0. Process-wide. */
+int gfgpu_set_strict(int strict);
+
+/* ============================ set-up on the host (integer bookkeeping) ==================== */
+
+/* Mesh::Quad4::Regular coor/conn (MeshQuad4.h:87-126). coor [nnode,2], conn [nelem,4]. */
+int gfgpu_host_quad4_regular(int64_t nx, int64_t ny, double h, double* coor, int32_t* conn);
+/* Mesh::Hex8::Regular coor/conn (MeshHex8.h:77-130). coor [nnode,3], conn [nelem,8]. */
+int gfgpu_host_hex8_regular(int64_t nx, int64_t ny, int64_t nz, double h, double* coor,
+                            int32_t* conn);
+/* Mesh::dofs (Mesh.h:93-96): arange(nnode*ndim).reshape(nnode, ndim). */
+int gfgpu_host_dofs(int64_t nnode, int32_t ndim, int32_t* dofs);
+/* RegularBase2d::nodesPeriodic (Mesh.h:511-540) of Quad4 Regular; out [(nx-1)+(ny-1)+3, 2]. */
+int gfgpu_host_quad4_nodes_periodic(int64_t nx, int64_t ny, int32_t* out, int64_t* nper);
+/* RegularBase::dofsPeriodic (Mesh.h:291-306) given a nodesPeriodic table. */
+int gfgpu_host_dofs_periodic(int64_t nnode, int32_t ndim, const int32_t* nodes_periodic,
+                             int64_t nper, int32_t* dofs);
+/* Mesh::Renumber (Mesh.h:114-166): index of each entry in the sorted unique list. */
+int gfgpu_host_renumber(const int32_t* in, int64_t n, int32_t* out);
+/* VectorPartitioned / MatrixDiagonalPartitioned bookkeeping (VectorPartitioned.h:72-88):
+ * iiu = setdiff1d(dofs, iip) (sorted unique), part = Reorder({iiu, iip}).apply(dofs)
+ * (Mesh.h:2384-2450). iiu needs room for n entries; *nnu receives its length. */
+int gfgpu_host_partition(const int32_t* dofs, int64_t n, const int32_t* iip, int64_t nnp,
+                         int32_t* iiu, int32_t* part, int64_t* nnu);
+/* Mesh::coordination (Mesh.h:2462-2477). */
+int gfgpu_host_coordination(const int32_t* conn, int64_t nelem, int32_t nne, int64_t nnode,
+                            int32_t* N);
+/* Mesh::elem2node, sorted (Mesh.h:2485-2513) as CSR: ptr [nnode+1], idx [nelem*nne]. */
+int gfgpu_host_elem2node(const int32_t* conn, int64_t nelem, int32_t nne, int64_t nnode,
+                         int32_t* ptr, int32_t* idx);
+/* Dof-centric incidence CSR behind the deterministic assembly (replaces the serial scatter of
+ * Vector.h:724-741 and MatrixDiagonal.h:151-167): for dof d, idx[ptr[d]:ptr[d+1]] lists the
+ * flat elemvec indices (e*nne+m)*ndim+i with dofs[conn[e,m], i] == d in ascending order, i.e.
+ * the reference's serial summation order. ptr [ndof+1], idx [nelem*nne*ndim]. `dofs` may be
+ * any dof numbering (GooseFEM dofs, or the partitioned numbering `part`). */
+int gfgpu_host_dof_csr(const int32_t* conn, const int32_t* dofs, int64_t nelem, int32_t nne,
+                       int64_t nnode, int32_t ndim, int64_t ndof, int32_t* ptr, int32_t* idx);
+/* Same for nodevec sources (Vector.h:703-718): idx lists flat nodevec indices m*ndim+i. */
+int gfgpu_host_dof_csr_nodevec(const int32_t* dofs, int64_t nnode, int32_t ndim, int64_t ndof,
+                               int32_t* ptr, int32_t* idx);
+
+/* ============================ Element quadrature (device) ================================= */
+
+/* Quadrature(x, xi, w) set-up: shape functions and compute_dN.
+ * Quad4: ElementQuad4.h:277-318 + compute_dN_impl :493-532 (detail.h:26-36 inverse).
+ * Hex8:  ElementHex8.h:255-317 + Element.h:1178-1229 (detail.h:49-69), restated as written.
+ * x elemvec [nelem,nne,ndim]; xi [nip,ndim]; w [nip]; out: N [nip,nne], dNxi [nip,nne,ndim]
+ * (either may be NULL), dNx [nelem,nip,nne,ndim], vol [nelem,nip]. Always strict (bit-exact). */
+int gfgpu_quad4_compute_dN(const double* x, int64_t nelem, const double* xi, const double* w,
+                           int32_t nip, double* N, double* dNxi, double* dNx, double* vol,
+                           gfgpu_stream_t stream);
+int gfgpu_hex8_compute_dN(const double* x, int64_t nelem, const double* xi, const double* w,
+                          int32_t nip, double* N, double* dNxi, double* dNx, double* vol,
+                          gfgpu_stream_t stream);
+
+/* InterpQuad_vector (ElementQuad4.h:325-346; Element.h:893-922): qvector [nelem,nip,n]. */
+int gfgpu_interp_quad_vector(const double* N, const double* elemvec, int64_t nelem, int32_t nne,
+                             int32_t nip, int32_t n, double* qvector, gfgpu_stream_t stream);
+/* GradN_vector / GradN_vector_T / SymGradN_vector (ElementQuad4.h:349-434; Element.h:925-1022).
+ * dNx [nelem,nip,nne,ndim], elemvec [nelem,nne,ndim] -> qtensor [nelem,nip,ndim,ndim]. */
+int gfgpu_grad_n_vector(const double* dNx, const double* elemvec, int64_t nelem, int32_t nne,
+                        int32_t nip, int32_t ndim, double* qtensor, gfgpu_stream_t stream);
+int gfgpu_grad_n_vector_T(const double* dNx, const double* elemvec, int64_t nelem, int32_t nne,
+                          int32_t nip, int32_t ndim, double* qtensor, gfgpu_stream_t stream);
+int gfgpu_sym_grad_n_vector(const double* dNx, const double* elemvec, int64_t nelem, int32_t nne,
+                            int32_t nip, int32_t ndim, double* qtensor, gfgpu_stream_t stream);
+/* Int_N_vector_dV (Element.h:1025-1056): qvector [nelem,nip,n] -> elemvec [nelem,nne,n]. */
+int gfgpu_int_n_vector_dv(const double* N, const double* vol, const double* qvector,
+                          int64_t nelem, int32_t nne, int32_t nip, int32_t n, double* elemvec,
+                          gfgpu_stream_t stream);
+/* Int_N_scalar_NT_dV (ElementQuad4.h:437-464; ElementHex8.h:324-352): -> elemmat. */
+int gfgpu_int_n_scalar_nt_dv(const double* N, const double* vol, const double* qscalar,
+                             int64_t nelem, int32_t nne, int32_t nip, int32_t ndim,
+                             double* elemmat, gfgpu_stream_t stream);
+/* Int_gradN_dot_tensor2_dV (ElementQuad4.h:467-491; ElementHex8.h:355-383): -> elemvec. */
+int gfgpu_int_grad_n_dot_tensor2_dv(const double* dNx, const double* vol, const double* qtensor,
+                                    int64_t nelem, int32_t nne, int32_t nip, int32_t ndim,
+                                    double* elemvec, gfgpu_stream_t stream);
+/* Int_gradN_dot_tensor4_dot_gradNT_dV (Element.h:1132-1176): qtensor4 [nelem,nip,d,d,d,d]. */
+int gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv(const double* dNx, const double* vol,
+                                                const double* qtensor4, int64_t nelem,
+                                                int32_t nne, int32_t nip, int32_t ndim,
+                                                double* elemmat, gfgpu_stream_t stream);
+
+/* Linear elastic stress (external GMat in the reference; convention of
+ * docs/theory/examples/cartesian_linear-elasticity.py:146-186): sigma = K tr(eps) I + 2G dev(eps)
+ * with a 3-d trace (ndim=2: plane strain). K, G per element [nelem]. */
+int gfgpu_elastic_stress(const double* eps, const double* K, const double* G, int64_t nelem,
+                         int32_t nip, int32_t ndim, double* sig, gfgpu_stream_t stream);
+
+/* ============================ Vector (device) ============================================= */
+
+/* Vector::asElement nodevec -> elemvec (Vector.h:681-697). */
+int gfgpu_as_element(const int32_t* conn, int64_t nelem, int32_t nne, int32_t ndim,
+                     const double* nodevec, double* elemvec, gfgpu_stream_t stream);
+/* Vector::asElement dofval -> elemvec (Vector.h:659-675). */
+int gfgpu_as_element_dofval(const int32_t* conn, const int32_t* dofs, int64_t nelem, int32_t nne,
+                            int32_t ndim, const double* dofval, double* elemvec,
+                            gfgpu_stream_t stream);
+/* Vector::asNode dofval -> nodevec (Vector.h:615-629). */
+int gfgpu_as_node(const int32_t* dofs, int64_t nnode, int32_t ndim, const double* dofval,
+                  double* nodevec, gfgpu_stream_t stream);
+/* Vector::asDofs (Vector.h:569-608): the last writer of each dof wins, unwritten dofs are 0.
+ * `last` [ndof] holds the flat source index of the last writer (or -1); it is the final entry of
+ * each CSR segment (gfgpu_host_dof_csr / _nodevec), see gfgpu_csr_last. */
+int gfgpu_as_dofs(const int32_t* last, int64_t ndof, const double* src, double* dofval,
+                  gfgpu_stream_t stream);
+/* last[d] = ptr[d+1] > ptr[d] ? idx[ptr[d+1]-1] : -1. */
+int gfgpu_csr_last(const int32_t* ptr, const int32_t* idx, int64_t ndof, int32_t* last,
+                   gfgpu_stream_t stream);
+/* Vector::assembleDofs (Vector.h:703-741): dofval[d] = sum of src[idx[k]], k in the dof's CSR
+ * segment, in ascending order from 0.0 (deterministic; the reference's serial order). */
+int gfgpu_assemble_dofs(const int32_t* ptr, const int32_t* idx, int64_t ndof, const double* src,
+                        double* dofval, gfgpu_stream_t stream);
+/* Vector::assembleNode (Vector.h:747-757): AssembleDofs then asNode, fused (no dofval). */
+int gfgpu_assemble_node(const int32_t* ptr, const int32_t* idx, const int32_t* dofs,
+                        int64_t nnode, int32_t ndim, const double* elemvec, double* nodevec,
+                        gfgpu_stream_t stream);
+
+/* ============================ MatrixDiagonal (device) ===================================== */
+
+/* Element::isDiagonal (Element.h:122-145): *is_diag (host int) = 1 if every off-diagonal
+ * |entry| <= DBL_EPSILON. Synchronises `stream`. */
+int gfgpu_is_diagonal(const double* elemmat, int64_t nelem, int32_t K, int* is_diag,
+                      gfgpu_stream_t stream);
+/* MatrixDiagonal::assemble (MatrixDiagonal.h:151-167) through the dof CSR of elemvec indices:
+ * A[d] = sum of elemmat diagonal entries of the dof's incidences, in the reference's order.
+ * For MatrixDiagonalPartitioned (MatrixDiagonalPartitioned.h:73-98) pass the CSR built on
+ * `part`; A then holds [Auu, App] back to back. */
+int gfgpu_diag_assemble(const int32_t* ptr, const int32_t* idx, int64_t ndof, int32_t nne,
+                        int32_t ndim, const double* elemmat, double* A, gfgpu_stream_t stream);
+/* MatrixDiagonal::factorize (MatrixDiagonal.h:268-280): inv = 1 / A, n entries. */
+int gfgpu_diag_factorize(const double* A, int64_t n, double* inv, gfgpu_stream_t stream);
+/* MatrixDiagonal::solve nodevec (MatrixDiagonal.h:237-250) and, with nnu < ndof and
+ * `dofs` = part, MatrixDiagonalPartitioned::solve (MatrixDiagonalPartitioned.h:306-322):
+ * x(m,i) = inv[dofs(m,i)] * b(m,i) where dofs(m,i) < nnu; other entries of x are untouched. */
+int gfgpu_diag_solve_nodevec(const int32_t* dofs, int64_t nnode, int32_t ndim, int64_t nnu,
+                             const double* inv, const double* b, double* x,
+                             gfgpu_stream_t stream);
+/* MatrixDiagonal::dot nodevec (MatrixDiagonal.h:213-222): b(m,i) = A[dofs(m,i)] * x(m,i). */
+int gfgpu_diag_dot_nodevec(const int32_t* dofs, int64_t nnode, int32_t ndim, const double* A,
+                           const double* x, double* b, gfgpu_stream_t stream);
+/* MatrixDiagonalPartitioned::reaction nodevec (MatrixDiagonalPartitioned.h:378-392):
+ * b(m,i) = App[part(m,i) - nnu] * x(m,i) where part(m,i) >= nnu. */
+int gfgpu_diagp_reaction_nodevec(const int32_t* part, int64_t nnode, int32_t ndim, int64_t nnu,
+                                 const double* App, const double* x, double* b,
+                                 gfgpu_stream_t stream);
+/* Element-wise dofval products: MatrixDiagonal::dot / solve dofval (MatrixDiagonal.h:224-259):
+ * out[k] = a[k] * b[k]. */
+int gfgpu_dofval_mul(const double* a, const double* b, int64_t n, double* out,
+                     gfgpu_stream_t stream);
+
+/* ============================ explicit velocity-Verlet (device) =========================== */
+
+/* One or more increments of the explicit scheme of
+ * docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:110-157 (three velocity estimates,
+ * docs/examples/dynamics_inertia-damping.rst:6-66) on a linear elastic Quad4/Hex8 mesh:
+ *   u += dt v + dt^2/2 a;  f = assembleNode(int_gradN_dot_tensor2_dV(sigma(symGradN(u))));
+ *   3x { v = v_n + ...; fres = fext - f - eta v; a = M^-1 fres (free dofs only) }.
+ * The force chain runs as two kernels per increment: an element kernel writing the element
+ * forces to `fe` [nelem,nne,ndim] (caller-provided scratch), then a node kernel that gathers
+ * them through the dof CSR (deterministic, the reference's order) and updates v, a and the next
+ * displacement. */
+typedef struct {
+    int64_t nelem, nnode;
+    int32_t nne, ndim, nip; /* Quad4: 4,2,4; Hex8: 8,3,8 (Gauss) */
+    const int32_t* conn;    /* [nelem, nne] */
+    const int32_t* dofs;    /* [nnode, ndim] Vector dofs (periodic ties allowed) */
+    const int32_t* csr_ptr; /* [ndof+1] dof CSR over elemvec indices (gfgpu_host_dof_csr) */
+    const int32_t* csr_idx; /* [nelem*nne*ndim] */
+    const int32_t* part;    /* [nnode, ndim] solve numbering: free iff part < nnu */
+    int64_t nnu;
+    const double* inv;      /* [nnu] inverse lumped mass of the free dofs */
+    const double* dNx;      /* [nelem, nip, nne, ndim] (general path) */
+    const double* vol;      /* [nelem, nip] (general path) */
+    const double* K;        /* [nelem] bulk modulus */
+    const double* G;        /* [nelem] shear modulus */
+    const double* fext;     /* [nnode, ndim] or NULL (= 0) */
+    double dt, eta;
+    /* uniform-geometry fast path (set by gfgpu_verlet_detect_uniform or by the caller):
+     * all elements are congruent axis-aligned boxes of edge lengths hx, hy(, hz) with the
+     * reference's Gauss quadrature; 0 = general per-Gauss-point path. */
+    int32_t uniform;
+    double hx, hy, hz;
+} gfgpu_verlet_desc;
+
+/* Bytes of scratch the step needs (the element-force buffer), 256-byte aligned size. */
+int64_t gfgpu_verlet_workspace_bytes(const gfgpu_verlet_desc* d);
+/* Checks on the host that dNx/vol (copied to the host by the caller: dNx_host, vol_host, nelem
+ * entries each) describe congruent axis-aligned boxes with the Gauss rule, within `rtol`; on
+ * success sets d->uniform = 1 and d->hx, hy, hz. Returns GFGPU_OK either way (d->uniform tells). */
+int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
+                                const double* vol_host, double rtol);
+/* Advance nsteps increments; u, v, a are nodevec [nnode, ndim] device arrays updated in place.
+ * `workspace` is device memory of gfgpu_verlet_workspace_bytes(d). */
+int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                      int64_t nsteps, void* workspace, gfgpu_stream_t stream);
+/* Internal force only: fint (nodevec) = assembleNode(int_gradN_dot_tensor2_dV(sigma(u))), using
+ * the same element kernel as the step. */
+int gfgpu_internal_force(const gfgpu_verlet_desc* d, const double* u, double* fint,
+                         void* workspace, gfgpu_stream_t stream);
+
+/* Element forces only (the element kernel of the step): fe elemvec [nelem,nne,ndim] =
+ * Int_gradN_dot_tensor2_dV(sigma(SymGradN_vector(asElement(u)))). */
+int gfgpu_verlet_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
+                                gfgpu_stream_t stream);
+
+/* ============================ probes ====================================================== */
+
+/* FP64 FMA throughput probe: a kernel of independent DFMA chains, `blocks` x 256 threads,
+ * `iters` iterations of 8 chains; writes a checksum to out[0]. 2*8*iters*blocks*256 flops. */
+int gfgpu_probe_fp64(int64_t blocks, int64_t iters, double* out, gfgpu_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFGPU_H */

@@ -1,0 +1,119 @@
+"""CPU-only checks of libgfgpu.so: it loads, exports every entry point of include/gfgpu.h, and
+its host-side set-up (GooseFEM Mesh / Vector bookkeeping) is bit-exact with the oracle."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from _common import seeded_field
+
+KAT = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kat.json")))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from goosefem_gb300 import _lib
+
+    return _lib
+
+
+def test_exports_every_declared_symbol(lib):
+    L = lib.lib()
+    protos = lib.protos()
+    assert len(protos) > 40
+    for name in protos:
+        assert hasattr(L, name), name
+    assert lib.lib().gfgpu_version().startswith(b"gfgpu")
+
+
+def test_mesh_against_reference_kat(lib):
+    import goosefem_gb300 as gf
+
+    m = gf.Mesh.Quad4.Regular(5, 3)
+    assert np.array_equal(m.coor(), np.array(KAT["quad4_5x3_coor"]["value"]))
+    assert np.array_equal(m.conn(), np.array(KAT["quad4_5x3_conn"]["value"]))
+    assert np.array_equal(m.dofs(), np.array(KAT["quad4_5x3_dofs"]["value"]))
+    assert np.array_equal(m.nodesPeriodic(), np.array(KAT["quad4_5x3_nodesPeriodic"]["value"]))
+    assert np.array_equal(m.dofsPeriodic(), np.array(KAT["quad4_5x3_dofsPeriodic"]["value"]))
+    h = gf.Mesh.Hex8.Regular(3, 3, 3)
+    assert np.array_equal(h.coor(), np.array(KAT["hex8_3x3x3_coor"]["value"]))
+    assert np.array_equal(h.conn(), np.array(KAT["hex8_3x3x3_conn"]["value"]))
+    assert np.array_equal(h.nodesFront(), np.array(KAT["hex8_3x3x3_nodesFront"]["value"]))
+    assert np.array_equal(h.nodesBack(), np.array(KAT["hex8_3x3x3_nodesBack"]["value"]))
+    npr = np.array(KAT["hex8_3x3x3_nodesPeriodic"]["value"])
+    assert np.array_equal(h.dofsPeriodic(npr), np.array(KAT["hex8_3x3x3_dofsPeriodic"]["value"]))
+    q = gf.Mesh.Quad4.Regular(3, 3)
+    assert np.array_equal(gf.Mesh.coordination(q.conn()),
+                          np.array(KAT["quad4_3x3_coordination"]["value"]))
+    assert gf.Mesh.elem2node(q.conn()) == KAT["quad4_3x3_elem2node"]["value"]
+
+
+@pytest.mark.parametrize("nx,ny", [(1, 1), (2, 1), (7, 4), (64, 33)])
+def test_mesh_setup_matches_oracle(lib, oracle, nx, ny):
+    import goosefem_gb300 as gf
+
+    m = gf.Mesh.Quad4.Regular(nx, ny, 0.37)
+    coor, conn = oracle.quad4_regular(nx, ny, 0.37)
+    assert np.array_equal(m.coor(), coor) and np.array_equal(m.conn(), conn)
+    npr = oracle.quad4_nodes_periodic(nx, ny)
+    assert np.array_equal(m.nodesPeriodic(), npr)
+    assert np.array_equal(m.dofsPeriodic(), oracle.dofs_periodic(m.nnode(), 2, npr))
+    h = gf.Mesh.Hex8.Regular(nx, ny, 3, 0.37)
+    hc, hn = oracle.hex8_regular(nx, ny, 3, 0.37)
+    assert np.array_equal(h.coor(), hc) and np.array_equal(h.conn(), hn)
+
+
+def test_partition_and_renumber_match_oracle(lib, oracle):
+    import goosefem_gb300 as gf
+
+    m = gf.Mesh.Quad4.Regular(11, 7)
+    dofs = m.dofsPeriodic()
+    rng = np.random.default_rng(3)
+    iip = rng.choice(int(dofs.max()) + 1, 17, replace=False)
+    iiu, part = gf.Mesh.partition(dofs, iip)
+    iiu_r, part_r = oracle.partition(dofs, iip)
+    assert np.array_equal(iiu, iiu_r) and np.array_equal(part, part_r)
+    a = rng.integers(0, 1000, 500)
+    assert np.array_equal(gf.Mesh.renumber(a), oracle.renumber(a))
+    with pytest.raises(lib.GFGPUError):
+        gf.Mesh.partition(dofs, np.array([1, 1]))  # not unique (GOOSEFEM_ASSERT(is_unique(iip)))
+
+
+def test_dof_csr_is_the_serial_order(lib, oracle):
+    """Summing an elemvec through the dof CSR in segment order reproduces the reference's serial
+    assembleDofs bit for bit (checked here on the host with numpy)."""
+    from goosefem_gb300 import _dev
+
+    m = oracle.quad4_regular(13, 9)
+    conn = m[1]
+    dofs = oracle.dofs_periodic(14 * 10, 2, oracle.quad4_nodes_periodic(13, 9))
+    ndof = int(dofs.max()) + 1
+    ptr, idx = _dev.dof_csr(conn, dofs, ndof)
+    ev = seeded_field((conn.shape[0], 4, 2), 31).ravel()
+    out = np.zeros(ndof)
+    for d in range(ndof):
+        acc = 0.0
+        for k in range(ptr[d], ptr[d + 1]):
+            acc += ev[idx[k]]
+        out[d] = acc
+    assert np.array_equal(out, oracle.assemble_dofs_elemvec(conn, dofs, ev.reshape(-1, 4, 2)))
+    assert all(np.all(np.diff(idx[ptr[d]:ptr[d + 1]]) > 0) for d in range(ndof))
+
+
+def test_host_errors(lib):
+    import goosefem_gb300 as gf
+
+    with pytest.raises(ValueError):
+        gf.Mesh.Quad4.Regular(0, 3)
+    conn = np.array([[0, 1, 2, 99]], dtype=np.int32)
+    dofs = np.arange(8, dtype=np.int32).reshape(4, 2)
+    from goosefem_gb300 import _dev
+
+    with pytest.raises(lib.GFGPUError) as ei:
+        _dev.dof_csr(conn, dofs, 8)
+    assert ei.value.code == -2
