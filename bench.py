@@ -45,6 +45,7 @@ def parse():
     p.add_argument("--increments", type=int, default=1000)
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="bounded CPU-baseline sample length")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--path", default="auto", choices=["auto", "general"],
                    help="element kernel: auto (uniform fast path when applicable) or general")
     return p.parse_args()
@@ -100,16 +101,18 @@ def cpu_sample(w, seconds, parallel):
     u = np.zeros_like(w["v0"])
     v = w["v0"].copy()
     a = np.zeros_like(u)
-    n = 0
-    t0 = time.perf_counter()
-    while True:
-        R.verlet_run(conn, dofs, dNx, vol, w["K"], w["G"], A, free, None, w["dt"], w["eta"], 1, u,
+
+    def run(n):
+        t0 = time.perf_counter()
+        R.verlet_run(conn, dofs, dNx, vol, w["K"], w["G"], A, free, None, w["dt"], w["eta"], n, u,
                      v, a, parallel=parallel)
-        n += 1
-        el = time.perf_counter() - t0
-        if el >= seconds or n >= 1000:
-            break
-    return n, el
+        return time.perf_counter() - t0
+
+    # calibrate with 2 increments (first-touch of the work arrays included), then one call of
+    # as many increments as fit in the requested sample length
+    t2 = run(2)
+    n = max(1, min(1000, int(seconds / max(t2 / 2.0, 1e-9))))
+    return n, run(n)
 
 
 class ClockSampler:
@@ -354,7 +357,7 @@ def run_gpu(args, rank, world):
         "gpu_launches": args.steps * (1 + 2 * inc),
         "clocks": clocks,
     }
-    if world == 1:
+    if world == 1 and not args.no_cpu:
         threads = 1
         try:
             from oracle import gfref as R

@@ -15,6 +15,8 @@ from . import element as Element  # noqa: E402
 from .vector import Vector, VectorPartitioned  # noqa: E402
 from .matrix import MatrixDiagonal, MatrixDiagonalPartitioned  # noqa: E402
 from .dynamics import VelocityVerlet, elastic_stress, critical_dt  # noqa: E402
+from . import statics  # noqa: E402
+from .statics import ElasticStatic  # noqa: E402
 from ._lib import set_strict, GFGPUError  # noqa: E402
 
 __all__ = ["Mesh", "Element", "Vector", "VectorPartitioned", "MatrixDiagonal",

@@ -62,7 +62,8 @@ def parse_header(path=HEADER):
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     text = re.sub(r"//[^\n]*", "", text)
     protos = {}
-    for m in re.finditer(r"([A-Za-z_][A-Za-z0-9_ \*]*?)\b(gfgpu_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text):
+    for m in re.finditer(r"([A-Za-z_][A-Za-z0-9_ \*]*?)\b(gfgpu_[A-Za-z0-9_]+)\s*\(([^;{]*?)\)\s*;",
+                         text):
         ret, name, args = m.group(1).strip(), m.group(2), m.group(3).strip()
         if ret.startswith("typedef"):
             continue
@@ -105,8 +106,16 @@ def last_error():
 
 
 def call(name, *args):
-    """Call an int-returning entry point; raise GFGPUError on a non-zero status."""
-    f = getattr(lib(), name)
+    """Call an int-returning entry point; raise GFGPUError on a non-zero status.
+
+    Only entry points whose prototype was read from include/gfgpu.h are callable: without
+    argtypes ctypes would pass 64-bit pointers and sizes as 32-bit ints."""
+    L = lib()
+    if name not in _protos:
+        raise KeyError(f"{name} is not declared in {HEADER}")
+    if len(args) != len(_protos[name][1]):
+        raise TypeError(f"{name} takes {len(_protos[name][1])} arguments, got {len(args)}")
+    f = getattr(L, name)
     rc = f(*args)
     if f.restype is C.c_int and rc != 0:
         raise GFGPUError(name, rc, last_error())

@@ -176,6 +176,152 @@ k_elem_force_quad4_uniform(const int32_t* __restrict__ conn, const double* __res
     }
 }
 
+// Constants of the uniform Hex8 path (see k_elem_force_hex8_uniform).
+struct Hex8Uniform {
+    double dx, dy, dz;    // 1 / (4 h_i): dNx(m,0) = dx s_xi(m) (1 + s_eta eta)(1 + s_zeta zeta)
+    double w0x, w0y, w0z; // 8 vol d_i (constant-mode weights)
+    double w1x, w1y, w1z; // 8 g^2 vol d_i (linear modes)
+    double w2;            // 8 g^4 vol (trilinear mode)
+};
+
+// Uniform Hex8 (congruent axis-aligned boxes, 2x2x2 Gauss). Nodes in binary order
+// b = bx + 2 by + 4 bz (GooseFEM order 0,1,3,2,4,5,7,6), H = Walsh-Hadamard transform of the
+// nodal values. With A1 = -H1, A2 = -H2, A3 = -H4 (xi, eta, zeta), A4 = H3 (xi eta),
+// A6 = H5 (xi zeta), A5 = H6 (eta zeta), A7 = -H7 (xi eta zeta) the displacement gradient at a
+// Gauss point is
+//   du_j/dx = dx (A1 + eta A4 + zeta A6 + eta zeta A7), du_j/dy = dy (A2 + xi A4 + zeta A5 + ...),
+//   du_j/dz = dz (A3 + xi A6 + eta A5 + xi eta A7),
+// i.e. a constant part, three linear parts (xi, eta, zeta) and three bilinear parts. The 2x2x2
+// rule integrates products of distinct monomials to zero, so each part contributes its own
+// stress (lam tr(eps) I + 2G eps) and generalised force:
+//   F1..3 = 8 vol d_i sigma0(i,:),  F4 = 8g^2 vol (dx s_eta(0,:) + dy s_xi(1,:)),
+//   F5 = 8g^2 vol (dy s_zeta(1,:) + dz s_eta(2,:)),  F6 = 8g^2 vol (dx s_zeta(0,:) + dz s_xi(2,:)),
+//   F7_j = 8g^4 vol A7_j (d_j^2 (lam + 2G) + (sum of the other two d^2) G),
+// and the element force is the inverse transform f = sum_k P_k F_k (P_k the sign patterns).
+__device__ __forceinline__ void fwht8(double (&v)[8])
+{
+#pragma unroll
+    for (int h = 1; h < 8; h <<= 1)
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if ((i & h) == 0) {
+                double a = v[i], b = v[i + h];
+                v[i] = a + b;
+                v[i + h] = a - b;
+            }
+}
+
+__global__ void __launch_bounds__(128)
+k_elem_force_hex8_uniform(const int32_t* __restrict__ conn, const double* __restrict__ u,
+                          const double* __restrict__ Km, const double* __restrict__ Gm,
+                          int64_t nelem, Hex8Uniform c, double* __restrict__ fe)
+{
+    // GooseFEM node m -> binary position
+    constexpr int pos[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+    GF_FOR(e, nelem)
+    {
+        double H[3][8];
+        const int4* cp = reinterpret_cast<const int4*>(conn + e * 8);
+        int4 c0 = __ldg(cp), c1 = __ldg(cp + 1);
+        int nodes[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const double* un = u + static_cast<int64_t>(nodes[m]) * 3;
+            H[0][pos[m]] = __ldg(un);
+            H[1][pos[m]] = __ldg(un + 1);
+            H[2][pos[m]] = __ldg(un + 2);
+        }
+        fwht8(H[0]);
+        fwht8(H[1]);
+        fwht8(H[2]);
+        double K = __ldg(Km + e), G = __ldg(Gm + e);
+        double lam = fma(-2.0 / 3.0, G, K);
+        double G2 = 2.0 * G;
+        double l2g = lam + G2;
+        // A-vectors (component j)
+        double A1[3], A2[3], A3[3], A4[3], A5[3], A6[3], A7[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            A1[j] = -H[j][1];
+            A2[j] = -H[j][2];
+            A4[j] = H[j][3];
+            A3[j] = -H[j][4];
+            A6[j] = H[j][5];
+            A5[j] = H[j][6];
+            A7[j] = -H[j][7];
+        }
+        double F[8][3];
+        // constant part
+        {
+            double a[3][3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                a[0][j] = c.dx * A1[j];
+                a[1][j] = c.dy * A2[j];
+                a[2][j] = c.dz * A3[j];
+            }
+            double lt = lam * (a[0][0] + a[1][1] + a[2][2]);
+            double s00 = fma(G2, a[0][0], lt), s11 = fma(G2, a[1][1], lt), s22 = fma(G2, a[2][2], lt);
+            double s01 = G * (a[0][1] + a[1][0]);
+            double s02 = G * (a[0][2] + a[2][0]);
+            double s12 = G * (a[1][2] + a[2][1]);
+            F[1][0] = c.w0x * s00; F[1][1] = c.w0x * s01; F[1][2] = c.w0x * s02;
+            F[2][0] = c.w0y * s01; F[2][1] = c.w0y * s11; F[2][2] = c.w0y * s12;
+            F[3][0] = c.w0z * s02; F[3][1] = c.w0z * s12; F[3][2] = c.w0z * s22;
+        }
+        // linear parts
+        {
+            double p[3], q[3], r[3], s[3], t[3], w[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                p[j] = c.dy * A4[j]; // xi:   row 1
+                q[j] = c.dz * A6[j]; // xi:   row 2
+                r[j] = c.dx * A4[j]; // eta:  row 0
+                s[j] = c.dz * A5[j]; // eta:  row 2
+                t[j] = c.dx * A6[j]; // zeta: row 0
+                w[j] = c.dy * A5[j]; // zeta: row 1
+            }
+            double lxi = lam * (p[1] + q[2]);
+            double let = lam * (r[0] + s[2]);
+            double lze = lam * (t[0] + w[1]);
+            // sigma_xi rows 1, 2
+            double x10 = G * p[0], x11 = fma(G2, p[1], lxi), x12 = G * (p[2] + q[1]);
+            double x20 = G * q[0], x22 = fma(G2, q[2], lxi);
+            // sigma_eta rows 0, 2
+            double e00 = fma(G2, r[0], let), e01 = G * r[1], e02 = G * (r[2] + s[0]);
+            double e21 = G * s[1], e22 = fma(G2, s[2], let);
+            // sigma_zeta rows 0, 1
+            double z00 = fma(G2, t[0], lze), z01 = G * (t[1] + w[0]), z02 = G * t[2];
+            double z11 = fma(G2, w[1], lze), z12 = G * w[2];
+            F[4][0] = fma(c.w1x, e00, c.w1y * x10);
+            F[4][1] = fma(c.w1x, e01, c.w1y * x11);
+            F[4][2] = fma(c.w1x, e02, c.w1y * x12);
+            F[5][0] = fma(c.w1y, z01, c.w1z * e02);
+            F[5][1] = fma(c.w1y, z11, c.w1z * e21);
+            F[5][2] = fma(c.w1y, z12, c.w1z * e22);
+            F[6][0] = fma(c.w1x, z00, c.w1z * x20);
+            F[6][1] = fma(c.w1x, z01, c.w1z * x12);
+            F[6][2] = fma(c.w1x, z02, c.w1z * x22);
+        }
+        // trilinear part
+        {
+            double dx2 = c.dx * c.dx, dy2 = c.dy * c.dy, dz2 = c.dz * c.dz;
+            F[7][0] = c.w2 * A7[0] * fma(dx2, l2g, (dy2 + dz2) * G);
+            F[7][1] = c.w2 * A7[1] * fma(dy2, l2g, (dx2 + dz2) * G);
+            F[7][2] = c.w2 * A7[2] * fma(dz2, l2g, (dx2 + dy2) * G);
+        }
+        // inverse transform: f[b] = WHT(F')[b], F'_k = (-1)^|k| F_k in binary order
+        double* out = fe + e * 24;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double v[8] = {0.0, -F[1][j], -F[2][j], F[4][j], -F[3][j], F[6][j], F[5][j], -F[7][j]};
+            fwht8(v);
+#pragma unroll
+            for (int m = 0; m < 8; ++m) out[m * 3 + j] = v[pos[m]];
+        }
+    }
+}
+
 // ------------------------------------------------------------------ node kernels
 
 struct VerletCoef {
@@ -223,17 +369,17 @@ k_verlet_node(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
     }
 }
 
-__global__ void k_detect_quad4_uniform(const double* __restrict__ dNx, const double* __restrict__ vol,
-                                       int64_t nelem, const double* __restrict__ ref, double vref,
-                                       double tol_g, double tol_v, int* __restrict__ bad)
+// Flags any (element, Gauss point) whose dNx / vol differ from the uniform-box reference.
+__global__ void k_detect_uniform(const double* __restrict__ dNx, const double* __restrict__ vol,
+                                 int64_t nelem, int nip, int kk, const double* __restrict__ ref,
+                                 double vref, double tol_g, double tol_v, int* __restrict__ bad)
 {
-    GF_FOR(t, nelem * 4)
+    GF_FOR(t, nelem * nip)
     {
-        int q = static_cast<int>(t & 3);
-        const double* g = dNx + t * 8;
+        int q = static_cast<int>(t % nip);
+        const double* g = dNx + t * kk;
         bool ok = fabs(vol[t] - vref) <= tol_v;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) ok = ok && fabs(g[k] - ref[q * 8 + k]) <= tol_g;
+        for (int k = 0; k < kk; ++k) ok = ok && fabs(g[k] - ref[q * kk + k]) <= tol_g;
         if (!ok) *bad = 1;
     }
 }
@@ -257,15 +403,25 @@ __global__ void k_probe_fp64(int64_t iters, double* out)
 
 using namespace gfgpu;
 
-static int check_desc(const gfgpu_verlet_desc* d)
+// Checks of the elastic operator part of the descriptor (element kernel + assembly tables).
+static int check_operator(const gfgpu_verlet_desc* d)
 {
     GF_REQUIRE(d, "null descriptor");
     GF_REQUIRE((d->nne == 4 && d->ndim == 2) || (d->nne == 8 && d->ndim == 3),
                "only Quad4 and Hex8");
-    GF_REQUIRE(d->conn && d->dofs && d->csr_ptr && d->csr_idx && d->part && d->inv && d->K && d->G,
-               "null table");
+    GF_REQUIRE(d->conn && d->dofs && d->csr_ptr && d->csr_idx && d->K && d->G, "null table");
     GF_REQUIRE(d->uniform || (d->dNx && d->vol && d->nip > 0), "general path needs dNx and vol");
+    GF_REQUIRE(!d->uniform || (d->hx > 0.0 && d->hy > 0.0 && (d->ndim == 2 || d->hz > 0.0)),
+               "uniform path needs positive edge lengths");
     GF_REQUIRE(!too_big(d->nelem * d->nne * d->ndim) && !too_big(d->nnode * d->ndim), "too large");
+    return GFGPU_OK;
+}
+
+// Additional checks of the time-integration part.
+static int check_desc(const gfgpu_verlet_desc* d)
+{
+    GF_TRY(check_operator(d));
+    GF_REQUIRE(d->part && d->inv, "null table");
     GF_REQUIRE(d->dt > 0.0, "dt must be positive");
     return GFGPU_OK;
 }
@@ -293,7 +449,21 @@ static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, 
             d->conn, u, d->K, d->G, d->nelem, c, fe);
     }
     else if (d->uniform) {
-        return fail(GFGPU_ERR_UNSUPPORTED, "uniform path: Quad4 only in the explicit step");
+        Hex8Uniform c;
+        double g = 1.0 / std::sqrt(3.0);
+        double vq = d->hx * d->hy * d->hz / 8.0;
+        c.dx = 1.0 / (4.0 * d->hx);
+        c.dy = 1.0 / (4.0 * d->hy);
+        c.dz = 1.0 / (4.0 * d->hz);
+        c.w0x = 8.0 * vq * c.dx;
+        c.w0y = 8.0 * vq * c.dy;
+        c.w0z = 8.0 * vq * c.dz;
+        c.w1x = 8.0 * (g * g) * vq * c.dx;
+        c.w1y = 8.0 * (g * g) * vq * c.dy;
+        c.w1z = 8.0 * (g * g) * vq * c.dz;
+        c.w2 = 8.0 * (g * g) * (g * g) * vq;
+        k_elem_force_hex8_uniform<<<grid_for(d->nelem, 128), 128, 0, s>>>(d->conn, u, d->K, d->G,
+                                                                          d->nelem, c, fe);
     }
     else {
         unsigned g = grid_for(d->nelem, 128);
@@ -317,6 +487,14 @@ static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, 
     return check_launch("verlet element kernel");
 }
 
+// Element-kernel launch shared with the static solver (pcg.cu).
+int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
+                                  cudaStream_t s)
+{
+    GF_TRY(check_operator(d));
+    return launch_elem(d, u, fe, s);
+}
+
 extern "C" {
 
 int64_t gfgpu_verlet_workspace_bytes(const gfgpu_verlet_desc* d)
@@ -329,33 +507,50 @@ int64_t gfgpu_verlet_workspace_bytes(const gfgpu_verlet_desc* d)
 int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
                                 const double* vol_host, double rtol)
 {
-    // dNx_host / vol_host: the first element's dNx [nip,4,2] and vol [nip] (host copies); the
-    // device arrays d->dNx / d->vol are scanned on the GPU against the rectangle they imply.
+    // dNx_host / vol_host: the first element's dNx [nip,nne,ndim] and vol [nip] (host copies);
+    // the device arrays d->dNx / d->vol are scanned on the GPU against the box they imply.
     GF_REQUIRE(d && dNx_host && vol_host, "bad argument");
     d->uniform = 0;
-    if (!(d->nne == 4 && d->ndim == 2 && d->nip == 4) || !d->dNx || !d->vol) return GFGPU_OK;
+    bool q4 = d->nne == 4 && d->ndim == 2 && d->nip == 4;
+    bool h8 = d->nne == 8 && d->ndim == 3 && d->nip == 8;
+    if (!(q4 || h8) || !d->dNx || !d->vol) return GFGPU_OK;
+    const int nne = d->nne, nd = d->ndim, nip = d->nip, kk = nne * nd;
     double g = 1.0 / std::sqrt(3.0);
-    const double xi[4][2] = {{-g, -g}, {+g, -g}, {+g, +g}, {-g, +g}};
-    const double sx[4] = {-1, +1, +1, -1}, se[4] = {-1, -1, +1, +1};
-    // edge lengths from the first Gauss point: dNx(m=1,0) = ax (1 - eta_0), dNx(m=3,1) = ay (1 - xi_0)
-    double ax = dNx_host[1 * 2 + 0] / (1.0 - xi[0][1]);
-    double ay = dNx_host[3 * 2 + 1] / (1.0 - xi[0][0]);
-    if (!(ax > 0.0) || !(ay > 0.0)) return GFGPU_OK;
-    double hx = 1.0 / (2.0 * ax), hy = 1.0 / (2.0 * ay);
-    double ref[32];
+    // GooseFEM node and Gauss-point sign patterns (same order for nodes and Gauss points)
+    const int sg[8][3] = {{-1, -1, -1}, {+1, -1, -1}, {+1, +1, -1}, {-1, +1, -1},
+                          {-1, -1, +1}, {+1, -1, +1}, {+1, +1, +1}, {-1, +1, +1}};
+    // dN/dxi of the reference element: s_i(m) prod_{k != i} (1 + s_k(m) xi_k(q)) / 2^nd
+    double dn[8][8][3];
+    double scale = q4 ? 0.25 : 0.125;
+    for (int q = 0; q < nip; ++q)
+        for (int m = 0; m < nne; ++m)
+            for (int i = 0; i < nd; ++i) {
+                double v = scale * sg[m][i];
+                for (int k = 0; k < nd; ++k)
+                    if (k != i) v *= 1.0 + sg[m][k] * sg[q][k] * g;
+                dn[q][m][i] = v;
+            }
+    // box edge lengths from the first Gauss point of node 1 (all components non-zero)
+    double hh[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < nd; ++i) {
+        double ratio = dNx_host[1 * nd + i] / dn[0][1][i]; // = 2 / h_i
+        if (!(ratio > 0.0)) return GFGPU_OK;
+        hh[i] = 2.0 / ratio;
+    }
+    double ref[8 * 24];
     double gmax = 0.0;
-    for (int q = 0; q < 4; ++q)
-        for (int m = 0; m < 4; ++m) {
-            ref[q * 8 + m * 2 + 0] = ax * sx[m] * (1.0 + se[m] * xi[q][1]);
-            ref[q * 8 + m * 2 + 1] = ay * se[m] * (1.0 + sx[m] * xi[q][0]);
-            gmax = std::fmax(gmax, std::fabs(ref[q * 8 + m * 2 + 0]));
-            gmax = std::fmax(gmax, std::fabs(ref[q * 8 + m * 2 + 1]));
-        }
-    double vref = hx * hy / 4.0;
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < nip; ++q)
+        for (int m = 0; m < nne; ++m)
+            for (int i = 0; i < nd; ++i) {
+                double v = dn[q][m][i] * (2.0 / hh[i]);
+                ref[q * kk + m * nd + i] = v;
+                gmax = std::fmax(gmax, std::fabs(v));
+            }
+    double vref = q4 ? hh[0] * hh[1] / 4.0 : hh[0] * hh[1] * hh[2] / 8.0;
+    for (int q = 0; q < nip; ++q) {
         if (std::fabs(vol_host[q] - vref) > rtol * vref) return GFGPU_OK;
-        for (int k = 0; k < 8; ++k)
-            if (std::fabs(dNx_host[q * 8 + k] - ref[q * 8 + k]) > rtol * gmax) return GFGPU_OK;
+        for (int k = 0; k < kk; ++k)
+            if (std::fabs(dNx_host[q * kk + k] - ref[q * kk + k]) > rtol * gmax) return GFGPU_OK;
     }
     double* dref = nullptr;
     int* bad = nullptr;
@@ -363,8 +558,8 @@ int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
     GF_TRY(check_cuda(cudaMalloc(&bad, sizeof(int)), "cudaMalloc"));
     cudaMemcpy(dref, ref, sizeof(ref), cudaMemcpyHostToDevice);
     cudaMemset(bad, 0, sizeof(int));
-    k_detect_quad4_uniform<<<grid_for(d->nelem * 4), kBlock>>>(d->dNx, d->vol, d->nelem, dref, vref,
-                                                               rtol * gmax, rtol * vref, bad);
+    k_detect_uniform<<<grid_for(d->nelem * nip), kBlock>>>(d->dNx, d->vol, d->nelem, nip, kk, dref,
+                                                           vref, rtol * gmax, rtol * vref, bad);
     int hbad = 1;
     int rc = check_launch("detect_uniform");
     if (rc == GFGPU_OK)
@@ -374,9 +569,9 @@ int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
     GF_TRY(rc);
     if (!hbad) {
         d->uniform = 1;
-        d->hx = hx;
-        d->hy = hy;
-        d->hz = 0.0;
+        d->hx = hh[0];
+        d->hy = hh[1];
+        d->hz = hh[2];
     }
     return GFGPU_OK;
 }
@@ -417,7 +612,7 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
 int gfgpu_internal_force(const gfgpu_verlet_desc* d, const double* u, double* fint,
                          void* workspace, gfgpu_stream_t stream)
 {
-    GF_TRY(check_desc(d));
+    GF_TRY(check_operator(d));
     GF_REQUIRE(u && fint && workspace, "bad argument");
     double* fe = static_cast<double*>(workspace);
     GF_TRY(launch_elem(d, u, fe, S(stream)));
@@ -427,7 +622,7 @@ int gfgpu_internal_force(const gfgpu_verlet_desc* d, const double* u, double* fi
 int gfgpu_verlet_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                 gfgpu_stream_t stream)
 {
-    GF_TRY(check_desc(d));
+    GF_TRY(check_operator(d));
     GF_REQUIRE(u && fe, "bad argument");
     GF_REQUIRE((reinterpret_cast<uintptr_t>(fe) & 15u) == 0, "fe must be 16-byte aligned");
     return launch_elem(d, u, fe, S(stream));

@@ -1,0 +1,355 @@
+// Matrix-free Jacobi-preconditioned conjugate gradients for the static linear elastic problem
+// with prescribed displacements (the partitioned solve of MatrixPartitionedSolver,
+// MatrixPartitioned.h:526-642: A_uu x_u = b_u - A_up x_p), in FP64.
+//
+// The stiffness action A p is the internal force of the displacement p: the element kernel of
+// the explicit step (uniform closed form or general per-Gauss-point path) followed by a dof-CSR
+// gather. All vectors are nodevecs [nnode, ndim]; prescribed dofs (part >= nnu) are held at zero
+// in p, r, z. Dot products use a fixed grid and a fixed reduction tree, so every run gives the
+// same bits. The iteration scalars (alpha, beta) stay on the device; the host reads the residual
+// only every `check_every` iterations.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gfgpu {
+
+constexpr int kRedBlocks = 1024; // fixed: determinism of the reductions
+constexpr int kRedThreads = 256;
+
+// scalar slots
+enum { SC_RZ = 0, SC_RZ_NEW, SC_PQ, SC_RR, SC_BB, SC_ALPHA, SC_BETA, SC_COUNT };
+
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = lane < (blockDim.x >> 5) ? sh[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+    }
+    __syncthreads();
+    return r; // valid in thread 0
+}
+
+// Final fixed-order reduction of `nparts` partial rows (kRedBlocks each) into scalars.
+__global__ void k_reduce(const double* __restrict__ partials, int nparts, double* __restrict__ sc,
+                         int slot0)
+{
+    __shared__ double sh[32];
+    for (int p = 0; p < nparts; ++p) {
+        double v = 0.0;
+        for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) v += partials[p * kRedBlocks + i];
+        double s = block_sum(v, sh);
+        if (threadIdx.x == 0) sc[slot0 + p] = s;
+        __syncthreads();
+    }
+}
+
+// q = A p on free dofs (gather of the element forces), 0 on prescribed dofs; partial p.q.
+__global__ void __launch_bounds__(kRedThreads)
+k_pcg_gather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
+             const int32_t* __restrict__ idx, const int32_t* __restrict__ part, int64_t nnu,
+             const double* __restrict__ fe, const double* __restrict__ p, int64_t n,
+             double* __restrict__ q, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double acc = 0.0;
+    GF_FOR(t, n)
+    {
+        double f = 0.0;
+        if (__ldg(part + t) < nnu) {
+            int32_t d = __ldg(dofs + t);
+            int32_t b = __ldg(ptr + d), e = __ldg(ptr + d + 1);
+            for (int32_t j = b; j < e; ++j) f += __ldg(fe + __ldg(idx + j));
+            acc = fma(p[t], f, acc);
+        }
+        q[t] = f;
+    }
+    double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+__global__ void k_pcg_alpha(double* sc)
+{
+    if (threadIdx.x == 0) sc[SC_ALPHA] = sc[SC_RZ] / sc[SC_PQ];
+}
+
+// x += alpha p, r -= alpha q, z = M^-1 r (free dofs); partials r.z and r.r.
+__global__ void __launch_bounds__(kRedThreads)
+k_pcg_update(const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ minv,
+             const double* __restrict__ p, const double* __restrict__ q, int64_t n,
+             const double* __restrict__ sc, double* __restrict__ x, double* __restrict__ r,
+             double* __restrict__ z, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double alpha = sc[SC_ALPHA];
+    double rz = 0.0, rr = 0.0;
+    GF_FOR(t, n)
+    {
+        if (__ldg(part + t) < nnu) {
+            x[t] = fma(alpha, p[t], x[t]);
+            double rv = fma(-alpha, q[t], r[t]);
+            double zv = minv[t] * rv;
+            r[t] = rv;
+            z[t] = zv;
+            rz = fma(rv, zv, rz);
+            rr = fma(rv, rv, rr);
+        }
+    }
+    double s1 = block_sum(rz, sh);
+    double s2 = block_sum(rr, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = s1;
+        partial[kRedBlocks + blockIdx.x] = s2;
+    }
+}
+
+__global__ void k_pcg_beta(double* sc)
+{
+    if (threadIdx.x == 0) {
+        sc[SC_BETA] = sc[SC_RZ_NEW] / sc[SC_RZ];
+        sc[SC_RZ] = sc[SC_RZ_NEW];
+    }
+}
+
+// p = z + beta p
+__global__ void k_pcg_direction(const double* __restrict__ z, const double* __restrict__ sc,
+                                int64_t n, double* __restrict__ p)
+{
+    double beta = sc[SC_BETA];
+    GF_FOR(t, n) p[t] = fma(beta, p[t], z[t]);
+}
+
+// r = -(A x) on free dofs, 0 elsewhere; z = M^-1 r; partials r.z, r.r.
+__global__ void __launch_bounds__(kRedThreads)
+k_pcg_residual(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
+               const int32_t* __restrict__ idx, const int32_t* __restrict__ part, int64_t nnu,
+               const double* __restrict__ fe, const double* __restrict__ b,
+               const double* __restrict__ minv, int64_t n, double* __restrict__ r,
+               double* __restrict__ z, double* __restrict__ p, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double rz = 0.0, rr = 0.0;
+    GF_FOR(t, n)
+    {
+        double rv = 0.0, zv = 0.0;
+        if (__ldg(part + t) < nnu) {
+            int32_t d = __ldg(dofs + t);
+            double f = 0.0;
+            for (int32_t j = __ldg(ptr + d); j < __ldg(ptr + d + 1); ++j) f += __ldg(fe + __ldg(idx + j));
+            rv = (b ? b[t] : 0.0) - f;
+            zv = minv[t] * rv;
+            rz = fma(rv, zv, rz);
+            rr = fma(rv, rv, rr);
+        }
+        r[t] = rv;
+        z[t] = zv;
+        if (p) p[t] = zv;
+    }
+    double s1 = block_sum(rz, sh);
+    double s2 = block_sum(rr, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = s1;
+        partial[kRedBlocks + blockIdx.x] = s2;
+    }
+}
+
+// free dofs of v set to zero (copy of x with the unknowns removed)
+__global__ void k_keep_prescribed(const int32_t* __restrict__ part, int64_t nnu,
+                                  const double* __restrict__ x, int64_t n, double* __restrict__ o)
+{
+    GF_FOR(t, n) o[t] = part[t] < nnu ? 0.0 : x[t];
+}
+
+// Jacobi: diagonal of the element stiffness per (element, node, direction) for isotropic
+// linear elasticity, K_e[(m,j),(m,j)] = sum_q vol (lam dNx(m,j)^2 + G dNx(m,j)^2 + G |dNx(m,:)|^2).
+template <int NNE, int ND>
+__global__ void k_elem_diag(const double* __restrict__ dNx, const double* __restrict__ vol,
+                            const double* __restrict__ Km, const double* __restrict__ Gm,
+                            int64_t nelem, int nip, double* __restrict__ out)
+{
+    GF_FOR(t, nelem * NNE)
+    {
+        int64_t e = t / NNE;
+        int m = static_cast<int>(t - e * NNE);
+        double G = Gm[e], lam = Km[e] - 2.0 * G / 3.0;
+        double acc[ND];
+#pragma unroll
+        for (int j = 0; j < ND; ++j) acc[j] = 0.0;
+        for (int q = 0; q < nip; ++q) {
+            const double* g = dNx + ((e * nip + q) * NNE + m) * ND;
+            double v = vol[e * nip + q];
+            double n2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < ND; ++k) n2 += g[k] * g[k];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) acc[j] += v * ((lam + G) * g[j] * g[j] + G * n2);
+        }
+#pragma unroll
+        for (int j = 0; j < ND; ++j) out[t * ND + j] = acc[j];
+    }
+}
+
+__global__ void k_inv_free(const int32_t* __restrict__ part, int64_t nnu,
+                           const double* __restrict__ diag, int64_t n, double* __restrict__ minv)
+{
+    GF_FOR(t, n) minv[t] = part[t] < nnu ? 1.0 / diag[t] : 0.0;
+}
+
+struct PcgWs {
+    double *fe, *p, *r, *z, *q, *minv, *bvec, *partial, *sc;
+};
+
+static int64_t align256(int64_t b)
+{
+    return (b + 255) / 256 * 256;
+}
+
+static PcgWs carve(const gfgpu_verlet_desc* d, void* ws)
+{
+    char* c = static_cast<char*>(ws);
+    int64_t n = d->nnode * d->ndim;
+    PcgWs w;
+    w.fe = reinterpret_cast<double*>(c);
+    c += align256(d->nelem * d->nne * d->ndim * 8);
+    double** vecs[] = {&w.p, &w.r, &w.z, &w.q, &w.minv, &w.bvec};
+    for (auto v : vecs) {
+        *v = reinterpret_cast<double*>(c);
+        c += align256(n * 8);
+    }
+    w.partial = reinterpret_cast<double*>(c);
+    c += align256(2 * kRedBlocks * 8);
+    w.sc = reinterpret_cast<double*>(c);
+    return w;
+}
+
+static int64_t pcg_bytes(const gfgpu_verlet_desc* d)
+{
+    int64_t n = d->nnode * d->ndim;
+    return align256(d->nelem * d->nne * d->ndim * 8) + 6 * align256(n * 8) +
+           align256(2 * kRedBlocks * 8) + align256(SC_COUNT * 8 + 64);
+}
+
+} // namespace gfgpu
+
+using namespace gfgpu;
+
+// element kernel launch shared with the explicit step (dynamics.cu)
+int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
+                                  cudaStream_t s);
+
+extern "C" {
+
+int64_t gfgpu_pcg_workspace_bytes(const gfgpu_verlet_desc* d)
+{
+    return d ? pcg_bytes(d) : 0;
+}
+
+int gfgpu_elastic_diagonal(const gfgpu_verlet_desc* d, double* diag, void* workspace,
+                           gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d && diag && workspace && d->dNx && d->vol, "bad argument (needs dNx and vol)");
+    GF_REQUIRE((d->nne == 4 && d->ndim == 2) || (d->nne == 8 && d->ndim == 3), "Quad4 / Hex8 only");
+    double* fe = static_cast<double*>(workspace);
+    cudaStream_t s = S(stream);
+    if (d->nne == 4)
+        k_elem_diag<4, 2><<<grid_for(d->nelem * 4), kBlock, 0, s>>>(d->dNx, d->vol, d->K, d->G,
+                                                                   d->nelem, d->nip, fe);
+    else
+        k_elem_diag<8, 3><<<grid_for(d->nelem * 8), kBlock, 0, s>>>(d->dNx, d->vol, d->K, d->G,
+                                                                   d->nelem, d->nip, fe);
+    GF_TRY(check_launch("elastic_diagonal"));
+    return gfgpu_assemble_node(d->csr_ptr, d->csr_idx, d->dofs, d->nnode, d->ndim, fe, diag, stream);
+}
+
+int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, double tol,
+                    int64_t maxiter, int32_t check_every, void* workspace, gfgpu_stream_t stream,
+                    int64_t* iters, double* relres)
+{
+    GF_REQUIRE(d && diag && x && workspace && iters && relres && tol > 0.0 && maxiter >= 0,
+               "bad argument");
+    GF_REQUIRE(d->part && d->conn && d->csr_ptr && d->csr_idx && d->dofs && d->K && d->G,
+               "null table");
+    if (check_every < 1) check_every = 1;
+    cudaStream_t s = S(stream);
+    PcgWs w = carve(d, workspace);
+    int64_t n = d->nnode * d->ndim;
+    const unsigned gb = kRedBlocks;
+    double* hsc = nullptr;
+    GF_TRY(check_cuda(cudaMallocHost(&hsc, SC_COUNT * sizeof(double)), "cudaMallocHost"));
+    int rc = GFGPU_OK;
+    auto fail_out = [&](int code) {
+        cudaFreeHost(hsc);
+        return code;
+    };
+    k_inv_free<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, diag, n, w.minv);
+    // b = -(A x_p) on the free dofs
+    k_keep_prescribed<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.p);
+    if ((rc = gfgpu_internal_element_forces(d, w.p, w.fe, s)) != GFGPU_OK) return fail_out(rc);
+    k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
+                                               nullptr, w.minv, n, w.bvec, w.z, nullptr, w.partial);
+    k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_BB);
+    // r = b - A x, z = M^-1 r, p = z
+    if ((rc = gfgpu_internal_element_forces(d, x, w.fe, s)) != GFGPU_OK) return fail_out(rc);
+    k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
+                                               nullptr, w.minv, n, w.r, w.z, w.p, w.partial);
+    k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ); // SC_RZ, SC_RZ_NEW(=rr, overwritten)
+    if ((rc = check_launch("pcg set-up")) != GFGPU_OK) return fail_out(rc);
+    cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg set-up")) != GFGPU_OK) return fail_out(rc);
+    double bb = hsc[SC_BB];
+    double rr = hsc[SC_RZ_NEW];
+    double bnorm = std::sqrt(bb);
+    if (bnorm == 0.0) bnorm = 1.0;
+    int64_t it = 0;
+    double rel = std::sqrt(rr) / bnorm;
+    while (rel > tol && it < maxiter) {
+        int64_t nb = std::min<int64_t>(check_every, maxiter - it);
+        for (int64_t k = 0; k < nb; ++k) {
+            if ((rc = gfgpu_internal_element_forces(d, w.p, w.fe, s)) != GFGPU_OK) return fail_out(rc);
+            k_pcg_gather<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
+                                                     w.fe, w.p, n, w.q, w.partial);
+            k_reduce<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, SC_PQ);
+            k_pcg_alpha<<<1, 32, 0, s>>>(w.sc);
+            k_pcg_update<<<gb, kRedThreads, 0, s>>>(d->part, d->nnu, w.minv, w.p, w.q, n, w.sc, x,
+                                                     w.r, w.z, w.partial);
+            k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ_NEW); // SC_RZ_NEW, SC_PQ <- rr
+            k_pcg_beta<<<1, 32, 0, s>>>(w.sc);
+            k_pcg_direction<<<grid_for(n), kBlock, 0, s>>>(w.z, w.sc, n, w.p);
+        }
+        it += nb;
+        if ((rc = check_launch("pcg iteration")) != GFGPU_OK) return fail_out(rc);
+        cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
+        if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg iteration")) != GFGPU_OK)
+            return fail_out(rc);
+        rr = hsc[SC_PQ]; // second reduced row of the update: r.r
+        if (!std::isfinite(rr)) {
+            *iters = it;
+            *relres = rr;
+            return fail_out(fail(GFGPU_ERR_NAN, "gfgpu_pcg_solve: non-finite residual"));
+        }
+        rel = std::sqrt(rr) / bnorm;
+    }
+    // true residual b - A x
+    if ((rc = gfgpu_internal_element_forces(d, x, w.fe, s)) != GFGPU_OK) return fail_out(rc);
+    k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
+                                               w.bvec, w.minv, n, w.r, w.z, nullptr, w.partial);
+    k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ_NEW);
+    cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg final residual")) != GFGPU_OK)
+        return fail_out(rc);
+    *iters = it;
+    *relres = std::sqrt(hsc[SC_PQ]) / bnorm;
+    cudaFreeHost(hsc);
+    if (*relres > tol) return fail(GFGPU_ERR_DIVERGED, "gfgpu_pcg_solve: tolerance not reached");
+    return GFGPU_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,95 @@
+"""Static linear elastic solve with prescribed displacements, matrix-free on the GPU.
+
+The reference solves A_uu x_u = b_u - A_up x_p with an assembled sparse matrix and a direct
+factorisation (MatrixPartitioned.h:526-642). Here the stiffness action is the element kernel of the
+explicit step plus the deterministic CSR gather, and the solve is Jacobi-preconditioned CG in FP64
+(gfgpu_pcg_solve).
+"""
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+from . import mesh as _mesh
+from .element import Quad4, Hex8
+
+
+class ElasticStatic:
+    """Matrix-free linear elastic operator of a Quad4/Hex8 mesh with prescribed dofs `iip`.
+
+    K, G: per-element bulk and shear moduli. uniform: "auto" | True | False (closed-form element
+    kernel for congruent axis-aligned elements, see gfgpu_verlet_detect_uniform)."""
+
+    def __init__(self, coor, conn, dofs, K, G, iip, uniform="auto"):
+        from .vector import Vector
+
+        conn_h = _dev.host_i32(conn)
+        dofs_h = _dev.host_i32(dofs)
+        nelem, nne = conn_h.shape
+        nnode, nd = dofs_h.shape
+        self.nelem, self.nnode, self.nne, self.ndim = nelem, nnode, nne, nd
+        E = Quad4 if nne == 4 else Hex8
+        self.vector = Vector(conn_h, dofs_h)
+        self.quad = E.Quadrature(self.vector.AsElement(_dev.dev_f64(coor)))
+        self.iip = _dev.host_i32(iip)
+        self.iiu, part = _mesh.partition(dofs_h, self.iip)
+        self.part_d = _dev.dev_i32(part)
+        self.K = _dev.dev_f64(K)
+        self.G = _dev.dev_f64(G)
+        d = _lib.VerletDesc()
+        d.nelem, d.nnode, d.nne, d.ndim, d.nip = nelem, nnode, nne, nd, self.quad.nip()
+        d.conn = self.vector.conn_d.data_ptr()
+        d.dofs = self.vector.dofs_d.data_ptr()
+        d.csr_ptr = self.vector.csr_ptr.data_ptr()
+        d.csr_idx = self.vector.csr_idx.data_ptr()
+        d.part = self.part_d.data_ptr()
+        d.nnu = int(self.iiu.size)
+        d.dNx = self.quad.GradN().data_ptr()
+        d.vol = self.quad.dV().data_ptr()
+        d.K = self.K.data_ptr()
+        d.G = self.G.data_ptr()
+        d.dt = 1.0
+        d.uniform = 0
+        self.desc = d
+        if uniform is True or uniform == "auto":
+            g0 = self.quad.GradN()[0].detach().cpu().numpy().copy()
+            v0 = self.quad.dV()[0].detach().cpu().numpy().copy()
+            _lib.call("gfgpu_verlet_detect_uniform", C.addressof(d), g0.ctypes.data,
+                      v0.ctypes.data, 1e-12)
+            if uniform is True and not d.uniform:
+                raise RuntimeError("mesh is not uniform")
+        nbytes = int(_lib.lib().gfgpu_pcg_workspace_bytes(C.addressof(d)))
+        self.ws = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device=_dev.device())
+        self.diag = torch.empty((nnode, nd), dtype=torch.float64, device=_dev.device())
+        _lib.call("gfgpu_elastic_diagonal", C.addressof(d), self.diag.data_ptr(),
+                  self.ws.data_ptr(), _dev.stream())
+
+    @property
+    def uniform(self):
+        return bool(self.desc.uniform)
+
+    def use_general_path(self):
+        self.desc.uniform = 0
+
+    def force(self, u):
+        """Internal force (= stiffness action) of a displacement nodevec."""
+        u = _dev.dev_f64(u)
+        out = torch.empty_like(u)
+        _lib.call("gfgpu_internal_force", C.addressof(self.desc), u.data_ptr(), out.data_ptr(),
+                  self.ws.data_ptr(), _dev.stream())
+        return out
+
+    def solve(self, x, tol=1e-8, maxiter=100000, check_every=16):
+        """Solve in place: x (device nodevec) holds the prescribed values and the initial guess.
+        Returns (iterations, relative residual of the true residual)."""
+        if not (x.is_cuda and x.dtype == torch.float64 and x.is_contiguous()):
+            raise ValueError("x must be a contiguous float64 CUDA tensor")
+        _dev.check_shape(x, (self.nnode, self.ndim), "solve")
+        it = C.c_int64(0)
+        rel = C.c_double(0.0)
+        _lib.call("gfgpu_pcg_solve", C.addressof(self.desc), self.diag.data_ptr(), x.data_ptr(),
+                  float(tol), int(maxiter), int(check_every), self.ws.data_ptr(), _dev.stream(),
+                  C.addressof(it), C.addressof(rel))
+        return int(it.value), float(rel.value)

@@ -253,6 +253,27 @@ int gfgpu_internal_force(const gfgpu_verlet_desc* d, const double* u, double* fi
 int gfgpu_verlet_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                 gfgpu_stream_t stream);
 
+/* ============================ static solve (device) ======================================= */
+
+/* Matrix-free replacement of the partitioned direct solve (MatrixPartitioned.h:526-642,
+ * MatrixPartitionedSolver::solve: A_uu x_u = b_u - A_up x_p with b_u = 0) for linear
+ * elasticity: Jacobi-preconditioned CG in FP64 on the stiffness action of the element kernel.
+ * The descriptor `d` is the one of the explicit step (dt, eta, inv, fext are ignored); `part`
+ * and `nnu` mark the unknown dofs (part < nnu), all other dofs are prescribed. */
+int64_t gfgpu_pcg_workspace_bytes(const gfgpu_verlet_desc* d);
+/* Diagonal of the assembled stiffness as a nodevec (Jacobi preconditioner), from dNx/vol.
+ * `workspace` needs nelem*nne*ndim doubles. */
+int gfgpu_elastic_diagonal(const gfgpu_verlet_desc* d, double* diag, void* workspace,
+                           gfgpu_stream_t stream);
+/* Solve for the unknown dofs of the nodevec x (prescribed dofs hold the prescribed values and the
+ * unknown dofs the initial guess on entry). Stops when ||r|| / ||b|| <= tol (checked every
+ * `check_every` iterations on the host), then verifies the true residual b - A x. Synchronises.
+ * Returns GFGPU_ERR_DIVERGED when maxiter is reached first. Deterministic: fixed-grid
+ * reductions in a fixed order. */
+int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, double tol,
+                    int64_t maxiter, int32_t check_every, void* workspace, gfgpu_stream_t stream,
+                    int64_t* iters, double* relres);
+
 /* ============================ probes ====================================================== */
 
 /* FP64 FMA throughput probe: a kernel of independent DFMA chains, `blocks` x 256 threads,

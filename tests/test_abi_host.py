@@ -31,6 +31,26 @@ def test_exports_every_declared_symbol(lib):
     assert lib.lib().gfgpu_version().startswith(b"gfgpu")
 
 
+def test_binding_covers_every_declaration(lib):
+    """Every gfgpu_* prototype of the header is bound with the right number of argument types:
+    an unbound entry point would receive 64-bit pointers as 32-bit ints."""
+    import re
+
+    text = open(lib.HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    protos = lib.protos()
+    declared = re.findall(r"\b(gfgpu_\w+)\s*\(([^;{]*?)\)\s*;", text)
+    assert declared
+    for name, args in declared:
+        assert name in protos, name
+        nargs = 0 if args.strip() in ("", "void") else args.count(",") + 1
+        assert len(protos[name][1]) == nargs, name
+    with pytest.raises(KeyError):
+        lib.call("gfgpu_not_declared")
+    with pytest.raises(TypeError):
+        lib.call("gfgpu_set_strict")
+
+
 def test_mesh_against_reference_kat(lib):
     import goosefem_gb300 as gf
 

@@ -1,0 +1,125 @@
+"""GPU matrix-free Jacobi-PCG (static linear elasticity with prescribed displacements) against
+the oracle's assembled partitioned direct solve (oracle/statics.py)."""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from _common import RTOL, rel_err, seeded_field, seeded_material, to_np
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def gf():
+    import goosefem_gb300 as gf
+
+    return gf
+
+
+def _hex8_case(n, seed):
+    from oracle import gfref as R
+
+    coor, conn = R.hex8_regular(n, n, n)
+    K, G = seeded_material(n ** 3, seed)
+    nxy = (n + 1) ** 2
+    front = np.arange(nxy)
+    back = front + n * nxy
+    iip = np.unique(np.concatenate([(front[:, None] * 3 + np.arange(3)).ravel(), back * 3 + 2]))
+    xp = np.where(np.isin(iip, back * 3 + 2), -1e-2, 0.0)
+    return coor, conn, K, G, iip, xp
+
+
+def _solve_gpu(gf, coor, conn, K, G, iip, xp, uniform):
+    nnode, nd = coor.shape
+    dofs = np.arange(nnode * nd).reshape(nnode, nd)
+    st = gf.statics.ElasticStatic(coor, conn, dofs, K, G, iip, uniform=uniform)
+    x = torch.zeros((nnode, nd), dtype=torch.float64, device="cuda")
+    xv = x.view(-1)
+    xv[torch.as_tensor(iip, device="cuda").long()] = torch.as_tensor(xp, device="cuda")
+    it, rel = st.solve(x, tol=1e-8)
+    return st, x, it, rel
+
+
+@pytest.mark.parametrize("uniform", [True, False])
+def test_hex8_uniform_force_matches_oracle(gf, oracle, uniform):
+    """Stiffness action: closed-form uniform Hex8 kernel and general kernel vs the reference
+    chain (SymGradN_vector -> stress -> Int_gradN_dot_tensor2_dV -> AssembleNode)."""
+    R = oracle
+    for (nx, ny, nz, sc) in ((5, 4, 3, (1.0, 1.0, 1.0)), (4, 3, 5, (0.6, 1.3, 0.9))):
+        coor, conn = R.hex8_regular(nx, ny, nz)
+        coor = coor * np.array(sc)
+        K, G = seeded_material(conn.shape[0], 40)
+        nnode = coor.shape[0]
+        dofs = np.arange(nnode * 3).reshape(nnode, 3)
+        st = gf.statics.ElasticStatic(coor, conn, dofs, K, G, np.array([0, 1, 2]),
+                                      uniform=uniform)
+        assert st.uniform == uniform
+        u = seeded_field((nnode, 3), 41)
+        dNx, vol = R.compute_dN(R.as_element(conn, coor), *R.hex8_gauss())
+        eps = R.sym_grad_n_vector(dNx, R.as_element(conn, u))
+        f_r = R.assemble_node(conn, dofs, R.int_grad_n_dot_tensor2_dv(dNx, vol, R.elastic_stress(
+            eps, K, G)))
+        assert rel_err(to_np(st.force(u)), f_r) <= RTOL
+
+
+@pytest.mark.parametrize("uniform", [True, False])
+def test_pcg_vs_direct_solve_small(gf, oracle, uniform):
+    from oracle import statics as S
+
+    coor, conn, K, G, iip, xp = _hex8_case(10, 42)
+    A = S.stiffness(coor, conn, K, G)
+    x_ref = S.solve_partitioned(A, iip, xp)
+    st, x, it, rel = _solve_gpu(gf, coor, conn, K, G, iip, xp, uniform)
+    xg = to_np(x).ravel()
+    assert rel <= 1e-8
+    assert S.residual(A, iip, xg) <= 1e-8  # the oracle's own residual of the GPU answer
+    assert np.linalg.norm(xg - x_ref) / np.linalg.norm(x_ref) <= 1e-6
+    assert np.array_equal(xg[iip], xp)
+
+
+def test_pcg_vs_direct_solve_32(gf, oracle):
+    """The 32^3 case against the committed direct-solve fixture (tests/golden/hex8_32_static.npz,
+    made by tests/golden/make_static_golden.py)."""
+    from oracle import statics as S
+
+    path = os.path.join(HERE, "golden", "hex8_32_static.npz")
+    fx = np.load(path)
+    coor, conn, K, G, iip, xp = _hex8_case(32, 3)
+    st, x, it, rel = _solve_gpu(gf, coor, conn, K, G, iip, xp, True)
+    xg = to_np(x).ravel()
+    A = S.stiffness(coor, conn, K, G)
+    assert rel <= 1e-8 and S.residual(A, iip, xg) <= 1e-8
+    x_ref = fx["x"].ravel()
+    assert np.linalg.norm(xg - x_ref) / np.linalg.norm(x_ref) <= 1e-6
+
+
+def test_pcg_is_deterministic(gf, oracle):
+    coor, conn, K, G, iip, xp = _hex8_case(8, 43)
+    _, x1, it1, r1 = _solve_gpu(gf, coor, conn, K, G, iip, xp, True)
+    _, x2, it2, r2 = _solve_gpu(gf, coor, conn, K, G, iip, xp, True)
+    assert it1 == it2 and r1 == r2 and torch.equal(x1, x2)
+
+
+def test_pcg_quad4(gf, oracle):
+    """2-d: bottom edge fixed, top edge uy = -1e-2."""
+    from oracle import statics as S
+
+    R = oracle
+    coor, conn = R.quad4_regular(24, 16)
+    K, G = seeded_material(conn.shape[0], 44)
+    bot = np.arange(25)
+    top = bot + 16 * 25
+    iip = np.unique(np.concatenate([(bot[:, None] * 2 + np.arange(2)).ravel(), top * 2 + 1]))
+    xp = np.where(np.isin(iip, top * 2 + 1), -1e-2, 0.0)
+    A = S.stiffness(coor, conn, K, G)
+    x_ref = S.solve_partitioned(A, iip, xp)
+    st, x, it, rel = _solve_gpu(gf, coor, conn, K, G, iip, xp, "auto")
+    assert st.uniform
+    xg = to_np(x).ravel()
+    assert S.residual(A, iip, xg) <= 1e-8
+    assert np.linalg.norm(xg - x_ref) / np.linalg.norm(x_ref) <= 1e-6
