@@ -46,8 +46,15 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="bounded CPU-baseline sample length")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
-    p.add_argument("--path", default="auto", choices=["auto", "general"],
-                   help="element kernel: auto (uniform fast path when applicable) or general")
+    p.add_argument("--workload", default="explicit", choices=["explicit", "static", "batch"],
+                   help="explicit: 2048^2 Quad4 dynamics (headline); static: Hex8 n3d^3 Jacobi-PCG;"
+                        " batch: periodic Quad4 instances")
+    p.add_argument("--n3d", type=int, default=128)
+    p.add_argument("--ninst", type=int, default=256)
+    p.add_argument("--batch-steps", type=int, default=500)
+    p.add_argument("--path", default="auto", choices=["auto", "uniform", "general"],
+                   help="element kernel: auto (fastest applicable), uniform (closed form with K, G "
+                        "read every increment) or general (per Gauss point, stored dNx)")
     return p.parse_args()
 
 
@@ -218,8 +225,10 @@ def run_gpu(args, rank, world):
     w = workload(args.nx, gf.Mesh)
     nnode, nelem, inc = w["nnode"], w["nelem"], args.increments
     vv = gf.VelocityVerlet(w["coor"], w["conn"], w["dofs"], w["K"], w["G"], rho=1.0, dt=w["dt"],
-                           eta=w["eta"], iip=w["iip"], uniform=("auto" if args.path == "auto"
-                                                                else False))
+                           eta=w["eta"], iip=w["iip"], uniform=(False if args.path == "general"
+                                                                else "auto"))
+    if args.path == "uniform":
+        vv.use_uniform_onthefly()
     u = torch.zeros((nnode, 2), dtype=torch.float64, device=dev)
     v = torch.tensor(w["v0"], device=dev)
     a = torch.zeros_like(u)
@@ -317,14 +326,26 @@ def run_gpu(args, rank, world):
     if os.path.exists(peaks_path):
         hbm_peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
-    uniform = vv.uniform
-    # algorithmic bytes of one element-kernel launch: u (16 B/node), conn (16 B/elem),
-    # K and G (16 B/elem), element forces out (64 B/elem); general path adds dNx + vol (72 B/elem)
-    b_elem = 16 * nnode + (16 + 16 + 64) * nelem + (0 if uniform else 72 * nelem)
+    path = vv.path
+    kernel = {"uniform-square": "k_elem_force_quad4_square", "uniform": "k_elem_force_quad4_uniform",
+              "general": "k_elem_force_general"}[path]
+    # algorithmic bytes of one element-kernel launch: u (16 B/node), conn (16 B/elem), material
+    # (K, G: 16 B/elem, or the 4 precomputed coefficients: 32 B/elem), element forces out
+    # (64 B/elem); the general path also streams dNx and vol (72 B/elem)
+    mat = 32 if path == "uniform-square" else 16
+    b_elem = 16 * nnode + (16 + mat + 64) * nelem + (72 * nelem if path == "general" else 0)
     achieved = b_elem / (ms_elem * 1e-3) / 1e9
-    # FP64 operations of the element kernel per element (DFMA counted as 2)
-    fl_elem = 55 if uniform else 4 * (8 * 2 + 8 * 2 + 2 + 12 + 16 * 2 + 8)
+    # FP64 operations of the element kernel per element, DFMA counted as 2 (from the source:
+    # square 34 instructions incl. 2 DFMA; uniform 48 incl. 7; general per Gauss point 8+8+9 FMA
+    # strain, 7 stress, 16 FMA + 8 force)
+    fl_elem = {"uniform-square": 36, "uniform": 55, "general": 4 * (2 * 25 + 7 + 2 * 16 + 8)}[path]
     fp64_ach = fl_elem * nelem / (ms_elem * 1e-3)
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", f"{kernel}_{args.nx}.txt")
+    if os.path.exists(prof):
+        for ln in open(prof):
+            if ln.startswith("dram_bytes_per_launch:"):
+                traffic = float(ln.split(":", 1)[1])
     # fused-step minimum traffic: u, v, a read+write (96 B/node), inverse mass (16 B/node),
     # K, G (16 B/elem)
     b_step = 112 * nnode + 16 * nelem
@@ -336,12 +357,12 @@ def run_gpu(args, rank, world):
         "config": {"workload": f"Quad4 Regular {args.nx}x{args.nx} explicit velocity-Verlet, "
                                "per-element K,G, density 1, damping 0.1, bottom row fixed",
                    "nelem": nelem, "nnode": nnode, "increments_per_step": inc,
-                   "element_path": "uniform" if uniform else "general",
+                   "element_path": path,
                    "l2": "inputs larger than L2 (working set > 0.6 GB); no flush",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "kernel": "k_elem_force_quad4_uniform" if uniform
-                     else "k_elem_force_general", "achieved": achieved, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+        "roofline": {"bound": "hbm", "binding_resource": "fp64 issue rate (see fp64)",
+                     "kernel": kernel, "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                      "peak_source": peak_src, "ms_per_launch": ms_elem,
                      "alg_bytes_per_launch": b_elem,
                      "fp64": {"achieved_tflops": fp64_ach / 1e12,
@@ -376,12 +397,119 @@ def run_gpu(args, rank, world):
     return 0
 
 
+def static_case(n, seed=3):
+    """Hex8 Regular n^3 (h = 1), K ~ U[0.5,1.5], G ~ U[0.25,0.75] per element, z = 0 face fixed,
+    z = top face uz = -1e-2 (ux, uy free)."""
+    from oracle import gfref as R
+
+    coor, conn = R.hex8_regular(n, n, n)
+    rng = np.random.default_rng(seed)
+    K = rng.uniform(0.5, 1.5, n ** 3)
+    G = rng.uniform(0.25, 0.75, n ** 3)
+    nxy = (n + 1) ** 2
+    front = np.arange(nxy)
+    back = front + n * nxy
+    iip = np.unique(np.concatenate([(front[:, None] * 3 + np.arange(3)).ravel(), back * 3 + 2]))
+    xp = np.where(np.isin(iip, back * 3 + 2), -1e-2, 0.0)
+    return coor, conn, K, G, iip, xp
+
+
+def run_static(args):
+    """3-d static case: Hex8 128^3 matrix-free Jacobi-PCG to 1e-8 relative residual (FP64).
+    One bench step = one full solve from a zero initial guess."""
+    import torch
+
+    import goosefem_gb300 as gf
+
+    n = args.n3d
+    coor, conn, K, G, iip, xp = static_case(n)
+    nnode = coor.shape[0]
+    dofs = np.arange(nnode * 3).reshape(nnode, 3)
+    st = gf.ElasticStatic(coor, conn, dofs, K, G, iip,
+                          uniform=("auto" if args.path == "auto" else False))
+    iip_d = torch.as_tensor(iip, device="cuda").long()
+    xp_d = torch.as_tensor(xp, device="cuda")
+    x = torch.zeros((nnode, 3), dtype=torch.float64, device="cuda")
+
+    def solve():
+        x.zero_()
+        x.view(-1)[iip_d] = xp_d
+        return st.solve(x, tol=1e-8, check_every=16)
+
+    for _ in range(args.warmup):
+        solve()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    its = []
+    for _ in range(args.steps):
+        its.append(solve())
+    torch.cuda.synchronize()
+    sec = (time.perf_counter() - t0) / args.steps
+    it, rel = its[-1]
+    line = {"metric": "time-to-1e-8 resid (Jacobi-PCG)", "value": sec, "unit": "s",
+            "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": sec * 1e3, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"Hex8 Regular {n}^3 static, z=0 fixed, top uz=-1e-2, "
+                                   "matrix-free Jacobi-PCG", "element_path":
+                       "uniform" if st.uniform else "general"},
+            "iterations": it, "relres_true": rel, "ms_per_iteration": sec * 1e3 / it,
+            "elem_updates_per_s": n ** 3 * 8 * it / sec}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batch(args):
+    """256 periodic Quad4 instances (nx, ny ~ U{32..512}), 500 increments each, one batched
+    launch schedule (autotuned) vs the instances one at a time."""
+    import torch
+
+    from goosefem_gb300 import batch as B
+
+    inst = B.seeded_instances(args.ninst, 256)
+    bv = B.BatchedVerlet(inst)
+    table = bv.autotune(nsteps=20, reps=2)
+    nsteps = args.batch_steps
+    u, v, a = bv.state()
+    bv.run_graph(u, v, a, nsteps)  # warm-up (also builds the graph)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    u, v, a = bv.state()
+    e0.record()
+    bv.run_graph(u, v, a, nsteps)
+    e1.record()
+    torch.cuda.synchronize()
+    if bv.mode == 1:
+        bv.check_status()
+    sec = e0.elapsed_time(e1) * 1e-3
+    seq = B.run_sequential(inst, nsteps, bv.dt)
+    line = {"metric": "elem-Gauss-pt updates/s (batched)", "value": bv.nelem * 4 * nsteps / sec,
+            "unit": "elem-Gauss-pt/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"{len(inst)} periodic Quad4 Regular instances, nx,ny~U{{32..512}},"
+                                   f" {nsteps} increments, applied shear 1e-3",
+                       "nelem_total": bv.nelem, "schedule": {"mode": ["graph of 2 kernels",
+                                                                       "persistent"][bv.mode],
+                                                             "block": bv.block,
+                                                             "blocks_per_sm": bv.bps}},
+            "seconds": sec, "sequential_seconds": seq, "speedup_vs_sequential": seq / sec,
+            "autotune": [{"mode": r[0], "block": r[1], "bps": r[2], "ms_per_increment": r[3]}
+                         for r in table]}
+    print(json.dumps(line), flush=True)
+    bv.release()
+    return 0
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "static":
+        return run_static(args)
+    if args.workload == "batch":
+        return run_batch(args)
     if world > 1:
         import torch
 

@@ -33,6 +33,7 @@ class VerletDesc(C.Structure):
         ("dNx", C.c_void_p), ("vol", C.c_void_p), ("K", C.c_void_p), ("G", C.c_void_p),
         ("fext", C.c_void_p), ("dt", C.c_double), ("eta", C.c_double),
         ("uniform", C.c_int32), ("hx", C.c_double), ("hy", C.c_double), ("hz", C.c_double),
+        ("coef", C.c_void_p),
     ]
 
 
@@ -42,6 +43,7 @@ _CTYPE = {
     "int64_t": C.c_int64,
     "double": C.c_double,
     "gfgpu_stream_t": C.c_void_p,
+    "gfgpu_graph_t": C.c_void_p,
     "void": None,
 }
 

@@ -1,0 +1,194 @@
+"""Batched explicit dynamics of many independent Quad4 Regular meshes on one GPU.
+
+Every instance has its own size, per-element moduli, fully periodic dofs
+(RegularBase::dofsPeriodic, Mesh.h:291-306) and an applied mean shear (the affine displacement
+of docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:88-98). The instances are concatenated
+into one block-diagonal mesh (node and dof numbers offset per instance), so one launch covers
+all of them: either a CUDA graph of the two kernels per increment, or one persistent cooperative
+kernel for all increments. `autotune` times both (and the persistent block shapes) on a few
+increments and keeps the fastest.
+"""
+
+import ctypes as C
+import time
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+from .dynamics import VelocityVerlet, critical_dt
+from . import mesh as _mesh
+
+
+class Instance:
+    """One periodic Quad4 Regular mesh with per-element K, G and an applied shear."""
+
+    def __init__(self, nx, ny, K, G, gamma):
+        self.nx, self.ny = int(nx), int(ny)
+        self.mesh = _mesh.Quad4.Regular(self.nx, self.ny)
+        self.K = np.asarray(K, dtype=np.float64)
+        self.G = np.asarray(G, dtype=np.float64)
+        self.gamma = float(gamma)
+
+    def initial_displacement(self):
+        """u_x = gamma (y - y0): the affine simple shear of main.cpp:88-98 (mean eps_01 = gamma/2)."""
+        coor = self.mesh.coor()
+        u = np.zeros_like(coor)
+        u[:, 0] = self.gamma * (coor[:, 1] - coor[0, 1])
+        return u
+
+
+def seeded_instances(n, seed, nmin=32, nmax=512, eps01=1e-3):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        nx, ny = rng.integers(nmin, nmax + 1, 2)
+        K = rng.uniform(0.5, 1.5, nx * ny)
+        G = rng.uniform(0.25, 0.75, nx * ny)
+        out.append(Instance(nx, ny, K, G, 2.0 * eps01))
+    return out
+
+
+class BatchedVerlet:
+    """All instances in one device-resident block-diagonal system."""
+
+    def __init__(self, instances, dt=None, eta=0.1, rho=1.0):
+        coor, conn, dofs, K, G, u0 = [], [], [], [], [], []
+        noff = doff = 0
+        self.offsets = []
+        for inst in instances:
+            m = inst.mesh
+            c = m.coor()
+            # shift instances apart in space (geometry only; they share no nodes)
+            coor.append(c)
+            conn.append(m.conn() + noff)
+            d = m.dofsPeriodic()
+            dofs.append(d + doff)
+            K.append(inst.K)
+            G.append(inst.G)
+            u0.append(inst.initial_displacement())
+            self.offsets.append((noff, m.nnode()))
+            noff += m.nnode()
+            doff += int(d.max()) + 1
+        self.instances = instances
+        self.coor = np.concatenate(coor)
+        self.conn = np.concatenate(conn)
+        self.dofs = np.concatenate(dofs)
+        self.K = np.concatenate(K)
+        self.G = np.concatenate(G)
+        self.u0 = np.concatenate(u0)
+        self.nelem = self.conn.shape[0]
+        self.nnode = self.coor.shape[0]
+        self.dt = 0.1 * critical_dt(self.K, self.G, rho) if dt is None else float(dt)
+        self.vv = VelocityVerlet(self.coor, self.conn, self.dofs, self.K, self.G, rho=rho,
+                                 dt=self.dt, eta=eta, iip=None)
+        if not self.vv.uniform:
+            raise RuntimeError("batched instances must be uniform Quad4 meshes")
+        nbytes = int(_lib.lib().gfgpu_verlet_persistent_workspace_bytes(C.addressof(self.vv.desc)))
+        self.pws = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device=_dev.device())
+        self.mode = 0
+        self.block = 256
+        self.bps = 0
+        self.timeout = 4_000_000_000  # SM cycles (about 2 s) per barrier wait
+        self._graph = None
+        self._graph_key = None
+
+    def state(self):
+        u = torch.tensor(self.u0, device=_dev.device())
+        v = torch.zeros_like(u)
+        a = torch.zeros_like(u)
+        return u, v, a
+
+    # ------------------------------------------------------------------ execution
+    def run_direct(self, u, v, a, nsteps):
+        if self.mode == 0:
+            self.vv.step(u, v, a, nsteps)
+        else:
+            _lib.call("gfgpu_verlet_persistent", C.addressof(self.vv.desc), u.data_ptr(),
+                      v.data_ptr(), a.data_ptr(), int(nsteps), self.block, self.bps, self.timeout,
+                      self.pws.data_ptr(), _dev.stream())
+            self.check_status()
+
+    def check_status(self):
+        st = C.c_int(0)
+        _lib.call("gfgpu_verlet_persistent_status", C.addressof(self.vv.desc), self.pws.data_ptr(),
+                  C.addressof(st), _dev.stream())
+        if st.value != 0:
+            raise _lib.GFGPUError("gfgpu_verlet_persistent", st.value, "grid barrier timed out")
+
+    def graph(self, u, v, a, nsteps):
+        key = (u.data_ptr(), v.data_ptr(), a.data_ptr(), int(nsteps), self.mode, self.block,
+               self.bps)
+        if self._graph_key != key:
+            self.release()
+            g = C.c_void_p(None)
+            ws = self.vv.ws if self.mode == 0 else self.pws
+            _lib.call("gfgpu_verlet_graph_create", C.addressof(self.vv.desc), u.data_ptr(),
+                      v.data_ptr(), a.data_ptr(), int(nsteps), self.mode, self.block, self.bps,
+                      self.timeout, ws.data_ptr(), C.addressof(g))
+            self._graph, self._graph_key = g.value, key
+        return self._graph
+
+    def run_graph(self, u, v, a, nsteps):
+        _lib.call("gfgpu_graph_launch", self.graph(u, v, a, nsteps), _dev.stream())
+
+    def release(self):
+        if self._graph is not None:
+            _lib.call("gfgpu_graph_destroy", self._graph)
+            self._graph, self._graph_key = None, None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def autotune(self, nsteps=20, reps=2):
+        """Time the candidate schedules on `nsteps` increments; keep the fastest. Returns the
+        table of (mode, block, blocks_per_sm, ms per increment)."""
+        cands = [(0, 256, 0)] + [(1, b, bps) for b in (128, 256) for bps in (0, 1, 2)]
+        table = []
+        best = None
+        for mode, block, bps in cands:
+            self.mode, self.block, self.bps = mode, block, bps
+            u, v, a = self.state()
+            try:
+                self.run_direct(u, v, a, 2)
+                torch.cuda.synchronize()
+                t = []
+                for _ in range(reps):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    self.run_direct(u, v, a, nsteps)
+                    e1.record()
+                    torch.cuda.synchronize()
+                    t.append(e0.elapsed_time(e1) / nsteps)
+                ms = min(t)
+            except _lib.GFGPUError:
+                ms = float("inf")
+            table.append((mode, block, bps, ms))
+            if best is None or ms < best[3]:
+                best = (mode, block, bps, ms)
+        self.mode, self.block, self.bps = best[:3]
+        return table
+
+
+def run_sequential(instances, nsteps, dt, eta=0.1):
+    """The instances one at a time (their own VelocityVerlet each); returns the GPU seconds."""
+    total = 0.0
+    for inst in instances:
+        m = inst.mesh
+        vv = VelocityVerlet(m.coor(), m.conn(), m.dofsPeriodic(), inst.K, inst.G, dt=dt, eta=eta)
+        u = torch.tensor(inst.initial_displacement(), device=_dev.device())
+        v = torch.zeros_like(u)
+        a = torch.zeros_like(u)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        vv.step(u, v, a, nsteps)
+        e1.record()
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1) * 1e-3
+    return total

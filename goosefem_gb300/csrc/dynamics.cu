@@ -13,6 +13,7 @@
 // (e, m, i) order (the serial order of Vector.h:724-741, deterministic), then performs the three
 // velocity estimates of docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:129-157 and the
 // displacement predictor of the next increment (main.cpp:119).
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -135,12 +136,12 @@ struct Quad4Uniform {
 //   P = cx [sigma_bar(0,0), sigma_bar(0,1)],  Q = cy [sigma_bar(1,0), sigma_bar(1,1)],
 //   H_0 = (hx2 (lam + 2G) + hy2 G) A3_x,  H_1 = (hx2 G + hy2 (lam + 2G)) A3_y,
 // sigma_bar the plane-strain stress of the mean strain, lam = K - 2G/3.
-__global__ void __launch_bounds__(256)
-k_elem_force_quad4_uniform(const int32_t* __restrict__ conn, const double* __restrict__ u,
-                           const double* __restrict__ Km, const double* __restrict__ Gm,
-                           int64_t nelem, Quad4Uniform c, double* __restrict__ fe)
+__device__ __forceinline__ void quad4_uniform_elem(int64_t e, const int32_t* __restrict__ conn,
+                                                   const double* __restrict__ u,
+                                                   const double* __restrict__ Km,
+                                                   const double* __restrict__ Gm,
+                                                   const Quad4Uniform& c, double* __restrict__ fe)
 {
-    GF_FOR(e, nelem)
     {
         int4 cn = __ldg(reinterpret_cast<const int4*>(conn) + e);
         double2 u0 = __ldg(reinterpret_cast<const double2*>(u) + cn.x);
@@ -174,6 +175,75 @@ k_elem_force_quad4_uniform(const int32_t* __restrict__ conn, const double* __res
         fo[2] = make_double2(Sx + H0, Sy + H1);
         fo[3] = make_double2(-(Dx + H0), -(Dy + H1));
     }
+}
+
+__global__ void __launch_bounds__(256)
+k_elem_force_quad4_uniform(const int32_t* __restrict__ conn, const double* __restrict__ u,
+                           const double* __restrict__ Km, const double* __restrict__ Gm,
+                           int64_t nelem, Quad4Uniform c, double* __restrict__ fe)
+{
+    GF_FOR(e, nelem) quad4_uniform_elem(e, conn, u, Km, Gm, c, fe);
+}
+
+// Square elements (hx = hy): the constants of the closed form reduce to four per-element
+// coefficients that depend on K and G only (c ax = 1/4, hx2 = hy2 = g^2/4):
+//   P0 = L t + M A1x, Q1 = L t + M A2y (t = A1x + A2y), P1 = Q0 = N (A1y + A2x),
+//   H_j = kH A3_j,  with L = lam/4, M = G/2, N = G/4, kH = g^2 (lam + 3G) / 4.
+// They are computed once (gfgpu_verlet_precompute); the element kernel then needs 34 FP64
+// instructions per element.
+__global__ void k_quad4_square_coef(const double* __restrict__ Km, const double* __restrict__ Gm,
+                                    int64_t nelem, double g2, double* __restrict__ coef)
+{
+    GF_FOR(e, nelem)
+    {
+        double K = Km[e], G = Gm[e];
+        double lam = K - 2.0 * G / 3.0;
+        double2* o = reinterpret_cast<double2*>(coef) + e * 2;
+        o[0] = make_double2(0.25 * lam, 0.5 * G);
+        o[1] = make_double2(0.25 * G, 0.25 * g2 * (lam + 3.0 * G));
+    }
+}
+
+template <bool CG>
+__device__ __forceinline__ double2 ld2(const double2* p)
+{
+    if constexpr (CG) return __ldcg(p);
+    else return __ldg(p);
+}
+
+template <bool CG>
+__device__ __forceinline__ void quad4_square_elem(int64_t e, const int32_t* __restrict__ conn,
+                                                  const double* u,
+                                                  const double* __restrict__ coef, double* fe)
+{
+    int4 cn = __ldg(reinterpret_cast<const int4*>(conn) + e);
+    const double2* u2 = reinterpret_cast<const double2*>(u);
+    double2 u0 = ld2<CG>(u2 + cn.x), u1 = ld2<CG>(u2 + cn.y), u2v = ld2<CG>(u2 + cn.z),
+            u3 = ld2<CG>(u2 + cn.w);
+    double2 c01 = __ldg(reinterpret_cast<const double2*>(coef) + 2 * e);
+    double2 c23 = __ldg(reinterpret_cast<const double2*>(coef) + 2 * e + 1);
+    double L = c01.x, M = c01.y, N = c23.x, kH = c23.y;
+    double px = u2v.x - u0.x, qx = u1.x - u3.x;
+    double py = u2v.y - u0.y, qy = u1.y - u3.y;
+    double A1x = px + qx, A2x = px - qx, A3x = (u0.x + u2v.x) - (u1.x + u3.x);
+    double A1y = py + qy, A2y = py - qy, A3y = (u0.y + u2v.y) - (u1.y + u3.y);
+    double Lt = L * (A1x + A2y);
+    double P0 = fma(M, A1x, Lt), Q1 = fma(M, A2y, Lt);
+    double P1 = N * (A1y + A2x); // = Q0
+    double H0 = kH * A3x, H1 = kH * A3y;
+    double Sx = P0 + P1, Dx = P0 - P1, Sy = P1 + Q1, Dy = P1 - Q1;
+    double2* fo = reinterpret_cast<double2*>(fe) + e * 4;
+    fo[0] = make_double2(H0 - Sx, H1 - Sy);
+    fo[1] = make_double2(Dx - H0, Dy - H1);
+    fo[2] = make_double2(Sx + H0, Sy + H1);
+    fo[3] = make_double2(-(Dx + H0), -(Dy + H1));
+}
+
+__global__ void __launch_bounds__(256, 4)
+k_elem_force_quad4_square(const int32_t* __restrict__ conn, const double* __restrict__ u,
+                          const double* __restrict__ coef, int64_t nelem, double* __restrict__ fe)
+{
+    GF_FOR(e, nelem) quad4_square_elem<false>(e, conn, u, coef, fe);
 }
 
 // Constants of the uniform Hex8 path (see k_elem_force_hex8_uniform).
@@ -335,6 +405,96 @@ __global__ void k_predict(double* __restrict__ u, const double* __restrict__ v,
     GF_FOR(t, n) u[t] = __dadd_rn(__dadd_rn(u[t], __dmul_rn(k.dt, v[t])), __dmul_rn(k.c, a[t]));
 }
 
+// One node-dof t of the increment: fint by the CSR gather, three velocity estimates, predictor.
+template <bool S>
+__device__ __forceinline__ void
+verlet_node_one(int64_t t, const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
+                const int32_t* __restrict__ idx, const int32_t* __restrict__ part, int64_t nnu,
+                const double* __restrict__ inv, const double* __restrict__ fe,
+                const double* __restrict__ fext, const VerletCoef& k, int advance,
+                double* __restrict__ u, double* __restrict__ v, double* __restrict__ a)
+{
+    int32_t d = __ldg(dofs + t);
+    int32_t b = __ldg(ptr + d), en = __ldg(ptr + d + 1);
+    double fint = 0.0;
+    for (int32_t j = b; j < en; ++j) fint = __dadd_rn(fint, __ldg(fe + __ldg(idx + j)));
+    double R = sub<S>(fext ? __ldg(fext + t) : 0.0, fint);
+    int32_t p = __ldg(part + t);
+    bool fr = p < nnu;
+    double mi = fr ? __ldg(inv + p) : 0.0;
+    double vn = v[t], an = a[t];
+    // estimate 1 (main.cpp:129-137)
+    double vv = madd<S>(k.dt, an, vn);
+    double aa = fr ? mul<S>(mi, sub<S>(R, mul<S>(k.eta, vv))) : an;
+    // estimate 2 (main.cpp:139-147)
+    vv = madd<S>(k.h, add<S>(an, aa), vn);
+    aa = fr ? mul<S>(mi, sub<S>(R, mul<S>(k.eta, vv))) : aa;
+    // final (main.cpp:149-157)
+    vv = madd<S>(k.h, add<S>(an, aa), vn);
+    aa = fr ? mul<S>(mi, sub<S>(R, mul<S>(k.eta, vv))) : aa;
+    v[t] = vv;
+    a[t] = aa;
+    if (advance) u[t] = madd<S>(k.c, aa, madd<S>(k.dt, vv, u[t]));
+}
+
+template <bool CG>
+__device__ __forceinline__ double ld1(const double* p)
+{
+    if constexpr (CG) return __ldcg(p);
+    else return __ldg(p);
+}
+
+// Fast node update (reassociated, not bit-exact with the reference order): the solve
+// a = inv (R - eta v) is evaluated as inv R - (inv eta) v and v_n + h a_n is shared by the second
+// and third estimates: 14 FP64 instructions per dof without external force.
+template <bool CG>
+__device__ __forceinline__ void
+verlet_node_fast_one(int64_t t, const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
+                     const int32_t* __restrict__ idx, const int32_t* __restrict__ part,
+                     int64_t nnu, const double* __restrict__ inv, const double* fe,
+                     const double* __restrict__ fext, const VerletCoef& k, int advance,
+                     double* __restrict__ u, double* __restrict__ v, double* __restrict__ a)
+{
+    int32_t d = __ldg(dofs + t);
+    int32_t b = __ldg(ptr + d), en = __ldg(ptr + d + 1);
+    double fint = en > b ? ld1<CG>(fe + __ldg(idx + b)) : 0.0;
+    for (int32_t j = b + 1; j < en; ++j) fint += ld1<CG>(fe + __ldg(idx + j));
+    int32_t p = __ldg(part + t);
+    double vn = v[t], an = a[t];
+    double vv, aa;
+    if (p < nnu) {
+        double mi = __ldg(inv + p);
+        double mR = fext ? mi * (__ldg(fext + t) - fint) : -mi * fint;
+        double be = mi * k.eta;
+        double v1 = fma(k.dt, an, vn);
+        double a1 = fma(-be, v1, mR);
+        double w = fma(k.h, an, vn);
+        double v2 = fma(k.h, a1, w);
+        double a2 = fma(-be, v2, mR);
+        vv = fma(k.h, a2, w);
+        aa = fma(-be, vv, mR);
+    }
+    else {
+        // prescribed dof: the solve leaves a untouched; v follows the three estimates
+        aa = an;
+        vv = fma(k.h, an + an, vn);
+    }
+    v[t] = vv;
+    a[t] = aa;
+    if (advance) u[t] = fma(k.c, aa, fma(k.dt, vv, u[t]));
+}
+
+__global__ void __launch_bounds__(256)
+k_verlet_node_fast(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
+                   const int32_t* __restrict__ idx, const int32_t* __restrict__ part, int64_t nnu,
+                   const double* __restrict__ inv, const double* __restrict__ fe,
+                   const double* __restrict__ fext, int64_t n, VerletCoef k, int advance,
+                   double* __restrict__ u, double* __restrict__ v, double* __restrict__ a)
+{
+    GF_FOR(t, n)
+    verlet_node_fast_one<false>(t, dofs, ptr, idx, part, nnu, inv, fe, fext, k, advance, u, v, a);
+}
+
 template <bool S>
 __global__ void __launch_bounds__(256)
 k_verlet_node(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
@@ -343,30 +503,7 @@ k_verlet_node(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
               const double* __restrict__ fext, int64_t n, VerletCoef k, int advance,
               double* __restrict__ u, double* __restrict__ v, double* __restrict__ a)
 {
-    GF_FOR(t, n)
-    {
-        int32_t d = __ldg(dofs + t);
-        int32_t b = __ldg(ptr + d), en = __ldg(ptr + d + 1);
-        double fint = 0.0;
-        for (int32_t j = b; j < en; ++j) fint = __dadd_rn(fint, __ldg(fe + __ldg(idx + j)));
-        double R = sub<S>(fext ? __ldg(fext + t) : 0.0, fint);
-        int32_t p = __ldg(part + t);
-        bool fr = p < nnu;
-        double mi = fr ? __ldg(inv + p) : 0.0;
-        double vn = v[t], an = a[t];
-        // estimate 1 (main.cpp:129-137)
-        double vv = madd<S>(k.dt, an, vn);
-        double aa = fr ? mul<S>(mi, sub<S>(R, mul<S>(k.eta, vv))) : an;
-        // estimate 2 (main.cpp:139-147)
-        vv = madd<S>(k.h, add<S>(an, aa), vn);
-        aa = fr ? mul<S>(mi, sub<S>(R, mul<S>(k.eta, vv))) : aa;
-        // final (main.cpp:149-157)
-        vv = madd<S>(k.h, add<S>(an, aa), vn);
-        aa = fr ? mul<S>(mi, sub<S>(R, mul<S>(k.eta, vv))) : aa;
-        v[t] = vv;
-        a[t] = aa;
-        if (advance) u[t] = madd<S>(k.c, aa, madd<S>(k.dt, vv, u[t]));
-    }
+    GF_FOR(t, n) verlet_node_one<S>(t, dofs, ptr, idx, part, nnu, inv, fe, fext, k, advance, u, v, a);
 }
 
 // Flags any (element, Gauss point) whose dNx / vol differ from the uniform-box reference.
@@ -382,6 +519,85 @@ __global__ void k_detect_uniform(const double* __restrict__ dNx, const double* _
         for (int k = 0; k < kk; ++k) ok = ok && fabs(g[k] - ref[q * kk + k]) <= tol_g;
         if (!ok) *bad = 1;
     }
+}
+
+// ------------------------------------------------------------------ persistent increment kernel
+
+// Grid-wide barrier for a cooperative launch (all blocks co-resident). Bounded: a block that
+// waits more than `limit` clock cycles sets *err and leaves the barrier; every block checks *err
+// after each barrier and returns, so no wait is unbounded and the context stays usable.
+struct GridBar {
+    unsigned* count;
+    unsigned* gen;
+    int* err;
+    long long limit;
+    unsigned expected; // blocks that must arrive (gridDim.x; larger only in the self-test)
+};
+
+__device__ __forceinline__ bool grid_sync(const GridBar& b)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = b.gen;
+        volatile int* err = b.err;
+        unsigned g = *gen;
+        __threadfence();
+        unsigned arrived = atomicAdd(b.count, 1u);
+        if (arrived == b.expected - 1) {
+            atomicExch(b.count, 0u);
+            __threadfence();
+            atomicAdd(b.gen, 1u);
+        }
+        else {
+            long long t0 = clock64();
+            while (*gen == g) {
+                if (*err) break;
+                if (clock64() - t0 > b.limit) {
+                    atomicExch(b.err, 1);
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int*)b.err == 0;
+}
+
+// All increments in one launch: predictor, then per increment the element phase (uniform Quad4
+// closed form) and the node phase, separated by grid barriers. Data written by other blocks in
+// the previous phase (u, fe) is read through L2 (ld.global.cg), never through the incoherent
+// per-SM caches.
+__global__ void __launch_bounds__(256, 4)
+k_verlet_persistent(const int32_t* __restrict__ conn, const double* __restrict__ coef,
+                    int64_t nelem, const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
+                    const int32_t* __restrict__ idx, const int32_t* __restrict__ part, int64_t nnu,
+                    const double* __restrict__ inv, const double* __restrict__ fext, int64_t n,
+                    VerletCoef k, int64_t nsteps, double* u, double* v, double* a, double* fe,
+                    GridBar bar)
+{
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int64_t t0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (int64_t t = t0; t < n; t += stride)
+        u[t] = __dadd_rn(__dadd_rn(u[t], __dmul_rn(k.dt, v[t])), __dmul_rn(k.c, a[t]));
+    if (!grid_sync(bar)) return;
+    for (int64_t s = 0; s < nsteps; ++s) {
+        for (int64_t e = t0; e < nelem; e += stride) quad4_square_elem<true>(e, conn, u, coef, fe);
+        if (!grid_sync(bar)) return;
+        int advance = s + 1 < nsteps;
+        for (int64_t t = t0; t < n; t += stride)
+            verlet_node_fast_one<true>(t, dofs, ptr, idx, part, nnu, inv, fe, fext, k, advance, u, v,
+                                       a);
+        if (!grid_sync(bar)) return;
+    }
+}
+
+// Barrier self-test: every block waits for one more arrival than there are blocks, which never
+// comes; each wait must give up after `limit` cycles and report through *err.
+__global__ void k_barrier_selftest(GridBar bar)
+{
+    grid_sync(bar);
 }
 
 // FP64 probe: 8 independent DFMA chains per thread.
@@ -426,27 +642,41 @@ static int check_desc(const gfgpu_verlet_desc* d)
     return GFGPU_OK;
 }
 
+static Quad4Uniform quad4_uniform_constants(const gfgpu_verlet_desc* d)
+{
+    Quad4Uniform c;
+    double g = 1.0 / std::sqrt(3.0);
+    double vq = d->hx * d->hy / 4.0;
+    c.ax = 1.0 / (2.0 * d->hx);
+    c.ay = 1.0 / (2.0 * d->hy);
+    c.cx = 4.0 * vq * c.ax;
+    c.cy = 4.0 * vq * c.ay;
+    c.hx2 = 4.0 * (g * g) * vq * c.ax * c.ax;
+    c.hy2 = 4.0 * (g * g) * vq * c.ay * c.ay;
+    return c;
+}
+
+static VerletCoef verlet_coefficients(const gfgpu_verlet_desc* d)
+{
+    VerletCoef k;
+    k.dt = d->dt;
+    k.h = 0.5 * d->dt;
+    k.c = 0.5 * std::pow(d->dt, 2.0);
+    k.eta = d->eta;
+    return k;
+}
+
 static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, cudaStream_t s)
 {
     if (d->nelem == 0) return GFGPU_OK;
-    if (d->uniform && d->nne == 4) {
-        Quad4Uniform c;
-        double g = 1.0 / std::sqrt(3.0);
-        double vq = d->hx * d->hy / 4.0;
-        c.ax = 1.0 / (2.0 * d->hx);
-        c.ay = 1.0 / (2.0 * d->hy);
-        c.cx = 4.0 * vq * c.ax;
-        c.cy = 4.0 * vq * c.ay;
-        c.hx2 = 4.0 * (g * g) * vq * c.ax * c.ax;
-        c.hy2 = 4.0 * (g * g) * vq * c.ay * c.ay;
-        int dev = 0, sms = 148;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        int64_t blocks = (d->nelem + 255) / 256;
-        int64_t cap = static_cast<int64_t>(sms) * 8 * 16;
-        if (blocks > cap) blocks = cap;
-        k_elem_force_quad4_uniform<<<static_cast<unsigned>(blocks), 256, 0, s>>>(
-            d->conn, u, d->K, d->G, d->nelem, c, fe);
+    if (d->uniform && d->nne == 4 && d->coef) {
+        k_elem_force_quad4_square<<<grid_for(d->nelem), 256, 0, s>>>(d->conn, u, d->coef, d->nelem,
+                                                                     fe);
+    }
+    else if (d->uniform && d->nne == 4) {
+        Quad4Uniform c = quad4_uniform_constants(d);
+        k_elem_force_quad4_uniform<<<grid_for(d->nelem), 256, 0, s>>>(d->conn, u, d->K, d->G,
+                                                                      d->nelem, c, fe);
     }
     else if (d->uniform) {
         Hex8Uniform c;
@@ -585,11 +815,7 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
     if (nsteps == 0) return GFGPU_OK;
     cudaStream_t s = S(stream);
     double* fe = static_cast<double*>(workspace);
-    VerletCoef k;
-    k.dt = d->dt;
-    k.h = 0.5 * d->dt;
-    k.c = 0.5 * std::pow(d->dt, 2.0);
-    k.eta = d->eta;
+    VerletCoef k = verlet_coefficients(d);
     int64_t n = d->nnode * d->ndim;
     unsigned gn = grid_for(n);
     k_predict<<<gn, kBlock, 0, s>>>(u, v, a, n, k);
@@ -602,8 +828,8 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
             k_verlet_node<true><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
                                                       d->inv, fe, d->fext, n, k, adv, u, v, a);
         else
-            k_verlet_node<false><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
-                                                       d->inv, fe, d->fext, n, k, adv, u, v, a);
+            k_verlet_node_fast<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
+                                                     d->inv, fe, d->fext, n, k, adv, u, v, a);
         GF_TRY(check_launch("verlet node kernel"));
     }
     return GFGPU_OK;
@@ -626,6 +852,147 @@ int gfgpu_verlet_element_forces(const gfgpu_verlet_desc* d, const double* u, dou
     GF_REQUIRE(u && fe, "bad argument");
     GF_REQUIRE((reinterpret_cast<uintptr_t>(fe) & 15u) == 0, "fe must be 16-byte aligned");
     return launch_elem(d, u, fe, S(stream));
+}
+
+int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stream_t stream)
+{
+    GF_TRY(check_operator(d));
+    GF_REQUIRE(coef, "null coefficient array");
+    GF_REQUIRE((reinterpret_cast<uintptr_t>(coef) & 15u) == 0, "coef must be 16-byte aligned");
+    if (!(d->uniform && d->nne == 4 && std::fabs(d->hx - d->hy) <= 1e-12 * d->hx))
+        return fail(GFGPU_ERR_UNSUPPORTED, "gfgpu_verlet_precompute: uniform square Quad4 only");
+    if (d->nelem == 0) return GFGPU_OK;
+    double g = 1.0 / std::sqrt(3.0);
+    k_quad4_square_coef<<<grid_for(d->nelem), kBlock, 0, S(stream)>>>(d->K, d->G, d->nelem, g * g,
+                                                                      coef);
+    return check_launch("verlet_precompute");
+}
+
+int64_t gfgpu_verlet_persistent_workspace_bytes(const gfgpu_verlet_desc* d)
+{
+    return d ? gfgpu_verlet_workspace_bytes(d) + 256 : 0;
+}
+
+int gfgpu_verlet_persistent(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                            int64_t nsteps, int32_t block, int32_t blocks_per_sm,
+                            int64_t timeout_cycles, void* workspace, gfgpu_stream_t stream)
+{
+    GF_TRY(check_desc(d));
+    GF_REQUIRE(d->uniform && d->nne == 4 && d->coef,
+               "persistent path: uniform square Quad4 meshes with precomputed coefficients only");
+    GF_REQUIRE(u && v && a && workspace && nsteps >= 0, "bad argument");
+    GF_REQUIRE(block == 64 || block == 128 || block == 256, "block must be 64, 128 or 256");
+    GF_REQUIRE(timeout_cycles > 0, "timeout must be positive");
+    if (nsteps == 0) return GFGPU_OK;
+    cudaStream_t s = S(stream);
+    double* fe = static_cast<double*>(workspace);
+    char* tail = static_cast<char*>(workspace) + gfgpu_verlet_workspace_bytes(d);
+    GF_TRY(check_cuda(cudaMemsetAsync(tail, 0, 256, s), "cudaMemsetAsync"));
+    int dev = 0, sms = 0, maxb = 0;
+    GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+    GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr"));
+    GF_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, k_verlet_persistent,
+                                                                    block, 0),
+                      "occupancy"));
+    GF_REQUIRE(maxb >= 1, "persistent kernel does not fit on an SM");
+    int bps = blocks_per_sm > 0 ? std::min(blocks_per_sm, maxb) : maxb;
+    GridBar bar;
+    bar.count = reinterpret_cast<unsigned*>(tail);
+    bar.gen = reinterpret_cast<unsigned*>(tail + 64);
+    bar.err = reinterpret_cast<int*>(tail + 128);
+    bar.limit = timeout_cycles;
+    bar.expected = static_cast<unsigned>(sms * bps);
+    VerletCoef k = verlet_coefficients(d);
+    int64_t n = d->nnode * d->ndim;
+    int64_t nelem = d->nelem, nnu = d->nnu;
+    const int32_t *conn = d->conn, *dofs = d->dofs, *ptr = d->csr_ptr, *idx = d->csr_idx,
+                  *part = d->part;
+    const double *coef = d->coef, *inv = d->inv, *fext = d->fext;
+    void* args[] = {(void*)&conn, (void*)&coef, (void*)&nelem, (void*)&dofs, (void*)&ptr,
+                    (void*)&idx,  (void*)&part, (void*)&nnu,   (void*)&inv,  (void*)&fext,
+                    (void*)&n,    (void*)&k,    (void*)&nsteps, (void*)&u,   (void*)&v,
+                    (void*)&a,    (void*)&fe,   (void*)&bar};
+    return check_cuda(cudaLaunchCooperativeKernel((const void*)k_verlet_persistent,
+                                                  dim3(sms * bps), dim3(block), args, 0, s),
+                      "cudaLaunchCooperativeKernel");
+}
+
+int gfgpu_verlet_persistent_status(const gfgpu_verlet_desc* d, const void* workspace,
+                                   int* status, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d && workspace && status, "bad argument");
+    const char* tail = static_cast<const char*>(workspace) + gfgpu_verlet_workspace_bytes(d);
+    int err = 0;
+    GF_TRY(check_cuda(cudaMemcpyAsync(&err, tail + 128, sizeof(int), cudaMemcpyDeviceToHost,
+                                      S(stream)),
+                      "cudaMemcpyAsync"));
+    GF_TRY(check_cuda(cudaStreamSynchronize(S(stream)), "cudaStreamSynchronize"));
+    *status = err ? GFGPU_ERR_TIMEOUT : GFGPU_OK;
+    return GFGPU_OK;
+}
+
+int gfgpu_verlet_graph_create(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                              int64_t nsteps, int32_t mode, int32_t block, int32_t blocks_per_sm,
+                              int64_t timeout_cycles, void* workspace, gfgpu_graph_t* graph)
+{
+    GF_REQUIRE(graph && (mode == 0 || mode == 1), "bad argument");
+    cudaStream_t cs = nullptr;
+    GF_TRY(check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate"));
+    int rc = check_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "BeginCapture");
+    if (rc == GFGPU_OK) {
+        if (mode == 0)
+            rc = gfgpu_verlet_step(d, u, v, a, nsteps, workspace, cs);
+        else
+            rc = gfgpu_verlet_persistent(d, u, v, a, nsteps, block, blocks_per_sm, timeout_cycles,
+                                         workspace, cs);
+        cudaGraph_t g = nullptr;
+        int rc2 = check_cuda(cudaStreamEndCapture(cs, &g), "EndCapture");
+        if (rc == GFGPU_OK) rc = rc2;
+        cudaGraphExec_t ge = nullptr;
+        if (rc == GFGPU_OK)
+            rc = check_cuda(cudaGraphInstantiate(&ge, g, 0), "cudaGraphInstantiate");
+        if (g) cudaGraphDestroy(g);
+        if (rc == GFGPU_OK) *graph = static_cast<gfgpu_graph_t>(ge);
+    }
+    cudaStreamDestroy(cs);
+    return rc;
+}
+
+int gfgpu_graph_launch(gfgpu_graph_t graph, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(graph, "null graph");
+    return check_cuda(cudaGraphLaunch(static_cast<cudaGraphExec_t>(graph), S(stream)),
+                      "cudaGraphLaunch");
+}
+
+int gfgpu_graph_destroy(gfgpu_graph_t graph)
+{
+    if (!graph) return GFGPU_OK;
+    return check_cuda(cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(graph)),
+                      "cudaGraphExecDestroy");
+}
+
+int gfgpu_barrier_selftest(int64_t timeout_cycles, int* status)
+{
+    GF_REQUIRE(status && timeout_cycles > 0, "bad argument");
+    char* mem = nullptr;
+    GF_TRY(check_cuda(cudaMalloc(&mem, 256), "cudaMalloc"));
+    cudaMemset(mem, 0, 256);
+    GridBar bar;
+    bar.count = reinterpret_cast<unsigned*>(mem);
+    bar.gen = reinterpret_cast<unsigned*>(mem + 64);
+    bar.err = reinterpret_cast<int*>(mem + 128);
+    bar.limit = timeout_cycles;
+    bar.expected = 2; // one block is launched: the second arrival never comes
+    k_barrier_selftest<<<1, 32>>>(bar);
+    int rc = check_launch("barrier_selftest");
+    int err = 0;
+    if (rc == GFGPU_OK)
+        rc = check_cuda(cudaMemcpy(&err, mem + 128, sizeof(int), cudaMemcpyDeviceToHost), "memcpy");
+    cudaFree(mem);
+    GF_TRY(rc);
+    *status = err ? GFGPU_ERR_TIMEOUT : GFGPU_OK;
+    return GFGPU_OK;
 }
 
 int gfgpu_probe_fp64(int64_t blocks, int64_t iters, double* out, gfgpu_stream_t stream)

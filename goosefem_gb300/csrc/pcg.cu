@@ -337,10 +337,10 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
         }
         rel = std::sqrt(rr) / bnorm;
     }
-    // true residual b - A x
+    // true residual of the partitioned system: b_u - A_uu x_u = -(A x)_u, x holding x_p as well
     if ((rc = gfgpu_internal_element_forces(d, x, w.fe, s)) != GFGPU_OK) return fail_out(rc);
     k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
-                                               w.bvec, w.minv, n, w.r, w.z, nullptr, w.partial);
+                                               nullptr, w.minv, n, w.r, w.z, nullptr, w.partial);
     k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ_NEW);
     cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
     if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg final residual")) != GFGPU_OK)

@@ -109,6 +109,12 @@ class VelocityVerlet:
                       v0.ctypes.data, 1e-12)
             if uniform is True and not d.uniform:
                 raise RuntimeError("mesh is not a uniform axis-aligned Quad4 mesh")
+        self.coef = None
+        if d.uniform and nne == 4 and abs(d.hx - d.hy) <= 1e-12 * d.hx:
+            self.coef = torch.empty((nelem, 4), dtype=torch.float64, device=_dev.device())
+            _lib.call("gfgpu_verlet_precompute", C.addressof(d), self.coef.data_ptr(),
+                      _dev.stream())
+            d.coef = self.coef.data_ptr()
         self.ws = torch.empty(int(_lib.lib().gfgpu_verlet_workspace_bytes(C.addressof(d))) // 8,
                               dtype=torch.float64, device=_dev.device())
 
@@ -116,8 +122,19 @@ class VelocityVerlet:
     def uniform(self):
         return bool(self.desc.uniform)
 
+    @property
+    def path(self):
+        if not self.desc.uniform:
+            return "general"
+        return "uniform-square" if self.desc.coef else "uniform"
+
     def use_general_path(self):
         self.desc.uniform = 0
+        self.desc.coef = None
+
+    def use_uniform_onthefly(self):
+        """Uniform closed form with K, G read every increment (no precomputed coefficients)."""
+        self.desc.coef = None
 
     def step(self, u, v, a, nsteps=1):
         """Advance nsteps increments in place (u, v, a: device nodevec float64)."""

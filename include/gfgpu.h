@@ -43,10 +43,11 @@ const char* gfgpu_last_error(void);
 /* Library version string. */
 const char* gfgpu_version(void);
 
-/* Arithmetic mode of the operator kernels (not of the fused explicit step):
- * 0 = fast (FMA contraction allowed; agreement with the reference ~1e-16 relative),
+/* Arithmetic mode of the operator kernels and of the general-path explicit step:
+ * 0 = fast (FMA contraction and reassociation allowed; agreement with the reference ~1e-15),
  * 1 = strict (every product and sum rounded separately in the reference's order, which
- *     reproduces the reference's FP64 results bit for bit). Default 0. Process-wide. */
+ *     reproduces the reference's FP64 results bit for bit). Default 0. Process-wide.
+ * The closed-form uniform element kernels are never bit-exact (they sum differently). */
 int gfgpu_set_strict(int strict);
 
 /* ============================ set-up on the host (integer bookkeeping) ==================== */
@@ -230,6 +231,9 @@ typedef struct {
      * reference's Gauss quadrature; 0 = general per-Gauss-point path. */
     int32_t uniform;
     double hx, hy, hz;
+    /* optional per-element coefficients of the uniform square Quad4 kernel [nelem, 4]
+     * (gfgpu_verlet_precompute); NULL = derive them from K and G in every increment */
+    const double* coef;
 } gfgpu_verlet_desc;
 
 /* Bytes of scratch the step needs (the element-force buffer), 256-byte aligned size. */
@@ -239,7 +243,13 @@ int64_t gfgpu_verlet_workspace_bytes(const gfgpu_verlet_desc* d);
  * success sets d->uniform = 1 and d->hx, hy, hz. Returns GFGPU_OK either way (d->uniform tells). */
 int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
                                 const double* vol_host, double rtol);
+/* Uniform square Quad4 meshes: fill coef [nelem, 4] with the element coefficients that depend on
+ * K and G only (lam/4, G/2, G/4, g^2 (lam + 3G)/4, lam = K - 2G/3); set d->coef = coef to use
+ * them. Returns GFGPU_ERR_UNSUPPORTED for other meshes. */
+int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stream_t stream);
 /* Advance nsteps increments; u, v, a are nodevec [nnode, ndim] device arrays updated in place.
+ * Strict mode (gfgpu_set_strict) with the general path reproduces the reference's operation
+ * order bit for bit; fast mode reassociates the lumped solve (a = inv R - (inv eta) v).
  * `workspace` is device memory of gfgpu_verlet_workspace_bytes(d). */
 int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
                       int64_t nsteps, void* workspace, gfgpu_stream_t stream);
@@ -252,6 +262,35 @@ int gfgpu_internal_force(const gfgpu_verlet_desc* d, const double* u, double* fi
  * Int_gradN_dot_tensor2_dV(sigma(SymGradN_vector(asElement(u)))). */
 int gfgpu_verlet_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                 gfgpu_stream_t stream);
+
+/* Persistent variant of gfgpu_verlet_step for uniform Quad4 meshes (used for batches of many
+ * independent meshes concatenated into one block-diagonal mesh): ONE cooperative launch runs the
+ * predictor and all nsteps increments; the element and node phases are separated by a grid-wide
+ * barrier whose waits give up after `timeout_cycles` SM clock cycles (the kernel then returns
+ * and gfgpu_verlet_persistent_status reports GFGPU_ERR_TIMEOUT). `block` = 64, 128 or 256 threads,
+ * `blocks_per_sm` <= 0 = as many as fit. Workspace: gfgpu_verlet_persistent_workspace_bytes. */
+int64_t gfgpu_verlet_persistent_workspace_bytes(const gfgpu_verlet_desc* d);
+int gfgpu_verlet_persistent(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                            int64_t nsteps, int32_t block, int32_t blocks_per_sm,
+                            int64_t timeout_cycles, void* workspace, gfgpu_stream_t stream);
+/* Synchronises `stream`, then *status = GFGPU_OK or GFGPU_ERR_TIMEOUT (a barrier gave up). */
+int gfgpu_verlet_persistent_status(const gfgpu_verlet_desc* d, const void* workspace,
+                                   int* status, gfgpu_stream_t stream);
+
+/* CUDA graph of nsteps increments on fixed u, v, a, workspace addresses: mode 0 = the two kernels
+ * per increment of gfgpu_verlet_step, mode 1 = the persistent launch. Replay with
+ * gfgpu_graph_launch; release with gfgpu_graph_destroy. */
+typedef void* gfgpu_graph_t;
+int gfgpu_verlet_graph_create(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                              int64_t nsteps, int32_t mode, int32_t block, int32_t blocks_per_sm,
+                              int64_t timeout_cycles, void* workspace, gfgpu_graph_t* graph);
+int gfgpu_graph_launch(gfgpu_graph_t graph, gfgpu_stream_t stream);
+int gfgpu_graph_destroy(gfgpu_graph_t graph);
+
+/* Failure-detection self-test of the bounded grid barrier: a one-block launch waits for an
+ * arrival that never comes; *status must come back GFGPU_ERR_TIMEOUT after about
+ * `timeout_cycles` SM cycles, with the context still usable. Synchronises. */
+int gfgpu_barrier_selftest(int64_t timeout_cycles, int* status);
 
 /* ============================ static solve (device) ======================================= */
 

@@ -1,0 +1,117 @@
+"""Batched periodic explicit dynamics: the concatenated block-diagonal system (graph of two
+kernels per increment, or one persistent cooperative kernel) against each instance run alone and
+against the oracle; the bounded grid barrier's failure path."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from _common import RTOL, rel_err, to_np
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gf():
+    import goosefem_gb300 as gf
+
+    gf.set_strict(False)
+    return gf
+
+
+@pytest.fixture(scope="module")
+def batch(gf):
+    from goosefem_gb300 import batch as B
+
+    inst = B.seeded_instances(6, 50, nmin=8, nmax=40)
+    return B, inst, B.BatchedVerlet(inst)
+
+
+def _split(bv, x):
+    x = to_np(x)
+    return [x[o:o + n] for o, n in bv.offsets]
+
+
+def _alone(gf, inst, dt, nsteps):
+    m = inst.mesh
+    vv = gf.VelocityVerlet(m.coor(), m.conn(), m.dofsPeriodic(), inst.K, inst.G, dt=dt, eta=0.1)
+    u = torch.tensor(inst.initial_displacement(), device="cuda")
+    v = torch.zeros_like(u)
+    a = torch.zeros_like(u)
+    vv.step(u, v, a, nsteps)
+    return to_np(u), to_np(v), to_np(a)
+
+
+@pytest.mark.parametrize("mode,block,bps", [(0, 256, 0), (1, 256, 0), (1, 128, 1)])
+def test_batched_equals_instances_alone(gf, batch, mode, block, bps):
+    B, inst, bv = batch
+    bv.mode, bv.block, bv.bps = mode, block, bps
+    u, v, a = bv.state()
+    bv.run_direct(u, v, a, 60)
+    torch.cuda.synchronize()
+    for k, (us, vs, as_) in enumerate(zip(_split(bv, u), _split(bv, v), _split(bv, a))):
+        ur, vr, ar = _alone(gf, inst[k], bv.dt, 60)
+        assert rel_err(us, ur) <= RTOL and rel_err(vs, vr) <= RTOL and rel_err(as_, ar) <= RTOL
+
+
+def test_batched_matches_oracle(gf, oracle, batch):
+    """One instance of the batch against the oracle's loop (periodic dofs, applied shear)."""
+    B, inst, bv = batch
+    R = oracle
+    bv.mode = 0
+    u, v, a = bv.state()
+    bv.run_direct(u, v, a, 40)
+    k = 2
+    i = inst[k]
+    m = i.mesh
+    coor, conn, dofs = m.coor(), m.conn(), m.dofsPeriodic()
+    xr = R.as_element(conn, coor)
+    dNx, vol = R.compute_dN(xr, *R.quad4_gauss())
+    xin, win = R.quad4_nodal()
+    _, voln = R.compute_dN(xr, xin, win)
+    Nn, _ = R.shape(xin)
+    A = R.diag_assemble(conn, dofs, R.int_n_scalar_nt_dv(Nn, voln, np.ones((m.nelem(), 4)), 2))
+    ur = i.initial_displacement()
+    vr = np.zeros_like(ur)
+    ar = np.zeros_like(ur)
+    R.verlet_run(conn, dofs, dNx, vol, i.K, i.G, A, np.ones(ur.size, dtype=np.uint8), None, bv.dt,
+                 0.1, 40, ur, vr, ar)
+    assert rel_err(_split(bv, u)[k], ur) <= RTOL
+    assert rel_err(_split(bv, v)[k], vr) <= RTOL
+    assert rel_err(_split(bv, a)[k], ar) <= RTOL
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_graph_replay_equals_direct(gf, batch, mode):
+    B, inst, bv = batch
+    bv.mode, bv.block, bv.bps = mode, 256, 0
+    u1, v1, a1 = bv.state()
+    bv.run_direct(u1, v1, a1, 25)
+    u2, v2, a2 = bv.state()
+    bv.run_graph(u2, v2, a2, 25)
+    torch.cuda.synchronize()
+    if mode == 1:
+        bv.check_status()
+    assert torch.equal(u1, u2) and torch.equal(v1, v2) and torch.equal(a1, a2)
+    bv.release()
+
+
+def test_autotune_picks_a_valid_schedule(gf, batch):
+    B, inst, bv = batch
+    table = bv.autotune(nsteps=5, reps=1)
+    assert len(table) >= 2 and all(np.isfinite(r[3]) for r in table)
+    assert (bv.mode, bv.block, bv.bps) in [(r[0], r[1], r[2]) for r in table]
+
+
+def test_grid_barrier_timeout_is_reported(gf):
+    """Failure detection without a GPU fault: a barrier that can never complete gives up after
+    its cycle limit, reports GFGPU_ERR_TIMEOUT, and the context keeps working."""
+    from goosefem_gb300 import _lib
+
+    st = C.c_int(0)
+    _lib.call("gfgpu_barrier_selftest", 20_000_000, C.addressof(st))  # ~10 ms of SM cycles
+    assert st.value == -4
+    x = torch.ones(1000, dtype=torch.float64, device="cuda")
+    assert float((x * 2).sum()) == 2000.0

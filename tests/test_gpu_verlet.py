@@ -90,14 +90,19 @@ def test_verlet_split_calls_equal_one_call(gf, oracle):
         assert torch.equal(x, y)
 
 
+@pytest.mark.parametrize("variant", ["square", "onthefly"])
 @pytest.mark.parametrize("periodic", [False, True])
-def test_verlet_uniform_path(gf, oracle, periodic):
-    """The closed-form uniform Quad4 element kernel against the reference chain."""
+def test_verlet_uniform_path(gf, oracle, periodic, variant):
+    """The closed-form uniform Quad4 element kernels (precomputed square coefficients, or K, G
+    read every increment) against the reference chain."""
     gf.set_strict(False)
     mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 64, 48, periodic,
                                                             not periodic, 25)
     vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip)
-    assert vv.uniform
+    assert vv.path == "uniform-square"
+    if variant == "onthefly":
+        vv.use_uniform_onthefly()
+        assert vv.path == "uniform"
     # internal force of a random displacement
     u_rand = seeded_field((mesh.nnode(), 2), 26)
     R = oracle
