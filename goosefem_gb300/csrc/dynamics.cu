@@ -398,11 +398,13 @@ struct VerletCoef {
     double dt, h, c, eta; // h = 0.5 dt, c = 0.5 dt^2
 };
 
+// u = u + dt v + 0.5 dt^2 a (main.cpp:119), with the same arithmetic as the predictor that the
+// node kernels fuse into the previous increment, so that split and single calls agree bit for bit.
+template <bool S>
 __global__ void k_predict(double* __restrict__ u, const double* __restrict__ v,
                           const double* __restrict__ a, int64_t n, VerletCoef k)
 {
-    // u = u + dt v + 0.5 dt^2 a  (main.cpp:119)
-    GF_FOR(t, n) u[t] = __dadd_rn(__dadd_rn(u[t], __dmul_rn(k.dt, v[t])), __dmul_rn(k.c, a[t]));
+    GF_FOR(t, n) u[t] = madd<S>(k.c, a[t], madd<S>(k.dt, v[t], u[t]));
 }
 
 // One node-dof t of the increment: fint by the CSR gather, three velocity estimates, predictor.
@@ -580,7 +582,7 @@ k_verlet_persistent(const int32_t* __restrict__ conn, const double* __restrict__
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     const int64_t t0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     for (int64_t t = t0; t < n; t += stride)
-        u[t] = __dadd_rn(__dadd_rn(u[t], __dmul_rn(k.dt, v[t])), __dmul_rn(k.c, a[t]));
+        u[t] = fma(k.c, a[t], fma(k.dt, v[t], u[t]));
     if (!grid_sync(bar)) return;
     for (int64_t s = 0; s < nsteps; ++s) {
         for (int64_t e = t0; e < nelem; e += stride) quad4_square_elem<true>(e, conn, u, coef, fe);
@@ -818,9 +820,12 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
     VerletCoef k = verlet_coefficients(d);
     int64_t n = d->nnode * d->ndim;
     unsigned gn = grid_for(n);
-    k_predict<<<gn, kBlock, 0, s>>>(u, v, a, n, k);
-    GF_TRY(check_launch("verlet predict"));
     bool st = strict_mode();
+    if (st)
+        k_predict<true><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
+    else
+        k_predict<false><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
+    GF_TRY(check_launch("verlet predict"));
     for (int64_t it = 0; it < nsteps; ++it) {
         GF_TRY(launch_elem(d, u, fe, s));
         int adv = it + 1 < nsteps ? 1 : 0;

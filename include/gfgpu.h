@@ -50,6 +50,18 @@ const char* gfgpu_version(void);
  * The closed-form uniform element kernels are never bit-exact (they sum differently). */
 int gfgpu_set_strict(int strict);
 
+/* ============================ device memory helpers ======================================= */
+
+/* Thin wrappers of the CUDA runtime so that a host program can use the library without
+ * including CUDA headers (the C++ layer include/gfgpu/GooseFEM.hpp uses them). */
+int gfgpu_malloc(void** ptr, int64_t bytes);
+int gfgpu_free(void* ptr);
+int gfgpu_memcpy_h2d(void* dst, const void* src, int64_t bytes);
+int gfgpu_memcpy_d2h(void* dst, const void* src, int64_t bytes);
+int gfgpu_memcpy_d2d(void* dst, const void* src, int64_t bytes);
+int gfgpu_memset(void* ptr, int value, int64_t bytes);
+int gfgpu_synchronize(void);
+
 /* ============================ set-up on the host (integer bookkeeping) ==================== */
 
 /* Mesh::Quad4::Regular coor/conn (MeshQuad4.h:87-126). coor [nnode,2], conn [nelem,4]. */

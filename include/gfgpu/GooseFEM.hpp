@@ -1,0 +1,718 @@
+/*
+ * GooseFEM-compatible C++ interface of the element hot path, running on the GPU through the
+ * C ABI of gfgpu.h (libgfgpu.so). Header-only; needs no CUDA headers.
+ *
+ * Names and semantics follow GooseFEM (the headers in include/GooseFEM of the reference):
+ *   gfgpu::Mesh::Quad4::Regular / Mesh::Hex8::Regular          (MeshQuad4.h, MeshHex8.h)
+ *   gfgpu::Vector, gfgpu::VectorPartitioned                    (Vector.h, VectorPartitioned.h)
+ *   gfgpu::Element::Quad4::Quadrature / Element::Hex8::Quadrature  (ElementQuad4.h, ElementHex8.h)
+ *   gfgpu::MatrixDiagonal, gfgpu::MatrixDiagonalPartitioned   (MatrixDiagonal*.h)
+ * Capitalised methods allocate and return, lower-case methods write into a caller-provided
+ * array (the reference's convention). Mesh tables are host arrays (gfgpu::host::array); nodal,
+ * element and integration-point fields are device arrays (gfgpu::array). Errors throw
+ * std::runtime_error with the library's message (GOOSEFEM_ASSERT style).
+ */
+#ifndef GFGPU_GOOSEFEM_HPP
+#define GFGPU_GOOSEFEM_HPP
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../gfgpu.h"
+
+namespace gfgpu {
+
+inline void check(int rc, const char* what)
+{
+    if (rc != GFGPU_OK)
+        throw std::runtime_error(std::string(what) + ": " + gfgpu_last_error());
+}
+
+using shape_t = std::vector<int64_t>;
+
+inline int64_t numel(const shape_t& s)
+{
+    return std::accumulate(s.begin(), s.end(), int64_t(1), std::multiplies<int64_t>());
+}
+
+namespace host {
+
+/* Row-major host array (the role of array_type::tensor for mesh tables). */
+template <class T>
+class array {
+public:
+    array() = default;
+    explicit array(shape_t shape, T val = T()) : m_shape(std::move(shape)), m_data(numel(m_shape), val)
+    {
+    }
+    static array from_shape(shape_t shape) { return array(std::move(shape)); }
+    const shape_t& shape() const { return m_shape; }
+    int64_t shape(size_t i) const { return m_shape.at(i); }
+    size_t dimension() const { return m_shape.size(); }
+    int64_t size() const { return static_cast<int64_t>(m_data.size()); }
+    T* data() { return m_data.data(); }
+    const T* data() const { return m_data.data(); }
+    T& operator[](int64_t i) { return m_data[i]; }
+    const T& operator[](int64_t i) const { return m_data[i]; }
+    T& operator()(int64_t i, int64_t j) { return m_data[i * m_shape[1] + j]; }
+    const T& operator()(int64_t i, int64_t j) const { return m_data[i * m_shape[1] + j]; }
+    void fill(T v) { std::fill(m_data.begin(), m_data.end(), v); }
+
+private:
+    shape_t m_shape;
+    std::vector<T> m_data;
+};
+
+} // namespace host
+
+/* Owning device array (FP64 fields and int32 tables). Move-only. */
+template <class T>
+class array {
+public:
+    array() = default;
+    explicit array(shape_t shape) : m_shape(std::move(shape))
+    {
+        void* p = nullptr;
+        check(gfgpu_malloc(&p, numel(m_shape) * sizeof(T)), "gfgpu_malloc");
+        m_ptr = static_cast<T*>(p);
+    }
+    static array from_shape(shape_t shape) { return array(std::move(shape)); }
+    static array from_host(const host::array<T>& h)
+    {
+        array a(h.shape());
+        check(gfgpu_memcpy_h2d(a.m_ptr, h.data(), h.size() * sizeof(T)), "gfgpu_memcpy_h2d");
+        return a;
+    }
+    static array from_host(const T* p, shape_t shape)
+    {
+        array a(std::move(shape));
+        check(gfgpu_memcpy_h2d(a.m_ptr, p, a.size() * sizeof(T)), "gfgpu_memcpy_h2d");
+        return a;
+    }
+    host::array<T> to_host() const
+    {
+        host::array<T> h(m_shape);
+        check(gfgpu_memcpy_d2h(h.data(), m_ptr, size() * sizeof(T)), "gfgpu_memcpy_d2h");
+        return h;
+    }
+    array copy() const
+    {
+        array a(m_shape);
+        check(gfgpu_memcpy_d2d(a.m_ptr, m_ptr, size() * sizeof(T)), "gfgpu_memcpy_d2d");
+        return a;
+    }
+    void fill_zero() { check(gfgpu_memset(m_ptr, 0, size() * sizeof(T)), "gfgpu_memset"); }
+    ~array() { gfgpu_free(m_ptr); }
+    array(const array&) = delete;
+    array& operator=(const array&) = delete;
+    array(array&& o) noexcept : m_shape(std::move(o.m_shape)), m_ptr(o.m_ptr) { o.m_ptr = nullptr; }
+    array& operator=(array&& o) noexcept
+    {
+        std::swap(m_shape, o.m_shape);
+        std::swap(m_ptr, o.m_ptr);
+        return *this;
+    }
+    const shape_t& shape() const { return m_shape; }
+    int64_t shape(size_t i) const { return m_shape.at(i); }
+    size_t dimension() const { return m_shape.size(); }
+    int64_t size() const { return numel(m_shape); }
+    T* data() { return m_ptr; }
+    const T* data() const { return m_ptr; }
+
+private:
+    shape_t m_shape;
+    T* m_ptr = nullptr;
+};
+
+inline void require_shape(const shape_t& a, const shape_t& b, const char* what)
+{
+    if (a != b) throw std::runtime_error(std::string(what) + ": shape mismatch");
+}
+
+// ------------------------------------------------------------------------------------- Mesh
+
+namespace Mesh {
+
+/* Mesh::dofs (Mesh.h:93-96). */
+inline host::array<int32_t> dofs(int64_t nnode, int32_t ndim)
+{
+    host::array<int32_t> out({nnode, ndim});
+    check(gfgpu_host_dofs(nnode, ndim, out.data()), "Mesh::dofs");
+    return out;
+}
+
+/* Mesh::renumber (Mesh.h:114-175). */
+inline host::array<int32_t> renumber(const host::array<int32_t>& in)
+{
+    host::array<int32_t> out(in.shape());
+    check(gfgpu_host_renumber(in.data(), in.size(), out.data()), "Mesh::renumber");
+    return out;
+}
+
+namespace Quad4 {
+
+/* Mesh::Quad4::Regular (MeshQuad4.h:32-195). */
+class Regular {
+public:
+    Regular(int64_t nelx, int64_t nely, double h = 1.0) : m_nx(nelx), m_ny(nely), m_h(h)
+    {
+        if (nelx < 1 || nely < 1) throw std::runtime_error("Mesh::Quad4::Regular: nel < 1");
+    }
+    int64_t nelem() const { return m_nx * m_ny; }
+    int64_t nnode() const { return (m_nx + 1) * (m_ny + 1); }
+    int32_t nne() const { return 4; }
+    int32_t ndim() const { return 2; }
+    int64_t nelx() const { return m_nx; }
+    int64_t nely() const { return m_ny; }
+    double h() const { return m_h; }
+    host::array<double> coor() const
+    {
+        host::array<double> c({nnode(), 2});
+        host::array<int32_t> n({nelem(), 4});
+        check(gfgpu_host_quad4_regular(m_nx, m_ny, m_h, c.data(), n.data()), "Regular::coor");
+        return c;
+    }
+    host::array<int32_t> conn() const
+    {
+        host::array<double> c({nnode(), 2});
+        host::array<int32_t> n({nelem(), 4});
+        check(gfgpu_host_quad4_regular(m_nx, m_ny, m_h, c.data(), n.data()), "Regular::conn");
+        return n;
+    }
+    host::array<int32_t> dofs() const { return Mesh::dofs(nnode(), 2); }
+    host::array<int32_t> nodesBottomEdge() const { return range(0, m_nx + 1, 1); }
+    host::array<int32_t> nodesTopEdge() const
+    {
+        return range(m_ny * (m_nx + 1), m_ny * (m_nx + 1) + m_nx + 1, 1);
+    }
+    host::array<int32_t> nodesLeftEdge() const
+    {
+        return range(0, (m_ny + 1) * (m_nx + 1), m_nx + 1);
+    }
+    host::array<int32_t> nodesRightEdge() const
+    {
+        return range(m_nx, (m_ny + 1) * (m_nx + 1), m_nx + 1);
+    }
+    host::array<int32_t> nodesPeriodic() const
+    {
+        host::array<int32_t> out({(m_nx - 1) + (m_ny - 1) + 3, 2});
+        int64_t n = 0;
+        check(gfgpu_host_quad4_nodes_periodic(m_nx, m_ny, out.data(), &n), "nodesPeriodic");
+        return out;
+    }
+    host::array<int32_t> dofsPeriodic() const
+    {
+        auto npr = nodesPeriodic();
+        host::array<int32_t> out({nnode(), 2});
+        check(gfgpu_host_dofs_periodic(nnode(), 2, npr.data(), npr.shape(0), out.data()),
+              "dofsPeriodic");
+        return out;
+    }
+
+private:
+    static host::array<int32_t> range(int64_t a, int64_t b, int64_t s)
+    {
+        host::array<int32_t> r({(b - a + s - 1) / s});
+        for (int64_t i = 0; i < r.size(); ++i) r[i] = static_cast<int32_t>(a + i * s);
+        return r;
+    }
+    int64_t m_nx, m_ny;
+    double m_h;
+};
+
+} // namespace Quad4
+
+namespace Hex8 {
+
+/* Mesh::Hex8::Regular (MeshHex8.h:26-608). */
+class Regular {
+public:
+    Regular(int64_t nelx, int64_t nely, int64_t nelz, double h = 1.0)
+        : m_nx(nelx), m_ny(nely), m_nz(nelz), m_h(h)
+    {
+        if (nelx < 1 || nely < 1 || nelz < 1) throw std::runtime_error("Mesh::Hex8::Regular");
+    }
+    int64_t nelem() const { return m_nx * m_ny * m_nz; }
+    int64_t nnode() const { return (m_nx + 1) * (m_ny + 1) * (m_nz + 1); }
+    int32_t nne() const { return 8; }
+    int32_t ndim() const { return 3; }
+    host::array<double> coor() const { return build().first; }
+    host::array<int32_t> conn() const { return build().second; }
+    host::array<int32_t> dofs() const { return Mesh::dofs(nnode(), 3); }
+    host::array<int32_t> nodesFront() const
+    {
+        host::array<int32_t> r({(m_nx + 1) * (m_ny + 1)});
+        for (int64_t i = 0; i < r.size(); ++i) r[i] = static_cast<int32_t>(i);
+        return r;
+    }
+    host::array<int32_t> nodesBack() const
+    {
+        host::array<int32_t> r({(m_nx + 1) * (m_ny + 1)});
+        for (int64_t i = 0; i < r.size(); ++i) r[i] = static_cast<int32_t>(i + m_nz * r.size());
+        return r;
+    }
+
+private:
+    std::pair<host::array<double>, host::array<int32_t>> build() const
+    {
+        host::array<double> c({nnode(), 3});
+        host::array<int32_t> n({nelem(), 8});
+        check(gfgpu_host_hex8_regular(m_nx, m_ny, m_nz, m_h, c.data(), n.data()), "Hex8::Regular");
+        return {std::move(c), std::move(n)};
+    }
+    int64_t m_nx, m_ny, m_nz;
+    double m_h;
+};
+
+} // namespace Hex8
+
+} // namespace Mesh
+
+// ------------------------------------------------------------------------------------- Vector
+
+namespace detail {
+
+struct Csr {
+    array<int32_t> ptr, idx, last;
+};
+
+inline Csr elemvec_csr(const host::array<int32_t>& conn, const host::array<int32_t>& dofs,
+                       int64_t ndof)
+{
+    host::array<int32_t> p({ndof + 1}), i({conn.size() * dofs.shape(1)});
+    check(gfgpu_host_dof_csr(conn.data(), dofs.data(), conn.shape(0), int32_t(conn.shape(1)),
+                             dofs.shape(0), int32_t(dofs.shape(1)), ndof, p.data(), i.data()),
+          "gfgpu_host_dof_csr");
+    Csr c{array<int32_t>::from_host(p), array<int32_t>::from_host(i), array<int32_t>({ndof})};
+    check(gfgpu_csr_last(c.ptr.data(), c.idx.data(), ndof, c.last.data(), nullptr), "csr_last");
+    return c;
+}
+
+inline Csr nodevec_csr(const host::array<int32_t>& dofs, int64_t ndof)
+{
+    host::array<int32_t> p({ndof + 1}), i({dofs.size()});
+    check(gfgpu_host_dof_csr_nodevec(dofs.data(), dofs.shape(0), int32_t(dofs.shape(1)), ndof,
+                                     p.data(), i.data()),
+          "gfgpu_host_dof_csr_nodevec");
+    Csr c{array<int32_t>::from_host(p), array<int32_t>::from_host(i), array<int32_t>({ndof})};
+    check(gfgpu_csr_last(c.ptr.data(), c.idx.data(), ndof, c.last.data(), nullptr), "csr_last");
+    return c;
+}
+
+inline int64_t max_plus_one(const host::array<int32_t>& a)
+{
+    int64_t m = -1;
+    for (int64_t i = 0; i < a.size(); ++i) m = std::max<int64_t>(m, a[i]);
+    return m + 1;
+}
+
+} // namespace detail
+
+/* Vector(conn, dofs) (Vector.h:23-767). */
+class Vector {
+public:
+    Vector(const host::array<int32_t>& conn, const host::array<int32_t>& dofs)
+        : m_conn_h(conn), m_dofs_h(dofs)
+    {
+        if (conn.dimension() != 2 || dofs.dimension() != 2)
+            throw std::runtime_error("Vector: conn and dofs must be 2-d");
+        m_nelem = conn.shape(0);
+        m_nne = int32_t(conn.shape(1));
+        m_nnode = dofs.shape(0);
+        m_ndim = int32_t(dofs.shape(1));
+        m_ndof = detail::max_plus_one(dofs);
+        if (detail::max_plus_one(conn) > m_nnode) throw std::runtime_error("Vector: conn > nnode");
+        m_conn = array<int32_t>::from_host(conn);
+        m_dofs = array<int32_t>::from_host(dofs);
+        m_csr = detail::elemvec_csr(conn, dofs, m_ndof);
+        m_csrn = detail::nodevec_csr(dofs, m_ndof);
+    }
+    int64_t nelem() const { return m_nelem; }
+    int32_t nne() const { return m_nne; }
+    int64_t nnode() const { return m_nnode; }
+    int32_t ndim() const { return m_ndim; }
+    int64_t ndof() const { return m_ndof; }
+    const host::array<int32_t>& conn() const { return m_conn_h; }
+    const host::array<int32_t>& dofs() const { return m_dofs_h; }
+    shape_t shape_dofval() const { return {m_ndof}; }
+    shape_t shape_nodevec() const { return {m_nnode, m_ndim}; }
+    shape_t shape_elemvec() const { return {m_nelem, m_nne, m_ndim}; }
+    array<double> allocate_dofval() const { return array<double>(shape_dofval()); }
+    array<double> allocate_nodevec() const { return array<double>(shape_nodevec()); }
+    array<double> allocate_elemvec() const { return array<double>(shape_elemvec()); }
+
+    /* nodevec or dofval -> elemvec (Vector.h:659-697) */
+    void asElement(const array<double>& arg, array<double>& ret) const
+    {
+        require_shape(ret.shape(), shape_elemvec(), "Vector::asElement");
+        if (arg.shape() == shape_nodevec())
+            check(gfgpu_as_element(m_conn.data(), m_nelem, m_nne, m_ndim, arg.data(), ret.data(),
+                                   nullptr),
+                  "Vector::asElement");
+        else if (arg.shape() == shape_dofval())
+            check(gfgpu_as_element_dofval(m_conn.data(), m_dofs.data(), m_nelem, m_nne, m_ndim,
+                                          arg.data(), ret.data(), nullptr),
+                  "Vector::asElement");
+        else
+            throw std::runtime_error("Vector::asElement unknown dimension for conversion");
+    }
+    array<double> AsElement(const array<double>& arg) const
+    {
+        auto r = allocate_elemvec();
+        asElement(arg, r);
+        return r;
+    }
+    /* dofval -> nodevec (Vector.h:615-629) */
+    void asNode(const array<double>& arg, array<double>& ret) const
+    {
+        require_shape(arg.shape(), shape_dofval(), "Vector::asNode");
+        require_shape(ret.shape(), shape_nodevec(), "Vector::asNode");
+        check(gfgpu_as_node(m_dofs.data(), m_nnode, m_ndim, arg.data(), ret.data(), nullptr),
+              "Vector::asNode");
+    }
+    array<double> AsNode(const array<double>& arg) const
+    {
+        auto r = allocate_nodevec();
+        asNode(arg, r);
+        return r;
+    }
+    /* nodevec or elemvec -> dofval, last writer wins (Vector.h:569-608) */
+    void asDofs(const array<double>& arg, array<double>& ret) const
+    {
+        require_shape(ret.shape(), shape_dofval(), "Vector::asDofs");
+        const auto& last = arg.shape() == shape_nodevec() ? m_csrn.last : m_csr.last;
+        check(gfgpu_as_dofs(last.data(), m_ndof, arg.data(), ret.data(), nullptr), "Vector::asDofs");
+    }
+    array<double> AsDofs(const array<double>& arg) const
+    {
+        auto r = allocate_dofval();
+        asDofs(arg, r);
+        return r;
+    }
+    /* nodevec or elemvec -> dofval, summed in the reference's order (Vector.h:703-741) */
+    void assembleDofs(const array<double>& arg, array<double>& ret) const
+    {
+        require_shape(ret.shape(), shape_dofval(), "Vector::assembleDofs");
+        const auto& c = arg.shape() == shape_nodevec() ? m_csrn : m_csr;
+        check(gfgpu_assemble_dofs(c.ptr.data(), c.idx.data(), m_ndof, arg.data(), ret.data(), nullptr),
+              "Vector::assembleDofs");
+    }
+    array<double> AssembleDofs(const array<double>& arg) const
+    {
+        auto r = allocate_dofval();
+        assembleDofs(arg, r);
+        return r;
+    }
+    /* elemvec -> nodevec (Vector.h:747-757) */
+    void assembleNode(const array<double>& arg, array<double>& ret) const
+    {
+        require_shape(arg.shape(), shape_elemvec(), "Vector::assembleNode");
+        require_shape(ret.shape(), shape_nodevec(), "Vector::assembleNode");
+        check(gfgpu_assemble_node(m_csr.ptr.data(), m_csr.idx.data(), m_dofs.data(), m_nnode, m_ndim,
+                                  arg.data(), ret.data(), nullptr),
+              "Vector::assembleNode");
+    }
+    array<double> AssembleNode(const array<double>& arg) const
+    {
+        auto r = allocate_nodevec();
+        assembleNode(arg, r);
+        return r;
+    }
+    const array<int32_t>& conn_device() const { return m_conn; }
+    const array<int32_t>& dofs_device() const { return m_dofs; }
+    const detail::Csr& csr() const { return m_csr; }
+
+protected:
+    host::array<int32_t> m_conn_h, m_dofs_h;
+    int64_t m_nelem, m_nnode, m_ndof;
+    int32_t m_nne, m_ndim;
+    array<int32_t> m_conn, m_dofs;
+    detail::Csr m_csr, m_csrn;
+};
+
+// ------------------------------------------------------------------------------------- Element
+
+namespace Element {
+
+namespace detail {
+
+template <int NNE, int ND>
+class Quadrature {
+public:
+    Quadrature(const array<double>& x, const host::array<double>& xi, const host::array<double>& w)
+        : m_x(x.copy()), m_xi(array<double>::from_host(xi)), m_w(array<double>::from_host(w))
+    {
+        if (x.dimension() != 3 || x.shape(1) != NNE || x.shape(2) != ND)
+            throw std::runtime_error("Quadrature: x must be [nelem, nne, ndim]");
+        m_nelem = x.shape(0);
+        m_nip = int32_t(w.size());
+        m_N = array<double>({m_nip, NNE});
+        m_dNxi = array<double>({m_nip, NNE, ND});
+        m_dNx = array<double>({m_nelem, m_nip, NNE, ND});
+        m_vol = array<double>({m_nelem, m_nip});
+        compute_dN();
+    }
+    void update_x(const array<double>& x)
+    {
+        require_shape(x.shape(), m_x.shape(), "Quadrature::update_x");
+        m_x = x.copy();
+        compute_dN();
+    }
+    int64_t nelem() const { return m_nelem; }
+    int32_t nne() const { return NNE; }
+    int32_t ndim() const { return ND; }
+    int32_t tdim() const { return ND; }
+    int32_t nip() const { return m_nip; }
+    const array<double>& GradN() const { return m_dNx; }
+    const array<double>& dV() const { return m_vol; }
+    shape_t shape_elemvec() const { return {m_nelem, NNE, ND}; }
+    shape_t shape_elemmat() const { return {m_nelem, NNE * ND, NNE * ND}; }
+    shape_t shape_qscalar() const { return {m_nelem, m_nip}; }
+    shape_t shape_qtensor2() const { return {m_nelem, m_nip, ND, ND}; }
+
+    void gradN_vector(const array<double>& ev, array<double>& q) const { grad(gfgpu_grad_n_vector, ev, q); }
+    array<double> GradN_vector(const array<double>& ev) const { return alloc2(gfgpu_grad_n_vector, ev); }
+    void gradN_vector_T(const array<double>& ev, array<double>& q) const { grad(gfgpu_grad_n_vector_T, ev, q); }
+    array<double> GradN_vector_T(const array<double>& ev) const { return alloc2(gfgpu_grad_n_vector_T, ev); }
+    void symGradN_vector(const array<double>& ev, array<double>& q) const { grad(gfgpu_sym_grad_n_vector, ev, q); }
+    array<double> SymGradN_vector(const array<double>& ev) const { return alloc2(gfgpu_sym_grad_n_vector, ev); }
+
+    void interpQuad_vector(const array<double>& ev, array<double>& qv) const
+    {
+        int32_t n = int32_t(ev.shape(2));
+        check(gfgpu_interp_quad_vector(m_N.data(), ev.data(), m_nelem, NNE, m_nip, n, qv.data(), nullptr),
+              "interpQuad_vector");
+    }
+    array<double> InterpQuad_vector(const array<double>& ev) const
+    {
+        array<double> qv({m_nelem, m_nip, ev.shape(2)});
+        interpQuad_vector(ev, qv);
+        return qv;
+    }
+    void int_N_vector_dV(const array<double>& qv, array<double>& ev) const
+    {
+        int32_t n = int32_t(qv.shape(2));
+        check(gfgpu_int_n_vector_dv(m_N.data(), m_vol.data(), qv.data(), m_nelem, NNE, m_nip, n,
+                                    ev.data(), nullptr),
+              "int_N_vector_dV");
+    }
+    array<double> Int_N_vector_dV(const array<double>& qv) const
+    {
+        array<double> ev({m_nelem, NNE, qv.shape(2)});
+        int_N_vector_dV(qv, ev);
+        return ev;
+    }
+    void int_N_scalar_NT_dV(const array<double>& qs, array<double>& em) const
+    {
+        require_shape(qs.shape(), shape_qscalar(), "int_N_scalar_NT_dV");
+        require_shape(em.shape(), shape_elemmat(), "int_N_scalar_NT_dV");
+        check(gfgpu_int_n_scalar_nt_dv(m_N.data(), m_vol.data(), qs.data(), m_nelem, NNE, m_nip, ND,
+                                       em.data(), nullptr),
+              "int_N_scalar_NT_dV");
+    }
+    array<double> Int_N_scalar_NT_dV(const array<double>& qs) const
+    {
+        array<double> em(shape_elemmat());
+        int_N_scalar_NT_dV(qs, em);
+        return em;
+    }
+    void int_gradN_dot_tensor2_dV(const array<double>& qt, array<double>& ev) const
+    {
+        require_shape(qt.shape(), shape_qtensor2(), "int_gradN_dot_tensor2_dV");
+        require_shape(ev.shape(), shape_elemvec(), "int_gradN_dot_tensor2_dV");
+        check(gfgpu_int_grad_n_dot_tensor2_dv(m_dNx.data(), m_vol.data(), qt.data(), m_nelem, NNE,
+                                              m_nip, ND, ev.data(), nullptr),
+              "int_gradN_dot_tensor2_dV");
+    }
+    array<double> Int_gradN_dot_tensor2_dV(const array<double>& qt) const
+    {
+        array<double> ev(shape_elemvec());
+        int_gradN_dot_tensor2_dV(qt, ev);
+        return ev;
+    }
+    void int_gradN_dot_tensor4_dot_gradNT_dV(const array<double>& qt, array<double>& em) const
+    {
+        require_shape(em.shape(), shape_elemmat(), "int_gradN_dot_tensor4_dot_gradNT_dV");
+        check(gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv(m_dNx.data(), m_vol.data(), qt.data(),
+                                                          m_nelem, NNE, m_nip, ND, em.data(), nullptr),
+              "int_gradN_dot_tensor4_dot_gradNT_dV");
+    }
+    array<double> Int_gradN_dot_tensor4_dot_gradNT_dV(const array<double>& qt) const
+    {
+        array<double> em(shape_elemmat());
+        int_gradN_dot_tensor4_dot_gradNT_dV(qt, em);
+        return em;
+    }
+
+protected:
+    using grad_fn = int (*)(const double*, const double*, int64_t, int32_t, int32_t, int32_t,
+                            double*, gfgpu_stream_t);
+    void grad(grad_fn f, const array<double>& ev, array<double>& q) const
+    {
+        require_shape(ev.shape(), shape_elemvec(), "GradN_vector");
+        require_shape(q.shape(), shape_qtensor2(), "GradN_vector");
+        check(f(m_dNx.data(), ev.data(), m_nelem, NNE, m_nip, ND, q.data(), nullptr), "GradN_vector");
+    }
+    array<double> alloc2(grad_fn f, const array<double>& ev) const
+    {
+        array<double> q(shape_qtensor2());
+        grad(f, ev, q);
+        return q;
+    }
+    void compute_dN()
+    {
+        auto fn = NNE == 4 ? gfgpu_quad4_compute_dN : gfgpu_hex8_compute_dN;
+        check(fn(m_x.data(), m_nelem, m_xi.data(), m_w.data(), m_nip, m_N.data(), m_dNxi.data(),
+                 m_dNx.data(), m_vol.data(), nullptr),
+              "compute_dN");
+    }
+    array<double> m_x, m_xi, m_w, m_N, m_dNxi, m_dNx, m_vol;
+    int64_t m_nelem;
+    int32_t m_nip;
+};
+
+inline host::array<double> rule(int nip, int nd, double a)
+{
+    static const int s[8][3] = {{-1, -1, -1}, {+1, -1, -1}, {+1, +1, -1}, {-1, +1, -1},
+                                {-1, -1, +1}, {+1, -1, +1}, {+1, +1, +1}, {-1, +1, +1}};
+    host::array<double> xi({nip, nd});
+    for (int q = 0; q < nip; ++q)
+        for (int d = 0; d < nd; ++d) xi(q, d) = s[q][d] * a;
+    return xi;
+}
+
+} // namespace detail
+
+namespace Quad4 {
+namespace Gauss {
+inline int64_t nip() { return 4; }
+inline host::array<double> xi() { return detail::rule(4, 2, 1.0 / std::sqrt(3.0)); }
+inline host::array<double> w() { return host::array<double>({4}, 1.0); }
+} // namespace Gauss
+namespace Nodal {
+inline int64_t nip() { return 4; }
+inline host::array<double> xi() { return detail::rule(4, 2, 1.0); }
+inline host::array<double> w() { return host::array<double>({4}, 1.0); }
+} // namespace Nodal
+
+/* Element::Quad4::Quadrature (ElementQuad4.h:234-549). */
+class Quadrature : public detail::Quadrature<4, 2> {
+public:
+    explicit Quadrature(const array<double>& x) : detail::Quadrature<4, 2>(x, Gauss::xi(), Gauss::w()) {}
+    Quadrature(const array<double>& x, const host::array<double>& xi, const host::array<double>& w)
+        : detail::Quadrature<4, 2>(x, xi, w)
+    {
+    }
+};
+} // namespace Quad4
+
+namespace Hex8 {
+namespace Gauss {
+inline int64_t nip() { return 8; }
+inline host::array<double> xi() { return detail::rule(8, 3, 1.0 / std::sqrt(3.0)); }
+inline host::array<double> w() { return host::array<double>({8}, 1.0); }
+} // namespace Gauss
+namespace Nodal {
+inline int64_t nip() { return 8; }
+inline host::array<double> xi() { return detail::rule(8, 3, 1.0); }
+inline host::array<double> w() { return host::array<double>({8}, 1.0); }
+} // namespace Nodal
+
+/* Element::Hex8::Quadrature (ElementHex8.h:212-400). */
+class Quadrature : public detail::Quadrature<8, 3> {
+public:
+    explicit Quadrature(const array<double>& x) : detail::Quadrature<8, 3>(x, Gauss::xi(), Gauss::w()) {}
+    Quadrature(const array<double>& x, const host::array<double>& xi, const host::array<double>& w)
+        : detail::Quadrature<8, 3>(x, xi, w)
+    {
+    }
+};
+} // namespace Hex8
+
+/* Element::isDiagonal (Element.h:122-145). */
+inline bool isDiagonal(const array<double>& elemmat)
+{
+    int flag = 0;
+    check(gfgpu_is_diagonal(elemmat.data(), elemmat.shape(0), int32_t(elemmat.shape(1)), &flag,
+                            nullptr),
+          "isDiagonal");
+    return flag != 0;
+}
+
+} // namespace Element
+
+// ------------------------------------------------------------------------------ MatrixDiagonal
+
+/* MatrixDiagonal(conn, dofs) (MatrixDiagonal.h:114-281). */
+class MatrixDiagonal {
+public:
+    MatrixDiagonal(const host::array<int32_t>& conn, const host::array<int32_t>& dofs)
+        : m_vec(conn, dofs), m_A({m_vec.ndof()}), m_inv({m_vec.ndof()})
+    {
+    }
+    int64_t ndof() const { return m_vec.ndof(); }
+    /* MatrixDiagonal::assemble (MatrixDiagonal.h:151-167) */
+    void assemble(const array<double>& elemmat)
+    {
+        if (!Element::isDiagonal(elemmat)) throw std::runtime_error("MatrixDiagonal: not diagonal");
+        check(gfgpu_diag_assemble(m_vec.csr().ptr.data(), m_vec.csr().idx.data(), ndof(), m_vec.nne(),
+                                  m_vec.ndim(), elemmat.data(), m_A.data(), nullptr),
+              "MatrixDiagonal::assemble");
+        m_changed = true;
+    }
+    void set(const array<double>& A)
+    {
+        require_shape(A.shape(), {ndof()}, "MatrixDiagonal::set");
+        check(gfgpu_memcpy_d2d(m_A.data(), A.data(), ndof() * 8), "MatrixDiagonal::set");
+        m_changed = true;
+    }
+    const array<double>& data() const { return m_A; }
+    /* nodevec solve (MatrixDiagonal.h:237-250) */
+    void solve(const array<double>& b, array<double>& x)
+    {
+        factorize();
+        check(gfgpu_diag_solve_nodevec(m_vec.dofs_device().data(), m_vec.nnode(), m_vec.ndim(), ndof(),
+                                       m_inv.data(), b.data(), x.data(), nullptr),
+              "MatrixDiagonal::solve");
+    }
+    array<double> Solve(const array<double>& b)
+    {
+        array<double> x(b.shape());
+        solve(b, x);
+        return x;
+    }
+    void dot(const array<double>& x, array<double>& b) const
+    {
+        check(gfgpu_diag_dot_nodevec(m_vec.dofs_device().data(), m_vec.nnode(), m_vec.ndim(),
+                                     m_A.data(), x.data(), b.data(), nullptr),
+              "MatrixDiagonal::dot");
+    }
+    array<double> Dot(const array<double>& x) const
+    {
+        array<double> b(x.shape());
+        dot(x, b);
+        return b;
+    }
+
+private:
+    void factorize()
+    {
+        if (!m_changed) return;
+        check(gfgpu_diag_factorize(m_A.data(), ndof(), m_inv.data(), nullptr), "factorize");
+        m_changed = false;
+    }
+    Vector m_vec;
+    array<double> m_A, m_inv;
+    bool m_changed = true;
+};
+
+} // namespace gfgpu
+
+#endif

@@ -1,0 +1,96 @@
+// Drives the GooseFEM-compatible C++ interface (include/gfgpu/GooseFEM.hpp) through the 64x64
+// Quad4 force chain and the lumped mass, the way a GooseFEM user program would
+// (docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:32-86, 123-127):
+//   Vector(conn, dofs); Quadrature(vector.AsElement(coor)); asElement; symGradN_vector;
+//   stress; int_gradN_dot_tensor2_dV; assembleNode; MatrixDiagonal::assemble(Int_N_scalar_NT_dV).
+// Usage: test_api <inputs.bin> <outputs.bin>
+//   inputs:  nx (int64), K[nelem], G[nelem], u[nnode*2] (float64)
+//   outputs: dNx, vol, ue, eps, sig, fe, fint, M (float64, concatenated)
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <vector>
+
+#include "gfgpu/GooseFEM.hpp"
+
+namespace GF = gfgpu;
+
+static std::vector<double> read(std::ifstream& f, size_t n)
+{
+    std::vector<double> v(n);
+    f.read(reinterpret_cast<char*>(v.data()), n * sizeof(double));
+    return v;
+}
+
+template <class A>
+static void dump(std::ofstream& o, const A& a)
+{
+    auto h = a.to_host();
+    o.write(reinterpret_cast<const char*>(h.data()), h.size() * sizeof(double));
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 3) return 2;
+    std::ifstream in(argv[1], std::ios::binary);
+    int64_t nx = 0;
+    in.read(reinterpret_cast<char*>(&nx), sizeof(nx));
+    GF::Mesh::Quad4::Regular mesh(nx, nx);
+    int64_t nelem = mesh.nelem(), nnode = mesh.nnode();
+    auto K = read(in, nelem), G = read(in, nelem), uh = read(in, nnode * 2);
+
+    try {
+        GF::Vector vector(mesh.conn(), mesh.dofs());
+        GF::Element::Quad4::Quadrature quad(vector.AsElement(GF::array<double>::from_host(mesh.coor())));
+        auto u = GF::array<double>::from_host(uh.data(), {nnode, 2});
+        auto Kd = GF::array<double>::from_host(K.data(), {nelem});
+        auto Gd = GF::array<double>::from_host(G.data(), {nelem});
+
+        auto ue = vector.allocate_elemvec();
+        auto Eps = GF::array<double>(quad.shape_qtensor2());
+        auto Sig = GF::array<double>(quad.shape_qtensor2());
+        auto fe = vector.allocate_elemvec();
+        auto fint = vector.allocate_nodevec();
+        vector.asElement(u, ue);
+        quad.symGradN_vector(ue, Eps);
+        GF::check(gfgpu_elastic_stress(Eps.data(), Kd.data(), Gd.data(), nelem, quad.nip(), 2,
+                                       Sig.data(), nullptr),
+                  "stress");
+        quad.int_gradN_dot_tensor2_dV(Sig, fe);
+        vector.assembleNode(fe, fint);
+
+        GF::Element::Quad4::Quadrature nodal(vector.AsElement(GF::array<double>::from_host(mesh.coor())),
+                                             GF::Element::Quad4::Nodal::xi(),
+                                             GF::Element::Quad4::Nodal::w());
+        GF::host::array<double> rho({nelem, 4}, 1.0);
+        GF::MatrixDiagonal M(mesh.conn(), mesh.dofs());
+        M.assemble(nodal.Int_N_scalar_NT_dV(GF::array<double>::from_host(rho)));
+
+        std::ofstream out(argv[2], std::ios::binary);
+        dump(out, quad.GradN());
+        dump(out, quad.dV());
+        dump(out, ue);
+        dump(out, Eps);
+        dump(out, Sig);
+        dump(out, fe);
+        dump(out, fint);
+        dump(out, M.data());
+
+        // error path: a shape mismatch is reported as std::runtime_error
+        bool threw = false;
+        try {
+            auto bad = GF::array<double>({3, 3});
+            vector.asElement(u, bad);
+        }
+        catch (const std::runtime_error&) {
+            threw = true;
+        }
+        if (!threw) return 3;
+    }
+    catch (const std::exception& e) {
+        std::cerr << e.what() << std::endl;
+        return 1;
+    }
+    std::cout << "ok" << std::endl;
+    return 0;
+}
