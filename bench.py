@@ -339,6 +339,8 @@ def run_gpu(args, rank, world):
     # square 34 instructions incl. 2 DFMA; uniform 48 incl. 7; general per Gauss point 8+8+9 FMA
     # strain, 7 stress, 16 FMA + 8 force)
     fl_elem = {"uniform-square": 36, "uniform": 55, "general": 4 * (2 * 25 + 7 + 2 * 16 + 8)}[path]
+    # FP64 instructions per element (DADD, DMUL and DFMA issue at the same rate)
+    in_elem = {"uniform-square": 34, "uniform": 48, "general": 4 * (25 + 7 + 16 + 8)}[path]
     fp64_ach = fl_elem * nelem / (ms_elem * 1e-3)
     traffic = None
     prof = os.path.join(ROOT, "profiles", f"{kernel}_{args.nx}.txt")
@@ -369,7 +371,11 @@ def run_gpu(args, rank, world):
                               "peak_tflops": fp64_peak / 1e12,
                               "frac": fp64_ach / fp64_peak,
                               "flops_per_elem": fl_elem,
-                              "peak_source": "measured live (gfgpu_probe_fp64)"},
+                              "instr_per_elem": in_elem,
+                              "achieved_ginstr_s": in_elem * nelem / (ms_elem * 1e-3) / 1e9,
+                              "peak_ginstr_s": fp64_peak / 2.0 / 1e9,
+                              "instr_frac": in_elem * nelem / (ms_elem * 1e-3) / (fp64_peak / 2.0),
+                              "peak_source": "measured live (gfgpu_probe_fp64: DFMA chains)"},
                      "step": {"ms_per_increment": ms_inc, "ms_node_kernel": ms_node,
                               "alg_bytes": b_step,
                               "achieved_gbs": b_step / (ms_inc * 1e-3) / 1e9}},
