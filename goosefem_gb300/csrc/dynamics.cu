@@ -15,6 +15,7 @@
 // displacement predictor of the next increment (main.cpp:119).
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -848,6 +849,80 @@ int gfgpu_internal_force(const gfgpu_verlet_desc* d, const double* u, double* fi
     double* fe = static_cast<double*>(workspace);
     GF_TRY(launch_elem(d, u, fe, S(stream)));
     return gfgpu_assemble_node(d->csr_ptr, d->csr_idx, d->dofs, d->nnode, d->ndim, fe, fint, stream);
+}
+
+} // extern "C"
+
+// ------------------------------------------------------------------ allocation-free increments
+//
+// Scratch of gfgpu_verlet_step_noalloc: the element forces of one increment live in this
+// file-scope device array instead of caller- or library-allocated memory. Every GPU that loads
+// the library holds it (32 MiB) until the process exits. In host code the name is only a
+// host-side stand-in: its device address is obtained per device with cudaGetSymbolAddress and
+// passed to the kernels.
+static __device__ __align__(256) double g_noalloc_fe[GFGPU_NOALLOC_FE_DOUBLES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+double* g_noalloc_ptr[kMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+// Device address of g_noalloc_fe on the current device (looked up on the first call per device).
+int noalloc_scratch(double** out)
+{
+    int dev = 0;
+    GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+    if (dev < 0 || dev >= kMaxDevices) return fail(GFGPU_ERR_UNSUPPORTED, "device ordinal >= 64");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        GF_TRY(check_cuda(cudaGetSymbolAddress(&p, g_noalloc_fe), "cudaGetSymbolAddress"));
+        g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return GFGPU_OK;
+}
+} // namespace
+
+extern "C" {
+
+int gfgpu_verlet_step_noalloc(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                              int64_t nsteps, gfgpu_stream_t stream)
+{
+    GF_TRY(check_desc(d));
+    GF_REQUIRE(u && v && a && nsteps >= 0, "bad argument");
+    int64_t need = d->nelem * d->nne * d->ndim;
+    if (need > GFGPU_NOALLOC_FE_DOUBLES)
+        return fail(GFGPU_ERR_ARG,
+                    "gfgpu_verlet_step_noalloc: the mesh needs " + std::to_string(need) +
+                        " element-force values, the built-in scratch holds " +
+                        std::to_string(static_cast<int64_t>(GFGPU_NOALLOC_FE_DOUBLES)) +
+                        " (nelem * nne * ndim); use gfgpu_verlet_step with a workspace");
+    double* fe = nullptr;
+    GF_TRY(noalloc_scratch(&fe));
+    if (nsteps == 0) return GFGPU_OK;
+    cudaStream_t s = S(stream);
+    VerletCoef k = verlet_coefficients(d);
+    int64_t n = d->nnode * d->ndim;
+    unsigned gn = grid_for(n);
+    bool st = strict_mode();
+    if (st)
+        k_predict<true><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
+    else
+        k_predict<false><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
+    GF_TRY(check_launch("noalloc predict"));
+    for (int64_t it = 0; it < nsteps; ++it) {
+        GF_TRY(launch_elem(d, u, fe, s));
+        int adv = it + 1 < nsteps ? 1 : 0;
+        if (st)
+            k_verlet_node<true><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
+                                                      d->inv, fe, d->fext, n, k, adv, u, v, a);
+        else
+            k_verlet_node_fast<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
+                                                     d->inv, fe, d->fext, n, k, adv, u, v, a);
+        GF_TRY(check_launch("noalloc node kernel"));
+    }
+    return GFGPU_OK;
 }
 
 int gfgpu_verlet_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,

@@ -265,6 +265,24 @@ int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stre
  * `workspace` is device memory of gfgpu_verlet_workspace_bytes(d). */
 int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
                       int64_t nsteps, void* workspace, gfgpu_stream_t stream);
+/* Size of the built-in scratch of gfgpu_verlet_step_noalloc, in doubles (32 MiB). */
+#define GFGPU_NOALLOC_FE_DOUBLES 4194304
+
+/* The same increments as gfgpu_verlet_step, for callers that cannot allocate device memory:
+ * host codes that reach the GPU only through this C ABI and have no CUDA runtime of their own
+ * to call cudaMalloc with, or codes whose device memory is owned entirely by another allocator
+ * or pool, where an extra allocation is not allowed or could fail in the middle of a run.
+ * This entry point has no counterpart in the reference (GooseFEM allocates its temporaries on
+ * the host); it allocates nothing: the element-force scratch is a file-scope device array of
+ * GFGPU_NOALLOC_FE_DOUBLES values that every GPU loading the library keeps until the process
+ * exits. Meshes with nelem * nne * ndim above that size are rejected with GFGPU_ERR_ARG.
+ * The first call on a device looks up the array's device address (once per device, with that
+ * device current); make that first call before any stream capture. All calls share the one
+ * array, which keeps the last call's element forces (every increment overwrites it completely
+ * before reading it); calls whose work overlaps on the GPU (for example on two streams) race on
+ * it. u, v, a as in gfgpu_verlet_step. */
+int gfgpu_verlet_step_noalloc(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                              int64_t nsteps, gfgpu_stream_t stream);
 /* Internal force only: fint (nodevec) = assembleNode(int_gradN_dot_tensor2_dV(sigma(u))), using
  * the same element kernel as the step. */
 int gfgpu_internal_force(const gfgpu_verlet_desc* d, const double* u, double* fint,
