@@ -46,10 +46,14 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="bounded CPU-baseline sample length")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
-    p.add_argument("--workload", default="explicit", choices=["explicit", "static", "batch"],
+    p.add_argument("--workload", default="explicit",
+                   choices=["explicit", "static", "batch", "learned"],
                    help="explicit: 2048^2 Quad4 dynamics (headline); static: Hex8 n3d^3 Jacobi-PCG;"
-                        " batch: periodic Quad4 instances")
+                        " batch: periodic Quad4 instances; learned: n2d^2 learned-FCG vs Jacobi-PCG")
     p.add_argument("--n3d", type=int, default=128)
+    p.add_argument("--n2d", type=int, default=512)
+    p.add_argument("--nloads", type=int, default=64)
+    p.add_argument("--train-steps", type=int, default=2000)
     p.add_argument("--ninst", type=int, default=256)
     p.add_argument("--batch-steps", type=int, default=500)
     p.add_argument("--path", default="auto", choices=["auto", "uniform", "general"],
@@ -506,6 +510,63 @@ def run_batch(args):
     return 0
 
 
+def run_learned(args):
+    """Quad4 512^2 two-phase static case: learned-preconditioner FCG vs Jacobi-PCG, both to
+    1e-8 relative residual in FP64 (time-to-solution on the same GPU; training reported apart)."""
+    import torch
+
+    from goosefem_gb300 import learned as LR
+    from goosefem_gb300 import mesh as M
+
+    nx = args.n2d
+    K, G, inside = LR.inclusion_material(nx, nx, 512)
+    m = M.Quad4.Regular(nx, nx)
+    iip, xp = LR.static_bc(m)
+    lp = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0)
+
+    def timed(fn):
+        x = lp.initial_guess(xp)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it, rel = fn(x)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, it, rel
+
+    res = {}
+    for name, fn in (("jacobi_pcg", lambda x: lp.jacobi_pcg(x)),
+                     ("jacobi_fcg", lambda x: lp.fcg(x, use_nn=False))):
+        timed(fn)  # warm-up
+        best = min((timed(fn) for _ in range(args.steps)), key=lambda r: r[0])
+        res[name] = {"seconds": best[0], "iterations": best[1], "relres_true": best[2]}
+    t0 = time.perf_counter()
+    npairs = lp.make_pairs(nloads=args.nloads, snaps=64, every=16, inner=8, seed=1)
+    torch.cuda.synchronize()
+    t_pairs = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    losses = lp.train(steps=args.train_steps, batch=32, crop=64, margin=8, lr=2e-3,
+                      log_every=max(args.train_steps // 10, 1))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    fn = lambda x: lp.fcg(x, use_nn=True)  # noqa: E731
+    timed(fn)
+    best = min((timed(fn) for _ in range(args.steps)), key=lambda r: r[0])
+    res["learned_fcg"] = {"seconds": best[0], "iterations": best[1], "relres_true": best[2]}
+    line = {"metric": "time-to-1e-8 resid (learned FCG vs Jacobi PCG)",
+            "value": res["learned_fcg"]["seconds"], "unit": "s", "higher_is_better": False,
+            "n_gpus": 1, "dtype": "f64 solve, bf16-weight/fp32-accumulate network",
+            "data": "synthetic (seeded inclusions)",
+            "config": {"workload": f"Quad4 Regular {nx}x{nx}, two-phase (inclusions "
+                                   f"{100 * inside.mean():.1f}% area, x10 moduli), bottom fixed, "
+                                   "top uy=-1e-2", "pairs": npairs, "train_steps": args.train_steps},
+            "solvers": res,
+            "speedup_vs_jacobi_pcg": res["jacobi_pcg"]["seconds"] / res["learned_fcg"]["seconds"],
+            "iteration_ratio": res["jacobi_pcg"]["iterations"] / res["learned_fcg"]["iterations"],
+            "pair_generation_seconds": t_pairs, "training_seconds": t_train,
+            "loss_first_last": [losses[0], losses[-1]]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -516,6 +577,8 @@ def main():
         return run_static(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "learned":
+        return run_learned(args)
     if world > 1:
         import torch
 

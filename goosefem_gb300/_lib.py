@@ -42,6 +42,7 @@ _CTYPE = {
     "int32_t": C.c_int32,
     "int64_t": C.c_int64,
     "double": C.c_double,
+    "float": C.c_float,
     "gfgpu_stream_t": C.c_void_p,
     "gfgpu_graph_t": C.c_void_p,
     "void": None,

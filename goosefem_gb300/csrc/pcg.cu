@@ -352,4 +352,76 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
     return GFGPU_OK;
 }
 
+// ---------------------------------------------------------------- step-by-step session
+
+int gfgpu_pcg_begin(const gfgpu_verlet_desc* d, const double* diag, const double* rhs,
+                    const double* x, void* workspace, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d && diag && x && workspace, "bad argument");
+    cudaStream_t s = S(stream);
+    PcgWs w = carve(d, workspace);
+    int64_t n = d->nnode * d->ndim;
+    const unsigned gb = kRedBlocks;
+    k_inv_free<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, diag, n, w.minv);
+    // b = rhs_u - (A x_p)_u
+    k_keep_prescribed<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.p);
+    GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
+    k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
+                                               rhs, w.minv, n, w.bvec, w.z, nullptr, w.partial);
+    k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_BB);
+    // r = rhs_u - (A x)_u, z = M^-1 r, p = z
+    GF_TRY(gfgpu_internal_element_forces(d, x, w.fe, s));
+    k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
+                                               rhs, w.minv, n, w.r, w.z, w.p, w.partial);
+    k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ); // SC_RZ = r.z, SC_RZ_NEW = r.r
+    k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_RR);
+    return check_launch("pcg_begin");
+}
+
+int gfgpu_pcg_iterate(const gfgpu_verlet_desc* d, int64_t niter, double* x, void* workspace,
+                      gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d && x && workspace && niter >= 0, "bad argument");
+    cudaStream_t s = S(stream);
+    PcgWs w = carve(d, workspace);
+    int64_t n = d->nnode * d->ndim;
+    const unsigned gb = kRedBlocks;
+    for (int64_t k = 0; k < niter; ++k) {
+        GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
+        k_pcg_gather<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
+                                                 w.fe, w.p, n, w.q, w.partial);
+        k_reduce<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, SC_PQ);
+        k_pcg_alpha<<<1, 32, 0, s>>>(w.sc);
+        k_pcg_update<<<gb, kRedThreads, 0, s>>>(d->part, d->nnu, w.minv, w.p, w.q, n, w.sc, x, w.r,
+                                                 w.z, w.partial);
+        k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ_NEW);
+        k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_RR);
+        k_pcg_beta<<<1, 32, 0, s>>>(w.sc);
+        k_pcg_direction<<<grid_for(n), kBlock, 0, s>>>(w.z, w.sc, n, w.p);
+    }
+    return check_launch("pcg_iterate");
+}
+
+int gfgpu_pcg_vector(const gfgpu_verlet_desc* d, void* workspace, int32_t which, double** ptr)
+{
+    GF_REQUIRE(d && workspace && ptr && which >= 0 && which <= 2, "bad argument");
+    PcgWs w = carve(d, workspace);
+    *ptr = which == 0 ? w.r : (which == 1 ? w.z : w.p);
+    return GFGPU_OK;
+}
+
+int gfgpu_pcg_norms(const gfgpu_verlet_desc* d, const void* workspace, double* rr, double* bb,
+                    gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d && workspace && rr && bb, "bad argument");
+    PcgWs w = carve(d, const_cast<void*>(workspace));
+    double h[SC_COUNT];
+    GF_TRY(check_cuda(cudaMemcpyAsync(h, w.sc, sizeof(h), cudaMemcpyDeviceToHost, S(stream)),
+                      "cudaMemcpyAsync"));
+    GF_TRY(check_cuda(cudaStreamSynchronize(S(stream)), "cudaStreamSynchronize"));
+    *rr = h[SC_RR];
+    *bb = h[SC_BB];
+    return GFGPU_OK;
+}
+
 } // extern "C"

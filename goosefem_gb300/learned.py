@@ -1,0 +1,207 @@
+"""Learned preconditioner for the matrix-free static solve of a Regular Quad4 mesh.
+
+The network (4 convolution layers 3x3, 32 channels, dilations 1, 2, 4, 1: a 17 x 17 node
+receptive field; BF16 weights, FP32 accumulation; kernels in csrc/learned.cu) is trained to
+reproduce the correction that `inner` iterations of restarted Jacobi-PCG make from a residual.
+That map is local (its support grows by one node per iteration), which a local network can
+represent. The training pairs come from the plain solver itself: Jacobi-PCG runs on random loads,
+their residuals are snapshotted every few iterations, and each snapshot r is paired with the
+correction c = PCG_inner(A, r) (both scaled by the RMS of r). Inside the flexible CG of Notay
+(FCG(1), FP64 vectors and dot products) the trained network replaces those inner iterations in
+one application: z = RMS(r) * net(r / RMS(r)).
+"""
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+from .statics import ElasticStatic
+
+
+class NNDesc(C.Structure):
+    """Mirror of gfgpu_nn_desc (include/gfgpu.h)."""
+
+    _fields_ = [("weights_bf16", C.c_void_p), ("params_f32", C.c_void_p),
+                ("material", C.c_void_p), ("H", C.c_int32), ("W", C.c_int32)]
+
+
+def inclusion_material(nx, ny, seed, fraction=0.15, rmin=4.0, rmax=12.0, K0=1.0, G0=0.5, factor=10.0):
+    """Two-phase element moduli: matrix (K0, G0) and circular inclusions (x factor), radius
+    U[rmin, rmax] elements at seeded random centres, placed until the inclusion area (elements
+    whose centre lies in a circle) reaches `fraction`."""
+    rng = np.random.default_rng(seed)
+    cx = (np.arange(nx) + 0.5)[None, :].repeat(ny, 0)
+    cy = (np.arange(ny) + 0.5)[:, None].repeat(nx, 1)
+    inside = np.zeros((ny, nx), dtype=bool)
+    while inside.mean() < fraction:
+        r = rng.uniform(rmin, rmax)
+        x0, y0 = rng.uniform(0, nx), rng.uniform(0, ny)
+        inside |= (cx - x0) ** 2 + (cy - y0) ** 2 <= r * r
+    K = np.where(inside, K0 * factor, K0).ravel()
+    G = np.where(inside, G0 * factor, G0).ravel()
+    return K, G, inside
+
+
+def static_bc(mesh, uy_top=-1e-2):
+    """Bottom edge fixed, top edge uy prescribed (ux free): (iip, prescribed values)."""
+    dofs = mesh.dofs()
+    bot, top = mesh.nodesBottomEdge(), mesh.nodesTopEdge()
+    iip = np.unique(np.concatenate([dofs[bot, :].ravel(), dofs[top, 1]]))
+    xp = np.where(np.isin(iip, dofs[top, 1]), uy_top, 0.0)
+    return iip, xp
+
+
+class LearnedPreconditioner:
+    """Network parameters, training pairs, training loop and the preconditioned FCG solve for one
+    Regular Quad4 mesh (nx x ny elements, per-element K, G) with prescribed dofs iip."""
+
+    def __init__(self, nx, ny, K, G, iip, seed=0):
+        from . import mesh as M
+
+        self.nx, self.ny = int(nx), int(ny)
+        self.H, self.W = self.ny + 1, self.nx + 1
+        m = M.Quad4.Regular(nx, ny)
+        self.mesh = m
+        self.static = ElasticStatic(m.coor(), m.conn(), m.dofs(), K, G, iip)
+        self.iip = np.asarray(iip)
+        dev = _dev.device()
+        self.free = torch.ones(self.H * self.W * 2, dtype=torch.bool, device=dev)
+        self.free[torch.as_tensor(self.iip, device=dev).long()] = False
+        self.nfree = int(self.free.sum())
+        # nodal material channels: mean of the adjacent elements' K / max K and G / max G
+        Kn = np.zeros(self.H * self.W)
+        Gn = np.zeros(self.H * self.W)
+        cnt = np.zeros(self.H * self.W)
+        conn = m.conn()
+        for k in range(4):
+            np.add.at(Kn, conn[:, k], K)
+            np.add.at(Gn, conn[:, k], G)
+            np.add.at(cnt, conn[:, k], 1.0)
+        mat = np.stack([Kn / cnt / np.max(K), Gn / cnt / np.max(G)], axis=1).astype(np.float32)
+        self.material = torch.as_tensor(mat, device=dev).contiguous()
+        # parameters: He initialisation, zero biases, a small last layer
+        self.P = int(_lib.lib().gfgpu_nn_param_count())
+        rng = np.random.default_rng(seed)
+        p = np.zeros(self.P, dtype=np.float32)
+        for layer, (cin, cout) in enumerate(((4, 32), (32, 32), (32, 32), (32, 2))):
+            off = int(_lib.lib().gfgpu_nn_param_offset(layer, 0))
+            std = math.sqrt(2.0 / (9 * cin)) * (0.1 if layer == 3 else 1.0)
+            p[off:off + 9 * cin * cout] = rng.normal(0.0, std, 9 * cin * cout)
+        self.params = torch.as_tensor(p, device=dev)
+        self.wbf = self.params.to(torch.bfloat16)
+        self.grads = torch.zeros_like(self.params)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.step = 0
+        self.R = None
+        self.T = None
+        self.losses = []
+
+    # ------------------------------------------------------------------ helpers
+    def _desc(self):
+        return C.addressof(self.static.desc)
+
+    def nn_desc(self):
+        d = NNDesc()
+        d.weights_bf16 = self.wbf.data_ptr()
+        d.params_f32 = self.params.data_ptr()
+        d.material = self.material.data_ptr()
+        d.H, d.W = self.H, self.W
+        self._nnd = d
+        return d
+
+    def _pcg_ws(self):
+        nb = int(_lib.lib().gfgpu_pcg_workspace_bytes(self._desc()))
+        return torch.empty(nb // 8 + 1, dtype=torch.float64, device=_dev.device())
+
+    # ------------------------------------------------------------------ training pairs
+    def make_pairs(self, nloads=64, snaps=64, every=16, inner=8, seed=1):
+        """(residual, Jacobi-PCG correction) pairs from the plain solver on random loads."""
+        n = self.H * self.W * 2
+        npairs = nloads * snaps
+        dev = _dev.device()
+        self.R = torch.empty((npairs, self.H, self.W, 2), dtype=torch.float32, device=dev)
+        self.T = torch.empty_like(self.R)
+        ws1, ws2 = self._pcg_ws(), self._pcg_ws()
+        s = _dev.stream()
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(seed)
+        r_ptr = C.c_void_p(0)
+        _lib.call("gfgpu_pcg_vector", self._desc(), ws1.data_ptr(), 0, C.addressof(r_ptr))
+        r = torch.empty(n, dtype=torch.float64, device=dev)
+        k = 0
+        for _ in range(nloads):
+            b = (torch.rand(n, generator=gen, dtype=torch.float64, device=dev) * 2.0 - 1.0)
+            b[~self.free] = 0.0
+            x = torch.zeros(n, dtype=torch.float64, device=dev)
+            _lib.call("gfgpu_pcg_begin", self._desc(), self.static.diag.data_ptr(), b.data_ptr(),
+                      x.data_ptr(), ws1.data_ptr(), s)
+            for _ in range(snaps):
+                _lib.call("gfgpu_pcg_iterate", self._desc(), every, x.data_ptr(), ws1.data_ptr(), s)
+                _lib.call("gfgpu_memcpy_d2d", r.data_ptr(), r_ptr.value, n * 8)
+                sigma = torch.sqrt((r[self.free] ** 2).sum() / self.nfree)
+                c = torch.zeros(n, dtype=torch.float64, device=dev)
+                _lib.call("gfgpu_pcg_begin", self._desc(), self.static.diag.data_ptr(), r.data_ptr(),
+                          c.data_ptr(), ws2.data_ptr(), s)
+                _lib.call("gfgpu_pcg_iterate", self._desc(), inner, c.data_ptr(), ws2.data_ptr(), s)
+                self.R[k] = (r / sigma).view(self.H, self.W, 2).float()
+                self.T[k] = (c / sigma).view(self.H, self.W, 2).float()
+                k += 1
+        return npairs
+
+    # ------------------------------------------------------------------ training
+    def train(self, steps=2000, batch=32, crop=64, margin=8, lr=2e-3, seed=2, log_every=0):
+        dev = _dev.device()
+        B, S = int(batch), int(crop)
+        X = torch.empty((B, S, S, 4), dtype=torch.float32, device=dev)
+        Tc = torch.empty((B, S, S, 2), dtype=torch.float32, device=dev)
+        loss = torch.zeros(1, dtype=torch.float32, device=dev)
+        nb = int(_lib.lib().gfgpu_nn_train_workspace_bytes(B, S, S))
+        ws = torch.empty(nb // 4 + 64, dtype=torch.float32, device=dev)
+        rng = np.random.default_rng(seed)
+        npairs = self.R.shape[0]
+        s = _dev.stream()
+        for it in range(steps):
+            pos = np.stack([rng.integers(0, npairs, B),
+                            rng.integers(-margin, max(self.H - S + margin, -margin) + 1, B),
+                            rng.integers(-margin, max(self.W - S + margin, -margin) + 1, B)],
+                           axis=1).astype(np.int32)
+            pos_d = torch.as_tensor(pos, device=dev)
+            _lib.call("gfgpu_nn_gather_crops", self.R.data_ptr(), self.T.data_ptr(),
+                      self.material.data_ptr(), pos_d.data_ptr(), B, S, self.H, self.W,
+                      X.data_ptr(), Tc.data_ptr(), s)
+            _lib.call("gfgpu_nn_train_step", self.wbf.data_ptr(), self.params.data_ptr(),
+                      X.data_ptr(), Tc.data_ptr(), B, S, margin, self.grads.data_ptr(),
+                      loss.data_ptr(), ws.data_ptr(), s)
+            self.step += 1
+            cur = lr * 0.5 * (1.0 + math.cos(math.pi * it / max(steps, 1)))
+            _lib.call("gfgpu_nn_adam", self.params.data_ptr(), self.grads.data_ptr(),
+                      self.m.data_ptr(), self.v.data_ptr(), self.P, float(max(cur, lr * 0.02)),
+                      0.9, 0.999, 1e-8, self.step, self.wbf.data_ptr(), s)
+            if log_every and (it % log_every == 0 or it == steps - 1):
+                self.losses.append((it, float(loss.item())))
+        return self.losses
+
+    # ------------------------------------------------------------------ solves
+    def initial_guess(self, xp):
+        n = self.H * self.W * 2
+        x = torch.zeros(n, dtype=torch.float64, device=_dev.device())
+        x[torch.as_tensor(self.iip, device=x.device).long()] = torch.as_tensor(xp, device=x.device)
+        return x
+
+    def fcg(self, x, tol=1e-8, use_nn=True, maxiter=200000, check_every=8):
+        nb = int(_lib.lib().gfgpu_fcg_workspace_bytes(self._desc(), self.H, self.W))
+        ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=_dev.device())
+        it = C.c_int64(0)
+        rel = C.c_double(0.0)
+        nnd = C.addressof(self.nn_desc()) if use_nn else None
+        _lib.call("gfgpu_fcg_solve", self._desc(), self.static.diag.data_ptr(), nnd, x.data_ptr(),
+                  float(tol), int(maxiter), int(check_every), ws.data_ptr(), _dev.stream(),
+                  C.addressof(it), C.addressof(rel))
+        return int(it.value), float(rel.value)
+
+    def jacobi_pcg(self, x, tol=1e-8, check_every=16):
+        return self.static.solve(x.view(self.H * self.W, 2), tol=tol, check_every=check_every)

@@ -343,6 +343,67 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
                     int64_t maxiter, int32_t check_every, void* workspace, gfgpu_stream_t stream,
                     int64_t* iters, double* relres);
 
+/* Step-by-step Jacobi-PCG on the same workspace as gfgpu_pcg_solve (used to generate the
+ * training pairs of the learned preconditioner): begin sets b = rhs_u - (A x_p)_u (rhs may be
+ * NULL: no external load), r = b - (A x)_u, z = M^-1 r, p = z; iterate runs niter iterations
+ * without convergence checks; vector returns a device pointer to r (which = 0), z (1) or p (2)
+ * inside the workspace; norms synchronises and returns r.r and b.b. */
+int gfgpu_pcg_begin(const gfgpu_verlet_desc* d, const double* diag, const double* rhs,
+                    const double* x, void* workspace, gfgpu_stream_t stream);
+int gfgpu_pcg_iterate(const gfgpu_verlet_desc* d, int64_t niter, double* x, void* workspace,
+                      gfgpu_stream_t stream);
+int gfgpu_pcg_vector(const gfgpu_verlet_desc* d, void* workspace, int32_t which, double** ptr);
+int gfgpu_pcg_norms(const gfgpu_verlet_desc* d, const void* workspace, double* rr, double* bb,
+                    gfgpu_stream_t stream);
+
+/* ============================ learned preconditioner (device) ============================= */
+
+/* The network: 4 convolution layers 3x3 on the nodal grid of a Regular Quad4 mesh (NHWC, the
+ * nodevec [nnode, 2] is the [H, W, 2] image), channels 4 -> 32 -> 32 -> 32 -> 2, dilations
+ * 1, 2, 4, 1, ReLU after layers 1-3, zero padding. Input channels: the residual scaled by its
+ * RMS over the free dofs, and two nodal material channels. Parameters in one flat array: per
+ * layer W [9][cin][cout] then b [cout] (gfgpu_nn_param_offset); weights are used in BF16, biases
+ * and all accumulations in FP32. */
+typedef struct {
+    const void* weights_bf16; /* [gfgpu_nn_param_count()] BF16 bit patterns */
+    const float* params_f32;  /* [gfgpu_nn_param_count()] FP32 master copy (biases read here) */
+    const float* material;    /* [H, W, 2] nodal material channels */
+    int32_t H, W;             /* nodal grid: ny + 1 rows of nx + 1 nodes */
+} gfgpu_nn_desc;
+
+int32_t gfgpu_nn_param_count(void);
+int32_t gfgpu_nn_param_offset(int32_t layer, int32_t bias);
+/* Training (CUDA cores, FP32 accumulate) on B crops of H x W nodes. */
+int64_t gfgpu_nn_train_workspace_bytes(int32_t B, int32_t H, int32_t W);
+int gfgpu_nn_forward(const void* weights_bf16, const float* params_f32, const float* X, int32_t B,
+                     int32_t H, int32_t W, float* Y, void* workspace, gfgpu_stream_t stream);
+/* Forward, masked mean-squared error over the crop interior [margin, S - margin)^2 against T,
+ * backward: grads (flat, like the parameters) and *loss (device float). Deterministic. */
+int gfgpu_nn_train_step(const void* weights_bf16, const float* params_f32, const float* X,
+                        const float* T, int32_t B, int32_t S, int32_t margin, float* grads,
+                        float* loss, void* workspace, gfgpu_stream_t stream);
+/* Adam on the FP32 master parameters; rewrites the BF16 weights. */
+int gfgpu_nn_adam(float* params, const float* grads, float* m, float* v, int32_t n, float lr,
+                  float beta1, float beta2, float eps, int32_t step, void* weights_bf16,
+                  gfgpu_stream_t stream);
+/* Crops X [B, S, S, 4] (stored scaled residual + material) and targets T [B, S, S, 2] from
+ * stored pairs R, Tg [npairs, H, W, 2]; pos [B, 3] = (pair, y0, x0). */
+int gfgpu_nn_gather_crops(const float* R, const float* T, const float* material,
+                          const int32_t* pos, int32_t B, int32_t S, int32_t H, int32_t W,
+                          float* X, float* Tc, gfgpu_stream_t stream);
+/* Inference on one full grid with the middle layers on the tensor cores (mma.sync BF16, FP32
+ * accumulate): X0 [H, W, 4] -> Y [H, W, 2]; workspace 3 x H*W*32 BF16 (256-byte aligned). */
+int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* workspace,
+                   gfgpu_stream_t stream);
+/* Flexible CG (Notay's FCG(1): p = z - (z.q_prev / p_prev.q_prev) p_prev) in FP64 on the
+ * partitioned elastic system of gfgpu_pcg_solve, preconditioned by the network (nn != NULL;
+ * z = RMS(r) * net(r / RMS(r)), prescribed dofs 0) or by Jacobi (nn == NULL). Same stopping rule
+ * and true-residual check as gfgpu_pcg_solve. Synchronises. */
+int64_t gfgpu_fcg_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W);
+int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
+                    double* x, double tol, int64_t maxiter, int32_t check_every, void* workspace,
+                    gfgpu_stream_t stream, int64_t* iters, double* relres);
+
 /* ============================ probes ====================================================== */
 
 /* FP64 FMA throughput probe: a kernel of independent DFMA chains, `blocks` x 256 threads,

@@ -1,0 +1,172 @@
+"""The learned preconditioner: the network's training kernels against the FP64 numpy oracle
+(oracle/nn.py), the tensor-core inference against the FP32 path, the flexible CG against the
+direct solve, and what the trained network gains over the same solver without it."""
+
+import numpy as np
+import pytest
+import torch
+
+from _common import rel_err
+
+pytestmark = pytest.mark.gpu
+
+DILS = (1, 2, 4, 1)
+SHAPES = ((4, 32), (32, 32), (32, 32), (32, 2))
+
+
+@pytest.fixture(scope="module")
+def L():
+    import goosefem_gb300  # noqa: F401  (loads the library)
+    from goosefem_gb300 import _lib
+
+    return _lib
+
+
+def _random_params(L, seed, scale=1.0):
+    rng = np.random.default_rng(seed)
+    P = int(L.lib().gfgpu_nn_param_count())
+    p = np.zeros(P, dtype=np.float32)
+    for k, (ci, co) in enumerate(SHAPES):
+        w0 = int(L.lib().gfgpu_nn_param_offset(k, 0))
+        b0 = int(L.lib().gfgpu_nn_param_offset(k, 1))
+        p[w0:w0 + 9 * ci * co] = rng.normal(0, scale * np.sqrt(2.0 / (9 * ci)), 9 * ci * co)
+        p[b0:b0 + co] = rng.normal(0, 0.1, co)
+    pt = torch.as_tensor(p, device="cuda")
+    wb = pt.to(torch.bfloat16)
+    return pt, wb
+
+
+def _oracle_params(L, pt, wb):
+    """W as the BF16 values the kernels use (in FP64), biases FP32 -> FP64."""
+    wq = wb.float().cpu().numpy().astype(np.float64)
+    pf = pt.cpu().numpy().astype(np.float64)
+    out = []
+    for k, (ci, co) in enumerate(SHAPES):
+        w0 = int(L.lib().gfgpu_nn_param_offset(k, 0))
+        b0 = int(L.lib().gfgpu_nn_param_offset(k, 1))
+        out.append((wq[w0:w0 + 9 * ci * co].reshape(9, ci, co), pf[b0:b0 + co]))
+    return out
+
+
+def test_training_gradients_match_oracle(L):
+    from oracle import nn as O
+
+    B, S, margin = 2, 14, 2
+    pt, wb = _random_params(L, 0)
+    rng = np.random.default_rng(1)
+    X = rng.normal(size=(B, S, S, 4)).astype(np.float32)
+    T = rng.normal(size=(B, S, S, 2)).astype(np.float32)
+    Xd, Td = torch.as_tensor(X, device="cuda"), torch.as_tensor(T, device="cuda")
+    grads = torch.zeros_like(pt)
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    nb = int(L.lib().gfgpu_nn_train_workspace_bytes(B, S, S))
+    ws = torch.empty(nb // 4 + 64, dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    L.call("gfgpu_nn_train_step", wb.data_ptr(), pt.data_ptr(), Xd.data_ptr(), Td.data_ptr(), B, S,
+           margin, grads.data_ptr(), loss.data_ptr(), ws.data_ptr(), s)
+    params = _oracle_params(L, pt, wb)
+    mask = np.zeros((B, S, S))
+    mask[:, margin:S - margin, margin:S - margin] = 1.0
+    lref, gref = O.loss_and_grads(X.astype(np.float64), T.astype(np.float64), mask, params, DILS)
+    assert abs(float(loss.item()) - lref) <= 1e-5 * abs(lref)
+    g = grads.cpu().numpy().astype(np.float64)
+    for k, (ci, co) in enumerate(SHAPES):
+        w0 = int(L.lib().gfgpu_nn_param_offset(k, 0))
+        b0 = int(L.lib().gfgpu_nn_param_offset(k, 1))
+        assert rel_err(g[w0:w0 + 9 * ci * co].reshape(9, ci, co), gref[k][0]) <= 1e-4, k
+        assert rel_err(g[b0:b0 + co], gref[k][1]) <= 1e-4, k
+    # the same step twice gives the same bits (fixed-order reductions)
+    g1 = grads.clone()
+    L.call("gfgpu_nn_train_step", wb.data_ptr(), pt.data_ptr(), Xd.data_ptr(), Td.data_ptr(), B, S,
+           margin, grads.data_ptr(), loss.data_ptr(), ws.data_ptr(), s)
+    assert torch.equal(g1, grads)
+
+
+def test_tensor_core_inference_matches_fp32_and_oracle(L):
+    from oracle import nn as O
+    from goosefem_gb300.learned import NNDesc
+    import ctypes as C
+
+    H, W = 37, 45
+    pt, wb = _random_params(L, 3, scale=0.8)
+    rng = np.random.default_rng(4)
+    X0 = rng.normal(size=(H, W, 4)).astype(np.float32)
+    Xd = torch.as_tensor(X0, device="cuda")
+    mat = torch.zeros((H, W, 2), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    # FP32 path
+    y32 = torch.empty((H, W, 2), dtype=torch.float32, device="cuda")
+    nb = int(L.lib().gfgpu_nn_train_workspace_bytes(1, H, W))
+    ws = torch.empty(nb // 4 + 64, dtype=torch.float32, device="cuda")
+    L.call("gfgpu_nn_forward", wb.data_ptr(), pt.data_ptr(), Xd.data_ptr(), 1, H, W, y32.data_ptr(),
+           ws.data_ptr(), s)
+    # tensor-core path
+    d = NNDesc()
+    d.weights_bf16, d.params_f32, d.material, d.H, d.W = wb.data_ptr(), pt.data_ptr(), mat.data_ptr(), H, W
+    ytc = torch.empty((H, W, 2), dtype=torch.float32, device="cuda")
+    ws2 = torch.empty(3 * (H * W * 64 + 256) // 2 + 64, dtype=torch.bfloat16, device="cuda")
+    L.call("gfgpu_nn_infer", C.addressof(d), Xd.data_ptr(), ytc.data_ptr(), ws2.data_ptr(), s)
+    yref, _ = O.forward(X0[None].astype(np.float64), _oracle_params(L, pt, wb), DILS)
+    assert rel_err(y32.cpu().numpy(), yref[0]) <= 1e-5
+    # BF16 activations between the layers: agreement to the BF16 rounding level
+    assert rel_err(ytc.cpu().numpy(), yref[0]) <= 3e-2
+
+
+@pytest.fixture(scope="module")
+def small_problem():
+    from goosefem_gb300 import learned as LR
+    from goosefem_gb300 import mesh as M
+
+    nx = ny = 48
+    K, G, _ = LR.inclusion_material(nx, ny, 7, rmin=2.0, rmax=5.0)
+    m = M.Quad4.Regular(nx, ny)
+    iip, xp = LR.static_bc(m)
+    return nx, ny, K, G, iip, xp
+
+
+def _direct(nx, ny, K, G, iip, xp):
+    from oracle import gfref as R
+    from oracle import statics as S
+
+    coor, conn = R.quad4_regular(nx, ny)
+    A = S.stiffness(coor, conn, K, G)
+    return A, S.solve_partitioned(A, iip, xp)
+
+
+def test_fcg_jacobi_matches_direct_solve(small_problem):
+    from goosefem_gb300 import learned as LR
+    from oracle import statics as S
+
+    nx, ny, K, G, iip, xp = small_problem
+    lp = LR.LearnedPreconditioner(nx, ny, K, G, iip)
+    x = lp.initial_guess(xp)
+    it, rel = lp.fcg(x, use_nn=False)
+    A, xr = _direct(nx, ny, K, G, iip, xp)
+    xg = x.cpu().numpy()
+    assert rel <= 1e-8 and S.residual(A, iip, xg) <= 1e-8
+    assert np.linalg.norm(xg - xr) / np.linalg.norm(xr) <= 1e-6
+    # flexible CG with a fixed preconditioner takes the iterations of plain PCG
+    x2 = lp.initial_guess(xp)
+    it2, _ = lp.jacobi_pcg(x2)
+    assert abs(it - it2) <= max(16, it2 // 10)
+
+
+def test_trained_network_reduces_iterations(small_problem):
+    """What the trained network gains over the same flexible CG without it (Jacobi)."""
+    from goosefem_gb300 import learned as LR
+    from oracle import statics as S
+
+    nx, ny, K, G, iip, xp = small_problem
+    lp = LR.LearnedPreconditioner(nx, ny, K, G, iip, seed=0)
+    lp.make_pairs(nloads=8, snaps=24, every=6, inner=8, seed=1)
+    losses = lp.train(steps=300, batch=16, crop=40, margin=8, lr=2e-3, log_every=100)
+    assert losses[-1][1] < losses[0][1]
+    x_nn = lp.initial_guess(xp)
+    it_nn, rel_nn = lp.fcg(x_nn, use_nn=True)
+    x_j = lp.initial_guess(xp)
+    it_j, rel_j = lp.fcg(x_j, use_nn=False)
+    A, xr = _direct(nx, ny, K, G, iip, xp)
+    xg = x_nn.cpu().numpy()
+    assert rel_nn <= 1e-8 and S.residual(A, iip, xg) <= 1e-8  # FP64 answer, same tolerance
+    assert np.linalg.norm(xg - xr) / np.linalg.norm(xr) <= 1e-6
+    assert it_nn < it_j, (it_nn, it_j)
