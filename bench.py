@@ -286,13 +286,13 @@ def run_gpu(args, rank, world):
     # FP64 issue-rate probe (for the FP64 roof)
     probe_out = torch.zeros(2, dtype=torch.float64, device=dev)
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    blocks, iters = sms * 16, 20000
-    _lib.call("gfgpu_probe_fp64", blocks, 2000, probe_out.data_ptr(), stream.cuda_stream)
+    blocks, iters = sms * 16, 10000
+    _lib.call("gfgpu_probe_fp64", blocks, 1000, probe_out.data_ptr(), stream.cuda_stream)
     k0.record(stream)
     _lib.call("gfgpu_probe_fp64", blocks, iters, probe_out.data_ptr(), stream.cuda_stream)
     k1.record(stream)
     torch.cuda.synchronize()
-    fp64_peak = 2.0 * 8 * iters * blocks * 256 / (k0.elapsed_time(k1) * 1e-3)
+    fp64_peak = 2.0 * 16 * iters * blocks * 256 / (k0.elapsed_time(k1) * 1e-3)
 
     # ---------------------------------------------------------------- end-to-end (host buffers)
     hu = torch.zeros((nnode, 2), dtype=torch.float64).pin_memory()

@@ -18,6 +18,8 @@ int fail(int code, const std::string& msg);
 int check_cuda(cudaError_t e, const char* what);
 int check_launch(const char* what);
 bool strict_mode();
+int variant_elem();
+int variant_node();
 
 inline cudaStream_t S(gfgpu_stream_t s)
 {

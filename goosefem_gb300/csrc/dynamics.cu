@@ -247,6 +247,22 @@ k_elem_force_quad4_square(const int32_t* __restrict__ conn, const double* __rest
     GF_FOR(e, nelem) quad4_square_elem<false>(e, conn, u, coef, fe);
 }
 
+// Variant: two neighbouring elements per thread (two independent FP64 dependency chains per
+// thread, shared node loads).
+__global__ void __launch_bounds__(256, 2)
+k_elem_force_quad4_square_x2(const int32_t* __restrict__ conn, const double* __restrict__ u,
+                             const double* __restrict__ coef, int64_t nelem, double* __restrict__ fe)
+{
+    int64_t npair = nelem / 2;
+    GF_FOR(t, npair)
+    {
+        quad4_square_elem<false>(2 * t, conn, u, coef, fe);
+        quad4_square_elem<false>(2 * t + 1, conn, u, coef, fe);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (nelem & 1))
+        quad4_square_elem<false>(nelem - 1, conn, u, coef, fe);
+}
+
 // Constants of the uniform Hex8 path (see k_elem_force_hex8_uniform).
 struct Hex8Uniform {
     double dx, dy, dz;    // 1 / (4 h_i): dNx(m,0) = dx s_xi(m) (1 + s_eta eta)(1 + s_zeta zeta)
@@ -498,6 +514,24 @@ k_verlet_node_fast(const int32_t* __restrict__ dofs, const int32_t* __restrict__
     verlet_node_fast_one<false>(t, dofs, ptr, idx, part, nnu, inv, fe, fext, k, advance, u, v, a);
 }
 
+// Variant: both dofs of a 2-d node per thread (two independent dependency chains per thread).
+__global__ void __launch_bounds__(256)
+k_verlet_node_fast_x2(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
+                      const int32_t* __restrict__ idx, const int32_t* __restrict__ part, int64_t nnu,
+                      const double* __restrict__ inv, const double* __restrict__ fe,
+                      const double* __restrict__ fext, int64_t n, VerletCoef k, int advance,
+                      double* __restrict__ u, double* __restrict__ v, double* __restrict__ a)
+{
+    GF_FOR(t, n / 2)
+    {
+        verlet_node_fast_one<false>(2 * t, dofs, ptr, idx, part, nnu, inv, fe, fext, k, advance, u, v, a);
+        verlet_node_fast_one<false>(2 * t + 1, dofs, ptr, idx, part, nnu, inv, fe, fext, k, advance, u, v,
+                                    a);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1))
+        verlet_node_fast_one<false>(n - 1, dofs, ptr, idx, part, nnu, inv, fe, fext, k, advance, u, v, a);
+}
+
 template <bool S>
 __global__ void __launch_bounds__(256)
 k_verlet_node(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
@@ -603,17 +637,22 @@ __global__ void k_barrier_selftest(GridBar bar)
     grid_sync(bar);
 }
 
-// FP64 probe: 8 independent DFMA chains per thread.
+// FP64 probe: 16 independent DFMA chains per thread (enough independent work per warp to keep
+// the FP64 pipe issuing every cycle).
+constexpr int kProbeChains = 16;
 __global__ void k_probe_fp64(int64_t iters, double* out)
 {
-    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4,
-           a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    double a[kProbeChains];
+#pragma unroll
+    for (int k = 0; k < kProbeChains; ++k) a[k] = threadIdx.x * 1e-9 + k;
     const double m = 0.999999999, c = 1e-7;
     for (int64_t i = 0; i < iters; ++i) {
-        a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
-        a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+#pragma unroll
+        for (int k = 0; k < kProbeChains; ++k) a[k] = fma(a[k], m, c);
     }
-    double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < kProbeChains; ++k) s += a[k];
     if (s == 123.456) out[0] = s; // practically never taken; keeps the chains alive
     if (blockIdx.x == 0 && threadIdx.x == 0) out[1] = s;
 }
@@ -673,8 +712,12 @@ static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, 
 {
     if (d->nelem == 0) return GFGPU_OK;
     if (d->uniform && d->nne == 4 && d->coef) {
-        k_elem_force_quad4_square<<<grid_for(d->nelem), 256, 0, s>>>(d->conn, u, d->coef, d->nelem,
-                                                                     fe);
+        if (variant_elem() == 1)
+            k_elem_force_quad4_square_x2<<<grid_for((d->nelem + 1) / 2), 256, 0, s>>>(
+                d->conn, u, d->coef, d->nelem, fe);
+        else
+            k_elem_force_quad4_square<<<grid_for(d->nelem), 256, 0, s>>>(d->conn, u, d->coef,
+                                                                         d->nelem, fe);
     }
     else if (d->uniform && d->nne == 4) {
         Quad4Uniform c = quad4_uniform_constants(d);
@@ -833,6 +876,10 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
         if (st)
             k_verlet_node<true><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
                                                       d->inv, fe, d->fext, n, k, adv, u, v, a);
+        else if (variant_node() == 1)
+            k_verlet_node_fast_x2<<<grid_for((n + 1) / 2), kBlock, 0, s>>>(
+                d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, d->inv, fe, d->fext, n, k, adv, u,
+                v, a);
         else
             k_verlet_node_fast<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
                                                      d->inv, fe, d->fext, n, k, adv, u, v, a);

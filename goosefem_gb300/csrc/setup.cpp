@@ -13,6 +13,18 @@ namespace gfgpu {
 
 static thread_local std::string g_last_error;
 static int g_strict = 0;
+static int g_variant_elem = 0;
+static int g_variant_node = 0;
+
+int variant_elem()
+{
+    return g_variant_elem;
+}
+
+int variant_node()
+{
+    return g_variant_node;
+}
 
 void set_error(const std::string& msg)
 {
@@ -59,6 +71,15 @@ const char* gfgpu_version(void)
 int gfgpu_set_strict(int strict)
 {
     gfgpu::g_strict = strict ? 1 : 0;
+    return GFGPU_OK;
+}
+
+int gfgpu_set_variant(int elem_variant, int node_variant)
+{
+    if (elem_variant < 0 || elem_variant > 1 || node_variant < 0 || node_variant > 1)
+        return fail(GFGPU_ERR_ARG, "gfgpu_set_variant: variants are 0 or 1");
+    gfgpu::g_variant_elem = elem_variant;
+    gfgpu::g_variant_node = node_variant;
     return GFGPU_OK;
 }
 

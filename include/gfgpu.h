@@ -50,6 +50,11 @@ const char* gfgpu_version(void);
  * The closed-form uniform element kernels are never bit-exact (they sum differently). */
 int gfgpu_set_strict(int strict);
 
+/* Kernel variants of the fast explicit increment (process-wide, default 0 / 0):
+ * elem_variant 1 = two neighbouring elements per thread in the uniform square Quad4 kernel,
+ * node_variant 1 = both dofs of a node per thread in the node kernel. Same results. */
+int gfgpu_set_variant(int elem_variant, int node_variant);
+
 /* ============================ device memory helpers ======================================= */
 
 /* Thin wrappers of the CUDA runtime so that a host program can use the library without
@@ -407,7 +412,7 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
 /* ============================ probes ====================================================== */
 
 /* FP64 FMA throughput probe: a kernel of independent DFMA chains, `blocks` x 256 threads,
- * `iters` iterations of 8 chains; writes a checksum to out[0]. 2*8*iters*blocks*256 flops. */
+ * `iters` iterations of 16 chains; writes a checksum to out[0]. 2*16*iters*blocks*256 flops. */
 int gfgpu_probe_fp64(int64_t blocks, int64_t iters, double* out, gfgpu_stream_t stream);
 
 #ifdef __cplusplus
