@@ -6,13 +6,19 @@
 //
 //  * training kernels (CUDA cores, FP32 accumulate): forward with stored activations, backward
 //    for the inputs and the weights (per-block partial sums reduced in a fixed order:
-//    deterministic), masked mean-squared error, Adam;
+//    deterministic), masked mean-squared error or energy-norm loss, Adam;
 //  * inference: the 32 -> 32 layers on the tensor cores (mma.sync m16n8k16 BF16, FP32
 //    accumulate) from a shared-memory halo tile, first and last layer on the CUDA cores;
-//  * the flexible CG of Notay (FCG(1)) in FP64 that applies the network as preconditioner.
+//  * energy-norm training loss: for each crop, e^T A e / t^T A t with A the crop's stiffness
+//    (unit square Quad4 elements with the crop's moduli) and e the masked output error;
+//  * a flexible CG in FP64 (Notay's truncated FCG with two search directions per iteration, the
+//    Jacobi-preconditioned residual and the network's correction, each A-orthogonalised against
+//    a ring of earlier directions), replayed as a CUDA graph.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
+#include <numeric>
 
 #include "common.cuh"
 
@@ -204,6 +210,120 @@ __global__ void k_mse(const float* __restrict__ Y, const float* __restrict__ T, 
     if (threadIdx.x == 0) lpart[blockIdx.x] = sh[0];
 }
 
+// Stiffness of the unit square Quad4 element (2x2 Gauss, plane strain) split by modulus:
+// Ke = K * c_ke[0] + G * c_ke[1], rows / columns a*2+i (local node a, component i).
+__constant__ float c_ke[2][64];
+constexpr int kEnergyBlocks = 64; // fixed blocks per crop of the energy reduction
+
+// Energy-norm loss of the crops (sum over the crops of e^T A e over the sum of t'^T A t': a
+// ratio of sums, so a crop with a near-zero target cannot blow up the gradient), first pass. For node (b, y, x) of a crop, with
+// e = M F (y - t) and t' = M F t (M: crop interior, F: free dofs), sums over the <= 4 elements
+// around the node the element forces (Ke e) and (Ke t') at this node; writes the unscaled
+// gradient 2 M F (A e) and per-block partials of e.(A e) and t'.(A t').
+__global__ void __launch_bounds__(256)
+k_crop_energy(const float* __restrict__ Y, const float* __restrict__ T, const float* __restrict__ E,
+              const float* __restrict__ F, int B, int S, int m, float* __restrict__ dY,
+              float* __restrict__ part)
+{
+    __shared__ float sh[2][8];
+    int b = blockIdx.y;
+    int64_t nn = static_cast<int64_t>(S) * S;
+    const float* Yb = Y + b * nn * 2;
+    const float* Tb = T + b * nn * 2;
+    const float* Fb = F + b * nn * 2;
+    const float* Eb = E + static_cast<int64_t>(b) * (S - 1) * (S - 1) * 2;
+    float num = 0.0f, den = 0.0f;
+    for (int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; p < nn;
+         p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int y = static_cast<int>(p / S), x = static_cast<int>(p % S);
+        float ae[2] = {0.0f, 0.0f}, at[2] = {0.0f, 0.0f};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            // element (ey, ex) around the node, in which the node is local node a
+            int ey = y - (k >= 2 ? 1 : 0), ex = x - ((k == 1 || k == 2) ? 1 : 0);
+            int a = k == 0 ? 0 : (k == 1 ? 1 : (k == 2 ? 2 : 3));
+            if (ey < 0 || ex < 0 || ey >= S - 1 || ex >= S - 1) continue;
+            float Km = Eb[(static_cast<int64_t>(ey) * (S - 1) + ex) * 2];
+            float Gm = Eb[(static_cast<int64_t>(ey) * (S - 1) + ex) * 2 + 1];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                int ny = ey + (c >= 2 ? 1 : 0), nx = ex + ((c == 1 || c == 2) ? 1 : 0);
+                bool in = ny >= m && ny < S - m && nx >= m && nx < S - m;
+                int64_t q = (static_cast<int64_t>(ny) * S + nx) * 2;
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    float f = in ? Fb[q + j] : 0.0f;
+                    float ev = f * (Yb[q + j] - Tb[q + j]);
+                    float tv = f * Tb[q + j];
+#pragma unroll
+                    for (int i = 0; i < 2; ++i) {
+                        float kk = Km * c_ke[0][(a * 2 + i) * 8 + c * 2 + j] +
+                                   Gm * c_ke[1][(a * 2 + i) * 8 + c * 2 + j];
+                        ae[i] = fmaf(kk, ev, ae[i]);
+                        at[i] = fmaf(kk, tv, at[i]);
+                    }
+                }
+            }
+        }
+        bool in = y >= m && y < S - m && x >= m && x < S - m;
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            float f = in ? Fb[p * 2 + i] : 0.0f;
+            float ev = f * (Yb[p * 2 + i] - Tb[p * 2 + i]);
+            float tv = f * Tb[p * 2 + i];
+            num = fmaf(ev, ae[i], num);
+            den = fmaf(tv, at[i], den);
+            dY[(b * nn + p) * 2 + i] = 2.0f * f * ae[i];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        num += __shfl_down_sync(0xffffffffu, num, o);
+        den += __shfl_down_sync(0xffffffffu, den, o);
+    }
+    int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    if (lane == 0) {
+        sh[0][wi] = num;
+        sh[1][wi] = den;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float sn = 0.0f, sd = 0.0f;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            sn += sh[0][w];
+            sd += sh[1][w];
+        }
+        part[(static_cast<int64_t>(b) * gridDim.x + blockIdx.x) * 2] = sn;
+        part[(static_cast<int64_t>(b) * gridDim.x + blockIdx.x) * 2 + 1] = sd;
+    }
+}
+
+// loss = sum_b num_b / sum_b den_b (block, then crop order); scale = 1 / sum_b den_b
+__global__ void k_energy_reduce(const float* __restrict__ part, int B, int nblk,
+                                float* __restrict__ scale, float* __restrict__ loss)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    float sn = 0.0f, sd = 0.0f;
+    for (int b = 0; b < B; ++b) {
+        float cn = 0.0f, cd = 0.0f;
+        for (int k = 0; k < nblk; ++k) {
+            cn += part[(static_cast<int64_t>(b) * nblk + k) * 2];
+            cd += part[(static_cast<int64_t>(b) * nblk + k) * 2 + 1];
+        }
+        sn += cn;
+        sd += cd;
+    }
+    bool ok = sd > 0.0f;
+    *scale = ok ? 1.0f / sd : 0.0f;
+    *loss = ok ? sn / sd : 0.0f;
+}
+
+__global__ void k_scale_grad(const float* __restrict__ scale, int64_t n, float* __restrict__ dY)
+{
+    float f = *scale;
+    GF_FOR(i, n) dY[i] *= f;
+}
+
 // Adam on the FP32 master parameters; the BF16 copy feeds the convolutions.
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, int n, float lr, float b1, float b2, float eps,
@@ -220,10 +340,14 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
     pb[i] = __float2bfloat16_rn(w);
 }
 
-// crops [B, S, S, 4] (scaled residual + material) and targets [B, S, S, 2] from the stored pairs
+// crops [B, S, S, 4] (scaled residual + material) and targets [B, S, S, 2] from the stored
+// pairs; optionally the crops' element moduli E [B, S-1, S-1, 2] and free-dof mask F [B, S, S, 2]
+// (0 outside the mesh)
 __global__ void k_gather_crops(const float* __restrict__ R, const float* __restrict__ Tg,
-                               const float* __restrict__ mat, const int* __restrict__ pos, int B,
-                               int S, int H, int Wd, float* __restrict__ X, float* __restrict__ T)
+                               const float* __restrict__ mat, const float* __restrict__ ekg,
+                               const float* __restrict__ freem, const int* __restrict__ pos, int B,
+                               int S, int H, int Wd, float* __restrict__ X, float* __restrict__ T,
+                               float* __restrict__ E, float* __restrict__ F)
 {
     int64_t n = static_cast<int64_t>(B) * S * S;
     GF_FOR(i, n)
@@ -240,6 +364,17 @@ __global__ void k_gather_crops(const float* __restrict__ R, const float* __restr
         X[i * 4 + 3] = in ? mat[g * 2 + 1] : 0.0f;
         T[i * 2 + 0] = in ? Tg[q * 2 + 0] : 0.0f;
         T[i * 2 + 1] = in ? Tg[q * 2 + 1] : 0.0f;
+        if (F) {
+            F[i * 2 + 0] = in ? freem[g * 2 + 0] : 0.0f;
+            F[i * 2 + 1] = in ? freem[g * 2 + 1] : 0.0f;
+        }
+        if (E && y < S - 1 && x < S - 1) {
+            bool ein = yy >= 0 && yy < H - 1 && xx >= 0 && xx < Wd - 1;
+            int64_t e = static_cast<int64_t>(yy) * (Wd - 1) + xx;
+            int64_t o = (static_cast<int64_t>(b) * (S - 1) + y) * (S - 1) + x;
+            E[o * 2 + 0] = ein ? ekg[e * 2 + 0] : 0.0f;
+            E[o * 2 + 1] = ein ? ekg[e * 2 + 1] : 0.0f;
+        }
     }
 }
 
@@ -404,10 +539,10 @@ inline unsigned pix_grid(int64_t npix)
 }
 
 struct TrainWs {
-    float *a1, *a2, *a3, *y, *g3, *g2, *g1, *partial, *lpart;
+    float *a1, *a2, *a3, *y, *g3, *g2, *g1, *partial, *lpart, *epart, *escale;
 };
 
-inline TrainWs carve_train(void* ws, int64_t npix)
+inline TrainWs carve_train(void* ws, int64_t B, int64_t npix)
 {
     char* c = static_cast<char*>(ws);
     TrainWs w;
@@ -423,13 +558,75 @@ inline TrainWs carve_train(void* ws, int64_t npix)
     w.partial = reinterpret_cast<float*>(c);
     c += a256(int64_t(kWgtBlocks) * (9 * 32 * 32 + 32) * 4);
     w.lpart = reinterpret_cast<float*>(c);
+    c += a256(1024 * 4 + 16);
+    w.epart = reinterpret_cast<float*>(c);
+    c += a256(int64_t(B) * kEnergyBlocks * 2 * 4);
+    w.escale = reinterpret_cast<float*>(c);
     return w;
 }
 
-inline int64_t train_bytes(int64_t npix)
+inline int64_t loss_bytes(int64_t B)
+{
+    return a256(1024 * 4 + 16) + a256(B * kEnergyBlocks * 2 * 4) + a256(B * 4);
+}
+
+inline int64_t train_bytes(int64_t B, int64_t npix)
 {
     return 5 * a256(npix * 32 * 4) + 2 * a256(npix * 2 * 4) +
-           a256(int64_t(kWgtBlocks) * (9 * 32 * 32 + 32) * 4) + a256(1024 * 4 + 16);
+           a256(int64_t(kWgtBlocks) * (9 * 32 * 32 + 32) * 4) + loss_bytes(B);
+}
+
+// Element stiffness of the unit square (2x2 Gauss, plane strain) per unit K and per unit G.
+// Local nodes (0,0), (1,0), (1,1), (0,1); x = (1 + xi) / 2; rows / columns a*2+i.
+inline void unit_square_ke(double (&ke)[2][8][8])
+{
+    const double xa[4] = {-1, 1, 1, -1}, ya[4] = {-1, -1, 1, 1};
+    const double g = 1.0 / std::sqrt(3.0);
+    for (int m = 0; m < 2; ++m)
+        for (int r = 0; r < 8; ++r)
+            for (int c = 0; c < 8; ++c) ke[m][r][c] = 0.0;
+    for (int qy = 0; qy < 2; ++qy)
+        for (int qx = 0; qx < 2; ++qx) {
+            double xi = qx ? g : -g, eta = qy ? g : -g;
+            double dN[4][2];
+            for (int a = 0; a < 4; ++a) {
+                dN[a][0] = 2.0 * 0.25 * xa[a] * (1.0 + eta * ya[a]); // d/dx = 2 d/dxi
+                dN[a][1] = 2.0 * 0.25 * ya[a] * (1.0 + xi * xa[a]);
+            }
+            for (int a = 0; a < 4; ++a)
+                for (int i = 0; i < 2; ++i)
+                    for (int b = 0; b < 4; ++b)
+                        for (int k = 0; k < 2; ++k)
+                            for (int j = 0; j < 2; ++j)
+                                for (int l = 0; l < 2; ++l) {
+                                    double dij = i == j, dkl = k == l, dik = i == k, djl = j == l,
+                                           dil = i == l, djk = j == k;
+                                    double cK = dij * dkl;
+                                    double cG = dik * djl + dil * djk - 2.0 / 3.0 * dij * dkl;
+                                    double w = 0.25 * dN[a][j] * dN[b][l]; // weight x det(J)
+                                    ke[0][a * 2 + i][b * 2 + k] += w * cK;
+                                    ke[1][a * 2 + i][b * 2 + k] += w * cG;
+                                }
+        }
+}
+
+// c_ke, uploaded once per device
+inline int upload_ke()
+{
+    static bool done[64] = {};
+    int dev = 0;
+    GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+    if (dev < 0 || dev >= 64) return fail(GFGPU_ERR_ARG, "upload_ke: device index");
+    if (done[dev]) return GFGPU_OK;
+    double ke[2][8][8];
+    unit_square_ke(ke);
+    float h[2][64];
+    for (int m = 0; m < 2; ++m)
+        for (int r = 0; r < 8; ++r)
+            for (int c = 0; c < 8; ++c) h[m][r * 8 + c] = static_cast<float>(ke[m][r][c]);
+    GF_TRY(check_cuda(cudaMemcpyToSymbol(c_ke, h, sizeof(h)), "cudaMemcpyToSymbol"));
+    done[dev] = true;
+    return GFGPU_OK;
 }
 
 inline const __nv_bfloat16* wb(const void* p, int l)
@@ -462,7 +659,14 @@ inline void weight_grad(const float* X, const float* dY, int dil, int B, int H, 
 
 // ---------------------------------------------------------------- FCG kernels
 
-enum { F_RP = 0, F_PQ, F_ZQ, F_RR, F_BB, F_ALPHA, F_BETA, F_COUNT };
+// Ring of search directions of the flexible CG: slot j holds P_j, Q_j = (A P_j)_u.
+constexpr int kMaxSlots = 20;
+struct SlotList {
+    int n;
+    int s[kMaxSlots];
+};
+// device scalars: r.r, b.b, r.P (per new direction), P.Q (per slot), z.Q (per basis entry)
+enum { F_RR = 0, F_BB, F_RP0, F_RP1, F_PQ, F_DOT = F_PQ + kMaxSlots, F_COUNT = F_DOT + kMaxSlots };
 
 __device__ __forceinline__ double bsum(double v, double* sh)
 {
@@ -479,18 +683,6 @@ __device__ __forceinline__ double bsum(double v, double* sh)
     }
     __syncthreads();
     return r;
-}
-
-__global__ void k_fred(const double* __restrict__ partial, int nparts, double* __restrict__ sc, int slot0)
-{
-    __shared__ double sh[32];
-    for (int p = 0; p < nparts; ++p) {
-        double v = 0.0;
-        for (int i = threadIdx.x; i < kRed; i += blockDim.x) v += partial[p * kRed + i];
-        double s = bsum(v, sh);
-        if (threadIdx.x == 0) sc[slot0 + p] = s;
-        __syncthreads();
-    }
 }
 
 __global__ void k_finv(const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ diag,
@@ -557,83 +749,133 @@ k_fgather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr, con
     }
 }
 
-__global__ void k_falpha(double* sc)
-{
-    if (threadIdx.x == 0) sc[F_ALPHA] = sc[F_RP] / sc[F_PQ];
-}
-
-// x += alpha p, r -= alpha q; partial r.r
-__global__ void __launch_bounds__(256)
-k_fupdate(const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ p,
-          const double* __restrict__ q, int64_t n, const double* __restrict__ sc, double* __restrict__ x,
-          double* __restrict__ r, double* __restrict__ partial)
+// sc[dst.s[k]] = sum of partial row k (fixed order)
+__global__ void k_fredv(const double* __restrict__ partial, SlotList dst, double* __restrict__ sc)
 {
     __shared__ double sh[32];
-    double alpha = sc[F_ALPHA];
+    for (int p = 0; p < dst.n; ++p) {
+        double v = 0.0;
+        for (int i = threadIdx.x; i < kRed; i += blockDim.x) v += partial[p * kRed + i];
+        double t = bsum(v, sh);
+        if (threadIdx.x == 0) sc[dst.s[p]] = t;
+        __syncthreads();
+    }
+}
+
+// partial dots z.Q_j for the basis slots (z = minv * r when zin is null)
+__global__ void __launch_bounds__(256)
+k_mdot(const double* __restrict__ zin, const double* __restrict__ minv, const double* __restrict__ r,
+       const double* __restrict__ Q, int64_t ld, SlotList L, int64_t n, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double acc[kMaxSlots];
+#pragma unroll
+    for (int j = 0; j < kMaxSlots; ++j) acc[j] = 0.0;
+    GF_FOR(t, n)
+    {
+        double z = zin ? zin[t] : minv[t] * r[t];
+#pragma unroll
+        for (int j = 0; j < kMaxSlots; ++j)
+            if (j < L.n) acc[j] = fma(z, Q[L.s[j] * ld + t], acc[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < kMaxSlots; ++j) {
+        if (j < L.n) {
+            double v = bsum(acc[j], sh);
+            if (threadIdx.x == 0) partial[j * kRed + blockIdx.x] = v;
+        }
+    }
+}
+
+// P_new = z - sum_j (z.Q_j / P_j.Q_j) P_j over the basis slots (A-orthogonalisation)
+__global__ void k_mcombine(const double* __restrict__ zin, const double* __restrict__ minv,
+                           const double* __restrict__ r, const double* __restrict__ sc, double* P,
+                           int64_t ld, SlotList L, int snew, int64_t n)
+{
+    double c[kMaxSlots];
+#pragma unroll
+    for (int j = 0; j < kMaxSlots; ++j) {
+        double pq = j < L.n ? sc[F_PQ + L.s[j]] : 0.0;
+        double cj = (j < L.n && pq > 0.0 && isfinite(pq)) ? sc[F_DOT + j] / pq : 0.0;
+        c[j] = isfinite(cj) ? cj : 0.0; // a degenerate or non-finite direction is skipped
+    }
+    double* out = P + snew * ld;
+    GF_FOR(t, n)
+    {
+        double v = zin ? zin[t] : minv[t] * r[t];
+#pragma unroll
+        for (int j = 0; j < kMaxSlots; ++j)
+            if (j < L.n && c[j] != 0.0) v = fma(-c[j], P[L.s[j] * ld + t], v);
+        out[t] = v;
+    }
+}
+
+// x += sum_d alpha_d P_d, r -= sum_d alpha_d Q_d with alpha_d = r.P_d / P_d.Q_d (the new
+// directions are mutually A-orthogonal, so every alpha uses the same r); partial r.r
+__global__ void __launch_bounds__(256)
+k_mupdate(const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ P,
+          const double* __restrict__ Q, int64_t ld, int s0, int s1, int ndir,
+          const double* __restrict__ sc, int64_t n, double* __restrict__ x, double* __restrict__ r,
+          double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double pq0 = sc[F_PQ + s0], pq1 = ndir > 1 ? sc[F_PQ + s1] : 0.0;
+    double a0 = pq0 > 0.0 && isfinite(pq0) ? sc[F_RP0] / pq0 : 0.0;
+    double a1 = pq1 > 0.0 && isfinite(pq1) ? sc[F_RP1] / pq1 : 0.0;
+    if (!isfinite(a0)) a0 = 0.0; // a degenerate or non-finite direction takes no step
+    if (!isfinite(a1)) a1 = 0.0;
+    const double* P0 = P + s0 * ld;
+    const double* Q0 = Q + s0 * ld;
+    const double* P1 = P + s1 * ld;
+    const double* Q1 = Q + s1 * ld;
     double rr = 0.0;
     GF_FOR(t, n)
     {
         if (part[t] < nnu) {
-            x[t] = fma(alpha, p[t], x[t]);
-            double rv = fma(-alpha, q[t], r[t]);
+            double xv = x[t], rv = r[t];
+            if (a0 != 0.0) {
+                xv = fma(a0, P0[t], xv);
+                rv = fma(-a0, Q0[t], rv);
+            }
+            if (a1 != 0.0) {
+                xv = fma(a1, P1[t], xv);
+                rv = fma(-a1, Q1[t], rv);
+            }
+            x[t] = xv;
             r[t] = rv;
             rr = fma(rv, rv, rr);
         }
     }
-    double s = bsum(rr, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = s;
-}
-
-__global__ void k_fjacobi(const double* __restrict__ minv, const double* __restrict__ r, int64_t n,
-                          double* __restrict__ z)
-{
-    GF_FOR(t, n) z[t] = minv[t] * r[t];
-}
-
-// partial z.q
-__global__ void __launch_bounds__(256)
-k_fdot(const double* __restrict__ a, const double* __restrict__ b, int64_t n, double* __restrict__ partial)
-{
-    __shared__ double sh[32];
-    double acc = 0.0;
-    GF_FOR(t, n) acc = fma(a[t], b[t], acc);
-    double s = bsum(acc, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = s;
-}
-
-__global__ void k_fbeta(double* sc)
-{
-    if (threadIdx.x == 0) sc[F_BETA] = sc[F_ZQ] / sc[F_PQ];
-}
-
-// p = z - beta p
-__global__ void k_fdir(const double* __restrict__ z, const double* __restrict__ sc, int64_t n,
-                       double* __restrict__ p)
-{
-    double beta = sc[F_BETA];
-    GF_FOR(t, n) p[t] = fma(-beta, p[t], z[t]);
+    double v = bsum(rr, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v;
 }
 
 struct FcgWs {
-    double *fe, *p, *r, *z, *q, *minv, *partial, *sc;
+    double *fe, *r, *z, *minv, *P, *Q, *partial, *sc;
+    int64_t ld;
     float *x0, *y;
     __nv_bfloat16 *a1, *a2, *a3;
 };
 
-inline FcgWs carve_fcg(const gfgpu_verlet_desc* d, int64_t hw, void* ws)
+inline FcgWs carve_fcg(const gfgpu_verlet_desc* d, int64_t hw, int nslots, void* ws)
 {
     char* c = static_cast<char*>(ws);
     int64_t n = d->nnode * d->ndim;
     FcgWs w;
+    w.ld = a256(n * 8) / 8;
     w.fe = reinterpret_cast<double*>(c);
     c += a256(d->nelem * d->nne * d->ndim * 8);
-    double** v[] = {&w.p, &w.r, &w.z, &w.q, &w.minv};
+    double** v[] = {&w.r, &w.z, &w.minv};
     for (auto b : v) {
         *b = reinterpret_cast<double*>(c);
         c += a256(n * 8);
     }
+    w.P = reinterpret_cast<double*>(c);
+    c += nslots * w.ld * 8;
+    w.Q = reinterpret_cast<double*>(c);
+    c += nslots * w.ld * 8;
     w.partial = reinterpret_cast<double*>(c);
-    c += a256(2 * kRed * 8);
+    c += a256(int64_t(kMaxSlots) * kRed * 8);
     w.sc = reinterpret_cast<double*>(c);
     c += a256(F_COUNT * 8);
     w.x0 = reinterpret_cast<float*>(c);
@@ -648,11 +890,12 @@ inline FcgWs carve_fcg(const gfgpu_verlet_desc* d, int64_t hw, void* ws)
     return w;
 }
 
-inline int64_t fcg_bytes(const gfgpu_verlet_desc* d, int64_t hw)
+inline int64_t fcg_bytes(const gfgpu_verlet_desc* d, int64_t hw, int nslots)
 {
     int64_t n = d->nnode * d->ndim;
-    return a256(d->nelem * d->nne * d->ndim * 8) + 5 * a256(n * 8) + a256(2 * kRed * 8) +
-           a256(F_COUNT * 8) + a256(hw * 16) + a256(hw * 8) + 3 * a256(hw * 64);
+    return a256(d->nelem * d->nne * d->ndim * 8) + (3 + 2 * int64_t(nslots)) * a256(n * 8) +
+           a256(int64_t(kMaxSlots) * kRed * 8) + a256(F_COUNT * 8) + a256(hw * 16) + a256(hw * 8) +
+           3 * a256(hw * 64);
 }
 
 // z = network(r) on the nodal grid, with the tensor-core middle layers
@@ -692,6 +935,17 @@ inline int prepare_mma(cudaStream_t)
 
 extern "C" {
 
+int gfgpu_nn_unit_element_stiffness(double* out)
+{
+    GF_REQUIRE(out, "bad argument");
+    double ke[2][8][8];
+    unit_square_ke(ke);
+    for (int m = 0; m < 2; ++m)
+        for (int r = 0; r < 8; ++r)
+            for (int c = 0; c < 8; ++c) out[(m * 8 + r) * 8 + c] = ke[m][r][c];
+    return GFGPU_OK;
+}
+
 int32_t gfgpu_nn_param_count(void)
 {
     return kParams;
@@ -705,7 +959,7 @@ int32_t gfgpu_nn_param_offset(int32_t layer, int32_t bias)
 
 int64_t gfgpu_nn_train_workspace_bytes(int32_t B, int32_t H, int32_t W)
 {
-    return train_bytes(int64_t(B) * H * W);
+    return train_bytes(B, int64_t(B) * H * W);
 }
 
 int gfgpu_nn_forward(const void* weights_bf16, const float* params_f32, const float* X, int32_t B,
@@ -713,7 +967,7 @@ int gfgpu_nn_forward(const void* weights_bf16, const float* params_f32, const fl
 {
     GF_REQUIRE(weights_bf16 && params_f32 && X && Y && workspace && B > 0 && H > 0 && W > 0,
                "bad argument");
-    TrainWs w = carve_train(workspace, int64_t(B) * H * W);
+    TrainWs w = carve_train(workspace, B, int64_t(B) * H * W);
     forward_f32(weights_bf16, params_f32, X, B, H, W, w, S(stream));
     GF_TRY(check_cuda(cudaMemcpyAsync(Y, w.y, int64_t(B) * H * W * 2 * 4, cudaMemcpyDeviceToDevice,
                                       S(stream)),
@@ -722,17 +976,26 @@ int gfgpu_nn_forward(const void* weights_bf16, const float* params_f32, const fl
 }
 
 int gfgpu_nn_train_step(const void* weights_bf16, const float* params_f32, const float* X,
-                        const float* T, int32_t B, int32_t S_, int32_t margin, float* grads,
-                        float* loss, void* workspace, gfgpu_stream_t stream)
+                        const float* T, const float* E, const float* F, int32_t B, int32_t S_,
+                        int32_t margin, float* grads, float* loss, void* workspace,
+                        gfgpu_stream_t stream)
 {
     GF_REQUIRE(weights_bf16 && params_f32 && X && T && grads && loss && workspace, "bad argument");
-    GF_REQUIRE(B > 0 && S_ > 2 * margin && margin >= 0, "bad crop size");
+    GF_REQUIRE(B > 0 && B <= 1024 && S_ > 2 * margin && margin >= 0, "bad crop size");
+    GF_REQUIRE((E == nullptr) == (F == nullptr), "E and F are given together");
     cudaStream_t s = S(stream);
     int64_t npix = int64_t(B) * S_ * S_;
-    TrainWs w = carve_train(workspace, npix);
+    TrainWs w = carve_train(workspace, B, npix);
     forward_f32(weights_bf16, params_f32, X, B, S_, S_, w, s);
-    k_mse<<<1024, 256, 0, s>>>(w.y, T, B, S_, margin, 2, w.g3, w.lpart);
-    k_sum_partials<<<1, 32, 0, s>>>(w.lpart, 1024, 1, loss);
+    if (E) {
+        GF_TRY(upload_ke());
+        k_crop_energy<<<dim3(kEnergyBlocks, B), 256, 0, s>>>(w.y, T, E, F, B, S_, margin, w.g3, w.epart);
+        k_energy_reduce<<<1, 32, 0, s>>>(w.epart, B, kEnergyBlocks, w.escale, loss);
+        k_scale_grad<<<grid_for(npix * 2), kBlock, 0, s>>>(w.escale, npix * 2, w.g3);
+    } else {
+        k_mse<<<1024, 256, 0, s>>>(w.y, T, B, S_, margin, 2, w.g3, w.lpart);
+        k_sum_partials<<<1, 32, 0, s>>>(w.lpart, 1024, 1, loss);
+    }
     // layer 4 (32 -> 2)
     weight_grad<32, 2>(w.a3, w.g3, dil_of(3), B, S_, S_, w.partial, grads + w_off(3), s);
     unsigned g = pix_grid(npix);
@@ -760,19 +1023,24 @@ int gfgpu_nn_adam(float* params, const float* grads, float* m, float* v, int32_t
     return check_launch("nn_adam");
 }
 
-int gfgpu_nn_gather_crops(const float* R, const float* T, const float* material, const int32_t* pos,
+int gfgpu_nn_gather_crops(const float* R, const float* T, const float* material,
+                          const float* elem_kg, const float* free_mask, const int32_t* pos,
                           int32_t B, int32_t S_, int32_t H, int32_t W, float* X, float* Tc,
-                          gfgpu_stream_t stream)
+                          float* Ec, float* Fc, gfgpu_stream_t stream)
 {
-    GF_REQUIRE(R && T && material && pos && X && Tc && B > 0 && S_ > 0, "bad argument");
-    k_gather_crops<<<grid_for(int64_t(B) * S_ * S_), kBlock, 0, S(stream)>>>(R, T, material, pos, B, S_,
-                                                                           H, W, X, Tc);
+    GF_REQUIRE(R && T && material && pos && X && Tc && B > 0 && S_ > 1 && H > 1 && W > 1,
+               "bad argument");
+    GF_REQUIRE((!Ec || elem_kg) && (!Fc || free_mask), "Ec needs elem_kg and Fc needs free_mask");
+    k_gather_crops<<<grid_for(int64_t(B) * S_ * S_), kBlock, 0, S(stream)>>>(
+        R, T, material, elem_kg, free_mask, pos, B, S_, H, W, X, Tc, Ec, Fc);
     return check_launch("nn_gather_crops");
 }
 
-int64_t gfgpu_fcg_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W)
+int64_t gfgpu_fcg_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W, int32_t nkeep,
+                                  int32_t ndir)
 {
-    return d ? fcg_bytes(d, int64_t(H) * W) : 0;
+    if (!d || nkeep < 1 || ndir < 1 || ndir > 2 || nkeep + ndir > kMaxSlots) return 0;
+    return fcg_bytes(d, int64_t(H) * W, nkeep + ndir);
 }
 
 int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* workspace,
@@ -801,85 +1069,164 @@ int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* wor
 }
 
 int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
-                    double* x, double tol, int64_t maxiter, int32_t check_every, void* workspace,
-                    gfgpu_stream_t stream, int64_t* iters, double* relres)
+                    double* x, double tol, int64_t maxiter, int32_t nkeep, int32_t check_every,
+                    void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres)
 {
     GF_REQUIRE(d && diag && x && workspace && iters && relres && tol > 0.0 && maxiter >= 0,
                "bad argument");
     GF_REQUIRE(!nn || (d->nne == 4 && d->ndim == 2 && int64_t(nn->H) * nn->W == d->nnode &&
                        nn->weights_bf16 && nn->params_f32 && nn->material),
                "the network preconditioner needs a Quad4 Regular grid of H x W nodes");
+    const int ndir = nn ? 2 : 1;
+    GF_REQUIRE(nkeep >= 1 && nkeep + ndir <= kMaxSlots, "nkeep out of range");
     if (check_every < 1) check_every = 1;
     cudaStream_t s = S(stream);
     if (nn) GF_TRY(prepare_mma(s));
+    const int nslots = nkeep + ndir;
     int64_t hw = nn ? int64_t(nn->H) * nn->W : 0;
-    FcgWs w = carve_fcg(d, hw, workspace);
-    int64_t n = d->nnode * d->ndim;
-    double nfree = static_cast<double>(d->nnu);
+    FcgWs w = carve_fcg(d, hw, nslots, workspace);
+    const int64_t n = d->nnode * d->ndim;
+    const double nfree = static_cast<double>(d->nnu);
     const unsigned gb = kRed;
-    auto precond = [&]() -> int {
-        if (nn) return nn_apply(nn, w.r, w.sc, F_RR, nfree, d->part, d->nnu, w, w.z, s);
-        k_fjacobi<<<grid_for(n), kBlock, 0, s>>>(w.minv, w.r, n, w.z);
-        return check_launch("jacobi");
-    };
-    auto read_sc = [&](double* h) -> int {
+    double h[F_COUNT];
+    auto read_sc = [&]() -> int {
         GF_TRY(check_cuda(cudaMemcpyAsync(h, w.sc, F_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s),
                           "cudaMemcpyAsync"));
         return check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     };
-    double h[F_COUNT];
+    auto one = [](int slot) {
+        SlotList l{};
+        l.n = 1;
+        l.s[0] = slot;
+        return l;
+    };
+
+    // One iteration, direction counter `c0` on entry (slot of direction k: k mod nslots). New
+    // direction d is A-orthogonalised against the last nkeep directions of earlier iterations
+    // and the earlier directions of this iteration.
+    auto iteration = [&](int64_t c0, cudaStream_t st) -> int {
+        for (int dd = 0; dd < ndir; ++dd) {
+            int64_t cur = c0 + dd;
+            int snew = static_cast<int>(cur % nslots);
+            SlotList L{};
+            for (int64_t k = std::max<int64_t>(0, c0 - nkeep); k < cur; ++k)
+                L.s[L.n++] = static_cast<int>(k % nslots);
+            const double* zin = nullptr;
+            if (dd == 1) {
+                GF_TRY(nn_apply(nn, w.r, w.sc, F_RR, nfree, d->part, d->nnu, w, w.z, st));
+                zin = w.z;
+            }
+            if (L.n > 0) {
+                k_mdot<<<gb, 256, 0, st>>>(zin, w.minv, w.r, w.Q, w.ld, L, n, w.partial);
+                SlotList dst{};
+                dst.n = L.n;
+                for (int j = 0; j < L.n; ++j) dst.s[j] = F_DOT + j;
+                k_fredv<<<1, 1024, 0, st>>>(w.partial, dst, w.sc);
+            }
+            k_mcombine<<<grid_for(n), kBlock, 0, st>>>(zin, w.minv, w.r, w.sc, w.P, w.ld, L, snew, n);
+            double* Pn = w.P + snew * w.ld;
+            double* Qn = w.Q + snew * w.ld;
+            GF_TRY(gfgpu_internal_element_forces(d, Pn, w.fe, st));
+            k_fgather<<<gb, 256, 0, st>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, Pn,
+                                          w.r, n, Qn, w.partial);
+            SlotList dst{};
+            dst.n = 2;
+            dst.s[0] = F_PQ + snew;
+            dst.s[1] = dd == 0 ? F_RP0 : F_RP1;
+            k_fredv<<<1, 1024, 0, st>>>(w.partial, dst, w.sc);
+        }
+        k_mupdate<<<gb, 256, 0, st>>>(d->part, d->nnu, w.P, w.Q, w.ld, static_cast<int>(c0 % nslots),
+                                      static_cast<int>((c0 + 1) % nslots), ndir, w.sc, n, x, w.r,
+                                      w.partial);
+        k_fredv<<<1, 1024, 0, st>>>(w.partial, one(F_RR), w.sc);
+        return check_launch("fcg iteration");
+    };
+
     k_finv<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, diag, n, w.minv);
-    // ||b||, b = -(A x_p)_u
-    k_fkeep<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.p);
-    GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
+    // ||b||, b = -(A x_p)_u (P slot 0 as scratch)
+    k_fkeep<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.P);
+    GF_TRY(gfgpu_internal_element_forces(d, w.P, w.fe, s));
     k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, nullptr, n, w.z,
                               w.partial);
-    k_fred<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, F_BB);
-    // r = -(A x)_u, z = M(r), p = z
+    k_fredv<<<1, 1024, 0, s>>>(w.partial, one(F_BB), w.sc);
+    // r = -(A x)_u
     GF_TRY(gfgpu_internal_element_forces(d, x, w.fe, s));
     k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, nullptr, n, w.r,
                               w.partial);
-    k_fred<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, F_RR);
-    GF_TRY(precond());
-    GF_TRY(check_cuda(cudaMemcpyAsync(w.p, w.z, n * 8, cudaMemcpyDeviceToDevice, s), "copy"));
-    GF_TRY(read_sc(h));
+    k_fredv<<<1, 1024, 0, s>>>(w.partial, one(F_RR), w.sc);
+    GF_TRY(read_sc());
     double bnorm = std::sqrt(h[F_BB]);
     if (bnorm == 0.0) bnorm = 1.0;
     double rel = std::sqrt(h[F_RR]) / bnorm;
-    int64_t it = 0;
+
+    // Warm-up iterations run one by one until the ring is full and aligned (direction counter a
+    // multiple of nslots); from there `chunk` iterations repeat the same slot pattern and replay
+    // as one CUDA graph.
+    int64_t it = 0, c = 0;
+    const int64_t period = nslots / std::gcd(nslots, ndir); // iterations per ring turn
+    const int64_t chunk = period * ((check_every + period - 1) / period);
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cs = nullptr;
+    int rc = GFGPU_OK;
+    auto cleanup = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (cs) cudaStreamDestroy(cs);
+    };
     while (rel > tol && it < maxiter) {
-        int64_t nb = std::min<int64_t>(check_every, maxiter - it);
-        for (int64_t k = 0; k < nb; ++k) {
-            GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
-            k_fgather<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, w.p, w.r,
-                                         n, w.q, w.partial);
-            k_fred<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, F_PQ);
-            k_fred<<<1, 1024, 0, s>>>(w.partial + kRed, 1, w.sc, F_RP);
-            k_falpha<<<1, 32, 0, s>>>(w.sc);
-            k_fupdate<<<gb, 256, 0, s>>>(d->part, d->nnu, w.p, w.q, n, w.sc, x, w.r, w.partial);
-            k_fred<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, F_RR);
-            GF_TRY(precond());
-            k_fdot<<<gb, 256, 0, s>>>(w.z, w.q, n, w.partial);
-            k_fred<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, F_ZQ);
-            k_fbeta<<<1, 32, 0, s>>>(w.sc);
-            k_fdir<<<grid_for(n), kBlock, 0, s>>>(w.z, w.sc, n, w.p);
+        bool steady = c >= int64_t(nkeep) + ndir && c % nslots == 0;
+        if (steady && !exec && maxiter - it >= chunk) {
+            rc = check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate");
+            if (rc != GFGPU_OK) break;
+            cudaGraph_t graph = nullptr;
+            rc = check_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
+            if (rc != GFGPU_OK) break;
+            int crc = GFGPU_OK;
+            for (int64_t k = 0; k < chunk && crc == GFGPU_OK; ++k) crc = iteration(c + k * ndir, cs);
+            cudaError_t e = cudaStreamEndCapture(cs, &graph);
+            if (crc != GFGPU_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                rc = crc;
+                break;
+            }
+            rc = check_cuda(e, "cudaStreamEndCapture");
+            if (rc == GFGPU_OK) rc = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+            if (graph) cudaGraphDestroy(graph);
+            if (rc != GFGPU_OK) break;
         }
-        it += nb;
-        GF_TRY(check_launch("fcg iteration"));
-        GF_TRY(read_sc(h));
+        if (exec && maxiter - it >= chunk) {
+            rc = check_cuda(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+            if (rc != GFGPU_OK) break;
+            it += chunk;
+            c += chunk * ndir;
+        }
+        else {
+            int64_t nb = exec ? maxiter - it : std::min<int64_t>(check_every, maxiter - it);
+            for (int64_t k = 0; k < nb && rc == GFGPU_OK; ++k) {
+                rc = iteration(c, s);
+                ++it;
+                c += ndir;
+                if (!exec && c >= int64_t(nkeep) + ndir && c % nslots == 0 && maxiter - it >= chunk) break;
+            }
+            if (rc != GFGPU_OK) break;
+        }
+        rc = read_sc();
+        if (rc != GFGPU_OK) break;
         if (!std::isfinite(h[F_RR])) {
+            cleanup();
             *iters = it;
             *relres = h[F_RR];
             return fail(GFGPU_ERR_NAN, "gfgpu_fcg_solve: non-finite residual");
         }
         rel = std::sqrt(h[F_RR]) / bnorm;
     }
+    cleanup();
+    GF_TRY(rc);
     // true residual -(A x)_u
     GF_TRY(gfgpu_internal_element_forces(d, x, w.fe, s));
     k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, nullptr, n, w.r,
                               w.partial);
-    k_fred<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, F_RR);
-    GF_TRY(read_sc(h));
+    k_fredv<<<1, 1024, 0, s>>>(w.partial, one(F_RR), w.sc);
+    GF_TRY(read_sc());
     *iters = it;
     *relres = std::sqrt(h[F_RR]) / bnorm;
     if (*relres > tol) return fail(GFGPU_ERR_DIVERGED, "gfgpu_fcg_solve: tolerance not reached");

@@ -1,14 +1,22 @@
 """Learned preconditioner for the matrix-free static solve of a Regular Quad4 mesh.
 
 The network (4 convolution layers 3x3, 32 channels, dilations 1, 2, 4, 1: a 17 x 17 node
-receptive field; BF16 weights, FP32 accumulation; kernels in csrc/learned.cu) is trained to
-reproduce the correction that `inner` iterations of restarted Jacobi-PCG make from a residual.
+receptive field; BF16 weights, FP32 accumulation; kernels in csrc/learned.cu) learns what
+`inner` iterations of Jacobi-PCG add to a residual beyond the Jacobi step itself: for a residual
+r the target is c - D^-1 r with c = PCG_inner(A, r) from zero (both scaled by the RMS of r).
 That map is local (its support grows by one node per iteration), which a local network can
-represent. The training pairs come from the plain solver itself: Jacobi-PCG runs on random loads,
-their residuals are snapshotted every few iterations, and each snapshot r is paired with the
-correction c = PCG_inner(A, r) (both scaled by the RMS of r). Inside the flexible CG of Notay
-(FCG(1), FP64 vectors and dot products) the trained network replaces those inner iterations in
-one application: z = RMS(r) * net(r / RMS(r)).
+represent. The training pairs come from the plain solver: Jacobi-PCG runs on random loads (body
+forces, boundary displacements, smooth fields, point loads) and its residuals are snapshotted.
+
+The loss is the energy norm of the output error, sum e^T A e / sum t^T A t over the crops of a
+batch, with A each crop's own stiffness: a network output error of high spatial frequency costs
+what it costs the solver, which a mean-squared error under-weights.
+
+The solve is a flexible CG in FP64 (gfgpu_fcg_solve) with two search directions per iteration,
+D^-1 r and the network's correction RMS(r) * net(r / RMS(r)), A-orthogonalised against a ring of
+earlier directions, with an exact line search along each. The Jacobi direction keeps the solve
+convergent whatever the network returns; plain Jacobi-PCG remains the fallback and the check of
+the answer (same FP64 true-residual test).
 """
 
 import ctypes as C
@@ -82,6 +90,12 @@ class LearnedPreconditioner:
             np.add.at(cnt, conn[:, k], 1.0)
         mat = np.stack([Kn / cnt / np.max(K), Gn / cnt / np.max(G)], axis=1).astype(np.float32)
         self.material = torch.as_tensor(mat, device=dev).contiguous()
+        # element moduli and free-dof mask for the energy-norm loss
+        self.elem_kg = torch.as_tensor(np.stack([np.asarray(K), np.asarray(G)], 1).astype(np.float32),
+                                       device=dev).contiguous()
+        self.free_f = self.free.float().contiguous()
+        self.minv = torch.where(self.free, 1.0 / self.static.diag.reshape(-1),
+                                torch.zeros((), dtype=torch.float64, device=dev))
         # parameters: He initialisation, zero biases, a small last layer
         self.P = int(_lib.lib().gfgpu_nn_param_count())
         rng = np.random.default_rng(seed)
@@ -118,8 +132,42 @@ class LearnedPreconditioner:
         return torch.empty(nb // 8 + 1, dtype=torch.float64, device=_dev.device())
 
     # ------------------------------------------------------------------ training pairs
+    def _load(self, kind, gen, x):
+        """A random load: the right-hand side (body force) and, in x, prescribed displacements.
+        kind 0: uniform body force; 1: random prescribed displacements (boundary-concentrated
+        load); 2: smooth random body force (Gaussian filter of white noise, random length);
+        3: a few point forces."""
+        dev = _dev.device()
+        n = self.H * self.W * 2
+        b = torch.zeros(n, dtype=torch.float64, device=dev)
+        x.zero_()
+        if kind == 0:
+            b = torch.rand(n, generator=gen, dtype=torch.float64, device=dev) * 2.0 - 1.0
+        elif kind == 1:
+            iip = torch.as_tensor(self.iip, device=dev).long()
+            v = torch.rand(iip.numel(), generator=gen, dtype=torch.float64, device=dev) * 2.0 - 1.0
+            if float(torch.rand(1, generator=gen, device=dev)) < 0.5:
+                v = torch.full_like(v, float(v[0]))
+            x[iip] = v
+        elif kind == 2:
+            f = torch.randn((2, self.H, self.W), generator=gen, dtype=torch.float64, device=dev)
+            L = 2.0 + 10.0 * float(torch.rand(1, generator=gen, device=dev))
+            ky = torch.fft.fftfreq(self.H, device=dev, dtype=torch.float64)[:, None]
+            kx = torch.fft.fftfreq(self.W, device=dev, dtype=torch.float64)[None, :]
+            filt = torch.exp(-(ky ** 2 + kx ** 2) * (L * math.pi) ** 2)
+            f = torch.fft.ifft2(torch.fft.fft2(f) * filt).real
+            b = f.permute(1, 2, 0).reshape(-1).contiguous()
+        else:
+            k = int(torch.randint(1, 8, (1,), generator=gen, device=dev))
+            idx = torch.randint(0, n, (k,), generator=gen, device=dev)
+            b[idx] = torch.randn(k, generator=gen, dtype=torch.float64, device=dev)
+        b[~self.free] = 0.0
+        return b.contiguous()
+
     def make_pairs(self, nloads=64, snaps=64, every=16, inner=8, seed=1):
-        """(residual, Jacobi-PCG correction) pairs from the plain solver on random loads."""
+        """(residual, correction) pairs from the plain Jacobi-PCG solver on random loads: for the
+        residual r after 0, every, 2 every, ... iterations the target is PCG_inner(A, r) - D^-1 r;
+        both are divided by the RMS of r over the free dofs."""
         n = self.H * self.W * 2
         npairs = nloads * snaps
         dev = _dev.device()
@@ -132,38 +180,46 @@ class LearnedPreconditioner:
         r_ptr = C.c_void_p(0)
         _lib.call("gfgpu_pcg_vector", self._desc(), ws1.data_ptr(), 0, C.addressof(r_ptr))
         r = torch.empty(n, dtype=torch.float64, device=dev)
+        x = torch.zeros(n, dtype=torch.float64, device=dev)
+        c = torch.zeros(n, dtype=torch.float64, device=dev)
         k = 0
-        for _ in range(nloads):
-            b = (torch.rand(n, generator=gen, dtype=torch.float64, device=dev) * 2.0 - 1.0)
-            b[~self.free] = 0.0
-            x = torch.zeros(n, dtype=torch.float64, device=dev)
+        for load in range(nloads):
+            b = self._load(load % 4, gen, x)
             _lib.call("gfgpu_pcg_begin", self._desc(), self.static.diag.data_ptr(), b.data_ptr(),
                       x.data_ptr(), ws1.data_ptr(), s)
-            for _ in range(snaps):
-                _lib.call("gfgpu_pcg_iterate", self._desc(), every, x.data_ptr(), ws1.data_ptr(), s)
+            for snap in range(snaps):
+                if snap:
+                    _lib.call("gfgpu_pcg_iterate", self._desc(), every, x.data_ptr(), ws1.data_ptr(), s)
                 _lib.call("gfgpu_memcpy_d2d", r.data_ptr(), r_ptr.value, n * 8)
                 sigma = torch.sqrt((r[self.free] ** 2).sum() / self.nfree)
-                c = torch.zeros(n, dtype=torch.float64, device=dev)
+                c.zero_()
                 _lib.call("gfgpu_pcg_begin", self._desc(), self.static.diag.data_ptr(), r.data_ptr(),
                           c.data_ptr(), ws2.data_ptr(), s)
                 _lib.call("gfgpu_pcg_iterate", self._desc(), inner, c.data_ptr(), ws2.data_ptr(), s)
                 self.R[k] = (r / sigma).view(self.H, self.W, 2).float()
-                self.T[k] = (c / sigma).view(self.H, self.W, 2).float()
+                self.T[k] = ((c - self.minv * r) / sigma).view(self.H, self.W, 2).float()
                 k += 1
         return npairs
 
     # ------------------------------------------------------------------ training
-    def train(self, steps=2000, batch=32, crop=64, margin=8, lr=2e-3, seed=2, log_every=0):
+    def train(self, steps=2000, batch=32, crop=64, margin=8, lr=2e-3, seed=2, log_every=0,
+              loss="energy"):
+        """Adam on random crops of the stored pairs (cosine learning-rate decay). loss: "energy"
+        (e^T A e / t^T A t per crop) or "mse"."""
         dev = _dev.device()
         B, S = int(batch), int(crop)
         X = torch.empty((B, S, S, 4), dtype=torch.float32, device=dev)
         Tc = torch.empty((B, S, S, 2), dtype=torch.float32, device=dev)
-        loss = torch.zeros(1, dtype=torch.float32, device=dev)
+        energy = loss == "energy"
+        Ec = torch.empty((B, S - 1, S - 1, 2), dtype=torch.float32, device=dev) if energy else None
+        Fc = torch.empty((B, S, S, 2), dtype=torch.float32, device=dev) if energy else None
+        lossv = torch.zeros(1, dtype=torch.float32, device=dev)
         nb = int(_lib.lib().gfgpu_nn_train_workspace_bytes(B, S, S))
         ws = torch.empty(nb // 4 + 64, dtype=torch.float32, device=dev)
         rng = np.random.default_rng(seed)
         npairs = self.R.shape[0]
         s = _dev.stream()
+        ptr = lambda t: t.data_ptr() if t is not None else None
         for it in range(steps):
             pos = np.stack([rng.integers(0, npairs, B),
                             rng.integers(-margin, max(self.H - S + margin, -margin) + 1, B),
@@ -171,18 +227,19 @@ class LearnedPreconditioner:
                            axis=1).astype(np.int32)
             pos_d = torch.as_tensor(pos, device=dev)
             _lib.call("gfgpu_nn_gather_crops", self.R.data_ptr(), self.T.data_ptr(),
-                      self.material.data_ptr(), pos_d.data_ptr(), B, S, self.H, self.W,
-                      X.data_ptr(), Tc.data_ptr(), s)
+                      self.material.data_ptr(), self.elem_kg.data_ptr(), self.free_f.data_ptr(),
+                      pos_d.data_ptr(), B, S, self.H, self.W, X.data_ptr(), Tc.data_ptr(), ptr(Ec),
+                      ptr(Fc), s)
             _lib.call("gfgpu_nn_train_step", self.wbf.data_ptr(), self.params.data_ptr(),
-                      X.data_ptr(), Tc.data_ptr(), B, S, margin, self.grads.data_ptr(),
-                      loss.data_ptr(), ws.data_ptr(), s)
+                      X.data_ptr(), Tc.data_ptr(), ptr(Ec), ptr(Fc), B, S, margin,
+                      self.grads.data_ptr(), lossv.data_ptr(), ws.data_ptr(), s)
             self.step += 1
             cur = lr * 0.5 * (1.0 + math.cos(math.pi * it / max(steps, 1)))
             _lib.call("gfgpu_nn_adam", self.params.data_ptr(), self.grads.data_ptr(),
                       self.m.data_ptr(), self.v.data_ptr(), self.P, float(max(cur, lr * 0.02)),
                       0.9, 0.999, 1e-8, self.step, self.wbf.data_ptr(), s)
             if log_every and (it % log_every == 0 or it == steps - 1):
-                self.losses.append((it, float(loss.item())))
+                self.losses.append((it, float(lossv.item())))
         return self.losses
 
     # ------------------------------------------------------------------ solves
@@ -192,16 +249,39 @@ class LearnedPreconditioner:
         x[torch.as_tensor(self.iip, device=x.device).long()] = torch.as_tensor(xp, device=x.device)
         return x
 
-    def fcg(self, x, tol=1e-8, use_nn=True, maxiter=200000, check_every=8):
-        nb = int(_lib.lib().gfgpu_fcg_workspace_bytes(self._desc(), self.H, self.W))
+    def fcg(self, x, tol=1e-8, use_nn=True, maxiter=200000, nkeep=8, check_every=16):
+        """Flexible CG (gfgpu_fcg_solve) in place on x (prescribed values + initial guess): with
+        the network, two directions per iteration (D^-1 r and the network's correction); without,
+        Jacobi only. Returns (iterations, relative true residual)."""
+        ndir = 2 if use_nn else 1
+        nb = int(_lib.lib().gfgpu_fcg_workspace_bytes(self._desc(), self.H, self.W, nkeep, ndir))
+        if nb <= 0:
+            raise ValueError("nkeep out of range")
         ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=_dev.device())
         it = C.c_int64(0)
         rel = C.c_double(0.0)
         nnd = C.addressof(self.nn_desc()) if use_nn else None
         _lib.call("gfgpu_fcg_solve", self._desc(), self.static.diag.data_ptr(), nnd, x.data_ptr(),
-                  float(tol), int(maxiter), int(check_every), ws.data_ptr(), _dev.stream(),
-                  C.addressof(it), C.addressof(rel))
+                  float(tol), int(maxiter), int(nkeep), int(check_every), ws.data_ptr(),
+                  _dev.stream(), C.addressof(it), C.addressof(rel))
         return int(it.value), float(rel.value)
+
+    def solve(self, x, tol=1e-8, maxiter=20000, nkeep=8, check_every=16):
+        """The learned solve with Jacobi-PCG as its fallback: when the flexible CG with the
+        network does not reach tol within maxiter iterations, Jacobi-PCG continues from its
+        iterate. Returns (network iterations, fallback iterations, relative true residual)."""
+        x0 = x.clone()
+        try:
+            it, rel = self.fcg(x, tol=tol, use_nn=True, maxiter=maxiter, nkeep=nkeep,
+                               check_every=check_every)
+            return it, 0, rel
+        except _lib.GFGPUError as e:
+            if e.code not in (-8, -5):  # not converged / non-finite residual
+                raise
+        if not bool(torch.isfinite(x).all()):
+            x.copy_(x0)
+        itf, rel = self.jacobi_pcg(x, tol=tol)
+        return maxiter, itf, rel
 
     def jacobi_pcg(self, x, tol=1e-8, check_every=16):
         return self.static.solve(x.view(self.H * self.W, 2), tol=tol, check_every=check_every)

@@ -377,37 +377,56 @@ typedef struct {
 } gfgpu_nn_desc;
 
 int32_t gfgpu_nn_param_count(void);
+/* Host only: the unit square Quad4 element stiffness (2x2 Gauss, plane strain) per unit bulk
+ * modulus (out[0:64]) and per unit shear modulus (out[64:128]), 8 x 8 row-major, dof a*2+i for
+ * local node a = (0,0), (1,0), (1,1), (0,1) and component i; the energy-norm loss uses it. */
+int gfgpu_nn_unit_element_stiffness(double* out);
 int32_t gfgpu_nn_param_offset(int32_t layer, int32_t bias);
 /* Training (CUDA cores, FP32 accumulate) on B crops of H x W nodes. */
 int64_t gfgpu_nn_train_workspace_bytes(int32_t B, int32_t H, int32_t W);
 int gfgpu_nn_forward(const void* weights_bf16, const float* params_f32, const float* X, int32_t B,
                      int32_t H, int32_t W, float* Y, void* workspace, gfgpu_stream_t stream);
-/* Forward, masked mean-squared error over the crop interior [margin, S - margin)^2 against T,
- * backward: grads (flat, like the parameters) and *loss (device float). Deterministic. */
+/* Forward, loss over the crop interior [margin, S - margin)^2 against T, backward: grads (flat,
+ * like the parameters) and *loss (device float). Deterministic. With E and F null the loss is
+ * the mean-squared error; with E [B, S-1, S-1, 2] (element K, G of each crop; 0 outside the mesh)
+ * and F [B, S, S, 2] (1 on free dofs, else 0) it is the energy norm: sum_b e_b^T A_b e_b over
+ * sum_b t_b^T A_b t_b, e = M F (y - T), t = M F T, M the interior mask and A_b crop b's stiffness
+ * (unit square Quad4 elements, 2x2 Gauss, plane strain). B <= 1024. */
 int gfgpu_nn_train_step(const void* weights_bf16, const float* params_f32, const float* X,
-                        const float* T, int32_t B, int32_t S, int32_t margin, float* grads,
-                        float* loss, void* workspace, gfgpu_stream_t stream);
+                        const float* T, const float* E, const float* F, int32_t B, int32_t S,
+                        int32_t margin, float* grads, float* loss, void* workspace,
+                        gfgpu_stream_t stream);
 /* Adam on the FP32 master parameters; rewrites the BF16 weights. */
 int gfgpu_nn_adam(float* params, const float* grads, float* m, float* v, int32_t n, float lr,
                   float beta1, float beta2, float eps, int32_t step, void* weights_bf16,
                   gfgpu_stream_t stream);
 /* Crops X [B, S, S, 4] (stored scaled residual + material) and targets T [B, S, S, 2] from
- * stored pairs R, Tg [npairs, H, W, 2]; pos [B, 3] = (pair, y0, x0). */
+ * stored pairs R, Tg [npairs, H, W, 2]; pos [B, 3] = (pair, y0, x0). Optionally (non-null Ec /
+ * Fc) the crops' element moduli Ec [B, S-1, S-1, 2] from elem_kg [(H-1)(W-1), 2] and free-dof
+ * masks Fc [B, S, S, 2] from free_mask [H*W*2] (float 0 / 1), both 0 outside the mesh. */
 int gfgpu_nn_gather_crops(const float* R, const float* T, const float* material,
-                          const int32_t* pos, int32_t B, int32_t S, int32_t H, int32_t W,
-                          float* X, float* Tc, gfgpu_stream_t stream);
+                          const float* elem_kg, const float* free_mask, const int32_t* pos,
+                          int32_t B, int32_t S, int32_t H, int32_t W, float* X, float* Tc,
+                          float* Ec, float* Fc, gfgpu_stream_t stream);
 /* Inference on one full grid with the middle layers on the tensor cores (mma.sync BF16, FP32
  * accumulate): X0 [H, W, 4] -> Y [H, W, 2]; workspace 3 x H*W*32 BF16 (256-byte aligned). */
 int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* workspace,
                    gfgpu_stream_t stream);
-/* Flexible CG (Notay's FCG(1): p = z - (z.q_prev / p_prev.q_prev) p_prev) in FP64 on the
- * partitioned elastic system of gfgpu_pcg_solve, preconditioned by the network (nn != NULL;
- * z = RMS(r) * net(r / RMS(r)), prescribed dofs 0) or by Jacobi (nn == NULL). Same stopping rule
- * and true-residual check as gfgpu_pcg_solve. Synchronises. */
-int64_t gfgpu_fcg_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W);
+/* Flexible CG in FP64 on the partitioned elastic system of gfgpu_pcg_solve (Notay's truncated
+ * FCG). Every iteration takes ndir search directions, the Jacobi-preconditioned residual
+ * D^-1 r and, with nn != NULL, the network's correction RMS(r) * net(r / RMS(r)) (prescribed
+ * dofs 0); each is A-orthogonalised against the last nkeep directions of earlier iterations and
+ * the earlier directions of the same iteration, and x, r take the exact line-search step along
+ * each (the energy is minimised over their span). With nn == NULL and any nkeep >= 1 this is
+ * Jacobi-PCG in exact arithmetic. Once the ring of directions is full the iterations replay as a
+ * CUDA graph of check_every (rounded up to the ring period) iterations; the residual is checked
+ * between replays. Same stopping rule and true-residual check as gfgpu_pcg_solve. ndir = 2 with
+ * a network, else 1; nkeep + ndir <= 20. Synchronises. */
+int64_t gfgpu_fcg_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W, int32_t nkeep,
+                                  int32_t ndir);
 int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
-                    double* x, double tol, int64_t maxiter, int32_t check_every, void* workspace,
-                    gfgpu_stream_t stream, int64_t* iters, double* relres);
+                    double* x, double tol, int64_t maxiter, int32_t nkeep, int32_t check_every,
+                    void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres);
 
 /* ============================ probes ====================================================== */
 

@@ -1,8 +1,9 @@
 """FP64 numpy oracle of the preconditioner network (test infrastructure only).
 
 The network is the 4-layer 3x3 convolutional net that the learned preconditioner applies on the
-nodal grid (NHWC layout, zero padding, dilation per layer): forward, loss and backward (input and
-weight gradients) written out with explicit shifts, used to check the GPU training kernels.
+nodal grid (NHWC layout, zero padding, dilation per layer): forward, losses (masked mean-squared
+error; energy norm with the crop's assembled stiffness) and backward (input and weight
+gradients) written out with explicit shifts, used to check the GPU training kernels.
 """
 
 import numpy as np
@@ -54,13 +55,8 @@ def forward(x, params, dils):
     return h, acts
 
 
-def loss_and_grads(x, target, mask, params, dils):
-    """Masked mean-squared error and its gradients w.r.t. every W and b."""
-    y, acts = forward(x, params, dils)
-    n = mask.sum() * y.shape[-1]
-    diff = (y - target) * mask[..., None]
-    loss = float((diff ** 2).sum() / n)
-    g = 2.0 * diff / n
+def backward(acts, params, dils, g):
+    """Gradients w.r.t. every W and b for the output gradient g."""
     grads = [None] * len(params)
     for k in reversed(range(len(params))):
         W, b = params[k]
@@ -68,4 +64,48 @@ def loss_and_grads(x, target, mask, params, dils):
         grads[k] = (dW, db)
         if k > 0:
             g = dx * (acts[k] > 0.0)
-    return loss, grads
+    return grads
+
+
+def loss_and_grads(x, target, mask, params, dils):
+    """Masked mean-squared error and its gradients w.r.t. every W and b."""
+    y, acts = forward(x, params, dils)
+    n = mask.sum() * y.shape[-1]
+    diff = (y - target) * mask[..., None]
+    loss = float((diff ** 2).sum() / n)
+    g = 2.0 * diff / n
+    return loss, backward(acts, params, dils, g)
+
+
+def crop_stiffness(E):
+    """Assembled stiffness of one S x S node crop (scipy CSR, dof = node * 2 + component, node =
+    y * S + x) of unit square Quad4 elements with moduli E [S-1, S-1, 2] (K, G), through the
+    oracle's element integrals (oracle.statics.stiffness)."""
+    from . import gfref as R
+    from . import statics as ST
+
+    S = E.shape[0] + 1
+    coor, conn = R.quad4_regular(S - 1, S - 1)
+    return ST.stiffness(coor, conn, E[..., 0].ravel().astype(np.float64),
+                        E[..., 1].ravel().astype(np.float64))
+
+
+def energy_loss_and_grads(x, target, E, F, margin, params, dils):
+    """Energy-norm loss sum_b e_b^T A_b e_b / sum_b t_b^T A_b t_b (e = M F (y - T), t = M F T,
+    M the crop interior [margin, S - margin)^2, A_b the crop stiffness) and its gradients."""
+    y, acts = forward(x, params, dils)
+    B, S = y.shape[0], y.shape[1]
+    M = np.zeros((S, S, 1))
+    M[margin:S - margin, margin:S - margin] = 1.0
+    num, den = 0.0, 0.0
+    Ae_all = np.zeros_like(y)
+    for b in range(B):
+        A = crop_stiffness(E[b])
+        w = (M * F[b]).ravel()
+        e = w * (y[b] - target[b]).ravel()
+        t = w * target[b].ravel()
+        Ae = A @ e
+        num += float(e @ Ae)
+        den += float(t @ (A @ t))
+        Ae_all[b] = (w * Ae).reshape(S, S, 2)
+    return num / den, backward(acts, params, dils, 2.0 * Ae_all / den)

@@ -137,3 +137,20 @@ def test_host_errors(lib):
     with pytest.raises(lib.GFGPUError) as ei:
         _dev.dof_csr(conn, dofs, 8)
     assert ei.value.code == -2
+
+
+def test_unit_element_stiffness_matches_oracle(lib, oracle):
+    """The element stiffness behind the energy-norm training loss (host computation in the
+    library) against the oracle's element integrals, per unit bulk and per unit shear modulus."""
+    from oracle import nn as O
+
+    out = np.zeros(128)
+    lib.call("gfgpu_nn_unit_element_stiffness", out.ctypes.data)
+    for m, (K, G) in enumerate(((1.0, 0.0), (0.0, 1.0))):
+        A = O.crop_stiffness(np.array([[[K, G]]])).toarray()
+        # crop nodes (y, x) = (0,0), (0,1), (1,0), (1,1) -> element local nodes 0, 1, 3, 2
+        loc = [0, 1, 3, 2]
+        perm = [loc.index(a) * 2 + i for a in range(4) for i in range(2)]
+        ref = A[np.ix_(perm, perm)]
+        got = out[m * 64:(m + 1) * 64].reshape(8, 8)
+        assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
