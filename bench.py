@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--n2d", type=int, default=512)
     p.add_argument("--nloads", type=int, default=64)
     p.add_argument("--train-steps", type=int, default=2000)
+    p.add_argument("--profile-iters", type=int, default=0,
+                   help="learned workload, kernel-share probe: skip pair generation and training "
+                        "and run each solver for this many iterations (untrained network)")
     p.add_argument("--ninst", type=int, default=256)
     p.add_argument("--batch-steps", type=int, default=500)
     p.add_argument("--kernel-variant", default="0,0",
@@ -515,6 +518,12 @@ def run_batch(args):
     return 0
 
 
+def _lib_call_bytes(H, W):
+    from goosefem_gb300 import _lib
+
+    return _lib.lib().gfgpu_nn_infer_workspace_bytes(H, W)
+
+
 def run_learned(args):
     """Quad4 512^2 two-phase static case: learned-preconditioner flexible CG vs Jacobi-PCG, both
     to 1e-8 relative residual in FP64 (time-to-solution on the same GPU; pair generation and
@@ -540,6 +549,26 @@ def run_learned(args):
         torch.cuda.synchronize()
         return (time.perf_counter() - t0,) + tuple(out)
 
+    if args.profile_iters > 0:
+        from goosefem_gb300 import _lib
+
+        k = args.profile_iters
+        runs = {}
+        for name, fn in (("jacobi_pcg", lambda x: lp.static.solve(x.view(-1, 2), maxiter=k)),
+                         ("jacobi_pcg_graph", lambda x: lp.fcg(x, use_nn=False, nkeep=1, maxiter=k)),
+                         ("learned_fcg_keep8", lambda x: lp.fcg(x, use_nn=True, nkeep=8, maxiter=k))):
+            x = lp.initial_guess(xp)
+            try:
+                fn(x)
+                runs[name] = "converged"
+            except _lib.GFGPUError as e:
+                if e.code != -8:
+                    raise
+                runs[name] = f"stopped after {k} iterations"
+        torch.cuda.synchronize()
+        print(json.dumps({"workload": "learned kernel-share probe (untrained network)",
+                          "config": {"nx": nx, "iterations": k}, "runs": runs}), flush=True)
+        return 0
     res = {}
     for name, fn in (("jacobi_pcg", lambda x: lp.jacobi_pcg(x)),
                      ("jacobi_pcg_graph", lambda x: lp.fcg(x, use_nn=False, nkeep=1))):
@@ -555,11 +584,36 @@ def run_learned(args):
                       log_every=max(args.train_steps // 10, 1))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
-    fn = lambda x: lp.solve(x, nkeep=8)  # noqa: E731
-    timed(fn)
-    best = min((timed(fn) for _ in range(args.steps)), key=lambda r: r[0])
-    res["learned_fcg"] = {"seconds": best[0], "iterations": best[1], "fallback_iterations": best[2],
-                          "relres_true": best[3]}
+    for nkeep in (4, 8, 16):
+        fn = lambda x: lp.solve(x, nkeep=nkeep)  # noqa: E731
+        timed(fn)
+        best = min((timed(fn) for _ in range(args.steps)), key=lambda r: r[0])
+        res[f"learned_fcg_keep{nkeep}"] = {"seconds": best[0], "iterations": best[1],
+                                           "fallback_iterations": best[2], "relres_true": best[3]}
+    res["learned_fcg"] = min((v for k, v in res.items() if k.startswith("learned_fcg_keep")),
+                             key=lambda v: v["seconds"])
+    for v in res.values():
+        v["us_per_iteration"] = 1e6 * v["seconds"] / max(v["iterations"] + v.get("fallback_iterations", 0), 1)
+    # one network application (gfgpu_nn_infer: the same four layers), CUDA events
+    H = W = nx + 1
+    X0 = torch.randn((H, W, 4), dtype=torch.float32, device="cuda")
+    Y = torch.empty((H, W, 2), dtype=torch.float32, device="cuda")
+    wsi = torch.empty(int(_lib_call_bytes(H, W)) // 8 + 1, dtype=torch.float64, device="cuda")
+    nnd = lp.nn_desc()
+    import ctypes as C
+    from goosefem_gb300 import _lib
+    st = torch.cuda.current_stream()
+    call = lambda: _lib.call("gfgpu_nn_infer", C.addressof(nnd), X0.data_ptr(), Y.data_ptr(),  # noqa: E731
+                             wsi.data_ptr(), st.cuda_stream)
+    for _ in range(5):
+        call()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(50):
+        call()
+    e1.record(st)
+    torch.cuda.synchronize()
+    nn_ms = e0.elapsed_time(e1) / 50
     jac = min(res["jacobi_pcg"]["seconds"], res["jacobi_pcg_graph"]["seconds"])
     line = {"metric": "time-to-1e-8 resid (learned FCG vs Jacobi PCG)",
             "value": res["learned_fcg"]["seconds"], "unit": "s", "higher_is_better": False,
@@ -569,11 +623,12 @@ def run_learned(args):
             "config": {"workload": f"Quad4 Regular {nx}x{nx}, two-phase (inclusions "
                                    f"{100 * inside.mean():.1f}% area, x10 moduli), bottom fixed, "
                                    "top uy=-1e-2", "pairs": npairs, "train_steps": args.train_steps,
-                       "loss": "energy norm", "directions_kept": 8},
+                       "loss": "energy norm", "directions_kept": [4, 8, 16]},
             "solvers": res,
             "speedup_vs_jacobi_pcg": jac / res["learned_fcg"]["seconds"],
             "iteration_ratio": res["jacobi_pcg"]["iterations"] / max(res["learned_fcg"]["iterations"], 1),
             "pair_generation_seconds": t_pairs, "training_seconds": t_train,
+            "network_application_ms": nn_ms,
             "loss_first_last": [losses[0], losses[-1]]}
     print(json.dumps(line), flush=True)
     return 0

@@ -383,7 +383,8 @@ __global__ void k_gather_crops(const float* __restrict__ R, const float* __restr
 // Weights in shared memory as [t][co][ci] with the ci row padded to 40 BF16 (80 B): the 32-bit
 // fragment loads of 8 rows x 4 column pairs then hit 32 different banks.
 constexpr int kPadC = 40;
-constexpr int kTileY = 8, kTileX = 16;
+constexpr int kTileY = 16, kTileX = 16;
+constexpr int kMmaThreads = 256; // 8 warps, warp w computes tile rows 2w and 2w + 1
 
 __device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2,
                                          uint32_t a3, uint32_t b0, uint32_t b1)
@@ -395,11 +396,22 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// Y = relu(conv(X, W) + b) for 32 -> 32 channels, X and Y BF16 [H, W, 32]. CTA: 128 threads,
-// output tile 8 rows x 16 columns; warp w computes rows 2w, 2w+1 (one m16 tile of 16 pixels
-// each) for the 4 n8 tiles of output channels, K = 9 taps x 32 input channels.
-__global__ void __launch_bounds__(128)
-k_conv32_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ W,
+// W [t][ci][co] (BF16) -> WT [t][co][kPadC] with zero padding: the shared-memory layout of
+// the tensor-core layer, prepared once per set of weights
+__global__ void k_nn_wprep(const __nv_bfloat16* __restrict__ W, __nv_bfloat16* __restrict__ WT)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 9 * 32 * kPadC) return;
+    int t = i / (32 * kPadC), co = (i / kPadC) % 32, ci = i % kPadC;
+    WT[i] = ci < 32 ? W[(t * 32 + ci) * 32 + co] : __float2bfloat16_rn(0.0f);
+}
+
+// Y = relu(conv(X, W) + b) for 32 -> 32 channels, X and Y BF16 [H, W, 32], WT the prepared
+// weights. CTA: 256 threads, output tile 16 rows x 16 columns; warp w computes rows 2w, 2w+1
+// (one m16 tile of 16 pixels each) for the 4 n8 tiles of output channels, K = 9 taps x 32
+// input channels.
+__global__ void __launch_bounds__(kMmaThreads)
+k_conv32_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ WT,
              const float* __restrict__ bias, int dil, int H, int Wd, __nv_bfloat16* __restrict__ Y)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -407,11 +419,8 @@ k_conv32_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restric
     __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(smem);          // [hh][hw][40]
     __nv_bfloat16* ws = halo + hh * hw * kPadC;                             // [9][32][40]
     const int y0 = blockIdx.y * kTileY, x0 = blockIdx.x * kTileX;
-    // weights: W [t][ci][co] -> ws [t][co][ci]
-    for (int i = threadIdx.x; i < 9 * 32 * 32; i += blockDim.x) {
-        int t = i / 1024, ci = (i / 32) % 32, co = i % 32;
-        ws[(t * 32 + co) * kPadC + ci] = W[i];
-    }
+    for (int i = threadIdx.x; i < 9 * 32 * kPadC / 8; i += blockDim.x)
+        reinterpret_cast<uint4*>(ws)[i] = reinterpret_cast<const uint4*>(WT)[i];
     // halo: 16-byte chunks (8 channels)
     for (int i = threadIdx.x; i < hh * hw * 4; i += blockDim.x) {
         int pix = i >> 2, ch = (i & 3) * 8;
@@ -484,29 +493,120 @@ inline size_t mma_smem_bytes(int dil)
 
 // ------------------------------------------------------------------ preconditioner glue (FP64)
 
-// network input from the FP64 residual nodevec: (r / sigma, K_node, G_node), sigma = sqrt(rr/n)
-__global__ void k_nn_input(const double* __restrict__ r, const float* __restrict__ mat,
-                           const double* __restrict__ sc, int rr_slot, double nfree, int64_t nnode,
-                           float* __restrict__ X0)
+// First layer (4 -> 32, dilation 1, ReLU) on the CUDA cores, BF16 output [H, W, 32]. Input
+// channels per node: with r != null the FP64 residual scaled by 1 / sigma, sigma = RMS of r over
+// the free dofs (sqrt(sc[rr_slot] / nfree)), and the two material channels; else X0 [H, W, 4].
+__global__ void __launch_bounds__(256)
+k_nn_first(const double* __restrict__ r, const double* __restrict__ sc, int rr_slot, double nfree,
+           const float* __restrict__ mat, const float* __restrict__ X0,
+           const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias, int H, int Wd,
+           __nv_bfloat16* __restrict__ Y)
 {
-    double sigma = sqrt(sc[rr_slot] / nfree);
-    double inv = sigma > 0.0 ? 1.0 / sigma : 0.0;
-    GF_FOR(p, nnode)
+    __shared__ float Ws[9 * 4 * 32];
+    __shared__ float bs[32];
+    __shared__ float s_inv;
+    for (int i = threadIdx.x; i < 9 * 4 * 32; i += blockDim.x) Ws[i] = __bfloat162float(W[i]);
+    if (threadIdx.x < 32) bs[threadIdx.x] = bias[threadIdx.x];
+    if (threadIdx.x == 0 && r) {
+        double sigma = sqrt(sc[rr_slot] / nfree);
+        s_inv = sigma > 0.0 ? static_cast<float>(1.0 / sigma) : 0.0f;
+    }
+    __syncthreads();
+    const float inv = r ? s_inv : 1.0f;
+    const int64_t hw = static_cast<int64_t>(H) * Wd;
+    GF_FOR(p, hw)
     {
-        X0[p * 4 + 0] = static_cast<float>(r[2 * p] * inv);
-        X0[p * 4 + 1] = static_cast<float>(r[2 * p + 1] * inv);
-        X0[p * 4 + 2] = mat[2 * p];
-        X0[p * 4 + 3] = mat[2 * p + 1];
+        int y = static_cast<int>(p / Wd), x = static_cast<int>(p % Wd);
+        float acc[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) acc[c] = bs[c];
+#pragma unroll 1
+        for (int t = 0; t < 9; ++t) {
+            int yy = y + (t / 3 - 1), xx = x + (t % 3 - 1);
+            if (yy < 0 || yy >= H || xx < 0 || xx >= Wd) continue;
+            int64_t q = static_cast<int64_t>(yy) * Wd + xx;
+            float v[4];
+            if (r) {
+                double2 rv = *reinterpret_cast<const double2*>(r + 2 * q);
+                float2 mv = *reinterpret_cast<const float2*>(mat + 2 * q);
+                v[0] = static_cast<float>(rv.x) * inv;
+                v[1] = static_cast<float>(rv.y) * inv;
+                v[2] = mv.x;
+                v[3] = mv.y;
+            }
+            else {
+                float4 xv = *reinterpret_cast<const float4*>(X0 + 4 * q);
+                v[0] = xv.x;
+                v[1] = xv.y;
+                v[2] = xv.z;
+                v[3] = xv.w;
+            }
+#pragma unroll
+            for (int ci = 0; ci < 4; ++ci)
+#pragma unroll
+                for (int c = 0; c < 32; ++c) acc[c] = fmaf(v[ci], Ws[(t * 4 + ci) * 32 + c], acc[c]);
+        }
+        uint4* yp = reinterpret_cast<uint4*>(Y + p * 32);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            __nv_bfloat162 h[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                h[j] = __floats2bfloat162_rn(fmaxf(acc[k * 8 + 2 * j], 0.0f), fmaxf(acc[k * 8 + 2 * j + 1], 0.0f));
+            yp[k] = *reinterpret_cast<uint4*>(h);
+        }
     }
 }
 
-// z = sigma * y on the free dofs, 0 on the prescribed dofs
-__global__ void k_nn_output(const float* __restrict__ y, const double* __restrict__ sc, int rr_slot,
-                            double nfree, const int32_t* __restrict__ part, int64_t nnu, int64_t n,
-                            double* __restrict__ z)
+// Last layer (32 -> 2, dilation 1, no activation) on the CUDA cores from BF16 [H, W, 32]. With
+// z != null: z = sigma * y on the free dofs and 0 on the prescribed ones (FP64 nodevec);
+// else Y [H, W, 2] in FP32.
+__global__ void __launch_bounds__(256)
+k_nn_last(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ W,
+          const float* __restrict__ bias, int H, int Wd, const double* __restrict__ sc, int rr_slot,
+          double nfree, const int32_t* __restrict__ part, int64_t nnu, double* __restrict__ z,
+          float* __restrict__ Y)
 {
-    double sigma = sqrt(sc[rr_slot] / nfree);
-    GF_FOR(t, n) z[t] = part[t] < nnu ? sigma * static_cast<double>(y[t]) : 0.0;
+    __shared__ float Ws[9 * 32 * 2];
+    __shared__ double s_sigma;
+    for (int i = threadIdx.x; i < 9 * 32 * 2; i += blockDim.x) Ws[i] = __bfloat162float(W[i]);
+    if (threadIdx.x == 0 && z) s_sigma = sqrt(sc[rr_slot] / nfree);
+    __syncthreads();
+    const float b0 = bias[0], b1 = bias[1];
+    const int64_t hw = static_cast<int64_t>(H) * Wd;
+    GF_FOR(p, hw)
+    {
+        int y = static_cast<int>(p / Wd), x = static_cast<int>(p % Wd);
+        float a0 = b0, a1 = b1;
+#pragma unroll 1
+        for (int t = 0; t < 9; ++t) {
+            int yy = y + (t / 3 - 1), xx = x + (t % 3 - 1);
+            if (yy < 0 || yy >= H || xx < 0 || xx >= Wd) continue;
+            const uint4* xp = reinterpret_cast<const uint4*>(X + (static_cast<int64_t>(yy) * Wd + xx) * 32);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                uint4 u = xp[k];
+                const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    float2 f = __bfloat1622float2(h[j]);
+                    int ci = k * 8 + 2 * j;
+                    a0 = fmaf(f.x, Ws[(t * 32 + ci) * 2 + 0], a0);
+                    a1 = fmaf(f.x, Ws[(t * 32 + ci) * 2 + 1], a1);
+                    a0 = fmaf(f.y, Ws[(t * 32 + ci + 1) * 2 + 0], a0);
+                    a1 = fmaf(f.y, Ws[(t * 32 + ci + 1) * 2 + 1], a1);
+                }
+            }
+        }
+        if (z) {
+            double sg = s_sigma;
+            z[2 * p] = part[2 * p] < nnu ? sg * static_cast<double>(a0) : 0.0;
+            z[2 * p + 1] = part[2 * p + 1] < nnu ? sg * static_cast<double>(a1) : 0.0;
+        }
+        else {
+            *reinterpret_cast<float2*>(Y + 2 * p) = make_float2(a0, a1);
+        }
+    }
 }
 
 } // namespace nn
@@ -665,8 +765,9 @@ struct SlotList {
     int n;
     int s[kMaxSlots];
 };
-// device scalars: r.r, b.b, r.P (per new direction), P.Q (per slot), z.Q (per basis entry)
-enum { F_RR = 0, F_BB, F_RP0, F_RP1, F_PQ, F_DOT = F_PQ + kMaxSlots, F_COUNT = F_DOT + kMaxSlots };
+// device scalars: r.r, b.b, step length per new direction, P.Q per slot, orthogonalisation
+// coefficient per basis entry
+enum { F_RR = 0, F_BB, F_A0, F_A1, F_PQ, F_C = F_PQ + kMaxSlots, F_COUNT = F_C + kMaxSlots };
 
 __device__ __forceinline__ double bsum(double v, double* sh)
 {
@@ -762,24 +863,87 @@ __global__ void k_fredv(const double* __restrict__ partial, SlotList dst, double
     }
 }
 
-// partial dots z.Q_j for the basis slots (z = minv * r when zin is null)
+// Coefficient c_k = (z.Q_j) / (P_j.Q_j) of basis entry k (slot j = L.s[k]) from partial row k:
+// warp k sums its row (fixed order: lane-strided, then the shuffle tree); 0 for a degenerate or
+// non-finite direction, which the combination then skips. Launch: 32 warps.
+__global__ void k_fred_coef(const double* __restrict__ partial, SlotList L, double* __restrict__ sc)
+{
+    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (k >= L.n) return;
+    double v = 0.0;
+    for (int i = lane; i < kRed; i += 32) v += partial[k * kRed + i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+        double pq = sc[F_PQ + L.s[k]];
+        double c = (pq > 0.0 && isfinite(pq)) ? v / pq : 0.0;
+        sc[F_C + k] = isfinite(c) ? c : 0.0;
+    }
+}
+
+// rows 0, 1 = P.Q, r.P of new direction d in slot `slot`: stores P.Q and the step length
+// alpha_d = r.P / P.Q (0 for a degenerate or non-finite direction, which then takes no step)
+__global__ void k_fred_dir(const double* __restrict__ partial, int slot, int d, double* __restrict__ sc)
+{
+    __shared__ double sh[32];
+    double v0 = 0.0, v1 = 0.0;
+    for (int i = threadIdx.x; i < kRed; i += blockDim.x) {
+        v0 += partial[i];
+        v1 += partial[kRed + i];
+    }
+    double pq = bsum(v0, sh);
+    double rp = bsum(v1, sh);
+    if (threadIdx.x == 0) {
+        sc[F_PQ + slot] = pq;
+        double a = (pq > 0.0 && isfinite(pq)) ? rp / pq : 0.0;
+        sc[F_A0 + d] = isfinite(a) ? a : 0.0;
+    }
+}
+
+// partial dots z.Q_j for the basis slots (z = minv * r when zin is null); NS >= L.n. Vectors
+// are read as double2 (n even, slots 256-byte aligned).
+template <int NS>
 __global__ void __launch_bounds__(256)
 k_mdot(const double* __restrict__ zin, const double* __restrict__ minv, const double* __restrict__ r,
        const double* __restrict__ Q, int64_t ld, SlotList L, int64_t n, double* __restrict__ partial)
 {
     __shared__ double sh[32];
-    double acc[kMaxSlots];
+    double acc[NS];
+    const double2* q[NS];
 #pragma unroll
-    for (int j = 0; j < kMaxSlots; ++j) acc[j] = 0.0;
-    GF_FOR(t, n)
+    for (int j = 0; j < NS; ++j) {
+        acc[j] = 0.0;
+        q[j] = reinterpret_cast<const double2*>(Q + (j < L.n ? L.s[j] : 0) * ld);
+    }
+    const int64_t n2 = n / 2;
+    GF_FOR(t, n2)
     {
+        double2 z;
+        if (zin) {
+            z = reinterpret_cast<const double2*>(zin)[t];
+        }
+        else {
+            double2 m = reinterpret_cast<const double2*>(minv)[t];
+            double2 rv = reinterpret_cast<const double2*>(r)[t];
+            z = make_double2(m.x * rv.x, m.y * rv.y);
+        }
+#pragma unroll
+        for (int j = 0; j < NS; ++j)
+            if (j < L.n) {
+                double2 qv = q[j][t];
+                acc[j] = fma(z.x, qv.x, acc[j]);
+                acc[j] = fma(z.y, qv.y, acc[j]);
+            }
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) { // odd length: the last entry
+        const int64_t t = n - 1;
         double z = zin ? zin[t] : minv[t] * r[t];
 #pragma unroll
-        for (int j = 0; j < kMaxSlots; ++j)
-            if (j < L.n) acc[j] = fma(z, Q[L.s[j] * ld + t], acc[j]);
+        for (int j = 0; j < NS; ++j)
+            if (j < L.n) acc[j] = fma(z, Q[(j < L.n ? L.s[j] : 0) * ld + t], acc[j]);
     }
 #pragma unroll
-    for (int j = 0; j < kMaxSlots; ++j) {
+    for (int j = 0; j < NS; ++j) {
         if (j < L.n) {
             double v = bsum(acc[j], sh);
             if (threadIdx.x == 0) partial[j * kRed + blockIdx.x] = v;
@@ -787,31 +951,55 @@ k_mdot(const double* __restrict__ zin, const double* __restrict__ minv, const do
     }
 }
 
-// P_new = z - sum_j (z.Q_j / P_j.Q_j) P_j over the basis slots (A-orthogonalisation)
-__global__ void k_mcombine(const double* __restrict__ zin, const double* __restrict__ minv,
-                           const double* __restrict__ r, const double* __restrict__ sc, double* P,
-                           int64_t ld, SlotList L, int snew, int64_t n)
+// P_new = z - sum_k c_k P_{L.s[k]} (A-orthogonalisation with the precomputed coefficients),
+// double2 access as in k_mdot
+template <int NS>
+__global__ void __launch_bounds__(256)
+k_mcombine(const double* __restrict__ zin, const double* __restrict__ minv,
+           const double* __restrict__ r, const double* __restrict__ sc, double* P, int64_t ld,
+           SlotList L, int snew, int64_t n)
 {
-    double c[kMaxSlots];
+    double c[NS];
+    const double2* p[NS];
 #pragma unroll
-    for (int j = 0; j < kMaxSlots; ++j) {
-        double pq = j < L.n ? sc[F_PQ + L.s[j]] : 0.0;
-        double cj = (j < L.n && pq > 0.0 && isfinite(pq)) ? sc[F_DOT + j] / pq : 0.0;
-        c[j] = isfinite(cj) ? cj : 0.0; // a degenerate or non-finite direction is skipped
+    for (int j = 0; j < NS; ++j) {
+        c[j] = j < L.n ? sc[F_C + j] : 0.0;
+        p[j] = reinterpret_cast<const double2*>(P + (j < L.n ? L.s[j] : 0) * ld);
     }
-    double* out = P + snew * ld;
-    GF_FOR(t, n)
+    double2* out = reinterpret_cast<double2*>(P + snew * ld);
+    const int64_t n2 = n / 2;
+    GF_FOR(t, n2)
     {
+        double2 v;
+        if (zin) {
+            v = reinterpret_cast<const double2*>(zin)[t];
+        }
+        else {
+            double2 m = reinterpret_cast<const double2*>(minv)[t];
+            double2 rv = reinterpret_cast<const double2*>(r)[t];
+            v = make_double2(m.x * rv.x, m.y * rv.y);
+        }
+#pragma unroll
+        for (int j = 0; j < NS; ++j)
+            if (c[j] != 0.0) {
+                double2 pv = p[j][t];
+                v.x = fma(-c[j], pv.x, v.x);
+                v.y = fma(-c[j], pv.y, v.y);
+            }
+        out[t] = v;
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) { // odd length: the last entry
+        const int64_t t = n - 1;
         double v = zin ? zin[t] : minv[t] * r[t];
 #pragma unroll
-        for (int j = 0; j < kMaxSlots; ++j)
-            if (j < L.n && c[j] != 0.0) v = fma(-c[j], P[L.s[j] * ld + t], v);
-        out[t] = v;
+        for (int j = 0; j < NS; ++j)
+            if (c[j] != 0.0) v = fma(-c[j], P[(j < L.n ? L.s[j] : 0) * ld + t], v);
+        P[snew * ld + t] = v;
     }
 }
 
-// x += sum_d alpha_d P_d, r -= sum_d alpha_d Q_d with alpha_d = r.P_d / P_d.Q_d (the new
-// directions are mutually A-orthogonal, so every alpha uses the same r); partial r.r
+// x += sum_d alpha_d P_d, r -= sum_d alpha_d Q_d (the new directions are mutually
+// A-orthogonal, so every alpha is taken with the same r); partial r.r
 __global__ void __launch_bounds__(256)
 k_mupdate(const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ P,
           const double* __restrict__ Q, int64_t ld, int s0, int s1, int ndir,
@@ -819,11 +1007,7 @@ k_mupdate(const int32_t* __restrict__ part, int64_t nnu, const double* __restric
           double* __restrict__ partial)
 {
     __shared__ double sh[32];
-    double pq0 = sc[F_PQ + s0], pq1 = ndir > 1 ? sc[F_PQ + s1] : 0.0;
-    double a0 = pq0 > 0.0 && isfinite(pq0) ? sc[F_RP0] / pq0 : 0.0;
-    double a1 = pq1 > 0.0 && isfinite(pq1) ? sc[F_RP1] / pq1 : 0.0;
-    if (!isfinite(a0)) a0 = 0.0; // a degenerate or non-finite direction takes no step
-    if (!isfinite(a1)) a1 = 0.0;
+    double a0 = sc[F_A0], a1 = ndir > 1 ? sc[F_A1] : 0.0;
     const double* P0 = P + s0 * ld;
     const double* Q0 = Q + s0 * ld;
     const double* P1 = P + s1 * ld;
@@ -850,12 +1034,65 @@ k_mupdate(const int32_t* __restrict__ part, int64_t nnu, const double* __restric
     if (threadIdx.x == 0) partial[blockIdx.x] = v;
 }
 
+// launch k_mdot / k_mcombine with the smallest slot-count instantiation that holds L.n
+template <template <int> class F, class... A>
+inline void with_ns(int n, A&&... a)
+{
+    if (n <= 1) F<1>::go(a...);
+    else if (n <= 2) F<2>::go(a...);
+    else if (n <= 4) F<4>::go(a...);
+    else if (n <= 8) F<8>::go(a...);
+    else if (n <= 12) F<12>::go(a...);
+    else if (n <= 16) F<16>::go(a...);
+    else F<kMaxSlots>::go(a...);
+}
+
+template <int NS>
+struct MdotL {
+    static void go(unsigned g, cudaStream_t st, const double* zin, const double* minv, const double* r,
+                   const double* Q, int64_t ld, const SlotList& L, int64_t n, double* partial)
+    {
+        k_mdot<NS><<<g, 256, 0, st>>>(zin, minv, r, Q, ld, L, n, partial);
+    }
+};
+
+template <int NS>
+struct McombineL {
+    static void go(unsigned g, cudaStream_t st, const double* zin, const double* minv, const double* r,
+                   const double* sc, double* P, int64_t ld, const SlotList& L, int snew, int64_t n)
+    {
+        k_mcombine<NS><<<g, 256, 0, st>>>(zin, minv, r, sc, P, ld, L, snew, n);
+    }
+};
+
 struct FcgWs {
     double *fe, *r, *z, *minv, *P, *Q, *partial, *sc;
     int64_t ld;
-    float *x0, *y;
-    __nv_bfloat16 *a1, *a2, *a3;
+    __nv_bfloat16 *a1, *a2, *a3, *wt1, *wt2;
 };
+
+constexpr int64_t kWtBytes = 9 * 32 * kPadC * 2; // prepared weights of one tensor-core layer
+
+// network buffers: three activations [hw][32] BF16 and the two prepared weight sets
+inline char* carve_nn(char* c, int64_t hw, __nv_bfloat16** a1, __nv_bfloat16** a2,
+                      __nv_bfloat16** a3, __nv_bfloat16** wt1, __nv_bfloat16** wt2)
+{
+    __nv_bfloat16** a[] = {a1, a2, a3};
+    for (auto b : a) {
+        *b = reinterpret_cast<__nv_bfloat16*>(c);
+        c += a256(hw * 32 * 2);
+    }
+    *wt1 = reinterpret_cast<__nv_bfloat16*>(c);
+    c += a256(kWtBytes);
+    *wt2 = reinterpret_cast<__nv_bfloat16*>(c);
+    c += a256(kWtBytes);
+    return c;
+}
+
+inline int64_t nn_bytes(int64_t hw)
+{
+    return 3 * a256(hw * 32 * 2) + 2 * a256(kWtBytes);
+}
 
 inline FcgWs carve_fcg(const gfgpu_verlet_desc* d, int64_t hw, int nslots, void* ws)
 {
@@ -878,15 +1115,7 @@ inline FcgWs carve_fcg(const gfgpu_verlet_desc* d, int64_t hw, int nslots, void*
     c += a256(int64_t(kMaxSlots) * kRed * 8);
     w.sc = reinterpret_cast<double*>(c);
     c += a256(F_COUNT * 8);
-    w.x0 = reinterpret_cast<float*>(c);
-    c += a256(hw * 4 * 4);
-    w.y = reinterpret_cast<float*>(c);
-    c += a256(hw * 2 * 4);
-    __nv_bfloat16** a[] = {&w.a1, &w.a2, &w.a3};
-    for (auto b : a) {
-        *b = reinterpret_cast<__nv_bfloat16*>(c);
-        c += a256(hw * 32 * 2);
-    }
+    carve_nn(c, hw, &w.a1, &w.a2, &w.a3, &w.wt1, &w.wt2);
     return w;
 }
 
@@ -894,29 +1123,47 @@ inline int64_t fcg_bytes(const gfgpu_verlet_desc* d, int64_t hw, int nslots)
 {
     int64_t n = d->nnode * d->ndim;
     return a256(d->nelem * d->nne * d->ndim * 8) + (3 + 2 * int64_t(nslots)) * a256(n * 8) +
-           a256(int64_t(kMaxSlots) * kRed * 8) + a256(F_COUNT * 8) + a256(hw * 16) + a256(hw * 8) +
-           3 * a256(hw * 64);
+           a256(int64_t(kMaxSlots) * kRed * 8) + a256(F_COUNT * 8) + nn_bytes(hw);
 }
 
-// z = network(r) on the nodal grid, with the tensor-core middle layers
+// the tensor-core layers' weights in their shared-memory layout
+inline void nn_prepare_weights(const gfgpu_nn_desc* nn, __nv_bfloat16* wt1, __nv_bfloat16* wt2,
+                               cudaStream_t s)
+{
+    const unsigned g = (9 * 32 * kPadC + 255) / 256;
+    k_nn_wprep<<<g, 256, 0, s>>>(wb(nn->weights_bf16, 1), wt1);
+    k_nn_wprep<<<g, 256, 0, s>>>(wb(nn->weights_bf16, 2), wt2);
+}
+
+// the four layers on one H x W grid: input from the FP64 residual (r != null) or from X0,
+// output to the FP64 correction z (z != null) or to Y
+inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0, const double* sc,
+                      int rr_slot, double nfree, const int32_t* part, int64_t nnu,
+                      __nv_bfloat16* a1, __nv_bfloat16* a2, __nv_bfloat16* a3,
+                      const __nv_bfloat16* wt1, const __nv_bfloat16* wt2, double* z, float* Y,
+                      cudaStream_t s)
+{
+    const int H = nn->H, W = nn->W;
+    const int64_t hw = int64_t(H) * W;
+    const unsigned g = grid_for(hw);
+    k_nn_first<<<g, 256, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wb(nn->weights_bf16, 0),
+                                 nn->params_f32 + b_off(0), H, W, a1);
+    dim3 grid((W + kTileX - 1) / kTileX, (H + kTileY - 1) / kTileY);
+    k_conv32_mma<<<grid, kMmaThreads, mma_smem_bytes(dil_of(1)), s>>>(
+        a1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
+    k_conv32_mma<<<grid, kMmaThreads, mma_smem_bytes(dil_of(2)), s>>>(
+        a2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
+    k_nn_last<<<g, 256, 0, s>>>(a3, wb(nn->weights_bf16, 3), nn->params_f32 + b_off(3), H, W, sc,
+                                rr_slot, nfree, part, nnu, z, Y);
+    return check_launch("nn_forward");
+}
+
+// z = RMS(r) * net(r / RMS(r)) on the nodal grid (0 on prescribed dofs)
 inline int nn_apply(const gfgpu_nn_desc* nn, const double* r, const double* sc, int rr_slot,
                     double nfree, const int32_t* part, int64_t nnu, FcgWs& w, double* z, cudaStream_t s)
 {
-    int H = nn->H, W = nn->W;
-    int64_t hw = int64_t(H) * W;
-    k_nn_input<<<grid_for(hw), kBlock, 0, s>>>(r, nn->material, sc, rr_slot, nfree, hw, w.x0);
-    unsigned g = pix_grid(hw);
-    k_conv_fwd<4, 32, true, float, __nv_bfloat16><<<g, 128, 0, s>>>(
-        w.x0, wb(nn->weights_bf16, 0), nn->params_f32 + b_off(0), dil_of(0), 1, H, W, w.a1);
-    dim3 grid((W + kTileX - 1) / kTileX, (H + kTileY - 1) / kTileY);
-    k_conv32_mma<<<grid, 128, mma_smem_bytes(dil_of(1)), s>>>(
-        w.a1, wb(nn->weights_bf16, 1), nn->params_f32 + b_off(1), dil_of(1), H, W, w.a2);
-    k_conv32_mma<<<grid, 128, mma_smem_bytes(dil_of(2)), s>>>(
-        w.a2, wb(nn->weights_bf16, 2), nn->params_f32 + b_off(2), dil_of(2), H, W, w.a3);
-    k_conv_fwd<32, 2, false, __nv_bfloat16, float><<<g, 128, 0, s>>>(
-        w.a3, wb(nn->weights_bf16, 3), nn->params_f32 + b_off(3), dil_of(3), 1, H, W, w.y);
-    k_nn_output<<<grid_for(hw * 2), kBlock, 0, s>>>(w.y, sc, rr_slot, nfree, part, nnu, hw * 2, z);
-    return check_launch("nn_apply");
+    return nn_forward(nn, r, nullptr, sc, rr_slot, nfree, part, nnu, w.a1, w.a2, w.a3, w.wt1, w.wt2,
+                      z, nullptr, s);
 }
 
 inline int prepare_mma(cudaStream_t)
@@ -1043,29 +1290,25 @@ int64_t gfgpu_fcg_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t
     return fcg_bytes(d, int64_t(H) * W, nkeep + ndir);
 }
 
+int64_t gfgpu_nn_infer_workspace_bytes(int32_t H, int32_t W)
+{
+    return H > 0 && W > 0 ? nn_bytes(int64_t(H) * W) : 0;
+}
+
 int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* workspace,
                    gfgpu_stream_t stream)
 {
     GF_REQUIRE(nn && X0 && Y && workspace && nn->H > 0 && nn->W > 0, "bad argument");
+    GF_REQUIRE(nn->weights_bf16 && nn->params_f32, "bad network descriptor");
+    GF_REQUIRE((reinterpret_cast<uintptr_t>(X0) & 15u) == 0 && (reinterpret_cast<uintptr_t>(Y) & 7u) == 0 &&
+                   (reinterpret_cast<uintptr_t>(workspace) & 255u) == 0,
+               "X0 must be 16-byte, Y 8-byte and the workspace 256-byte aligned");
     GF_TRY(prepare_mma(S(stream)));
     cudaStream_t s = S(stream);
-    int H = nn->H, W = nn->W;
-    int64_t hw = int64_t(H) * W;
-    char* c = static_cast<char*>(workspace);
-    __nv_bfloat16* a1 = reinterpret_cast<__nv_bfloat16*>(c);
-    __nv_bfloat16* a2 = reinterpret_cast<__nv_bfloat16*>(c + a256(hw * 64));
-    __nv_bfloat16* a3 = reinterpret_cast<__nv_bfloat16*>(c + 2 * a256(hw * 64));
-    unsigned g = pix_grid(hw);
-    k_conv_fwd<4, 32, true, float, __nv_bfloat16><<<g, 128, 0, s>>>(
-        X0, wb(nn->weights_bf16, 0), nn->params_f32 + b_off(0), dil_of(0), 1, H, W, a1);
-    dim3 grid((W + kTileX - 1) / kTileX, (H + kTileY - 1) / kTileY);
-    k_conv32_mma<<<grid, 128, mma_smem_bytes(dil_of(1)), s>>>(a1, wb(nn->weights_bf16, 1),
-                                                             nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
-    k_conv32_mma<<<grid, 128, mma_smem_bytes(dil_of(2)), s>>>(a2, wb(nn->weights_bf16, 2),
-                                                             nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
-    k_conv_fwd<32, 2, false, __nv_bfloat16, float><<<g, 128, 0, s>>>(
-        a3, wb(nn->weights_bf16, 3), nn->params_f32 + b_off(3), dil_of(3), 1, H, W, Y);
-    return check_launch("nn_infer");
+    __nv_bfloat16 *a1, *a2, *a3, *wt1, *wt2;
+    carve_nn(static_cast<char*>(workspace), int64_t(nn->H) * nn->W, &a1, &a2, &a3, &wt1, &wt2);
+    nn_prepare_weights(nn, wt1, wt2, s);
+    return nn_forward(nn, nullptr, X0, nullptr, 0, 1.0, nullptr, 0, a1, a2, a3, wt1, wt2, nullptr, Y, s);
 }
 
 int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
@@ -1117,23 +1360,16 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
                 zin = w.z;
             }
             if (L.n > 0) {
-                k_mdot<<<gb, 256, 0, st>>>(zin, w.minv, w.r, w.Q, w.ld, L, n, w.partial);
-                SlotList dst{};
-                dst.n = L.n;
-                for (int j = 0; j < L.n; ++j) dst.s[j] = F_DOT + j;
-                k_fredv<<<1, 1024, 0, st>>>(w.partial, dst, w.sc);
+                with_ns<MdotL>(L.n, gb, st, zin, w.minv, w.r, w.Q, w.ld, L, n, w.partial);
+                k_fred_coef<<<1, 32 * kMaxSlots, 0, st>>>(w.partial, L, w.sc);
             }
-            k_mcombine<<<grid_for(n), kBlock, 0, st>>>(zin, w.minv, w.r, w.sc, w.P, w.ld, L, snew, n);
+            with_ns<McombineL>(L.n, grid_for(n / 2), st, zin, w.minv, w.r, w.sc, w.P, w.ld, L, snew, n);
             double* Pn = w.P + snew * w.ld;
             double* Qn = w.Q + snew * w.ld;
             GF_TRY(gfgpu_internal_element_forces(d, Pn, w.fe, st));
             k_fgather<<<gb, 256, 0, st>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, Pn,
                                           w.r, n, Qn, w.partial);
-            SlotList dst{};
-            dst.n = 2;
-            dst.s[0] = F_PQ + snew;
-            dst.s[1] = dd == 0 ? F_RP0 : F_RP1;
-            k_fredv<<<1, 1024, 0, st>>>(w.partial, dst, w.sc);
+            k_fred_dir<<<1, 1024, 0, st>>>(w.partial, snew, dd, w.sc);
         }
         k_mupdate<<<gb, 256, 0, st>>>(d->part, d->nnu, w.P, w.Q, w.ld, static_cast<int>(c0 % nslots),
                                       static_cast<int>((c0 + 1) % nslots), ndir, w.sc, n, x, w.r,
@@ -1142,6 +1378,7 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
         return check_launch("fcg iteration");
     };
 
+    if (nn) nn_prepare_weights(nn, w.wt1, w.wt2, s);
     k_finv<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, diag, n, w.minv);
     // ||b||, b = -(A x_p)_u (P slot 0 as scratch)
     k_fkeep<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.P);

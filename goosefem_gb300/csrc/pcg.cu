@@ -76,9 +76,17 @@ k_pcg_gather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
-__global__ void k_pcg_alpha(double* sc)
+// p.q from the gather's partial row, then alpha = r.z / p.q (one launch)
+__global__ void k_reduce_alpha(const double* __restrict__ partials, double* __restrict__ sc)
 {
-    if (threadIdx.x == 0) sc[SC_ALPHA] = sc[SC_RZ] / sc[SC_PQ];
+    __shared__ double sh[32];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) v += partials[i];
+    double s = block_sum(v, sh);
+    if (threadIdx.x == 0) {
+        sc[SC_PQ] = s;
+        sc[SC_ALPHA] = sc[SC_RZ] / s;
+    }
 }
 
 // x += alpha p, r -= alpha q, z = M^-1 r (free dofs); partials r.z and r.r.
@@ -111,11 +119,22 @@ k_pcg_update(const int32_t* __restrict__ part, int64_t nnu, const double* __rest
     }
 }
 
-__global__ void k_pcg_beta(double* sc)
+// r.z (new) and r.r from the update's partial rows, then beta = r.z_new / r.z (one launch)
+__global__ void k_reduce_beta(const double* __restrict__ partials, double* __restrict__ sc)
 {
+    __shared__ double sh[32];
+    double v0 = 0.0, v1 = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) {
+        v0 += partials[i];
+        v1 += partials[kRedBlocks + i];
+    }
+    double rz = block_sum(v0, sh);
+    double rr = block_sum(v1, sh);
     if (threadIdx.x == 0) {
-        sc[SC_BETA] = sc[SC_RZ_NEW] / sc[SC_RZ];
-        sc[SC_RZ] = sc[SC_RZ_NEW];
+        sc[SC_RZ_NEW] = rz;
+        sc[SC_RR] = rr;
+        sc[SC_BETA] = rz / sc[SC_RZ];
+        sc[SC_RZ] = rz;
     }
 }
 
@@ -269,6 +288,22 @@ int gfgpu_elastic_diagonal(const gfgpu_verlet_desc* d, double* diag, void* works
     return gfgpu_assemble_node(d->csr_ptr, d->csr_idx, d->dofs, d->nnode, d->ndim, fe, diag, stream);
 }
 
+// One Jacobi-PCG iteration: 6 launches (element forces, gather, alpha, update, beta, direction).
+static int pcg_iteration(const gfgpu_verlet_desc* d, const PcgWs& w, double* x, int64_t n,
+                         cudaStream_t s)
+{
+    const unsigned gb = kRedBlocks;
+    GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
+    k_pcg_gather<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
+                                             w.p, n, w.q, w.partial);
+    k_reduce_alpha<<<1, 1024, 0, s>>>(w.partial, w.sc);
+    k_pcg_update<<<gb, kRedThreads, 0, s>>>(d->part, d->nnu, w.minv, w.p, w.q, n, w.sc, x, w.r, w.z,
+                                             w.partial);
+    k_reduce_beta<<<1, 1024, 0, s>>>(w.partial, w.sc);
+    k_pcg_direction<<<grid_for(n), kBlock, 0, s>>>(w.z, w.sc, n, w.p);
+    return GFGPU_OK;
+}
+
 int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, double tol,
                     int64_t maxiter, int32_t check_every, void* workspace, gfgpu_stream_t stream,
                     int64_t* iters, double* relres)
@@ -310,43 +345,77 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
     if (bnorm == 0.0) bnorm = 1.0;
     int64_t it = 0;
     double rel = std::sqrt(rr) / bnorm;
+    // check_every iterations replay as one CUDA graph (captured on a private stream, launched on
+    // the caller's); a remainder shorter than that runs eagerly
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cs = nullptr;
+    auto release = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (cs) cudaStreamDestroy(cs);
+        exec = nullptr;
+        cs = nullptr;
+    };
     while (rel > tol && it < maxiter) {
         int64_t nb = std::min<int64_t>(check_every, maxiter - it);
-        for (int64_t k = 0; k < nb; ++k) {
-            if ((rc = gfgpu_internal_element_forces(d, w.p, w.fe, s)) != GFGPU_OK) return fail_out(rc);
-            k_pcg_gather<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
-                                                     w.fe, w.p, n, w.q, w.partial);
-            k_reduce<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, SC_PQ);
-            k_pcg_alpha<<<1, 32, 0, s>>>(w.sc);
-            k_pcg_update<<<gb, kRedThreads, 0, s>>>(d->part, d->nnu, w.minv, w.p, w.q, n, w.sc, x,
-                                                     w.r, w.z, w.partial);
-            k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ_NEW); // SC_RZ_NEW, SC_PQ <- rr
-            k_pcg_beta<<<1, 32, 0, s>>>(w.sc);
-            k_pcg_direction<<<grid_for(n), kBlock, 0, s>>>(w.z, w.sc, n, w.p);
+        if (nb == check_every && !exec) {
+            rc = check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate");
+            cudaGraph_t graph = nullptr;
+            if (rc == GFGPU_OK)
+                rc = check_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
+            if (rc == GFGPU_OK) {
+                int crc = GFGPU_OK;
+                for (int64_t k = 0; k < nb && crc == GFGPU_OK; ++k) crc = pcg_iteration(d, w, x, n, cs);
+                cudaError_t e = cudaStreamEndCapture(cs, &graph);
+                rc = crc != GFGPU_OK ? crc : check_cuda(e, "cudaStreamEndCapture");
+                if (rc == GFGPU_OK)
+                    rc = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+                if (graph) cudaGraphDestroy(graph);
+            }
+            if (rc != GFGPU_OK) {
+                release();
+                return fail_out(rc);
+            }
+        }
+        if (nb == check_every) {
+            rc = check_cuda(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+        }
+        else {
+            for (int64_t k = 0; k < nb && rc == GFGPU_OK; ++k) rc = pcg_iteration(d, w, x, n, s);
+        }
+        if (rc != GFGPU_OK) {
+            release();
+            return fail_out(rc);
         }
         it += nb;
-        if ((rc = check_launch("pcg iteration")) != GFGPU_OK) return fail_out(rc);
-        cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
-        if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg iteration")) != GFGPU_OK)
+        if ((rc = check_launch("pcg iteration")) != GFGPU_OK) {
+            release();
             return fail_out(rc);
-        rr = hsc[SC_PQ]; // second reduced row of the update: r.r
+        }
+        cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
+        if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg iteration")) != GFGPU_OK) {
+            release();
+            return fail_out(rc);
+        }
+        rr = hsc[SC_RR];
         if (!std::isfinite(rr)) {
+            release();
             *iters = it;
             *relres = rr;
             return fail_out(fail(GFGPU_ERR_NAN, "gfgpu_pcg_solve: non-finite residual"));
         }
         rel = std::sqrt(rr) / bnorm;
     }
+    release();
     // true residual of the partitioned system: b_u - A_uu x_u = -(A x)_u, x holding x_p as well
     if ((rc = gfgpu_internal_element_forces(d, x, w.fe, s)) != GFGPU_OK) return fail_out(rc);
     k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
                                                nullptr, w.minv, n, w.r, w.z, nullptr, w.partial);
-    k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ_NEW);
+    k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_RR);
     cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
     if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg final residual")) != GFGPU_OK)
         return fail_out(rc);
     *iters = it;
-    *relres = std::sqrt(hsc[SC_PQ]) / bnorm;
+    *relres = std::sqrt(hsc[SC_RR]) / bnorm;
     cudaFreeHost(hsc);
     if (*relres > tol) return fail(GFGPU_ERR_DIVERGED, "gfgpu_pcg_solve: tolerance not reached");
     return GFGPU_OK;
@@ -385,20 +454,7 @@ int gfgpu_pcg_iterate(const gfgpu_verlet_desc* d, int64_t niter, double* x, void
     cudaStream_t s = S(stream);
     PcgWs w = carve(d, workspace);
     int64_t n = d->nnode * d->ndim;
-    const unsigned gb = kRedBlocks;
-    for (int64_t k = 0; k < niter; ++k) {
-        GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
-        k_pcg_gather<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
-                                                 w.fe, w.p, n, w.q, w.partial);
-        k_reduce<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, SC_PQ);
-        k_pcg_alpha<<<1, 32, 0, s>>>(w.sc);
-        k_pcg_update<<<gb, kRedThreads, 0, s>>>(d->part, d->nnu, w.minv, w.p, w.q, n, w.sc, x, w.r,
-                                                 w.z, w.partial);
-        k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ_NEW);
-        k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_RR);
-        k_pcg_beta<<<1, 32, 0, s>>>(w.sc);
-        k_pcg_direction<<<grid_for(n), kBlock, 0, s>>>(w.z, w.sc, n, w.p);
-    }
+    for (int64_t k = 0; k < niter; ++k) GF_TRY(pcg_iteration(d, w, x, n, s));
     return check_launch("pcg_iterate");
 }
 

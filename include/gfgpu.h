@@ -408,8 +408,11 @@ int gfgpu_nn_gather_crops(const float* R, const float* T, const float* material,
                           const float* elem_kg, const float* free_mask, const int32_t* pos,
                           int32_t B, int32_t S, int32_t H, int32_t W, float* X, float* Tc,
                           float* Ec, float* Fc, gfgpu_stream_t stream);
-/* Inference on one full grid with the middle layers on the tensor cores (mma.sync BF16, FP32
- * accumulate): X0 [H, W, 4] -> Y [H, W, 2]; workspace 3 x H*W*32 BF16 (256-byte aligned). */
+/* Inference on one full grid: first and last layer on the CUDA cores, the two 32 -> 32 layers
+ * on the tensor cores (mma.sync BF16, FP32 accumulate): X0 [H, W, 4] -> Y [H, W, 2];
+ * workspace of gfgpu_nn_infer_workspace_bytes(H, W) bytes (256-byte aligned; X0 16-byte, Y
+ * 8-byte aligned). */
+int64_t gfgpu_nn_infer_workspace_bytes(int32_t H, int32_t W);
 int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* workspace,
                    gfgpu_stream_t stream);
 /* Flexible CG in FP64 on the partitioned elastic system of gfgpu_pcg_solve (Notay's truncated

@@ -182,7 +182,8 @@ def test_tensor_core_inference_matches_fp32_and_oracle(L):
     d = NNDesc()
     d.weights_bf16, d.params_f32, d.material, d.H, d.W = wb.data_ptr(), pt.data_ptr(), mat.data_ptr(), H, W
     ytc = torch.empty((H, W, 2), dtype=torch.float32, device="cuda")
-    ws2 = torch.empty(3 * (H * W * 64 + 256) // 2 + 64, dtype=torch.bfloat16, device="cuda")
+    nbi = int(L.lib().gfgpu_nn_infer_workspace_bytes(H, W))
+    ws2 = torch.empty(nbi // 8 + 1, dtype=torch.float64, device="cuda")
     L.call("gfgpu_nn_infer", C.addressof(d), Xd.data_ptr(), ytc.data_ptr(), ws2.data_ptr(), s)
     yref, _ = O.forward(X0[None].astype(np.float64), _oracle_params(L, pt, wb), DILS)
     assert rel_err(y32.cpu().numpy(), yref[0]) <= 1e-5

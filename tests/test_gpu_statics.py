@@ -123,3 +123,30 @@ def test_pcg_quad4(gf, oracle):
     xg = to_np(x).ravel()
     assert S.residual(A, iip, xg) <= 1e-8
     assert np.linalg.norm(xg - x_ref) / np.linalg.norm(x_ref) <= 1e-6
+
+
+@pytest.mark.parametrize("n", [6, 7])
+def test_flexible_cg_jacobi_hex8(gf, oracle, n):
+    """gfgpu_fcg_solve without a network (Jacobi direction, ring of earlier directions) on Hex8:
+    an odd dof count (n = 6: 7^3 nodes x 3) and an even one, against the direct solve."""
+    import ctypes as C
+
+    from goosefem_gb300 import _dev, _lib
+    from oracle import statics as S
+
+    coor, conn, K, G, iip, xp = _hex8_case(n, 45)
+    nnode, nd = coor.shape
+    dofs = np.arange(nnode * nd).reshape(nnode, nd)
+    st = gf.statics.ElasticStatic(coor, conn, dofs, K, G, iip, uniform=True)
+    x = torch.zeros(nnode * nd, dtype=torch.float64, device="cuda")
+    x[torch.as_tensor(iip, device="cuda").long()] = torch.as_tensor(xp, device="cuda")
+    nb = int(_lib.lib().gfgpu_fcg_workspace_bytes(C.addressof(st.desc), 0, 0, 3, 1))
+    ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device="cuda")
+    it, rel = C.c_int64(0), C.c_double(0.0)
+    _lib.call("gfgpu_fcg_solve", C.addressof(st.desc), st.diag.data_ptr(), None, x.data_ptr(), 1e-8,
+              100000, 3, 4, ws.data_ptr(), _dev.stream(), C.addressof(it), C.addressof(rel))
+    A = S.stiffness(coor, conn, K, G)
+    x_ref = S.solve_partitioned(A, iip, xp)
+    xg = to_np(x)
+    assert rel.value <= 1e-8 and S.residual(A, iip, xg) <= 1e-8
+    assert np.linalg.norm(xg - x_ref) / np.linalg.norm(x_ref) <= 1e-6
