@@ -98,9 +98,12 @@ __global__ void k_shape(const double* xi, int nip, int nd, double* N, double* dN
 }
 
 // ElementQuad4.h:493-532 + detail.h:26-36. Strict arithmetic: dNx and vol are bit-exact.
+// QuadraturePlanar (ElementQuad4Planar.h:280-318) is the same with vol = w * det(J) * thick; for
+// plain Quad4 thick = 1 (an exact product, so the bits are unchanged).
 __global__ void k_quad4_compute_dN(const double* __restrict__ x, int64_t nelem,
                                    const double* __restrict__ xi, const double* __restrict__ w,
-                                   int nip, double* __restrict__ dNx, double* __restrict__ vol)
+                                   int nip, double thick, double* __restrict__ dNx,
+                                   double* __restrict__ vol)
 {
     GF_FOR(t, nelem * nip)
     {
@@ -131,7 +134,7 @@ __global__ void k_quad4_compute_dN(const double* __restrict__ x, int64_t nelem,
             o[m * 2 + 1] = __dadd_rn(__dmul_rn(i10, dn[m * 2 + 0]), __dmul_rn(i11, dn[m * 2 + 1]));
         }
         store<8>(dNx + t * 8, o);
-        vol[t] = __dmul_rn(w[q], det);
+        vol[t] = __dmul_rn(__dmul_rn(w[q], det), thick);
     }
 }
 
@@ -203,8 +206,10 @@ __device__ __forceinline__ double dot4(const double* a, int sa, const double* b,
     return r;
 }
 
-// mode 0: GradN_vector, 1: GradN_vector_T, 2: SymGradN_vector.
-template <bool S, int NNE, int ND, int MODE>
+// mode 0: GradN_vector, 1: GradN_vector_T, 2: SymGradN_vector. TD: tensor dimension of the
+// output (TD = 3 with ND = 2: QuadraturePlanar, ElementQuad4Planar.h:130-221, the in-plane block
+// of a zero-filled 3x3 tensor).
+template <bool S, int NNE, int ND, int MODE, int TD = ND>
 __global__ void k_grad(const double* __restrict__ dNx, const double* __restrict__ elemvec,
                        int64_t nelem, int nip, double* __restrict__ qtensor)
 {
@@ -261,7 +266,16 @@ __global__ void k_grad(const double* __restrict__ dNx, const double* __restrict_
                         }
                     }
         }
-        store<ND * ND>(qtensor + t * ND * ND, o);
+        if constexpr (TD == ND) {
+            store<ND * ND>(qtensor + t * ND * ND, o);
+        }
+        else {
+            double* out = qtensor + t * TD * TD;
+#pragma unroll
+            for (int i = 0; i < TD; ++i)
+#pragma unroll
+                for (int j = 0; j < TD; ++j) out[i * TD + j] = (i < ND && j < ND) ? o[i * ND + j] : 0.0;
+        }
     }
 }
 
@@ -295,7 +309,9 @@ __global__ void k_interp(const double* __restrict__ N, const double* __restrict_
 // ---------------------------------------------------------------- integrals (thread per element)
 
 // Int_gradN_dot_tensor2_dV: ElementQuad4.h:467-491 / ElementHex8.h:355-383.
-template <bool S, int NNE, int ND>
+// TD = 3 with ND = 2: QuadraturePlanar (ElementQuad4Planar.h:254-277), the in-plane block of
+// each 3x3 tensor.
+template <bool S, int NNE, int ND, int TD = ND>
 __global__ void k_int_grad_tensor2(const double* __restrict__ dNx, const double* __restrict__ vol,
                                    const double* __restrict__ qtensor, int64_t nelem, int nip,
                                    double* __restrict__ elemvec)
@@ -309,7 +325,13 @@ __global__ void k_int_grad_tensor2(const double* __restrict__ dNx, const double*
             int64_t t = e * nip + q;
             double g[NNE * ND], s[ND * ND];
             load<NNE * ND>(dNx + t * NNE * ND, g);
-            if constexpr (ND == 2) load<4>(qtensor + t * 4, s);
+            if constexpr (ND == 2 && TD == 2) load<4>(qtensor + t * 4, s);
+            else if constexpr (ND == 2) {
+                s[0] = __ldg(qtensor + t * 9 + 0);
+                s[1] = __ldg(qtensor + t * 9 + 1);
+                s[2] = __ldg(qtensor + t * 9 + 3);
+                s[3] = __ldg(qtensor + t * 9 + 4);
+            }
             else {
 #pragma unroll
                 for (int k = 0; k < 9; ++k) s[k] = __ldg(qtensor + t * 9 + k);
@@ -373,10 +395,12 @@ __global__ void k_int_n_scalar(const double* __restrict__ N, const double* __res
 
 // Int_gradN_dot_tensor4_dot_gradNT_dV: Element.h:1132-1176. Thread per elemmat entry; the
 // entry (m*nd+j, n*nd+k) accumulates over q, then i, then l as in the reference loop nest.
+// td: tensor dimension of C (td = 3 with nd = 2: QuadraturePlanar, the in-plane indices of a
+// [3,3,3,3] tensor).
 template <bool S>
 __global__ void k_int_tensor4(const double* __restrict__ dNx, const double* __restrict__ vol,
                               const double* __restrict__ C, int64_t nelem, int nne, int nip,
-                              int nd, double* __restrict__ elemmat)
+                              int nd, int td, double* __restrict__ elemmat)
 {
     int K = nne * nd;
     GF_FOR(t, nelem * K * K)
@@ -388,11 +412,11 @@ __global__ void k_int_tensor4(const double* __restrict__ dNx, const double* __re
         double acc = 0.0;
         for (int q = 0; q < nip; ++q) {
             const double* g = dNx + (e * nip + q) * nne * nd;
-            const double* Cq = C + (e * nip + q) * nd * nd * nd * nd;
+            const double* Cq = C + (e * nip + q) * td * td * td * td;
             double v = vol[e * nip + q];
             for (int i = 0; i < nd; ++i)
                 for (int l = 0; l < nd; ++l)
-                    acc = madd<S>(mul<S>(mul<S>(g[m * nd + i], Cq[((i * nd + j) * nd + k) * nd + l]),
+                    acc = madd<S>(mul<S>(mul<S>(g[m * nd + i], Cq[((i * td + j) * td + k) * td + l]),
                                          g[n * nd + l]),
                                   v, acc);
         }
@@ -452,7 +476,7 @@ using namespace gfgpu;
 
 template <int MODE>
 static int grad(const double* dNx, const double* elemvec, int64_t nelem, int32_t nne, int32_t nip,
-                int32_t nd, double* qtensor, gfgpu_stream_t stream)
+                int32_t nd, double* qtensor, gfgpu_stream_t stream, bool planar = false)
 {
     GF_REQUIRE(dNx && elemvec && qtensor && nip > 0, "bad argument");
     GF_TRY(check_elem(nne, nd));
@@ -460,7 +484,9 @@ static int grad(const double* dNx, const double* elemvec, int64_t nelem, int32_t
     GF_REQUIRE(aligned16(dNx) && aligned16(elemvec), "dNx and elemvec must be 16-byte aligned");
     if (nelem == 0) return GFGPU_OK;
     unsigned g = grid_for(nelem * nip);
-    if (nd == 2)
+    if (planar)
+        DISPATCH_S(k_grad<kS, 4, 2, MODE, 3><<<g, kBlock, 0, S(stream)>>>(dNx, elemvec, nelem, nip, qtensor));
+    else if (nd == 2)
         DISPATCH_S(k_grad<kS, 4, 2, MODE><<<g, kBlock, 0, S(stream)>>>(dNx, elemvec, nelem, nip, qtensor));
     else
         DISPATCH_S(k_grad<kS, 8, 3, MODE><<<g, kBlock, 0, S(stream)>>>(dNx, elemvec, nelem, nip, qtensor));
@@ -471,7 +497,7 @@ extern "C" {
 
 static int compute_dN(int nd, const double* x, int64_t nelem, const double* xi, const double* w,
                       int32_t nip, double* N, double* dNxi, double* dNx, double* vol,
-                      gfgpu_stream_t stream)
+                      gfgpu_stream_t stream, double thick = 1.0)
 {
     GF_REQUIRE(x && xi && w && dNx && vol && nip > 0 && nelem >= 0, "bad argument");
     GF_REQUIRE(!too_big(nelem * nip * 24), "too many elements");
@@ -480,7 +506,7 @@ static int compute_dN(int nd, const double* x, int64_t nelem, const double* xi, 
     if (nelem > 0) {
         if (nd == 2)
             k_quad4_compute_dN<<<grid_for(nelem * nip), kBlock, 0, S(stream)>>>(x, nelem, xi, w, nip,
-                                                                              dNx, vol);
+                                                                              thick, dNx, vol);
         else
             k_hex8_compute_dN<<<grid_for(nelem * nip), kBlock, 0, S(stream)>>>(x, nelem, xi, w, nip,
                                                                              dNx, vol);
@@ -587,8 +613,62 @@ int gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv(const double* dNx, const double*
     GF_REQUIRE(!too_big(nelem * K * K), "too many elements");
     if (nelem == 0) return GFGPU_OK;
     DISPATCH_S(k_int_tensor4<kS><<<grid_for(nelem * K * K), kBlock, 0, S(stream)>>>(
-        dNx, vol, qtensor4, nelem, nne, nip, ndim, elemmat));
+        dNx, vol, qtensor4, nelem, nne, nip, ndim, ndim, elemmat));
     return check_launch("int_grad_n_dot_tensor4_dot_grad_nt_dv");
+}
+
+// ---------------------------------------------------------------- QuadraturePlanar
+
+int gfgpu_quad4_planar_compute_dN(const double* x, int64_t nelem, const double* xi,
+                                  const double* w, int32_t nip, double thick, double* N,
+                                  double* dNxi, double* dNx, double* vol, gfgpu_stream_t stream)
+{
+    return compute_dN(2, x, nelem, xi, w, nip, N, dNxi, dNx, vol, stream, thick);
+}
+
+int gfgpu_grad_n_vector_planar(const double* dNx, const double* elemvec, int64_t nelem,
+                               int32_t nip, double* qtensor, gfgpu_stream_t stream)
+{
+    return grad<0>(dNx, elemvec, nelem, 4, nip, 2, qtensor, stream, true);
+}
+
+int gfgpu_grad_n_vector_T_planar(const double* dNx, const double* elemvec, int64_t nelem,
+                                 int32_t nip, double* qtensor, gfgpu_stream_t stream)
+{
+    return grad<1>(dNx, elemvec, nelem, 4, nip, 2, qtensor, stream, true);
+}
+
+int gfgpu_sym_grad_n_vector_planar(const double* dNx, const double* elemvec, int64_t nelem,
+                                   int32_t nip, double* qtensor, gfgpu_stream_t stream)
+{
+    return grad<2>(dNx, elemvec, nelem, 4, nip, 2, qtensor, stream, true);
+}
+
+int gfgpu_int_grad_n_dot_tensor2_dv_planar(const double* dNx, const double* vol,
+                                           const double* qtensor, int64_t nelem, int32_t nip,
+                                           double* elemvec, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(dNx && vol && qtensor && elemvec && nip > 0, "bad argument");
+    GF_REQUIRE(!too_big(nelem * nip * 9), "too many elements");
+    GF_REQUIRE(aligned16(dNx), "dNx must be 16-byte aligned");
+    if (nelem == 0) return GFGPU_OK;
+    unsigned g = grid_for(nelem, 128);
+    DISPATCH_S(k_int_grad_tensor2<kS, 4, 2, 3><<<g, 128, 0, S(stream)>>>(dNx, vol, qtensor, nelem,
+                                                                         nip, elemvec));
+    return check_launch("int_grad_n_dot_tensor2_dv_planar");
+}
+
+int gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv_planar(const double* dNx, const double* vol,
+                                                       const double* qtensor4, int64_t nelem,
+                                                       int32_t nip, double* elemmat,
+                                                       gfgpu_stream_t stream)
+{
+    GF_REQUIRE(dNx && vol && qtensor4 && elemmat && nip > 0, "bad argument");
+    GF_REQUIRE(!too_big(nelem * 64) && !too_big(nelem * nip * 81), "too many elements");
+    if (nelem == 0) return GFGPU_OK;
+    DISPATCH_S(k_int_tensor4<kS><<<grid_for(nelem * 64), kBlock, 0, S(stream)>>>(
+        dNx, vol, qtensor4, nelem, 4, nip, 2, 3, elemmat));
+    return check_launch("int_grad_n_dot_tensor4_dot_grad_nt_dv_planar");
 }
 
 int gfgpu_elastic_stress(const double* eps, const double* K, const double* G, int64_t nelem,

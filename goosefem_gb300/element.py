@@ -59,6 +59,7 @@ def _hex8_nodal():
 class _QuadratureBase:
     _nne = None
     _ndim = None
+    _tdim = None
     _fn = None
 
     def __init__(self, x, xi=None, w=None):
@@ -103,7 +104,7 @@ class _QuadratureBase:
         return self._ndim
 
     def tdim(self):
-        return self._ndim
+        return self._ndim if self._tdim is None else self._tdim
 
     def nip(self):
         return self._nip
@@ -116,7 +117,7 @@ class _QuadratureBase:
         return (self._nelem, k, k)
 
     def shape_qtensor(self, rank=0, n=None):
-        return (self._nelem, self._nip) + (self._ndim if n is None else n,) * rank
+        return (self._nelem, self._nip) + (self.tdim() if n is None else n,) * rank
 
     def shape_qscalar(self):
         return (self._nelem, self._nip)
@@ -255,6 +256,56 @@ class Quad4:
         @staticmethod
         def _gauss():
             return _quad4_gauss()
+
+
+class _QuadraturePlanar(_QuadratureBase):
+    """Element::Quad4::QuadraturePlanar (ElementQuad4Planar.h:38-335): Quad4 with 3x3
+    quadrature-point tensors (plane strain) and the out-of-plane thickness in dV."""
+
+    _nne, _ndim, _tdim = 4, 2, 3
+
+    def __init__(self, x, xi=None, w=None, thick=1.0):
+        self._thick = float(thick)
+        super().__init__(x, xi, w)
+
+    @staticmethod
+    def _gauss():
+        return _quad4_gauss()
+
+    def _compute_dN(self):
+        _lib.call("gfgpu_quad4_planar_compute_dN", self._x.data_ptr(), self._nelem,
+                  self._xi.data_ptr(), self._w.data_ptr(), self._nip, self._thick,
+                  self._N.data_ptr(), self._dNxi.data_ptr(), self._dNx.data_ptr(),
+                  self._vol.data_ptr(), _dev.stream())
+
+    def _grad(self, fn, elemvec, qtensor):
+        ev = _dev.dev_f64(elemvec)
+        _dev.check_shape(ev, self.shape_elemvec(), fn)
+        _dev.check_shape(qtensor, self.shape_qtensor(2), fn)
+        _lib.call(fn + "_planar", self._dNx.data_ptr(), ev.data_ptr(), self._nelem, self._nip,
+                  qtensor.data_ptr(), _dev.stream())
+        return qtensor
+
+    def int_gradN_dot_tensor2_dV(self, qtensor, elemvec):
+        qt = _dev.dev_f64(qtensor)
+        _dev.check_shape(qt, self.shape_qtensor(2), "int_gradN_dot_tensor2_dV")
+        _dev.check_shape(elemvec, self.shape_elemvec(), "int_gradN_dot_tensor2_dV")
+        _lib.call("gfgpu_int_grad_n_dot_tensor2_dv_planar", self._dNx.data_ptr(),
+                  self._vol.data_ptr(), qt.data_ptr(), self._nelem, self._nip, elemvec.data_ptr(),
+                  _dev.stream())
+        return elemvec
+
+    def int_gradN_dot_tensor4_dot_gradNT_dV(self, qtensor, elemmat):
+        qt = _dev.dev_f64(qtensor)
+        _dev.check_shape(qt, self.shape_qtensor(4), "int_gradN_dot_tensor4_dot_gradNT_dV")
+        _dev.check_shape(elemmat, self.shape_elemmat(), "int_gradN_dot_tensor4_dot_gradNT_dV")
+        _lib.call("gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv_planar", self._dNx.data_ptr(),
+                  self._vol.data_ptr(), qt.data_ptr(), self._nelem, self._nip,
+                  elemmat.data_ptr(), _dev.stream())
+        return elemmat
+
+
+Quad4.QuadraturePlanar = _QuadraturePlanar
 
 
 class Hex8:

@@ -148,6 +148,32 @@ int gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv(const double* dNx, const double*
                                                 int32_t nne, int32_t nip, int32_t ndim,
                                                 double* elemmat, gfgpu_stream_t stream);
 
+/* Element::Quad4::QuadraturePlanar (ElementQuad4Planar.h): Quad4 with 3x3 quadrature-point
+ * tensors (plane strain) and an out-of-plane thickness.
+ * compute_dN: ElementQuad4Planar.h:81-123, 280-318, vol = w det(J) thick. The gradients
+ * (:130-221) write the in-plane block of a zero-filled qtensor [nelem,nip,3,3];
+ * Int_gradN_dot_tensor2_dV (:254-277) reads the in-plane block of [nelem,nip,3,3];
+ * Int_gradN_dot_tensor4_dot_gradNT_dV (Element.h:1132-1176) the in-plane indices of
+ * [nelem,nip,3,3,3,3]. InterpQuad_vector, Int_N_vector_dV and Int_N_scalar_NT_dV are the Quad4
+ * entry points (gfgpu_interp_quad_vector, ...) with this vol. Stress: gfgpu_elastic_stress with
+ * ndim = 3 on the 3x3 strain gives the plane-strain stress including sigma_zz. */
+int gfgpu_quad4_planar_compute_dN(const double* x, int64_t nelem, const double* xi,
+                                  const double* w, int32_t nip, double thick, double* N,
+                                  double* dNxi, double* dNx, double* vol, gfgpu_stream_t stream);
+int gfgpu_grad_n_vector_planar(const double* dNx, const double* elemvec, int64_t nelem,
+                               int32_t nip, double* qtensor, gfgpu_stream_t stream);
+int gfgpu_grad_n_vector_T_planar(const double* dNx, const double* elemvec, int64_t nelem,
+                                 int32_t nip, double* qtensor, gfgpu_stream_t stream);
+int gfgpu_sym_grad_n_vector_planar(const double* dNx, const double* elemvec, int64_t nelem,
+                                   int32_t nip, double* qtensor, gfgpu_stream_t stream);
+int gfgpu_int_grad_n_dot_tensor2_dv_planar(const double* dNx, const double* vol,
+                                           const double* qtensor, int64_t nelem, int32_t nip,
+                                           double* elemvec, gfgpu_stream_t stream);
+int gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv_planar(const double* dNx, const double* vol,
+                                                       const double* qtensor4, int64_t nelem,
+                                                       int32_t nip, double* elemmat,
+                                                       gfgpu_stream_t stream);
+
 /* Linear elastic stress (external GMat in the reference; convention of
  * docs/theory/examples/cartesian_linear-elasticity.py:146-186): sigma = K tr(eps) I + 2G dev(eps)
  * with a 3-d trace (ndim=2: plane strain). K, G per element [nelem]. */

@@ -446,8 +446,10 @@ namespace detail {
 template <int NNE, int ND>
 class Quadrature {
 public:
-    Quadrature(const array<double>& x, const host::array<double>& xi, const host::array<double>& w)
-        : m_x(x.copy()), m_xi(array<double>::from_host(xi)), m_w(array<double>::from_host(w))
+    Quadrature(const array<double>& x, const host::array<double>& xi, const host::array<double>& w,
+               bool planar = false, double thick = 1.0)
+        : m_x(x.copy()), m_xi(array<double>::from_host(xi)), m_w(array<double>::from_host(w)),
+          m_planar(planar), m_thick(thick)
     {
         if (x.dimension() != 3 || x.shape(1) != NNE || x.shape(2) != ND)
             throw std::runtime_error("Quadrature: x must be [nelem, nne, ndim]");
@@ -468,21 +470,21 @@ public:
     int64_t nelem() const { return m_nelem; }
     int32_t nne() const { return NNE; }
     int32_t ndim() const { return ND; }
-    int32_t tdim() const { return ND; }
+    int32_t tdim() const { return m_planar ? 3 : ND; }
     int32_t nip() const { return m_nip; }
     const array<double>& GradN() const { return m_dNx; }
     const array<double>& dV() const { return m_vol; }
     shape_t shape_elemvec() const { return {m_nelem, NNE, ND}; }
     shape_t shape_elemmat() const { return {m_nelem, NNE * ND, NNE * ND}; }
     shape_t shape_qscalar() const { return {m_nelem, m_nip}; }
-    shape_t shape_qtensor2() const { return {m_nelem, m_nip, ND, ND}; }
+    shape_t shape_qtensor2() const { return {m_nelem, m_nip, tdim(), tdim()}; }
 
-    void gradN_vector(const array<double>& ev, array<double>& q) const { grad(gfgpu_grad_n_vector, ev, q); }
-    array<double> GradN_vector(const array<double>& ev) const { return alloc2(gfgpu_grad_n_vector, ev); }
-    void gradN_vector_T(const array<double>& ev, array<double>& q) const { grad(gfgpu_grad_n_vector_T, ev, q); }
-    array<double> GradN_vector_T(const array<double>& ev) const { return alloc2(gfgpu_grad_n_vector_T, ev); }
-    void symGradN_vector(const array<double>& ev, array<double>& q) const { grad(gfgpu_sym_grad_n_vector, ev, q); }
-    array<double> SymGradN_vector(const array<double>& ev) const { return alloc2(gfgpu_sym_grad_n_vector, ev); }
+    void gradN_vector(const array<double>& ev, array<double>& q) const { grad(0, ev, q); }
+    array<double> GradN_vector(const array<double>& ev) const { return alloc2(0, ev); }
+    void gradN_vector_T(const array<double>& ev, array<double>& q) const { grad(1, ev, q); }
+    array<double> GradN_vector_T(const array<double>& ev) const { return alloc2(1, ev); }
+    void symGradN_vector(const array<double>& ev, array<double>& q) const { grad(2, ev, q); }
+    array<double> SymGradN_vector(const array<double>& ev) const { return alloc2(2, ev); }
 
     void interpQuad_vector(const array<double>& ev, array<double>& qv) const
     {
@@ -527,9 +529,14 @@ public:
     {
         require_shape(qt.shape(), shape_qtensor2(), "int_gradN_dot_tensor2_dV");
         require_shape(ev.shape(), shape_elemvec(), "int_gradN_dot_tensor2_dV");
-        check(gfgpu_int_grad_n_dot_tensor2_dv(m_dNx.data(), m_vol.data(), qt.data(), m_nelem, NNE,
-                                              m_nip, ND, ev.data(), nullptr),
-              "int_gradN_dot_tensor2_dV");
+        if (m_planar)
+            check(gfgpu_int_grad_n_dot_tensor2_dv_planar(m_dNx.data(), m_vol.data(), qt.data(),
+                                                         m_nelem, m_nip, ev.data(), nullptr),
+                  "int_gradN_dot_tensor2_dV");
+        else
+            check(gfgpu_int_grad_n_dot_tensor2_dv(m_dNx.data(), m_vol.data(), qt.data(), m_nelem,
+                                                  NNE, m_nip, ND, ev.data(), nullptr),
+                  "int_gradN_dot_tensor2_dV");
     }
     array<double> Int_gradN_dot_tensor2_dV(const array<double>& qt) const
     {
@@ -540,9 +547,17 @@ public:
     void int_gradN_dot_tensor4_dot_gradNT_dV(const array<double>& qt, array<double>& em) const
     {
         require_shape(em.shape(), shape_elemmat(), "int_gradN_dot_tensor4_dot_gradNT_dV");
-        check(gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv(m_dNx.data(), m_vol.data(), qt.data(),
-                                                          m_nelem, NNE, m_nip, ND, em.data(), nullptr),
-              "int_gradN_dot_tensor4_dot_gradNT_dV");
+        int32_t t = tdim();
+        require_shape(qt.shape(), {m_nelem, m_nip, t, t, t, t}, "int_gradN_dot_tensor4_dot_gradNT_dV");
+        if (m_planar)
+            check(gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv_planar(
+                      m_dNx.data(), m_vol.data(), qt.data(), m_nelem, m_nip, em.data(), nullptr),
+                  "int_gradN_dot_tensor4_dot_gradNT_dV");
+        else
+            check(gfgpu_int_grad_n_dot_tensor4_dot_grad_nt_dv(m_dNx.data(), m_vol.data(), qt.data(),
+                                                              m_nelem, NNE, m_nip, ND, em.data(),
+                                                              nullptr),
+                  "int_gradN_dot_tensor4_dot_gradNT_dV");
     }
     array<double> Int_gradN_dot_tensor4_dot_gradNT_dV(const array<double>& qt) const
     {
@@ -552,30 +567,48 @@ public:
     }
 
 protected:
-    using grad_fn = int (*)(const double*, const double*, int64_t, int32_t, int32_t, int32_t,
-                            double*, gfgpu_stream_t);
-    void grad(grad_fn f, const array<double>& ev, array<double>& q) const
+    // mode 0: GradN_vector, 1: GradN_vector_T, 2: SymGradN_vector
+    void grad(int mode, const array<double>& ev, array<double>& q) const
     {
         require_shape(ev.shape(), shape_elemvec(), "GradN_vector");
         require_shape(q.shape(), shape_qtensor2(), "GradN_vector");
-        check(f(m_dNx.data(), ev.data(), m_nelem, NNE, m_nip, ND, q.data(), nullptr), "GradN_vector");
+        int rc;
+        if (m_planar) {
+            auto f = mode == 0 ? gfgpu_grad_n_vector_planar
+                               : (mode == 1 ? gfgpu_grad_n_vector_T_planar : gfgpu_sym_grad_n_vector_planar);
+            rc = f(m_dNx.data(), ev.data(), m_nelem, m_nip, q.data(), nullptr);
+        }
+        else {
+            auto f = mode == 0 ? gfgpu_grad_n_vector
+                               : (mode == 1 ? gfgpu_grad_n_vector_T : gfgpu_sym_grad_n_vector);
+            rc = f(m_dNx.data(), ev.data(), m_nelem, NNE, m_nip, ND, q.data(), nullptr);
+        }
+        check(rc, "GradN_vector");
     }
-    array<double> alloc2(grad_fn f, const array<double>& ev) const
+    array<double> alloc2(int mode, const array<double>& ev) const
     {
         array<double> q(shape_qtensor2());
-        grad(f, ev, q);
+        grad(mode, ev, q);
         return q;
     }
     void compute_dN()
     {
-        auto fn = NNE == 4 ? gfgpu_quad4_compute_dN : gfgpu_hex8_compute_dN;
-        check(fn(m_x.data(), m_nelem, m_xi.data(), m_w.data(), m_nip, m_N.data(), m_dNxi.data(),
-                 m_dNx.data(), m_vol.data(), nullptr),
-              "compute_dN");
+        int rc;
+        if (m_planar)
+            rc = gfgpu_quad4_planar_compute_dN(m_x.data(), m_nelem, m_xi.data(), m_w.data(), m_nip,
+                                               m_thick, m_N.data(), m_dNxi.data(), m_dNx.data(),
+                                               m_vol.data(), nullptr);
+        else
+            rc = (NNE == 4 ? gfgpu_quad4_compute_dN : gfgpu_hex8_compute_dN)(
+                m_x.data(), m_nelem, m_xi.data(), m_w.data(), m_nip, m_N.data(), m_dNxi.data(),
+                m_dNx.data(), m_vol.data(), nullptr);
+        check(rc, "compute_dN");
     }
     array<double> m_x, m_xi, m_w, m_N, m_dNxi, m_dNx, m_vol;
     int64_t m_nelem;
     int32_t m_nip;
+    bool m_planar;
+    double m_thick;
 };
 
 inline host::array<double> rule(int nip, int nd, double a)
@@ -608,6 +641,21 @@ public:
     explicit Quadrature(const array<double>& x) : detail::Quadrature<4, 2>(x, Gauss::xi(), Gauss::w()) {}
     Quadrature(const array<double>& x, const host::array<double>& xi, const host::array<double>& w)
         : detail::Quadrature<4, 2>(x, xi, w)
+    {
+    }
+};
+
+/* Element::Quad4::QuadraturePlanar (ElementQuad4Planar.h:38-335): 3x3 quadrature-point tensors
+ * (plane strain), out-of-plane thickness in dV. */
+class QuadraturePlanar : public detail::Quadrature<4, 2> {
+public:
+    explicit QuadraturePlanar(const array<double>& x, double thick = 1.0)
+        : detail::Quadrature<4, 2>(x, Gauss::xi(), Gauss::w(), true, thick)
+    {
+    }
+    QuadraturePlanar(const array<double>& x, const host::array<double>& xi,
+                     const host::array<double>& w, double thick = 1.0)
+        : detail::Quadrature<4, 2>(x, xi, w, true, thick)
     {
     }
 };

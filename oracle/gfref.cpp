@@ -551,6 +551,71 @@ void ref_int_grad_n_dot_tensor4_dot_grad_nt_dv(const double* dNx, const double* 
 }
 
 // ------------------------------------------------------------------------------------------------
+// Element::Quad4::QuadraturePlanar (ElementQuad4Planar.h): the Quad4 operators with 3x3
+// quadrature-point tensors (plane strain) and the out-of-plane thickness in the volume.
+// ------------------------------------------------------------------------------------------------
+
+// ElementQuad4Planar.h:81-123 + compute_dN_impl :280-318: the Quad4 Jacobian, inverse and dNx,
+// vol = w * det(J) * thick (:315), evaluated left to right.
+void ref_quad4_planar_compute_dN(const double* x, idx nelem, const double* xi, const double* w,
+                                 idx nip, double thick, double* dNx, double* vol)
+{
+    ref_quad4_compute_dN(x, nelem, xi, w, nip, dNx, vol);
+    for (idx t = 0; t < nelem * nip; ++t) vol[t] = vol[t] * thick;
+}
+
+// ElementQuad4Planar.h:130-221 (gradN_vector / gradN_vector_T / symGradN_vector): the output is
+// zero-filled [nelem, nip, 3, 3] and only the in-plane 2x2 block is written, with the Quad4
+// expressions (mode as in ref_grad_n_vector).
+void ref_grad_n_vector_planar(const double* dNx, const double* elemvec, idx nelem, idx nip,
+                              int mode, double* qtensor)
+{
+    std::vector<double> t2(static_cast<size_t>(nelem * nip * 4));
+    ref_grad_n_vector(dNx, elemvec, nelem, 4, nip, 2, mode, t2.data());
+    for (idx t = 0; t < nelem * nip; ++t) {
+        double* o = qtensor + t * 9;
+        for (int k = 0; k < 9; ++k) o[k] = 0.0;
+        o[0] = t2[t * 4 + 0];
+        o[1] = t2[t * 4 + 1];
+        o[3] = t2[t * 4 + 2];
+        o[4] = t2[t * 4 + 3];
+    }
+}
+
+// ElementQuad4Planar.h:254-277 (int_gradN_dot_tensor2_dV): reads sig(0,0), sig(1,0), sig(0,1),
+// sig(1,1) of each 3x3 tensor, with the Quad4 expression.
+void ref_int_grad_n_dot_tensor2_dv_planar(const double* dNx, const double* vol,
+                                          const double* qtensor, idx nelem, idx nip,
+                                          double* elemvec)
+{
+    std::vector<double> t2(static_cast<size_t>(nelem * nip * 4));
+    for (idx t = 0; t < nelem * nip; ++t) {
+        t2[t * 4 + 0] = qtensor[t * 9 + 0];
+        t2[t * 4 + 1] = qtensor[t * 9 + 1];
+        t2[t * 4 + 2] = qtensor[t * 9 + 3];
+        t2[t * 4 + 3] = qtensor[t * 9 + 4];
+    }
+    ref_int_grad_n_dot_tensor2_dv(dNx, vol, t2.data(), nelem, 4, nip, 2, elemvec);
+}
+
+// Element.h:1132-1176 (base int_gradN_dot_tensor4_dot_gradNT_dV) for QuadraturePlanar: the
+// tensor is viewed as [3,3,3,3] and i, j, k, l run over the two in-plane indices.
+void ref_int_grad_n_dot_tensor4_dot_grad_nt_dv_planar(const double* dNx, const double* vol,
+                                                      const double* qtensor, idx nelem, idx nip,
+                                                      double* elemmat)
+{
+    std::vector<double> t2(static_cast<size_t>(nelem * nip * 16));
+    for (idx t = 0; t < nelem * nip; ++t)
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k)
+                    for (int l = 0; l < 2; ++l)
+                        t2[t * 16 + ((i * 2 + j) * 2 + k) * 2 + l] =
+                            qtensor[t * 81 + ((i * 3 + j) * 3 + k) * 3 + l];
+    ref_int_grad_n_dot_tensor4_dot_grad_nt_dv(dNx, vol, t2.data(), nelem, 4, nip, 2, elemmat);
+}
+
+// ------------------------------------------------------------------------------------------------
 // Vector (Vector.h)
 // ------------------------------------------------------------------------------------------------
 

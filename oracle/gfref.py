@@ -235,6 +235,41 @@ def int_grad_n_dot_tensor4_dot_grad_nt_dv(dNx, vol, qtensor):
     return out
 
 
+def quad4_planar_compute_dN(x, xi, w, thick=1.0):
+    """QuadraturePlanar set-up: dNx [nelem,nip,4,2], vol including the thickness."""
+    x, xi, w = _f64(x), _f64(xi), _f64(w)
+    nelem, nip = x.shape[0], w.size
+    dNx = np.empty((nelem, nip, 4, 2))
+    vol = np.empty((nelem, nip))
+    _call("ref_quad4_planar_compute_dN", x, nelem, xi, w, nip, float(thick), dNx, vol)
+    return dNx, vol
+
+
+def grad_n_vector_planar(dNx, elemvec, mode):
+    """QuadraturePlanar GradN_vector (mode 0), _T (1), SymGradN_vector (2): [nelem,nip,3,3]."""
+    dNx, ev = _f64(dNx), _f64(elemvec)
+    nelem, nip = dNx.shape[:2]
+    out = np.empty((nelem, nip, 3, 3))
+    _call("ref_grad_n_vector_planar", dNx, ev, nelem, nip, mode, out)
+    return out
+
+
+def int_grad_n_dot_tensor2_dv_planar(dNx, vol, qtensor):
+    dNx, vol, qt = _f64(dNx), _f64(vol), _f64(qtensor)
+    nelem, nip = dNx.shape[:2]
+    out = np.empty((nelem, 4, 2))
+    _call("ref_int_grad_n_dot_tensor2_dv_planar", dNx, vol, qt, nelem, nip, out)
+    return out
+
+
+def int_grad_n_dot_tensor4_dot_grad_nt_dv_planar(dNx, vol, qtensor):
+    dNx, vol, qt = _f64(dNx), _f64(vol), _f64(qtensor)
+    nelem, nip = dNx.shape[:2]
+    out = np.empty((nelem, 8, 8))
+    _call("ref_int_grad_n_dot_tensor4_dot_grad_nt_dv_planar", dNx, vol, qt, nelem, nip, out)
+    return out
+
+
 # ---------------------------------------------------------------- vector
 
 

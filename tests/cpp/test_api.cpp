@@ -1,11 +1,13 @@
 // Drives the GooseFEM-compatible C++ interface (include/gfgpu/GooseFEM.hpp) through the 64x64
 // Quad4 force chain and the lumped mass, the way a GooseFEM user program would
 // (docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:32-86, 123-127):
-//   Vector(conn, dofs); Quadrature(vector.AsElement(coor)); asElement; symGradN_vector;
+//   Vector(conn, dofs); Quadrature(vector.AsElement(coor)); QuadraturePlanar(.., thick);
+//   asElement; symGradN_vector;
 //   stress; int_gradN_dot_tensor2_dV; assembleNode; MatrixDiagonal::assemble(Int_N_scalar_NT_dV).
 // Usage: test_api <inputs.bin> <outputs.bin>
 //   inputs:  nx (int64), K[nelem], G[nelem], u[nnode*2] (float64)
-//   outputs: dNx, vol, ue, eps, sig, fe, fint, M (float64, concatenated)
+//   outputs: dNx, vol, ue, eps, sig, fe, fint, M, then the planar dV, eps, sig, fe (float64,
+//   concatenated)
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -66,6 +68,17 @@ int main(int argc, char** argv)
         GF::MatrixDiagonal M(mesh.conn(), mesh.dofs());
         M.assemble(nodal.Int_N_scalar_NT_dV(GF::array<double>::from_host(rho)));
 
+        // QuadraturePlanar: 3x3 tensors, thickness 2
+        GF::Element::Quad4::QuadraturePlanar planar(
+            vector.AsElement(GF::array<double>::from_host(mesh.coor())), 2.0);
+        if (planar.tdim() != 3) return 4;
+        auto Eps3 = planar.SymGradN_vector(ue);
+        auto Sig3 = GF::array<double>(planar.shape_qtensor2());
+        GF::check(gfgpu_elastic_stress(Eps3.data(), Kd.data(), Gd.data(), nelem, planar.nip(), 3,
+                                       Sig3.data(), nullptr),
+                  "stress");
+        auto fe3 = planar.Int_gradN_dot_tensor2_dV(Sig3);
+
         std::ofstream out(argv[2], std::ios::binary);
         dump(out, quad.GradN());
         dump(out, quad.dV());
@@ -75,6 +88,10 @@ int main(int argc, char** argv)
         dump(out, fe);
         dump(out, fint);
         dump(out, M.data());
+        dump(out, planar.dV());
+        dump(out, Eps3);
+        dump(out, Sig3);
+        dump(out, fe3);
 
         // error path: a shape mismatch is reported as std::runtime_error
         bool threw = false;

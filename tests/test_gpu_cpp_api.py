@@ -53,7 +53,11 @@ def test_cpp_api_force_chain_and_mass(oracle, tmp_path):
     _, voln = R.compute_dN(x, xin, win)
     Nn, _ = R.shape(xin)
     M = R.diag_assemble(conn, dofs, R.int_n_scalar_nt_dv(Nn, voln, np.ones((nelem, 4)), 2))
-    expect = [dNx, vol, ue, eps, sig, fe, fint, M]
+    _, vol3 = R.quad4_planar_compute_dN(x, *R.quad4_gauss(), thick=2.0)
+    eps3 = R.grad_n_vector_planar(dNx, ue, 2)
+    sig3 = R.elastic_stress(eps3, K, G)
+    fe3 = R.int_grad_n_dot_tensor2_dv_planar(dNx, vol3, sig3)
+    expect = [dNx, vol, ue, eps, sig, fe, fint, M, vol3, eps3, sig3, fe3]
     k = 0
     for ref in expect:
         got = data[k:k + ref.size].reshape(ref.shape)

@@ -156,6 +156,44 @@ def test_quadrature_operators(gf, oracle, strict, elem):
           R.int_grad_n_dot_tensor4_dot_grad_nt_dv(dNx_r, vol_r, C4), strict)
 
 
+@pytest.mark.parametrize("strict", [True, False])
+def test_quad4_planar_operators(gf, oracle, strict):
+    """Element::Quad4::QuadraturePlanar on a distorted mesh with thickness 1.7: dV, the 3x3
+    gradients, the plane-strain force chain (3-d stress incl. sigma_zz), Int_N_scalar_NT_dV and
+    the in-plane stiffness integral of a [3,3,3,3] tensor, against the oracle."""
+    gf.set_strict(strict)
+    R = oracle
+    mesh = gf.Mesh.Quad4.Regular(7, 5)
+    coor = mesh.coor() + seeded_field((mesh.nnode(), 2), 16, amp=0.15)
+    conn, dofs = mesh.conn(), mesh.dofs()
+    vector = gf.Vector(conn, dofs)
+    quad = gf.Element.Quad4.QuadraturePlanar(vector.AsElement(coor), thick=1.7)
+    assert quad.tdim() == 3 and quad.shape_qtensor(2) == (mesh.nelem(), 4, 3, 3)
+    xr = R.as_element(conn, coor)
+    dNx_r, vol_r = R.quad4_planar_compute_dN(xr, *R.quad4_gauss(), thick=1.7)
+    assert np.array_equal(to_np(quad.GradN()), dNx_r)
+    assert np.array_equal(to_np(quad.dV()), vol_r)
+    u = seeded_field((mesh.nnode(), 2), 17)
+    ue_r = R.as_element(conn, u)
+    ue = vector.AsElement(u)
+    for mode, fn in enumerate((quad.GradN_vector, quad.GradN_vector_T, quad.SymGradN_vector)):
+        _same(to_np(fn(ue)), R.grad_n_vector_planar(dNx_r, ue_r, mode), strict)
+    K, G = seeded_material(mesh.nelem(), 18)
+    eps_r = R.grad_n_vector_planar(dNx_r, ue_r, 2)
+    sig = gf.elastic_stress(quad.SymGradN_vector(ue), K, G)
+    sig_r = R.elastic_stress(eps_r, K, G)
+    _same(to_np(sig), sig_r, strict)
+    assert np.abs(sig_r[..., 2, 2]).max() > 0.0  # plane strain: sigma_zz != 0
+    _same(to_np(quad.Int_gradN_dot_tensor2_dV(sig)),
+          R.int_grad_n_dot_tensor2_dv_planar(dNx_r, vol_r, sig_r), strict)
+    N_r, _ = R.shape(R.quad4_gauss()[0])
+    qs = seeded_field((mesh.nelem(), 4), 19)
+    _same(to_np(quad.Int_N_scalar_NT_dV(qs)), R.int_n_scalar_nt_dv(N_r, vol_r, qs, 2), strict)
+    C4 = seeded_field((mesh.nelem(), 4) + (3,) * 4, 20)
+    _same(to_np(quad.Int_gradN_dot_tensor4_dot_gradNT_dV(C4)),
+          R.int_grad_n_dot_tensor4_dot_grad_nt_dv_planar(dNx_r, vol_r, C4), strict)
+
+
 def test_vector_periodic(gf, oracle):
     """Vector conversions with periodic dofs (ties): asDofs (last writer wins), asNode,
     assembleDofs (nodevec and elemvec) and assembleNode are bit-exact."""

@@ -193,3 +193,51 @@ def test_hex8_compute_dn_index_anomaly_is_inert_on_boxes(oracle):
     Jinv = np.linalg.inv(J)
     textbook = np.einsum("eqij,qmj->eqmi", Jinv, dNxi)
     assert np.allclose(dNx, textbook, rtol=1e-14, atol=0)
+
+
+def test_quad4_planar_properties(oracle):
+    # tests/basic/ElementQuad4Planar.cpp:8-207: shapes, dV = 0.25 (x thickness), 3x3 GradN_vector
+    # (F^T), GradN_vector_T (F), SymGradN_vector and its volume average, lumped mass = 1 on
+    # periodic dofs, equilibrium of a homogeneous strain.
+    coor, conn = oracle.quad4_regular(3, 3)
+    xi, w = oracle.quad4_gauss()
+    x = oracle.as_element(conn, coor)
+    dNx, vol = oracle.quad4_planar_compute_dN(x, xi, w)
+    assert dNx.shape == (9, 4, 4, 2) and np.allclose(vol, 0.25)
+    dNq, volq = oracle.compute_dN(x, xi, w)
+    assert np.array_equal(dNx, dNq) and np.array_equal(vol, volq)
+    _, vol2 = oracle.quad4_planar_compute_dN(x, xi, w, thick=2.5)
+    assert np.array_equal(vol2, volq * 2.5)
+    F = np.zeros((3, 3))
+    F[0, 1] = 0.1
+    ue = oracle.as_element(conn, coor @ F[:2, :2].T)
+    g = oracle.grad_n_vector_planar(dNx, ue, 0)
+    gT = oracle.grad_n_vector_planar(dNx, ue, 1)
+    eps = oracle.grad_n_vector_planar(dNx, ue, 2)
+    assert g.shape == (9, 4, 3, 3)
+    assert np.allclose(g, F.T) and np.allclose(gT, F) and np.allclose(eps, 0.5 * (F + F.T))
+    epsbar = np.average(eps, axis=(0, 1), weights=np.broadcast_to(vol[..., None, None], eps.shape))
+    assert np.allclose(epsbar, 0.5 * (F + F.T))
+    # the in-plane blocks are the Quad4 operators bit for bit; everything else is 0
+    for mode in (0, 1, 2):
+        q4 = oracle._grad(dNq, ue, mode)
+        p = oracle.grad_n_vector_planar(dNx, ue, mode)
+        assert np.array_equal(p[..., :2, :2], q4)
+        assert not p[..., 2, :].any() and not p[..., :, 2].any()
+    dofs = oracle.dofs_periodic(16, 2, oracle.quad4_nodes_periodic(3, 3))
+    xin, wn = oracle.quad4_nodal()
+    Nn, _ = oracle.shape(xin)
+    _, voln = oracle.quad4_planar_compute_dN(x, xin, wn)
+    M = oracle.int_n_scalar_nt_dv(Nn, voln, np.ones((9, 4)), 2)
+    A = oracle.diag_assemble(conn, dofs, M)
+    assert np.allclose(A, 1.0)
+    fe = oracle.int_grad_n_dot_tensor2_dv_planar(dNx, vol, eps)
+    fi = oracle.assemble_dofs_elemvec(conn, dofs, fe)
+    assert np.allclose(fi, 0.0)
+    # stiffness: the in-plane block of a 3x3x3x3 tensor, equal to the Quad4 integral
+    rng = np.random.default_rng(3)
+    C3 = rng.normal(size=(9, 4, 3, 3, 3, 3))
+    Kp = oracle.int_grad_n_dot_tensor4_dot_grad_nt_dv_planar(dNx, vol, C3)
+    C2 = np.ascontiguousarray(C3[..., :2, :2, :2, :2])
+    Kq = oracle.int_grad_n_dot_tensor4_dot_grad_nt_dv(dNq, volq, C2)
+    assert np.array_equal(Kp, Kq)
