@@ -1,0 +1,432 @@
+// Assembled sparse matrices on the device: GooseFEM's Matrix and MatrixPartitioned (Matrix.h,
+// MatrixPartitioned.h) as CSR. The pattern and, per nonzero, the list of element-matrix entries
+// that land on it (in the order Eigen's setFromTriplets sums them: the triplet push order) are
+// built once on the host (gfgpu_host_matrix_pattern). Assembly is then a deterministic gather:
+// bit-exact in strict mode. Products follow Eigen's column-major sparse x dense product (per row
+// a sum from zero in ascending column order); the partitioned product sums the unknown and the
+// prescribed columns apart and adds them, as B_u = A_uu X_u + A_up X_p does. The solve of the
+// unknown block (MatrixPartitionedSolver, Eigen SimplicialLDLT in the reference) is a Jacobi-PCG
+// with fixed-order reductions, replayed as a CUDA graph.
+#include "common.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace gfgpu {
+
+namespace {
+
+constexpr int kMRed = 1024; // fixed grid of the solver reductions
+
+// MatrixPartitioned.h:156-200 / Matrix.h:704-733 through setFromTriplets: first entry, then +=
+template <bool S>
+__global__ void k_matrix_assemble(const int32_t* __restrict__ cptr, const int32_t* __restrict__ cidx,
+                                  int64_t nnz, const double* __restrict__ elemmat,
+                                  double* __restrict__ val)
+{
+    GF_FOR(k, nnz)
+    {
+        int32_t q0 = cptr[k], q1 = cptr[k + 1];
+        double acc = elemmat[cidx[q0]];
+        for (int32_t q = q0 + 1; q < q1; ++q) acc = add<S>(acc, elemmat[cidx[q]]);
+        val[k] = acc;
+    }
+}
+
+// b = A x on dofval (Matrix.h:810-815)
+template <bool S>
+__global__ void k_matrix_dot(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                             const double* __restrict__ val, int64_t n, const double* __restrict__ x,
+                             double* __restrict__ b)
+{
+    GF_FOR(r, n)
+    {
+        double acc = 0.0;
+        for (int32_t k = rowptr[r]; k < rowptr[r + 1]; ++k) acc = madd<S>(val[k], x[col[k]], acc);
+        b[r] = acc;
+    }
+}
+
+// Partitioned rows [r0, r1): b[iperm[r]] = (A_.u x_u) + (A_.p x_p), x and b dofval in the
+// original numbering, iperm[p] = original dof of partitioned index p
+// (MatrixPartitioned.h:378-398 dot, :421-433 reaction)
+template <bool S>
+__global__ void k_matrixp_rows(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                               const double* __restrict__ val, int64_t r0, int64_t r1, int64_t nnu,
+                               const int32_t* __restrict__ iperm, const double* __restrict__ x,
+                               double* __restrict__ b)
+{
+    GF_FOR(t, r1 - r0)
+    {
+        int64_t r = r0 + t;
+        double su = 0.0, sp = 0.0;
+        for (int32_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+            int32_t c = col[k];
+            if (c < nnu) su = madd<S>(val[k], x[iperm[c]], su);
+            else sp = madd<S>(val[k], x[iperm[c]], sp);
+        }
+        b[iperm[r]] = add<S>(su, sp);
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = lane < static_cast<int>(blockDim.x >> 5) ? sh[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+    }
+    __syncthreads();
+    return r;
+}
+
+// ---------------------------------------------------------------- Jacobi-PCG on A_uu
+
+enum { M_RZ = 0, M_RR, M_PQ, M_BB, M_ALPHA, M_BETA, M_COUNT };
+
+// rhs = b_u - A_up x_p, r = rhs - A_uu x_u, z = D^-1 r, p = z (x_u from x); partials rhs.rhs,
+// r.z, r.r
+__global__ void __launch_bounds__(256)
+k_mp_init(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+          const double* __restrict__ val, int64_t nnu, const int32_t* __restrict__ iperm,
+          const double* __restrict__ b, const double* __restrict__ x, double* __restrict__ xu,
+          double* __restrict__ dinv, double* __restrict__ r, double* __restrict__ z,
+          double* __restrict__ p, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double bb = 0.0, rz = 0.0, rr = 0.0;
+    GF_FOR(i, nnu)
+    {
+        double su = 0.0, sp = 0.0, d = 0.0;
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            int32_t c = col[k];
+            double xv = x[iperm[c]];
+            if (c < nnu) su = fma(val[k], xv, su);
+            else sp = fma(val[k], xv, sp);
+            if (c == i) d = val[k];
+        }
+        double rhs = b[iperm[i]] - sp;
+        double rv = rhs - su;
+        double di = 1.0 / d;
+        double zv = di * rv;
+        xu[i] = x[iperm[i]];
+        dinv[i] = di;
+        r[i] = rv;
+        z[i] = zv;
+        p[i] = zv;
+        bb = fma(rhs, rhs, bb);
+        rz = fma(rv, zv, rz);
+        rr = fma(rv, rv, rr);
+    }
+    double s0 = block_sum(bb, sh), s1 = block_sum(rz, sh), s2 = block_sum(rr, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = s0;
+        partial[kMRed + blockIdx.x] = s1;
+        partial[2 * kMRed + blockIdx.x] = s2;
+    }
+}
+
+// q = A_uu p (the row's columns < nnu; columns are sorted); partial p.q
+__global__ void __launch_bounds__(256)
+k_mp_spmv(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+          const double* __restrict__ val, int64_t nnu, const double* __restrict__ p,
+          double* __restrict__ q, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double pq = 0.0;
+    GF_FOR(i, nnu)
+    {
+        double acc = 0.0;
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            int32_t c = col[k];
+            if (c >= nnu) break;
+            acc = fma(val[k], p[c], acc);
+        }
+        q[i] = acc;
+        pq = fma(p[i], acc, pq);
+    }
+    double s = block_sum(pq, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// sc[dst0 + row] = fixed-order sum of partial row `row`, rows [0, nrows); with_alpha: then
+// alpha = r.z / p.q
+__global__ void k_mp_reduce(const double* __restrict__ partial, int nrows, double* __restrict__ sc,
+                            int dst0, int with_alpha)
+{
+    __shared__ double sh[32];
+    for (int row = 0; row < nrows; ++row) {
+        double v = 0.0;
+        for (int i = threadIdx.x; i < kMRed; i += blockDim.x) v += partial[row * kMRed + i];
+        double s = block_sum(v, sh);
+        if (threadIdx.x == 0) sc[dst0 + row] = s;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && with_alpha) sc[M_ALPHA] = sc[M_RZ] / sc[M_PQ];
+}
+
+// x_u += alpha p, r -= alpha q, z = D^-1 r; partials r.z, r.r
+__global__ void __launch_bounds__(256)
+k_mp_update(int64_t nnu, const double* __restrict__ dinv, const double* __restrict__ p,
+            const double* __restrict__ q, const double* __restrict__ sc, double* __restrict__ xu,
+            double* __restrict__ r, double* __restrict__ z, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double alpha = sc[M_ALPHA];
+    double rz = 0.0, rr = 0.0;
+    GF_FOR(i, nnu)
+    {
+        xu[i] = fma(alpha, p[i], xu[i]);
+        double rv = fma(-alpha, q[i], r[i]);
+        double zv = dinv[i] * rv;
+        r[i] = rv;
+        z[i] = zv;
+        rz = fma(rv, zv, rz);
+        rr = fma(rv, rv, rr);
+    }
+    double s0 = block_sum(rz, sh), s1 = block_sum(rr, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = s0;
+        partial[kMRed + blockIdx.x] = s1;
+    }
+}
+
+// r.z_new, r.r from the update's partials; beta = r.z_new / r.z
+__global__ void k_mp_beta(const double* __restrict__ partial, double* __restrict__ sc)
+{
+    __shared__ double sh[32];
+    double v0 = 0.0, v1 = 0.0;
+    for (int i = threadIdx.x; i < kMRed; i += blockDim.x) {
+        v0 += partial[i];
+        v1 += partial[kMRed + i];
+    }
+    double rz = block_sum(v0, sh);
+    double rr = block_sum(v1, sh);
+    if (threadIdx.x == 0) {
+        sc[M_BETA] = rz / sc[M_RZ];
+        sc[M_RZ] = rz;
+        sc[M_RR] = rr;
+    }
+}
+
+__global__ void k_mp_direction(int64_t nnu, const double* __restrict__ z,
+                               const double* __restrict__ sc, double* __restrict__ p)
+{
+    double beta = sc[M_BETA];
+    GF_FOR(i, nnu) p[i] = fma(beta, p[i], z[i]);
+}
+
+__global__ void k_mp_scatter(int64_t nnu, const int32_t* __restrict__ iperm,
+                             const double* __restrict__ xu, double* __restrict__ x)
+{
+    GF_FOR(i, nnu) x[iperm[i]] = xu[i];
+}
+
+// true residual of the unknown block: r = (b_u - A_up x_p) - A_uu x_u; partial r.r
+__global__ void __launch_bounds__(256)
+k_mp_residual(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+              const double* __restrict__ val, int64_t nnu, const int32_t* __restrict__ iperm,
+              const double* __restrict__ b, const double* __restrict__ x,
+              double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double rr = 0.0;
+    GF_FOR(i, nnu)
+    {
+        double su = 0.0, sp = 0.0;
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            int32_t c = col[k];
+            if (c < nnu) su = fma(val[k], x[iperm[c]], su);
+            else sp = fma(val[k], x[iperm[c]], sp);
+        }
+        double rv = (b[iperm[i]] - sp) - su;
+        rr = fma(rv, rv, rr);
+    }
+    double s = block_sum(rr, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+struct MpWs {
+    double *xu, *dinv, *r, *z, *p, *q, *partial, *sc;
+};
+
+inline int64_t a256(int64_t b)
+{
+    return (b + 255) / 256 * 256;
+}
+
+inline MpWs carve_mp(int64_t nnu, void* ws)
+{
+    char* c = static_cast<char*>(ws);
+    MpWs w;
+    double** v[] = {&w.xu, &w.dinv, &w.r, &w.z, &w.p, &w.q};
+    for (auto b : v) {
+        *b = reinterpret_cast<double*>(c);
+        c += a256(nnu * 8);
+    }
+    w.partial = reinterpret_cast<double*>(c);
+    c += a256(3 * kMRed * 8);
+    w.sc = reinterpret_cast<double*>(c);
+    return w;
+}
+
+} // namespace
+
+} // namespace gfgpu
+
+using namespace gfgpu;
+
+extern "C" {
+
+int gfgpu_matrix_assemble(const int32_t* cptr, const int32_t* cidx, int64_t nnz,
+                          const double* elemmat, double* val, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(cptr && cidx && elemmat && val && nnz >= 0 && !too_big(nnz), "bad argument");
+    if (nnz == 0) return GFGPU_OK;
+    if (strict_mode())
+        k_matrix_assemble<true><<<grid_for(nnz), kBlock, 0, S(stream)>>>(cptr, cidx, nnz, elemmat, val);
+    else
+        k_matrix_assemble<false><<<grid_for(nnz), kBlock, 0, S(stream)>>>(cptr, cidx, nnz, elemmat, val);
+    return check_launch("matrix_assemble");
+}
+
+int gfgpu_matrix_dot_dofval(const int32_t* rowptr, const int32_t* col, const double* val, int64_t n,
+                            const double* x, double* b, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(rowptr && col && val && x && b && n >= 0 && !too_big(n), "bad argument");
+    if (n == 0) return GFGPU_OK;
+    if (strict_mode())
+        k_matrix_dot<true><<<grid_for(n), kBlock, 0, S(stream)>>>(rowptr, col, val, n, x, b);
+    else
+        k_matrix_dot<false><<<grid_for(n), kBlock, 0, S(stream)>>>(rowptr, col, val, n, x, b);
+    return check_launch("matrix_dot");
+}
+
+static int matrixp_rows(const int32_t* rowptr, const int32_t* col, const double* val, int64_t ndof,
+                        int64_t nnu, const int32_t* iperm, const double* x, double* b, int64_t r0,
+                        gfgpu_stream_t stream)
+{
+    GF_REQUIRE(rowptr && col && val && iperm && x && b && nnu >= 0 && nnu <= ndof && !too_big(ndof),
+               "bad argument");
+    GF_REQUIRE(x != b, "x and b must not alias");
+    if (ndof - r0 <= 0) return GFGPU_OK;
+    unsigned g = grid_for(ndof - r0);
+    if (strict_mode())
+        k_matrixp_rows<true><<<g, kBlock, 0, S(stream)>>>(rowptr, col, val, r0, ndof, nnu, iperm, x, b);
+    else
+        k_matrixp_rows<false><<<g, kBlock, 0, S(stream)>>>(rowptr, col, val, r0, ndof, nnu, iperm, x, b);
+    return check_launch("matrixp product");
+}
+
+int gfgpu_matrixp_dot_dofval(const int32_t* rowptr, const int32_t* col, const double* val,
+                             int64_t ndof, int64_t nnu, const int32_t* iperm, const double* x,
+                             double* b, gfgpu_stream_t stream)
+{
+    return matrixp_rows(rowptr, col, val, ndof, nnu, iperm, x, b, 0, stream);
+}
+
+int gfgpu_matrixp_reaction_dofval(const int32_t* rowptr, const int32_t* col, const double* val,
+                                  int64_t ndof, int64_t nnu, const int32_t* iperm, const double* x,
+                                  double* b, gfgpu_stream_t stream)
+{
+    return matrixp_rows(rowptr, col, val, ndof, nnu, iperm, x, b, nnu, stream);
+}
+
+int64_t gfgpu_matrixp_solve_workspace_bytes(int64_t nnu)
+{
+    return nnu < 0 ? 0 : 6 * a256(nnu * 8) + a256(3 * kMRed * 8) + a256(M_COUNT * 8);
+}
+
+int gfgpu_matrixp_solve(const int32_t* rowptr, const int32_t* col, const double* val, int64_t ndof,
+                        int64_t nnu, const int32_t* iperm, const double* b, double* x, double tol,
+                        int64_t maxiter, int32_t check_every, void* workspace,
+                        gfgpu_stream_t stream, int64_t* iters, double* relres)
+{
+    GF_REQUIRE(rowptr && col && val && iperm && b && x && workspace && iters && relres,
+               "bad argument");
+    GF_REQUIRE(nnu > 0 && nnu <= ndof && !too_big(ndof) && tol > 0.0 && maxiter >= 0, "bad argument");
+    if (check_every < 1) check_every = 1;
+    cudaStream_t s = S(stream);
+    MpWs w = carve_mp(nnu, workspace);
+    const unsigned gb = kMRed;
+    double h[M_COUNT];
+    auto read = [&]() -> int {
+        GF_TRY(check_cuda(cudaMemcpyAsync(h, w.sc, sizeof(h), cudaMemcpyDeviceToHost, s), "copy"));
+        return check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    };
+    auto iteration = [&](cudaStream_t st) {
+        k_mp_spmv<<<gb, 256, 0, st>>>(rowptr, col, val, nnu, w.p, w.q, w.partial);
+        k_mp_reduce<<<1, 1024, 0, st>>>(w.partial, 1, w.sc, M_PQ, 1);
+        k_mp_update<<<gb, 256, 0, st>>>(nnu, w.dinv, w.p, w.q, w.sc, w.xu, w.r, w.z, w.partial);
+        k_mp_beta<<<1, 1024, 0, st>>>(w.partial, w.sc);
+        k_mp_direction<<<grid_for(nnu), kBlock, 0, st>>>(nnu, w.z, w.sc, w.p);
+    };
+    k_mp_init<<<gb, 256, 0, s>>>(rowptr, col, val, nnu, iperm, b, x, w.xu, w.dinv, w.r, w.z, w.p,
+                                 w.partial);
+    // rows 0, 1, 2 = rhs.rhs, r.z, r.r -> M_BB, M_RZ, M_RR
+    k_mp_reduce<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, M_BB, 0);
+    k_mp_reduce<<<1, 1024, 0, s>>>(w.partial + kMRed, 1, w.sc, M_RZ, 0);
+    k_mp_reduce<<<1, 1024, 0, s>>>(w.partial + 2 * kMRed, 1, w.sc, M_RR, 0);
+    GF_TRY(check_launch("matrixp_solve set-up"));
+    GF_TRY(read());
+    double bnorm = std::sqrt(h[M_BB]);
+    if (bnorm == 0.0) bnorm = 1.0;
+    double rel = std::sqrt(h[M_RR]) / bnorm;
+    int64_t it = 0;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cs = nullptr;
+    int rc = GFGPU_OK;
+    while (rel > tol && it < maxiter) {
+        int64_t nb = std::min<int64_t>(check_every, maxiter - it);
+        if (nb == check_every && !exec) {
+            rc = check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate");
+            cudaGraph_t graph = nullptr;
+            if (rc == GFGPU_OK)
+                rc = check_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
+            if (rc == GFGPU_OK) {
+                for (int64_t k = 0; k < nb; ++k) iteration(cs);
+                rc = check_cuda(cudaStreamEndCapture(cs, &graph), "cudaStreamEndCapture");
+                if (rc == GFGPU_OK)
+                    rc = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+                if (graph) cudaGraphDestroy(graph);
+            }
+            if (rc != GFGPU_OK) break;
+        }
+        if (nb == check_every) {
+            rc = check_cuda(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+        }
+        else {
+            for (int64_t k = 0; k < nb; ++k) iteration(s);
+            rc = check_launch("matrixp_solve iteration");
+        }
+        if (rc != GFGPU_OK) break;
+        it += nb;
+        rc = read();
+        if (rc != GFGPU_OK) break;
+        if (!std::isfinite(h[M_RR])) {
+            rc = fail(GFGPU_ERR_NAN, "gfgpu_matrixp_solve: non-finite residual");
+            break;
+        }
+        rel = std::sqrt(h[M_RR]) / bnorm;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (cs) cudaStreamDestroy(cs);
+    *iters = it;
+    GF_TRY(rc);
+    k_mp_scatter<<<grid_for(nnu), kBlock, 0, s>>>(nnu, iperm, w.xu, x);
+    k_mp_residual<<<gb, 256, 0, s>>>(rowptr, col, val, nnu, iperm, b, x, w.partial);
+    k_mp_reduce<<<1, 1024, 0, s>>>(w.partial, 1, w.sc, M_RR, 0);
+    GF_TRY(check_launch("matrixp_solve residual"));
+    GF_TRY(read());
+    *relres = std::sqrt(h[M_RR]) / bnorm;
+    if (*relres > tol) return fail(GFGPU_ERR_DIVERGED, "gfgpu_matrixp_solve: tolerance not reached");
+    return GFGPU_OK;
+}
+
+} // extern "C"

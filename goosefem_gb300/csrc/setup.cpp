@@ -302,6 +302,66 @@ int gfgpu_host_dof_csr(const int32_t* conn, const int32_t* dofs, int64_t nelem, 
     return GFGPU_OK;
 }
 
+int gfgpu_host_matrix_pattern(const int32_t* conn, const int32_t* dmap, int64_t nelem, int32_t nne,
+                              int64_t nnode, int32_t ndim, int64_t n, int32_t* rowptr,
+                              int32_t* col, int32_t* cptr, int32_t* cidx, int64_t* nnz)
+{
+    HREQ(conn && dmap && rowptr && col && cptr && cidx && nnz && nne > 0 && ndim > 0 && n >= 0,
+         "bad argument");
+    const int64_t K = int64_t(nne) * ndim;
+    const int64_t total = nelem * K * K;
+    HREQ(fits32(total) && fits32(n), "too large for int32 tables");
+    for (int64_t k = 0; k < nelem * nne; ++k)
+        if (conn[k] < 0 || conn[k] >= nnode)
+            return fail(GFGPU_ERR_INDEX, "gfgpu_host_matrix_pattern: conn out of range");
+    for (int64_t k = 0; k < nnode * ndim; ++k)
+        if (dmap[k] < 0 || dmap[k] >= n)
+            return fail(GFGPU_ERR_INDEX, "gfgpu_host_matrix_pattern: dof out of range");
+    // (row, col) of the triplet with flat elemmat index f = (e K + m ndim + i) K + n ndim + j: the
+    // push order of Matrix.h:704-733 / MatrixPartitioned.h:156-200
+    auto rc = [&](int64_t f, int32_t& r, int32_t& c) {
+        int64_t e = f / (K * K), rem = f % (K * K);
+        int64_t a = rem / K, b = rem % K;
+        r = dmap[int64_t(conn[e * nne + a / ndim]) * ndim + a % ndim];
+        c = dmap[int64_t(conn[e * nne + b / ndim]) * ndim + b % ndim];
+    };
+    // bucket by row, stable in f
+    std::vector<int64_t> start(n + 1, 0);
+    for (int64_t f = 0; f < total; ++f) {
+        int32_t r, c;
+        rc(f, r, c);
+        start[r + 1] += 1;
+    }
+    for (int64_t r = 0; r < n; ++r) start[r + 1] += start[r];
+    std::vector<int64_t> cur(start.begin(), start.end() - 1);
+    std::vector<int32_t> colof(total);
+    for (int64_t f = 0; f < total; ++f) {
+        int32_t r, c;
+        rc(f, r, c);
+        cidx[cur[r]++] = static_cast<int32_t>(f);
+        colof[f] = c;
+    }
+    // within a row: stable by column (triplet order kept among duplicates), then one nonzero per
+    // distinct column
+    int64_t k = 0;
+    rowptr[0] = 0;
+    for (int64_t r = 0; r < n; ++r) {
+        std::stable_sort(cidx + start[r], cidx + start[r + 1],
+                         [&](int32_t a, int32_t b) { return colof[a] < colof[b]; });
+        for (int64_t q = start[r]; q < start[r + 1]; ++q) {
+            if (q == start[r] || colof[cidx[q]] != colof[cidx[q - 1]]) {
+                col[k] = colof[cidx[q]];
+                cptr[k] = static_cast<int32_t>(q);
+                ++k;
+            }
+        }
+        rowptr[r + 1] = static_cast<int32_t>(k);
+    }
+    cptr[k] = static_cast<int32_t>(total);
+    *nnz = k;
+    return GFGPU_OK;
+}
+
 int gfgpu_host_dof_csr_nodevec(const int32_t* dofs, int64_t nnode, int32_t ndim, int64_t ndof,
                                int32_t* ptr, int32_t* idx)
 {

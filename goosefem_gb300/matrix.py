@@ -213,3 +213,196 @@ class MatrixDiagonalPartitioned(MatrixDiagonal):
         _lib.call("gfgpu_diag_dot_nodevec", self.part_d.data_ptr(), self._nnode, self._ndim,
                   self._App.data_ptr(), x.data_ptr(), b.data_ptr(), _dev.stream())
         return b
+
+
+def _pattern(conn_h, dmap_h, nnode, n):
+    """CSR pattern and per-nonzero triplet lists (gfgpu_host_matrix_pattern)."""
+    import ctypes as C
+
+    nelem, nne = conn_h.shape
+    nd = dmap_h.shape[1]
+    total = nelem * (nne * nd) ** 2
+    rowptr = np.empty(n + 1, dtype=np.int32)
+    col = np.empty(max(total, 1), dtype=np.int32)
+    cptr = np.empty(total + 1, dtype=np.int32)
+    cidx = np.empty(max(total, 1), dtype=np.int32)
+    nnz = C.c_int64(0)
+    _lib.call("gfgpu_host_matrix_pattern", conn_h.ctypes.data, dmap_h.ctypes.data, nelem, nne,
+              nnode, nd, n, rowptr.ctypes.data, col.ctypes.data, cptr.ctypes.data,
+              cidx.ctypes.data, C.addressof(nnz))
+    k = int(nnz.value)
+    return rowptr, col[:k].copy(), cptr[:k + 1].copy(), cidx[:total].copy()
+
+
+class Matrix:
+    """Matrix(conn, dofs) (Matrix.h:653-863): assembled sparse matrix in CSR on the device.
+    assemble() sums the element-matrix entries of each nonzero in the triplet order of
+    Matrix.h:704-733 (Eigen setFromTriplets), bit-exact in strict mode."""
+
+    def __init__(self, conn, dofs):
+        self._conn_h = _dev.host_i32(conn)
+        self._dofs_h = _dev.host_i32(dofs)
+        self._nelem, self._nne = self._conn_h.shape
+        self._nnode, self._ndim = self._dofs_h.shape
+        self._ndof = int(self._dofs_h.max()) + 1
+        self._setup(self._dofs_h)
+
+    def _setup(self, dmap):
+        rp, col, cptr, cidx = _pattern(self._conn_h, dmap, self._nnode, self._ndof)
+        self._rowptr_h, self._col_h = rp, col
+        self.rowptr, self.col = _dev.dev_i32(rp), _dev.dev_i32(col)
+        self.cptr, self.cidx = _dev.dev_i32(cptr), _dev.dev_i32(cidx)
+        self._nnz = int(col.size)
+        self._val = torch.zeros(self._nnz, dtype=torch.float64, device=_dev.device())
+
+    def nelem(self):
+        return self._nelem
+
+    def nne(self):
+        return self._nne
+
+    def nnode(self):
+        return self._nnode
+
+    def ndim(self):
+        return self._ndim
+
+    def ndof(self):
+        return self._ndof
+
+    def nnz(self):
+        return self._nnz
+
+    def shape_elemmat(self):
+        k = self._nne * self._ndim
+        return (self._nelem, k, k)
+
+    def assemble(self, elemmat):
+        em = _dev.dev_f64(elemmat)
+        _dev.check_shape(em, self.shape_elemmat(), "assemble")
+        _lib.call("gfgpu_matrix_assemble", self.cptr.data_ptr(), self.cidx.data_ptr(), self._nnz,
+                  em.data_ptr(), self._val.data_ptr(), _dev.stream())
+
+    def data(self):
+        """(rowptr, col, val) of the CSR (device)."""
+        return self.rowptr, self.col, self._val
+
+    def _csr_host(self):
+        return self._rowptr_h, self._col_h, self._val.cpu().numpy()
+
+    def Todense(self):
+        """Matrix::Todense (Matrix.h:350-372), host array in the original dof numbering."""
+        rp, col, val = self._csr_host()
+        A = np.zeros((self._ndof, self._ndof))
+        rows = np.repeat(np.arange(self._ndof), np.diff(rp))
+        A[rows, col] = val
+        return A
+
+    def _dofval(self, x):
+        from .vector import Vector
+
+        x = _dev.dev_f64(x)
+        if x.dim() == 1:
+            return x, None
+        v = Vector(self._conn_h, self._dofs_h)
+        return v.AsDofs(x), v
+
+    def Dot(self, x):
+        """Matrix::Dot (Matrix.h:376-409), dofval or nodevec."""
+        xd, v = self._dofval(x)
+        b = torch.empty(self._ndof, dtype=torch.float64, device=xd.device)
+        _lib.call("gfgpu_matrix_dot_dofval", self.rowptr.data_ptr(), self.col.data_ptr(),
+                  self._val.data_ptr(), self._ndof, xd.contiguous().data_ptr(), b.data_ptr(),
+                  _dev.stream())
+        return b if v is None else v.AsNode(b)
+
+
+class MatrixPartitioned(Matrix):
+    """MatrixPartitioned(conn, dofs, iip) (MatrixPartitioned.h:34-460): one CSR in the
+    partitioned numbering (unknowns first); the blocks uu, up, pu, pp are its index ranges."""
+
+    def __init__(self, conn, dofs, iip):
+        self._conn_h = _dev.host_i32(conn)
+        self._dofs_h = _dev.host_i32(dofs)
+        self._nelem, self._nne = self._conn_h.shape
+        self._nnode, self._ndim = self._dofs_h.shape
+        self._ndof = int(self._dofs_h.max()) + 1
+        self._iip = _dev.host_i32(iip)
+        self._iiu, self._part = _mesh.partition(self._dofs_h, self._iip)
+        self._nnu, self._nnp = int(self._iiu.size), int(self._iip.size)
+        self._iperm_h = np.concatenate([self._iiu, self._iip]).astype(np.int32)
+        self.iperm = _dev.dev_i32(self._iperm_h)
+        self._setup(self._part)
+
+    def nnu(self):
+        return self._nnu
+
+    def nnp(self):
+        return self._nnp
+
+    def iiu(self):
+        return self._iiu.copy()
+
+    def iip(self):
+        return self._iip.copy()
+
+    def Todense(self):
+        """MatrixPartitioned::Todense (MatrixPartitioned.h:324-351), original numbering."""
+        rp, col, val = self._csr_host()
+        A = np.zeros((self._ndof, self._ndof))
+        rows = np.repeat(np.arange(self._ndof), np.diff(rp))
+        A[self._iperm_h[rows], self._iperm_h[col]] = val
+        return A
+
+    def Dot(self, x):
+        """MatrixPartitioned::Dot (MatrixPartitioned.h:354-398), dofval or nodevec."""
+        xd, v = self._dofval(x)
+        b = torch.empty(self._ndof, dtype=torch.float64, device=xd.device)
+        _lib.call("gfgpu_matrixp_dot_dofval", self.rowptr.data_ptr(), self.col.data_ptr(),
+                  self._val.data_ptr(), self._ndof, self._nnu, self.iperm.data_ptr(),
+                  xd.contiguous().data_ptr(), b.data_ptr(), _dev.stream())
+        return b if v is None else v.AsNode(b)
+
+    def Reaction(self, x, b):
+        """MatrixPartitioned::Reaction (MatrixPartitioned.h:401-433): copy of b with
+        b_p = A_pu x_u + A_pp x_p, dofval or nodevec."""
+        xd, v = self._dofval(x)
+        bd, _ = self._dofval(b)
+        bd = bd.clone()
+        _lib.call("gfgpu_matrixp_reaction_dofval", self.rowptr.data_ptr(), self.col.data_ptr(),
+                  self._val.data_ptr(), self._ndof, self._nnu, self.iperm.data_ptr(),
+                  xd.contiguous().data_ptr(), bd.data_ptr(), _dev.stream())
+        return bd if v is None else v.AsNode(bd)
+
+
+class MatrixPartitionedSolver:
+    """MatrixPartitionedSolver (MatrixPartitioned.h:471-642): x_u = A_uu^-1 (b_u - A_up x_p).
+    The reference factorises A_uu (Eigen SimplicialLDLT); here a Jacobi-PCG on the assembled
+    A_uu in FP64 to a relative residual `tol` (gfgpu_matrixp_solve)."""
+
+    def __init__(self, tol=1e-12, maxiter=1000000, check_every=16):
+        self.tol, self.maxiter, self.check_every = float(tol), int(maxiter), int(check_every)
+        self.iterations = 0
+        self.relres = 0.0
+
+    def Solve(self, A, b, x):
+        """Copy of x with the unknown dofs solved (dofval or nodevec; x holds x_p)."""
+        import ctypes as C
+
+        xd, v = A._dofval(x)
+        bd, _ = A._dofval(b)
+        xd = xd.clone().contiguous()
+        nb = int(_lib.lib().gfgpu_matrixp_solve_workspace_bytes(A._nnu))
+        ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=xd.device)
+        it, rel = C.c_int64(0), C.c_double(0.0)
+        _lib.call("gfgpu_matrixp_solve", A.rowptr.data_ptr(), A.col.data_ptr(), A._val.data_ptr(),
+                  A._ndof, A._nnu, A.iperm.data_ptr(), bd.contiguous().data_ptr(), xd.data_ptr(),
+                  self.tol, self.maxiter, self.check_every, ws.data_ptr(), _dev.stream(),
+                  C.addressof(it), C.addressof(rel))
+        self.iterations, self.relres = int(it.value), float(rel.value)
+        return xd if v is None else v.AsNode(xd)
+
+    def solve(self, A, b, x):
+        out = self.Solve(A, b, x)
+        x.copy_(out)
+        return x

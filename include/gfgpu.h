@@ -387,6 +387,44 @@ int gfgpu_pcg_vector(const gfgpu_verlet_desc* d, void* workspace, int32_t which,
 int gfgpu_pcg_norms(const gfgpu_verlet_desc* d, const void* workspace, double* rr, double* bb,
                     gfgpu_stream_t stream);
 
+/* ============================ assembled sparse matrices ================================== */
+
+/* Matrix / MatrixPartitioned (Matrix.h:653-863, MatrixPartitioned.h:34-460) as CSR.
+ * Host set-up of the pattern: for the triplets pushed by Matrix::assemble_impl (Matrix.h:704-733;
+ * dmap = dofs, n = ndof) or MatrixPartitioned::assemble_impl (MatrixPartitioned.h:156-200;
+ * dmap = part, n = ndof, unknowns first: the blocks uu, up, pu, pp are index ranges of this one
+ * matrix), rowptr [n+1] and col [nnz] (columns ascending per row) and, per nonzero k, the flat
+ * elemmat indices cidx[cptr[k]:cptr[k+1]] that Eigen's setFromTriplets sums into it, in that
+ * order. col, cidx: capacity nelem*K*K, cptr: nelem*K*K + 1 (K = nne*ndim); *nnz on return. */
+int gfgpu_host_matrix_pattern(const int32_t* conn, const int32_t* dmap, int64_t nelem, int32_t nne,
+                              int64_t nnode, int32_t ndim, int64_t n, int32_t* rowptr,
+                              int32_t* col, int32_t* cptr, int32_t* cidx, int64_t* nnz);
+/* assemble(elemmat): val[k] = sum of the listed elemmat entries (first, then +=, in order). */
+int gfgpu_matrix_assemble(const int32_t* cptr, const int32_t* cidx, int64_t nnz,
+                          const double* elemmat, double* val, gfgpu_stream_t stream);
+/* Matrix::dot on dofval (Matrix.h:810-815): b = A x, per row from 0 in ascending columns. */
+int gfgpu_matrix_dot_dofval(const int32_t* rowptr, const int32_t* col, const double* val, int64_t n,
+                            const double* x, double* b, gfgpu_stream_t stream);
+/* MatrixPartitioned::dot / reaction on dofval (MatrixPartitioned.h:378-398, 421-433) on the
+ * partitioned CSR: per row (A_.u x_u) + (A_.p x_p); iperm [ndof]: original dof of partitioned
+ * index (iiu then iip); x, b in the original numbering (must not alias). dot writes every entry
+ * of b, reaction only the prescribed ones. */
+int gfgpu_matrixp_dot_dofval(const int32_t* rowptr, const int32_t* col, const double* val,
+                             int64_t ndof, int64_t nnu, const int32_t* iperm, const double* x,
+                             double* b, gfgpu_stream_t stream);
+int gfgpu_matrixp_reaction_dofval(const int32_t* rowptr, const int32_t* col, const double* val,
+                                  int64_t ndof, int64_t nnu, const int32_t* iperm, const double* x,
+                                  double* b, gfgpu_stream_t stream);
+/* MatrixPartitionedSolver::solve (MatrixPartitioned.h:583-613; Eigen SimplicialLDLT there):
+ * x_u = A_uu^-1 (b_u - A_up x_p) by Jacobi-PCG in FP64 to ||r|| <= tol ||b_u - A_up x_p||, from
+ * the initial guess in x; b, x dofval in the original numbering (x_p read from x, x_u written).
+ * check_every iterations replay as a CUDA graph. Deterministic. Synchronises. */
+int64_t gfgpu_matrixp_solve_workspace_bytes(int64_t nnu);
+int gfgpu_matrixp_solve(const int32_t* rowptr, const int32_t* col, const double* val, int64_t ndof,
+                        int64_t nnu, const int32_t* iperm, const double* b, double* x, double tol,
+                        int64_t maxiter, int32_t check_every, void* workspace,
+                        gfgpu_stream_t stream, int64_t* iters, double* relres);
+
 /* ============================ learned preconditioner (device) ============================= */
 
 /* The network: 4 convolution layers 3x3 on the nodal grid of a Regular Quad4 mesh (NHWC, the

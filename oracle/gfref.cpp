@@ -23,6 +23,8 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <utility>
 #include <vector>
 
 #ifdef _OPENMP
@@ -613,6 +615,77 @@ void ref_int_grad_n_dot_tensor4_dot_grad_nt_dv_planar(const double* dNx, const d
                         t2[t * 16 + ((i * 2 + j) * 2 + k) * 2 + l] =
                             qtensor[t * 81 + ((i * 3 + j) * 3 + k) * 3 + l];
     ref_int_grad_n_dot_tensor4_dot_grad_nt_dv(dNx, vol, t2.data(), nelem, 4, nip, 2, elemmat);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Assembled sparse matrices (Matrix.h, MatrixPartitioned.h). Eigen's setFromTriplets sums the
+// triplets of one (row, col) in the order they were pushed and stores every row's columns in
+// ascending order; restated with an ordered map. The matrix is returned as CSR.
+// ------------------------------------------------------------------------------------------------
+
+// Matrix::assemble_impl (Matrix.h:704-733) with dmap = dofs, or MatrixPartitioned::assemble_impl
+// (MatrixPartitioned.h:156-200) with dmap = part (the four blocks are the index ranges of the one
+// partitioned matrix: the triplet order within each block is the global order). First call with
+// rowptr == nullptr returns nnz; the second fills rowptr [n+1], col [nnz], val [nnz].
+idx ref_matrix_assemble(const idx* conn, const idx* dmap, idx nelem, idx nne, idx nd, idx n,
+                        const double* elemmat, idx* rowptr, idx* col, double* val)
+{
+    std::map<std::pair<idx, idx>, double> A;
+    idx K = nne * nd;
+    for (idx e = 0; e < nelem; ++e)
+        for (idx m = 0; m < nne; ++m)
+            for (idx i = 0; i < nd; ++i)
+                for (idx nn = 0; nn < nne; ++nn)
+                    for (idx j = 0; j < nd; ++j) {
+                        idx r = dmap[conn[e * nne + m] * nd + i];
+                        idx c = dmap[conn[e * nne + nn] * nd + j];
+                        double v = elemmat[(e * K + m * nd + i) * K + nn * nd + j];
+                        auto it = A.find({r, c});
+                        if (it == A.end()) A.emplace(std::make_pair(r, c), v);
+                        else it->second = it->second + v;
+                    }
+    if (!rowptr) return static_cast<idx>(A.size());
+    for (idx r = 0; r <= n; ++r) rowptr[r] = 0;
+    idx k = 0;
+    for (auto& kv : A) {
+        rowptr[kv.first.first + 1] += 1;
+        col[k] = kv.first.second;
+        val[k] = kv.second;
+        ++k;
+    }
+    for (idx r = 0; r < n; ++r) rowptr[r + 1] += rowptr[r];
+    return k;
+}
+
+// Matrix::dot_dofval_impl (Matrix.h:810-815): b = A x with Eigen's column-major product, i.e.
+// per row a sum from 0 of A(r,c) x(c) over ascending c.
+void ref_matrix_dot(const idx* rowptr, const idx* col, const double* val, idx n, const double* x,
+                    double* b)
+{
+    for (idx r = 0; r < n; ++r) {
+        double acc = 0.0;
+        for (idx k = rowptr[r]; k < rowptr[r + 1]; ++k) acc = acc + val[k] * x[col[k]];
+        b[r] = acc;
+    }
+}
+
+// MatrixPartitioned::dot_dofval_impl (MatrixPartitioned.h:378-398) on the partitioned CSR
+// (rows / columns < nnu: unknown): B = A_.u X_u + A_.p X_p (each product summed from 0, then
+// added); x and b dofval in the original numbering, part1d [ndof] the partitioned index of dof d.
+void ref_matrixp_dot(const idx* rowptr, const idx* col, const double* val, idx ndof, idx nnu,
+                     const idx* part1d, const double* x, double* b)
+{
+    std::vector<double> xp(ndof), bp(ndof);
+    for (idx d = 0; d < ndof; ++d) xp[part1d[d]] = x[d];
+    for (idx r = 0; r < ndof; ++r) {
+        double su = 0.0, sp = 0.0;
+        for (idx k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+            if (col[k] < nnu) su = su + val[k] * xp[col[k]];
+            else sp = sp + val[k] * xp[col[k]];
+        }
+        bp[r] = su + sp;
+    }
+    for (idx d = 0; d < ndof; ++d) b[d] = bp[part1d[d]];
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -270,6 +270,35 @@ def int_grad_n_dot_tensor4_dot_grad_nt_dv_planar(dNx, vol, qtensor):
     return out
 
 
+def matrix_assemble(conn, dmap, elemmat, n):
+    """Assembled sparse matrix (Eigen setFromTriplets semantics) as CSR (rowptr, col, val);
+    dmap: dofs (Matrix) or part (MatrixPartitioned), n: number of rows."""
+    conn, dm, em = _ix(conn), _ix(dmap), _f64(elemmat)
+    nelem, nne = conn.shape
+    nd = dm.shape[1]
+    nnz = _call("ref_matrix_assemble", conn, dm, nelem, nne, nd, n, em, None, None, None,
+                restype=_i64)
+    rowptr = np.empty(n + 1, dtype=np.int64)
+    col = np.empty(nnz, dtype=np.int64)
+    val = np.empty(nnz)
+    _call("ref_matrix_assemble", conn, dm, nelem, nne, nd, n, em, rowptr, col, val, restype=_i64)
+    return rowptr, col, val
+
+
+def matrix_dot(rowptr, col, val, x):
+    n = rowptr.size - 1
+    b = np.empty(n)
+    _call("ref_matrix_dot", _ix(rowptr), _ix(col), _f64(val), n, _f64(x), b)
+    return b
+
+
+def matrixp_dot(rowptr, col, val, nnu, part1d, x):
+    ndof = rowptr.size - 1
+    b = np.empty(ndof)
+    _call("ref_matrixp_dot", _ix(rowptr), _ix(col), _f64(val), ndof, nnu, _ix(part1d), _f64(x), b)
+    return b
+
+
 # ---------------------------------------------------------------- vector
 
 

@@ -154,3 +154,46 @@ def test_unit_element_stiffness_matches_oracle(lib, oracle):
         ref = A[np.ix_(perm, perm)]
         got = out[m * 64:(m + 1) * 64].reshape(8, 8)
         assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_matrix_pattern_matches_oracle(lib, oracle, periodic):
+    """gfgpu_host_matrix_pattern (host set-up of the assembled sparse matrix): CSR pattern equal
+    to the oracle's, and the per-nonzero triplet lists summed in order give the oracle's values
+    bit for bit (Eigen setFromTriplets order), with periodic dofs (repeated dofs in an element)."""
+    import ctypes as C
+
+    R = oracle
+    nx, ny = 5, 4
+    coor, conn = R.quad4_regular(nx, ny)
+    nnode = coor.shape[0]
+    if periodic:
+        dofs = R.dofs_periodic(nnode, 2, R.quad4_nodes_periodic(nx, ny))
+    else:
+        dofs = R.dofs(nnode, 2)
+    ndof = int(dofs.max()) + 1
+    rng = np.random.default_rng(4)
+    elemmat = rng.normal(size=(conn.shape[0], 8, 8))
+    rp_r, col_r, val_r = R.matrix_assemble(conn, dofs, elemmat, ndof)
+    total = conn.shape[0] * 64
+    rp = np.empty(ndof + 1, dtype=np.int32)
+    col = np.empty(total, dtype=np.int32)
+    cptr = np.empty(total + 1, dtype=np.int32)
+    cidx = np.empty(total, dtype=np.int32)
+    nnz = C.c_int64(0)
+    c32, d32 = conn.astype(np.int32), dofs.astype(np.int32)
+    lib.call("gfgpu_host_matrix_pattern", c32.ctypes.data, d32.ctypes.data, conn.shape[0], 4,
+             nnode, 2, ndof, rp.ctypes.data, col.ctypes.data, cptr.ctypes.data, cidx.ctypes.data,
+             C.addressof(nnz))
+    k = nnz.value
+    assert np.array_equal(rp, rp_r) and np.array_equal(col[:k], col_r)
+    flat = elemmat.ravel()
+    val = np.empty(k)
+    for j in range(k):
+        idx = cidx[cptr[j]:cptr[j + 1]]
+        acc = flat[idx[0]]
+        for q in idx[1:]:
+            acc = acc + flat[q]
+        val[j] = acc
+        assert np.all(np.diff(idx) > 0)  # triplet order
+    assert np.array_equal(val, val_r)
