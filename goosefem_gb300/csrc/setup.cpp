@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/gfgpu.h"
@@ -359,6 +360,127 @@ int gfgpu_host_matrix_pattern(const int32_t* conn, const int32_t* dmap, int64_t 
     }
     cptr[k] = static_cast<int32_t>(total);
     *nnz = k;
+    return GFGPU_OK;
+}
+
+int gfgpu_host_tyings_periodic(const int32_t* dofs, int64_t nnode, int32_t ndim,
+                               const int32_t* control_dofs, const int32_t* tyings, int64_t nties,
+                               const int32_t* iip, int64_t nnp, int32_t* dofs_out,
+                               int32_t* control_out, int64_t* counts)
+{
+    HREQ(dofs && control_dofs && dofs_out && control_out && counts && nnode > 0 && ndim > 0,
+         "bad argument");
+    HREQ((nties == 0 || tyings) && (nnp == 0 || iip) && nties >= 0 && nnp >= 0, "bad argument");
+    const int64_t n = nnode * ndim;
+    HREQ(fits32(n), "too large for int32 tables");
+    int32_t mn = *std::min_element(dofs, dofs + n), mx = *std::max_element(dofs, dofs + n);
+    if (mn < 0) return fail(GFGPU_ERR_INDEX, "gfgpu_host_tyings_periodic: negative dof");
+    for (int64_t k = 0; k < int64_t(ndim) * ndim; ++k)
+        if (control_dofs[k] < mn || control_dofs[k] > mx)
+            return fail(GFGPU_ERR_INDEX, "gfgpu_host_tyings_periodic: control dof out of range");
+    for (int64_t k = 0; k < nnp; ++k)
+        if (iip[k] < mn || iip[k] > mx)
+            return fail(GFGPU_ERR_INDEX, "gfgpu_host_tyings_periodic: iip out of range");
+    for (int64_t k = 0; k < 2 * nties; ++k)
+        if (tyings[k] < 0 || tyings[k] >= nnode)
+            return fail(GFGPU_ERR_INDEX, "gfgpu_host_tyings_periodic: tying node out of range");
+    // iid = flatten(dofs[dependent nodes]), iii = setdiff1d(dofs, iid), iiu = setdiff1d(iii, iip)
+    // (TyingsPeriodic.h:105-109); Reorder({iiu, iip, iid}) (Mesh.h:2384-2450)
+    std::vector<int32_t> iid;
+    iid.reserve(static_cast<size_t>(nties) * ndim);
+    std::vector<char> dep(static_cast<size_t>(mx) + 1, 0), pre(static_cast<size_t>(mx) + 1, 0),
+        present(static_cast<size_t>(mx) + 1, 0);
+    for (int64_t t = 0; t < nties; ++t)
+        for (int32_t j = 0; j < ndim; ++j) {
+            int32_t d = dofs[int64_t(tyings[2 * t + 1]) * ndim + j];
+            iid.push_back(d);
+            dep[d] = 1;
+        }
+    for (int64_t k = 0; k < nnp; ++k) pre[iip[k]] = 1;
+    for (int64_t k = 0; k < n; ++k) present[dofs[k]] = 1;
+    std::vector<int32_t> renum(static_cast<size_t>(mx) + 1, 0);
+    int32_t next = 0;
+    int64_t nni = 0, nnu = 0;
+    for (int32_t d = 0; d <= mx; ++d)
+        if (present[d] && !dep[d]) {
+            ++nni;
+            if (!pre[d]) {
+                renum[d] = next++;
+                ++nnu;
+            }
+        }
+    for (int64_t k = 0; k < nnp; ++k) renum[iip[k]] = next++;
+    for (int32_t d : iid) renum[d] = next++;
+    for (int64_t k = 0; k < n; ++k) dofs_out[k] = renum[dofs[k]];
+    for (int64_t k = 0; k < int64_t(ndim) * ndim; ++k) control_out[k] = renum[control_dofs[k]];
+    counts[0] = nnu;
+    counts[1] = nnp;
+    counts[2] = nni;
+    counts[3] = static_cast<int64_t>(iid.size());
+    return GFGPU_OK;
+}
+
+int gfgpu_host_tyings_cdi(const double* coor, const int32_t* tdofs, const int32_t* tcontrol,
+                          const int32_t* tyings, int64_t nties, int32_t ndim, int32_t* rowptr,
+                          int32_t* col, double* val, int64_t* nnz)
+{
+    HREQ(coor && tdofs && tcontrol && rowptr && col && val && nnz && ndim > 0 && nties >= 0 &&
+             (nties == 0 || tyings),
+         "bad argument");
+    // TyingsPeriodic.h:238-264: row i*ndim+j gets (dofs(ni, j), +1) and, per k,
+    // (control(j, k), x(nd, k) - x(ni, k)); setFromTriplets sums equal columns in push order and
+    // sorts each row's columns
+    int64_t k = 0;
+    rowptr[0] = 0;
+    std::vector<std::pair<int32_t, double>> row;
+    for (int64_t i = 0; i < nties; ++i) {
+        int64_t ni = tyings[2 * i], nd = tyings[2 * i + 1];
+        for (int32_t j = 0; j < ndim; ++j) {
+            row.clear();
+            row.emplace_back(tdofs[ni * ndim + j], 1.0);
+            for (int32_t q = 0; q < ndim; ++q)
+                row.emplace_back(tcontrol[j * ndim + q], coor[nd * ndim + q] - coor[ni * ndim + q]);
+            std::stable_sort(row.begin(), row.end(),
+                             [](const std::pair<int32_t, double>& a, const std::pair<int32_t, double>& b) {
+                                 return a.first < b.first;
+                             });
+            for (size_t q = 0; q < row.size(); ++q) {
+                if (q > 0 && row[q].first == row[q - 1].first) {
+                    val[k - 1] = val[k - 1] + row[q].second;
+                }
+                else {
+                    col[k] = row[q].first;
+                    val[k] = row[q].second;
+                    ++k;
+                }
+            }
+            rowptr[i * ndim + j + 1] = static_cast<int32_t>(k);
+        }
+    }
+    *nnz = k;
+    return GFGPU_OK;
+}
+
+int gfgpu_host_csr_transpose(const int32_t* rowptr, const int32_t* col, const double* val,
+                             int64_t nrow, int64_t ncol, int32_t* trowptr, int32_t* tcol,
+                             double* tval)
+{
+    HREQ(rowptr && col && val && trowptr && tcol && tval && nrow >= 0 && ncol >= 0, "bad argument");
+    int64_t nnz = rowptr[nrow];
+    std::fill(trowptr, trowptr + ncol + 1, 0);
+    for (int64_t k = 0; k < nnz; ++k) {
+        if (col[k] < 0 || col[k] >= ncol) return fail(GFGPU_ERR_INDEX, "gfgpu_host_csr_transpose: column out of range");
+        trowptr[col[k] + 1] += 1;
+    }
+    for (int64_t c = 0; c < ncol; ++c) trowptr[c + 1] += trowptr[c];
+    std::vector<int32_t> cur(trowptr, trowptr + ncol);
+    // rows visited in ascending order: every output row is sorted by the original row
+    for (int64_t r = 0; r < nrow; ++r)
+        for (int32_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+            int32_t q = cur[col[k]]++;
+            tcol[q] = static_cast<int32_t>(r);
+            tval[q] = val[k];
+        }
     return GFGPU_OK;
 }
 

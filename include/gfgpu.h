@@ -425,6 +425,50 @@ int gfgpu_matrixp_solve(const int32_t* rowptr, const int32_t* col, const double*
                         int64_t maxiter, int32_t check_every, void* workspace,
                         gfgpu_stream_t stream, int64_t* iters, double* relres);
 
+/* ============================ periodic tyings ============================================= */
+
+/* Tyings::Periodic (TyingsPeriodic.h:46-344) set-up, host: iid = flatten(dofs[tyings[:,1]]),
+ * iii = setdiff1d(dofs, iid), iiu = setdiff1d(iii, iip), and the renumbering
+ * Reorder({iiu, iip, iid}) (Mesh.h:2384-2450) of dofs -> dofs_out [nnode, ndim] and of
+ * control_dofs -> control_out [ndim, ndim]; counts = (nnu, nnp, nni, nnd). tyings [nties, 2] =
+ * (independent node, dependent node). */
+int gfgpu_host_tyings_periodic(const int32_t* dofs, int64_t nnode, int32_t ndim,
+                               const int32_t* control_dofs, const int32_t* tyings, int64_t nties,
+                               const int32_t* iip, int64_t nnp, int32_t* dofs_out,
+                               int32_t* control_out, int64_t* counts);
+/* Tyings::Periodic::Cdi (TyingsPeriodic.h:238-264) as CSR [nnd = nties*ndim rows, nni columns]
+ * (Eigen setFromTriplets: equal columns summed in push order, columns sorted). Cdu and Cdp
+ * (:272-344) are its column ranges [0, nnu) and [nnu, nni). col, val: capacity
+ * nties*ndim*(ndim+1). tdofs / tcontrol: the renumbered tables. */
+int gfgpu_host_tyings_cdi(const double* coor, const int32_t* tdofs, const int32_t* tcontrol,
+                          const int32_t* tyings, int64_t nties, int32_t ndim, int32_t* rowptr,
+                          int32_t* col, double* val, int64_t* nnz);
+/* Transpose of a CSR (rows of the result sorted by the original row): C_id = Cdi^T. */
+int gfgpu_host_csr_transpose(const int32_t* rowptr, const int32_t* col, const double* val,
+                             int64_t nrow, int64_t ncol, int32_t* trowptr, int32_t* tcol,
+                             double* tval);
+/* VectorPartitionedTyings::asDofs_i (VectorPartitionedTyings.h:208-239): dofval_i [nni] = the
+ * independent entries of nodevec, plus (apply_tyings) C_id times its dependent entries.
+ * work_d: nnd doubles. */
+int gfgpu_tyings_as_dofs_i(const int32_t* tdofs, int64_t nnode, int32_t ndim, int64_t nni,
+                           int64_t nnd, const int32_t* cid_rowptr, const int32_t* cid_col,
+                           const double* cid_val, const double* nodevec, int32_t apply_tyings,
+                           double* dofval_i, double* work_d, gfgpu_stream_t stream);
+/* MatrixPartitionedTyingsSolver::solve nodevec (MatrixPartitionedTyings.h, solve_nodevec_impl):
+ * B_u += C_ud B_d; x_u = AC_uu^-1 (B_u - AC_up x_p) with AC = the condensed matrix
+ * A_uu + A_ud C_du + C_ud A_du + C_ud A_dd C_du (factorize()); x_d = C_du x_u + C_dp x_p.
+ * Here: Jacobi-PCG (exact condensed diagonal) in FP64 to tol, the condensed operator applied
+ * from the blocks of the assembled CSR a_* (gfgpu_matrix_assemble with dmap = tdofs, n = ndof)
+ * without forming it. b, x nodevec (x_p read from x, x_u and x_d written). Synchronises. */
+int64_t gfgpu_tyings_solve_workspace_bytes(int64_t nnu, int64_t nnp, int64_t nnd);
+int gfgpu_tyings_solve(const int32_t* a_rowptr, const int32_t* a_col, const double* a_val,
+                       const int32_t* cdi_rowptr, const int32_t* cdi_col, const double* cdi_val,
+                       const int32_t* cid_rowptr, const int32_t* cid_col, const double* cid_val,
+                       const int32_t* tdofs, int64_t nnode, int32_t ndim, int64_t nnu, int64_t nnp,
+                       int64_t nnd, const double* b, double* x, double tol, int64_t maxiter,
+                       int32_t check_every, void* workspace, gfgpu_stream_t stream, int64_t* iters,
+                       double* relres);
+
 /* ============================ learned preconditioner (device) ============================= */
 
 /* The network: 4 convolution layers 3x3 on the nodal grid of a Regular Quad4 mesh (NHWC, the

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <iterator>
 #include <limits>
 #include <map>
 #include <utility>
@@ -686,6 +687,87 @@ void ref_matrixp_dot(const idx* rowptr, const idx* col, const double* val, idx n
         bp[r] = su + sp;
     }
     for (idx d = 0; d < ndof; ++d) b[d] = bp[part1d[d]];
+}
+
+// ------------------------------------------------------------------------------------------------
+// Periodic tyings (TyingsPeriodic.h, VectorPartitionedTyings.h)
+// ------------------------------------------------------------------------------------------------
+
+// TyingsPeriodic.h:85-122: iid = flatten(dofs[dependent]), iii = setdiff1d(dofs, iid),
+// iiu = setdiff1d(iii, iip) (sorted unique), renumbering Reorder({iiu, iip, iid}) (Mesh.h:2384-2450)
+// applied to dofs and control_dofs. counts = (nnu, nnp, nni, nnd).
+void ref_tyings_periodic(const idx* dofs, idx nnode, idx nd, const idx* control, const idx* tyings,
+                         idx nties, const idx* iip, idx nnp, idx* dofs_out, idx* control_out,
+                         idx* counts)
+{
+    std::vector<idx> iid;
+    for (idx t = 0; t < nties; ++t)
+        for (idx j = 0; j < nd; ++j) iid.push_back(dofs[tyings[t * 2 + 1] * nd + j]);
+    std::vector<idx> all(dofs, dofs + nnode * nd);
+    std::sort(all.begin(), all.end());
+    all.erase(std::unique(all.begin(), all.end()), all.end());
+    std::vector<idx> sid(iid), sip(iip, iip + nnp);
+    std::sort(sid.begin(), sid.end());
+    std::sort(sip.begin(), sip.end());
+    std::vector<idx> iii, iiu;
+    std::set_difference(all.begin(), all.end(), sid.begin(), sid.end(), std::back_inserter(iii));
+    std::set_difference(iii.begin(), iii.end(), sip.begin(), sip.end(), std::back_inserter(iiu));
+    idx mx = all.empty() ? 0 : all.back();
+    std::vector<idx> renum(mx + 1, 0);
+    idx i = 0;
+    for (idx v : iiu) renum[v] = i++;
+    for (idx k = 0; k < nnp; ++k) renum[iip[k]] = i++;
+    for (idx v : iid) renum[v] = i++;
+    for (idx k = 0; k < nnode * nd; ++k) dofs_out[k] = renum[dofs[k]];
+    for (idx k = 0; k < nd * nd; ++k) control_out[k] = renum[control[k]];
+    counts[0] = static_cast<idx>(iiu.size());
+    counts[1] = nnp;
+    counts[2] = static_cast<idx>(iii.size());
+    counts[3] = static_cast<idx>(iid.size());
+}
+
+// TyingsPeriodic.h:238-264 (Cdi) through setFromTriplets; dense [nnd, nni] output.
+void ref_tyings_cdi_dense(const double* coor, const idx* tdofs, const idx* tcontrol,
+                          const idx* tyings, idx nties, idx nd, idx nni, double* Cdi)
+{
+    std::map<std::pair<idx, idx>, double> A;
+    auto push = [&](idx r, idx c, double v) {
+        auto it = A.find({r, c});
+        if (it == A.end()) A.emplace(std::make_pair(r, c), v);
+        else it->second = it->second + v;
+    };
+    for (idx i = 0; i < nties; ++i)
+        for (idx j = 0; j < nd; ++j) {
+            idx ni = tyings[i * 2], ndn = tyings[i * 2 + 1];
+            push(i * nd + j, tdofs[ni * nd + j], +1.0);
+            for (idx k = 0; k < nd; ++k)
+                push(i * nd + j, tcontrol[j * nd + k], coor[ndn * nd + k] - coor[ni * nd + k]);
+        }
+    for (idx k = 0; k < nties * nd * nni; ++k) Cdi[k] = 0.0;
+    for (auto& kv : A) Cdi[kv.first.first * nni + kv.first.second] = kv.second;
+}
+
+// VectorPartitionedTyings.h:208-239 (asDofs_i): the independent entries, then + C_id u_d with
+// Eigen's column-major product (per entry i a sum from 0 over ascending d of Cdi(d, i) u_d).
+void ref_tyings_as_dofs_i(const idx* tdofs, idx nnode, idx nd, idx nni, idx nnd,
+                          const double* Cdi_dense, const double* nodevec, int apply,
+                          double* dofval_i)
+{
+    for (idx i = 0; i < nni; ++i) dofval_i[i] = 0.0;
+    std::vector<double> ud(nnd, 0.0);
+    for (idx k = 0; k < nnode * nd; ++k) {
+        if (tdofs[k] < nni) dofval_i[tdofs[k]] = nodevec[k];
+        else ud[tdofs[k] - nni] = nodevec[k];
+    }
+    if (!apply) return;
+    for (idx i = 0; i < nni; ++i) {
+        double acc = 0.0;
+        for (idx d = 0; d < nnd; ++d) {
+            double c = Cdi_dense[d * nni + i];
+            if (c != 0.0) acc = acc + c * ud[d];
+        }
+        dofval_i[i] = dofval_i[i] + acc;
+    }
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -299,6 +299,30 @@ def matrixp_dot(rowptr, col, val, nnu, part1d, x):
     return b
 
 
+def tyings_periodic(coor, dofs_, control, tyings, iip):
+    """Tyings::Periodic: (renumbered dofs, renumbered control, (nnu, nnp, nni, nnd), Cdi dense)."""
+    coor, d, c, t = _f64(coor), _ix(dofs_), _ix(control), _ix(tyings).reshape(-1, 2)
+    iip = _ix(iip).ravel()
+    nnode, nd = d.shape
+    dofs_out = np.empty_like(d)
+    ctrl_out = np.empty_like(c)
+    counts = np.zeros(4, dtype=np.int64)
+    _call("ref_tyings_periodic", d, nnode, nd, c, t, t.shape[0], iip, iip.size, dofs_out, ctrl_out,
+          counts)
+    nnu, nnp, nni, nnd = (int(v) for v in counts)
+    Cdi = np.empty((nnd, nni))
+    _call("ref_tyings_cdi_dense", coor, dofs_out, ctrl_out, t, t.shape[0], nd, nni, Cdi)
+    return dofs_out, ctrl_out, (nnu, nnp, nni, nnd), Cdi
+
+
+def tyings_as_dofs_i(tdofs, nni, Cdi, nodevec, apply=True):
+    td, nv, Cdi = _ix(tdofs), _f64(nodevec), _f64(Cdi)
+    nnode, nd = td.shape
+    out = np.empty(nni)
+    _call("ref_tyings_as_dofs_i", td, nnode, nd, nni, Cdi.shape[0], Cdi, nv, int(apply), out)
+    return out
+
+
 # ---------------------------------------------------------------- vector
 
 

@@ -70,3 +70,31 @@ def residual(A, iip, x):
     b = -(A @ xp)[iiu]
     r = b - (A[iiu][:, iiu] @ x[iiu])
     return float(np.linalg.norm(r) / np.linalg.norm(b))
+
+
+def solve_tyings(A, tdofs, nnu, nnp, Cdi, b, x):
+    """MatrixPartitionedTyingsSolver::solve nodevec (MatrixPartitionedTyings.h, solve_nodevec_impl
+    and factorize): the condensed system AC_uu x_u = B_u + C_ud B_d - AC_up x_p with
+    AC = A_uu + A_ud C_du + C_ud A_du + C_ud A_dd C_du, solved directly (scipy SuperLU in place of
+    Eigen's SimplicialLDLT); x_d = C_du x_u + C_dp x_p. A: assembled [ndof, ndof] matrix in the
+    tyings numbering; b, x nodevec; returns the new x."""
+    A = sp.csr_matrix(A)
+    nni = nnu + nnp
+    ndof = A.shape[0]
+    Cdu = sp.csr_matrix(Cdi[:, :nnu])
+    Cdp = sp.csr_matrix(Cdi[:, nnu:])
+    u, p, d = slice(0, nnu), slice(nnu, nni), slice(nni, ndof)
+    ACuu = A[u, u] + A[u, d] @ Cdu + Cdu.T @ A[d, u] + Cdu.T @ A[d, d] @ Cdu
+    ACup = A[u, p] + A[u, d] @ Cdp + Cdu.T @ A[d, p] + Cdu.T @ A[d, d] @ Cdp
+    td = np.asarray(tdofs).ravel()
+    bv, xv = np.asarray(b).ravel(), np.asarray(x, dtype=float).ravel().copy()
+    B = np.zeros(ndof)
+    X = np.zeros(ndof)
+    B[td] = bv
+    X[td] = xv
+    Bu = B[u] + Cdu.T @ B[d]
+    Xu = spla.spsolve(ACuu.tocsc(), Bu - ACup @ X[p])
+    Xd = Cdu @ Xu + Cdp @ X[p]
+    X[u] = Xu
+    X[d] = Xd
+    return X[td].reshape(np.asarray(x).shape)

@@ -197,3 +197,24 @@ def test_matrix_pattern_matches_oracle(lib, oracle, periodic):
         val[j] = acc
         assert np.all(np.diff(idx) > 0)  # triplet order
     assert np.array_equal(val, val_r)
+
+
+def test_tyings_setup_matches_oracle(lib, oracle):
+    """Tyings::Control + Tyings::Periodic set-up (host, in the library): the renumbering into
+    independent-unknown / -prescribed / dependent dofs and the tying matrix C_di, bit for bit
+    against the oracle's restatement."""
+    import goosefem_gb300 as gf
+
+    mesh = gf.Mesh.Quad4.Regular(5, 4)
+    control = gf.Tyings.Control(mesh.coor(), mesh.dofs())
+    coor, dofs = control.coor(), control.dofs()
+    cdofs = control.controlDofs()
+    iip = np.concatenate([cdofs.ravel(), dofs[mesh.nodesOrigin()].ravel()])
+    ty = gf.Tyings.Periodic(coor, dofs, cdofs, mesh.nodesPeriodic(), iip)
+    d_r, c_r, counts_r, Cdi_r = oracle.tyings_periodic(coor, dofs, cdofs, mesh.nodesPeriodic(), iip)
+    assert np.array_equal(ty.dofs(), d_r) and np.array_equal(ty.control(), c_r)
+    assert (ty.nnu(), ty.nnp(), ty.nni(), ty.nnd()) == counts_r
+    assert np.array_equal(ty.Cdi().toarray(), Cdi_r)
+    assert np.array_equal(ty.Cdu().toarray(), Cdi_r[:, :ty.nnu()])
+    assert np.array_equal(ty.Cdp().toarray(), Cdi_r[:, ty.nnu():])
+    assert ty.nnd() == mesh.nodesPeriodic().shape[0] * 2
