@@ -34,6 +34,7 @@ class VerletDesc(C.Structure):
         ("fext", C.c_void_p), ("dt", C.c_double), ("eta", C.c_double),
         ("uniform", C.c_int32), ("hx", C.c_double), ("hy", C.c_double), ("hz", C.c_double),
         ("coef", C.c_void_p),
+        ("mclass", C.c_void_p), ("mclass_inv", C.c_void_p), ("ncls", C.c_int32),
     ]
 
 

@@ -117,10 +117,33 @@ class VelocityVerlet:
             d.coef = self.coef.data_ptr()
         self.ws = torch.empty(int(_lib.lib().gfgpu_verlet_workspace_bytes(C.addressof(d))) // 8,
                               dtype=torch.float64, device=_dev.device())
+        self.classify()
 
     @property
     def uniform(self):
         return bool(self.desc.uniform)
+
+    def classify(self):
+        """Lumped-mass classes for the closed-form node update (gfgpu_verlet_classify): used
+        when the free dofs take at most 16 distinct inverse masses. Returns whether it applies."""
+        n = self.desc.nnode * self.desc.ndim
+        self._mclass = torch.empty(n, dtype=torch.uint8, device=_dev.device())
+        self._mclass_inv = np.zeros(16)
+        try:
+            _lib.call("gfgpu_verlet_classify", C.addressof(self.desc), self._mclass.data_ptr(),
+                      self._mclass_inv.ctypes.data, _dev.stream())
+            return True
+        except _lib.GFGPUError as e:
+            if e.code != -7:
+                raise
+            self._mclass = None
+            return False
+
+    def use_per_dof_mass(self):
+        """Node update with the inverse mass read per dof (no mass classes)."""
+        self.desc.mclass = None
+        self.desc.mclass_inv = None
+        self.desc.ncls = 0
 
     @property
     def path(self):

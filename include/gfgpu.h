@@ -277,7 +277,17 @@ typedef struct {
     /* optional per-element coefficients of the uniform square Quad4 kernel [nelem, 4]
      * (gfgpu_verlet_precompute); NULL = derive them from K and G in every increment */
     const double* coef;
+    /* optional lumped-mass classes (gfgpu_verlet_classify): per nodevec entry the index of its
+     * inverse lumped mass in a short table (GFGPU_PRESCRIBED_CLASS for prescribed dofs), and that
+     * table on the host; the fast node kernel then takes the three velocity estimates in closed
+     * form with per-class coefficients. NULL = read inv per dof. */
+    const uint8_t* mclass;     /* [nnode, ndim] device */
+    const double* mclass_inv;  /* [ncls] host */
+    int32_t ncls;
 } gfgpu_verlet_desc;
+
+#define GFGPU_MASS_CLASSES 16
+#define GFGPU_PRESCRIBED_CLASS 255
 
 /* Bytes of scratch the step needs (the element-force buffer), 256-byte aligned size. */
 int64_t gfgpu_verlet_workspace_bytes(const gfgpu_verlet_desc* d);
@@ -290,6 +300,13 @@ int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
  * K and G only (lam/4, G/2, G/4, g^2 (lam + 3G)/4, lam = K - 2G/3); set d->coef = coef to use
  * them. Returns GFGPU_ERR_UNSUPPORTED for other meshes. */
 int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stream_t stream);
+/* Host set-up of the lumped-mass classes: reads part and inv back from the device, and if the
+ * free dofs take at most GFGPU_MASS_CLASSES distinct inverse masses (a Regular mesh with uniform
+ * density: interior, edge and corner values) writes mclass [nnode*ndim] (device, uint8) and
+ * mclass_inv [GFGPU_MASS_CLASSES] (host) and sets d->mclass, d->mclass_inv, d->ncls; otherwise
+ * returns GFGPU_ERR_UNSUPPORTED and leaves d unchanged. Synchronises. */
+int gfgpu_verlet_classify(gfgpu_verlet_desc* d, uint8_t* mclass, double* mclass_inv,
+                          gfgpu_stream_t stream);
 /* Advance nsteps increments; u, v, a are nodevec [nnode, ndim] device arrays updated in place.
  * Strict mode (gfgpu_set_strict) with the general path reproduces the reference's operation
  * order bit for bit; fast mode reassociates the lumped solve (a = inv R - (inv eta) v).

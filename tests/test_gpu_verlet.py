@@ -144,3 +144,28 @@ def test_verlet_distorted_mesh_uses_general_path(gf, oracle):
     K, G = seeded_material(mesh.nelem(), 30)
     vv = gf.VelocityVerlet(coor, mesh.conn(), mesh.dofs(), K, G, dt=0.01)
     assert not vv.uniform
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_verlet_mass_class_node_update(gf, oracle, periodic):
+    """The closed-form node update with lumped-mass classes (set up by default on Regular
+    meshes) against the per-dof update and the oracle, with an external force as well."""
+    gf.set_strict(False)
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 40, 30, periodic,
+                                                            not periodic, 29)
+    fext = seeded_field((mesh.nnode(), 2), 30, amp=1e-4)
+    runs = []
+    for per_dof in (False, True):
+        vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip, fext=fext)
+        assert 1 <= vv.desc.ncls <= (4 if not periodic else 1)
+        if per_dof:
+            vv.use_per_dof_mass()
+        u = torch.zeros((mesh.nnode(), 2), dtype=torch.float64, device="cuda")
+        v = torch.tensor(v0, device="cuda")
+        a = torch.zeros_like(u)
+        vv.step(u, v, a, 100)
+        runs.append((to_np(u), to_np(v), to_np(a)))
+    ur, vr, ar = _run_oracle(oracle, ref, v0, dt, 0.1, 100, fext)
+    for k, r in enumerate((ur, vr, ar)):
+        assert rel_err(runs[0][k], runs[1][k]) <= 1e-13
+        assert rel_err(runs[0][k], r) <= RTOL
