@@ -589,6 +589,100 @@ k_verlet_node_cls(const int32_t* __restrict__ dofs, const int32_t* __restrict__ 
     }
 }
 
+// The same closed-form update for a Quad4 Regular(nx, ny) mesh with dofs = node * 2 + i, one
+// thread per node: the element forces of node (ix, iy) are fe[e][m] of the elements
+// (iy-1, ix-1) m=2, (iy-1, ix) m=3, (iy, ix-1) m=1, (iy, ix) m=0 (those that exist), summed in
+// that order: ascending element index, the order of the dof CSR.
+__global__ void __launch_bounds__(256)
+k_verlet_node_cls_regular(int64_t nx, int64_t ny, const uint8_t* __restrict__ mclass,
+                          MassClassTab tab, const double* __restrict__ fe,
+                          const double* __restrict__ fext, VerletCoef k, int advance,
+                          double* __restrict__ u, double* __restrict__ v, double* __restrict__ a)
+{
+    __shared__ double sm[5][GFGPU_MASS_CLASSES];
+    if (threadIdx.x < GFGPU_MASS_CLASSES) {
+        int c = threadIdx.x;
+        sm[0][c] = tab.mi[c];
+        sm[1][c] = tab.be[c];
+        sm[2][c] = tab.c1[c];
+        sm[3][c] = tab.c2[c];
+        sm[4][c] = tab.c3[c];
+    }
+    __syncthreads();
+    const int64_t W = nx + 1, nnode = W * (ny + 1);
+    const double2* f2 = reinterpret_cast<const double2*>(fe);
+    GF_FOR(node, nnode)
+    {
+        int64_t iy = node / W, ix = node - iy * W;
+        double fx = 0.0, fy = 0.0;
+        bool first = true;
+        auto take = [&](int64_t ey, int64_t ex, int m) {
+            if (ey < 0 || ey >= ny || ex < 0 || ex >= nx) return;
+            double2 g = __ldg(f2 + (ey * nx + ex) * 4 + m);
+            if (first) {
+                fx = g.x;
+                fy = g.y;
+                first = false;
+            }
+            else {
+                fx += g.x;
+                fy += g.y;
+            }
+        };
+        take(iy - 1, ix - 1, 2);
+        take(iy - 1, ix, 3);
+        take(iy, ix - 1, 1);
+        take(iy, ix, 0);
+        uchar2 cc = __ldg(reinterpret_cast<const uchar2*>(mclass) + node);
+        double2 vn = reinterpret_cast<const double2*>(v)[node];
+        double2 an = reinterpret_cast<const double2*>(a)[node];
+        double2 fx2 = fext ? __ldg(reinterpret_cast<const double2*>(fext) + node) : make_double2(0.0, 0.0);
+        double vv[2], aa[2];
+        const double fi[2] = {fx, fy}, vi[2] = {vn.x, vn.y}, ai[2] = {an.x, an.y},
+                     fxi[2] = {fx2.x, fx2.y};
+        const int ci[2] = {cc.x, cc.y};
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            int c = ci[i];
+            if (c < GFGPU_MASS_CLASSES) {
+                double mi = sm[0][c];
+                double mR = fext ? mi * (fxi[i] - fi[i]) : -mi * fi[i];
+                vv[i] = fma(sm[4][c], mR, fma(sm[3][c], ai[i], sm[2][c] * vi[i]));
+                aa[i] = fma(-sm[1][c], vv[i], mR);
+            }
+            else {
+                aa[i] = ai[i];
+                vv[i] = fma(k.h, ai[i] + ai[i], vi[i]);
+            }
+        }
+        reinterpret_cast<double2*>(v)[node] = make_double2(vv[0], vv[1]);
+        reinterpret_cast<double2*>(a)[node] = make_double2(aa[0], aa[1]);
+        if (advance) {
+            double2 un = reinterpret_cast<const double2*>(u)[node];
+            reinterpret_cast<double2*>(u)[node] =
+                make_double2(fma(k.c, aa[0], fma(k.dt, vv[0], un.x)), fma(k.c, aa[1], fma(k.dt, vv[1], un.y)));
+        }
+    }
+}
+
+// flag = 1 if conn differs from Regular(nx, ny) or dofs from arange
+__global__ void k_check_regular(const int32_t* __restrict__ conn, const int32_t* __restrict__ dofs,
+                                int64_t nx, int64_t ny, int* __restrict__ flag)
+{
+    const int64_t W = nx + 1;
+    GF_FOR(e, nx * ny)
+    {
+        int64_t ey = e / nx, ex = e - ey * nx;
+        int64_t n0 = ey * W + ex;
+        int4 c = reinterpret_cast<const int4*>(conn)[e];
+        if (c.x != n0 || c.y != n0 + 1 || c.z != n0 + W + 1 || c.w != n0 + W) *flag = 1;
+    }
+    GF_FOR(t, W * (ny + 1) * 2)
+    {
+        if (dofs[t] != t) *flag = 1;
+    }
+}
+
 template <bool S>
 __global__ void __launch_bounds__(256)
 k_verlet_node(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
@@ -946,6 +1040,9 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
         if (st)
             k_verlet_node<true><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
                                                       d->inv, fe, d->fext, n, k, adv, u, v, a);
+        else if (d->mclass && d->mclass_inv && d->ncls > 0 && d->reg_nx > 0)
+            k_verlet_node_cls_regular<<<grid_for(d->nnode), kBlock, 0, s>>>(
+                d->reg_nx, d->reg_ny, d->mclass, tab, fe, d->fext, k, adv, u, v, a);
         else if (d->mclass && d->mclass_inv && d->ncls > 0)
             k_verlet_node_cls<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->mclass, tab,
                                                     fe, d->fext, n, k, adv, u, v, a);
@@ -957,6 +1054,36 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
             k_verlet_node_fast<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
                                                      d->inv, fe, d->fext, n, k, adv, u, v, a);
         GF_TRY(check_launch("verlet node kernel"));
+    }
+    return GFGPU_OK;
+}
+
+int gfgpu_verlet_detect_regular(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, gfgpu_stream_t stream)
+{
+    GF_TRY(check_desc(d));
+    d->reg_nx = 0;
+    d->reg_ny = 0;
+    if (!(d->nne == 4 && d->ndim == 2 && nx > 0 && ny > 0 && d->nelem == nx * ny &&
+          d->nnode == (nx + 1) * (ny + 1)))
+        return GFGPU_OK;
+    GF_REQUIRE((reinterpret_cast<uintptr_t>(d->conn) & 15u) == 0, "conn must be 16-byte aligned");
+    cudaStream_t s = S(stream);
+    int* flag = nullptr;
+    GF_TRY(check_cuda(cudaMalloc(&flag, sizeof(int)), "cudaMalloc"));
+    int h = 1;
+    int rc = check_cuda(cudaMemsetAsync(flag, 0, sizeof(int), s), "cudaMemsetAsync");
+    if (rc == GFGPU_OK) {
+        k_check_regular<<<grid_for(std::max(nx * ny, (nx + 1) * (ny + 1) * 2)), kBlock, 0, s>>>(
+            d->conn, d->dofs, nx, ny, flag);
+        rc = check_launch("detect_regular");
+    }
+    if (rc == GFGPU_OK) rc = check_cuda(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    if (rc == GFGPU_OK) rc = check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    cudaFree(flag);
+    GF_TRY(rc);
+    if (h == 0) {
+        d->reg_nx = nx;
+        d->reg_ny = ny;
     }
     return GFGPU_OK;
 }

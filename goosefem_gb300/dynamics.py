@@ -118,6 +118,8 @@ class VelocityVerlet:
         self.ws = torch.empty(int(_lib.lib().gfgpu_verlet_workspace_bytes(C.addressof(d))) // 8,
                               dtype=torch.float64, device=_dev.device())
         self.classify()
+        if nne == 4:
+            self._detect_regular(np.asarray(coor))
 
     @property
     def uniform(self):
@@ -138,6 +140,22 @@ class VelocityVerlet:
                 raise
             self._mclass = None
             return False
+
+    def _detect_regular(self, coor):
+        """Mesh::Quad4::Regular numbering (gfgpu_verlet_detect_regular, checked on the device):
+        nx + 1 = the leading run of nodes at the first node's y."""
+        y = coor[:, 1]
+        run = int(np.argmax(y != y[0])) if np.any(y != y[0]) else y.size
+        nx = run - 1
+        if nx > 0 and self.desc.nelem % nx == 0:
+            _lib.call("gfgpu_verlet_detect_regular", C.addressof(self.desc), nx,
+                      self.desc.nelem // nx, _dev.stream())
+        return self.desc.reg_nx > 0
+
+    def use_csr_gather(self):
+        """Node kernel through the dof CSR even on a Regular mesh."""
+        self.desc.reg_nx = 0
+        self.desc.reg_ny = 0
 
     def use_per_dof_mass(self):
         """Node update with the inverse mass read per dof (no mass classes)."""

@@ -169,3 +169,28 @@ def test_verlet_mass_class_node_update(gf, oracle, periodic):
     for k, r in enumerate((ur, vr, ar)):
         assert rel_err(runs[0][k], runs[1][k]) <= 1e-13
         assert rel_err(runs[0][k], r) <= RTOL
+
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_verlet_regular_node_kernel_same_bits(gf, oracle, periodic):
+    """The Regular-mesh node kernel (element forces by index arithmetic) gives the same bits as
+    the CSR gather; periodic dofs are not Regular-identity and keep the CSR."""
+    gf.set_strict(False)
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 37, 23, periodic,
+                                                            not periodic, 31)
+    fext = seeded_field((mesh.nnode(), 2), 32, amp=1e-4)
+    out = []
+    for csr in (False, True):
+        vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip, fext=fext)
+        assert (vv.desc.reg_nx == 37 and vv.desc.reg_ny == 23) == (not periodic)
+        if csr:
+            vv.use_csr_gather()
+        u = torch.zeros((mesh.nnode(), 2), dtype=torch.float64, device="cuda")
+        v = torch.tensor(v0, device="cuda")
+        a = torch.zeros_like(u)
+        vv.step(u, v, a, 50)
+        out.append(torch.cat([u, v, a]))
+    assert torch.equal(out[0], out[1])
+    ur, vr, ar = _run_oracle(oracle, ref, v0, dt, 0.1, 50, fext)
+    assert rel_err(to_np(out[0][:mesh.nnode()]), ur) <= RTOL
