@@ -469,7 +469,8 @@ def run_static(args):
             "ms_per_step": sec * 1e3, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": f"Hex8 Regular {n}^3 static, z=0 fixed, top uz=-1e-2, "
                                    "matrix-free Jacobi-PCG", "element_path":
-                       "uniform" if st.uniform else "general"},
+                       ("uniform-cube" if st.coef is not None else "uniform") if st.uniform
+                       else "general"},
             "iterations": it, "relres_true": rel, "ms_per_iteration": sec * 1e3 / it,
             "elem_updates_per_s": n ** 3 * 8 * it / sec}
     print(json.dumps(line), flush=True)

@@ -412,6 +412,150 @@ k_elem_force_hex8_uniform(const int32_t* __restrict__ conn, const double* __rest
     }
 }
 
+// Cube Hex8 (hx = hy = hz = h) with per-element coefficients folded from K, G and the geometry
+// (gfgpu_verlet_precompute): L0 = w0 d lam, G0 = w0 d G, L1 = w1 d lam, G1 = w1 d G,
+// kH = w2 d^2 (lam + 4 G) with d = 1/(4h) and the weights of Hex8Uniform. The mode forces of
+// k_elem_force_hex8_uniform then merge term by term (e.g. F4_0 = 3 G1 A4_0 + L1 (A4_0 + A5_2)),
+// and the unused mean of the forward transform and the zero mean of the inverse are skipped:
+// ~171 FP64 instructions per element instead of ~250.
+__global__ void k_hex8_cube_coef(const double* __restrict__ Km, const double* __restrict__ Gm,
+                                 int64_t nelem, Hex8Uniform c, double* __restrict__ coef)
+{
+    GF_FOR(e, nelem)
+    {
+        double K = Km[e], G = Gm[e];
+        double lam = K - 2.0 * G / 3.0;
+        double a0 = c.w0x * c.dx, a1 = c.w1x * c.dx;
+        double2* o = reinterpret_cast<double2*>(coef) + e * 4;
+        o[0] = make_double2(a0 * lam, a0 * G);
+        o[1] = make_double2(2.0 * a0 * G, a1 * lam);
+        o[2] = make_double2(a1 * G, 2.0 * a1 * G);
+        o[3] = make_double2(3.0 * a1 * G, c.w2 * c.dx * c.dx * (lam + 4.0 * G));
+    }
+}
+
+__device__ __forceinline__ void fwht8_nomean(double (&v)[8])
+{
+    // stages 1, 2 in full; the last stage without the (unused) mean v[0]
+#pragma unroll
+    for (int h = 1; h < 4; h <<= 1)
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if ((i & h) == 0) {
+                double a = v[i], b = v[i + h];
+                v[i] = a + b;
+                v[i + h] = a - b;
+            }
+#pragma unroll
+    for (int i = 1; i < 4; ++i) {
+        double a = v[i], b = v[i + 4];
+        v[i] = a + b;
+        v[i + 4] = a - b;
+    }
+    v[4] = v[0] - v[4];
+}
+
+__global__ void __launch_bounds__(128)
+k_elem_force_hex8_cube(const int32_t* __restrict__ conn, const double* __restrict__ u,
+                       const double* __restrict__ coef, int64_t nelem, double* __restrict__ fe)
+{
+    constexpr int pos[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+    GF_FOR(e, nelem)
+    {
+        double H[3][8];
+        const int4* cp = reinterpret_cast<const int4*>(conn + e * 8);
+        int4 c0 = __ldg(cp), c1 = __ldg(cp + 1);
+        int nodes[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const double* un = u + static_cast<int64_t>(nodes[m]) * 3;
+            H[0][pos[m]] = __ldg(un);
+            H[1][pos[m]] = __ldg(un + 1);
+            H[2][pos[m]] = __ldg(un + 2);
+        }
+        fwht8_nomean(H[0]);
+        fwht8_nomean(H[1]);
+        fwht8_nomean(H[2]);
+        const double2* cf = reinterpret_cast<const double2*>(coef) + e * 4;
+        double2 k01 = __ldg(cf), k23 = __ldg(cf + 1), k45 = __ldg(cf + 2), k67 = __ldg(cf + 3);
+        double L0 = k01.x, G0 = k01.y, G0x2 = k23.x, L1 = k23.y, G1 = k45.x, G1x2 = k45.y,
+               G1x3 = k67.x, kH = k67.y;
+        // modes (A1 = -H1, A2 = -H2, A3 = -H4, A4 = H3, A5 = H6, A6 = H5, A7 = -H7)
+        double A1[3], A2[3], A3[3], A4[3], A5[3], A6[3], A7[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            A1[j] = -H[j][1];
+            A2[j] = -H[j][2];
+            A4[j] = H[j][3];
+            A3[j] = -H[j][4];
+            A6[j] = H[j][5];
+            A5[j] = H[j][6];
+            A7[j] = -H[j][7];
+        }
+        double F[8][3];
+        // constant strain
+        {
+            double Lt = L0 * (A1[0] + A2[1] + A3[2]);
+            F[1][0] = fma(G0x2, A1[0], Lt);
+            F[2][1] = fma(G0x2, A2[1], Lt);
+            F[3][2] = fma(G0x2, A3[2], Lt);
+            double s01 = G0 * (A1[1] + A2[0]);
+            double s02 = G0 * (A1[2] + A3[0]);
+            double s12 = G0 * (A2[2] + A3[1]);
+            F[1][1] = s01;
+            F[2][0] = s01;
+            F[1][2] = s02;
+            F[3][0] = s02;
+            F[2][2] = s12;
+            F[3][1] = s12;
+        }
+        // linear modes
+        {
+            double Lxi = L1 * (A4[1] + A6[2]);
+            double Let = L1 * (A4[0] + A5[2]);
+            double Lze = L1 * (A6[0] + A5[1]);
+            F[4][0] = fma(G1x3, A4[0], Let);
+            F[4][1] = fma(G1x3, A4[1], Lxi);
+            F[4][2] = fma(G1x2, A4[2], G1 * (A5[0] + A6[1]));
+            F[5][0] = fma(G1x2, A5[0], G1 * (A6[1] + A4[2]));
+            F[5][1] = fma(G1x3, A5[1], Lze);
+            F[5][2] = fma(G1x3, A5[2], Let);
+            F[6][0] = fma(G1x3, A6[0], Lze);
+            F[6][1] = fma(G1x2, A6[1], G1 * (A5[0] + A4[2]));
+            F[6][2] = fma(G1x3, A6[2], Lxi);
+        }
+        F[7][0] = kH * A7[0];
+        F[7][1] = kH * A7[1];
+        F[7][2] = kH * A7[2];
+        // inverse transform of (0, -F1, -F2, F4, -F3, F6, F5, -F7) in binary order; the first
+        // stage with a zero mean needs no arithmetic
+        double* out = fe + e * 24;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double b1 = -F[1][j];
+            double v[8] = {b1, -b1, -F[2][j] + F[4][j], -F[2][j] - F[4][j], 0.0, 0.0, 0.0, 0.0};
+            double x = -F[3][j] + F[6][j], y = -F[3][j] - F[6][j];
+            double z = F[5][j] - F[7][j], w = F[5][j] + F[7][j];
+            v[4] = x;
+            v[5] = y;
+            v[6] = z;
+            v[7] = w;
+            // stage 2 (h = 2) and stage 3 (h = 4)
+#pragma unroll
+            for (int h = 2; h < 8; h <<= 1)
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if ((i & h) == 0) {
+                        double a = v[i], b = v[i + h];
+                        v[i] = a + b;
+                        v[i + h] = a - b;
+                    }
+#pragma unroll
+            for (int m = 0; m < 8; ++m) out[m * 3 + j] = v[pos[m]];
+        }
+    }
+}
+
 // ------------------------------------------------------------------ node kernels
 
 struct VerletCoef {
@@ -849,6 +993,24 @@ static Quad4Uniform quad4_uniform_constants(const gfgpu_verlet_desc* d)
     return c;
 }
 
+static Hex8Uniform hex8_uniform_constants(const gfgpu_verlet_desc* d)
+{
+    Hex8Uniform c;
+    double g = 1.0 / std::sqrt(3.0);
+    double vq = d->hx * d->hy * d->hz / 8.0;
+    c.dx = 1.0 / (4.0 * d->hx);
+    c.dy = 1.0 / (4.0 * d->hy);
+    c.dz = 1.0 / (4.0 * d->hz);
+    c.w0x = 8.0 * vq * c.dx;
+    c.w0y = 8.0 * vq * c.dy;
+    c.w0z = 8.0 * vq * c.dz;
+    c.w1x = 8.0 * (g * g) * vq * c.dx;
+    c.w1y = 8.0 * (g * g) * vq * c.dy;
+    c.w1z = 8.0 * (g * g) * vq * c.dz;
+    c.w2 = 8.0 * (g * g) * (g * g) * vq;
+    return c;
+}
+
 static VerletCoef verlet_coefficients(const gfgpu_verlet_desc* d)
 {
     VerletCoef k;
@@ -875,20 +1037,12 @@ static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, 
         k_elem_force_quad4_uniform<<<grid_for(d->nelem), 256, 0, s>>>(d->conn, u, d->K, d->G,
                                                                       d->nelem, c, fe);
     }
+    else if (d->uniform && d->coef) {
+        k_elem_force_hex8_cube<<<grid_for(d->nelem, 128), 128, 0, s>>>(d->conn, u, d->coef, d->nelem,
+                                                                       fe);
+    }
     else if (d->uniform) {
-        Hex8Uniform c;
-        double g = 1.0 / std::sqrt(3.0);
-        double vq = d->hx * d->hy * d->hz / 8.0;
-        c.dx = 1.0 / (4.0 * d->hx);
-        c.dy = 1.0 / (4.0 * d->hy);
-        c.dz = 1.0 / (4.0 * d->hz);
-        c.w0x = 8.0 * vq * c.dx;
-        c.w0y = 8.0 * vq * c.dy;
-        c.w0z = 8.0 * vq * c.dz;
-        c.w1x = 8.0 * (g * g) * vq * c.dx;
-        c.w1y = 8.0 * (g * g) * vq * c.dy;
-        c.w1z = 8.0 * (g * g) * vq * c.dz;
-        c.w2 = 8.0 * (g * g) * (g * g) * vq;
+        Hex8Uniform c = hex8_uniform_constants(d);
         k_elem_force_hex8_uniform<<<grid_for(d->nelem, 128), 128, 0, s>>>(d->conn, u, d->K, d->G,
                                                                           d->nelem, c, fe);
     }
@@ -1229,12 +1383,20 @@ int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stre
     GF_TRY(check_operator(d));
     GF_REQUIRE(coef, "null coefficient array");
     GF_REQUIRE((reinterpret_cast<uintptr_t>(coef) & 15u) == 0, "coef must be 16-byte aligned");
-    if (!(d->uniform && d->nne == 4 && std::fabs(d->hx - d->hy) <= 1e-12 * d->hx))
-        return fail(GFGPU_ERR_UNSUPPORTED, "gfgpu_verlet_precompute: uniform square Quad4 only");
+    bool square = d->uniform && d->nne == 4 && std::fabs(d->hx - d->hy) <= 1e-12 * d->hx;
+    bool cube = d->uniform && d->nne == 8 && std::fabs(d->hx - d->hy) <= 1e-12 * d->hx &&
+                std::fabs(d->hx - d->hz) <= 1e-12 * d->hx;
+    if (!square && !cube)
+        return fail(GFGPU_ERR_UNSUPPORTED,
+                    "gfgpu_verlet_precompute: uniform square Quad4 or cube Hex8 only");
     if (d->nelem == 0) return GFGPU_OK;
     double g = 1.0 / std::sqrt(3.0);
-    k_quad4_square_coef<<<grid_for(d->nelem), kBlock, 0, S(stream)>>>(d->K, d->G, d->nelem, g * g,
-                                                                      coef);
+    if (square)
+        k_quad4_square_coef<<<grid_for(d->nelem), kBlock, 0, S(stream)>>>(d->K, d->G, d->nelem, g * g,
+                                                                          coef);
+    else
+        k_hex8_cube_coef<<<grid_for(d->nelem), kBlock, 0, S(stream)>>>(d->K, d->G, d->nelem,
+                                                                       hex8_uniform_constants(d), coef);
     return check_launch("verlet_precompute");
 }
 

@@ -110,8 +110,12 @@ class VelocityVerlet:
             if uniform is True and not d.uniform:
                 raise RuntimeError("mesh is not a uniform axis-aligned Quad4 mesh")
         self.coef = None
-        if d.uniform and nne == 4 and abs(d.hx - d.hy) <= 1e-12 * d.hx:
-            self.coef = torch.empty((nelem, 4), dtype=torch.float64, device=_dev.device())
+        square = d.uniform and nne == 4 and abs(d.hx - d.hy) <= 1e-12 * d.hx
+        cube = (d.uniform and nne == 8 and abs(d.hx - d.hy) <= 1e-12 * d.hx
+                and abs(d.hx - d.hz) <= 1e-12 * d.hx)
+        if square or cube:
+            self.coef = torch.empty((nelem, 4 if square else 8), dtype=torch.float64,
+                                    device=_dev.device())
             _lib.call("gfgpu_verlet_precompute", C.addressof(d), self.coef.data_ptr(),
                       _dev.stream())
             d.coef = self.coef.data_ptr()
@@ -167,7 +171,9 @@ class VelocityVerlet:
     def path(self):
         if not self.desc.uniform:
             return "general"
-        return "uniform-square" if self.desc.coef else "uniform"
+        if self.desc.coef:
+            return "uniform-square" if self.desc.nne == 4 else "uniform-cube"
+        return "uniform"
 
     def use_general_path(self):
         self.desc.uniform = 0

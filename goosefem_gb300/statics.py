@@ -60,11 +60,15 @@ class ElasticStatic:
                       v0.ctypes.data, 1e-12)
             if uniform is True and not d.uniform:
                 raise RuntimeError("mesh is not uniform")
-        # square Quad4 elements: 4 precomputed coefficients per element (34 FP64 instructions
-        # per element in the operator instead of recombining K, G every application)
+        # square Quad4 / cube Hex8 elements: precomputed per-element coefficients (34 / ~171 FP64
+        # instructions per element in the operator instead of recombining K, G every application)
         self.coef = None
-        if d.uniform and nne == 4 and abs(d.hx - d.hy) <= 1e-12 * d.hx:
-            self.coef = torch.empty((nelem, 4), dtype=torch.float64, device=_dev.device())
+        square = d.uniform and nne == 4 and abs(d.hx - d.hy) <= 1e-12 * d.hx
+        cube = (d.uniform and nne == 8 and abs(d.hx - d.hy) <= 1e-12 * d.hx
+                and abs(d.hx - d.hz) <= 1e-12 * d.hx)
+        if square or cube:
+            self.coef = torch.empty((nelem, 4 if square else 8), dtype=torch.float64,
+                                    device=_dev.device())
             _lib.call("gfgpu_verlet_precompute", C.addressof(d), self.coef.data_ptr(),
                       _dev.stream())
             d.coef = self.coef.data_ptr()

@@ -302,8 +302,11 @@ int64_t gfgpu_verlet_workspace_bytes(const gfgpu_verlet_desc* d);
 int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
                                 const double* vol_host, double rtol);
 /* Uniform square Quad4 meshes: fill coef [nelem, 4] with the element coefficients that depend on
- * K and G only (lam/4, G/2, G/4, g^2 (lam + 3G)/4, lam = K - 2G/3); set d->coef = coef to use
- * them. Returns GFGPU_ERR_UNSUPPORTED for other meshes. */
+ * K and G only (lam/4, G/2, G/4, g^2 (lam + 3G)/4, lam = K - 2G/3); uniform cube Hex8 meshes:
+ * coef [nelem, 8] with the folded mode coefficients (w0 d lam, w0 d G, 2 w0 d G, w1 d lam,
+ * w1 d G, 2 w1 d G, 3 w1 d G, w2 d^2 (lam + 4G); d = 1/(4h), w* the Gauss weights of the
+ * constant, linear and trilinear modes). Set d->coef = coef to use them. Returns
+ * GFGPU_ERR_UNSUPPORTED for other meshes. */
 int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stream_t stream);
 /* Host set-up of the lumped-mass classes: reads part and inv back from the device, and if the
  * free dofs take at most GFGPU_MASS_CLASSES distinct inverse masses (a Regular mesh with uniform

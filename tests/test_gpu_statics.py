@@ -150,3 +150,26 @@ def test_flexible_cg_jacobi_hex8(gf, oracle, n):
     xg = to_np(x)
     assert rel.value <= 1e-8 and S.residual(A, iip, xg) <= 1e-8
     assert np.linalg.norm(xg - x_ref) / np.linalg.norm(x_ref) <= 1e-6
+
+
+def test_hex8_cube_coefficients_match_uniform_kernel(gf, oracle):
+    """Cube Hex8 with folded per-element coefficients (gfgpu_verlet_precompute) against the
+    uniform-box kernel that recombines K, G in every application and against the oracle."""
+    R = oracle
+    coor, conn = R.hex8_regular(6, 5, 4)
+    coor = coor * 0.7
+    K, G = seeded_material(conn.shape[0], 46)
+    nnode = coor.shape[0]
+    dofs = np.arange(nnode * 3).reshape(nnode, 3)
+    st = gf.statics.ElasticStatic(coor, conn, dofs, K, G, np.array([0, 1, 2]), uniform=True)
+    assert st.coef is not None and tuple(st.coef.shape) == (conn.shape[0], 8)
+    u = seeded_field((nnode, 3), 47)
+    f_cube = to_np(st.force(u))
+    st.desc.coef = None
+    f_box = to_np(st.force(u))
+    assert rel_err(f_cube, f_box) <= 1e-13
+    dNx, vol = R.compute_dN(R.as_element(conn, coor), *R.hex8_gauss())
+    eps = R.sym_grad_n_vector(dNx, R.as_element(conn, u))
+    f_r = R.assemble_node(conn, dofs, R.int_grad_n_dot_tensor2_dv(dNx, vol, R.elastic_stress(
+        eps, K, G)))
+    assert rel_err(f_cube, f_r) <= RTOL
