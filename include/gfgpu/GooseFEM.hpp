@@ -761,6 +761,137 @@ private:
     bool m_changed = true;
 };
 
+/* MatrixPartitioned(conn, dofs, iip) (MatrixPartitioned.h:34-460): the assembled sparse matrix
+ * as one CSR in the partitioned numbering (unknown dofs first); assemble() sums the element
+ * matrices in the reference's triplet order (bit-exact). */
+class MatrixPartitioned {
+public:
+    MatrixPartitioned(const host::array<int32_t>& conn, const host::array<int32_t>& dofs,
+                      const host::array<int32_t>& iip)
+        : m_vec(conn, dofs)
+    {
+        int64_t n = dofs.size();
+        host::array<int32_t> iiu({n}), part(dofs.shape());
+        int64_t nnu = 0;
+        check(gfgpu_host_partition(dofs.data(), n, iip.data(), iip.size(), iiu.data(), part.data(), &nnu),
+              "MatrixPartitioned");
+        m_nnu = nnu;
+        m_ndof = m_vec.ndof();
+        host::array<int32_t> iperm({m_ndof});
+        for (int64_t i = 0; i < nnu; ++i) iperm[i] = iiu[i];
+        for (int64_t i = 0; i < iip.size(); ++i) iperm[nnu + i] = iip[i];
+        int64_t nelem = conn.shape(0);
+        int32_t nne = int32_t(conn.shape(1)), nd = int32_t(dofs.shape(1));
+        int64_t K = int64_t(nne) * nd, total = nelem * K * K;
+        host::array<int32_t> rowptr({m_ndof + 1}), col({std::max<int64_t>(total, 1)}),
+            cptr({total + 1}), cidx({std::max<int64_t>(total, 1)});
+        int64_t nnz = 0;
+        check(gfgpu_host_matrix_pattern(conn.data(), part.data(), nelem, nne, dofs.shape(0), nd, m_ndof,
+                                        rowptr.data(), col.data(), cptr.data(), cidx.data(), &nnz),
+              "MatrixPartitioned: pattern");
+        m_nnz = nnz;
+        m_rowptr = array<int32_t>::from_host(rowptr);
+        m_col = array<int32_t>::from_host(col.data(), {std::max<int64_t>(nnz, 1)});
+        m_cptr = array<int32_t>::from_host(cptr.data(), {nnz + 1});
+        m_cidx = array<int32_t>::from_host(cidx);
+        m_val = array<double>({std::max<int64_t>(nnz, 1)});
+        m_iperm = array<int32_t>::from_host(iperm);
+    }
+    int64_t ndof() const { return m_ndof; }
+    int64_t nnu() const { return m_nnu; }
+    int64_t nnp() const { return m_ndof - m_nnu; }
+    int64_t nnz() const { return m_nnz; }
+    const Vector& vector() const { return m_vec; }
+    /* MatrixPartitioned::assemble (MatrixPartitioned.h:156-200) */
+    void assemble(const array<double>& elemmat)
+    {
+        check(gfgpu_matrix_assemble(m_cptr.data(), m_cidx.data(), m_nnz, elemmat.data(), m_val.data(),
+                                    nullptr),
+              "MatrixPartitioned::assemble");
+    }
+    /* dot / Dot on dofval (MatrixPartitioned.h:378-398) or nodevec (:354-376) */
+    void dot(const array<double>& x, array<double>& b) const
+    {
+        if (x.dimension() == 1) {
+            check(gfgpu_matrixp_dot_dofval(m_rowptr.data(), m_col.data(), m_val.data(), m_ndof, m_nnu,
+                                           m_iperm.data(), x.data(), b.data(), nullptr),
+                  "MatrixPartitioned::dot");
+            return;
+        }
+        array<double> xd = m_vec.AsDofs(x), bd({m_ndof});
+        dot(xd, bd);
+        m_vec.asNode(bd, b);
+    }
+    array<double> Dot(const array<double>& x) const
+    {
+        array<double> b(x.shape());
+        dot(x, b);
+        return b;
+    }
+    /* Reaction (MatrixPartitioned.h:401-433): copy of b with b_p = A_pu x_u + A_pp x_p */
+    array<double> Reaction(const array<double>& x, const array<double>& b) const
+    {
+        if (x.dimension() == 1) {
+            array<double> r = b.copy();
+            check(gfgpu_matrixp_reaction_dofval(m_rowptr.data(), m_col.data(), m_val.data(), m_ndof,
+                                                m_nnu, m_iperm.data(), x.data(), r.data(), nullptr),
+                  "MatrixPartitioned::Reaction");
+            return r;
+        }
+        array<double> xd = m_vec.AsDofs(x), bd = m_vec.AsDofs(b);
+        array<double> rd = Reaction(xd, bd);
+        return m_vec.AsNode(rd);
+    }
+
+private:
+    friend class MatrixPartitionedSolver;
+    Vector m_vec;
+    int64_t m_ndof = 0, m_nnu = 0, m_nnz = 0;
+    array<int32_t> m_rowptr, m_col, m_cptr, m_cidx, m_iperm;
+    array<double> m_val;
+};
+
+/* MatrixPartitionedSolver (MatrixPartitioned.h:471-642): x_u = A_uu^-1 (b_u - A_up x_p). The
+ * reference factorises A_uu (Eigen SimplicialLDLT); here Jacobi-PCG on the assembled A_uu in FP64
+ * to the relative residual tol (gfgpu_matrixp_solve). */
+class MatrixPartitionedSolver {
+public:
+    explicit MatrixPartitionedSolver(double tol = 1e-12, int64_t maxiter = 1000000)
+        : m_tol(tol), m_maxiter(maxiter)
+    {
+    }
+    /* solve on dofval or nodevec: x holds x_p (and the initial guess of x_u) */
+    void solve(MatrixPartitioned& A, const array<double>& b, array<double>& x)
+    {
+        if (x.dimension() != 1) {
+            array<double> bd = A.m_vec.AsDofs(b), xd = A.m_vec.AsDofs(x);
+            solve(A, bd, xd);
+            A.m_vec.asNode(xd, x);
+            return;
+        }
+        int64_t nb = gfgpu_matrixp_solve_workspace_bytes(A.m_nnu);
+        array<double> ws({nb / 8 + 1});
+        check(gfgpu_matrixp_solve(A.m_rowptr.data(), A.m_col.data(), A.m_val.data(), A.m_ndof, A.m_nnu,
+                                  A.m_iperm.data(), b.data(), x.data(), m_tol, m_maxiter, 16,
+                                  ws.data(), nullptr, &m_iters, &m_relres),
+              "MatrixPartitionedSolver::solve");
+    }
+    array<double> Solve(MatrixPartitioned& A, const array<double>& b, const array<double>& x)
+    {
+        array<double> r = x.copy();
+        solve(A, b, r);
+        return r;
+    }
+    int64_t iterations() const { return m_iters; }
+    double relres() const { return m_relres; }
+
+private:
+    double m_tol;
+    int64_t m_maxiter;
+    int64_t m_iters = 0;
+    double m_relres = 0.0;
+};
+
 } // namespace gfgpu
 
 #endif

@@ -6,8 +6,9 @@
 //   stress; int_gradN_dot_tensor2_dV; assembleNode; MatrixDiagonal::assemble(Int_N_scalar_NT_dV).
 // Usage: test_api <inputs.bin> <outputs.bin>
 //   inputs:  nx (int64), K[nelem], G[nelem], u[nnode*2] (float64)
-//   outputs: dNx, vol, ue, eps, sig, fe, fint, M, then the planar dV, eps, sig, fe (float64,
-//   concatenated)
+//   outputs: dNx, vol, ue, eps, sig, fe, fint, M, then the planar dV, eps, sig, fe, then the
+//   static solution (float64, concatenated)
+#include <algorithm>
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -79,6 +80,43 @@ int main(int argc, char** argv)
                   "stress");
         auto fe3 = planar.Int_gradN_dot_tensor2_dV(Sig3);
 
+        // static solve with the assembled stiffness: bottom edge fixed, top edge uy = -0.01
+        // (MatrixPartitioned + MatrixPartitionedSolver, the pattern of
+        // docs/examples/statics/FixedDisplacements_LinearElastic)
+        GF::host::array<double> C4({nelem, 4, 2, 2, 2, 2});
+        for (int64_t e = 0; e < nelem; ++e)
+            for (int q = 0; q < 4; ++q)
+                for (int i = 0; i < 2; ++i)
+                    for (int j = 0; j < 2; ++j)
+                        for (int k = 0; k < 2; ++k)
+                            for (int l = 0; l < 2; ++l) {
+                                double dij = i == j, dkl = k == l, dik = i == k, djl = j == l,
+                                       dil = i == l, djk = j == k;
+                                C4[((((e * 4 + q) * 2 + i) * 2 + j) * 2 + k) * 2 + l] =
+                                    K[e] * dij * dkl + G[e] * (dik * djl + dil * djk - 2.0 / 3.0 * dij * dkl);
+                            }
+        auto Ke = quad.Int_gradN_dot_tensor4_dot_gradNT_dV(GF::array<double>::from_host(C4));
+        auto bot = mesh.nodesBottomEdge(), top = mesh.nodesTopEdge();
+        GF::host::array<int32_t> iip({bot.size() * 2 + top.size()});
+        std::vector<int32_t> ip;
+        for (int64_t i = 0; i < bot.size(); ++i) {
+            ip.push_back(bot[i] * 2);
+            ip.push_back(bot[i] * 2 + 1);
+        }
+        for (int64_t i = 0; i < top.size(); ++i) ip.push_back(top[i] * 2 + 1);
+        std::sort(ip.begin(), ip.end());
+        for (size_t i = 0; i < ip.size(); ++i) iip[int64_t(i)] = ip[i];
+        GF::MatrixPartitioned Kmat(mesh.conn(), mesh.dofs(), iip);
+        Kmat.assemble(Ke);
+        GF::host::array<double> xh({nnode, 2}, 0.0);
+        for (int64_t i = 0; i < top.size(); ++i) xh(top[i], 1) = -0.01;
+        auto xs = GF::array<double>::from_host(xh);
+        GF::MatrixPartitionedSolver solver(1e-12);
+        auto zero = GF::array<double>({nnode, 2});
+        zero.fill_zero();
+        solver.solve(Kmat, zero, xs);
+        if (solver.relres() > 1e-12) return 5;
+
         std::ofstream out(argv[2], std::ios::binary);
         dump(out, quad.GradN());
         dump(out, quad.dV());
@@ -92,6 +130,7 @@ int main(int argc, char** argv)
         dump(out, Eps3);
         dump(out, Sig3);
         dump(out, fe3);
+        dump(out, xs);
 
         // error path: a shape mismatch is reported as std::runtime_error
         bool threw = false;

@@ -63,5 +63,16 @@ def test_cpp_api_force_chain_and_mass(oracle, tmp_path):
         got = data[k:k + ref.size].reshape(ref.shape)
         k += ref.size
         assert rel_err(got, ref) <= RTOL
+    # static solve through MatrixPartitioned + MatrixPartitionedSolver vs the direct solve
+    from oracle import statics as S
+
+    bot = np.arange(nx + 1)
+    top = bot + nx * (nx + 1)
+    iip = np.unique(np.concatenate([(bot[:, None] * 2 + np.arange(2)).ravel(), top * 2 + 1]))
+    xp = np.where(np.isin(iip, top * 2 + 1), -0.01, 0.0)
+    x_ref = S.solve_partitioned(S.stiffness(coor, conn, K, G), iip, xp)
+    xs = data[k:k + nnode * 2]
+    k += nnode * 2
+    assert np.linalg.norm(xs - x_ref) / np.linalg.norm(x_ref) <= 1e-9
     assert k == data.size
     assert np.array_equal(data[:dNx.size].reshape(dNx.shape), dNx)  # set-up is bit-exact
