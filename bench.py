@@ -187,6 +187,18 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def job_rate(units_per_rank, ms_local, world, device="cpu"):
+    """Whole-job throughput of `world` replicas that each processed `units_per_rank` units: the
+    slowest rank's time (MAX over ranks) bounds the job. Returns (units/s, max ms)."""
+    import torch
+
+    t = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(t.item())
+    return world * units_per_rank / (ms * 1e-3), ms
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -266,11 +278,7 @@ def run_gpu(args, rank, world):
     barrier()
     ms = e0.elapsed_time(e1)
     clocks = sampler.stop() if sampler else None
-    ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(ms_t.item())
-    value = world * nelem * NIP * inc * args.steps / (ms * 1e-3)
+    value, ms = job_rate(nelem * NIP * inc * args.steps, ms, world, dev)
 
     # ---------------------------------------------------------------- per-kernel timing
     # element kernel alone (same launch as inside the step), on the launching stream
@@ -322,11 +330,7 @@ def run_gpu(args, rank, world):
     e1.record(stream)
     barrier()
     ms_e2e = e0.elapsed_time(e1)
-    t = torch.tensor([ms_e2e], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_e2e = float(t.item())
-    e2e_value = world * nelem * NIP * inc * args.steps / (ms_e2e * 1e-3)
+    e2e_value, ms_e2e = job_rate(nelem * NIP * inc * args.steps, ms_e2e, world, dev)
     state_bytes = 3 * nnode * 2 * 8
 
     if rank != 0:
