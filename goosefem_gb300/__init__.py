@@ -14,7 +14,7 @@ from . import mesh as Mesh  # noqa: E402
 from . import element as Element  # noqa: E402
 from .vector import Vector, VectorPartitioned  # noqa: E402
 from .matrix import MatrixDiagonal, MatrixDiagonalPartitioned  # noqa: E402
-from .matrix import Matrix, MatrixPartitioned, MatrixPartitionedSolver  # noqa: E402
+from .matrix import Matrix, MatrixPartitioned, MatrixPartitionedSolver, MatrixSolver  # noqa: E402
 from . import tyings as Tyings  # noqa: E402
 from .tyings import VectorPartitionedTyings, MatrixPartitionedTyings  # noqa: E402
 from .tyings import MatrixPartitionedTyingsSolver  # noqa: E402
@@ -24,7 +24,7 @@ from .statics import ElasticStatic  # noqa: E402
 from ._lib import set_strict, GFGPUError  # noqa: E402
 
 __all__ = ["Mesh", "Element", "Vector", "VectorPartitioned", "MatrixDiagonal",
-           "MatrixDiagonalPartitioned", "Matrix", "MatrixPartitioned", "MatrixPartitionedSolver",
+           "MatrixDiagonalPartitioned", "Matrix", "MatrixPartitioned", "MatrixPartitionedSolver", "MatrixSolver",
            "Tyings", "VectorPartitionedTyings", "MatrixPartitionedTyings",
            "MatrixPartitionedTyingsSolver", "VelocityVerlet", "elastic_stress", "critical_dt",
            "set_strict", "GFGPUError"]

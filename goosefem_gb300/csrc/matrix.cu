@@ -252,6 +252,196 @@ k_mp_residual(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ co
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
+// ---------------------------------------------------------------- MINRES on a full CSR
+
+// Scalar slots of the MINRES recurrences (Paige & Saunders 1975, preconditioned form).
+enum {
+    R_BETA = 0, R_OLDB, R_ALFA, R_DBAR, R_EPS, R_OLDEPS, R_CS, R_SN, R_PHI, R_PHIBAR, R_DELTA,
+    R_DENOM, R_BETA1, R_BB, R_RR, R_COUNT
+};
+
+// v = y / beta; Av = A v - (beta / oldb) r1 (k > 0); partial v.Av -> alfa
+__global__ void __launch_bounds__(256)
+k_mr_lanczos(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+             const double* __restrict__ val, int64_t n, const double* __restrict__ sc, int first,
+             const double* __restrict__ yv, double* __restrict__ v, const double* __restrict__ r1,
+             double* __restrict__ yo, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    const double s = 1.0 / sc[R_BETA];
+    const double c = first ? 0.0 : sc[R_BETA] / sc[R_OLDB];
+    double a = 0.0;
+    GF_FOR(i, n)
+    {
+        double acc = 0.0;
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) acc = fma(val[k], s * yv[col[k]], acc);
+        double vi = s * yv[i];
+        double yi = first ? acc : fma(-c, r1[i], acc);
+        v[i] = vi;
+        yo[i] = yi;
+        a = fma(vi, yi, a);
+    }
+    double t = block_sum(a, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+// y -= (alfa / beta) r2; r1 = r2; r2 = y; z = Minv r2; partial r2.z
+__global__ void __launch_bounds__(256)
+k_mr_rotate(int64_t n, const double* __restrict__ sc, const double* __restrict__ minv,
+            const double* __restrict__ yo, double* __restrict__ r1, double* __restrict__ r2,
+            double* __restrict__ z, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    const double c = sc[R_ALFA] / sc[R_BETA];
+    double a = 0.0;
+    GF_FOR(i, n)
+    {
+        double yi = fma(-c, r2[i], yo[i]);
+        r1[i] = r2[i];
+        r2[i] = yi;
+        double zi = minv[i] * yi;
+        z[i] = zi;
+        a = fma(yi, zi, a);
+    }
+    double t = block_sum(a, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+// fixed-order sum of a partial row into sc[slot]; then the scalar step of MINRES (mode 1: after
+// alfa; mode 2: after beta_new)
+__global__ void k_mr_scalar(const double* __restrict__ partial, double* __restrict__ sc, int mode)
+{
+    __shared__ double sh[32];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < kMRed; i += blockDim.x) a += partial[i];
+    double t = block_sum(a, sh);
+    if (threadIdx.x != 0) return;
+    if (mode == 1) {
+        sc[R_ALFA] = t;
+        return;
+    }
+    double alfa = sc[R_ALFA];
+    double oldb = sc[R_BETA];
+    double beta = sqrt(fmax(t, 0.0));
+    double oldeps = sc[R_EPS];
+    double cs = sc[R_CS], sn = sc[R_SN], dbar = sc[R_DBAR];
+    double delta = cs * dbar + sn * alfa;
+    double gbar = sn * dbar - cs * alfa;
+    double epsln = sn * beta;
+    dbar = -cs * beta;
+    double gamma = fmax(sqrt(gbar * gbar + beta * beta), 1e-300);
+    cs = gbar / gamma;
+    sn = beta / gamma;
+    double phi = cs * sc[R_PHIBAR];
+    sc[R_PHIBAR] = sn * sc[R_PHIBAR];
+    sc[R_OLDB] = oldb;
+    sc[R_BETA] = beta;
+    sc[R_OLDEPS] = oldeps;
+    sc[R_EPS] = epsln;
+    sc[R_DBAR] = dbar;
+    sc[R_CS] = cs;
+    sc[R_SN] = sn;
+    sc[R_PHI] = phi;
+    sc[R_DELTA] = delta;
+    sc[R_DENOM] = 1.0 / gamma;
+}
+
+// w1 = w2; w2 = w; w = (v - oldeps w1 - delta w2) / gamma; x += phi w; next y = z
+__global__ void k_mr_step(int64_t n, const double* __restrict__ sc, const double* __restrict__ v,
+                          double* __restrict__ w1, double* __restrict__ w2, double* __restrict__ w,
+                          double* __restrict__ x)
+{
+    const double oe = sc[R_OLDEPS], de = sc[R_DELTA], dn = sc[R_DENOM], ph = sc[R_PHI];
+    GF_FOR(i, n)
+    {
+        double a = w2[i], b = w[i];
+        double wn = (v[i] - oe * a - de * b) * dn;
+        w1[i] = a;
+        w2[i] = b;
+        w[i] = wn;
+        x[i] = fma(ph, wn, x[i]);
+    }
+}
+
+// r = b - A x (partial r.r in row 0, b.b in row 1), z = Minv r; minv = 1 / |diag| (1 if 0)
+__global__ void __launch_bounds__(256)
+k_mr_init(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+          const double* __restrict__ val, int64_t n, const double* __restrict__ b,
+          const double* __restrict__ x, double* __restrict__ minv, double* __restrict__ r,
+          double* __restrict__ z, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double rz = 0.0, bb = 0.0;
+    GF_FOR(i, n)
+    {
+        double acc = 0.0, d = 0.0;
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            acc = fma(val[k], x[col[k]], acc);
+            if (col[k] == i) d = val[k];
+        }
+        double mi = d != 0.0 ? 1.0 / fabs(d) : 1.0;
+        double ri = b[i] - acc;
+        minv[i] = mi;
+        r[i] = ri;
+        z[i] = mi * ri;
+        rz = fma(ri, mi * ri, rz);
+        bb = fma(b[i], b[i], bb);
+    }
+    double t0 = block_sum(rz, sh), t1 = block_sum(bb, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = t0;
+        partial[kMRed + blockIdx.x] = t1;
+    }
+}
+
+__global__ void k_mr_start(const double* __restrict__ partial, double* __restrict__ sc)
+{
+    __shared__ double sh[32];
+    double a = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < kMRed; i += blockDim.x) {
+        a += partial[i];
+        c += partial[kMRed + i];
+    }
+    double rz = block_sum(a, sh), bb = block_sum(c, sh);
+    if (threadIdx.x == 0) {
+        double beta1 = sqrt(fmax(rz, 0.0));
+        for (int k = 0; k < R_COUNT; ++k) sc[k] = 0.0;
+        sc[R_BETA] = beta1;
+        sc[R_BETA1] = beta1;
+        sc[R_PHIBAR] = beta1;
+        sc[R_CS] = -1.0;
+        sc[R_BB] = bb;
+    }
+}
+
+// true residual: partial ||b - A x||^2
+__global__ void __launch_bounds__(256)
+k_mr_resid(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+           const double* __restrict__ val, int64_t n, const double* __restrict__ b,
+           const double* __restrict__ x, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double rr = 0.0;
+    GF_FOR(i, n)
+    {
+        double acc = 0.0;
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) acc = fma(val[k], x[col[k]], acc);
+        double ri = b[i] - acc;
+        rr = fma(ri, ri, rr);
+    }
+    double t = block_sum(rr, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+__global__ void k_mr_rr(const double* __restrict__ partial, double* __restrict__ sc)
+{
+    __shared__ double sh[32];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < kMRed; i += blockDim.x) a += partial[i];
+    double t = block_sum(a, sh);
+    if (threadIdx.x == 0) sc[R_RR] = t;
+}
+
 struct MpWs {
     double *xu, *dinv, *r, *z, *p, *q, *partial, *sc;
 };
@@ -426,6 +616,91 @@ int gfgpu_matrixp_solve(const int32_t* rowptr, const int32_t* col, const double*
     GF_TRY(read());
     *relres = std::sqrt(h[M_RR]) / bnorm;
     if (*relres > tol) return fail(GFGPU_ERR_DIVERGED, "gfgpu_matrixp_solve: tolerance not reached");
+    return GFGPU_OK;
+}
+
+int64_t gfgpu_matrix_solve_workspace_bytes(int64_t n)
+{
+    return n < 0 ? 0 : 10 * a256(std::max<int64_t>(n, 1) * 8) + a256(2 * kMRed * 8) + a256(R_COUNT * 8);
+}
+
+int gfgpu_matrix_solve(const int32_t* rowptr, const int32_t* col, const double* val, int64_t n,
+                       const double* b, double* x, double tol, int64_t maxiter, int32_t check_every,
+                       void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres)
+{
+    GF_REQUIRE(rowptr && col && val && b && x && workspace && iters && relres, "bad argument");
+    GF_REQUIRE(n > 0 && !too_big(n) && tol > 0.0 && maxiter >= 0, "bad argument");
+    if (check_every < 1) check_every = 1;
+    cudaStream_t s = S(stream);
+    char* c = static_cast<char*>(workspace);
+    double* vec[10];
+    for (auto& p : vec) {
+        p = reinterpret_cast<double*>(c);
+        c += a256(n * 8);
+    }
+    double *minv = vec[0], *r1 = vec[1], *r2 = vec[2], *y = vec[3], *v = vec[4], *yo = vec[5],
+           *w = vec[6], *w1 = vec[7], *w2 = vec[8];
+    double* partial = reinterpret_cast<double*>(c);
+    c += a256(2 * kMRed * 8);
+    double* sc = reinterpret_cast<double*>(c);
+    const unsigned gb = kMRed;
+    double h[R_COUNT];
+    auto read = [&]() -> int {
+        GF_TRY(check_cuda(cudaMemcpyAsync(h, sc, sizeof(h), cudaMemcpyDeviceToHost, s), "copy"));
+        return check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    };
+    // r1 = r2 = b - A x, y = Minv r1, beta1 = sqrt(r1.y), w = w1 = w2 = 0
+    k_mr_init<<<gb, 256, 0, s>>>(rowptr, col, val, n, b, x, minv, r1, y, partial);
+    k_mr_start<<<1, 1024, 0, s>>>(partial, sc);
+    GF_TRY(check_cuda(cudaMemcpyAsync(r2, r1, n * 8, cudaMemcpyDeviceToDevice, s), "copy"));
+    GF_TRY(check_cuda(cudaMemsetAsync(w, 0, n * 8, s), "memset"));
+    GF_TRY(check_cuda(cudaMemsetAsync(w1, 0, n * 8, s), "memset"));
+    GF_TRY(check_cuda(cudaMemsetAsync(w2, 0, n * 8, s), "memset"));
+    GF_TRY(check_launch("matrix_solve set-up"));
+    GF_TRY(read());
+    double bnorm = std::sqrt(h[R_BB]);
+    if (bnorm == 0.0) bnorm = 1.0;
+    const double beta1 = h[R_BETA1];
+    int64_t it = 0;
+    // MINRES (Paige & Saunders) with the SPD preconditioner diag(|A_ii|); phibar estimates the
+    // preconditioned residual norm, the exit test uses the true residual
+    double rel = beta1 > 0.0 ? 1.0 : 0.0;
+    int rc = GFGPU_OK;
+    while (rel > tol && it < maxiter) {
+        int64_t nb = std::min<int64_t>(check_every, maxiter - it);
+        for (int64_t k = 0; k < nb; ++k) {
+            k_mr_lanczos<<<gb, 256, 0, s>>>(rowptr, col, val, n, sc, it + k == 0, y, v, r1, yo, partial);
+            k_mr_scalar<<<1, 1024, 0, s>>>(partial, sc, 1);
+            k_mr_rotate<<<gb, 256, 0, s>>>(n, sc, minv, yo, r1, r2, y, partial);
+            k_mr_scalar<<<1, 1024, 0, s>>>(partial, sc, 2);
+            k_mr_step<<<grid_for(n), kBlock, 0, s>>>(n, sc, v, w1, w2, w, x);
+        }
+        it += nb;
+        rc = check_launch("matrix_solve iteration");
+        if (rc != GFGPU_OK) break;
+        rc = read();
+        if (rc != GFGPU_OK) break;
+        if (!std::isfinite(h[R_PHIBAR])) {
+            rc = fail(GFGPU_ERR_NAN, "gfgpu_matrix_solve: non-finite residual");
+            break;
+        }
+        if (h[R_PHIBAR] <= tol * beta1 || h[R_BETA] == 0.0) {
+            k_mr_resid<<<gb, 256, 0, s>>>(rowptr, col, val, n, b, x, partial);
+            k_mr_rr<<<1, 1024, 0, s>>>(partial, sc);
+            rc = read();
+            if (rc != GFGPU_OK) break;
+            rel = std::sqrt(h[R_RR]) / bnorm;
+            if (h[R_BETA] == 0.0) break; // exact Krylov breakdown: the solution is reached
+        }
+    }
+    *iters = it;
+    GF_TRY(rc);
+    k_mr_resid<<<gb, 256, 0, s>>>(rowptr, col, val, n, b, x, partial);
+    k_mr_rr<<<1, 1024, 0, s>>>(partial, sc);
+    GF_TRY(check_launch("matrix_solve residual"));
+    GF_TRY(read());
+    *relres = std::sqrt(h[R_RR]) / bnorm;
+    if (*relres > tol) return fail(GFGPU_ERR_DIVERGED, "gfgpu_matrix_solve: tolerance not reached");
     return GFGPU_OK;
 }
 

@@ -248,6 +248,7 @@ class Matrix:
         self._setup(self._dofs_h)
 
     def _setup(self, dmap):
+        self._dmap = dmap
         rp, col, cptr, cidx = _pattern(self._conn_h, dmap, self._nnode, self._ndof)
         self._rowptr_h, self._col_h = rp, col
         self.rowptr, self.col = _dev.dev_i32(rp), _dev.dev_i32(col)
@@ -280,8 +281,70 @@ class Matrix:
     def assemble(self, elemmat):
         em = _dev.dev_f64(elemmat)
         _dev.check_shape(em, self.shape_elemmat(), "assemble")
+        if getattr(self, "_custom", False):  # set() / add() replaced the element pattern
+            self._setup(self._dmap)
+            self._custom = False
         _lib.call("gfgpu_matrix_assemble", self.cptr.data_ptr(), self.cidx.data_ptr(), self._nnz,
                   em.data_ptr(), self._val.data_ptr(), _dev.stream())
+
+    @staticmethod
+    def _triplets_csr(r, c, v, n):
+        """CSR of triplets with equal (row, col) summed in their order (Eigen setFromTriplets)."""
+        order = np.lexsort((np.arange(r.size), c, r))
+        r, c, v = r[order], c[order], v[order]
+        rowptr = np.zeros(n + 1, dtype=np.int64)
+        cols, vals = [], []
+        k = 0
+        while k < r.size:
+            j = k
+            acc = v[k]
+            while j + 1 < r.size and r[j + 1] == r[k] and c[j + 1] == c[k]:
+                j += 1
+                acc = acc + v[j]
+            cols.append(c[k])
+            vals.append(acc)
+            rowptr[r[k] + 1] += 1
+            k = j + 1
+        return np.cumsum(rowptr), np.asarray(cols, dtype=np.int64), np.asarray(vals)
+
+    def _replace(self, rowptr, col, val):
+        self._rowptr_h = rowptr.astype(np.int32)
+        self._col_h = col.astype(np.int32)
+        self.rowptr = _dev.dev_i32(self._rowptr_h)
+        self.col = _dev.dev_i32(self._col_h if col.size else np.zeros(1, np.int32))
+        self._nnz = int(col.size)
+        self._val = torch.as_tensor(val if val.size else np.zeros(1), dtype=torch.float64,
+                                    device=_dev.device()).contiguous()
+        self._custom = True
+
+    def _block(self, rows, cols, matrix):
+        rows = np.asarray(rows, dtype=np.int64).ravel()
+        cols = np.asarray(cols, dtype=np.int64).ravel()
+        m = np.asarray(matrix.cpu() if isinstance(matrix, torch.Tensor) else matrix, dtype=np.float64)
+        if m.shape != (rows.size, cols.size):
+            raise ValueError("matrix must be [rows.size, cols.size]")
+        if rows.size and (rows.max() >= self._ndof or cols.max() >= self._ndof):
+            raise ValueError("row / column out of range")
+        r = np.repeat(rows, cols.size)
+        c = np.tile(cols, rows.size)
+        return self._triplets_csr(r, c, m.ravel(), self._ndof)
+
+    def set(self, rows, cols, matrix):
+        """Matrix::set (Matrix.h:737-764): the matrix becomes the given block (setFromTriplets)."""
+        self._replace(*self._block(rows, cols, matrix))
+
+    def add(self, rows, cols, matrix):
+        """Matrix::add (Matrix.h:766-790): the given block is added (sparse sum)."""
+        rp_b, col_b, val_b = self._block(rows, cols, matrix)
+        rp_a, col_a, val_a = self._csr_host()
+        rp_a = rp_a.astype(np.int64)
+        ra = np.repeat(np.arange(self._ndof), np.diff(rp_a))
+        rb = np.repeat(np.arange(self._ndof), np.diff(rp_b))
+        # union: A entries first, then B, so that equal entries are summed as a + b
+        r = np.concatenate([ra, rb])
+        c = np.concatenate([col_a[:ra.size].astype(np.int64), col_b])
+        v = np.concatenate([val_a[:ra.size], val_b])
+        self._replace(*self._triplets_csr(r, c, v, self._ndof))
 
     def data(self):
         """(rowptr, col, val) of the CSR (device)."""
@@ -399,6 +462,43 @@ class MatrixPartitionedSolver:
                   A._ndof, A._nnu, A.iperm.data_ptr(), bd.contiguous().data_ptr(), xd.data_ptr(),
                   self.tol, self.maxiter, self.check_every, ws.data_ptr(), _dev.stream(),
                   C.addressof(it), C.addressof(rel))
+        self.iterations, self.relres = int(it.value), float(rel.value)
+        return xd if v is None else v.AsNode(xd)
+
+    def solve(self, A, b, x):
+        out = self.Solve(A, b, x)
+        x.copy_(out)
+        return x
+
+
+class MatrixSolver:
+    """MatrixSolver (Matrix.h:866-912): x = A^-1 b for a Matrix. The reference factorises A
+    (Eigen SimplicialLDLT: any symmetric, possibly indefinite, nonsingular matrix); here MINRES
+    with the preconditioner diag(|A_ii|) in FP64 to the relative residual `tol`
+    (gfgpu_matrix_solve)."""
+
+    def __init__(self, tol=1e-12, maxiter=1000000, check_every=16):
+        self.tol, self.maxiter, self.check_every = float(tol), int(maxiter), int(check_every)
+        self.iterations = 0
+        self.relres = 0.0
+
+    def Solve(self, A, b, x0=None):
+        """dofval or nodevec b; returns x (x0: optional initial guess)."""
+        import ctypes as C
+
+        bd, v = A._dofval(b)
+        bd = bd.contiguous()
+        if x0 is None:
+            xd = torch.zeros(A._ndof, dtype=torch.float64, device=bd.device)
+        else:
+            xd, _ = A._dofval(x0)
+            xd = xd.clone().contiguous()
+        nb = int(_lib.lib().gfgpu_matrix_solve_workspace_bytes(A._ndof))
+        ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=bd.device)
+        it, rel = C.c_int64(0), C.c_double(0.0)
+        _lib.call("gfgpu_matrix_solve", A.rowptr.data_ptr(), A.col.data_ptr(), A._val.data_ptr(),
+                  A._ndof, bd.data_ptr(), xd.data_ptr(), self.tol, self.maxiter, self.check_every,
+                  ws.data_ptr(), _dev.stream(), C.addressof(it), C.addressof(rel))
         self.iterations, self.relres = int(it.value), float(rel.value)
         return xd if v is None else v.AsNode(xd)
 

@@ -444,6 +444,14 @@ int gfgpu_matrixp_dot_dofval(const int32_t* rowptr, const int32_t* col, const do
 int gfgpu_matrixp_reaction_dofval(const int32_t* rowptr, const int32_t* col, const double* val,
                                   int64_t ndof, int64_t nnu, const int32_t* iperm, const double* x,
                                   double* b, gfgpu_stream_t stream);
+/* MatrixSolver::solve (Matrix.h:866-912; Eigen SimplicialLDLT there) for a symmetric matrix,
+ * possibly indefinite: x = A^-1 b by MINRES (Paige & Saunders) with the preconditioner
+ * diag(|A_ii|), from the initial guess in x, to ||b - A x|| <= tol ||b|| (true residual).
+ * Deterministic. Synchronises. */
+int64_t gfgpu_matrix_solve_workspace_bytes(int64_t n);
+int gfgpu_matrix_solve(const int32_t* rowptr, const int32_t* col, const double* val, int64_t n,
+                       const double* b, double* x, double tol, int64_t maxiter, int32_t check_every,
+                       void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres);
 /* MatrixPartitionedSolver::solve (MatrixPartitioned.h:583-613; Eigen SimplicialLDLT there):
  * x_u = A_uu^-1 (b_u - A_up x_p) by Jacobi-PCG in FP64 to ||r|| <= tol ||b_u - A_up x_p||, from
  * the initial guess in x; b, x dofval in the original numbering (x_p read from x, x_u written).

@@ -140,3 +140,70 @@ def test_matrix_partitioned_solver_vs_direct(gf, oracle):
     xn.ravel()[iip] = xp
     x2 = to_np(solver.Solve(A, np.zeros_like(xn), xn))
     assert np.array_equal(x2.ravel(), xg)
+
+
+def test_reference_matrix_solve(gf):
+    """tests/basic/Matrix.cpp "solve": random symmetric element matrices on a 2x2 mesh,
+    C = A b, Solve(A, C) recovers b (MINRES: the assembled matrix is indefinite)."""
+    rng = np.random.default_rng(50)
+    mesh = gf.Mesh.Quad4.Regular(2, 2)
+    nelem = mesh.nelem()
+    a = rng.uniform(size=(nelem, 8, 8))
+    a = 0.5 * (a + np.transpose(a, (0, 2, 1)))
+    b = rng.uniform(size=mesh.nnode() * 2)
+    A = gf.Matrix(mesh.conn(), mesh.dofs())
+    A.assemble(a)
+    C = A.Dot(b)
+    solver = gf.MatrixSolver(tol=1e-13)
+    B = to_np(solver.Solve(A, C))
+    assert np.allclose(B, b, rtol=1e-8, atol=1e-10)
+
+
+@pytest.mark.parametrize("nodevec", [False, True])
+def test_reference_matrix_set_add_dot_solve(gf, oracle, nodevec):
+    """tests/basic/Matrix.cpp "set/add/dot/solve": K.set(a) then K.add(a^T) gives A = a + a^T;
+    Todense, Dot and Solve (dofval and nodevec)."""
+    rng = np.random.default_rng(51)
+    a = rng.uniform(size=(10, 10))
+    A = a + a.T
+    conn = np.zeros((1, 5), dtype=np.int64)
+    dofs = np.arange(10).reshape(5, 2)
+    K = gf.Matrix(conn, dofs)
+    K.set(np.arange(10), np.arange(10), a)
+    K.add(np.arange(10), np.arange(10), a.T)
+    assert np.allclose(K.Todense(), A, rtol=0, atol=1e-15)
+    x = rng.uniform(size=(5, 2) if nodevec else 10)
+    b = (A @ x.ravel()).reshape(x.shape)
+    assert np.allclose(to_np(K.Dot(x)), b, rtol=1e-14, atol=1e-14)
+    solver = gf.MatrixSolver(tol=1e-13)
+    assert np.allclose(to_np(solver.Solve(K, b)), x, rtol=1e-8, atol=1e-10)
+    # an element assembly afterwards restores the element pattern (here all five local nodes
+    # are node 0, as in the reference test)
+    em = rng.uniform(size=(1, 10, 10))
+    K.assemble(em)
+    rp, col, val = oracle.matrix_assemble(conn, dofs, em, 10)
+    ref = np.zeros((10, 10))
+    ref[np.repeat(np.arange(10), np.diff(rp)), col] = val
+    assert np.array_equal(K.Todense(), ref)
+
+
+def test_matrix_solver_spd_stiffness(gf, oracle):
+    """MatrixSolver on an SPD system: the full stiffness plus a stiff spring at the fixed dofs
+    (penalty) against a dense solve."""
+    from oracle import statics as S
+
+    mesh = gf.Mesh.Quad4.Regular(8, 6)
+    coor, conn, dofs = mesh.coor(), mesh.conn(), mesh.dofs()
+    Kmat, G = seeded_material(mesh.nelem(), 52)
+    Ke = _stiffness_elemmat(oracle, coor, conn, Kmat, G)
+    A = gf.Matrix(conn, dofs)
+    A.assemble(Ke)
+    fixed = dofs[mesh.nodesBottomEdge()].ravel()
+    A.add(fixed, fixed, 1e3 * np.eye(fixed.size))
+    rng = np.random.default_rng(53)
+    b = rng.normal(size=A.ndof())
+    solver = gf.MatrixSolver(tol=1e-12)
+    x = to_np(solver.Solve(A, b))
+    Ad = A.Todense()
+    assert np.linalg.norm(Ad @ x - b) <= 1e-11 * np.linalg.norm(b)
+    assert np.linalg.norm(x - np.linalg.solve(Ad, b)) <= 1e-8 * np.linalg.norm(x)
