@@ -263,7 +263,8 @@ enum {
 // v = y / beta; Av = A v - (beta / oldb) r1 (k > 0); partial v.Av -> alfa
 __global__ void __launch_bounds__(256)
 k_mr_lanczos(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-             const double* __restrict__ val, int64_t n, const double* __restrict__ sc, int first,
+             const double* __restrict__ val, int64_t n, int64_t clim, const double* __restrict__ sc,
+             int first,
              const double* __restrict__ yv, double* __restrict__ v, const double* __restrict__ r1,
              double* __restrict__ yo, double* __restrict__ partial)
 {
@@ -274,7 +275,8 @@ k_mr_lanczos(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col
     GF_FOR(i, n)
     {
         double acc = 0.0;
-        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) acc = fma(val[k], s * yv[col[k]], acc);
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            if (col[k] < clim) acc = fma(val[k], s * yv[col[k]], acc);
         double vi = s * yv[i];
         double yi = first ? acc : fma(-c, r1[i], acc);
         v[i] = vi;
@@ -366,7 +368,7 @@ __global__ void k_mr_step(int64_t n, const double* __restrict__ sc, const double
 // r = b - A x (partial r.r in row 0, b.b in row 1), z = Minv r; minv = 1 / |diag| (1 if 0)
 __global__ void __launch_bounds__(256)
 k_mr_init(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-          const double* __restrict__ val, int64_t n, const double* __restrict__ b,
+          const double* __restrict__ val, int64_t n, int64_t clim, const double* __restrict__ b,
           const double* __restrict__ x, double* __restrict__ minv, double* __restrict__ r,
           double* __restrict__ z, double* __restrict__ partial)
 {
@@ -376,6 +378,7 @@ k_mr_init(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
     {
         double acc = 0.0, d = 0.0;
         for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            if (col[k] >= clim) continue;
             acc = fma(val[k], x[col[k]], acc);
             if (col[k] == i) d = val[k];
         }
@@ -417,7 +420,7 @@ __global__ void k_mr_start(const double* __restrict__ partial, double* __restric
 // true residual: partial ||b - A x||^2
 __global__ void __launch_bounds__(256)
 k_mr_resid(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-           const double* __restrict__ val, int64_t n, const double* __restrict__ b,
+           const double* __restrict__ val, int64_t n, int64_t clim, const double* __restrict__ b,
            const double* __restrict__ x, double* __restrict__ partial)
 {
     __shared__ double sh[32];
@@ -425,7 +428,8 @@ k_mr_resid(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
     GF_FOR(i, n)
     {
         double acc = 0.0;
-        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) acc = fma(val[k], x[col[k]], acc);
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            if (col[k] < clim) acc = fma(val[k], x[col[k]], acc);
         double ri = b[i] - acc;
         rr = fma(ri, ri, rr);
     }
@@ -440,6 +444,22 @@ __global__ void k_mr_rr(const double* __restrict__ partial, double* __restrict__
     for (int i = threadIdx.x; i < kMRed; i += blockDim.x) a += partial[i];
     double t = block_sum(a, sh);
     if (threadIdx.x == 0) sc[R_RR] = t;
+}
+
+// rhs_u = b_u - A_up x_p and x_u from x (original numbering through iperm)
+__global__ void k_mp_rhs(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                         const double* __restrict__ val, int64_t nnu, const int32_t* __restrict__ iperm,
+                         const double* __restrict__ b, const double* __restrict__ x,
+                         double* __restrict__ rhs, double* __restrict__ xu)
+{
+    GF_FOR(i, nnu)
+    {
+        double sp = 0.0;
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            if (col[k] >= nnu) sp = fma(val[k], x[iperm[col[k]]], sp);
+        rhs[i] = b[iperm[i]] - sp;
+        xu[i] = x[iperm[i]];
+    }
 }
 
 struct MpWs {
@@ -624,14 +644,12 @@ int64_t gfgpu_matrix_solve_workspace_bytes(int64_t n)
     return n < 0 ? 0 : 10 * a256(std::max<int64_t>(n, 1) * 8) + a256(2 * kMRed * 8) + a256(R_COUNT * 8);
 }
 
-int gfgpu_matrix_solve(const int32_t* rowptr, const int32_t* col, const double* val, int64_t n,
-                       const double* b, double* x, double tol, int64_t maxiter, int32_t check_every,
-                       void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres)
+static int minres_core(const int32_t* rowptr, const int32_t* col, const double* val, int64_t n,
+                       int64_t clim, const double* b, double* x, double tol, int64_t maxiter,
+                       int32_t check_every, void* workspace, cudaStream_t s, int64_t* iters,
+                       double* relres)
 {
-    GF_REQUIRE(rowptr && col && val && b && x && workspace && iters && relres, "bad argument");
-    GF_REQUIRE(n > 0 && !too_big(n) && tol > 0.0 && maxiter >= 0, "bad argument");
     if (check_every < 1) check_every = 1;
-    cudaStream_t s = S(stream);
     char* c = static_cast<char*>(workspace);
     double* vec[10];
     for (auto& p : vec) {
@@ -650,7 +668,7 @@ int gfgpu_matrix_solve(const int32_t* rowptr, const int32_t* col, const double* 
         return check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     };
     // r1 = r2 = b - A x, y = Minv r1, beta1 = sqrt(r1.y), w = w1 = w2 = 0
-    k_mr_init<<<gb, 256, 0, s>>>(rowptr, col, val, n, b, x, minv, r1, y, partial);
+    k_mr_init<<<gb, 256, 0, s>>>(rowptr, col, val, n, clim, b, x, minv, r1, y, partial);
     k_mr_start<<<1, 1024, 0, s>>>(partial, sc);
     GF_TRY(check_cuda(cudaMemcpyAsync(r2, r1, n * 8, cudaMemcpyDeviceToDevice, s), "copy"));
     GF_TRY(check_cuda(cudaMemsetAsync(w, 0, n * 8, s), "memset"));
@@ -669,7 +687,7 @@ int gfgpu_matrix_solve(const int32_t* rowptr, const int32_t* col, const double* 
     while (rel > tol && it < maxiter) {
         int64_t nb = std::min<int64_t>(check_every, maxiter - it);
         for (int64_t k = 0; k < nb; ++k) {
-            k_mr_lanczos<<<gb, 256, 0, s>>>(rowptr, col, val, n, sc, it + k == 0, y, v, r1, yo, partial);
+            k_mr_lanczos<<<gb, 256, 0, s>>>(rowptr, col, val, n, clim, sc, it + k == 0, y, v, r1, yo, partial);
             k_mr_scalar<<<1, 1024, 0, s>>>(partial, sc, 1);
             k_mr_rotate<<<gb, 256, 0, s>>>(n, sc, minv, yo, r1, r2, y, partial);
             k_mr_scalar<<<1, 1024, 0, s>>>(partial, sc, 2);
@@ -681,11 +699,11 @@ int gfgpu_matrix_solve(const int32_t* rowptr, const int32_t* col, const double* 
         rc = read();
         if (rc != GFGPU_OK) break;
         if (!std::isfinite(h[R_PHIBAR])) {
-            rc = fail(GFGPU_ERR_NAN, "gfgpu_matrix_solve: non-finite residual");
+            rc = fail(GFGPU_ERR_NAN, "MINRES: non-finite residual");
             break;
         }
         if (h[R_PHIBAR] <= tol * beta1 || h[R_BETA] == 0.0) {
-            k_mr_resid<<<gb, 256, 0, s>>>(rowptr, col, val, n, b, x, partial);
+            k_mr_resid<<<gb, 256, 0, s>>>(rowptr, col, val, n, clim, b, x, partial);
             k_mr_rr<<<1, 1024, 0, s>>>(partial, sc);
             rc = read();
             if (rc != GFGPU_OK) break;
@@ -695,13 +713,55 @@ int gfgpu_matrix_solve(const int32_t* rowptr, const int32_t* col, const double* 
     }
     *iters = it;
     GF_TRY(rc);
-    k_mr_resid<<<gb, 256, 0, s>>>(rowptr, col, val, n, b, x, partial);
+    k_mr_resid<<<gb, 256, 0, s>>>(rowptr, col, val, n, clim, b, x, partial);
     k_mr_rr<<<1, 1024, 0, s>>>(partial, sc);
     GF_TRY(check_launch("matrix_solve residual"));
     GF_TRY(read());
     *relres = std::sqrt(h[R_RR]) / bnorm;
-    if (*relres > tol) return fail(GFGPU_ERR_DIVERGED, "gfgpu_matrix_solve: tolerance not reached");
+    if (*relres > tol) return fail(GFGPU_ERR_DIVERGED, "MINRES: tolerance not reached");
     return GFGPU_OK;
+}
+
+
+int gfgpu_matrix_solve(const int32_t* rowptr, const int32_t* col, const double* val, int64_t n,
+                       const double* b, double* x, double tol, int64_t maxiter, int32_t check_every,
+                       void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres)
+{
+    GF_REQUIRE(rowptr && col && val && b && x && workspace && iters && relres, "bad argument");
+    GF_REQUIRE(n > 0 && !too_big(n) && tol > 0.0 && maxiter >= 0, "bad argument");
+    return minres_core(rowptr, col, val, n, n, b, x, tol, maxiter, check_every, workspace, S(stream),
+                       iters, relres);
+}
+
+int64_t gfgpu_matrixp_solve_minres_workspace_bytes(int64_t nnu)
+{
+    return nnu < 0 ? 0 : gfgpu_matrix_solve_workspace_bytes(nnu) + 2 * a256(std::max<int64_t>(nnu, 1) * 8);
+}
+
+int gfgpu_matrixp_solve_minres(const int32_t* rowptr, const int32_t* col, const double* val,
+                               int64_t ndof, int64_t nnu, const int32_t* iperm, const double* b,
+                               double* x, double tol, int64_t maxiter, int32_t check_every,
+                               void* workspace, gfgpu_stream_t stream, int64_t* iters,
+                               double* relres)
+{
+    GF_REQUIRE(rowptr && col && val && iperm && b && x && workspace && iters && relres,
+               "bad argument");
+    GF_REQUIRE(nnu > 0 && nnu <= ndof && !too_big(ndof) && tol > 0.0 && maxiter >= 0, "bad argument");
+    cudaStream_t s = S(stream);
+    char* c = static_cast<char*>(workspace);
+    double* rhs = reinterpret_cast<double*>(c);
+    c += a256(nnu * 8);
+    double* xu = reinterpret_cast<double*>(c);
+    c += a256(nnu * 8);
+    k_mp_rhs<<<grid_for(nnu), kBlock, 0, s>>>(rowptr, col, val, nnu, iperm, b, x, rhs, xu);
+    GF_TRY(check_launch("matrixp_solve_minres rhs"));
+    int rc = minres_core(rowptr, col, val, nnu, nnu, rhs, xu, tol, maxiter, check_every, c, s, iters,
+                         relres);
+    if (rc == GFGPU_OK || rc == GFGPU_ERR_DIVERGED) {
+        k_mp_scatter<<<grid_for(nnu), kBlock, 0, s>>>(nnu, iperm, xu, x);
+        GF_TRY(check_launch("matrixp_solve_minres scatter"));
+    }
+    return rc;
 }
 
 } // extern "C"

@@ -409,6 +409,14 @@ class MatrixPartitioned(Matrix):
     def iip(self):
         return self._iip.copy()
 
+    def _block(self, rows, cols, matrix):
+        """set / add blocks (MatrixPartitioned.h:213-320) in the partitioned numbering."""
+        part1d = np.empty(self._ndof, dtype=np.int64)
+        part1d[self._iperm_h] = np.arange(self._ndof)
+        rows = part1d[np.asarray(rows, dtype=np.int64).ravel()]
+        cols = part1d[np.asarray(cols, dtype=np.int64).ravel()]
+        return super()._block(rows, cols, matrix)
+
     def Todense(self):
         """MatrixPartitioned::Todense (MatrixPartitioned.h:324-351), original numbering."""
         rp, col, val = self._csr_host()
@@ -440,11 +448,16 @@ class MatrixPartitioned(Matrix):
 
 class MatrixPartitionedSolver:
     """MatrixPartitionedSolver (MatrixPartitioned.h:471-642): x_u = A_uu^-1 (b_u - A_up x_p).
-    The reference factorises A_uu (Eigen SimplicialLDLT); here a Jacobi-PCG on the assembled
-    A_uu in FP64 to a relative residual `tol` (gfgpu_matrixp_solve)."""
+    The reference factorises A_uu (Eigen SimplicialLDLT: any symmetric nonsingular A_uu); here
+    a Krylov solve of the assembled A_uu in FP64 to a relative residual `tol`: method "minres"
+    (default; gfgpu_matrixp_solve_minres, indefinite allowed) or "pcg" (Jacobi-PCG,
+    gfgpu_matrixp_solve, SPD only)."""
 
-    def __init__(self, tol=1e-12, maxiter=1000000, check_every=16):
+    def __init__(self, tol=1e-12, maxiter=1000000, check_every=16, method="minres"):
+        if method not in ("minres", "pcg"):
+            raise ValueError("method is 'minres' or 'pcg'")
         self.tol, self.maxiter, self.check_every = float(tol), int(maxiter), int(check_every)
+        self.method = method
         self.iterations = 0
         self.relres = 0.0
 
@@ -455,10 +468,11 @@ class MatrixPartitionedSolver:
         xd, v = A._dofval(x)
         bd, _ = A._dofval(b)
         xd = xd.clone().contiguous()
-        nb = int(_lib.lib().gfgpu_matrixp_solve_workspace_bytes(A._nnu))
+        fn = "gfgpu_matrixp_solve_minres" if self.method == "minres" else "gfgpu_matrixp_solve"
+        nb = int(getattr(_lib.lib(), fn + "_workspace_bytes")(A._nnu))
         ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=xd.device)
         it, rel = C.c_int64(0), C.c_double(0.0)
-        _lib.call("gfgpu_matrixp_solve", A.rowptr.data_ptr(), A.col.data_ptr(), A._val.data_ptr(),
+        _lib.call(fn, A.rowptr.data_ptr(), A.col.data_ptr(), A._val.data_ptr(),
                   A._ndof, A._nnu, A.iperm.data_ptr(), bd.contiguous().data_ptr(), xd.data_ptr(),
                   self.tol, self.maxiter, self.check_every, ws.data_ptr(), _dev.stream(),
                   C.addressof(it), C.addressof(rel))

@@ -452,6 +452,15 @@ int64_t gfgpu_matrix_solve_workspace_bytes(int64_t n);
 int gfgpu_matrix_solve(const int32_t* rowptr, const int32_t* col, const double* val, int64_t n,
                        const double* b, double* x, double tol, int64_t maxiter, int32_t check_every,
                        void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres);
+/* The same solve of the partitioned system as gfgpu_matrixp_solve (below) by MINRES with the
+ * preconditioner diag(|A_ii|): for symmetric A_uu that may be indefinite (the reference's
+ * Eigen LDLT accepts those). */
+int64_t gfgpu_matrixp_solve_minres_workspace_bytes(int64_t nnu);
+int gfgpu_matrixp_solve_minres(const int32_t* rowptr, const int32_t* col, const double* val,
+                               int64_t ndof, int64_t nnu, const int32_t* iperm, const double* b,
+                               double* x, double tol, int64_t maxiter, int32_t check_every,
+                               void* workspace, gfgpu_stream_t stream, int64_t* iters,
+                               double* relres);
 /* MatrixPartitionedSolver::solve (MatrixPartitioned.h:583-613; Eigen SimplicialLDLT there):
  * x_u = A_uu^-1 (b_u - A_up x_p) by Jacobi-PCG in FP64 to ||r|| <= tol ||b_u - A_up x_p||, from
  * the initial guess in x; b, x dofval in the original numbering (x_p read from x, x_u written).

@@ -852,12 +852,13 @@ private:
 };
 
 /* MatrixPartitionedSolver (MatrixPartitioned.h:471-642): x_u = A_uu^-1 (b_u - A_up x_p). The
- * reference factorises A_uu (Eigen SimplicialLDLT); here Jacobi-PCG on the assembled A_uu in FP64
- * to the relative residual tol (gfgpu_matrixp_solve). */
+ * reference factorises A_uu (Eigen SimplicialLDLT); here a Krylov solve of the assembled A_uu in
+ * FP64 to the relative residual tol: MINRES (default, symmetric indefinite allowed;
+ * gfgpu_matrixp_solve_minres) or Jacobi-PCG (pcg = true, SPD; gfgpu_matrixp_solve). */
 class MatrixPartitionedSolver {
 public:
-    explicit MatrixPartitionedSolver(double tol = 1e-12, int64_t maxiter = 1000000)
-        : m_tol(tol), m_maxiter(maxiter)
+    explicit MatrixPartitionedSolver(double tol = 1e-12, int64_t maxiter = 1000000, bool pcg = false)
+        : m_tol(tol), m_maxiter(maxiter), m_pcg(pcg)
     {
     }
     /* solve on dofval or nodevec: x holds x_p (and the initial guess of x_u) */
@@ -869,11 +870,12 @@ public:
             A.m_vec.asNode(xd, x);
             return;
         }
-        int64_t nb = gfgpu_matrixp_solve_workspace_bytes(A.m_nnu);
+        int64_t nb = m_pcg ? gfgpu_matrixp_solve_workspace_bytes(A.m_nnu)
+                           : gfgpu_matrixp_solve_minres_workspace_bytes(A.m_nnu);
         array<double> ws({nb / 8 + 1});
-        check(gfgpu_matrixp_solve(A.m_rowptr.data(), A.m_col.data(), A.m_val.data(), A.m_ndof, A.m_nnu,
-                                  A.m_iperm.data(), b.data(), x.data(), m_tol, m_maxiter, 16,
-                                  ws.data(), nullptr, &m_iters, &m_relres),
+        auto fn = m_pcg ? gfgpu_matrixp_solve : gfgpu_matrixp_solve_minres;
+        check(fn(A.m_rowptr.data(), A.m_col.data(), A.m_val.data(), A.m_ndof, A.m_nnu, A.m_iperm.data(),
+                 b.data(), x.data(), m_tol, m_maxiter, 16, ws.data(), nullptr, &m_iters, &m_relres),
               "MatrixPartitionedSolver::solve");
     }
     array<double> Solve(MatrixPartitioned& A, const array<double>& b, const array<double>& x)
@@ -888,6 +890,7 @@ public:
 private:
     double m_tol;
     int64_t m_maxiter;
+    bool m_pcg;
     int64_t m_iters = 0;
     double m_relres = 0.0;
 };

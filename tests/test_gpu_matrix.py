@@ -128,7 +128,7 @@ def test_matrix_partitioned_solver_vs_direct(gf, oracle):
     ndof = int(dofs.max()) + 1
     x = np.zeros(ndof)
     x[iip] = xp
-    solver = gf.MatrixPartitionedSolver(tol=1e-12)
+    solver = gf.MatrixPartitionedSolver(tol=1e-12, method="pcg")
     xg = to_np(solver.Solve(A, np.zeros(ndof), x))
     Ad = S.stiffness(coor, conn, K, G)
     x_ref = S.solve_partitioned(Ad, iip, xp)
@@ -207,3 +207,54 @@ def test_matrix_solver_spd_stiffness(gf, oracle):
     Ad = A.Todense()
     assert np.linalg.norm(Ad @ x - b) <= 1e-11 * np.linalg.norm(b)
     assert np.linalg.norm(x - np.linalg.solve(Ad, b)) <= 1e-8 * np.linalg.norm(x)
+
+
+
+@pytest.mark.parametrize("method", ["minres", "pcg"])
+def test_matrix_partitioned_solver_methods_agree(gf, oracle, method):
+    from oracle import statics as S
+
+    mesh = gf.Mesh.Quad4.Regular(12, 9)
+    coor, conn, dofs = mesh.coor(), mesh.conn(), mesh.dofs()
+    K, G = seeded_material(mesh.nelem(), 54)
+    bot, top = mesh.nodesBottomEdge(), mesh.nodesTopEdge()
+    iip = np.unique(np.concatenate([dofs[bot].ravel(), dofs[top, 1]]))
+    xp = np.where(np.isin(iip, dofs[top, 1]), -1e-2, 0.0)
+    A = gf.MatrixPartitioned(conn, dofs, iip)
+    A.assemble(_stiffness_elemmat(oracle, coor, conn, K, G))
+    x = np.zeros(int(dofs.max()) + 1)
+    x[iip] = xp
+    solver = gf.MatrixPartitionedSolver(tol=1e-12, method=method)
+    xg = to_np(solver.Solve(A, np.zeros_like(x), x))
+    x_ref = S.solve_partitioned(S.stiffness(coor, conn, K, G), iip, xp)
+    assert np.linalg.norm(xg - x_ref) / np.linalg.norm(x_ref) <= 1e-9
+
+
+@pytest.mark.parametrize("nodevec", [False, True])
+def test_reference_matrix_partitioned(gf, nodevec):
+    """tests/basic/MatrixParitioned.cpp: random symmetric (indefinite) matrices, "solve" on a
+    2x2 mesh with iip = {0, 5, 7, 13} and "set/add/dot/solve" with iip = {0, 2, 4}."""
+    rng = np.random.default_rng(55)
+    mesh = gf.Mesh.Quad4.Regular(2, 2)
+    a = rng.uniform(size=(mesh.nelem(), 8, 8))
+    a = 0.5 * (a + np.transpose(a, (0, 2, 1)))
+    x = rng.uniform(size=mesh.nnode() * 2)
+    A = gf.MatrixPartitioned(mesh.conn(), mesh.dofs(), np.array([0, 5, 7, 13]))
+    A.assemble(a)
+    b = A.Dot(x)
+    xc = to_np(gf.MatrixPartitionedSolver(tol=1e-13).Solve(A, b, x))
+    assert np.allclose(xc, x, rtol=1e-8, atol=1e-10)
+    # set / add / dot / solve
+    a = rng.uniform(size=(10, 10))
+    Ad = a + a.T
+    conn = np.zeros((1, 5), dtype=np.int64)
+    dofs = np.arange(10).reshape(5, 2)
+    K = gf.MatrixPartitioned(conn, dofs, np.array([0, 2, 4]))
+    K.set(np.arange(10), np.arange(10), a)
+    K.add(np.arange(10), np.arange(10), a.T)
+    assert np.allclose(K.Todense(), Ad, rtol=0, atol=1e-15)
+    xv = rng.uniform(size=(5, 2) if nodevec else 10)
+    bv = (Ad @ xv.ravel()).reshape(xv.shape)
+    assert np.allclose(to_np(K.Dot(xv)), bv, rtol=1e-14, atol=1e-14)
+    assert np.allclose(to_np(gf.MatrixPartitionedSolver(tol=1e-13).Solve(K, bv, xv)), xv,
+                       rtol=1e-8, atol=1e-10)
