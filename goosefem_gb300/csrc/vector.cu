@@ -155,6 +155,42 @@ __global__ void k_mul(const double* __restrict__ a, const double* __restrict__ b
     GF_FOR(t, n) o[t] = __dmul_rn(a[t], b[t]);
 }
 
+// out[t] = [u | p][idx[t]]: the partitioned vector read back through a partitioned index table
+__global__ void k_from_partitioned(const int32_t* __restrict__ idx, int64_t n, int64_t nnu,
+                                   const double* __restrict__ u, const double* __restrict__ p,
+                                   double* __restrict__ out)
+{
+    GF_FOR(t, n)
+    {
+        int64_t d = __ldg(idx + t);
+        out[t] = d < nnu ? __ldg(u + d) : __ldg(p + (d - nnu));
+    }
+}
+
+__global__ void k_from_partitioned_elem(const int32_t* __restrict__ conn,
+                                        const int32_t* __restrict__ part, int64_t nem, int nd,
+                                        int64_t nnu, const double* __restrict__ u,
+                                        const double* __restrict__ p, double* __restrict__ elemvec)
+{
+    GF_FOR(t, nem * nd)
+    {
+        int64_t k = t / nd;
+        int i = static_cast<int>(t - k * nd);
+        int64_t d = __ldg(part + static_cast<int64_t>(__ldg(conn + k)) * nd + i);
+        elemvec[t] = d < nnu ? __ldg(u + d) : __ldg(p + (d - nnu));
+    }
+}
+
+__global__ void k_copy_part(const int32_t* __restrict__ part, int64_t n, int64_t lo, int64_t hi,
+                            const double* __restrict__ src, double* __restrict__ dest)
+{
+    GF_FOR(t, n)
+    {
+        int64_t d = __ldg(part + t);
+        if (d >= lo && d < hi) dest[t] = src[t];
+    }
+}
+
 } // namespace gfgpu
 
 using namespace gfgpu;
@@ -304,6 +340,44 @@ int gfgpu_dofval_mul(const double* a, const double* b, int64_t n, double* out,
     if (n == 0) return GFGPU_OK;
     k_mul<<<grid_for(n), kBlock, 0, S(stream)>>>(a, b, n, out);
     return check_launch("dofval_mul");
+}
+
+int gfgpu_from_partitioned(const int32_t* idx, int64_t n, int64_t nnu, int64_t nnp,
+                           const double* u, const double* p, double* out, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(idx && out && (u || nnu == 0) && (p || nnp == 0) && nnu >= 0 && nnp >= 0,
+               "bad argument");
+    GF_REQUIRE(!too_big(n) && !too_big(nnu + nnp), "too many values");
+    if (n == 0) return GFGPU_OK;
+    k_from_partitioned<<<grid_for(n), kBlock, 0, S(stream)>>>(idx, n, nnu, u, p, out);
+    return check_launch("from_partitioned");
+}
+
+int gfgpu_from_partitioned_elemvec(const int32_t* conn, const int32_t* part, int64_t nelem,
+                                   int32_t nne, int32_t ndim, int64_t nnu, int64_t nnp,
+                                   const double* u, const double* p, double* elemvec,
+                                   gfgpu_stream_t stream)
+{
+    GF_REQUIRE(conn && part && elemvec && (u || nnu == 0) && (p || nnp == 0) && nne > 0 &&
+                   ndim > 0 && nnu >= 0 && nnp >= 0,
+               "bad argument");
+    GF_REQUIRE(!too_big(nelem * nne * ndim) && !too_big(nnu + nnp), "too many elements");
+    if (nelem == 0) return GFGPU_OK;
+    k_from_partitioned_elem<<<grid_for(nelem * nne * ndim), kBlock, 0, S(stream)>>>(
+        conn, part, nelem * nne, ndim, nnu, u, p, elemvec);
+    return check_launch("from_partitioned_elemvec");
+}
+
+int gfgpu_copy_partitioned_nodevec(const int32_t* part, int64_t nnode, int32_t ndim, int64_t lo,
+                                   int64_t hi, const double* src, double* dest,
+                                   gfgpu_stream_t stream)
+{
+    GF_REQUIRE(part && src && dest && ndim > 0 && lo >= 0 && hi >= lo, "bad argument");
+    GF_REQUIRE(!too_big(nnode * ndim), "too many nodes");
+    if (nnode == 0 || hi == lo) return GFGPU_OK;
+    k_copy_part<<<grid_for(nnode * ndim), kBlock, 0, S(stream)>>>(part, nnode * ndim, lo, hi, src,
+                                                                  dest);
+    return check_launch("copy_partitioned_nodevec");
 }
 
 } // extern "C"

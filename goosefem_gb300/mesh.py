@@ -125,6 +125,19 @@ class Quad4:
         def nodesRightEdge(self):
             return (np.arange(self._ny + 1) * (self._nx + 1) + self._nx).astype(np.int32)
 
+        def nodesBottomOpenEdge(self):
+            """Bottom edge without corners (MeshQuad4.h:148-151)."""
+            return np.arange(1, self._nx, dtype=np.int32)
+
+        def nodesTopOpenEdge(self):
+            return (np.arange(1, self._nx) + self._ny * (self._nx + 1)).astype(np.int32)
+
+        def nodesLeftOpenEdge(self):
+            return (np.arange(1, self._ny) * (self._nx + 1)).astype(np.int32)
+
+        def nodesRightOpenEdge(self):
+            return (np.arange(1, self._ny) * (self._nx + 1) + self._nx).astype(np.int32)
+
         def nodesBottomLeftCorner(self):
             return 0
 
@@ -136,6 +149,12 @@ class Quad4:
 
         def nodesTopRightCorner(self):
             return self._ny * (self._nx + 1) + self._nx
+
+        # the reference's aliases (Mesh.h:466-500)
+        nodesLeftBottomCorner = nodesBottomLeftCorner
+        nodesLeftTopCorner = nodesTopLeftCorner
+        nodesRightBottomCorner = nodesBottomRightCorner
+        nodesRightTopCorner = nodesTopRightCorner
 
         def nodesOrigin(self):
             return 0
@@ -196,6 +215,29 @@ class Hex8:
             """z = top face (MeshHex8.h:146-158)."""
             n = (self._nx + 1) * (self._ny + 1)
             return (np.arange(n) + self._nz * n).astype(np.int32)
+
+        def _grid(self):
+            nx, ny, nz = self._nx + 1, self._ny + 1, self._nz + 1
+            return np.arange(nx * ny * nz, dtype=np.int32).reshape(nz, ny, nx)
+
+        def nodesLeft(self):
+            """x = 0 face, iz outer, iy inner (MeshHex8.h:160-171)."""
+            return self._grid()[:, :, 0].ravel().copy()
+
+        def nodesRight(self):
+            """x = top face (MeshHex8.h:173-185)."""
+            return self._grid()[:, :, -1].ravel().copy()
+
+        def nodesBottom(self):
+            """y = 0 face, iz outer, ix inner (MeshHex8.h:187-198)."""
+            return self._grid()[:, 0, :].ravel().copy()
+
+        def nodesTop(self):
+            """y = top face (MeshHex8.h:200-212)."""
+            return self._grid()[:, -1, :].ravel().copy()
+
+        def nodesOrigin(self):
+            return 0
 
         def dofsPeriodic(self, nodes_periodic):
             """RegularBase::dofsPeriodic (Mesh.h:291-306) for a given nodesPeriodic table."""

@@ -187,16 +187,21 @@ class Vector:
 
 class VectorPartitioned(Vector):
     """VectorPartitioned(conn, dofs, iip) (VectorPartitioned.h:45-661): dofs split into
-    unknown (iiu) and prescribed (iip) parts."""
+    unknown (iiu) and prescribed (iip) parts; `part` [nnode, ndim] numbers every dof by its
+    position in [iiu, iip]."""
 
     def __init__(self, conn, dofs, iip):
         super().__init__(conn, dofs)
         iip = _dev.host_i32(iip)
         self._iiu, self._part = _mesh.partition(self._dofs_h, iip)
         self._iip = iip.copy()
+        dof2part = np.empty(self._ndof, dtype=np.int32)
+        dof2part[self._iiu] = np.arange(self._iiu.size, dtype=np.int32)
+        dof2part[self._iip] = self._iiu.size + np.arange(self._iip.size, dtype=np.int32)
         self.iiu_d = _dev.dev_i32(self._iiu)
         self.iip_d = _dev.dev_i32(self._iip)
         self.part_d = _dev.dev_i32(self._part)
+        self.dof2part_d = _dev.dev_i32(dof2part)
 
     def nnu(self):
         return self._iiu.size
@@ -211,29 +216,103 @@ class VectorPartitioned(Vector):
         return self._iip.copy()
 
     def dofs_is_u(self):
+        """VectorPartitioned::dofs_is_u (VectorPartitioned.h:126-140)."""
         return self._part < self.nnu()
 
     def dofs_is_p(self):
+        """VectorPartitioned::dofs_is_p (VectorPartitioned.h:147-161)."""
         return self._part >= self.nnu()
 
-    def AsDofs_u(self, arg):
-        return self.AsDofs(arg)[self.iiu_d.long()]
+    # -------------------------------------------------------------- copy_u / copy_p
+    def _copy_part(self, src, dest, lo, hi, name):
+        src = _dev.dev_f64(src)
+        _dev.check_shape(src, self.shape_nodevec(), name)
+        _dev.check_shape(dest, self.shape_nodevec(), name)
+        _lib.call("gfgpu_copy_partitioned_nodevec", self.part_d.data_ptr(), self._nnode,
+                  self._ndim, lo, hi, src.data_ptr(), dest.data_ptr(), _dev.stream())
+        return dest
 
-    def AsDofs_p(self, arg):
-        return self.AsDofs(arg)[self.iip_d.long()]
+    def copy_u(self, nodevec_src, nodevec_dest):
+        """VectorPartitioned::copy_u (VectorPartitioned.h:198-216): unknown dofs of
+        `nodevec_dest` overwritten from `nodevec_src`, in place."""
+        return self._copy_part(nodevec_src, nodevec_dest, 0, self.nnu(), "copy_u")
+
+    def copy_p(self, nodevec_src, nodevec_dest):
+        """VectorPartitioned::copy_p (VectorPartitioned.h:251-269): prescribed dofs."""
+        return self._copy_part(nodevec_src, nodevec_dest, self.nnu(), self._ndof, "copy_p")
 
     def Copy_u(self, nodevec_src, nodevec_dest):
-        """VectorPartitioned::copy_u (VectorPartitioned.h:198): unknown dofs from src."""
-        out = _dev.dev_f64(nodevec_dest).clone()
-        mask = torch.as_tensor(self._part < self.nnu(), device=out.device)
-        src = _dev.dev_f64(nodevec_src)
-        out[mask] = src[mask]
-        return out
+        """VectorPartitioned::Copy_u (VectorPartitioned.h:176-184)."""
+        return self.copy_u(nodevec_src, _dev.dev_f64(nodevec_dest).clone())
 
     def Copy_p(self, nodevec_src, nodevec_dest):
-        """VectorPartitioned::copy_p (VectorPartitioned.h:251): prescribed dofs from src."""
-        out = _dev.dev_f64(nodevec_dest).clone()
-        mask = torch.as_tensor(self._part >= self.nnu(), device=out.device)
-        src = _dev.dev_f64(nodevec_src)
-        out[mask] = src[mask]
-        return out
+        """VectorPartitioned::Copy_p (VectorPartitioned.h:229-237)."""
+        return self.copy_p(nodevec_src, _dev.dev_f64(nodevec_dest).clone())
+
+    # ------------------------------------------------------ from partitioned storage
+    def _uv(self, dofval_u, dofval_p, name):
+        u, p = _dev.dev_f64(dofval_u), _dev.dev_f64(dofval_p)
+        _dev.check_shape(u, (self.nnu(),), name)
+        _dev.check_shape(p, (self.nnp(),), name)
+        return u, p
+
+    def dofsFromParitioned(self, dofval_u, dofval_p, dofval):
+        """VectorPartitioned::dofsFromParitioned (VectorPartitioned.h:293-314); the reference's
+        spelling is kept."""
+        u, p = self._uv(dofval_u, dofval_p, "dofsFromParitioned")
+        _dev.check_shape(dofval, self.shape_dofval(), "dofsFromParitioned")
+        _lib.call("gfgpu_from_partitioned", self.dof2part_d.data_ptr(), self._ndof, self.nnu(),
+                  self.nnp(), u.data_ptr(), p.data_ptr(), dofval.data_ptr(), _dev.stream())
+        return dofval
+
+    def DofsFromParitioned(self, dofval_u, dofval_p):
+        return self.dofsFromParitioned(dofval_u, dofval_p, self.allocate_dofval())
+
+    def nodeFromPartitioned(self, dofval_u, dofval_p, nodevec):
+        """VectorPartitioned::nodeFromPartitioned (VectorPartitioned.h:344-365)."""
+        u, p = self._uv(dofval_u, dofval_p, "nodeFromPartitioned")
+        _dev.check_shape(nodevec, self.shape_nodevec(), "nodeFromPartitioned")
+        _lib.call("gfgpu_from_partitioned", self.part_d.data_ptr(), self._nnode * self._ndim,
+                  self.nnu(), self.nnp(), u.data_ptr(), p.data_ptr(), nodevec.data_ptr(),
+                  _dev.stream())
+        return nodevec
+
+    def NodeFromPartitioned(self, dofval_u, dofval_p):
+        return self.nodeFromPartitioned(dofval_u, dofval_p, self.allocate_nodevec())
+
+    def elementFromPartitioned(self, dofval_u, dofval_p, elemvec):
+        """VectorPartitioned::elementFromPartitioned (VectorPartitioned.h:395-418)."""
+        u, p = self._uv(dofval_u, dofval_p, "elementFromPartitioned")
+        _dev.check_shape(elemvec, self.shape_elemvec(), "elementFromPartitioned")
+        _lib.call("gfgpu_from_partitioned_elemvec", self.conn_d.data_ptr(), self.part_d.data_ptr(),
+                  self._nelem, self._nne, self._ndim, self.nnu(), self.nnp(), u.data_ptr(),
+                  p.data_ptr(), elemvec.data_ptr(), _dev.stream())
+        return elemvec
+
+    def ElementFromPartitioned(self, dofval_u, dofval_p):
+        return self.elementFromPartitioned(dofval_u, dofval_p, self.allocate_elemvec())
+
+    # ----------------------------------------------------------- asDofs_u / asDofs_p
+    def _as_dofs_sub(self, arg, ret, sel, n, name):
+        arg = _dev.dev_f64(arg)
+        _dev.check_shape(ret, (n,), name)
+        if self._kind(arg) != "dofval":
+            arg = self.AsDofs(arg)  # last writer wins, as the reference's serial loops
+        _lib.call("gfgpu_from_partitioned", sel.data_ptr(), n, self._ndof, 0, arg.data_ptr(), None,
+                  ret.data_ptr(), _dev.stream())
+        return ret
+
+    def asDofs_u(self, arg, dofval_u):
+        """VectorPartitioned::asDofs_u of a dofval, nodevec or elemvec
+        (VectorPartitioned.h:428-539)."""
+        return self._as_dofs_sub(arg, dofval_u, self.iiu_d, self.nnu(), "asDofs_u")
+
+    def asDofs_p(self, arg, dofval_p):
+        """VectorPartitioned::asDofs_p (VectorPartitioned.h:549-660)."""
+        return self._as_dofs_sub(arg, dofval_p, self.iip_d, self.nnp(), "asDofs_p")
+
+    def AsDofs_u(self, arg):
+        return self.asDofs_u(arg, _dev.empty((self.nnu(),)))
+
+    def AsDofs_p(self, arg):
+        return self.asDofs_p(arg, _dev.empty((self.nnp(),)))

@@ -242,6 +242,25 @@ int gfgpu_diagp_reaction_nodevec(const int32_t* part, int64_t nnode, int32_t ndi
 int gfgpu_dofval_mul(const double* a, const double* b, int64_t n, double* out,
                      gfgpu_stream_t stream);
 
+/* VectorPartitioned::dofsFromParitioned / nodeFromPartitioned (VectorPartitioned.h:276-365):
+ * out[t] = idx[t] < nnu ? u[idx[t]] : p[idx[t] - nnu], n entries. For a dofval pass as `idx` the
+ * position of every dof in [iiu, iip] (ndof entries); for a nodevec pass `part` [nnode, ndim].
+ * The same gather with `idx` = iiu (or iip) and nnp = 0 is asDofs_u (asDofs_p) of a dofval
+ * (VectorPartitioned.h:428-458, 549-579). */
+int gfgpu_from_partitioned(const int32_t* idx, int64_t n, int64_t nnu, int64_t nnp,
+                           const double* u, const double* p, double* out, gfgpu_stream_t stream);
+/* VectorPartitioned::elementFromPartitioned (VectorPartitioned.h:376-418):
+ * elemvec(e,m,i) = [u | p][part(conn(e,m), i)]. */
+int gfgpu_from_partitioned_elemvec(const int32_t* conn, const int32_t* part, int64_t nelem,
+                                   int32_t nne, int32_t ndim, int64_t nnu, int64_t nnp,
+                                   const double* u, const double* p, double* elemvec,
+                                   gfgpu_stream_t stream);
+/* VectorPartitioned::copy_u / copy_p (VectorPartitioned.h:176-270): dest(m,i) = src(m,i) where
+ * lo <= part(m,i) < hi (copy_u: [0, nnu); copy_p: [nnu, ndof)); other entries untouched. */
+int gfgpu_copy_partitioned_nodevec(const int32_t* part, int64_t nnode, int32_t ndim, int64_t lo,
+                                   int64_t hi, const double* src, double* dest,
+                                   gfgpu_stream_t stream);
+
 /* ============================ explicit velocity-Verlet (device) =========================== */
 
 /* One or more increments of the explicit scheme of

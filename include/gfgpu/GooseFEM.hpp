@@ -200,6 +200,25 @@ public:
     {
         return range(m_nx, (m_ny + 1) * (m_nx + 1), m_nx + 1);
     }
+    /* edges without their corners (MeshQuad4.h:148-166) */
+    host::array<int32_t> nodesBottomOpenEdge() const { return range(1, m_nx, 1); }
+    host::array<int32_t> nodesTopOpenEdge() const
+    {
+        return range(m_ny * (m_nx + 1) + 1, m_ny * (m_nx + 1) + m_nx, 1);
+    }
+    host::array<int32_t> nodesLeftOpenEdge() const
+    {
+        return range(m_nx + 1, m_ny * (m_nx + 1), m_nx + 1);
+    }
+    host::array<int32_t> nodesRightOpenEdge() const
+    {
+        return range(2 * m_nx + 1, m_ny * (m_nx + 1), m_nx + 1);
+    }
+    int64_t nodesBottomLeftCorner() const { return 0; }
+    int64_t nodesBottomRightCorner() const { return m_nx; }
+    int64_t nodesTopLeftCorner() const { return m_ny * (m_nx + 1); }
+    int64_t nodesTopRightCorner() const { return m_ny * (m_nx + 1) + m_nx; }
+    int64_t nodesOrigin() const { return 0; }
     host::array<int32_t> nodesPeriodic() const
     {
         host::array<int32_t> out({(m_nx - 1) + (m_ny - 1) + 3, 2});
@@ -435,6 +454,163 @@ protected:
     int32_t m_nne, m_ndim;
     array<int32_t> m_conn, m_dofs;
     detail::Csr m_csr, m_csrn;
+};
+
+/* VectorPartitioned(conn, dofs, iip) (VectorPartitioned.h:45-661): the dofs split into unknown
+ * (iiu) and prescribed (iip) parts; part(m, i) is the position of dofs(m, i) in [iiu, iip]. */
+class VectorPartitioned : public Vector {
+public:
+    VectorPartitioned(const host::array<int32_t>& conn, const host::array<int32_t>& dofs,
+                      const host::array<int32_t>& iip)
+        : Vector(conn, dofs), m_iip_h(iip), m_iiu_h({dofs.size()}), m_part_h(dofs.shape())
+    {
+        int64_t nnu = 0;
+        check(gfgpu_host_partition(dofs.data(), dofs.size(), iip.data(), iip.size(), m_iiu_h.data(),
+                                   m_part_h.data(), &nnu),
+              "VectorPartitioned");
+        m_nnu = nnu;
+        m_nnp = iip.size();
+        host::array<int32_t> iiu({m_nnu}), dof2part({m_ndof});
+        for (int64_t i = 0; i < m_nnu; ++i) {
+            iiu[i] = m_iiu_h[i];
+            dof2part[m_iiu_h[i]] = int32_t(i);
+        }
+        for (int64_t i = 0; i < m_nnp; ++i) dof2part[iip[i]] = int32_t(m_nnu + i);
+        m_iiu_h = std::move(iiu);
+        m_iiu = array<int32_t>::from_host(m_iiu_h);
+        m_iip = array<int32_t>::from_host(m_iip_h);
+        m_part = array<int32_t>::from_host(m_part_h);
+        m_dof2part = array<int32_t>::from_host(dof2part);
+    }
+    int64_t nnu() const { return m_nnu; }
+    int64_t nnp() const { return m_nnp; }
+    const host::array<int32_t>& iiu() const { return m_iiu_h; }
+    const host::array<int32_t>& iip() const { return m_iip_h; }
+    const host::array<int32_t>& part() const { return m_part_h; }
+    /* dofs_is_u / dofs_is_p (VectorPartitioned.h:126-161), 1 = true */
+    host::array<uint8_t> dofs_is_u() const { return is_part(true); }
+    host::array<uint8_t> dofs_is_p() const { return is_part(false); }
+
+    /* copy_u / copy_p (VectorPartitioned.h:176-270): overwrite the unknown (prescribed) dofs of
+     * dest from src, in place */
+    void copy_u(const array<double>& src, array<double>& dest) const { copy_part(src, dest, 0, m_nnu); }
+    void copy_p(const array<double>& src, array<double>& dest) const
+    {
+        copy_part(src, dest, m_nnu, m_ndof);
+    }
+    array<double> Copy_u(const array<double>& src, const array<double>& dest) const
+    {
+        auto r = dest.copy();
+        copy_u(src, r);
+        return r;
+    }
+    array<double> Copy_p(const array<double>& src, const array<double>& dest) const
+    {
+        auto r = dest.copy();
+        copy_p(src, r);
+        return r;
+    }
+
+    /* dofsFromParitioned / nodeFromPartitioned / elementFromPartitioned
+     * (VectorPartitioned.h:276-418; the reference's spelling is kept) */
+    void dofsFromParitioned(const array<double>& u, const array<double>& p, array<double>& dofval) const
+    {
+        require_up(u, p, "VectorPartitioned::dofsFromParitioned");
+        require_shape(dofval.shape(), shape_dofval(), "VectorPartitioned::dofsFromParitioned");
+        check(gfgpu_from_partitioned(m_dof2part.data(), m_ndof, m_nnu, m_nnp, u.data(), p.data(),
+                                     dofval.data(), nullptr),
+              "VectorPartitioned::dofsFromParitioned");
+    }
+    array<double> DofsFromParitioned(const array<double>& u, const array<double>& p) const
+    {
+        auto r = allocate_dofval();
+        dofsFromParitioned(u, p, r);
+        return r;
+    }
+    void nodeFromPartitioned(const array<double>& u, const array<double>& p, array<double>& nodevec) const
+    {
+        require_up(u, p, "VectorPartitioned::nodeFromPartitioned");
+        require_shape(nodevec.shape(), shape_nodevec(), "VectorPartitioned::nodeFromPartitioned");
+        check(gfgpu_from_partitioned(m_part.data(), m_nnode * m_ndim, m_nnu, m_nnp, u.data(), p.data(),
+                                     nodevec.data(), nullptr),
+              "VectorPartitioned::nodeFromPartitioned");
+    }
+    array<double> NodeFromPartitioned(const array<double>& u, const array<double>& p) const
+    {
+        auto r = allocate_nodevec();
+        nodeFromPartitioned(u, p, r);
+        return r;
+    }
+    void elementFromPartitioned(const array<double>& u, const array<double>& p,
+                                array<double>& elemvec) const
+    {
+        require_up(u, p, "VectorPartitioned::elementFromPartitioned");
+        require_shape(elemvec.shape(), shape_elemvec(), "VectorPartitioned::elementFromPartitioned");
+        check(gfgpu_from_partitioned_elemvec(m_conn.data(), m_part.data(), m_nelem, m_nne, m_ndim, m_nnu,
+                                             m_nnp, u.data(), p.data(), elemvec.data(), nullptr),
+              "VectorPartitioned::elementFromPartitioned");
+    }
+    array<double> ElementFromPartitioned(const array<double>& u, const array<double>& p) const
+    {
+        auto r = allocate_elemvec();
+        elementFromPartitioned(u, p, r);
+        return r;
+    }
+
+    /* asDofs_u / asDofs_p of a dofval, nodevec or elemvec (VectorPartitioned.h:428-660); for a
+     * nodevec or elemvec the last writer wins, as in the reference's serial loops */
+    void asDofs_u(const array<double>& arg, array<double>& ret) const { as_sub(arg, ret, m_iiu, m_nnu); }
+    void asDofs_p(const array<double>& arg, array<double>& ret) const { as_sub(arg, ret, m_iip, m_nnp); }
+    array<double> AsDofs_u(const array<double>& arg) const
+    {
+        array<double> r({m_nnu});
+        asDofs_u(arg, r);
+        return r;
+    }
+    array<double> AsDofs_p(const array<double>& arg) const
+    {
+        array<double> r({m_nnp});
+        asDofs_p(arg, r);
+        return r;
+    }
+    const array<int32_t>& part_device() const { return m_part; }
+
+private:
+    host::array<uint8_t> is_part(bool u) const
+    {
+        host::array<uint8_t> r(m_part_h.shape());
+        for (int64_t i = 0; i < r.size(); ++i) r[i] = uint8_t((m_part_h[i] < m_nnu) == u);
+        return r;
+    }
+    void copy_part(const array<double>& src, array<double>& dest, int64_t lo, int64_t hi) const
+    {
+        require_shape(src.shape(), shape_nodevec(), "VectorPartitioned::copy");
+        require_shape(dest.shape(), shape_nodevec(), "VectorPartitioned::copy");
+        check(gfgpu_copy_partitioned_nodevec(m_part.data(), m_nnode, m_ndim, lo, hi, src.data(),
+                                             dest.data(), nullptr),
+              "VectorPartitioned::copy");
+    }
+    void require_up(const array<double>& u, const array<double>& p, const char* what) const
+    {
+        require_shape(u.shape(), {m_nnu}, what);
+        require_shape(p.shape(), {m_nnp}, what);
+    }
+    void as_sub(const array<double>& arg, array<double>& ret, const array<int32_t>& sel, int64_t n) const
+    {
+        require_shape(ret.shape(), {n}, "VectorPartitioned::asDofs_u/p");
+        if (arg.shape() == shape_dofval()) {
+            check(gfgpu_from_partitioned(sel.data(), n, m_ndof, 0, arg.data(), nullptr, ret.data(),
+                                         nullptr),
+                  "VectorPartitioned::asDofs_u/p");
+            return;
+        }
+        array<double> d = AsDofs(arg);
+        check(gfgpu_from_partitioned(sel.data(), n, m_ndof, 0, d.data(), nullptr, ret.data(), nullptr),
+              "VectorPartitioned::asDofs_u/p");
+    }
+    int64_t m_nnu = 0, m_nnp = 0;
+    host::array<int32_t> m_iip_h, m_iiu_h, m_part_h;
+    array<int32_t> m_iiu, m_iip, m_part, m_dof2part;
 };
 
 // ------------------------------------------------------------------------------------- Element
@@ -757,6 +933,91 @@ private:
         m_changed = false;
     }
     Vector m_vec;
+    array<double> m_A, m_inv;
+    bool m_changed = true;
+};
+
+/* MatrixDiagonalPartitioned(conn, dofs, iip) (MatrixDiagonalPartitioned.h:42-392): the diagonal
+ * stored as [A_uu, A_pp] back to back in the partitioned numbering. */
+class MatrixDiagonalPartitioned {
+public:
+    MatrixDiagonalPartitioned(const host::array<int32_t>& conn, const host::array<int32_t>& dofs,
+                              const host::array<int32_t>& iip)
+        : m_vec(conn, dofs, iip),
+          m_csr(detail::elemvec_csr(conn, m_vec.part(), m_vec.ndof())),
+          m_A({m_vec.ndof()}),
+          m_inv({std::max<int64_t>(m_vec.nnu(), 1)})
+    {
+    }
+    int64_t ndof() const { return m_vec.ndof(); }
+    int64_t nnu() const { return m_vec.nnu(); }
+    int64_t nnp() const { return m_vec.nnp(); }
+    const VectorPartitioned& vector() const { return m_vec; }
+    /* MatrixDiagonalPartitioned::assemble (MatrixDiagonalPartitioned.h:73-98) */
+    void assemble(const array<double>& elemmat)
+    {
+        if (!Element::isDiagonal(elemmat))
+            throw std::runtime_error("MatrixDiagonalPartitioned: not diagonal");
+        check(gfgpu_diag_assemble(m_csr.ptr.data(), m_csr.idx.data(), ndof(), m_vec.nne(), m_vec.ndim(),
+                                  elemmat.data(), m_A.data(), nullptr),
+              "MatrixDiagonalPartitioned::assemble");
+        m_changed = true;
+    }
+    /* [A_uu, A_pp] back to back */
+    const array<double>& data_partitioned() const { return m_A; }
+    /* solve nodevec (MatrixDiagonalPartitioned.h:306-322): writes the unknown dofs of x only */
+    void solve(const array<double>& b, array<double>& x)
+    {
+        require_shape(b.shape(), m_vec.shape_nodevec(), "MatrixDiagonalPartitioned::solve");
+        require_shape(x.shape(), m_vec.shape_nodevec(), "MatrixDiagonalPartitioned::solve");
+        if (m_changed) {
+            check(gfgpu_diag_factorize(m_A.data(), nnu(), m_inv.data(), nullptr), "factorize");
+            m_changed = false;
+        }
+        check(gfgpu_diag_solve_nodevec(m_vec.part_device().data(), m_vec.nnode(), m_vec.ndim(), nnu(),
+                                       m_inv.data(), b.data(), x.data(), nullptr),
+              "MatrixDiagonalPartitioned::solve");
+    }
+    array<double> Solve(const array<double>& b, const array<double>& x)
+    {
+        auto r = x.copy();
+        solve(b, r);
+        return r;
+    }
+    /* dot nodevec (MatrixDiagonalPartitioned.h:189-205) */
+    void dot(const array<double>& x, array<double>& b) const
+    {
+        require_shape(x.shape(), m_vec.shape_nodevec(), "MatrixDiagonalPartitioned::dot");
+        require_shape(b.shape(), m_vec.shape_nodevec(), "MatrixDiagonalPartitioned::dot");
+        check(gfgpu_diag_dot_nodevec(m_vec.part_device().data(), m_vec.nnode(), m_vec.ndim(), m_A.data(),
+                                     x.data(), b.data(), nullptr),
+              "MatrixDiagonalPartitioned::dot");
+    }
+    array<double> Dot(const array<double>& x) const
+    {
+        array<double> b(x.shape());
+        dot(x, b);
+        return b;
+    }
+    /* reaction nodevec (MatrixDiagonalPartitioned.h:378-392): b_p = A_pp x_p, b_u untouched */
+    void reaction(const array<double>& x, array<double>& b) const
+    {
+        require_shape(x.shape(), m_vec.shape_nodevec(), "MatrixDiagonalPartitioned::reaction");
+        require_shape(b.shape(), m_vec.shape_nodevec(), "MatrixDiagonalPartitioned::reaction");
+        check(gfgpu_diagp_reaction_nodevec(m_vec.part_device().data(), m_vec.nnode(), m_vec.ndim(), nnu(),
+                                           m_A.data() + nnu(), x.data(), b.data(), nullptr),
+              "MatrixDiagonalPartitioned::reaction");
+    }
+    array<double> Reaction(const array<double>& x, const array<double>& b) const
+    {
+        auto r = b.copy();
+        reaction(x, r);
+        return r;
+    }
+
+private:
+    VectorPartitioned m_vec;
+    detail::Csr m_csr;
     array<double> m_A, m_inv;
     bool m_changed = true;
 };

@@ -117,6 +117,42 @@ int main(int argc, char** argv)
         solver.solve(Kmat, zero, xs);
         if (solver.relres() > 1e-12) return 5;
 
+        // VectorPartitioned (tests/basic/VectorPartitioned.cpp "asDofs" and "copy_u, copy_p"):
+        // right open edge tied to the left one, top and bottom edges prescribed
+        auto dofs_lr = mesh.dofs();
+        auto left = mesh.nodesLeftOpenEdge(), right = mesh.nodesRightOpenEdge();
+        for (int64_t i = 0; i < left.size(); ++i)
+            for (int d = 0; d < 2; ++d) dofs_lr(right[i], d) = dofs_lr(left[i], d);
+        dofs_lr = GF::Mesh::renumber(dofs_lr);
+        GF::host::array<int32_t> iip_lr({(bot.size() + top.size()) * 2});
+        int64_t c = 0;
+        for (int d = 0; d < 2; ++d)
+            for (int64_t i = 0; i < top.size(); ++i) iip_lr[c++] = dofs_lr(top[i], d);
+        for (int d = 0; d < 2; ++d)
+            for (int64_t i = 0; i < bot.size(); ++i) iip_lr[c++] = dofs_lr(bot[i], d);
+        auto uh2 = uh;
+        for (int64_t i = 0; i < left.size(); ++i)
+            for (int d = 0; d < 2; ++d) uh2[right[i] * 2 + d] = uh2[left[i] * 2 + d];
+        auto u2 = GF::array<double>::from_host(uh2.data(), {nnode, 2});
+        GF::VectorPartitioned vp(mesh.conn(), dofs_lr, iip_lr);
+        auto isp = vp.dofs_is_p();
+        int64_t np = 0;
+        for (int64_t i = 0; i < isp.size(); ++i) np += isp[i];
+        if (np != int64_t(top.size() + bot.size()) * 2) return 6;
+        auto u_u = vp.AsDofs_u(u2), u_p = vp.AsDofs_p(u2);
+        auto u2_back = vp.NodeFromPartitioned(u_u, u_p);
+        auto v = GF::array<double>({nnode, 2});
+        v.fill_zero();
+        vp.copy_u(u2, v);
+        vp.copy_p(u2, v);
+
+        // MatrixDiagonalPartitioned with the lumped mass and the static solve's iip
+        GF::MatrixDiagonalPartitioned Mp(mesh.conn(), mesh.dofs(), iip);
+        Mp.assemble(nodal.Int_N_scalar_NT_dV(GF::array<double>::from_host(rho)));
+        auto Mp_dot = Mp.Dot(u);
+        auto Mp_solve = Mp.Solve(u, zero);
+        auto Mp_reaction = Mp.Reaction(u, zero);
+
         std::ofstream out(argv[2], std::ios::binary);
         dump(out, quad.GradN());
         dump(out, quad.dV());
@@ -131,6 +167,11 @@ int main(int argc, char** argv)
         dump(out, Sig3);
         dump(out, fe3);
         dump(out, xs);
+        dump(out, u2_back);
+        dump(out, v);
+        dump(out, Mp_dot);
+        dump(out, Mp_solve);
+        dump(out, Mp_reaction);
 
         // error path: a shape mismatch is reported as std::runtime_error
         bool threw = false;

@@ -74,5 +74,22 @@ def test_cpp_api_force_chain_and_mass(oracle, tmp_path):
     xs = data[k:k + nnode * 2]
     k += nnode * 2
     assert np.linalg.norm(xs - x_ref) / np.linalg.norm(x_ref) <= 1e-9
+    # VectorPartitioned round trip and copies: both equal u with the right open edge = the left
+    left = np.arange(1, nx) * (nx + 1)
+    u2 = u.copy()
+    u2[left + nx] = u2[left]
+    for _ in range(2):
+        assert np.array_equal(data[k:k + nnode * 2].reshape(nnode, 2), u2)
+        k += nnode * 2
+    # MatrixDiagonalPartitioned: dot, solve (unknown dofs only), reaction (prescribed dofs only)
+    Mn = M[dofs]
+    isp = np.isin(dofs, iip)
+    got = [data[k + j * nnode * 2:k + (j + 1) * nnode * 2].reshape(nnode, 2) for j in range(3)]
+    k += 3 * nnode * 2
+    assert rel_err(got[0], Mn * u) <= RTOL
+    assert rel_err(got[1], np.where(isp, 0.0, u / Mn)) <= RTOL
+    assert np.all(got[1][isp] == 0.0)
+    assert rel_err(got[2], np.where(isp, Mn * u, 0.0)) <= RTOL
+    assert np.all(got[2][~isp] == 0.0)
     assert k == data.size
     assert np.array_equal(data[:dNx.size].reshape(dNx.shape), dNx)  # set-up is bit-exact
