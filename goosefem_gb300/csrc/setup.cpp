@@ -181,6 +181,39 @@ int gfgpu_host_quad4_nodes_periodic(int64_t nx, int64_t ny, int32_t* out, int64_
     return GFGPU_OK;
 }
 
+int gfgpu_host_hex8_nodes_periodic(int64_t nx, int64_t ny, int64_t nz, int32_t* out, int64_t* nper)
+{
+    HREQ(nx >= 1 && ny >= 1 && nz >= 1 && out && nper, "bad argument");
+    HREQ(fits32((nx + 1) * (ny + 1) * (nz + 1)), "too many nodes");
+    const int64_t sy = nx + 1, sz = (nx + 1) * (ny + 1);
+    int64_t n = 0;
+    auto put = [&](int64_t a, int64_t b) {
+        out[n * 2 + 0] = static_cast<int32_t>(a);
+        out[n * 2 + 1] = static_cast<int32_t>(b);
+        ++n;
+    };
+    // offsets of the far side along x, y, z
+    const int64_t X = nx, Y = ny * sy, Z = nz * sz;
+    // corners: every other corner tied to the origin (front-bottom-left)
+    for (int64_t c : {X, X + Z, Z, Y, X + Y, X + Y + Z, Y + Z}) put(0, c);
+    // open edges along x, then along z, then along y, each tied to the three parallel edges
+    for (int64_t dst : {Z, Y + Z, Y})
+        for (int64_t i = 1; i < nx; ++i) put(i, i + dst);
+    for (int64_t dst : {X, X + Y, Y})
+        for (int64_t i = 1; i < nz; ++i) put(i * sz, i * sz + dst);
+    for (int64_t dst : {X, X + Z, Z})
+        for (int64_t i = 1; i < ny; ++i) put(i * sy, i * sy + dst);
+    // open faces: front -> back (iy outer), left -> right (iz outer), bottom -> top (iz outer)
+    for (int64_t iy = 1; iy < ny; ++iy)
+        for (int64_t ix = 1; ix < nx; ++ix) put(ix + iy * sy, ix + iy * sy + Z);
+    for (int64_t iz = 1; iz < nz; ++iz)
+        for (int64_t iy = 1; iy < ny; ++iy) put(iy * sy + iz * sz, iy * sy + iz * sz + X);
+    for (int64_t iz = 1; iz < nz; ++iz)
+        for (int64_t ix = 1; ix < nx; ++ix) put(ix + iz * sz, ix + iz * sz + Y);
+    *nper = n;
+    return GFGPU_OK;
+}
+
 int gfgpu_host_renumber(const int32_t* in, int64_t n, int32_t* out)
 {
     HREQ(n >= 0 && (n == 0 || (in && out)), "bad argument");

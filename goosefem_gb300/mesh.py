@@ -239,8 +239,21 @@ class Hex8:
         def nodesOrigin(self):
             return 0
 
-        def dofsPeriodic(self, nodes_periodic):
-            """RegularBase::dofsPeriodic (Mesh.h:291-306) for a given nodesPeriodic table."""
+        def nodesPeriodic(self):
+            """RegularBase3d::nodesPeriodic (Mesh.h:1577-1692)."""
+            nx, ny, nz = self._nx, self._ny, self._nz
+            n = 7 + 3 * (nx - 1 + ny - 1 + nz - 1) + (nx - 1) * (ny - 1) + (ny - 1) * (nz - 1) \
+                + (nx - 1) * (nz - 1)
+            out = np.empty((n, 2), dtype=np.int32)
+            k = np.zeros(1, dtype=np.int64)
+            _lib.call("gfgpu_host_hex8_nodes_periodic", nx, ny, nz, out.ctypes.data, k.ctypes.data)
+            return out[: int(k[0])].copy()
+
+        def dofsPeriodic(self, nodes_periodic=None):
+            """RegularBase::dofsPeriodic (Mesh.h:291-306); `nodes_periodic` defaults to
+            nodesPeriodic()."""
+            if nodes_periodic is None:
+                nodes_periodic = self.nodesPeriodic()
             npr = np.ascontiguousarray(nodes_periodic, dtype=np.int32)
             out = np.empty((self._nnode, 3), dtype=np.int32)
             _lib.call("gfgpu_host_dofs_periodic", self._nnode, 3, npr.ctypes.data, npr.shape[0],

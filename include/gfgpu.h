@@ -78,6 +78,11 @@ int gfgpu_host_hex8_regular(int64_t nx, int64_t ny, int64_t nz, double h, double
 int gfgpu_host_dofs(int64_t nnode, int32_t ndim, int32_t* dofs);
 /* RegularBase2d::nodesPeriodic (Mesh.h:511-540) of Quad4 Regular; out [(nx-1)+(ny-1)+3, 2]. */
 int gfgpu_host_quad4_nodes_periodic(int64_t nx, int64_t ny, int32_t* out, int64_t* nper);
+/* RegularBase3d::nodesPeriodic for Mesh::Hex8::Regular (Mesh.h:1577-1692 with the face / edge /
+ * corner sets of MeshHex8.h:214-600): 7 corner pairs, the open edges, then the open faces.
+ * `out` holds 7 + 3((nx-1) + (ny-1) + (nz-1)) + (nx-1)(ny-1) + (ny-1)(nz-1) + (nx-1)(nz-1)
+ * rows of (independent, dependent). */
+int gfgpu_host_hex8_nodes_periodic(int64_t nx, int64_t ny, int64_t nz, int32_t* out, int64_t* nper);
 /* RegularBase::dofsPeriodic (Mesh.h:291-306) given a nodesPeriodic table. */
 int gfgpu_host_dofs_periodic(int64_t nnode, int32_t ndim, const int32_t* nodes_periodic,
                              int64_t nper, int32_t* dofs);

@@ -277,6 +277,25 @@ public:
         for (int64_t i = 0; i < r.size(); ++i) r[i] = static_cast<int32_t>(i + m_nz * r.size());
         return r;
     }
+    /* RegularBase3d::nodesPeriodic / dofsPeriodic (Mesh.h:1577-1692, 291-306) */
+    host::array<int32_t> nodesPeriodic() const
+    {
+        int64_t n = 7 + 3 * (m_nx - 1 + m_ny - 1 + m_nz - 1) + (m_nx - 1) * (m_ny - 1) +
+                    (m_ny - 1) * (m_nz - 1) + (m_nx - 1) * (m_nz - 1);
+        host::array<int32_t> out({n, 2});
+        int64_t k = 0;
+        check(gfgpu_host_hex8_nodes_periodic(m_nx, m_ny, m_nz, out.data(), &k), "nodesPeriodic");
+        return out;
+    }
+    host::array<int32_t> dofsPeriodic() const
+    {
+        auto npr = nodesPeriodic();
+        host::array<int32_t> out({nnode(), 3});
+        check(gfgpu_host_dofs_periodic(nnode(), 3, npr.data(), npr.shape(0), out.data()),
+              "dofsPeriodic");
+        return out;
+    }
+    int64_t nodesOrigin() const { return 0; }
 
 private:
     std::pair<host::array<double>, host::array<int32_t>> build() const

@@ -138,6 +138,80 @@ idx ref_quad4_nodes_periodic(idx nx, idx ny, idx* out)
     return n;
 }
 
+// Mesh.h:1577-1692 (RegularBase3d::nodesPeriodic_impl) with the Hex8 face, open-edge and corner
+// sets of MeshHex8.h:214-600, written as the reference lists them: 7 corners tied to the origin,
+// then the open edges of each axis direction, then the open faces.
+idx ref_hex8_nodes_periodic(idx nx, idx ny, idx nz, idx* out)
+{
+    idx nxy = (nx + 1) * (ny + 1);
+    auto node = [&](idx ix, idx iy, idx iz) { return ix + iy * (nx + 1) + iz * nxy; };
+    std::vector<idx> froBot, bckBot, bckTop, froTop, botLft, botRgt, topRgt, topLft, froLft, froRgt,
+        bckRgt, bckLft, fro, bck, lft, rgt, bot, top;
+    for (idx ix = 1; ix < nx; ++ix) {
+        froBot.push_back(node(ix, 0, 0));
+        froTop.push_back(node(ix, ny, 0));
+        bckBot.push_back(node(ix, 0, nz));
+        bckTop.push_back(node(ix, ny, nz));
+    }
+    for (idx iz = 1; iz < nz; ++iz) {
+        botLft.push_back(node(0, 0, iz));
+        botRgt.push_back(node(nx, 0, iz));
+        topLft.push_back(node(0, ny, iz));
+        topRgt.push_back(node(nx, ny, iz));
+    }
+    for (idx iy = 1; iy < ny; ++iy) {
+        froLft.push_back(node(0, iy, 0));
+        froRgt.push_back(node(nx, iy, 0));
+        bckLft.push_back(node(0, iy, nz));
+        bckRgt.push_back(node(nx, iy, nz));
+    }
+    for (idx iy = 1; iy < ny; ++iy)
+        for (idx ix = 1; ix < nx; ++ix) {
+            fro.push_back(node(ix, iy, 0));
+            bck.push_back(node(ix, iy, nz));
+        }
+    for (idx iz = 1; iz < nz; ++iz)
+        for (idx iy = 1; iy < ny; ++iy) {
+            lft.push_back(node(0, iy, iz));
+            rgt.push_back(node(nx, iy, iz));
+        }
+    for (idx iz = 1; iz < nz; ++iz)
+        for (idx ix = 1; ix < nx; ++ix) {
+            bot.push_back(node(ix, 0, iz));
+            top.push_back(node(ix, ny, iz));
+        }
+    idx n = 0;
+    auto put = [&](idx a, idx b) {
+        out[n * 2 + 0] = a;
+        out[n * 2 + 1] = b;
+        ++n;
+    };
+    idx o = node(0, 0, 0);
+    put(o, node(nx, 0, 0));
+    put(o, node(nx, 0, nz));
+    put(o, node(0, 0, nz));
+    put(o, node(0, ny, 0));
+    put(o, node(nx, ny, 0));
+    put(o, node(nx, ny, nz));
+    put(o, node(0, ny, nz));
+    auto pairs = [&](const std::vector<idx>& a, const std::vector<idx>& b) {
+        for (size_t j = 0; j < a.size(); ++j) put(a[j], b[j]);
+    };
+    pairs(froBot, bckBot);
+    pairs(froBot, bckTop);
+    pairs(froBot, froTop);
+    pairs(botLft, botRgt);
+    pairs(botLft, topRgt);
+    pairs(botLft, topLft);
+    pairs(froLft, froRgt);
+    pairs(froLft, bckRgt);
+    pairs(froLft, bckLft);
+    pairs(fro, bck);
+    pairs(lft, rgt);
+    pairs(bot, top);
+    return n;
+}
+
 // Mesh.h:114-166 (Renumber): ret = index-in-sorted-unique-list of each entry.
 void ref_renumber(const idx* in, idx n, idx* out)
 {

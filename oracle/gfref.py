@@ -83,6 +83,15 @@ def quad4_nodes_periodic(nx, ny):
     return out[:n]
 
 
+def hex8_nodes_periodic(nx, ny, nz):
+    n = 7 + 3 * (nx - 1 + ny - 1 + nz - 1) + (nx - 1) * (ny - 1) + (ny - 1) * (nz - 1) \
+        + (nx - 1) * (nz - 1)
+    out = np.empty((n, 2), dtype=np.int64)
+    k = _call("ref_hex8_nodes_periodic", nx, ny, nz, out, restype=C.c_int64)
+    assert k == n
+    return out
+
+
 def dofs_periodic(nnode, ndim, nodes_periodic):
     out = np.empty((nnode, ndim), dtype=np.int64)
     npr = _ix(nodes_periodic)

@@ -66,7 +66,9 @@ def test_mesh_against_reference_kat(lib):
     assert np.array_equal(h.nodesFront(), np.array(KAT["hex8_3x3x3_nodesFront"]["value"]))
     assert np.array_equal(h.nodesBack(), np.array(KAT["hex8_3x3x3_nodesBack"]["value"]))
     npr = np.array(KAT["hex8_3x3x3_nodesPeriodic"]["value"])
+    assert np.array_equal(h.nodesPeriodic(), npr)
     assert np.array_equal(h.dofsPeriodic(npr), np.array(KAT["hex8_3x3x3_dofsPeriodic"]["value"]))
+    assert np.array_equal(h.dofsPeriodic(), np.array(KAT["hex8_3x3x3_dofsPeriodic"]["value"]))
     q = gf.Mesh.Quad4.Regular(3, 3)
     assert np.array_equal(gf.Mesh.coordination(q.conn()),
                           np.array(KAT["quad4_3x3_coordination"]["value"]))
@@ -86,6 +88,9 @@ def test_mesh_setup_matches_oracle(lib, oracle, nx, ny):
     h = gf.Mesh.Hex8.Regular(nx, ny, 3, 0.37)
     hc, hn = oracle.hex8_regular(nx, ny, 3, 0.37)
     assert np.array_equal(h.coor(), hc) and np.array_equal(h.conn(), hn)
+    assert np.array_equal(h.nodesPeriodic(), oracle.hex8_nodes_periodic(nx, ny, 3))
+    assert np.array_equal(h.dofsPeriodic(),
+                          oracle.dofs_periodic(h.nnode(), 3, oracle.hex8_nodes_periodic(nx, ny, 3)))
 
 
 def test_partition_and_renumber_match_oracle(lib, oracle):

@@ -41,6 +41,8 @@ def test_hex8_regular_golden(oracle):
     # dofsPeriodic from the reference's own nodesPeriodic list (Mesh.h:291-306)
     npr = kat("hex8_3x3x3_nodesPeriodic", np.int64)
     assert np.array_equal(oracle.dofs_periodic(64, 3, npr), kat("hex8_3x3x3_dofsPeriodic", np.int64))
+    # the restated 3-d nodesPeriodic list itself (Mesh.h:1577-1692)
+    assert np.array_equal(oracle.hex8_nodes_periodic(3, 3, 3), npr)
     front = np.arange(16)
     assert np.array_equal(front, kat("hex8_3x3x3_nodesFront"))
     assert np.array_equal(front + 3 * 16, kat("hex8_3x3x3_nodesBack"))
