@@ -155,6 +155,13 @@ __global__ void k_mul(const double* __restrict__ a, const double* __restrict__ b
     GF_FOR(t, n) o[t] = __dmul_rn(a[t], b[t]);
 }
 
+// out[i * k + j] = src[i]: a scalar per entry repeated over k trailing tensor components
+__global__ void k_broadcast(const double* __restrict__ src, int64_t n, int64_t k,
+                            double* __restrict__ out)
+{
+    GF_FOR(t, n * k) out[t] = __ldg(src + t / k);
+}
+
 // out[t] = [u | p][idx[t]]: the partitioned vector read back through a partitioned index table
 __global__ void k_from_partitioned(const int32_t* __restrict__ idx, int64_t n, int64_t nnu,
                                    const double* __restrict__ u, const double* __restrict__ p,
@@ -340,6 +347,15 @@ int gfgpu_dofval_mul(const double* a, const double* b, int64_t n, double* out,
     if (n == 0) return GFGPU_OK;
     k_mul<<<grid_for(n), kBlock, 0, S(stream)>>>(a, b, n, out);
     return check_launch("dofval_mul");
+}
+
+int gfgpu_broadcast(const double* src, int64_t n, int64_t k, double* out, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(src && out && n >= 0 && k >= 1, "bad argument");
+    GF_REQUIRE(!too_big(n * k), "too many values");
+    if (n == 0) return GFGPU_OK;
+    k_broadcast<<<grid_for(n * k), kBlock, 0, S(stream)>>>(src, n, k, out);
+    return check_launch("broadcast");
 }
 
 int gfgpu_from_partitioned(const int32_t* idx, int64_t n, int64_t nnu, int64_t nnp,

@@ -140,6 +140,22 @@ class _QuadratureBase:
         t = _dev.empty(self.shape_elemmat())
         return t if val is None else t.fill_(val)
 
+    def asTensor(self, qscalar, qtensor):
+        """QuadratureBase::asTensor (Element.h:215-220): qscalar repeated over the tensor
+        components of `qtensor` [nelem, nip, tdim, ...]."""
+        src = _dev.dev_f64(qscalar)
+        _dev.check_shape(src, self.shape_qscalar(), "asTensor")
+        if tuple(qtensor.shape[:2]) != self.shape_qscalar():
+            raise ValueError(f"asTensor: shape {tuple(qtensor.shape)} is not a qtensor")
+        k = int(np.prod(qtensor.shape[2:], dtype=np.int64))
+        _lib.call("gfgpu_broadcast", src.data_ptr(), self._nelem * self._nip, k, qtensor.data_ptr(),
+                  _dev.stream())
+        return qtensor
+
+    def AsTensor(self, rank, qscalar):
+        """QuadratureBase::AsTensor(rank, qscalar) (Element.h:241-246)."""
+        return self.asTensor(qscalar, self.allocate_qtensor(rank))
+
     def GradN(self):
         return self._dNx
 

@@ -120,14 +120,21 @@ class MatrixDiagonal:
 
 
 class MatrixDiagonalPartitioned(MatrixDiagonal):
-    """MatrixDiagonalPartitioned(conn, dofs, iip) (MatrixDiagonalPartitioned.h:42-70)."""
+    """MatrixDiagonalPartitioned(conn, dofs, iip) (MatrixDiagonalPartitioned.h:42-452): the
+    diagonal stored as [A_uu, A_pp] back to back in the partitioned numbering."""
 
     def __init__(self, conn, dofs, iip):
         super().__init__(conn, dofs)
         self._iip = _dev.host_i32(iip)
         self._iiu, self._part = _mesh.partition(self._dofs_h, self._iip)
         self._nnu, self._nnp = self._iiu.size, self._iip.size
+        dof2part = np.empty(self._ndof, dtype=np.int32)
+        dof2part[self._iiu] = np.arange(self._nnu, dtype=np.int32)
+        dof2part[self._iip] = self._nnu + np.arange(self._nnp, dtype=np.int32)
         self.part_d = _dev.dev_i32(self._part)
+        self.dof2part_d = _dev.dev_i32(dof2part)
+        self.iiu_d = _dev.dev_i32(self._iiu)
+        self.iip_d = _dev.dev_i32(self._iip)
         p, i = _dev.dof_csr(self._conn_h, self._part, self._ndof)
         self.pcsr_ptr, self.pcsr_idx = _dev.dev_i32(p), _dev.dev_i32(i)
         self._App = _dev.empty((self._ndof,))  # [Auu, App] back to back
@@ -165,15 +172,23 @@ class MatrixDiagonalPartitioned(MatrixDiagonal):
         return self._App[self._nnu:]
 
     def data(self):
-        out = torch.zeros(self._ndof, dtype=torch.float64, device=self._App.device)
-        out[torch.as_tensor(self._iiu, device=out.device).long()] = self.data_uu()
-        out[torch.as_tensor(self._iip, device=out.device).long()] = self.data_pp()
+        """MatrixDiagonalPartitioned::data (MatrixDiagonalPartitioned.h:142-155): the diagonal in
+        the plain dof numbering."""
+        out = _dev.empty((self._ndof,))
+        _lib.call("gfgpu_from_partitioned", self.dof2part_d.data_ptr(), self._ndof, self._nnu,
+                  self._nnp, self._App.data_ptr(), self._App[self._nnu:].data_ptr(),
+                  out.data_ptr(), _dev.stream())
         return out
 
     def set(self, A):
+        """MatrixDiagonalPartitioned::set (MatrixDiagonalPartitioned.h:121-135)."""
         A = _dev.dev_f64(A)
-        self._App[: self._nnu] = A[torch.as_tensor(self._iiu, device=A.device).long()]
-        self._App[self._nnu:] = A[torch.as_tensor(self._iip, device=A.device).long()]
+        _dev.check_shape(A, (self._ndof,), "set")
+        s = _dev.stream()
+        _lib.call("gfgpu_from_partitioned", self.iiu_d.data_ptr(), self._nnu, self._ndof, 0,
+                  A.data_ptr(), None, self._App.data_ptr(), s)
+        _lib.call("gfgpu_from_partitioned", self.iip_d.data_ptr(), self._nnp, self._ndof, 0,
+                  A.data_ptr(), None, self._App[self._nnu:].data_ptr(), s)
         self._changed = True
 
     def _factorize(self):
@@ -182,25 +197,39 @@ class MatrixDiagonalPartitioned(MatrixDiagonal):
                       self._inv.data_ptr(), _dev.stream())
             self._changed = False
 
+    def _table(self, x):
+        """(index table, rows, columns) of a nodevec or a dofval argument."""
+        if x.dim() == 2:
+            _dev.check_shape(x, (self._nnode, self._ndim), "MatrixDiagonalPartitioned")
+            return self.part_d, self._nnode, self._ndim
+        _dev.check_shape(x, (self._ndof,), "MatrixDiagonalPartitioned")
+        return self.dof2part_d, self._ndof, 1
+
     def solve(self, b, x):
-        """MatrixDiagonalPartitioned::solve nodevec (MatrixDiagonalPartitioned.h:306-322):
-        writes the unknown dofs of x only."""
+        """MatrixDiagonalPartitioned::solve, nodevec or dofval (MatrixDiagonalPartitioned.h:
+        306-337): writes the unknown dofs of x only."""
         b = _dev.dev_f64(b)
+        tab, n, m = self._table(b)
+        _dev.check_shape(x, tuple(b.shape), "solve")
         self._factorize()
-        _lib.call("gfgpu_diag_solve_nodevec", self.part_d.data_ptr(), self._nnode, self._ndim,
-                  self._nnu, self._inv.data_ptr(), b.data_ptr(), x.data_ptr(), _dev.stream())
+        _lib.call("gfgpu_diag_solve_nodevec", tab.data_ptr(), n, m, self._nnu,
+                  self._inv.data_ptr(), b.data_ptr(), x.data_ptr(), _dev.stream())
         return x
 
-    def Solve(self, b, x):
-        x = _dev.dev_f64(x).clone()
+    def Solve(self, b, x=None):
+        """Solve with the prescribed dofs taken from `x` (zero if not given)."""
+        b = _dev.dev_f64(b)
+        x = torch.zeros_like(b) if x is None else _dev.dev_f64(x).clone()
         return self.solve(b, x)
 
     def reaction(self, x, b):
-        """MatrixDiagonalPartitioned::reaction nodevec (MatrixDiagonalPartitioned.h:378-392)."""
+        """MatrixDiagonalPartitioned::reaction, nodevec or dofval (MatrixDiagonalPartitioned.h:
+        378-403): b_p = A_pp x_p, other entries of b untouched."""
         x = _dev.dev_f64(x)
-        _lib.call("gfgpu_diagp_reaction_nodevec", self.part_d.data_ptr(), self._nnode, self._ndim,
-                  self._nnu, self._App[self._nnu:].data_ptr(), x.data_ptr(), b.data_ptr(),
-                  _dev.stream())
+        tab, n, m = self._table(x)
+        _dev.check_shape(b, tuple(x.shape), "reaction")
+        _lib.call("gfgpu_diagp_reaction_nodevec", tab.data_ptr(), n, m, self._nnu,
+                  self._App[self._nnu:].data_ptr(), x.data_ptr(), b.data_ptr(), _dev.stream())
         return b
 
     def Reaction(self, x, b):
@@ -208,11 +237,43 @@ class MatrixDiagonalPartitioned(MatrixDiagonal):
         return self.reaction(x, b)
 
     def dot(self, x, b):
-        """MatrixDiagonalPartitioned::dot nodevec (MatrixDiagonalPartitioned.h:189-205)."""
+        """MatrixDiagonalPartitioned::dot, nodevec or dofval (MatrixDiagonalPartitioned.h:
+        189-225)."""
         x = _dev.dev_f64(x)
-        _lib.call("gfgpu_diag_dot_nodevec", self.part_d.data_ptr(), self._nnode, self._ndim,
-                  self._App.data_ptr(), x.data_ptr(), b.data_ptr(), _dev.stream())
+        tab, n, m = self._table(x)
+        _dev.check_shape(b, tuple(x.shape), "dot")
+        _lib.call("gfgpu_diag_dot_nodevec", tab.data_ptr(), n, m, self._App.data_ptr(),
+                  x.data_ptr(), b.data_ptr(), _dev.stream())
         return b
+
+    # ------------------------------------------------- partitioned (x_u, x_p) variants
+    def _mul(self, a, x, n, name):
+        x = _dev.dev_f64(x)
+        _dev.check_shape(x, (n,), name)
+        out = _dev.empty((n,))
+        _lib.call("gfgpu_dofval_mul", a.data_ptr(), x.data_ptr(), n, out.data_ptr(), _dev.stream())
+        return out
+
+    def Dot_u(self, x_u, x_p):
+        """b_u = A_uu x_u (MatrixDiagonalPartitioned.h:234-262)."""
+        _dev.check_shape(x_p, (self._nnp,), "Dot_u")
+        return self._mul(self._App, x_u, self._nnu, "Dot_u")
+
+    def Dot_p(self, x_u, x_p):
+        """b_p = A_pp x_p (MatrixDiagonalPartitioned.h:272-300)."""
+        _dev.check_shape(x_u, (self._nnu,), "Dot_p")
+        return self._mul(self._App[self._nnu:], x_p, self._nnp, "Dot_p")
+
+    def Solve_u(self, b_u, x_p):
+        """x_u = A_uu^-1 b_u (MatrixDiagonalPartitioned.h:343-372)."""
+        _dev.check_shape(x_p, (self._nnp,), "Solve_u")
+        self._factorize()
+        return self._mul(self._inv, b_u, self._nnu, "Solve_u")
+
+    def Reaction_p(self, x_u, x_p):
+        """b_p = A_pp x_p (MatrixDiagonalPartitioned.h:405-421)."""
+        _dev.check_shape(x_u, (self._nnu,), "Reaction_p")
+        return self._mul(self._App[self._nnu:], x_p, self._nnp, "Reaction_p")
 
 
 def _pattern(conn_h, dmap_h, nnode, n):

@@ -247,6 +247,9 @@ int gfgpu_diagp_reaction_nodevec(const int32_t* part, int64_t nnode, int32_t ndi
 int gfgpu_dofval_mul(const double* a, const double* b, int64_t n, double* out,
                      gfgpu_stream_t stream);
 
+/* asTensor (Allocate.h asTensor / Element.h:215-246 QuadratureBase::AsTensor): out[i * k + j] =
+ * src[i], e.g. a qscalar [nelem, nip] repeated into a qtensor [nelem, nip, tdim^rank]. */
+int gfgpu_broadcast(const double* src, int64_t n, int64_t k, double* out, gfgpu_stream_t stream);
 /* VectorPartitioned::dofsFromParitioned / nodeFromPartitioned (VectorPartitioned.h:276-365):
  * out[t] = idx[t] < nnu ? u[idx[t]] : p[idx[t] - nnu], n entries. For a dofval pass as `idx` the
  * position of every dof in [iiu, iip] (ndof entries); for a nodevec pass `part` [nnode, ndim].
