@@ -620,6 +620,10 @@ using namespace gfgpu::nn;
 // element-kernel launch shared with the explicit step (dynamics.cu)
 int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                   cudaStream_t s);
+// two-level correction z = P ainv P^T r + minv r (coarse.cu)
+int gfgpu_internal_coarse_apply(const gfgpu_coarse_desc* g, const int32_t* part, int64_t nnu,
+                                const double* minv, const double* r, double* vc, double* yc,
+                                double* z, cudaStream_t s);
 
 namespace gfgpu {
 namespace nn {
@@ -1311,9 +1315,14 @@ int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* wor
     return nn_forward(nn, nullptr, X0, nullptr, 0, 1.0, nullptr, 0, a1, a2, a3, wt1, wt2, nullptr, Y, s);
 }
 
-int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
-                    double* x, double tol, int64_t maxiter, int32_t nkeep, int32_t check_every,
-                    void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres)
+} // extern "C"
+
+// the flexible CG of gfgpu_fcg_solve; with g != NULL the first direction of every iteration is
+// the two-level correction D^-1 r + P ainv P^T r (buffers after the ring workspace)
+static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
+                    const gfgpu_coarse_desc* g, double* x, double tol, int64_t maxiter,
+                    int32_t nkeep, int32_t check_every, void* workspace, gfgpu_stream_t stream,
+                    int64_t* iters, double* relres)
 {
     GF_REQUIRE(d && diag && x && workspace && iters && relres && tol > 0.0 && maxiter >= 0,
                "bad argument");
@@ -1329,6 +1338,14 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
     int64_t hw = nn ? int64_t(nn->H) * nn->W : 0;
     FcgWs w = carve_fcg(d, hw, nslots, workspace);
     const int64_t n = d->nnode * d->ndim;
+    double *zc = nullptr, *vc = nullptr, *yc = nullptr;
+    if (g) {
+        char* c = static_cast<char*>(workspace) + fcg_bytes(d, hw, nslots);
+        const int64_t nc = int64_t(g->ncx) * g->ncy * 2;
+        zc = reinterpret_cast<double*>(c);
+        vc = reinterpret_cast<double*>(c + a256(n * 8));
+        yc = reinterpret_cast<double*>(c + a256(n * 8) + a256(nc * 8));
+    }
     const double nfree = static_cast<double>(d->nnu);
     const unsigned gb = kRed;
     double h[F_COUNT];
@@ -1355,6 +1372,10 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
             for (int64_t k = std::max<int64_t>(0, c0 - nkeep); k < cur; ++k)
                 L.s[L.n++] = static_cast<int>(k % nslots);
             const double* zin = nullptr;
+            if (dd == 0 && g) {
+                GF_TRY(gfgpu_internal_coarse_apply(g, d->part, d->nnu, w.minv, w.r, vc, yc, zc, st));
+                zin = zc;
+            }
             if (dd == 1) {
                 GF_TRY(nn_apply(nn, w.r, w.sc, F_RR, nfree, d->part, d->nnu, w, w.z, st));
                 zin = w.z;
@@ -1468,6 +1489,39 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
     *relres = std::sqrt(h[F_RR]) / bnorm;
     if (*relres > tol) return fail(GFGPU_ERR_DIVERGED, "gfgpu_fcg_solve: tolerance not reached");
     return GFGPU_OK;
+}
+
+extern "C" {
+
+int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
+                    double* x, double tol, int64_t maxiter, int32_t nkeep, int32_t check_every,
+                    void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres)
+{
+    return fcg_core(d, diag, nn, nullptr, x, tol, maxiter, nkeep, check_every, workspace, stream,
+                    iters, relres);
+}
+
+int64_t gfgpu_fcg_coarse_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W,
+                                         int32_t nkeep, int32_t ndir, const gfgpu_coarse_desc* g)
+{
+    int64_t base = gfgpu_fcg_workspace_bytes(d, H, W, nkeep, ndir);
+    if (base == 0 || !g) return 0;
+    const int64_t nc = int64_t(g->ncx) * g->ncy * 2;
+    return base + a256(d->nnode * d->ndim * 8) + 2 * a256(nc * 8);
+}
+
+int gfgpu_fcg_solve_coarse(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
+                           const gfgpu_coarse_desc* g, double* x, double tol, int64_t maxiter,
+                           int32_t nkeep, int32_t check_every, void* workspace,
+                           gfgpu_stream_t stream, int64_t* iters, double* relres)
+{
+    GF_REQUIRE(g && g->ainv && d && d->nne == 4 && d->ndim == 2 &&
+                   int64_t(g->nx + 1) * (g->ny + 1) == d->nnode &&
+                   g->ncx == (g->nx + g->hc - 1) / g->hc + 1 && g->ncy == (g->ny + g->hc - 1) / g->hc + 1 &&
+                   int64_t(g->ncx) * g->ncy * 2 <= 8192,
+               "bad coarse grid");
+    return fcg_core(d, diag, nn, g, x, tol, maxiter, nkeep, check_every, workspace, stream, iters,
+                    relres);
 }
 
 } // extern "C"

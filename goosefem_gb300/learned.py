@@ -36,6 +36,13 @@ class NNDesc(C.Structure):
                 ("material", C.c_void_p), ("H", C.c_int32), ("W", C.c_int32)]
 
 
+class CoarseDesc(C.Structure):
+    """Mirror of gfgpu_coarse_desc (include/gfgpu.h)."""
+
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("hc", C.c_int32), ("ncx", C.c_int32),
+                ("ncy", C.c_int32), ("ainv", C.c_void_p)]
+
+
 def inclusion_material(nx, ny, seed, fraction=0.15, rmin=4.0, rmax=12.0, K0=1.0, G0=0.5, factor=10.0):
     """Two-phase element moduli: matrix (K0, G0) and circular inclusions (x factor), radius
     U[rmin, rmax] elements at seeded random centres, placed until the inclusion area (elements
@@ -113,6 +120,7 @@ class LearnedPreconditioner:
         self.R = None
         self.T = None
         self.losses = []
+        self.coarse = None
 
     # ------------------------------------------------------------------ helpers
     def _desc(self):
@@ -249,21 +257,62 @@ class LearnedPreconditioner:
         x[torch.as_tensor(self.iip, device=x.device).long()] = torch.as_tensor(xp, device=x.device)
         return x
 
-    def fcg(self, x, tol=1e-8, use_nn=True, maxiter=200000, nkeep=8, check_every=16):
+    def coarse_setup(self, hc=16):
+        """Two-level correction (gfgpu_coarse_setup): Galerkin matrix of bilinear hats on every
+        hc-th node, inverted once. Returns the FP64 coarse matrix (device) for checks."""
+        g = CoarseDesc()
+        _lib.call("gfgpu_coarse_grid", self.nx, self.ny, int(hc), C.addressof(g))
+        nc = g.ncx * g.ncy * 2
+        dev = _dev.device()
+        self.ainv = torch.empty((nc, nc), dtype=torch.float32, device=dev)
+        ac = torch.empty((nc, nc), dtype=torch.float64, device=dev)
+        nb = int(_lib.lib().gfgpu_coarse_setup_workspace_bytes(self._desc(), C.addressof(g)))
+        ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=dev)
+        _lib.call("gfgpu_coarse_setup", self._desc(), C.addressof(g), self.ainv.data_ptr(),
+                  ac.data_ptr(), ws.data_ptr(), _dev.stream())
+        g.ainv = self.ainv.data_ptr()
+        self.coarse = g
+        return ac
+
+    def coarse_apply(self, r):
+        """z = P A_c^-1 P^T r on the free dofs (gfgpu_coarse_apply)."""
+        r = _dev.dev_f64(r).contiguous()
+        z = torch.empty_like(r)
+        nc = self.coarse.ncx * self.coarse.ncy * 2
+        ws = torch.empty(2 * ((nc * 8 + 255) // 256 * 256) // 8, dtype=torch.float64,
+                         device=r.device)
+        _lib.call("gfgpu_coarse_apply", self._desc(), C.addressof(self.coarse), r.data_ptr(),
+                  z.data_ptr(), ws.data_ptr(), _dev.stream())
+        return z
+
+    def fcg(self, x, tol=1e-8, use_nn=True, maxiter=200000, nkeep=8, check_every=16,
+            coarse=False):
         """Flexible CG (gfgpu_fcg_solve) in place on x (prescribed values + initial guess): with
         the network, two directions per iteration (D^-1 r and the network's correction); without,
-        Jacobi only. Returns (iterations, relative true residual)."""
+        Jacobi only. coarse=True adds the two-level correction to the first direction
+        (gfgpu_fcg_solve_coarse; coarse_setup first). Returns (iterations, relative true
+        residual)."""
         ndir = 2 if use_nn else 1
-        nb = int(_lib.lib().gfgpu_fcg_workspace_bytes(self._desc(), self.H, self.W, nkeep, ndir))
+        if coarse:
+            nb = int(_lib.lib().gfgpu_fcg_coarse_workspace_bytes(
+                self._desc(), self.H, self.W, nkeep, ndir, C.addressof(self.coarse)))
+        else:
+            nb = int(_lib.lib().gfgpu_fcg_workspace_bytes(self._desc(), self.H, self.W, nkeep, ndir))
         if nb <= 0:
             raise ValueError("nkeep out of range")
         ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=_dev.device())
         it = C.c_int64(0)
         rel = C.c_double(0.0)
         nnd = C.addressof(self.nn_desc()) if use_nn else None
-        _lib.call("gfgpu_fcg_solve", self._desc(), self.static.diag.data_ptr(), nnd, x.data_ptr(),
-                  float(tol), int(maxiter), int(nkeep), int(check_every), ws.data_ptr(),
-                  _dev.stream(), C.addressof(it), C.addressof(rel))
+        if coarse:
+            _lib.call("gfgpu_fcg_solve_coarse", self._desc(), self.static.diag.data_ptr(), nnd,
+                      C.addressof(self.coarse), x.data_ptr(), float(tol), int(maxiter), int(nkeep),
+                      int(check_every), ws.data_ptr(), _dev.stream(), C.addressof(it),
+                      C.addressof(rel))
+        else:
+            _lib.call("gfgpu_fcg_solve", self._desc(), self.static.diag.data_ptr(), nnd,
+                      x.data_ptr(), float(tol), int(maxiter), int(nkeep), int(check_every),
+                      ws.data_ptr(), _dev.stream(), C.addressof(it), C.addressof(rel))
         return int(it.value), float(rel.value)
 
     def solve(self, x, tol=1e-8, maxiter=20000, nkeep=8, check_every=16):

@@ -612,6 +612,37 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
                     double* x, double tol, int64_t maxiter, int32_t nkeep, int32_t check_every,
                     void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres);
 
+/* ---- two-level correction (no counterpart in the reference; used with gfgpu_fcg_solve_coarse) */
+/* Coarse space of a Regular Quad4 grid of nx x ny elements (node iy (nx + 1) + ix): bilinear
+ * hats on every hc-th node along each axis (the last interval may be shorter), ncx x ncy coarse
+ * nodes, two dofs each (coarse dof (jy ncx + jx) 2 + c), restricted to the free fine dofs.
+ * `ainv` is the dense FP32 inverse of the Galerkin matrix P^T A_uu P, [nc, nc], nc = 2 ncx ncy
+ * (at most 8192), filled by gfgpu_coarse_setup. */
+typedef struct {
+    int32_t nx, ny, hc, ncx, ncy;
+    const float* ainv;
+} gfgpu_coarse_desc;
+/* Fills nx, ny, hc and the coarse node counts; ainv = NULL. */
+int gfgpu_coarse_grid(int32_t nx, int32_t ny, int32_t hc, gfgpu_coarse_desc* g);
+int64_t gfgpu_coarse_setup_workspace_bytes(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g);
+/* Measures A_c = P^T A_uu P with the matrix-free operator of `d` (18 coloured probes), writes it
+ * to `ac` (FP64 [nc, nc], optional), inverts it in FP64 (Gauss-Jordan; A_c is SPD) and writes the
+ * FP32 inverse to `ainv`. Synchronises `stream`. GFGPU_ERR_NAN for a singular coarse matrix. */
+int gfgpu_coarse_setup(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g, float* ainv,
+                       double* ac, void* workspace, gfgpu_stream_t stream);
+/* z = P ainv P^T r on the free dofs (0 on prescribed); r, z [nnode * 2]; workspace 2 x
+ * 256-byte-rounded nc doubles. */
+int gfgpu_coarse_apply(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g, const double* r,
+                       double* z, void* workspace, gfgpu_stream_t stream);
+/* gfgpu_fcg_solve with the two-level first direction D^-1 r + P ainv P^T r (the network
+ * direction, when `nn` is given, unchanged). Workspace: gfgpu_fcg_coarse_workspace_bytes. */
+int64_t gfgpu_fcg_coarse_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W,
+                                         int32_t nkeep, int32_t ndir, const gfgpu_coarse_desc* g);
+int gfgpu_fcg_solve_coarse(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
+                           const gfgpu_coarse_desc* g, double* x, double tol, int64_t maxiter,
+                           int32_t nkeep, int32_t check_every, void* workspace,
+                           gfgpu_stream_t stream, int64_t* iters, double* relres);
+
 /* ============================ probes ====================================================== */
 
 /* FP64 FMA throughput probe: a kernel of independent DFMA chains, `blocks` x 256 threads,
