@@ -32,29 +32,35 @@ __host__ __device__ inline int coarse_x(int j, int hc, int nel)
     return min(j * hc, nel);
 }
 
+// Interval j of an axis spans [coarse_x(j), coarse_x(j + 1)]: length hc (reciprocal rh) except
+// the last one, j = nc - 2 (reciprocal rl). No division on the device.
+__device__ inline double rlen(int j, int nc, double rh, double rl)
+{
+    return j == nc - 2 ? rl : rh;
+}
+
 // fine node i on an axis: left coarse index j0 and the weight w0 of j0 (1 - w0 for j0 + 1)
-__device__ inline void hat(int i, int hc, int nel, int nc, int& j0, double& w0)
+__device__ inline void hat(int i, int hc, int nel, int nc, double rh, double rl, int& j0, double& w0)
 {
     int j = i / hc;
     if (j > nc - 2) j = nc - 2;
-    int x0 = coarse_x(j, hc, nel), x1 = coarse_x(j + 1, hc, nel);
     j0 = j;
-    w0 = double(x1 - i) / double(x1 - x0);
+    w0 = double(coarse_x(j + 1, hc, nel) - i) * rlen(j, nc, rh, rl);
 }
 
 // weight of coarse index j at fine node i (0 outside its support)
-__device__ inline double hat_w(int j, int i, int hc, int nel, int nc)
+__device__ inline double hat_w(int j, int i, int hc, int nel, int nc, double rh, double rl)
 {
     int x = coarse_x(j, hc, nel);
     if (i == x) return 1.0;
     if (i < x) {
         if (j == 0) return 0.0;
         int xl = coarse_x(j - 1, hc, nel);
-        return i > xl ? double(i - xl) / double(x - xl) : 0.0;
+        return i > xl ? double(i - xl) * rlen(j - 1, nc, rh, rl) : 0.0;
     }
     if (j == nc - 1) return 0.0;
     int xr = coarse_x(j + 1, hc, nel);
-    return i < xr ? double(xr - i) / double(xr - x) : 0.0;
+    return i < xr ? double(xr - i) * rlen(j, nc, rh, rl) : 0.0;
 }
 
 __device__ __forceinline__ double bsum(double v, double* sh)
@@ -89,7 +95,7 @@ k_restrict(gfgpu_coarse_desc g, const int32_t* __restrict__ part, int64_t nnu,
     double a0 = 0.0, a1 = 0.0;
     for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
         int ix = x0 + k % sx, iy = y0 + k / sx;
-        double w = hat_w(jx, ix, g.hc, g.nx, g.ncx) * hat_w(jy, iy, g.hc, g.ny, g.ncy);
+        double w = hat_w(jx, ix, g.hc, g.nx, g.ncx, g.rhx, g.rlx) * hat_w(jy, iy, g.hc, g.ny, g.ncy, g.rhy, g.rly);
         int64_t t = (iy * W + ix) * 2;
         if (part[t] < nnu) a0 = fma(w, f[t], a0);
         if (part[t + 1] < nnu) a1 = fma(w, f[t + 1], a1);
@@ -113,8 +119,8 @@ __global__ void k_prolong(gfgpu_coarse_desc g, const int32_t* __restrict__ part,
         int ix = static_cast<int>(node % W), iy = static_cast<int>(node / W);
         int jx, jy;
         double wx, wy;
-        hat(ix, g.hc, g.nx, g.ncx, jx, wx);
-        hat(iy, g.hc, g.ny, g.ncy, jy, wy);
+        hat(ix, g.hc, g.nx, g.ncx, g.rhx, g.rlx, jx, wx);
+        hat(iy, g.hc, g.ny, g.ncy, g.rhy, g.rly, jy, wy);
         const double w[4] = {wx * wy, (1.0 - wx) * wy, wx * (1.0 - wy), (1.0 - wx) * (1.0 - wy)};
         const int64_t c[4] = {int64_t(jy) * g.ncx + jx, int64_t(jy) * g.ncx + jx + 1,
                               int64_t(jy + 1) * g.ncx + jx, int64_t(jy + 1) * g.ncx + jx + 1};
@@ -283,12 +289,17 @@ int gfgpu_internal_coarse_apply(const gfgpu_coarse_desc* g, const int32_t* part,
 
 static int check_grid(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g)
 {
+    GF_REQUIRE(g != nullptr, "bad argument");
     GF_REQUIRE(d && g && d->nne == 4 && d->ndim == 2, "a Quad4 mesh is required");
     GF_REQUIRE(g->nx >= 1 && g->ny >= 1 && g->hc >= 1, "bad coarse grid");
     GF_REQUIRE(int64_t(g->nx + 1) * (g->ny + 1) == d->nnode, "nodes != (nx + 1) (ny + 1)");
     GF_REQUIRE(g->ncx == (g->nx + g->hc - 1) / g->hc + 1 && g->ncy == (g->ny + g->hc - 1) / g->hc + 1,
                "ncx, ncy do not match nx, ny, hc");
     GF_REQUIRE(ncoarse(g) <= kMaxCoarseDofs, "coarse grid too large (more than 8192 coarse dofs)");
+    gfgpu_coarse_desc e;
+    gfgpu_coarse_grid(g->nx, g->ny, g->hc, &e);
+    GF_REQUIRE(g->rhx == e.rhx && g->rlx == e.rlx && g->rhy == e.rhy && g->rly == e.rly,
+               "reciprocal interval lengths do not match nx, ny, hc (use gfgpu_coarse_grid)");
     return GFGPU_OK;
 }
 
@@ -303,6 +314,9 @@ int gfgpu_coarse_grid(int32_t nx, int32_t ny, int32_t hc, gfgpu_coarse_desc* g)
     g->ncx = (nx + hc - 1) / hc + 1;
     g->ncy = (ny + hc - 1) / hc + 1;
     g->ainv = nullptr;
+    g->rhx = g->rhy = 1.0 / hc;
+    g->rlx = 1.0 / (nx - (g->ncx - 2) * hc);
+    g->rly = 1.0 / (ny - (g->ncy - 2) * hc);
     return GFGPU_OK;
 }
 

@@ -1320,7 +1320,7 @@ int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* wor
 // the flexible CG of gfgpu_fcg_solve; with g != NULL the first direction of every iteration is
 // the two-level correction D^-1 r + P ainv P^T r (buffers after the ring workspace)
 static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
-                    const gfgpu_coarse_desc* g, double* x, double tol, int64_t maxiter,
+                    const gfgpu_coarse_desc* g, const double* rhs, double* x, double tol, int64_t maxiter,
                     int32_t nkeep, int32_t check_every, void* workspace, gfgpu_stream_t stream,
                     int64_t* iters, double* relres)
 {
@@ -1404,12 +1404,12 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
     // ||b||, b = -(A x_p)_u (P slot 0 as scratch)
     k_fkeep<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.P);
     GF_TRY(gfgpu_internal_element_forces(d, w.P, w.fe, s));
-    k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, nullptr, n, w.z,
+    k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, rhs, n, w.z,
                               w.partial);
     k_fredv<<<1, 1024, 0, s>>>(w.partial, one(F_BB), w.sc);
     // r = -(A x)_u
     GF_TRY(gfgpu_internal_element_forces(d, x, w.fe, s));
-    k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, nullptr, n, w.r,
+    k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, rhs, n, w.r,
                               w.partial);
     k_fredv<<<1, 1024, 0, s>>>(w.partial, one(F_RR), w.sc);
     GF_TRY(read_sc());
@@ -1481,7 +1481,7 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
     GF_TRY(rc);
     // true residual -(A x)_u
     GF_TRY(gfgpu_internal_element_forces(d, x, w.fe, s));
-    k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, nullptr, n, w.r,
+    k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, rhs, n, w.r,
                               w.partial);
     k_fredv<<<1, 1024, 0, s>>>(w.partial, one(F_RR), w.sc);
     GF_TRY(read_sc());
@@ -1497,8 +1497,8 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
                     double* x, double tol, int64_t maxiter, int32_t nkeep, int32_t check_every,
                     void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres)
 {
-    return fcg_core(d, diag, nn, nullptr, x, tol, maxiter, nkeep, check_every, workspace, stream,
-                    iters, relres);
+    return fcg_core(d, diag, nn, nullptr, nullptr, x, tol, maxiter, nkeep, check_every, workspace,
+                    stream, iters, relres);
 }
 
 int64_t gfgpu_fcg_coarse_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W,
@@ -1511,7 +1511,8 @@ int64_t gfgpu_fcg_coarse_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, 
 }
 
 int gfgpu_fcg_solve_coarse(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
-                           const gfgpu_coarse_desc* g, double* x, double tol, int64_t maxiter,
+                           const gfgpu_coarse_desc* g, const double* rhs, double* x, double tol,
+                           int64_t maxiter,
                            int32_t nkeep, int32_t check_every, void* workspace,
                            gfgpu_stream_t stream, int64_t* iters, double* relres)
 {
@@ -1520,8 +1521,8 @@ int gfgpu_fcg_solve_coarse(const gfgpu_verlet_desc* d, const double* diag, const
                    g->ncx == (g->nx + g->hc - 1) / g->hc + 1 && g->ncy == (g->ny + g->hc - 1) / g->hc + 1 &&
                    int64_t(g->ncx) * g->ncy * 2 <= 8192,
                "bad coarse grid");
-    return fcg_core(d, diag, nn, g, x, tol, maxiter, nkeep, check_every, workspace, stream, iters,
-                    relres);
+    return fcg_core(d, diag, nn, g, rhs, x, tol, maxiter, nkeep, check_every, workspace, stream,
+                    iters, relres);
 }
 
 } // extern "C"

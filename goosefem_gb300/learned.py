@@ -40,7 +40,8 @@ class CoarseDesc(C.Structure):
     """Mirror of gfgpu_coarse_desc (include/gfgpu.h)."""
 
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("hc", C.c_int32), ("ncx", C.c_int32),
-                ("ncy", C.c_int32), ("ainv", C.c_void_p)]
+                ("ncy", C.c_int32), ("ainv", C.c_void_p), ("rhx", C.c_double), ("rlx", C.c_double),
+                ("rhy", C.c_double), ("rly", C.c_double)]
 
 
 def inclusion_material(nx, ny, seed, fraction=0.15, rmin=4.0, rmax=12.0, K0=1.0, G0=0.5, factor=10.0):
@@ -209,6 +210,101 @@ class LearnedPreconditioner:
                 k += 1
         return npairs
 
+    def _residual(self, x, b):
+        """r = b - A x on the free dofs (0 on prescribed), FP64."""
+        f = self.static.force(x.view(self.H * self.W, 2)).view(-1)
+        return torch.where(self.free, b - f, torch.zeros((), dtype=torch.float64, device=x.device))
+
+    def _apply_free(self, v):
+        """(A v) on the free dofs for v that is 0 on the prescribed dofs."""
+        f = self.static.force(v.view(self.H * self.W, 2)).view(-1)
+        return torch.where(self.free, f, torch.zeros((), dtype=torch.float64, device=v.device))
+
+    def _lambda_max(self, iters=40, seed=5):
+        """Largest eigenvalue of D^-1 A_uu (power iteration), cached."""
+        if getattr(self, "_lmax", None) is None:
+            gen = torch.Generator(device=_dev.device())
+            gen.manual_seed(seed)
+            v = torch.rand(self.H * self.W * 2, generator=gen, dtype=torch.float64,
+                           device=_dev.device()) * self.free
+            lam = 0.0
+            for _ in range(iters):
+                w = self.minv * self._apply_free(v)
+                lam = float((v * w).sum() / (v * v).sum())
+                v = w / torch.linalg.vector_norm(w)
+            self._lmax = 1.05 * lam
+        return self._lmax
+
+    def chebyshev(self, r, degree=8, ratio=30.0):
+        """Chebyshev semi-iteration for A_uu c = r, Jacobi-preconditioned, on the interval
+        [lambda_max / ratio, lambda_max] of D^-1 A_uu: a fixed linear map whose support grows by
+        one node per degree (17 x 17 nodes at degree 8)."""
+        hi = self._lambda_max()
+        lo = hi / ratio
+        th, de = 0.5 * (hi + lo), 0.5 * (hi - lo)
+        sig = th / de
+        rho = 1.0 / sig
+        x = torch.zeros_like(r)
+        res = r.clone()
+        d = self.minv * res / th
+        for _ in range(degree):
+            x += d
+            res -= self._apply_free(d)
+            rho_n = 1.0 / (2.0 * sig - rho)
+            d = rho_n * rho * d + (2.0 * rho_n / de) * (self.minv * res)
+            rho = rho_n
+        return x
+
+    def make_pairs_twolevel(self, nloads=64, snaps=48, every=4, seed=1, nkeep=4, target="cheb",
+                            degree=8):
+        """(residual, correction) pairs for the network as the fine-level part of the two-level
+        preconditioner (coarse_setup first). For each random load the exact solution x* comes
+        from the two-level solve to 1e-11; the snapshots x_k are the iterates of the same solver
+        restarted every `every` iterations. For r_k = b - A x_k the target is, with target="cheb",
+        what `degree` Chebyshev steps add beyond the Jacobi step, chebyshev(r_k) - D^-1 r_k (a
+        linear map of the network's receptive field), or, with target="error", what the
+        two-level direction misses of the exact error, (x* - x_k) - P A_c^-1 P^T r_k - D^-1 r_k;
+        both are divided by the RMS of r_k over the free dofs."""
+        if self.coarse is None:
+            raise RuntimeError("coarse_setup first")
+        npairs = nloads * snaps
+        dev = _dev.device()
+        self.R = torch.empty((npairs, self.H, self.W, 2), dtype=torch.float32, device=dev)
+        self.T = torch.empty_like(self.R)
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(seed)
+        n = self.H * self.W * 2
+        x = torch.zeros(n, dtype=torch.float64, device=dev)
+        k = 0
+        for load in range(nloads):
+            b = self._load(load % 4, gen, x)
+            xs = x.clone()
+            for _ in range(3):  # restarts clear the drift of the recurrence residual
+                try:
+                    self.fcg(xs, tol=1e-11, use_nn=False, nkeep=nkeep, coarse=True, rhs=b)
+                    break
+                except _lib.GFGPUError as e:
+                    if e.code != -8:
+                        raise
+            xk = x.clone()
+            for snap in range(snaps):
+                r = self._residual(xk, b)
+                sigma = torch.sqrt((r[self.free] ** 2).sum() / self.nfree)
+                if target == "cheb":
+                    t = self.chebyshev(r, degree) - self.minv * r
+                else:
+                    t = (xs - xk) - self.coarse_apply(r) - self.minv * r
+                self.R[k] = (r / sigma).view(self.H, self.W, 2).float()
+                self.T[k] = (t / sigma).view(self.H, self.W, 2).float()
+                k += 1
+                try:
+                    self.fcg(xk, tol=1e-14, use_nn=False, nkeep=nkeep, coarse=True, rhs=b,
+                             maxiter=every)
+                except _lib.GFGPUError as e:
+                    if e.code != -8:  # maxiter reached: the expected exit
+                        raise
+        return npairs
+
     # ------------------------------------------------------------------ training
     def train(self, steps=2000, batch=32, crop=64, margin=8, lr=2e-3, seed=2, log_every=0,
               loss="energy"):
@@ -286,12 +382,12 @@ class LearnedPreconditioner:
         return z
 
     def fcg(self, x, tol=1e-8, use_nn=True, maxiter=200000, nkeep=8, check_every=16,
-            coarse=False):
+            coarse=False, rhs=None):
         """Flexible CG (gfgpu_fcg_solve) in place on x (prescribed values + initial guess): with
         the network, two directions per iteration (D^-1 r and the network's correction); without,
         Jacobi only. coarse=True adds the two-level correction to the first direction
-        (gfgpu_fcg_solve_coarse; coarse_setup first). Returns (iterations, relative true
-        residual)."""
+        (gfgpu_fcg_solve_coarse; coarse_setup first), which also takes an external load `rhs`.
+        Returns (iterations, relative true residual)."""
         ndir = 2 if use_nn else 1
         if coarse:
             nb = int(_lib.lib().gfgpu_fcg_coarse_workspace_bytes(
@@ -306,7 +402,8 @@ class LearnedPreconditioner:
         nnd = C.addressof(self.nn_desc()) if use_nn else None
         if coarse:
             _lib.call("gfgpu_fcg_solve_coarse", self._desc(), self.static.diag.data_ptr(), nnd,
-                      C.addressof(self.coarse), x.data_ptr(), float(tol), int(maxiter), int(nkeep),
+                      C.addressof(self.coarse), None if rhs is None else rhs.data_ptr(),
+                      x.data_ptr(), float(tol), int(maxiter), int(nkeep),
                       int(check_every), ws.data_ptr(), _dev.stream(), C.addressof(it),
                       C.addressof(rel))
         else:

@@ -621,8 +621,9 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
 typedef struct {
     int32_t nx, ny, hc, ncx, ncy;
     const float* ainv;
+    double rhx, rlx, rhy, rly; /* 1 / hc and 1 / (length of the last interval), along x and y */
 } gfgpu_coarse_desc;
-/* Fills nx, ny, hc and the coarse node counts; ainv = NULL. */
+/* Fills nx, ny, hc, the coarse node counts and the reciprocal interval lengths; ainv = NULL. */
 int gfgpu_coarse_grid(int32_t nx, int32_t ny, int32_t hc, gfgpu_coarse_desc* g);
 int64_t gfgpu_coarse_setup_workspace_bytes(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g);
 /* Measures A_c = P^T A_uu P with the matrix-free operator of `d` (18 coloured probes), writes it
@@ -635,11 +636,13 @@ int gfgpu_coarse_setup(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g, f
 int gfgpu_coarse_apply(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g, const double* r,
                        double* z, void* workspace, gfgpu_stream_t stream);
 /* gfgpu_fcg_solve with the two-level first direction D^-1 r + P ainv P^T r (the network
- * direction, when `nn` is given, unchanged). Workspace: gfgpu_fcg_coarse_workspace_bytes. */
+ * direction, when `nn` is given, unchanged) and an optional external load `rhs` [nnode * 2]
+ * (b = rhs_u - (A x_p)_u; NULL: no load). Workspace: gfgpu_fcg_coarse_workspace_bytes. */
 int64_t gfgpu_fcg_coarse_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W,
                                          int32_t nkeep, int32_t ndir, const gfgpu_coarse_desc* g);
 int gfgpu_fcg_solve_coarse(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
-                           const gfgpu_coarse_desc* g, double* x, double tol, int64_t maxiter,
+                           const gfgpu_coarse_desc* g, const double* rhs, double* x, double tol,
+                           int64_t maxiter,
                            int32_t nkeep, int32_t check_every, void* workspace,
                            gfgpu_stream_t stream, int64_t* iters, double* relres);
 
