@@ -19,6 +19,7 @@ namespace coarse {
 
 constexpr int kRestrictThreads = 256;
 constexpr int64_t kMaxCoarseDofs = 8192; // dense inverse: 256 MB FP32, set-up 512 MB FP64
+static_assert(kMaxCoarseDofs * 4 <= 48 * 1024, "k_dense stages v in default shared memory");
 constexpr int kRowsPerBlock = 8;         // dense product: one warp per row
 
 inline int64_t a256(int64_t b)
@@ -33,46 +34,51 @@ __host__ __device__ inline int coarse_x(int j, int hc, int nel)
 }
 
 // Interval j of an axis spans [coarse_x(j), coarse_x(j + 1)]: length hc (reciprocal rh) except
-// the last one, j = nc - 2 (reciprocal rl). No division on the device.
-__device__ inline double rlen(int j, int nc, double rh, double rl)
+// the last one, j = nc - 2 (reciprocal rl). No division on the device. T = double for the set-up
+// (the Galerkin matrix), float for the correction inside the solve.
+template <typename T>
+__device__ inline T rlen(int j, int nc, double rh, double rl)
 {
-    return j == nc - 2 ? rl : rh;
+    return static_cast<T>(j == nc - 2 ? rl : rh);
 }
 
 // fine node i on an axis: left coarse index j0 and the weight w0 of j0 (1 - w0 for j0 + 1)
-__device__ inline void hat(int i, int hc, int nel, int nc, double rh, double rl, int& j0, double& w0)
+template <typename T>
+__device__ inline void hat(int i, int hc, int nel, int nc, double rh, double rl, int& j0, T& w0)
 {
     int j = i / hc;
     if (j > nc - 2) j = nc - 2;
     j0 = j;
-    w0 = double(coarse_x(j + 1, hc, nel) - i) * rlen(j, nc, rh, rl);
+    w0 = static_cast<T>(coarse_x(j + 1, hc, nel) - i) * rlen<T>(j, nc, rh, rl);
 }
 
 // weight of coarse index j at fine node i (0 outside its support)
-__device__ inline double hat_w(int j, int i, int hc, int nel, int nc, double rh, double rl)
+template <typename T>
+__device__ inline T hat_w(int j, int i, int hc, int nel, int nc, double rh, double rl)
 {
     int x = coarse_x(j, hc, nel);
-    if (i == x) return 1.0;
+    if (i == x) return T(1);
     if (i < x) {
-        if (j == 0) return 0.0;
+        if (j == 0) return T(0);
         int xl = coarse_x(j - 1, hc, nel);
-        return i > xl ? double(i - xl) * rlen(j - 1, nc, rh, rl) : 0.0;
+        return i > xl ? static_cast<T>(i - xl) * rlen<T>(j - 1, nc, rh, rl) : T(0);
     }
-    if (j == nc - 1) return 0.0;
+    if (j == nc - 1) return T(0);
     int xr = coarse_x(j + 1, hc, nel);
-    return i < xr ? double(xr - i) * rlen(j, nc, rh, rl) : 0.0;
+    return i < xr ? static_cast<T>(xr - i) * rlen<T>(j, nc, rh, rl) : T(0);
 }
 
-__device__ __forceinline__ double bsum(double v, double* sh)
+template <typename T>
+__device__ __forceinline__ T bsum(T v, T* sh)
 {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
     if (lane == 0) sh[wi] = v;
     __syncthreads();
-    double r = 0.0;
+    T r = T(0);
     if (wi == 0) {
-        r = lane < (blockDim.x >> 5) ? sh[lane] : 0.0;
+        r = lane < (blockDim.x >> 5) ? sh[lane] : T(0);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
     }
@@ -81,24 +87,27 @@ __device__ __forceinline__ double bsum(double v, double* sh)
 }
 
 // v[(jy * ncx + jx) * 2 + c] = sum over the hat's support of w(ix) w(iy) f[(iy W + ix) 2 + c] on
-// free dofs; one block per coarse node
+// free dofs, accumulated in T; one block per coarse node
+template <typename T>
 __global__ void __launch_bounds__(kRestrictThreads)
 k_restrict(gfgpu_coarse_desc g, const int32_t* __restrict__ part, int64_t nnu,
-           const double* __restrict__ f, double* __restrict__ v)
+           const double* __restrict__ f, T* __restrict__ v)
 {
-    __shared__ double sh[32];
+    __shared__ T sh[32];
     const int jx = blockIdx.x % g.ncx, jy = blockIdx.x / g.ncx;
     const int x0 = coarse_x(max(jx - 1, 0), g.hc, g.nx), x1 = coarse_x(min(jx + 1, g.ncx - 1), g.hc, g.nx);
     const int y0 = coarse_x(max(jy - 1, 0), g.hc, g.ny), y1 = coarse_x(min(jy + 1, g.ncy - 1), g.hc, g.ny);
     const int sx = x1 - x0 + 1, cnt = sx * (y1 - y0 + 1);
     const int64_t W = g.nx + 1;
-    double a0 = 0.0, a1 = 0.0;
+    T a0 = T(0), a1 = T(0);
     for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
         int ix = x0 + k % sx, iy = y0 + k / sx;
-        double w = hat_w(jx, ix, g.hc, g.nx, g.ncx, g.rhx, g.rlx) * hat_w(jy, iy, g.hc, g.ny, g.ncy, g.rhy, g.rly);
+        T w = hat_w<T>(jx, ix, g.hc, g.nx, g.ncx, g.rhx, g.rlx) * hat_w<T>(jy, iy, g.hc, g.ny, g.ncy, g.rhy, g.rly);
         int64_t t = (iy * W + ix) * 2;
-        if (part[t] < nnu) a0 = fma(w, f[t], a0);
-        if (part[t + 1] < nnu) a1 = fma(w, f[t + 1], a1);
+        int2 pt = __ldg(reinterpret_cast<const int2*>(part + t));
+        double2 ft = __ldg(reinterpret_cast<const double2*>(f + t));
+        if (pt.x < nnu) a0 += w * static_cast<T>(ft.x);
+        if (pt.y < nnu) a1 += w * static_cast<T>(ft.y);
     }
     a0 = bsum(a0, sh);
     a1 = bsum(a1, sh);
@@ -108,9 +117,10 @@ k_restrict(gfgpu_coarse_desc g, const int32_t* __restrict__ part, int64_t nnu,
     }
 }
 
-// z = (P y)_u  (+ minv * r when minv is given); 0 on prescribed dofs
+// z = (P y)_u  (+ minv * r when minv is given), interpolation in T; 0 on prescribed dofs
+template <typename T>
 __global__ void k_prolong(gfgpu_coarse_desc g, const int32_t* __restrict__ part, int64_t nnu,
-                          const double* __restrict__ y, const double* __restrict__ minv,
+                          const T* __restrict__ y, const double* __restrict__ minv,
                           const double* __restrict__ r, double* __restrict__ z)
 {
     const int64_t W = g.nx + 1, nn = W * (g.ny + 1);
@@ -118,42 +128,58 @@ __global__ void k_prolong(gfgpu_coarse_desc g, const int32_t* __restrict__ part,
     {
         int ix = static_cast<int>(node % W), iy = static_cast<int>(node / W);
         int jx, jy;
-        double wx, wy;
-        hat(ix, g.hc, g.nx, g.ncx, g.rhx, g.rlx, jx, wx);
-        hat(iy, g.hc, g.ny, g.ncy, g.rhy, g.rly, jy, wy);
-        const double w[4] = {wx * wy, (1.0 - wx) * wy, wx * (1.0 - wy), (1.0 - wx) * (1.0 - wy)};
+        T wx, wy;
+        hat<T>(ix, g.hc, g.nx, g.ncx, g.rhx, g.rlx, jx, wx);
+        hat<T>(iy, g.hc, g.ny, g.ncy, g.rhy, g.rly, jy, wy);
+        const T w[4] = {wx * wy, (T(1) - wx) * wy, wx * (T(1) - wy), (T(1) - wx) * (T(1) - wy)};
         const int64_t c[4] = {int64_t(jy) * g.ncx + jx, int64_t(jy) * g.ncx + jx + 1,
                               int64_t(jy + 1) * g.ncx + jx, int64_t(jy + 1) * g.ncx + jx + 1};
+        const int64_t t = node * 2;
+        const int2 pt = __ldg(reinterpret_cast<const int2*>(part + t));
+        T s0 = T(0), s1 = T(0);
 #pragma unroll
-        for (int comp = 0; comp < 2; ++comp) {
-            int64_t t = node * 2 + comp;
-            double s = 0.0;
-            if (part[t] < nnu) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) s = fma(w[k], y[c[k] * 2 + comp], s);
-                if (minv) s = fma(minv[t], r[t], s);
-            }
-            z[t] = s;
+        for (int k = 0; k < 4; ++k) {
+            s0 += w[k] * __ldg(y + c[k] * 2);
+            s1 += w[k] * __ldg(y + c[k] * 2 + 1);
         }
+        double z0 = static_cast<double>(s0), z1 = static_cast<double>(s1);
+        if (minv) {
+            z0 = fma(minv[t], r[t], z0);
+            z1 = fma(minv[t + 1], r[t + 1], z1);
+        }
+        z[t] = pt.x < nnu ? z0 : 0.0;
+        z[t + 1] = pt.y < nnu ? z1 : 0.0;
     }
 }
 
-// y = Ainv v (FP32 matrix, FP32 products, FP64 result); one warp per row, v staged in shared
+// y = Ainv v (FP32 matrix [nc, ld], FP32 vectors); one warp per row with 16-byte loads, v staged
+// in shared memory (zero padded to ld)
 __global__ void __launch_bounds__(32 * kRowsPerBlock)
-k_dense(const float* __restrict__ ainv, int64_t nc, const double* __restrict__ v, double* __restrict__ y)
+k_dense(const float* __restrict__ ainv, int64_t nc, int64_t ld, const float* __restrict__ v,
+        float* __restrict__ y)
 {
-    extern __shared__ float vs[];
-    for (int64_t k = threadIdx.x; k < nc; k += blockDim.x) vs[k] = static_cast<float>(v[k]);
+    extern __shared__ float4 vs4[];
+    float* vs = reinterpret_cast<float*>(vs4);
+    for (int64_t k = threadIdx.x; k < ld; k += blockDim.x) vs[k] = k < nc ? v[k] : 0.0f;
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int64_t row = int64_t(blockIdx.x) * kRowsPerBlock + (threadIdx.x >> 5);
     if (row >= nc) return;
-    const float* a = ainv + row * nc;
-    float acc = 0.0f;
-    for (int64_t k = lane; k < nc; k += 32) acc = fmaf(__ldg(a + k), vs[k], acc);
+    const float4* a = reinterpret_cast<const float4*>(ainv + row * ld);
+    const int64_t n4 = ld / 4;
+    float acc0 = 0.0f, acc1 = 0.0f;
+#pragma unroll 4
+    for (int64_t k = lane; k < n4; k += 32) {
+        float4 m = __ldg(a + k), u = vs4[k];
+        acc0 = fmaf(m.x, u.x, acc0);
+        acc1 = fmaf(m.y, u.y, acc1);
+        acc0 = fmaf(m.z, u.z, acc0);
+        acc1 = fmaf(m.w, u.w, acc1);
+    }
+    float acc = acc0 + acc1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) y[row] = static_cast<double>(acc);
+    if (lane == 0) y[row] = acc;
 }
 
 // ------------------------------------------------------------------------------ set-up kernels
@@ -259,9 +285,13 @@ __global__ void k_gj_col(double* __restrict__ A, int64_t nc, int64_t k, const do
     }
 }
 
-__global__ void k_to_f32(const double* __restrict__ a, int64_t n, float* __restrict__ o)
+__global__ void k_to_f32(const double* __restrict__ a, int64_t nc, int64_t ld, float* __restrict__ o)
 {
-    GF_FOR(t, n) o[t] = static_cast<float>(a[t]);
+    GF_FOR(t, nc * ld)
+    {
+        int64_t i = t / ld, j = t - i * ld;
+        o[t] = j < nc ? static_cast<float>(a[i * nc + j]) : 0.0f;
+    }
 }
 
 inline int64_t ncoarse(const gfgpu_coarse_desc* g)
@@ -275,15 +305,18 @@ inline int64_t ncoarse(const gfgpu_coarse_desc* g)
 using namespace gfgpu;
 using namespace gfgpu::coarse;
 
-// z = P Ainv P^T r (+ minv * r): the correction inside the flexible CG (learned.cu)
+// z = P Ainv P^T r (+ minv * r): the correction inside the flexible CG (learned.cu); vc, yc hold
+// nc floats each
 int gfgpu_internal_coarse_apply(const gfgpu_coarse_desc* g, const int32_t* part, int64_t nnu,
                                 const double* minv, const double* r, double* vc, double* yc,
                                 double* z, cudaStream_t s)
 {
     const int64_t nc = ncoarse(g);
-    k_restrict<<<g->ncx * g->ncy, kRestrictThreads, 0, s>>>(*g, part, nnu, r, vc);
-    k_dense<<<grid_for(nc, kRowsPerBlock), 32 * kRowsPerBlock, nc * sizeof(float), s>>>(g->ainv, nc, vc, yc);
-    k_prolong<<<grid_for(int64_t(g->nx + 1) * (g->ny + 1)), kBlock, 0, s>>>(*g, part, nnu, yc, minv, r, z);
+    float* v = reinterpret_cast<float*>(vc);
+    float* y = reinterpret_cast<float*>(yc);
+    k_restrict<float><<<g->ncx * g->ncy, kRestrictThreads, 0, s>>>(*g, part, nnu, r, v);
+    k_dense<<<grid_for(nc, kRowsPerBlock), 32 * kRowsPerBlock, g->ld * sizeof(float), s>>>(g->ainv, nc, g->ld, v, y);
+    k_prolong<float><<<grid_for(int64_t(g->nx + 1) * (g->ny + 1)), kBlock, 0, s>>>(*g, part, nnu, y, minv, r, z);
     return check_launch("coarse correction");
 }
 
@@ -298,7 +331,7 @@ static int check_grid(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g)
     GF_REQUIRE(ncoarse(g) <= kMaxCoarseDofs, "coarse grid too large (more than 8192 coarse dofs)");
     gfgpu_coarse_desc e;
     gfgpu_coarse_grid(g->nx, g->ny, g->hc, &e);
-    GF_REQUIRE(g->rhx == e.rhx && g->rlx == e.rlx && g->rhy == e.rhy && g->rly == e.rly,
+    GF_REQUIRE(g->ld == e.ld && g->rhx == e.rhx && g->rlx == e.rlx && g->rhy == e.rhy && g->rly == e.rly,
                "reciprocal interval lengths do not match nx, ny, hc (use gfgpu_coarse_grid)");
     return GFGPU_OK;
 }
@@ -313,6 +346,7 @@ int gfgpu_coarse_grid(int32_t nx, int32_t ny, int32_t hc, gfgpu_coarse_desc* g)
     g->hc = hc;
     g->ncx = (nx + hc - 1) / hc + 1;
     g->ncy = (ny + hc - 1) / hc + 1;
+    g->ld = static_cast<int32_t>((int64_t(g->ncx) * g->ncy * 2 + 31) / 32 * 32);
     g->ainv = nullptr;
     g->rhx = g->rhy = 1.0 / hc;
     g->rlx = 1.0 / (nx - (g->ncx - 2) * hc);
@@ -354,11 +388,12 @@ int gfgpu_coarse_setup(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g, f
         for (int b = 0; b < 3; ++b)
             for (int a = 0; a < 3; ++a) {
                 k_probe<<<grid_for(nc), kBlock, 0, s>>>(*g, a, b, comp, e);
-                k_prolong<<<grid_for(d->nnode), kBlock, 0, s>>>(*g, d->part, d->nnu, e, nullptr, nullptr, p);
+                k_prolong<double><<<grid_for(d->nnode), kBlock, 0, s>>>(*g, d->part, d->nnu, e, nullptr, nullptr,
+                                                                        p);
                 GF_TRY(gfgpu_internal_element_forces(d, p, fe, s));
                 k_apply_gather<<<grid_for(n), kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part,
                                                               d->nnu, fe, n, q);
-                k_restrict<<<g->ncx * g->ncy, kRestrictThreads, 0, s>>>(*g, d->part, d->nnu, q, v);
+                k_restrict<double><<<g->ncx * g->ncy, kRestrictThreads, 0, s>>>(*g, d->part, d->nnu, q, v);
                 k_probe_scatter<<<grid_for(nc), kBlock, 0, s>>>(*g, a, b, comp, v, A);
             }
     k_symmetrize<<<grid_for(nc * nc), kBlock, 0, s>>>(A, nc);
@@ -374,7 +409,7 @@ int gfgpu_coarse_setup(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g, f
     GF_TRY(check_cuda(cudaMemcpyAsync(flag, piv, 16, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync"));
     GF_TRY(check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
     if (flag[1] != 0.0) return fail(GFGPU_ERR_NAN, "gfgpu_coarse_setup: singular coarse matrix");
-    k_to_f32<<<grid_for(nc * nc), kBlock, 0, s>>>(A, nc * nc, ainv);
+    k_to_f32<<<grid_for(nc * g->ld), kBlock, 0, s>>>(A, nc, g->ld, ainv);
     return check_launch("coarse inverse f32");
 }
 

@@ -406,21 +406,50 @@ __global__ void k_nn_wprep(const __nv_bfloat16* __restrict__ W, __nv_bfloat16* _
     WT[i] = ci < 32 ? W[(t * 32 + ci) * 32 + co] : __float2bfloat16_rn(0.0f);
 }
 
-// Y = relu(conv(X, W) + b) for 32 -> 32 channels, X and Y BF16 [H, W, 32], WT the prepared
-// weights. CTA: 256 threads, output tile 16 rows x 16 columns; warp w computes rows 2w, 2w+1
-// (one m16 tile of 16 pixels each) for the 4 n8 tiles of output channels, K = 9 taps x 32
-// input channels.
+// W [t][ci][co=2] (layer 4) -> WL [t][8][kPadC]: output channels padded to one n8 tile
+__global__ void k_nn_wprep_last(const __nv_bfloat16* __restrict__ W, __nv_bfloat16* __restrict__ WL)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 9 * 8 * kPadC) return;
+    int t = i / (8 * kPadC), co = (i / kPadC) % 8, ci = i % kPadC;
+    WL[i] = (ci < 32 && co < 2) ? W[(t * 32 + ci) * 2 + co] : __float2bfloat16_rn(0.0f);
+}
+
+// First layer as three k16 steps of 4 taps x 4 input channels (taps 9..11 zero):
+// W [t][ci=4][co] -> WF [kk][co][kPadF], k = 4 tl + ci for tap 4 kk + tl. Row padding 24 BF16
+// (48 B) keeps the 32-bit fragment loads of 8 rows x 4 pairs on distinct banks.
+constexpr int kPadF = 24;
+__global__ void k_nn_wprep_first(const __nv_bfloat16* __restrict__ W, __nv_bfloat16* __restrict__ WF)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * 32 * kPadF) return;
+    int kk = i / (32 * kPadF), co = (i / kPadF) % 32, k = i % kPadF;
+    int t = kk * 4 + k / 4, ci = k % 4;
+    WF[i] = (k < 16 && t < 9) ? W[(t * 4 + ci) * 32 + co] : __float2bfloat16_rn(0.0f);
+}
+
+// 3x3 convolution from BF16 [H, W, 32] on the tensor cores (mma.sync m16n8k16, FP32 accumulate),
+// NT n8 tiles of output channels. CTA: 256 threads, output tile 16 rows x 16 columns; warp w
+// computes rows 2w, 2w+1 (one m16 tile of 16 pixels each), K = 9 taps x 32 input channels.
+// LAST = false: Y = relu(conv + b), BF16 [H, W, 32] (NT = 4). LAST = true (NT = 1, the 32 -> 2
+// output layer): z = sigma (conv + b) on the free dofs, 0 on prescribed (FP64 nodevec; sigma =
+// RMS of the residual, sqrt(sc[rr_slot] / nfree)), or Yf [H, W, 2] FP32 when z is null.
+template <int NT, bool LAST>
 __global__ void __launch_bounds__(kMmaThreads)
-k_conv32_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ WT,
-             const float* __restrict__ bias, int dil, int H, int Wd, __nv_bfloat16* __restrict__ Y)
+k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ WT,
+           const float* __restrict__ bias, int dil, int H, int Wd, __nv_bfloat16* __restrict__ Y,
+           const double* __restrict__ sc, int rr_slot, double nfree, const int32_t* __restrict__ part,
+           int64_t nnu, double* __restrict__ z, float* __restrict__ Yf)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_sigma;
     const int hh = kTileY + 2 * dil, hw = kTileX + 2 * dil;
     __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(smem);          // [hh][hw][40]
-    __nv_bfloat16* ws = halo + hh * hw * kPadC;                             // [9][32][40]
+    __nv_bfloat16* ws = halo + hh * hw * kPadC;                             // [9][8 NT][40]
     const int y0 = blockIdx.y * kTileY, x0 = blockIdx.x * kTileX;
-    for (int i = threadIdx.x; i < 9 * 32 * kPadC / 8; i += blockDim.x)
+    for (int i = threadIdx.x; i < 9 * 8 * NT * kPadC / 8; i += blockDim.x)
         reinterpret_cast<uint4*>(ws)[i] = reinterpret_cast<const uint4*>(WT)[i];
+    if (LAST && threadIdx.x == 0) s_sigma = z ? sqrt(sc[rr_slot] / nfree) : 1.0;
     // halo: 16-byte chunks (8 channels)
     for (int i = threadIdx.x; i < hh * hw * 4; i += blockDim.x) {
         int pix = i >> 2, ch = (i & 3) * 8;
@@ -433,11 +462,11 @@ k_conv32_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restric
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gid = lane >> 2, tig = lane & 3;
-    float c[2][4][4];
+    float c[2][NT][4];
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
+        for (int nt = 0; nt < NT; ++nt)
 #pragma unroll
             for (int k = 0; k < 4; ++k) c[mt][nt][k] = 0.0f;
 #pragma unroll
@@ -445,10 +474,10 @@ k_conv32_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restric
         const int dy = dil * (t / 3 - 1), dx = dil * (t % 3 - 1);
 #pragma unroll
         for (int kc = 0; kc < 2; ++kc) {
-            uint32_t b[4][2];
+            uint32_t b[NT][2];
 #pragma unroll
-            for (int nt = 0; nt < 4; ++nt) {
-                const __nv_bfloat16* wp = ws + (t * 32 + nt * 8 + gid) * kPadC + kc * 16 + tig * 2;
+            for (int nt = 0; nt < NT; ++nt) {
+                const __nv_bfloat16* wp = ws + (t * 8 * NT + nt * 8 + gid) * kPadC + kc * 16 + tig * 2;
                 b[nt][0] = *reinterpret_cast<const uint32_t*>(wp);
                 b[nt][1] = *reinterpret_cast<const uint32_t*>(wp + 8);
             }
@@ -462,8 +491,129 @@ k_conv32_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restric
                 uint32_t a2 = *reinterpret_cast<const uint32_t*>(ap0 + 8);
                 uint32_t a3 = *reinterpret_cast<const uint32_t*>(ap1 + 8);
 #pragma unroll
-                for (int nt = 0; nt < 4; ++nt) mma_bf16(c[mt][nt], a0, a1, a2, a3, b[nt][0], b[nt][1]);
+                for (int nt = 0; nt < NT; ++nt) mma_bf16(c[mt][nt], a0, a1, a2, a3, b[nt][0], b[nt][1]);
             }
+        }
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+        const int yy = y0 + 2 * warp + mt;
+        if (yy >= H) continue;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int xx = x0 + gid + 8 * half;
+            if (xx >= Wd) continue;
+            const int64_t p = static_cast<int64_t>(yy) * Wd + xx;
+            if constexpr (LAST) {
+                if (tig != 0) continue; // output channels 0, 1 live in the lanes with tig = 0
+                const float v0 = c[mt][0][2 * half + 0] + bias[0];
+                const float v1 = c[mt][0][2 * half + 1] + bias[1];
+                if (z) {
+                    const double sg = s_sigma;
+                    z[2 * p] = part[2 * p] < nnu ? sg * static_cast<double>(v0) : 0.0;
+                    z[2 * p + 1] = part[2 * p + 1] < nnu ? sg * static_cast<double>(v1) : 0.0;
+                }
+                else {
+                    *reinterpret_cast<float2*>(Yf + 2 * p) = make_float2(v0, v1);
+                }
+            }
+            else {
+                __nv_bfloat16* yp = Y + p * 32;
+#pragma unroll
+                for (int nt = 0; nt < NT; ++nt) {
+                    const int co = nt * 8 + tig * 2;
+                    float v0 = fmaxf(c[mt][nt][2 * half + 0] + bias[co], 0.0f);
+                    float v1 = fmaxf(c[mt][nt][2 * half + 1] + bias[co + 1], 0.0f);
+                    *reinterpret_cast<__nv_bfloat162*>(yp + co) = __floats2bfloat162_rn(v0, v1);
+                }
+            }
+        }
+    }
+}
+
+// First layer (4 -> 32, dilation 1, ReLU) on the tensor cores: the input channels (the FP64
+// residual scaled by 1 / sigma and the two material channels, or X0 [H, W, 4]) are rounded to
+// BF16 into a shared halo tile [18][18][4]; K = 3 steps of 4 taps x 4 channels. Output BF16
+// [H, W, 32]. Same tile and warp layout as k_conv_mma.
+__global__ void __launch_bounds__(kMmaThreads)
+k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_slot, double nfree,
+            const float* __restrict__ mat, const float* __restrict__ X0,
+            const __nv_bfloat16* __restrict__ WF, const float* __restrict__ bias, int H, int Wd,
+            __nv_bfloat16* __restrict__ Y)
+{
+    constexpr int hh = kTileY + 2, hw = kTileX + 2;
+    __shared__ __align__(16) __nv_bfloat16 halo[hh * hw * 4];
+    __shared__ __align__(16) __nv_bfloat16 wf[3 * 32 * kPadF];
+    __shared__ float s_inv;
+    const int y0 = blockIdx.y * kTileY, x0 = blockIdx.x * kTileX;
+    for (int i = threadIdx.x; i < 3 * 32 * kPadF / 8; i += blockDim.x)
+        reinterpret_cast<uint4*>(wf)[i] = reinterpret_cast<const uint4*>(WF)[i];
+    if (threadIdx.x == 0) {
+        double sigma = r ? sqrt(sc[rr_slot] / nfree) : 1.0;
+        s_inv = sigma > 0.0 ? static_cast<float>(1.0 / sigma) : 0.0f;
+    }
+    __syncthreads();
+    const float inv = s_inv;
+    for (int pix = threadIdx.x; pix < hh * hw; pix += blockDim.x) {
+        int yy = y0 - 1 + pix / hw, xx = x0 - 1 + pix % hw;
+        float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (yy >= 0 && yy < H && xx >= 0 && xx < Wd) {
+            int64_t q = static_cast<int64_t>(yy) * Wd + xx;
+            if (r) {
+                double2 rv = *reinterpret_cast<const double2*>(r + 2 * q);
+                float2 mv = *reinterpret_cast<const float2*>(mat + 2 * q);
+                v[0] = static_cast<float>(rv.x) * inv;
+                v[1] = static_cast<float>(rv.y) * inv;
+                v[2] = mv.x;
+                v[3] = mv.y;
+            }
+            else {
+                float4 xv = *reinterpret_cast<const float4*>(X0 + 4 * q);
+                v[0] = xv.x;
+                v[1] = xv.y;
+                v[2] = xv.z;
+                v[3] = xv.w;
+            }
+        }
+        __nv_bfloat162 h[2] = {__floats2bfloat162_rn(v[0], v[1]), __floats2bfloat162_rn(v[2], v[3])};
+        *reinterpret_cast<uint2*>(halo + pix * 4) = *reinterpret_cast<uint2*>(h);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gid = lane >> 2, tig = lane & 3;
+    const int ch = (tig & 1) * 2;
+    float c[2][4][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) c[mt][nt][k] = 0.0f;
+#pragma unroll
+    for (int kk = 0; kk < 3; ++kk) {
+        uint32_t b[4][2];
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            const __nv_bfloat16* wp = wf + (kk * 32 + nt * 8 + gid) * kPadF + tig * 2;
+            b[nt][0] = *reinterpret_cast<const uint32_t*>(wp);
+            b[nt][1] = *reinterpret_cast<const uint32_t*>(wp + 8);
+        }
+        // taps of the fragment's k pairs: k = tig * 2 (tap 4 kk + tig / 2) and k + 8 (2 taps on);
+        // taps past 8 have zero weights and read the tile centre
+        const int ta = kk * 4 + (tig >> 1), tb = ta + 2;
+        const int dya = ta < 9 ? ta / 3 - 1 : 0, dxa = ta < 9 ? ta % 3 - 1 : 0;
+        const int dyb = tb < 9 ? tb / 3 - 1 : 0, dxb = tb < 9 ? tb % 3 - 1 : 0;
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            const int hr = 2 * warp + mt + 1;
+            const __nv_bfloat16* pa = halo + ((hr + dya) * hw + gid + 1 + dxa) * 4 + ch;
+            const __nv_bfloat16* pb = halo + ((hr + dyb) * hw + gid + 1 + dxb) * 4 + ch;
+            uint32_t a0 = *reinterpret_cast<const uint32_t*>(pa);
+            uint32_t a1 = *reinterpret_cast<const uint32_t*>(pa + 8 * 4);
+            uint32_t a2 = *reinterpret_cast<const uint32_t*>(pb);
+            uint32_t a3 = *reinterpret_cast<const uint32_t*>(pb + 8 * 4);
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) mma_bf16(c[mt][nt], a0, a1, a2, a3, b[nt][0], b[nt][1]);
         }
     }
 #pragma unroll
@@ -486,128 +636,12 @@ k_conv32_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restric
     }
 }
 
-inline size_t mma_smem_bytes(int dil)
+inline size_t mma_smem_bytes(int dil, int nt = 4)
 {
-    return static_cast<size_t>((kTileY + 2 * dil) * (kTileX + 2 * dil) + 9 * 32) * kPadC * 2;
+    return static_cast<size_t>((kTileY + 2 * dil) * (kTileX + 2 * dil) + 9 * 8 * nt) * kPadC * 2;
 }
 
 // ------------------------------------------------------------------ preconditioner glue (FP64)
-
-// First layer (4 -> 32, dilation 1, ReLU) on the CUDA cores, BF16 output [H, W, 32]. Input
-// channels per node: with r != null the FP64 residual scaled by 1 / sigma, sigma = RMS of r over
-// the free dofs (sqrt(sc[rr_slot] / nfree)), and the two material channels; else X0 [H, W, 4].
-__global__ void __launch_bounds__(256)
-k_nn_first(const double* __restrict__ r, const double* __restrict__ sc, int rr_slot, double nfree,
-           const float* __restrict__ mat, const float* __restrict__ X0,
-           const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias, int H, int Wd,
-           __nv_bfloat16* __restrict__ Y)
-{
-    __shared__ float Ws[9 * 4 * 32];
-    __shared__ float bs[32];
-    __shared__ float s_inv;
-    for (int i = threadIdx.x; i < 9 * 4 * 32; i += blockDim.x) Ws[i] = __bfloat162float(W[i]);
-    if (threadIdx.x < 32) bs[threadIdx.x] = bias[threadIdx.x];
-    if (threadIdx.x == 0 && r) {
-        double sigma = sqrt(sc[rr_slot] / nfree);
-        s_inv = sigma > 0.0 ? static_cast<float>(1.0 / sigma) : 0.0f;
-    }
-    __syncthreads();
-    const float inv = r ? s_inv : 1.0f;
-    const int64_t hw = static_cast<int64_t>(H) * Wd;
-    GF_FOR(p, hw)
-    {
-        int y = static_cast<int>(p / Wd), x = static_cast<int>(p % Wd);
-        float acc[32];
-#pragma unroll
-        for (int c = 0; c < 32; ++c) acc[c] = bs[c];
-#pragma unroll 1
-        for (int t = 0; t < 9; ++t) {
-            int yy = y + (t / 3 - 1), xx = x + (t % 3 - 1);
-            if (yy < 0 || yy >= H || xx < 0 || xx >= Wd) continue;
-            int64_t q = static_cast<int64_t>(yy) * Wd + xx;
-            float v[4];
-            if (r) {
-                double2 rv = *reinterpret_cast<const double2*>(r + 2 * q);
-                float2 mv = *reinterpret_cast<const float2*>(mat + 2 * q);
-                v[0] = static_cast<float>(rv.x) * inv;
-                v[1] = static_cast<float>(rv.y) * inv;
-                v[2] = mv.x;
-                v[3] = mv.y;
-            }
-            else {
-                float4 xv = *reinterpret_cast<const float4*>(X0 + 4 * q);
-                v[0] = xv.x;
-                v[1] = xv.y;
-                v[2] = xv.z;
-                v[3] = xv.w;
-            }
-#pragma unroll
-            for (int ci = 0; ci < 4; ++ci)
-#pragma unroll
-                for (int c = 0; c < 32; ++c) acc[c] = fmaf(v[ci], Ws[(t * 4 + ci) * 32 + c], acc[c]);
-        }
-        uint4* yp = reinterpret_cast<uint4*>(Y + p * 32);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            __nv_bfloat162 h[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                h[j] = __floats2bfloat162_rn(fmaxf(acc[k * 8 + 2 * j], 0.0f), fmaxf(acc[k * 8 + 2 * j + 1], 0.0f));
-            yp[k] = *reinterpret_cast<uint4*>(h);
-        }
-    }
-}
-
-// Last layer (32 -> 2, dilation 1, no activation) on the CUDA cores from BF16 [H, W, 32]. With
-// z != null: z = sigma * y on the free dofs and 0 on the prescribed ones (FP64 nodevec);
-// else Y [H, W, 2] in FP32.
-__global__ void __launch_bounds__(256)
-k_nn_last(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ W,
-          const float* __restrict__ bias, int H, int Wd, const double* __restrict__ sc, int rr_slot,
-          double nfree, const int32_t* __restrict__ part, int64_t nnu, double* __restrict__ z,
-          float* __restrict__ Y)
-{
-    __shared__ float Ws[9 * 32 * 2];
-    __shared__ double s_sigma;
-    for (int i = threadIdx.x; i < 9 * 32 * 2; i += blockDim.x) Ws[i] = __bfloat162float(W[i]);
-    if (threadIdx.x == 0 && z) s_sigma = sqrt(sc[rr_slot] / nfree);
-    __syncthreads();
-    const float b0 = bias[0], b1 = bias[1];
-    const int64_t hw = static_cast<int64_t>(H) * Wd;
-    GF_FOR(p, hw)
-    {
-        int y = static_cast<int>(p / Wd), x = static_cast<int>(p % Wd);
-        float a0 = b0, a1 = b1;
-#pragma unroll 1
-        for (int t = 0; t < 9; ++t) {
-            int yy = y + (t / 3 - 1), xx = x + (t % 3 - 1);
-            if (yy < 0 || yy >= H || xx < 0 || xx >= Wd) continue;
-            const uint4* xp = reinterpret_cast<const uint4*>(X + (static_cast<int64_t>(yy) * Wd + xx) * 32);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                uint4 u = xp[k];
-                const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    float2 f = __bfloat1622float2(h[j]);
-                    int ci = k * 8 + 2 * j;
-                    a0 = fmaf(f.x, Ws[(t * 32 + ci) * 2 + 0], a0);
-                    a1 = fmaf(f.x, Ws[(t * 32 + ci) * 2 + 1], a1);
-                    a0 = fmaf(f.y, Ws[(t * 32 + ci + 1) * 2 + 0], a0);
-                    a1 = fmaf(f.y, Ws[(t * 32 + ci + 1) * 2 + 1], a1);
-                }
-            }
-        }
-        if (z) {
-            double sg = s_sigma;
-            z[2 * p] = part[2 * p] < nnu ? sg * static_cast<double>(a0) : 0.0;
-            z[2 * p + 1] = part[2 * p + 1] < nnu ? sg * static_cast<double>(a1) : 0.0;
-        }
-        else {
-            *reinterpret_cast<float2*>(Y + 2 * p) = make_float2(a0, a1);
-        }
-    }
-}
 
 } // namespace nn
 } // namespace gfgpu
@@ -771,7 +805,7 @@ struct SlotList {
 };
 // device scalars: r.r, b.b, step length per new direction, P.Q per slot, orthogonalisation
 // coefficient per basis entry
-enum { F_RR = 0, F_BB, F_A0, F_A1, F_PQ, F_C = F_PQ + kMaxSlots, F_COUNT = F_C + kMaxSlots };
+enum { F_RR = 0, F_BB, F_A0, F_A1, F_PQ, F_C = F_PQ + kMaxSlots, F_R1 = F_C + kMaxSlots, F_COUNT };
 
 __device__ __forceinline__ double bsum(double v, double* sh)
 {
@@ -852,6 +886,25 @@ k_fgather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr, con
         partial[blockIdx.x] = s1;
         partial[kRed + blockIdx.x] = s2;
     }
+}
+
+// r1 = r - alpha_0 q0 (the residual after the step along the first direction of the iteration);
+// partial r1.r1
+__global__ void __launch_bounds__(256)
+k_resid1(const double* __restrict__ r, const double* __restrict__ q0, const double* __restrict__ sc,
+         int64_t n, double* __restrict__ r1, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    const double a0 = sc[F_A0];
+    double rr = 0.0;
+    GF_FOR(t, n)
+    {
+        double v = fma(-a0, q0[t], r[t]);
+        r1[t] = v;
+        rr = fma(v, v, rr);
+    }
+    double s = bsum(rr, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
 // sc[dst.s[k]] = sum of partial row k (fixed order)
@@ -1072,30 +1125,33 @@ struct McombineL {
 struct FcgWs {
     double *fe, *r, *z, *minv, *P, *Q, *partial, *sc;
     int64_t ld;
-    __nv_bfloat16 *a1, *a2, *a3, *wt1, *wt2;
+    __nv_bfloat16 *a1, *a2, *a3, *wt1, *wt2, *wt0, *wt3;
 };
 
 constexpr int64_t kWtBytes = 9 * 32 * kPadC * 2; // prepared weights of one tensor-core layer
 
-// network buffers: three activations [hw][32] BF16 and the two prepared weight sets
+// network buffers: three activations [hw][32] BF16 and the four prepared weight sets (layers
+// 2, 3 in kWtBytes each; the first and last layer's smaller sets in the same room)
 inline char* carve_nn(char* c, int64_t hw, __nv_bfloat16** a1, __nv_bfloat16** a2,
-                      __nv_bfloat16** a3, __nv_bfloat16** wt1, __nv_bfloat16** wt2)
+                      __nv_bfloat16** a3, __nv_bfloat16** wt1, __nv_bfloat16** wt2,
+                      __nv_bfloat16** wt0, __nv_bfloat16** wt3)
 {
     __nv_bfloat16** a[] = {a1, a2, a3};
     for (auto b : a) {
         *b = reinterpret_cast<__nv_bfloat16*>(c);
         c += a256(hw * 32 * 2);
     }
-    *wt1 = reinterpret_cast<__nv_bfloat16*>(c);
-    c += a256(kWtBytes);
-    *wt2 = reinterpret_cast<__nv_bfloat16*>(c);
-    c += a256(kWtBytes);
+    __nv_bfloat16** wts[] = {wt1, wt2, wt0, wt3};
+    for (auto b : wts) {
+        *b = reinterpret_cast<__nv_bfloat16*>(c);
+        c += a256(kWtBytes);
+    }
     return c;
 }
 
 inline int64_t nn_bytes(int64_t hw)
 {
-    return 3 * a256(hw * 32 * 2) + 2 * a256(kWtBytes);
+    return 3 * a256(hw * 32 * 2) + 4 * a256(kWtBytes);
 }
 
 inline FcgWs carve_fcg(const gfgpu_verlet_desc* d, int64_t hw, int nslots, void* ws)
@@ -1119,7 +1175,7 @@ inline FcgWs carve_fcg(const gfgpu_verlet_desc* d, int64_t hw, int nslots, void*
     c += a256(int64_t(kMaxSlots) * kRed * 8);
     w.sc = reinterpret_cast<double*>(c);
     c += a256(F_COUNT * 8);
-    carve_nn(c, hw, &w.a1, &w.a2, &w.a3, &w.wt1, &w.wt2);
+    carve_nn(c, hw, &w.a1, &w.a2, &w.a3, &w.wt1, &w.wt2, &w.wt0, &w.wt3);
     return w;
 }
 
@@ -1130,13 +1186,15 @@ inline int64_t fcg_bytes(const gfgpu_verlet_desc* d, int64_t hw, int nslots)
            a256(int64_t(kMaxSlots) * kRed * 8) + a256(F_COUNT * 8) + nn_bytes(hw);
 }
 
-// the tensor-core layers' weights in their shared-memory layout
+// the tensor-core layers' weights in their shared-memory layouts
 inline void nn_prepare_weights(const gfgpu_nn_desc* nn, __nv_bfloat16* wt1, __nv_bfloat16* wt2,
-                               cudaStream_t s)
+                               __nv_bfloat16* wt0, __nv_bfloat16* wt3, cudaStream_t s)
 {
     const unsigned g = (9 * 32 * kPadC + 255) / 256;
     k_nn_wprep<<<g, 256, 0, s>>>(wb(nn->weights_bf16, 1), wt1);
     k_nn_wprep<<<g, 256, 0, s>>>(wb(nn->weights_bf16, 2), wt2);
+    k_nn_wprep_first<<<(3 * 32 * kPadF + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 0), wt0);
+    k_nn_wprep_last<<<(9 * 8 * kPadC + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 3), wt3);
 }
 
 // the four layers on one H x W grid: input from the FP64 residual (r != null) or from X0,
@@ -1144,21 +1202,22 @@ inline void nn_prepare_weights(const gfgpu_nn_desc* nn, __nv_bfloat16* wt1, __nv
 inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0, const double* sc,
                       int rr_slot, double nfree, const int32_t* part, int64_t nnu,
                       __nv_bfloat16* a1, __nv_bfloat16* a2, __nv_bfloat16* a3,
-                      const __nv_bfloat16* wt1, const __nv_bfloat16* wt2, double* z, float* Y,
-                      cudaStream_t s)
+                      const __nv_bfloat16* wt1, const __nv_bfloat16* wt2, const __nv_bfloat16* wt0,
+                      const __nv_bfloat16* wt3, double* z, float* Y, cudaStream_t s)
 {
     const int H = nn->H, W = nn->W;
-    const int64_t hw = int64_t(H) * W;
-    const unsigned g = grid_for(hw);
-    k_nn_first<<<g, 256, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wb(nn->weights_bf16, 0),
-                                 nn->params_f32 + b_off(0), H, W, a1);
     dim3 grid((W + kTileX - 1) / kTileX, (H + kTileY - 1) / kTileY);
-    k_conv32_mma<<<grid, kMmaThreads, mma_smem_bytes(dil_of(1)), s>>>(
-        a1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
-    k_conv32_mma<<<grid, kMmaThreads, mma_smem_bytes(dil_of(2)), s>>>(
-        a2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
-    k_nn_last<<<g, 256, 0, s>>>(a3, wb(nn->weights_bf16, 3), nn->params_f32 + b_off(3), H, W, sc,
-                                rr_slot, nfree, part, nnu, z, Y);
+    k_first_mma<<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
+                                             nn->params_f32 + b_off(0), H, W, a1);
+    k_conv_mma<4, false><<<grid, kMmaThreads, mma_smem_bytes(dil_of(1)), s>>>(
+        a1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2, nullptr, 0, 0.0, nullptr, 0, nullptr,
+        nullptr);
+    k_conv_mma<4, false><<<grid, kMmaThreads, mma_smem_bytes(dil_of(2)), s>>>(
+        a2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3, nullptr, 0, 0.0, nullptr, 0, nullptr,
+        nullptr);
+    k_conv_mma<1, true><<<grid, kMmaThreads, mma_smem_bytes(dil_of(3), 1), s>>>(
+        a3, wt3, nn->params_f32 + b_off(3), dil_of(3), H, W, nullptr, sc, rr_slot, nfree, part, nnu, z,
+        Y);
     return check_launch("nn_forward");
 }
 
@@ -1167,15 +1226,18 @@ inline int nn_apply(const gfgpu_nn_desc* nn, const double* r, const double* sc, 
                     double nfree, const int32_t* part, int64_t nnu, FcgWs& w, double* z, cudaStream_t s)
 {
     return nn_forward(nn, r, nullptr, sc, rr_slot, nfree, part, nnu, w.a1, w.a2, w.a3, w.wt1, w.wt2,
-                      z, nullptr, s);
+                      w.wt0, w.wt3, z, nullptr, s);
 }
 
 inline int prepare_mma(cudaStream_t)
 {
     static bool done = false;
     if (done) return GFGPU_OK;
-    GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_mma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv_mma<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(mma_smem_bytes(4))),
+                      "cudaFuncSetAttribute"));
+    GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv_mma<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(mma_smem_bytes(4, 1))),
                       "cudaFuncSetAttribute"));
     done = true;
     return GFGPU_OK;
@@ -1309,10 +1371,11 @@ int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* wor
                "X0 must be 16-byte, Y 8-byte and the workspace 256-byte aligned");
     GF_TRY(prepare_mma(S(stream)));
     cudaStream_t s = S(stream);
-    __nv_bfloat16 *a1, *a2, *a3, *wt1, *wt2;
-    carve_nn(static_cast<char*>(workspace), int64_t(nn->H) * nn->W, &a1, &a2, &a3, &wt1, &wt2);
-    nn_prepare_weights(nn, wt1, wt2, s);
-    return nn_forward(nn, nullptr, X0, nullptr, 0, 1.0, nullptr, 0, a1, a2, a3, wt1, wt2, nullptr, Y, s);
+    __nv_bfloat16 *a1, *a2, *a3, *wt1, *wt2, *wt0, *wt3;
+    carve_nn(static_cast<char*>(workspace), int64_t(nn->H) * nn->W, &a1, &a2, &a3, &wt1, &wt2, &wt0, &wt3);
+    nn_prepare_weights(nn, wt1, wt2, wt0, wt3, s);
+    return nn_forward(nn, nullptr, X0, nullptr, 0, 1.0, nullptr, 0, a1, a2, a3, wt1, wt2, wt0, wt3,
+                      nullptr, Y, s);
 }
 
 } // extern "C"
@@ -1320,7 +1383,8 @@ int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* wor
 // the flexible CG of gfgpu_fcg_solve; with g != NULL the first direction of every iteration is
 // the two-level correction D^-1 r + P ainv P^T r (buffers after the ring workspace)
 static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
-                    const gfgpu_coarse_desc* g, const double* rhs, double* x, double tol, int64_t maxiter,
+                    const gfgpu_coarse_desc* g, bool post, const double* rhs, double* x, double tol,
+                    int64_t maxiter,
                     int32_t nkeep, int32_t check_every, void* workspace, gfgpu_stream_t stream,
                     int64_t* iters, double* relres)
 {
@@ -1376,7 +1440,16 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
                 GF_TRY(gfgpu_internal_coarse_apply(g, d->part, d->nnu, w.minv, w.r, vc, yc, zc, st));
                 zin = zc;
             }
-            if (dd == 1) {
+            if (dd == 1 && post) {
+                // the network sees the residual left after the step along the two-level direction
+                // (zc is free again: its direction is stored in slot c0 % nslots)
+                const double* q0 = w.Q + static_cast<int>(c0 % nslots) * w.ld;
+                k_resid1<<<gb, 256, 0, st>>>(w.r, q0, w.sc, n, zc, w.partial);
+                k_fredv<<<1, 1024, 0, st>>>(w.partial, one(F_R1), w.sc);
+                GF_TRY(nn_apply(nn, zc, w.sc, F_R1, nfree, d->part, d->nnu, w, w.z, st));
+                zin = w.z;
+            }
+            else if (dd == 1) {
                 GF_TRY(nn_apply(nn, w.r, w.sc, F_RR, nfree, d->part, d->nnu, w, w.z, st));
                 zin = w.z;
             }
@@ -1399,7 +1472,7 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
         return check_launch("fcg iteration");
     };
 
-    if (nn) nn_prepare_weights(nn, w.wt1, w.wt2, s);
+    if (nn) nn_prepare_weights(nn, w.wt1, w.wt2, w.wt0, w.wt3, s);
     k_finv<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, diag, n, w.minv);
     // ||b||, b = -(A x_p)_u (P slot 0 as scratch)
     k_fkeep<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.P);
@@ -1497,8 +1570,8 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
                     double* x, double tol, int64_t maxiter, int32_t nkeep, int32_t check_every,
                     void* workspace, gfgpu_stream_t stream, int64_t* iters, double* relres)
 {
-    return fcg_core(d, diag, nn, nullptr, nullptr, x, tol, maxiter, nkeep, check_every, workspace,
-                    stream, iters, relres);
+    return fcg_core(d, diag, nn, nullptr, false, nullptr, x, tol, maxiter, nkeep, check_every,
+                    workspace, stream, iters, relres);
 }
 
 int64_t gfgpu_fcg_coarse_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W,
@@ -1511,18 +1584,18 @@ int64_t gfgpu_fcg_coarse_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, 
 }
 
 int gfgpu_fcg_solve_coarse(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
-                           const gfgpu_coarse_desc* g, const double* rhs, double* x, double tol,
-                           int64_t maxiter,
+                           const gfgpu_coarse_desc* g, int32_t post, const double* rhs, double* x,
+                           double tol, int64_t maxiter,
                            int32_t nkeep, int32_t check_every, void* workspace,
                            gfgpu_stream_t stream, int64_t* iters, double* relres)
 {
     GF_REQUIRE(g && g->ainv && d && d->nne == 4 && d->ndim == 2 &&
                    int64_t(g->nx + 1) * (g->ny + 1) == d->nnode &&
                    g->ncx == (g->nx + g->hc - 1) / g->hc + 1 && g->ncy == (g->ny + g->hc - 1) / g->hc + 1 &&
-                   int64_t(g->ncx) * g->ncy * 2 <= 8192,
+                   int64_t(g->ncx) * g->ncy * 2 <= 8192 && g->ld % 32 == 0 && g->ld >= 2 * g->ncx * g->ncy,
                "bad coarse grid");
-    return fcg_core(d, diag, nn, g, rhs, x, tol, maxiter, nkeep, check_every, workspace, stream,
-                    iters, relres);
+    return fcg_core(d, diag, nn, g, post != 0, rhs, x, tol, maxiter, nkeep, check_every, workspace,
+                    stream, iters, relres);
 }
 
 } // extern "C"

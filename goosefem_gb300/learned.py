@@ -40,7 +40,8 @@ class CoarseDesc(C.Structure):
     """Mirror of gfgpu_coarse_desc (include/gfgpu.h)."""
 
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("hc", C.c_int32), ("ncx", C.c_int32),
-                ("ncy", C.c_int32), ("ainv", C.c_void_p), ("rhx", C.c_double), ("rlx", C.c_double),
+                ("ncy", C.c_int32), ("ld", C.c_int32), ("ainv", C.c_void_p), ("rhx", C.c_double),
+                ("rlx", C.c_double),
                 ("rhy", C.c_double), ("rly", C.c_double)]
 
 
@@ -256,7 +257,7 @@ class LearnedPreconditioner:
         return x
 
     def make_pairs_twolevel(self, nloads=64, snaps=48, every=4, seed=1, nkeep=4, target="cheb",
-                            degree=8):
+                            degree=8, post=False):
         """(residual, correction) pairs for the network as the fine-level part of the two-level
         preconditioner (coarse_setup first). For each random load the exact solution x* comes
         from the two-level solve to 1e-11; the snapshots x_k are the iterates of the same solver
@@ -264,7 +265,9 @@ class LearnedPreconditioner:
         what `degree` Chebyshev steps add beyond the Jacobi step, chebyshev(r_k) - D^-1 r_k (a
         linear map of the network's receptive field), or, with target="error", what the
         two-level direction misses of the exact error, (x* - x_k) - P A_c^-1 P^T r_k - D^-1 r_k;
-        both are divided by the RMS of r_k over the free dofs."""
+        both are divided by the RMS of r_k over the free dofs. post=True takes as r_k the
+        residual left after the line search along the two-level direction (the network's input
+        in the solve with post=True; target "cheb" only)."""
         if self.coarse is None:
             raise RuntimeError("coarse_setup first")
         npairs = nloads * snaps
@@ -289,6 +292,10 @@ class LearnedPreconditioner:
             xk = x.clone()
             for snap in range(snaps):
                 r = self._residual(xk, b)
+                if post:  # the residual after the exact line search along the two-level direction
+                    d1 = self.coarse_apply(r) + self.minv * r
+                    q1 = self._apply_free(d1)
+                    r = r - ((r * d1).sum() / (d1 * q1).sum()) * q1
                 sigma = torch.sqrt((r[self.free] ** 2).sum() / self.nfree)
                 if target == "cheb":
                     t = self.chebyshev(r, degree) - self.minv * r
@@ -360,7 +367,7 @@ class LearnedPreconditioner:
         _lib.call("gfgpu_coarse_grid", self.nx, self.ny, int(hc), C.addressof(g))
         nc = g.ncx * g.ncy * 2
         dev = _dev.device()
-        self.ainv = torch.empty((nc, nc), dtype=torch.float32, device=dev)
+        self.ainv = torch.empty((nc, g.ld), dtype=torch.float32, device=dev)
         ac = torch.empty((nc, nc), dtype=torch.float64, device=dev)
         nb = int(_lib.lib().gfgpu_coarse_setup_workspace_bytes(self._desc(), C.addressof(g)))
         ws = torch.empty(nb // 8 + 1, dtype=torch.float64, device=dev)
@@ -382,12 +389,13 @@ class LearnedPreconditioner:
         return z
 
     def fcg(self, x, tol=1e-8, use_nn=True, maxiter=200000, nkeep=8, check_every=16,
-            coarse=False, rhs=None):
+            coarse=False, rhs=None, post=False):
         """Flexible CG (gfgpu_fcg_solve) in place on x (prescribed values + initial guess): with
         the network, two directions per iteration (D^-1 r and the network's correction); without,
         Jacobi only. coarse=True adds the two-level correction to the first direction
-        (gfgpu_fcg_solve_coarse; coarse_setup first), which also takes an external load `rhs`.
-        Returns (iterations, relative true residual)."""
+        (gfgpu_fcg_solve_coarse; coarse_setup first), which also takes an external load `rhs`;
+        post=True applies the network to the residual left after the two-level step. Returns
+        (iterations, relative true residual)."""
         ndir = 2 if use_nn else 1
         if coarse:
             nb = int(_lib.lib().gfgpu_fcg_coarse_workspace_bytes(
@@ -402,7 +410,8 @@ class LearnedPreconditioner:
         nnd = C.addressof(self.nn_desc()) if use_nn else None
         if coarse:
             _lib.call("gfgpu_fcg_solve_coarse", self._desc(), self.static.diag.data_ptr(), nnd,
-                      C.addressof(self.coarse), None if rhs is None else rhs.data_ptr(),
+                      C.addressof(self.coarse), int(bool(post)),
+                      None if rhs is None else rhs.data_ptr(),
                       x.data_ptr(), float(tol), int(maxiter), int(nkeep),
                       int(check_every), ws.data_ptr(), _dev.stream(), C.addressof(it),
                       C.addressof(rel))

@@ -616,14 +616,15 @@ int gfgpu_fcg_solve(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
 /* Coarse space of a Regular Quad4 grid of nx x ny elements (node iy (nx + 1) + ix): bilinear
  * hats on every hc-th node along each axis (the last interval may be shorter), ncx x ncy coarse
  * nodes, two dofs each (coarse dof (jy ncx + jx) 2 + c), restricted to the free fine dofs.
- * `ainv` is the dense FP32 inverse of the Galerkin matrix P^T A_uu P, [nc, nc], nc = 2 ncx ncy
- * (at most 8192), filled by gfgpu_coarse_setup. */
+ * `ainv` is the dense FP32 inverse of the Galerkin matrix P^T A_uu P, [nc, ld] (zero padded),
+ * nc = 2 ncx ncy (at most 8192), filled by gfgpu_coarse_setup. */
 typedef struct {
     int32_t nx, ny, hc, ncx, ncy;
+    int32_t ld; /* row stride of ainv: nc rounded up to a multiple of 32 */
     const float* ainv;
     double rhx, rlx, rhy, rly; /* 1 / hc and 1 / (length of the last interval), along x and y */
 } gfgpu_coarse_desc;
-/* Fills nx, ny, hc, the coarse node counts and the reciprocal interval lengths; ainv = NULL. */
+/* Fills nx, ny, hc, the coarse node counts, ld and the reciprocal interval lengths; ainv = NULL. */
 int gfgpu_coarse_grid(int32_t nx, int32_t ny, int32_t hc, gfgpu_coarse_desc* g);
 int64_t gfgpu_coarse_setup_workspace_bytes(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g);
 /* Measures A_c = P^T A_uu P with the matrix-free operator of `d` (18 coloured probes), writes it
@@ -635,16 +636,18 @@ int gfgpu_coarse_setup(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g, f
  * 256-byte-rounded nc doubles. */
 int gfgpu_coarse_apply(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g, const double* r,
                        double* z, void* workspace, gfgpu_stream_t stream);
-/* gfgpu_fcg_solve with the two-level first direction D^-1 r + P ainv P^T r (the network
- * direction, when `nn` is given, unchanged) and an optional external load `rhs` [nnode * 2]
- * (b = rhs_u - (A x_p)_u; NULL: no load). Workspace: gfgpu_fcg_coarse_workspace_bytes. */
+/* gfgpu_fcg_solve with the two-level first direction D^-1 r + P ainv P^T r and an optional
+ * external load `rhs` [nnode * 2] (b = rhs_u - (A x_p)_u; NULL: no load). With `nn`, the second
+ * direction is the network's correction of r (post = 0) or of the residual left after the step
+ * along the first direction, r - alpha_0 A p_0 (post = 1: the network as a post-smoother of the
+ * two-level step; no extra operator application). Workspace: gfgpu_fcg_coarse_workspace_bytes. */
 int64_t gfgpu_fcg_coarse_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t W,
                                          int32_t nkeep, int32_t ndir, const gfgpu_coarse_desc* g);
 int gfgpu_fcg_solve_coarse(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_nn_desc* nn,
-                           const gfgpu_coarse_desc* g, const double* rhs, double* x, double tol,
-                           int64_t maxiter,
-                           int32_t nkeep, int32_t check_every, void* workspace,
-                           gfgpu_stream_t stream, int64_t* iters, double* relres);
+                           const gfgpu_coarse_desc* g, int32_t post, const double* rhs, double* x,
+                           double tol, int64_t maxiter, int32_t nkeep,
+                           int32_t check_every, void* workspace, gfgpu_stream_t stream,
+                           int64_t* iters, double* relres);
 
 /* ============================ probes ====================================================== */
 
