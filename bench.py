@@ -49,11 +49,13 @@ def parse():
     p.add_argument("--workload", default="explicit",
                    choices=["explicit", "static", "batch", "learned"],
                    help="explicit: 2048^2 Quad4 dynamics (headline); static: Hex8 n3d^3 Jacobi-PCG;"
-                        " batch: periodic Quad4 instances; learned: n2d^2 learned-FCG vs Jacobi-PCG")
+                        " batch: periodic Quad4 instances; learned: n2d^2 learned two-level FCG vs"
+                        " Jacobi-PCG")
     p.add_argument("--n3d", type=int, default=128)
     p.add_argument("--n2d", type=int, default=512)
     p.add_argument("--nloads", type=int, default=64)
-    p.add_argument("--train-steps", type=int, default=2000)
+    p.add_argument("--train-steps", type=int, default=4000)
+    p.add_argument("--hc", type=int, default=16, help="learned workload: coarse-grid spacing (nodes)")
     p.add_argument("--profile-iters", type=int, default=0,
                    help="learned workload, kernel-share probe: skip pair generation and training "
                         "and run each solver for this many iterations (untrained network)")
@@ -530,11 +532,12 @@ def _lib_call_bytes(H, W):
 
 
 def run_learned(args):
-    """Quad4 512^2 two-phase static case: learned-preconditioner flexible CG vs Jacobi-PCG, both
-    to 1e-8 relative residual in FP64 (time-to-solution on the same GPU; pair generation and
-    training reported apart). Jacobi-PCG is timed twice: the step-by-step session solver and the
-    ring solver with the Jacobi direction alone (the same algorithm replayed as a CUDA graph, the
-    machinery the learned solve uses); the speed-up is taken against the faster of the two."""
+    """Quad4 512^2 two-phase static case, every solve to 1e-8 relative residual in FP64
+    (time-to-solution on the same GPU; coarse set-up, pair generation and training reported
+    apart): Jacobi-PCG (the baseline; step-by-step session solver and the ring solver with the
+    Jacobi direction alone replayed as a CUDA graph, the faster of the two counts), the two-level
+    flexible CG without the network (the method without it), and the learned two-level solve
+    (the network as the post-smoother of the two-level step)."""
     import torch
 
     from goosefem_gb300 import learned as LR
@@ -554,34 +557,41 @@ def run_learned(args):
         torch.cuda.synchronize()
         return (time.perf_counter() - t0,) + tuple(out)
 
+    def best_of(fn):
+        timed(fn)  # warm-up
+        return min((timed(fn) for _ in range(args.steps)), key=lambda r: r[0])
+
+    res = {}
+    for name, fn in (("jacobi_pcg", lambda x: lp.jacobi_pcg(x)),
+                     ("jacobi_pcg_graph", lambda x: lp.fcg(x, use_nn=False, nkeep=1))):
+        b = best_of(fn)
+        res[name] = {"seconds": b[0], "iterations": b[1], "relres_true": b[2]}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lp.coarse_setup(args.hc)
+    torch.cuda.synchronize()
+    t_coarse = time.perf_counter() - t0
+    b = best_of(lambda x: lp.fcg(x, use_nn=False, nkeep=1, coarse=True))
+    res["twolevel"] = {"seconds": b[0], "iterations": b[1], "relres_true": b[2]}
     if args.profile_iters > 0:
         from goosefem_gb300 import _lib
 
         k = args.profile_iters
-        runs = {}
-        for name, fn in (("jacobi_pcg", lambda x: lp.static.solve(x.view(-1, 2), maxiter=k)),
-                         ("jacobi_pcg_graph", lambda x: lp.fcg(x, use_nn=False, nkeep=1, maxiter=k)),
-                         ("learned_fcg_keep8", lambda x: lp.fcg(x, use_nn=True, nkeep=8, maxiter=k))):
+        for name, kw in (("twolevel", dict(use_nn=False, nkeep=1)),
+                         ("learned_twolevel_keep4", dict(use_nn=True, nkeep=4, post=True))):
             x = lp.initial_guess(xp)
             try:
-                fn(x)
-                runs[name] = "converged"
+                lp.fcg(x, maxiter=k, coarse=True, **kw)
             except _lib.GFGPUError as e:
                 if e.code != -8:
                     raise
-                runs[name] = f"stopped after {k} iterations"
         torch.cuda.synchronize()
         print(json.dumps({"workload": "learned kernel-share probe (untrained network)",
-                          "config": {"nx": nx, "iterations": k}, "runs": runs}), flush=True)
+                          "config": {"nx": nx, "hc": args.hc, "iterations": k}}), flush=True)
         return 0
-    res = {}
-    for name, fn in (("jacobi_pcg", lambda x: lp.jacobi_pcg(x)),
-                     ("jacobi_pcg_graph", lambda x: lp.fcg(x, use_nn=False, nkeep=1))):
-        timed(fn)  # warm-up
-        best = min((timed(fn) for _ in range(args.steps)), key=lambda r: r[0])
-        res[name] = {"seconds": best[0], "iterations": best[1], "relres_true": best[2]}
     t0 = time.perf_counter()
-    npairs = lp.make_pairs(nloads=args.nloads, snaps=64, every=16, inner=8, seed=1)
+    npairs = lp.make_pairs_twolevel(nloads=args.nloads, snaps=48, every=4, target="cheb",
+                                    degree=8, post=True)
     torch.cuda.synchronize()
     t_pairs = time.perf_counter() - t0
     t0 = time.perf_counter()
@@ -589,14 +599,12 @@ def run_learned(args):
                       log_every=max(args.train_steps // 10, 1))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
-    for nkeep in (4, 8, 16):
-        fn = lambda x: lp.solve(x, nkeep=nkeep)  # noqa: E731
-        timed(fn)
-        best = min((timed(fn) for _ in range(args.steps)), key=lambda r: r[0])
-        res[f"learned_fcg_keep{nkeep}"] = {"seconds": best[0], "iterations": best[1],
-                                           "fallback_iterations": best[2], "relres_true": best[3]}
-    res["learned_fcg"] = min((v for k, v in res.items() if k.startswith("learned_fcg_keep")),
-                             key=lambda v: v["seconds"])
+    for nkeep in (1, 2, 4):
+        b = best_of(lambda x: lp.solve(x, nkeep=nkeep))
+        res[f"learned_twolevel_keep{nkeep}"] = {"seconds": b[0], "iterations": b[1],
+                                                "fallback_iterations": b[2], "relres_true": b[3]}
+    res["learned_twolevel"] = min((v for k, v in res.items() if k.startswith("learned_twolevel_keep")),
+                                  key=lambda v: v["seconds"])
     for v in res.values():
         v["us_per_iteration"] = 1e6 * v["seconds"] / max(v["iterations"] + v.get("fallback_iterations", 0), 1)
     # one network application (gfgpu_nn_infer: the same four layers), CUDA events
@@ -620,20 +628,26 @@ def run_learned(args):
     torch.cuda.synchronize()
     nn_ms = e0.elapsed_time(e1) / 50
     jac = min(res["jacobi_pcg"]["seconds"], res["jacobi_pcg_graph"]["seconds"])
-    line = {"metric": "time-to-1e-8 resid (learned FCG vs Jacobi PCG)",
-            "value": res["learned_fcg"]["seconds"], "unit": "s", "higher_is_better": False,
+    learned = res["learned_twolevel"]
+    line = {"metric": "time-to-1e-8 resid (learned two-level FCG vs Jacobi PCG)",
+            "value": learned["seconds"], "unit": "s", "higher_is_better": False,
             "n_gpus": 1, "steps": args.steps,
-            "dtype": "f64 solve, bf16-weight/fp32-accumulate network",
+            "dtype": "f64 solve, bf16-weight/fp32-accumulate network, fp32 coarse correction",
             "data": "synthetic (seeded inclusions)",
             "config": {"workload": f"Quad4 Regular {nx}x{nx}, two-phase (inclusions "
                                    f"{100 * inside.mean():.1f}% area, x10 moduli), bottom fixed, "
-                                   "top uy=-1e-2", "pairs": npairs, "train_steps": args.train_steps,
-                       "loss": "energy norm", "directions_kept": [4, 8, 16]},
+                                   "top uy=-1e-2", "coarse_spacing": args.hc, "pairs": npairs,
+                       "train_steps": args.train_steps,
+                       "target": "Chebyshev-8 smoother minus Jacobi step, on the residual after "
+                                 "the two-level step", "loss": "energy norm",
+                       "directions_kept": [1, 2, 4]},
             "solvers": res,
-            "speedup_vs_jacobi_pcg": jac / res["learned_fcg"]["seconds"],
-            "iteration_ratio": res["jacobi_pcg"]["iterations"] / max(res["learned_fcg"]["iterations"], 1),
-            "pair_generation_seconds": t_pairs, "training_seconds": t_train,
-            "network_application_ms": nn_ms,
+            "speedup_vs_jacobi_pcg": jac / learned["seconds"],
+            "speedup_vs_twolevel_without_network": res["twolevel"]["seconds"] / learned["seconds"],
+            "iteration_ratio_vs_jacobi_pcg": res["jacobi_pcg"]["iterations"] / max(learned["iterations"], 1),
+            "iteration_ratio_vs_twolevel": res["twolevel"]["iterations"] / max(learned["iterations"], 1),
+            "coarse_setup_seconds": t_coarse, "pair_generation_seconds": t_pairs,
+            "training_seconds": t_train, "network_application_ms": nn_ms,
             "loss_first_last": [losses[0], losses[-1]]}
     print(json.dumps(line), flush=True)
     return 0

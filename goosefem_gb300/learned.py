@@ -424,11 +424,14 @@ class LearnedPreconditioner:
     def solve(self, x, tol=1e-8, maxiter=20000, nkeep=8, check_every=16):
         """The learned solve with Jacobi-PCG as its fallback: when the flexible CG with the
         network does not reach tol within maxiter iterations, Jacobi-PCG continues from its
-        iterate. Returns (network iterations, fallback iterations, relative true residual)."""
+        iterate. After coarse_setup the solve is the two-level one with the network as the
+        post-smoother of the two-level step (train it on make_pairs_twolevel(post=True) pairs).
+        Returns (network iterations, fallback iterations, relative true residual)."""
         x0 = x.clone()
+        two = self.coarse is not None
         try:
             it, rel = self.fcg(x, tol=tol, use_nn=True, maxiter=maxiter, nkeep=nkeep,
-                               check_every=check_every)
+                               check_every=check_every, coarse=two, post=two)
             return it, 0, rel
         except _lib.GFGPUError as e:
             if e.code not in (-8, -5):  # not converged / non-finite residual

@@ -271,3 +271,60 @@ def test_trained_network_reduces_iterations(small_problem):
     assert rel_nn <= 1e-8 and S.residual(A, iip, xg) <= 1e-8  # FP64 answer, same tolerance
     assert np.linalg.norm(xg - xr) / np.linalg.norm(xr) <= 1e-6
     assert it_nn < it_j, (it_nn, it_j)
+
+
+def test_chebyshev_target_matches_restatement(small_problem):
+    """The training target of the two-level network, `degree` Jacobi-preconditioned Chebyshev
+    steps, against the same recurrence on the scipy stiffness."""
+    from goosefem_gb300 import learned as LR
+
+    nx, ny, K, G, iip, xp = small_problem
+    lp = LR.LearnedPreconditioner(nx, ny, K, G, iip, seed=0)
+    A, _ = _direct(nx, ny, K, G, iip, xp)
+    free = np.ones(A.shape[0], dtype=bool)
+    free[iip] = False
+    Dinv = np.where(free, 1.0 / A.diagonal(), 0.0)
+    r = np.random.default_rng(8).standard_normal(A.shape[0]) * free
+    got = lp.chebyshev(torch.as_tensor(r, device="cuda"), degree=8).cpu().numpy()
+    hi = lp._lambda_max()
+    lo = hi / 30.0
+    th, de = 0.5 * (hi + lo), 0.5 * (hi - lo)
+    sig = th / de
+    rho = 1.0 / sig
+    x = np.zeros_like(r)
+    res = r.copy()
+    d = Dinv * res / th
+    for _ in range(8):
+        x += d
+        res -= free * (A @ d)
+        rho_n = 1.0 / (2.0 * sig - rho)
+        d = rho_n * rho * d + (2.0 * rho_n / de) * (Dinv * res)
+        rho = rho_n
+    assert rel_err(got, x) <= 1e-10
+
+
+def test_trained_network_reduces_twolevel_iterations():
+    """What the trained network gains in the two-level solve: the same flexible CG with the
+    two-level direction, with and without the network's post-smoothing direction."""
+    from goosefem_gb300 import learned as LR
+    from goosefem_gb300 import mesh as M
+    from oracle import statics as S
+
+    nx = ny = 128
+    K, G, _ = LR.inclusion_material(nx, ny, 11, rmin=2.0, rmax=6.0)
+    iip, xp = LR.static_bc(M.Quad4.Regular(nx, ny))
+    lp = LR.LearnedPreconditioner(nx, ny, K, G, iip, seed=0)
+    lp.coarse_setup(8)
+    x_2l = lp.initial_guess(xp)
+    it_2l, _ = lp.fcg(x_2l, use_nn=False, nkeep=1, coarse=True)
+    lp.make_pairs_twolevel(nloads=16, snaps=24, every=3, target="cheb", degree=8, post=True)
+    losses = lp.train(steps=1500, batch=16, crop=48, margin=8, lr=2e-3, log_every=100)
+    assert losses[-1][1] < 0.5 * losses[0][1]
+    x_nn = lp.initial_guess(xp)
+    it_nn, fb, rel_nn = lp.solve(x_nn, nkeep=4)
+    assert fb == 0
+    A, xr = _direct(nx, ny, K, G, iip, xp)
+    xg = x_nn.cpu().numpy()
+    assert rel_nn <= 1e-8 and S.residual(A, iip, xg) <= 1e-8
+    assert np.linalg.norm(xg - xr) / np.linalg.norm(xr) <= 1e-6
+    assert it_nn < 0.8 * it_2l, (it_nn, it_2l)
