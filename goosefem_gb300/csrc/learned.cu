@@ -386,6 +386,20 @@ constexpr int kPadC = 40;
 constexpr int kTileY = 16, kTileX = 16;
 constexpr int kMmaThreads = 256; // 8 warps, warp w computes tile rows 2w and 2w + 1
 
+// 16-byte asynchronous global -> shared copy (zero fill when !valid; src must still be a valid
+// address); completion: cp_async_wait_all() then __syncthreads()
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc, bool valid)
+{
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
+    const int n = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gsrc), "r"(n) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 __device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2,
                                          uint32_t a3, uint32_t b0, uint32_t b1)
 {
@@ -447,18 +461,19 @@ k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict_
     __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(smem);          // [hh][hw][40]
     __nv_bfloat16* ws = halo + hh * hw * kPadC;                             // [9][8 NT][40]
     const int y0 = blockIdx.y * kTileY, x0 = blockIdx.x * kTileX;
+    // weights and halo (16-byte chunks of 8 channels, zero outside the grid) staged with
+    // asynchronous copies, all in flight at once
     for (int i = threadIdx.x; i < 9 * 8 * NT * kPadC / 8; i += blockDim.x)
-        reinterpret_cast<uint4*>(ws)[i] = reinterpret_cast<const uint4*>(WT)[i];
-    if (LAST && threadIdx.x == 0) s_sigma = z ? sqrt(sc[rr_slot] / nfree) : 1.0;
-    // halo: 16-byte chunks (8 channels)
+        cp_async16(ws + i * 8, WT + i * 8, true);
     for (int i = threadIdx.x; i < hh * hw * 4; i += blockDim.x) {
         int pix = i >> 2, ch = (i & 3) * 8;
         int yy = y0 - dil + pix / hw, xx = x0 - dil + pix % hw;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (yy >= 0 && yy < H && xx >= 0 && xx < Wd)
-            v = *reinterpret_cast<const uint4*>(X + (static_cast<int64_t>(yy) * Wd + xx) * 32 + ch);
-        *reinterpret_cast<uint4*>(halo + pix * kPadC + ch) = v;
+        const bool in = yy >= 0 && yy < H && xx >= 0 && xx < Wd;
+        const __nv_bfloat16* src = in ? X + (static_cast<int64_t>(yy) * Wd + xx) * 32 + ch : X;
+        cp_async16(halo + pix * kPadC + ch, src, in);
     }
+    if (LAST && threadIdx.x == 0) s_sigma = z ? sqrt(sc[rr_slot] / nfree) : 1.0;
+    cp_async_wait_all();
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gid = lane >> 2, tig = lane & 3;
@@ -546,8 +561,7 @@ k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_
     __shared__ __align__(16) __nv_bfloat16 wf[3 * 32 * kPadF];
     __shared__ float s_inv;
     const int y0 = blockIdx.y * kTileY, x0 = blockIdx.x * kTileX;
-    for (int i = threadIdx.x; i < 3 * 32 * kPadF / 8; i += blockDim.x)
-        reinterpret_cast<uint4*>(wf)[i] = reinterpret_cast<const uint4*>(WF)[i];
+    for (int i = threadIdx.x; i < 3 * 32 * kPadF / 8; i += blockDim.x) cp_async16(wf + i * 8, WF + i * 8, true);
     if (threadIdx.x == 0) {
         double sigma = r ? sqrt(sc[rr_slot] / nfree) : 1.0;
         s_inv = sigma > 0.0 ? static_cast<float>(1.0 / sigma) : 0.0f;
@@ -578,6 +592,7 @@ k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_
         __nv_bfloat162 h[2] = {__floats2bfloat162_rn(v[0], v[1]), __floats2bfloat162_rn(v[2], v[3])};
         *reinterpret_cast<uint2*>(halo + pix * 4) = *reinterpret_cast<uint2*>(h);
     }
+    cp_async_wait_all();
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gid = lane >> 2, tig = lane & 3;
