@@ -421,7 +421,7 @@ class LearnedPreconditioner:
                       ws.data_ptr(), _dev.stream(), C.addressof(it), C.addressof(rel))
         return int(it.value), float(rel.value)
 
-    def solve(self, x, tol=1e-8, maxiter=20000, nkeep=8, check_every=16):
+    def solve(self, x, tol=1e-8, maxiter=20000, nkeep=2, check_every=4):
         """The learned solve with Jacobi-PCG as its fallback: when the flexible CG with the
         network does not reach tol within maxiter iterations, Jacobi-PCG continues from its
         iterate. After coarse_setup the solve is the two-level one with the network as the

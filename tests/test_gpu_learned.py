@@ -262,7 +262,7 @@ def test_trained_network_reduces_iterations(small_problem):
     losses = lp.train(steps=1200, batch=16, crop=40, margin=8, lr=2e-3, log_every=100)
     assert losses[-1][1] < losses[0][1]
     x_nn = lp.initial_guess(xp)
-    it_nn, fb, rel_nn = lp.solve(x_nn)
+    it_nn, fb, rel_nn = lp.solve(x_nn, nkeep=8, check_every=16)
     assert fb == 0  # no fallback needed
     x_j = lp.initial_guess(xp)
     it_j, rel_j = lp.fcg(x_j, use_nn=False)
