@@ -651,6 +651,187 @@ k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_
     }
 }
 
+// ------------------------------------------------------------------ tcgen05 32 -> 32 layer
+//
+// Implicit GEMM on the 5th-generation tensor cores: M = 128 output pixels of one grid row,
+// N = 32 output channels, K = 9 taps x 32 input channels = 18 MMAs of K = 16, FP32 accumulators
+// in tensor memory (TMEM), one CTA of 4 warps per RPC consecutive output rows. The input halo
+// tile, (RPC + 2 dil) rows x (128 + 2 dil) pixels, is staged (cp.async, zero outside the grid)
+// as 4 channel planes of 16 bytes per pixel: in that layout the A operand of every tap and
+// K half is the same canonical no-swizzle K-major matrix (core matrices of 8 pixels x 16 B,
+// 128 B apart along M, one plane apart along K) at a shifted start address, so the taps need
+// no data movement. Weights: [tap][k half][8-channel half][co][8 ci], core matrices 128 B apart
+// along N and 512 B apart along K. Thread 0 issues the MMAs and commits them to an mbarrier;
+// every wait is bounded (flag gfgpu_nn_tc_status on time-out), TMEM is always freed.
+
+__device__ int g_tc_timeout = 0;
+
+constexpr int kTcThreads = 128;
+constexpr int kTcM = 128;
+constexpr int kTcWBytes = 9 * 2 * 2 * 32 * 16; // 18432
+constexpr long kTcSpin = 1L << 22;
+
+// W [t][ci][co] -> WB [t][kc][h][co][8]: ci = 16 kc + 8 h + e
+__global__ void k_nn_wprep_tc(const __nv_bfloat16* __restrict__ W, __nv_bfloat16* __restrict__ WB)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 9 * 1024) return;
+    int t = i / 1024, kc = (i / 512) % 2, h = (i / 256) % 2, co = (i / 8) % 32, e = i % 8;
+    WB[i] = W[(t * 32 + kc * 16 + h * 8 + e) * 32 + co];
+}
+
+__host__ __device__ constexpr int tc_rows(int rpc, int dil)
+{
+    return rpc + 2 * dil;
+}
+
+__host__ __device__ constexpr int tc_cols(int dil)
+{
+    return kTcM + 2 * dil;
+}
+
+// shared memory: weights, 4 planes, mbarrier + TMEM address slot
+inline size_t tc_smem_bytes(int rpc, int dil)
+{
+    return static_cast<size_t>(kTcWBytes) + 4 * static_cast<size_t>(tc_rows(rpc, dil)) * tc_cols(dil) * 16 + 64;
+}
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    // no-swizzle K-major matrix descriptor: start, leading (K) and stride (M/N) byte offsets in
+    // 16-byte units, version 1 (bits 46-47), layout type 0 (no swizzle)
+    return static_cast<uint64_t>((saddr >> 4) & 0x3FFFu) | (static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16) |
+           (static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B (bits 7-9,
+// 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t phase)
+{
+    for (long it = 0; it < kTcSpin; ++it) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(mbar), "r"(phase)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <int RPC>
+__global__ void __launch_bounds__(kTcThreads)
+k_conv32_tc(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ WB,
+            const float* __restrict__ bias, int dil, int H, int Wd, __nv_bfloat16* __restrict__ Y)
+{
+    constexpr uint32_t kCols = 32 * RPC; // TMEM columns: one 32-column accumulator per row
+    extern __shared__ __align__(128) unsigned char tsmem[];
+    const int R = tc_rows(RPC, dil), C = tc_cols(dil);
+    const uint32_t PL = static_cast<uint32_t>(R * C * 16);
+    unsigned char* wsm = tsmem;
+    unsigned char* planes = tsmem + kTcWBytes;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(planes + 4 * PL);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+    const uint32_t s_w = static_cast<uint32_t>(__cvta_generic_to_shared(wsm));
+    const uint32_t s_a = static_cast<uint32_t>(__cvta_generic_to_shared(planes));
+    const uint32_t s_mbar = static_cast<uint32_t>(__cvta_generic_to_shared(mbar));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y0 = blockIdx.y * RPC, x0 = blockIdx.x * kTcM;
+
+    if (warp == 0) {
+        const uint32_t s_slot = static_cast<uint32_t>(__cvta_generic_to_shared(tslot));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_slot), "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    for (int i = threadIdx.x; i < kTcWBytes / 16; i += blockDim.x) cp_async16(wsm + i * 16, WB + i * 8, true);
+    for (int i = threadIdx.x; i < R * C * 4; i += blockDim.x) {
+        const int q = i & 3, pix = i >> 2;
+        const int yy = y0 - dil + pix / C, xx = x0 - dil + pix % C;
+        const bool in = yy >= 0 && yy < H && xx >= 0 && xx < Wd;
+        const __nv_bfloat16* src = in ? X + (static_cast<int64_t>(yy) * Wd + xx) * 32 + q * 8 : X;
+        cp_async16(planes + q * PL + pix * 16, src, in);
+    }
+    cp_async_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = *tslot;
+
+    if (threadIdx.x == 0) {
+#pragma unroll 1
+        for (int m = 0; m < RPC; ++m) {
+#pragma unroll 1
+            for (int t = 0; t < 9; ++t) {
+                const int dy = dil * (t / 3 - 1), dx = dil * (t % 3 - 1);
+                const uint32_t pix0 = static_cast<uint32_t>((m + dil + dy) * C + dil + dx);
+#pragma unroll
+                for (int kc = 0; kc < 2; ++kc) {
+                    const uint64_t da = tc_desc(s_a + 2 * kc * PL + pix0 * 16, PL, 128);
+                    const uint64_t db = tc_desc(s_w + (t * 2 + kc) * 1024, 512, 128);
+                    const uint32_t acc = (t | kc) ? 1u : 0u;
+                    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr + m * 32),
+                                 "l"(da), "l"(db), "r"(kTcIdesc), "r"(acc)
+                                 : "memory");
+                }
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(s_mbar)
+                     : "memory");
+    }
+    bool ok = __all_sync(0xffffffffu, tc_wait(s_mbar, 0)); // warp-uniform: tcgen05.ld is .sync.aligned
+    if (!ok) {
+        atomicExch(&g_tc_timeout, 1);
+        tc_wait(s_mbar, 0); // give the tensor cores a second bounded chance before TMEM is freed
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (ok) {
+#pragma unroll 1
+        for (int m = 0; m < RPC; ++m) {
+            uint32_t v[32];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr + (static_cast<uint32_t>(warp * 32) << 16) + m * 32));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            const int yy = y0 + m, xx = x0 + warp * 32 + lane;
+            if (yy < H && xx < Wd) {
+                uint4* yp = reinterpret_cast<uint4*>(Y + (static_cast<int64_t>(yy) * Wd + xx) * 32);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    __nv_bfloat162 h[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int co = k * 8 + 2 * j;
+                        h[j] = __floats2bfloat162_rn(fmaxf(__uint_as_float(v[co]) + bias[co], 0.0f),
+                                                     fmaxf(__uint_as_float(v[co + 1]) + bias[co + 1], 0.0f));
+                    }
+                    yp[k] = *reinterpret_cast<uint4*>(h);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(kCols) : "memory");
+    }
+}
+
 inline size_t mma_smem_bytes(int dil, int nt = 4)
 {
     return static_cast<size_t>((kTileY + 2 * dil) * (kTileX + 2 * dil) + 9 * 8 * nt) * kPadC * 2;
@@ -1205,9 +1386,16 @@ inline int64_t fcg_bytes(const gfgpu_verlet_desc* d, int64_t hw, int nslots)
 inline void nn_prepare_weights(const gfgpu_nn_desc* nn, __nv_bfloat16* wt1, __nv_bfloat16* wt2,
                                __nv_bfloat16* wt0, __nv_bfloat16* wt3, cudaStream_t s)
 {
-    const unsigned g = (9 * 32 * kPadC + 255) / 256;
-    k_nn_wprep<<<g, 256, 0, s>>>(wb(nn->weights_bf16, 1), wt1);
-    k_nn_wprep<<<g, 256, 0, s>>>(wb(nn->weights_bf16, 2), wt2);
+    static_assert(kTcWBytes <= kWtBytes, "tcgen05 weights fit the prepared-weight buffers");
+    if (nn_tensor_path() == 1) {
+        k_nn_wprep_tc<<<(9 * 1024 + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 1), wt1);
+        k_nn_wprep_tc<<<(9 * 1024 + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 2), wt2);
+    }
+    else {
+        const unsigned g = (9 * 32 * kPadC + 255) / 256;
+        k_nn_wprep<<<g, 256, 0, s>>>(wb(nn->weights_bf16, 1), wt1);
+        k_nn_wprep<<<g, 256, 0, s>>>(wb(nn->weights_bf16, 2), wt2);
+    }
     k_nn_wprep_first<<<(3 * 32 * kPadF + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 0), wt0);
     k_nn_wprep_last<<<(9 * 8 * kPadC + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 3), wt3);
 }
@@ -1224,12 +1412,23 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
     dim3 grid((W + kTileX - 1) / kTileX, (H + kTileY - 1) / kTileY);
     k_first_mma<<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
                                              nn->params_f32 + b_off(0), H, W, a1);
-    k_conv_mma<4, false><<<grid, kMmaThreads, mma_smem_bytes(dil_of(1)), s>>>(
-        a1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2, nullptr, 0, 0.0, nullptr, 0, nullptr,
-        nullptr);
-    k_conv_mma<4, false><<<grid, kMmaThreads, mma_smem_bytes(dil_of(2)), s>>>(
-        a2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3, nullptr, 0, 0.0, nullptr, 0, nullptr,
-        nullptr);
+    if (nn_tensor_path() == 1) {
+        // layer 2 (dilation 2): 4 rows per CTA; layer 3 (dilation 4): 2 rows, so that two CTAs
+        // share an SM (shared memory 87 / 105 KB)
+        dim3 g4((W + kTcM - 1) / kTcM, (H + 3) / 4), g2((W + kTcM - 1) / kTcM, (H + 1) / 2);
+        k_conv32_tc<4><<<g4, kTcThreads, tc_smem_bytes(4, dil_of(1)), s>>>(a1, wt1, nn->params_f32 + b_off(1),
+                                                                          dil_of(1), H, W, a2);
+        k_conv32_tc<2><<<g2, kTcThreads, tc_smem_bytes(2, dil_of(2)), s>>>(a2, wt2, nn->params_f32 + b_off(2),
+                                                                          dil_of(2), H, W, a3);
+    }
+    else {
+        k_conv_mma<4, false><<<grid, kMmaThreads, mma_smem_bytes(dil_of(1)), s>>>(
+            a1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2, nullptr, 0, 0.0, nullptr, 0, nullptr,
+            nullptr);
+        k_conv_mma<4, false><<<grid, kMmaThreads, mma_smem_bytes(dil_of(2)), s>>>(
+            a2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3, nullptr, 0, 0.0, nullptr, 0, nullptr,
+            nullptr);
+    }
     k_conv_mma<1, true><<<grid, kMmaThreads, mma_smem_bytes(dil_of(3), 1), s>>>(
         a3, wt3, nn->params_f32 + b_off(3), dil_of(3), H, W, nullptr, sc, rr_slot, nfree, part, nnu, z,
         Y);
@@ -1254,6 +1453,12 @@ inline int prepare_mma(cudaStream_t)
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv_mma<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(mma_smem_bytes(4, 1))),
                       "cudaFuncSetAttribute"));
+    GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(tc_smem_bytes(4, dil_of(1)))),
+                      "cudaFuncSetAttribute"));
+    GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(tc_smem_bytes(2, dil_of(2)))),
+                      "cudaFuncSetAttribute"));
     done = true;
     return GFGPU_OK;
 }
@@ -1262,6 +1467,18 @@ inline int prepare_mma(cudaStream_t)
 } // namespace gfgpu
 
 extern "C" {
+
+int gfgpu_nn_tc_status(void)
+{
+    int flag = 0, zero = 0;
+    GF_TRY(check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize"));
+    GF_TRY(check_cuda(cudaMemcpyFromSymbol(&flag, g_tc_timeout, sizeof(int)), "cudaMemcpyFromSymbol"));
+    if (flag) {
+        GF_TRY(check_cuda(cudaMemcpyToSymbol(g_tc_timeout, &zero, sizeof(int)), "cudaMemcpyToSymbol"));
+        return fail(GFGPU_ERR_TIMEOUT, "gfgpu_nn_tc_status: a tcgen05 layer's wait for the tensor cores gave up");
+    }
+    return GFGPU_OK;
+}
 
 int gfgpu_nn_unit_element_stiffness(double* out)
 {

@@ -16,6 +16,12 @@ static thread_local std::string g_last_error;
 static int g_strict = 0;
 static int g_variant_elem = 0;
 static int g_variant_node = 0;
+static int g_nn_path = 0;
+
+int nn_tensor_path()
+{
+    return g_nn_path;
+}
 
 int variant_elem()
 {
@@ -81,6 +87,13 @@ int gfgpu_set_variant(int elem_variant, int node_variant)
         return fail(GFGPU_ERR_ARG, "gfgpu_set_variant: variants are 0 or 1");
     gfgpu::g_variant_elem = elem_variant;
     gfgpu::g_variant_node = node_variant;
+    return GFGPU_OK;
+}
+
+int gfgpu_set_nn_tensor_path(int path)
+{
+    if (path < 0 || path > 1) return fail(GFGPU_ERR_ARG, "gfgpu_set_nn_tensor_path: path is 0 or 1");
+    gfgpu::g_nn_path = path;
     return GFGPU_OK;
 }
 

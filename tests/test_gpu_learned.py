@@ -160,12 +160,15 @@ def test_gather_crops(L):
         assert np.array_equal(got.cpu().numpy(), exp)
 
 
-def test_tensor_core_inference_matches_fp32_and_oracle(L):
+@pytest.mark.parametrize("H,W", [(37, 45), (29, 301)])
+def test_tensor_core_inference_matches_fp32_and_oracle(L, H, W):
+    """Inference with the 32 -> 32 layers on tcgen05 (TMEM accumulators) and on mma.sync against
+    the FP32 CUDA-core path and the FP64 oracle; grids narrower and wider than the 128-pixel
+    tcgen05 tile, with a partial last tile."""
     from oracle import nn as O
     from goosefem_gb300.learned import NNDesc
     import ctypes as C
 
-    H, W = 37, 45
     pt, wb = _random_params(L, 3, scale=0.8)
     rng = np.random.default_rng(4)
     X0 = rng.normal(size=(H, W, 4)).astype(np.float32)
@@ -181,14 +184,25 @@ def test_tensor_core_inference_matches_fp32_and_oracle(L):
     # tensor-core path
     d = NNDesc()
     d.weights_bf16, d.params_f32, d.material, d.H, d.W = wb.data_ptr(), pt.data_ptr(), mat.data_ptr(), H, W
-    ytc = torch.empty((H, W, 2), dtype=torch.float32, device="cuda")
     nbi = int(L.lib().gfgpu_nn_infer_workspace_bytes(H, W))
     ws2 = torch.empty(nbi // 8 + 1, dtype=torch.float64, device="cuda")
-    L.call("gfgpu_nn_infer", C.addressof(d), Xd.data_ptr(), ytc.data_ptr(), ws2.data_ptr(), s)
     yref, _ = O.forward(X0[None].astype(np.float64), _oracle_params(L, pt, wb), DILS)
     assert rel_err(y32.cpu().numpy(), yref[0]) <= 1e-5
-    # BF16 activations between the layers: agreement to the BF16 rounding level
-    assert rel_err(ytc.cpu().numpy(), yref[0]) <= 3e-2
+    out = {}
+    try:
+        for path in (0, 1):  # mma.sync, tcgen05
+            L.call("gfgpu_set_nn_tensor_path", path)
+            ytc = torch.full((H, W, 2), float("nan"), dtype=torch.float32, device="cuda")
+            L.call("gfgpu_nn_infer", C.addressof(d), Xd.data_ptr(), ytc.data_ptr(), ws2.data_ptr(), s)
+            L.call("gfgpu_nn_tc_status")
+            out[path] = ytc.cpu().numpy()
+            # BF16 activations between the layers: agreement to the BF16 rounding level
+            assert np.all(np.isfinite(out[path]))
+            assert rel_err(out[path], yref[0]) <= 3e-2, path
+    finally:
+        L.call("gfgpu_set_nn_tensor_path", 0)
+    # same products, different FP32 summation order
+    assert rel_err(out[0], out[1]) <= 1e-2
 
 
 @pytest.fixture(scope="module")
