@@ -20,7 +20,7 @@ int check_launch(const char* what);
 bool strict_mode();
 int variant_elem();
 int variant_node();
-int nn_tensor_path(); // 32 -> 32 network layers: 0 = mma.sync, 1 = tcgen05
+int nn_tensor_path(); // 32 -> 32 network layers: 0 = mma.sync, 1 = tcgen05, 2 = tcgen05 + TMA pipeline
 
 inline cudaStream_t S(gfgpu_stream_t s)
 {

@@ -14,7 +14,9 @@
 //  * a flexible CG in FP64 (Notay's truncated FCG with two search directions per iteration, the
 //    Jacobi-preconditioned residual and the network's correction, each A-orthogonalised against
 //    a ring of earlier directions), replayed as a CUDA graph.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -832,6 +834,206 @@ k_conv32_tc(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict
     }
 }
 
+// ------------------------------------------------------- tcgen05 + TMA, persistent pipeline
+//
+// The same implicit GEMM as k_conv32_tc, as a persistent kernel (one CTA per SM) that overlaps
+// the three stages of consecutive tiles of RPC rows x 128 pixels: warp 0 (one lane) loads the
+// halo tile's 4 channel planes with TMA (cp.async.bulk.tensor, 4-d view [H][W][4][8] of the
+// activation, box [R][C][1][8], zero fill outside the grid) into one of two shared-memory
+// stages; warp 1 (one lane) issues the 18 RPC MMAs of a tile into one of two TMEM accumulators
+// and commits them to the stage's "empty" and the accumulator's "full" mbarrier; warps 2-5 drain
+// an accumulator (tcgen05.ld, bias, ReLU, BF16) while the next tile is multiplied. Every wait is
+// bounded; a role that gives up sets the time-out flag and leaves its loop.
+
+constexpr int kTcpThreads = 192;
+constexpr int kTcpStages = 2;
+constexpr int kTcpRPC = 4;
+
+__host__ __device__ constexpr uint32_t tcp_plane_bytes(int dil)
+{
+    return static_cast<uint32_t>((tc_rows(kTcpRPC, dil) * tc_cols(dil) * 16 + 127) / 128 * 128);
+}
+
+inline size_t tcp_smem_bytes(int dil)
+{
+    return 1024 + kTcWBytes + static_cast<size_t>(kTcpStages) * 4 * tcp_plane_bytes(dil) + 128;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t a)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(a) : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t a)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(a)
+                 : "memory");
+}
+
+template <int RPC>
+__global__ void __launch_bounds__(kTcpThreads, 1)
+k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __restrict__ WB,
+             const float* __restrict__ bias, int dil, int H, int Wd, __nv_bfloat16* __restrict__ Y)
+{
+    constexpr uint32_t kCols = 2 * 32 * RPC; // two accumulators of RPC x 32 columns
+    extern __shared__ unsigned char tpsm[];
+    unsigned char* wsm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tpsm) + 1023) & ~uintptr_t(1023));
+    unsigned char* stages = wsm + kTcWBytes;
+    const int R = tc_rows(RPC, dil), C = tc_cols(dil);
+    const uint32_t PL = tcp_plane_bytes(dil), SB = 4 * PL;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(stages + kTcpStages * SB); // full[2] empty[2] tfull[2] tempty[2]
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
+    const uint32_t s_w = static_cast<uint32_t>(__cvta_generic_to_shared(wsm));
+    const uint32_t s_st = static_cast<uint32_t>(__cvta_generic_to_shared(stages));
+    const uint32_t s_bar = static_cast<uint32_t>(__cvta_generic_to_shared(bars));
+    auto full = [&](int i) { return s_bar + 8u * i; };
+    auto empty = [&](int i) { return s_bar + 8u * (2 + i); };
+    auto tfull = [&](int i) { return s_bar + 8u * (4 + i); };
+    auto tempty = [&](int i) { return s_bar + 8u * (6 + i); };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_x = (Wd + kTcM - 1) / kTcM, ntiles = tiles_x * ((H + RPC - 1) / RPC);
+
+    if (warp == 1) {
+        const uint32_t s_slot = static_cast<uint32_t>(__cvta_generic_to_shared(tslot));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_slot), "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(full(i), 1);
+            mbar_init(empty(i), 1);
+            mbar_init(tfull(i), 1);
+            mbar_init(tempty(i), 128);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
+    }
+    for (int i = threadIdx.x; i < kTcWBytes / 16; i += blockDim.x) cp_async16(wsm + i * 16, WB + i * 8, true);
+    cp_async_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = *tslot;
+
+    if (warp == 0) {
+        if (lane == 0) { // TMA producer
+            const uint32_t bytes = 4u * 16u * static_cast<uint32_t>(C * R);
+            for (int k = 0, tile = blockIdx.x; tile < ntiles; ++k, tile += gridDim.x) {
+                const int st = k % kTcpStages;
+                if (k >= kTcpStages && !tc_wait(empty(st), ((k / kTcpStages) - 1) & 1)) {
+                    atomicExch(&g_tc_timeout, 1);
+                    break;
+                }
+                const int y0 = (tile / tiles_x) * RPC, x0 = (tile % tiles_x) * kTcM;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(full(st)), "r"(bytes)
+                             : "memory");
+                for (int q = 0; q < 4; ++q)
+                    asm volatile(
+                        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(s_st + st * SB + q * PL),
+                        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(q), "r"(x0 - dil), "r"(y0 - dil),
+                        "r"(full(st))
+                        : "memory");
+            }
+        }
+    }
+    else if (warp == 1) {
+        if (lane == 0) { // MMA issuer
+            for (int k = 0, tile = blockIdx.x; tile < ntiles; ++k, tile += gridDim.x) {
+                const int st = k % kTcpStages, b = k & 1;
+                if (!tc_wait(full(st), (k / kTcpStages) & 1) || (k >= 2 && !tc_wait(tempty(b), ((k >> 1) - 1) & 1))) {
+                    atomicExch(&g_tc_timeout, 1);
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                // descriptors differ only in the start-address field (16-byte units, no carry:
+                // shared addresses < 256 KB): one base each, offsets added
+                const uint64_t da0 = tc_desc(s_st + st * SB, PL, 128), db0 = tc_desc(s_w, 512, 128);
+#pragma unroll 1
+                for (int m = 0; m < RPC; ++m) {
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) {
+                        const int dy = dil * (t / 3 - 1), dx = dil * (t % 3 - 1);
+                        const uint32_t pix0 = static_cast<uint32_t>((m + dil + dy) * C + dil + dx);
+#pragma unroll
+                        for (int kc = 0; kc < 2; ++kc) {
+                            const uint64_t da = da0 + pix0 + kc * (2 * PL >> 4);
+                            const uint64_t db = db0 + (t * 2 + kc) * 64;
+                            const uint32_t acc = (t | kc) ? 1u : 0u;
+                            asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                                             taddr + b * 32 * RPC + m * 32),
+                                         "l"(da), "l"(db), "r"(kTcIdesc), "r"(acc)
+                                         : "memory");
+                        }
+                    }
+                }
+                tc_commit(empty(st));
+                tc_commit(tfull(b));
+            }
+        }
+    }
+    else { // epilogue, warps 2-5: TMEM lane quarter warp % 4
+        const int q4 = warp & 3;
+        float bs[32];
+#pragma unroll
+        for (int co = 0; co < 32; ++co) bs[co] = bias[co];
+        for (int k = 0, tile = blockIdx.x; tile < ntiles; ++k, tile += gridDim.x) {
+            const int b = k & 1;
+            if (!__all_sync(0xffffffffu, tc_wait(tfull(b), (k >> 1) & 1))) {
+                atomicExch(&g_tc_timeout, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int y0 = (tile / tiles_x) * RPC, x0 = (tile % tiles_x) * kTcM;
+#pragma unroll 1
+            for (int m = 0; m < RPC; ++m) {
+                uint32_t v[32];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr + (static_cast<uint32_t>(q4 * 32) << 16) + b * 32 * RPC + m * 32));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                const int yy = y0 + m, xx = x0 + q4 * 32 + lane;
+                if (yy < H && xx < Wd) {
+                    uint4* yp = reinterpret_cast<uint4*>(Y + (static_cast<int64_t>(yy) * Wd + xx) * 32);
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        __nv_bfloat162 h[4];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int co = kk * 8 + 2 * j;
+                            h[j] = __floats2bfloat162_rn(fmaxf(__uint_as_float(v[co]) + bs[co], 0.0f),
+                                                         fmaxf(__uint_as_float(v[co + 1]) + bs[co + 1], 0.0f));
+                        }
+                        yp[kk] = *reinterpret_cast<uint4*>(h);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            mbar_arrive(tempty(b));
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(kCols) : "memory");
+    }
+}
+
 inline size_t mma_smem_bytes(int dil, int nt = 4)
 {
     return static_cast<size_t>((kTileY + 2 * dil) * (kTileX + 2 * dil) + 9 * 8 * nt) * kPadC * 2;
@@ -1387,7 +1589,7 @@ inline void nn_prepare_weights(const gfgpu_nn_desc* nn, __nv_bfloat16* wt1, __nv
                                __nv_bfloat16* wt0, __nv_bfloat16* wt3, cudaStream_t s)
 {
     static_assert(kTcWBytes <= kWtBytes, "tcgen05 weights fit the prepared-weight buffers");
-    if (nn_tensor_path() == 1) {
+    if (nn_tensor_path() >= 1) {
         k_nn_wprep_tc<<<(9 * 1024 + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 1), wt1);
         k_nn_wprep_tc<<<(9 * 1024 + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 2), wt2);
     }
@@ -1398,6 +1600,32 @@ inline void nn_prepare_weights(const gfgpu_nn_desc* nn, __nv_bfloat16* wt1, __nv
     }
     k_nn_wprep_first<<<(3 * 32 * kPadF + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 0), wt0);
     k_nn_wprep_last<<<(9 * 8 * kPadC + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 3), wt3);
+}
+
+// TMA view of a BF16 [H, W, 32] activation as [H][W][4 planes][8 channels]; box of one plane of
+// the halo tile of k_conv32_tcp (R rows x C pixels x 8 channels), zero fill outside the grid
+inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W, int dil)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        GF_TRY(check_cuda(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q),
+                          "cudaGetDriverEntryPointByVersion"));
+        if (q != cudaDriverEntryPointSuccess || !fn) return fail(GFGPU_ERR_CUDA, "cuTensorMapEncodeTiled not found");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    GF_REQUIRE((reinterpret_cast<uintptr_t>(X) & 15u) == 0, "activation not 16-byte aligned");
+    const cuuint64_t dims[4] = {8, 4, static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H)};
+    const cuuint64_t strides[3] = {16, 64, static_cast<cuuint64_t>(W) * 64};
+    const cuuint32_t box[4] = {8, 1, static_cast<cuuint32_t>(tc_cols(dil)),
+                               static_cast<cuuint32_t>(tc_rows(kTcpRPC, dil))};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult rc = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(X), dims, strides,
+                         box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (rc != CUDA_SUCCESS) return fail(GFGPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(rc)) + ")");
+    return GFGPU_OK;
 }
 
 // the four layers on one H x W grid: input from the FP64 residual (r != null) or from X0,
@@ -1412,7 +1640,20 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
     dim3 grid((W + kTileX - 1) / kTileX, (H + kTileY - 1) / kTileY);
     k_first_mma<<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
                                              nn->params_f32 + b_off(0), H, W, a1);
-    if (nn_tensor_path() == 1) {
+    if (nn_tensor_path() == 2) {
+        CUtensorMap m1, m2;
+        GF_TRY(tcp_tensor_map(&m1, a1, H, W, dil_of(1)));
+        GF_TRY(tcp_tensor_map(&m2, a2, H, W, dil_of(2)));
+        const int ntiles = ((W + kTcM - 1) / kTcM) * ((H + kTcpRPC - 1) / kTcpRPC);
+        int sms = 0;
+        GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0), "cudaDeviceGetAttribute"));
+        const unsigned g = static_cast<unsigned>(std::max(1, std::min(ntiles, sms)));
+        k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(1)), s>>>(
+            m1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
+        k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(2)), s>>>(
+            m2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
+    }
+    else if (nn_tensor_path() == 1) {
         // layer 2 (dilation 2): 4 rows per CTA; layer 3 (dilation 4): 2 rows, so that two CTAs
         // share an SM (shared memory 87 / 105 KB)
         dim3 g4((W + kTcM - 1) / kTcM, (H + 3) / 4), g2((W + kTcM - 1) / kTcM, (H + 1) / 2);
@@ -1452,6 +1693,10 @@ inline int prepare_mma(cudaStream_t)
                       "cudaFuncSetAttribute"));
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv_mma<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(mma_smem_bytes(4, 1))),
+                      "cudaFuncSetAttribute"));
+    GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_tcp<kTcpRPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(std::max(tcp_smem_bytes(dil_of(1)),
+                                                                     tcp_smem_bytes(dil_of(2))))),
                       "cudaFuncSetAttribute"));
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(tc_smem_bytes(4, dil_of(1)))),

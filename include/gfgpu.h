@@ -55,8 +55,9 @@ int gfgpu_set_strict(int strict);
  * node_variant 1 = both dofs of a node per thread in the node kernel. Same results. */
 int gfgpu_set_variant(int elem_variant, int node_variant);
 /* Tensor-core instructions of the network's 32 -> 32 layers (process-wide): 0 = mma.sync m16n8k16
- * (default), 1 = tcgen05.mma with TMEM accumulators. Same arithmetic (BF16 products, FP32
- * accumulation); the summation order differs. */
+ * (default), 1 = tcgen05.mma with TMEM accumulators, one tile per CTA, 2 = tcgen05.mma in a
+ * persistent pipeline fed by TMA (cp.async.bulk.tensor) with double-buffered shared memory and
+ * TMEM. Same arithmetic (BF16 products, FP32 accumulation); the summation order differs. */
 int gfgpu_set_nn_tensor_path(int path);
 /* Error flag of the tcgen05 layers' bounded waits: GFGPU_ERR_TIMEOUT if a wait for the tensor
  * cores gave up since the last call (the layer's output is then invalid), else GFGPU_OK. Clears
