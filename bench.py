@@ -56,6 +56,9 @@ def parse():
     p.add_argument("--nloads", type=int, default=64)
     p.add_argument("--train-steps", type=int, default=6000)
     p.add_argument("--hc", type=int, default=16, help="learned workload: coarse-grid spacing (nodes)")
+    p.add_argument("--nn-path", type=int, default=0,
+                   help="learned workload: tensor-core form of the network's 32->32 layers "
+                        "(gfgpu_set_nn_tensor_path: 0 mma.sync, 1 tcgen05, 2 tcgen05 + TMA pipeline)")
     p.add_argument("--profile-iters", type=int, default=0,
                    help="learned workload, kernel-share probe: skip pair generation and training "
                         "and run each solver for this many iterations (untrained network)")
@@ -543,6 +546,9 @@ def run_learned(args):
     from goosefem_gb300 import learned as LR
     from goosefem_gb300 import mesh as M
 
+    from goosefem_gb300 import _lib as _L
+
+    _L.call("gfgpu_set_nn_tensor_path", int(args.nn_path))
     nx = args.n2d
     K, G, inside = LR.inclusion_material(nx, nx, 512)
     m = M.Quad4.Regular(nx, nx)
@@ -647,7 +653,7 @@ def run_learned(args):
                        "residual_check": "learned every 4 iterations; two-level best of 4, 8, 16",
                        "target": "Chebyshev-8 smoother minus Jacobi step, on the residual after "
                                  "the two-level step", "loss": "energy norm",
-                       "directions_kept": [1, 2, 4]},
+                       "directions_kept": [1, 2, 4], "nn_tensor_path": args.nn_path},
             "solvers": res,
             "speedup_vs_jacobi_pcg": jac / learned["seconds"],
             "speedup_vs_twolevel_without_network": res["twolevel"]["seconds"] / learned["seconds"],

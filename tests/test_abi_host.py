@@ -223,3 +223,23 @@ def test_tyings_setup_matches_oracle(lib, oracle):
     assert np.array_equal(ty.Cdu().toarray(), Cdi_r[:, :ty.nnu()])
     assert np.array_equal(ty.Cdp().toarray(), Cdi_r[:, ty.nnu():])
     assert ty.nnd() == mesh.nodesPeriodic().shape[0] * 2
+
+
+@pytest.mark.parametrize("nx,ny,hc", [(512, 512, 16), (37, 30, 8), (5, 3, 7), (1, 1, 1)])
+def test_coarse_grid_matches_oracle(lib, nx, ny, hc):
+    """gfgpu_coarse_grid (host): coarse node counts, the padded row stride of the dense inverse and
+    the reciprocal interval lengths from the coarse coordinates of the oracle's restatement."""
+    from goosefem_gb300.learned import CoarseDesc
+    from oracle import coarse as OC
+    import ctypes as C
+
+    g = CoarseDesc()
+    lib.call("gfgpu_coarse_grid", nx, ny, hc, C.addressof(g))
+    X, Y = OC.coarse_coords(nx, hc), OC.coarse_coords(ny, hc)
+    assert (g.ncx, g.ncy) == (X.size, Y.size)
+    nc = 2 * X.size * Y.size
+    assert g.ld % 32 == 0 and nc <= g.ld < nc + 32
+    assert g.rhx == 1.0 / hc and g.rhy == 1.0 / hc
+    assert g.rlx == 1.0 / (X[-1] - X[-2]) and g.rly == 1.0 / (Y[-1] - Y[-2])
+    with pytest.raises(lib.GFGPUError):
+        lib.call("gfgpu_coarse_grid", nx, ny, 0, C.addressof(g))
