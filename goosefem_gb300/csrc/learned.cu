@@ -450,7 +450,7 @@ __global__ void k_nn_wprep_first(const __nv_bfloat16* __restrict__ W, __nv_bfloa
 // LAST = false: Y = relu(conv + b), BF16 [H, W, 32] (NT = 4). LAST = true (NT = 1, the 32 -> 2
 // output layer): z = sigma (conv + b) on the free dofs, 0 on prescribed (FP64 nodevec; sigma =
 // RMS of the residual, sqrt(sc[rr_slot] / nfree)), or Yf [H, W, 2] FP32 when z is null.
-template <int NT, bool LAST>
+template <int NT, bool LAST, bool PLANAR_IN = false>
 __global__ void __launch_bounds__(kMmaThreads)
 k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ WT,
            const float* __restrict__ bias, int dil, int H, int Wd, __nv_bfloat16* __restrict__ Y,
@@ -471,7 +471,9 @@ k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict_
         int pix = i >> 2, ch = (i & 3) * 8;
         int yy = y0 - dil + pix / hw, xx = x0 - dil + pix % hw;
         const bool in = yy >= 0 && yy < H && xx >= 0 && xx < Wd;
-        const __nv_bfloat16* src = in ? X + (static_cast<int64_t>(yy) * Wd + xx) * 32 + ch : X;
+        const int64_t gp = static_cast<int64_t>(yy) * Wd + xx;
+        const __nv_bfloat16* src =
+            !in ? X : (PLANAR_IN ? X + (ch / 8) * (static_cast<int64_t>(H) * Wd * 8) + gp * 8 : X + gp * 32 + ch);
         cp_async16(halo + pix * kPadC + ch, src, in);
     }
     if (LAST && threadIdx.x == 0) s_sigma = z ? sqrt(sc[rr_slot] / nfree) : 1.0;
@@ -552,6 +554,7 @@ k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict_
 // residual scaled by 1 / sigma and the two material channels, or X0 [H, W, 4]) are rounded to
 // BF16 into a shared halo tile [18][18][4]; K = 3 steps of 4 taps x 4 channels. Output BF16
 // [H, W, 32]. Same tile and warp layout as k_conv_mma.
+template <bool PLANAR_OUT = false>
 __global__ void __launch_bounds__(kMmaThreads)
 k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_slot, double nfree,
             const float* __restrict__ mat, const float* __restrict__ X0,
@@ -641,13 +644,15 @@ k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_
         for (int half = 0; half < 2; ++half) {
             const int xx = x0 + gid + 8 * half;
             if (xx >= Wd) continue;
-            __nv_bfloat16* yp = Y + (static_cast<int64_t>(yy) * Wd + xx) * 32;
+            const int64_t gp = static_cast<int64_t>(yy) * Wd + xx;
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt) {
                 const int co = nt * 8 + tig * 2;
                 float v0 = fmaxf(c[mt][nt][2 * half + 0] + bias[co], 0.0f);
                 float v1 = fmaxf(c[mt][nt][2 * half + 1] + bias[co + 1], 0.0f);
-                *reinterpret_cast<__nv_bfloat162*>(yp + co) = __floats2bfloat162_rn(v0, v1);
+                __nv_bfloat16* yp = PLANAR_OUT ? Y + nt * (static_cast<int64_t>(H) * Wd * 8) + gp * 8 + tig * 2
+                                               : Y + gp * 32 + co;
+                *reinterpret_cast<__nv_bfloat162*>(yp) = __floats2bfloat162_rn(v0, v1);
             }
         }
     }
@@ -837,9 +842,11 @@ k_conv32_tc(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict
 // ------------------------------------------------------- tcgen05 + TMA, persistent pipeline
 //
 // The same implicit GEMM as k_conv32_tc, as a persistent kernel (one CTA per SM) that overlaps
-// the three stages of consecutive tiles of RPC rows x 128 pixels: warp 0 (one lane) loads the
-// halo tile's 4 channel planes with TMA (cp.async.bulk.tensor, 4-d view [H][W][4][8] of the
-// activation, box [R][C][1][8], zero fill outside the grid) into one of two shared-memory
+// the three stages of consecutive tiles of RPC rows x 128 pixels. Activations in and out are
+// channel-planar, [4][H][W][8] BF16 (each plane contiguous), so that a plane of the halo tile is
+// one TMA box of contiguous 16-byte pixels per row. Warp 0 (one lane) loads the halo tile's 4
+// planes with TMA (cp.async.bulk.tensor, 4-d view [4][H][W][8], box [1][R][C][8], zero fill
+// outside the grid) into one of two shared-memory
 // stages; warp 1 (one lane) issues the 18 RPC MMAs of a tile into one of two TMEM accumulators
 // and commits them to the stage's "empty" and the accumulator's "full" mbarrier; warps 2-5 drain
 // an accumulator (tcgen05.ld, bias, ReLU, BF16) while the next tile is multiplied. Every wait is
@@ -938,7 +945,7 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __re
                     asm volatile(
                         "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
                         " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(s_st + st * SB + q * PL),
-                        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(q), "r"(x0 - dil), "r"(y0 - dil),
+                        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(x0 - dil), "r"(y0 - dil), "r"(q),
                         "r"(full(st))
                         : "memory");
             }
@@ -1008,7 +1015,9 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __re
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
                 const int yy = y0 + m, xx = x0 + q4 * 32 + lane;
                 if (yy < H && xx < Wd) {
-                    uint4* yp = reinterpret_cast<uint4*>(Y + (static_cast<int64_t>(yy) * Wd + xx) * 32);
+                    // planar output: the lanes of a warp write 32 consecutive 16-byte pixels of a plane
+                    __nv_bfloat16* yp = Y + (static_cast<int64_t>(yy) * Wd + xx) * 8;
+                    const int64_t plane = static_cast<int64_t>(H) * Wd * 8;
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk) {
                         __nv_bfloat162 h[4];
@@ -1018,7 +1027,7 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __re
                             h[j] = __floats2bfloat162_rn(fmaxf(__uint_as_float(v[co]) + bs[co], 0.0f),
                                                          fmaxf(__uint_as_float(v[co + 1]) + bs[co + 1], 0.0f));
                         }
-                        yp[kk] = *reinterpret_cast<uint4*>(h);
+                        *reinterpret_cast<uint4*>(yp + kk * plane) = *reinterpret_cast<uint4*>(h);
                     }
                 }
             }
@@ -1602,8 +1611,8 @@ inline void nn_prepare_weights(const gfgpu_nn_desc* nn, __nv_bfloat16* wt1, __nv
     k_nn_wprep_last<<<(9 * 8 * kPadC + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 3), wt3);
 }
 
-// TMA view of a BF16 [H, W, 32] activation as [H][W][4 planes][8 channels]; box of one plane of
-// the halo tile of k_conv32_tcp (R rows x C pixels x 8 channels), zero fill outside the grid
+// TMA view of a channel-planar BF16 activation [4][H][W][8]; box of one plane of the halo tile of
+// k_conv32_tcp (R rows x C pixels x 8 channels), zero fill outside the grid
 inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W, int dil)
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
@@ -1616,10 +1625,11 @@ inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
     GF_REQUIRE((reinterpret_cast<uintptr_t>(X) & 15u) == 0, "activation not 16-byte aligned");
-    const cuuint64_t dims[4] = {8, 4, static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H)};
-    const cuuint64_t strides[3] = {16, 64, static_cast<cuuint64_t>(W) * 64};
-    const cuuint32_t box[4] = {8, 1, static_cast<cuuint32_t>(tc_cols(dil)),
-                               static_cast<cuuint32_t>(tc_rows(kTcpRPC, dil))};
+    const cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H), 4};
+    const cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(W) * 16,
+                                   static_cast<cuuint64_t>(H) * static_cast<cuuint64_t>(W) * 16};
+    const cuuint32_t box[4] = {8, static_cast<cuuint32_t>(tc_cols(dil)), static_cast<cuuint32_t>(tc_rows(kTcpRPC, dil)),
+                               1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult rc = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(X), dims, strides,
                          box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -1638,8 +1648,13 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
 {
     const int H = nn->H, W = nn->W;
     dim3 grid((W + kTileX - 1) / kTileX, (H + kTileY - 1) / kTileY);
-    k_first_mma<<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
-                                             nn->params_f32 + b_off(0), H, W, a1);
+    const bool planar = nn_tensor_path() == 2; // path 2: channel-planar activations
+    if (planar)
+        k_first_mma<true><<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
+                                                       nn->params_f32 + b_off(0), H, W, a1);
+    else
+        k_first_mma<false><<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
+                                                        nn->params_f32 + b_off(0), H, W, a1);
     if (nn_tensor_path() == 2) {
         CUtensorMap m1, m2;
         GF_TRY(tcp_tensor_map(&m1, a1, H, W, dil_of(1)));
@@ -1670,9 +1685,14 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
             a2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3, nullptr, 0, 0.0, nullptr, 0, nullptr,
             nullptr);
     }
-    k_conv_mma<1, true><<<grid, kMmaThreads, mma_smem_bytes(dil_of(3), 1), s>>>(
-        a3, wt3, nn->params_f32 + b_off(3), dil_of(3), H, W, nullptr, sc, rr_slot, nfree, part, nnu, z,
-        Y);
+    if (planar)
+        k_conv_mma<1, true, true><<<grid, kMmaThreads, mma_smem_bytes(dil_of(3), 1), s>>>(
+            a3, wt3, nn->params_f32 + b_off(3), dil_of(3), H, W, nullptr, sc, rr_slot, nfree, part, nnu, z,
+            Y);
+    else
+        k_conv_mma<1, true><<<grid, kMmaThreads, mma_smem_bytes(dil_of(3), 1), s>>>(
+            a3, wt3, nn->params_f32 + b_off(3), dil_of(3), H, W, nullptr, sc, rr_slot, nfree, part, nnu, z,
+            Y);
     return check_launch("nn_forward");
 }
 
@@ -1692,6 +1712,9 @@ inline int prepare_mma(cudaStream_t)
                                            static_cast<int>(mma_smem_bytes(4))),
                       "cudaFuncSetAttribute"));
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv_mma<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(mma_smem_bytes(4, 1))),
+                      "cudaFuncSetAttribute"));
+    GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv_mma<1, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(mma_smem_bytes(4, 1))),
                       "cudaFuncSetAttribute"));
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_tcp<kTcpRPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
