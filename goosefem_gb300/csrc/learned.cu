@@ -1231,6 +1231,53 @@ __device__ __forceinline__ double bsum(double v, double* sh)
     return r;
 }
 
+// Last-block reductions: every block of a 1024-block (kRed) partial-sum kernel writes its partial,
+// fences and counts itself in; the last block to arrive reduces the partials (fixed order, so the
+// result does not depend on which block is last) and resets the counter for the next launch. This
+// replaces a separate one-block reduction launch.
+__device__ __forceinline__ bool last_block(unsigned int* counter)
+{
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int prev = atomicAdd(counter, 1u);
+        is_last = prev == gridDim.x - 1;
+        if (is_last) *counter = 0u;
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+
+// sum of partial[0 .. kRed) by the whole block in a fixed order
+__device__ __forceinline__ double block_sum_partials(const double* partial, double* sh)
+{
+    double v = 0.0;
+    for (int i = threadIdx.x; i < kRed; i += blockDim.x) v += __ldcg(partial + i);
+    return bsum(v, sh);
+}
+
+// coefficient c_k = (z.Q_j) / (P_j.Q_j) of basis entry k (slot j = L.s[k]) from partial row k,
+// computed by the last block (warp k -> rows k, k + nwarps, ...; lane-strided sums, then the
+// shuffle tree); 0 for a degenerate or non-finite direction, which the combination then skips
+__device__ __forceinline__ void coef_rows(const double* partial, const SlotList& L, double* sc)
+{
+    const int nw = blockDim.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x >> 5; k < L.n; k += nw) {
+        double v = 0.0;
+        for (int i = lane; i < kRed; i += 32) v += __ldcg(partial + k * kRed + i);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) {
+            double pq = sc[F_PQ + L.s[k]];
+            double c = (pq > 0.0 && isfinite(pq)) ? v / pq : 0.0;
+            sc[F_C + k] = isfinite(c) ? c : 0.0;
+        }
+    }
+}
+
+
 __global__ void k_finv(const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ diag,
                        int64_t n, double* __restrict__ minv)
 {
@@ -1272,7 +1319,8 @@ __global__ void __launch_bounds__(256)
 k_fgather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
           const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ fe,
           const double* __restrict__ p, const double* __restrict__ r, int64_t n, double* __restrict__ q,
-          double* __restrict__ partial)
+          double* __restrict__ partial, double* __restrict__ sc, int slot, int dd,
+          unsigned int* __restrict__ counter)
 {
     __shared__ double sh[32];
     double pq = 0.0, rp = 0.0;
@@ -1293,13 +1341,22 @@ k_fgather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr, con
         partial[blockIdx.x] = s1;
         partial[kRed + blockIdx.x] = s2;
     }
+    if (last_block(counter)) { // P.Q and the step length alpha_dd = r.P / P.Q (0 if degenerate)
+        const double tpq = block_sum_partials(partial, sh);
+        const double trp = block_sum_partials(partial + kRed, sh);
+        if (threadIdx.x == 0) {
+            sc[F_PQ + slot] = tpq;
+            double a = (tpq > 0.0 && isfinite(tpq)) ? trp / tpq : 0.0;
+            sc[F_A0 + dd] = isfinite(a) ? a : 0.0;
+        }
+    }
 }
 
 // r1 = r - alpha_0 q0 (the residual after the step along the first direction of the iteration);
 // partial r1.r1
 __global__ void __launch_bounds__(256)
-k_resid1(const double* __restrict__ r, const double* __restrict__ q0, const double* __restrict__ sc,
-         int64_t n, double* __restrict__ r1, double* __restrict__ partial)
+k_resid1(const double* __restrict__ r, const double* __restrict__ q0, double* __restrict__ sc,
+         int64_t n, double* __restrict__ r1, double* __restrict__ partial, unsigned int* __restrict__ counter)
 {
     __shared__ double sh[32];
     const double a0 = sc[F_A0];
@@ -1312,6 +1369,10 @@ k_resid1(const double* __restrict__ r, const double* __restrict__ q0, const doub
     }
     double s = bsum(rr, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
+    if (last_block(counter)) {
+        const double t = block_sum_partials(partial, sh);
+        if (threadIdx.x == 0) sc[F_R1] = t;
+    }
 }
 
 // sc[dst.s[k]] = sum of partial row k (fixed order)
@@ -1327,49 +1388,13 @@ __global__ void k_fredv(const double* __restrict__ partial, SlotList dst, double
     }
 }
 
-// Coefficient c_k = (z.Q_j) / (P_j.Q_j) of basis entry k (slot j = L.s[k]) from partial row k:
-// warp k sums its row (fixed order: lane-strided, then the shuffle tree); 0 for a degenerate or
-// non-finite direction, which the combination then skips. Launch: 32 warps.
-__global__ void k_fred_coef(const double* __restrict__ partial, SlotList L, double* __restrict__ sc)
-{
-    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (k >= L.n) return;
-    double v = 0.0;
-    for (int i = lane; i < kRed; i += 32) v += partial[k * kRed + i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) {
-        double pq = sc[F_PQ + L.s[k]];
-        double c = (pq > 0.0 && isfinite(pq)) ? v / pq : 0.0;
-        sc[F_C + k] = isfinite(c) ? c : 0.0;
-    }
-}
-
-// rows 0, 1 = P.Q, r.P of new direction d in slot `slot`: stores P.Q and the step length
-// alpha_d = r.P / P.Q (0 for a degenerate or non-finite direction, which then takes no step)
-__global__ void k_fred_dir(const double* __restrict__ partial, int slot, int d, double* __restrict__ sc)
-{
-    __shared__ double sh[32];
-    double v0 = 0.0, v1 = 0.0;
-    for (int i = threadIdx.x; i < kRed; i += blockDim.x) {
-        v0 += partial[i];
-        v1 += partial[kRed + i];
-    }
-    double pq = bsum(v0, sh);
-    double rp = bsum(v1, sh);
-    if (threadIdx.x == 0) {
-        sc[F_PQ + slot] = pq;
-        double a = (pq > 0.0 && isfinite(pq)) ? rp / pq : 0.0;
-        sc[F_A0 + d] = isfinite(a) ? a : 0.0;
-    }
-}
-
 // partial dots z.Q_j for the basis slots (z = minv * r when zin is null); NS >= L.n. Vectors
 // are read as double2 (n even, slots 256-byte aligned).
 template <int NS>
 __global__ void __launch_bounds__(256)
 k_mdot(const double* __restrict__ zin, const double* __restrict__ minv, const double* __restrict__ r,
-       const double* __restrict__ Q, int64_t ld, SlotList L, int64_t n, double* __restrict__ partial)
+       const double* __restrict__ Q, int64_t ld, SlotList L, int64_t n, double* __restrict__ partial,
+       double* __restrict__ sc, unsigned int* __restrict__ counter)
 {
     __shared__ double sh[32];
     double acc[NS];
@@ -1413,6 +1438,7 @@ k_mdot(const double* __restrict__ zin, const double* __restrict__ minv, const do
             if (threadIdx.x == 0) partial[j * kRed + blockIdx.x] = v;
         }
     }
+    if (last_block(counter)) coef_rows(partial, L, sc);
 }
 
 // P_new = z - sum_k c_k P_{L.s[k]} (A-orthogonalisation with the precomputed coefficients),
@@ -1467,8 +1493,8 @@ k_mcombine(const double* __restrict__ zin, const double* __restrict__ minv,
 __global__ void __launch_bounds__(256)
 k_mupdate(const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ P,
           const double* __restrict__ Q, int64_t ld, int s0, int s1, int ndir,
-          const double* __restrict__ sc, int64_t n, double* __restrict__ x, double* __restrict__ r,
-          double* __restrict__ partial)
+          double* __restrict__ sc, int64_t n, double* __restrict__ x, double* __restrict__ r,
+          double* __restrict__ partial, unsigned int* __restrict__ counter)
 {
     __shared__ double sh[32];
     double a0 = sc[F_A0], a1 = ndir > 1 ? sc[F_A1] : 0.0;
@@ -1496,6 +1522,10 @@ k_mupdate(const int32_t* __restrict__ part, int64_t nnu, const double* __restric
     }
     double v = bsum(rr, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = v;
+    if (last_block(counter)) {
+        const double t = block_sum_partials(partial, sh);
+        if (threadIdx.x == 0) sc[F_RR] = t;
+    }
 }
 
 // launch k_mdot / k_mcombine with the smallest slot-count instantiation that holds L.n
@@ -1514,9 +1544,10 @@ inline void with_ns(int n, A&&... a)
 template <int NS>
 struct MdotL {
     static void go(unsigned g, cudaStream_t st, const double* zin, const double* minv, const double* r,
-                   const double* Q, int64_t ld, const SlotList& L, int64_t n, double* partial)
+                   const double* Q, int64_t ld, const SlotList& L, int64_t n, double* partial, double* sc,
+                   unsigned int* counter)
     {
-        k_mdot<NS><<<g, 256, 0, st>>>(zin, minv, r, Q, ld, L, n, partial);
+        k_mdot<NS><<<g, 256, 0, st>>>(zin, minv, r, Q, ld, L, n, partial, sc, counter);
     }
 };
 
@@ -1530,6 +1561,7 @@ struct McombineL {
 };
 
 struct FcgWs {
+    unsigned int* cnt; // last-block counters: [0] dots, [1] gather, [2] update, [3] resid1
     double *fe, *r, *z, *minv, *P, *Q, *partial, *sc;
     int64_t ld;
     __nv_bfloat16 *a1, *a2, *a3, *wt1, *wt2, *wt0, *wt3;
@@ -1582,6 +1614,8 @@ inline FcgWs carve_fcg(const gfgpu_verlet_desc* d, int64_t hw, int nslots, void*
     c += a256(int64_t(kMaxSlots) * kRed * 8);
     w.sc = reinterpret_cast<double*>(c);
     c += a256(F_COUNT * 8);
+    w.cnt = reinterpret_cast<unsigned int*>(c);
+    c += 256;
     carve_nn(c, hw, &w.a1, &w.a2, &w.a3, &w.wt1, &w.wt2, &w.wt0, &w.wt3);
     return w;
 }
@@ -1590,7 +1624,7 @@ inline int64_t fcg_bytes(const gfgpu_verlet_desc* d, int64_t hw, int nslots)
 {
     int64_t n = d->nnode * d->ndim;
     return a256(d->nelem * d->nne * d->ndim * 8) + (3 + 2 * int64_t(nslots)) * a256(n * 8) +
-           a256(int64_t(kMaxSlots) * kRed * 8) + a256(F_COUNT * 8) + nn_bytes(hw);
+           a256(int64_t(kMaxSlots) * kRed * 8) + a256(F_COUNT * 8) + 256 + nn_bytes(hw);
 }
 
 // the tensor-core layers' weights in their shared-memory layouts
@@ -1944,8 +1978,7 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
                 // the network sees the residual left after the step along the two-level direction
                 // (zc is free again: its direction is stored in slot c0 % nslots)
                 const double* q0 = w.Q + static_cast<int>(c0 % nslots) * w.ld;
-                k_resid1<<<gb, 256, 0, st>>>(w.r, q0, w.sc, n, zc, w.partial);
-                k_fredv<<<1, 1024, 0, st>>>(w.partial, one(F_R1), w.sc);
+                k_resid1<<<gb, 256, 0, st>>>(w.r, q0, w.sc, n, zc, w.partial, w.cnt + 3);
                 GF_TRY(nn_apply(nn, zc, w.sc, F_R1, nfree, d->part, d->nnu, w, w.z, st));
                 zin = w.z;
             }
@@ -1954,25 +1987,23 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
                 zin = w.z;
             }
             if (L.n > 0) {
-                with_ns<MdotL>(L.n, gb, st, zin, w.minv, w.r, w.Q, w.ld, L, n, w.partial);
-                k_fred_coef<<<1, 32 * kMaxSlots, 0, st>>>(w.partial, L, w.sc);
+                with_ns<MdotL>(L.n, gb, st, zin, w.minv, w.r, w.Q, w.ld, L, n, w.partial, w.sc, w.cnt);
             }
             with_ns<McombineL>(L.n, grid_for(n / 2), st, zin, w.minv, w.r, w.sc, w.P, w.ld, L, snew, n);
             double* Pn = w.P + snew * w.ld;
             double* Qn = w.Q + snew * w.ld;
             GF_TRY(gfgpu_internal_element_forces(d, Pn, w.fe, st));
             k_fgather<<<gb, 256, 0, st>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, Pn,
-                                          w.r, n, Qn, w.partial);
-            k_fred_dir<<<1, 1024, 0, st>>>(w.partial, snew, dd, w.sc);
+                                          w.r, n, Qn, w.partial, w.sc, snew, dd, w.cnt + 1);
         }
         k_mupdate<<<gb, 256, 0, st>>>(d->part, d->nnu, w.P, w.Q, w.ld, static_cast<int>(c0 % nslots),
                                       static_cast<int>((c0 + 1) % nslots), ndir, w.sc, n, x, w.r,
-                                      w.partial);
-        k_fredv<<<1, 1024, 0, st>>>(w.partial, one(F_RR), w.sc);
+                                      w.partial, w.cnt + 2);
         return check_launch("fcg iteration");
     };
 
     if (nn) nn_prepare_weights(nn, w.wt1, w.wt2, w.wt0, w.wt3, s);
+    GF_TRY(check_cuda(cudaMemsetAsync(w.cnt, 0, 256, s), "cudaMemsetAsync"));
     k_finv<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, diag, n, w.minv);
     // ||b||, b = -(A x_p)_u (P slot 0 as scratch)
     k_fkeep<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.P);
