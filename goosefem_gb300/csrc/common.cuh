@@ -73,6 +73,30 @@ __device__ __forceinline__ double madd(double a, double b, double c)
     else return fma(a, b, c);
 }
 
+// Element forces of dof t summed in the dof CSR's order (ascending flat elemvec index), from 0.
+// On a Regular Quad4 mesh with plain dofs (reg_nx > 0, set by gfgpu_verlet_detect_regular) the
+// contributing elements are found by index arithmetic in the same order: same bits, no tables.
+__device__ __forceinline__ double gather_dof(int64_t t, const int32_t* __restrict__ dofs,
+                                             const int32_t* __restrict__ ptr,
+                                             const int32_t* __restrict__ idx,
+                                             const double* __restrict__ fe, int64_t reg_nx, int64_t reg_ny)
+{
+    double f = 0.0;
+    if (reg_nx > 0) {
+        const int64_t node = t >> 1, i = t & 1, W = reg_nx + 1;
+        const int64_t iy = node / W, ix = node - iy * W;
+        if (iy > 0 && ix > 0) f += __ldg(fe + (((iy - 1) * reg_nx + ix - 1) * 4 + 2) * 2 + i);
+        if (iy > 0 && ix < reg_nx) f += __ldg(fe + (((iy - 1) * reg_nx + ix) * 4 + 3) * 2 + i);
+        if (iy < reg_ny && ix > 0) f += __ldg(fe + ((iy * reg_nx + ix - 1) * 4 + 1) * 2 + i);
+        if (iy < reg_ny && ix < reg_nx) f += __ldg(fe + ((iy * reg_nx + ix) * 4 + 0) * 2 + i);
+        return f;
+    }
+    const int32_t d = __ldg(dofs + t);
+    const int32_t b = __ldg(ptr + d), e = __ldg(ptr + d + 1);
+    for (int32_t j = b; j < e; ++j) f += __ldg(fe + __ldg(idx + j));
+    return f;
+}
+
 inline bool too_big(int64_t n)
 {
     return n < 0 || n > INT32_MAX;

@@ -72,11 +72,25 @@ class ElasticStatic:
             _lib.call("gfgpu_verlet_precompute", C.addressof(d), self.coef.data_ptr(),
                       _dev.stream())
             d.coef = self.coef.data_ptr()
+        # Mesh::Quad4::Regular numbering with plain dofs: the operator's gather by index
+        # arithmetic (gfgpu_verlet_detect_regular, checked on the device; same bits as the CSR)
+        if nne == 4 and nd == 2:
+            y = np.asarray(coor)[:, 1]
+            run = int(np.argmax(y != y[0])) if np.any(y != y[0]) else y.size
+            nx = run - 1
+            if nx > 0 and nelem % nx == 0:
+                _lib.call("gfgpu_verlet_detect_regular", C.addressof(d), nx, nelem // nx,
+                          _dev.stream())
         nbytes = int(_lib.lib().gfgpu_pcg_workspace_bytes(C.addressof(d)))
         self.ws = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device=_dev.device())
         self.diag = torch.empty((nnode, nd), dtype=torch.float64, device=_dev.device())
         _lib.call("gfgpu_elastic_diagonal", C.addressof(d), self.diag.data_ptr(),
                   self.ws.data_ptr(), _dev.stream())
+
+    def use_csr_gather(self):
+        """Gather the operator's element forces through the dof CSR even on a Regular mesh."""
+        self.desc.reg_nx = 0
+        self.desc.reg_ny = 0
 
     @property
     def uniform(self):

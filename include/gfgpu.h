@@ -321,8 +321,9 @@ typedef struct {
     const double* mclass_inv;  /* [ncls] host */
     int32_t ncls;
     /* Quad4 Mesh::Quad4::Regular(reg_nx, reg_ny) numbering with dofs = node * 2 + i, verified
-     * on the device by gfgpu_verlet_detect_regular: the node kernel then finds the <= 4 element
-     * forces of a node by index arithmetic instead of the CSR (same summation order, same bits).
+     * on the device by gfgpu_verlet_detect_regular: the node kernel and the static solvers'
+     * operator (gfgpu_pcg_*, gfgpu_fcg_*, gfgpu_coarse_setup) then find the <= 4 element forces of
+     * a node by index arithmetic instead of the CSR (same summation order, same bits).
      * 0 = use the CSR. */
     int64_t reg_nx, reg_ny;
 } gfgpu_verlet_desc;
@@ -353,7 +354,7 @@ int gfgpu_verlet_classify(gfgpu_verlet_desc* d, uint8_t* mclass, double* mclass_
                           gfgpu_stream_t stream);
 /* Checks on the device that conn is MeshQuad4.h:87-126's Regular(nx, ny) connectivity and
  * dofs = arange(nnode * 2) (no periodic ties); on success sets d->reg_nx, d->reg_ny, else leaves
- * them 0. Returns GFGPU_OK either way. Synchronises. */
+ * them 0. Needs only d's sizes, conn and dofs. Returns GFGPU_OK either way. Synchronises. */
 int gfgpu_verlet_detect_regular(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, gfgpu_stream_t stream);
 /* Advance nsteps increments; u, v, a are nodevec [nnode, ndim] device arrays updated in place.
  * Strict mode (gfgpu_set_strict) with the general path reproduces the reference's operation

@@ -173,3 +173,45 @@ def test_hex8_cube_coefficients_match_uniform_kernel(gf, oracle):
     f_r = R.assemble_node(conn, dofs, R.int_grad_n_dot_tensor2_dv(dNx, vol, R.elastic_stress(
         eps, K, G)))
     assert rel_err(f_cube, f_r) <= RTOL
+
+
+@pytest.mark.parametrize("uniform", ["auto", False])
+def test_regular_gather_same_bits_as_csr(gf, oracle, uniform):
+    """On a Regular Quad4 mesh the static operator gathers element forces by index arithmetic
+    (detected on the device); the Jacobi-PCG iterates are bit-identical to the dof-CSR gather's,
+    and so are the flexible CG's with the two-level correction."""
+    from goosefem_gb300 import learned as LR
+
+    R = oracle
+    nx, ny = 37, 22
+    coor, conn = R.quad4_regular(nx, ny)
+    K, G = seeded_material(conn.shape[0], 45)
+    bot = np.arange(nx + 1)
+    top = bot + ny * (nx + 1)
+    iip = np.unique(np.concatenate([(bot[:, None] * 2 + np.arange(2)).ravel(), top * 2 + 1]))
+    xp = np.where(np.isin(iip, top * 2 + 1), -1e-2, 0.0)
+    out = []
+    for csr in (False, True):
+        dofs = np.arange(coor.shape[0] * 2).reshape(-1, 2)
+        st = gf.statics.ElasticStatic(coor, conn, dofs, K, G, iip, uniform=uniform)
+        assert st.desc.reg_nx == nx
+        if csr:
+            st.use_csr_gather()
+        x = torch.zeros(coor.shape[0] * 2, dtype=torch.float64, device="cuda")
+        x[torch.as_tensor(iip, device="cuda").long()] = torch.as_tensor(xp, device="cuda")
+        xv = x.view(-1, 2).clone()
+        it = st.solve(xv, tol=1e-10)
+        out.append((it, to_np(xv)))
+    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
+    # the flexible CG (two-level) through the learned-preconditioner object
+    res = []
+    for csr in (False, True):
+        lp = LR.LearnedPreconditioner(nx, ny, K, G, iip, seed=0)
+        assert lp.static.desc.reg_nx == nx
+        if csr:
+            lp.static.use_csr_gather()
+        lp.coarse_setup(8)
+        xx = lp.initial_guess(xp)
+        lp.fcg(xx, use_nn=False, nkeep=2, coarse=True)
+        res.append(to_np(xx))
+    assert np.array_equal(res[0], res[1])
