@@ -56,6 +56,10 @@ def parse():
     p.add_argument("--nloads", type=int, default=64)
     p.add_argument("--train-steps", type=int, default=6000)
     p.add_argument("--hc", type=int, default=16, help="learned workload: coarse-grid spacing (nodes)")
+    p.add_argument("--cheb-degree", type=int, default=8,
+                   help="learned workload: degree of the Chebyshev smoother the network is trained to "
+                        "reproduce (its support radius in nodes; the network's receptive field radius is 8)")
+    p.add_argument("--margin", type=int, default=8, help="learned workload: crop margin of the loss")
     p.add_argument("--nn-path", type=int, default=0,
                    help="learned workload: tensor-core form of the network's 32->32 layers "
                         "(gfgpu_set_nn_tensor_path: 0 mma.sync, 1 tcgen05, 2 tcgen05 + TMA pipeline)")
@@ -603,11 +607,11 @@ def run_learned(args):
                           key=lambda v: v["seconds"])
     t0 = time.perf_counter()
     npairs = lp.make_pairs_twolevel(nloads=args.nloads, snaps=48, every=4, target="cheb",
-                                    degree=8, post=True)
+                                    degree=args.cheb_degree, post=True)
     torch.cuda.synchronize()
     t_pairs = time.perf_counter() - t0
     t0 = time.perf_counter()
-    losses = lp.train(steps=args.train_steps, batch=32, crop=96, margin=8, lr=2e-3,
+    losses = lp.train(steps=args.train_steps, batch=32, crop=96, margin=args.margin, lr=2e-3,
                       log_every=max(args.train_steps // 10, 1))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
@@ -649,9 +653,10 @@ def run_learned(args):
             "config": {"workload": f"Quad4 Regular {nx}x{nx}, two-phase (inclusions "
                                    f"{100 * inside.mean():.1f}% area, x10 moduli), bottom fixed, "
                                    "top uy=-1e-2", "coarse_spacing": args.hc, "pairs": npairs,
-                       "train_steps": args.train_steps, "crop": 96,
+                       "train_steps": args.train_steps, "crop": 96, "margin": args.margin,
+                       "chebyshev_degree": args.cheb_degree,
                        "residual_check": "learned every 4 iterations; two-level best of 4, 8, 16",
-                       "target": "Chebyshev-8 smoother minus Jacobi step, on the residual after "
+                       "target": "Chebyshev smoother minus Jacobi step, on the residual after "
                                  "the two-level step", "loss": "energy norm",
                        "directions_kept": [1, 2, 4], "nn_tensor_path": args.nn_path},
             "solvers": res,

@@ -1744,10 +1744,10 @@ inline int prepare_mma(cudaStream_t)
                                            static_cast<int>(mma_smem_bytes(4))),
                       "cudaFuncSetAttribute"));
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv_mma<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(mma_smem_bytes(4, 1))),
+                                           static_cast<int>(mma_smem_bytes(dil_of(3), 1))),
                       "cudaFuncSetAttribute"));
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv_mma<1, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(mma_smem_bytes(4, 1))),
+                                           static_cast<int>(mma_smem_bytes(dil_of(3), 1))),
                       "cudaFuncSetAttribute"));
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_tcp<kTcpRPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(std::max(tcp_smem_bytes(dil_of(1)),
