@@ -55,7 +55,7 @@ def parse():
     p.add_argument("--n2d", type=int, default=512)
     p.add_argument("--nloads", type=int, default=64)
     p.add_argument("--train-steps", type=int, default=6000)
-    p.add_argument("--hc", type=int, default=16, help="learned workload: coarse-grid spacing (nodes)")
+    p.add_argument("--hc", type=int, default=12, help="learned workload: coarse-grid spacing (nodes)")
     p.add_argument("--cheb-degree", type=int, default=8,
                    help="learned workload: degree of the Chebyshev smoother the network is trained to "
                         "reproduce (its support radius in nodes; the network's receptive field radius is 8)")
