@@ -1692,8 +1692,9 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
         GF_TRY(tcp_tensor_map(&m1, a1, H, W, dil_of(1)));
         GF_TRY(tcp_tensor_map(&m2, a2, H, W, dil_of(2)));
         const int ntiles = ((W + kTcM - 1) / kTcM) * ((H + kTcpRPC - 1) / kTcpRPC);
-        int sms = 0;
-        GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0), "cudaDeviceGetAttribute"));
+        int sms = 0, dev = 0;
+        GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+        GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
         const unsigned g = static_cast<unsigned>(std::max(1, std::min(ntiles, sms)));
         k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(1)), s>>>(
             m1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
