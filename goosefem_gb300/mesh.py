@@ -35,15 +35,72 @@ def coordination(conn, nnode=None):
     return out
 
 
-def elem2node(conn, nnode=None):
-    """Mesh::elem2node, sorted (Mesh.h:2485-2513): list of element lists per node."""
+def elem2node(conn, dofs=None, nnode=None):
+    """Mesh::elem2node, sorted (Mesh.h:2485-2513): list of element lists per node. With `dofs`
+    (Mesh.h:2517-2548) the lists of nodes tied by periodicity (nodes sharing their dofs) are
+    merged, sorted, and given to every node of the tie."""
     conn = np.ascontiguousarray(conn, dtype=np.int32)
+    if dofs is not None and nnode is None:
+        nnode = np.asarray(dofs).shape[0]
     nnode = int(conn.max()) + 1 if nnode is None else nnode
     ptr = np.empty(nnode + 1, dtype=np.int32)
     idx = np.empty(conn.size, dtype=np.int32)
     _lib.call("gfgpu_host_elem2node", conn.ctypes.data, conn.shape[0], conn.shape[1], nnode,
               ptr.ctypes.data, idx.ctypes.data)
-    return [list(idx[ptr[i]:ptr[i + 1]]) for i in range(nnode)]
+    ret = [list(idx[ptr[i]:ptr[i + 1]]) for i in range(nnode)]
+    if dofs is None:
+        return ret
+    ties = nodaltyings(dofs)
+    for m in range(nnode):
+        t = ties[m]
+        if len(t) <= 1 or m > t[0]:
+            continue
+        merged = sorted(ret[m] + [e for j in t[1:] for e in ret[j]])
+        ret[m] = merged
+        for j in t[1:]:
+            ret[j] = list(merged)
+    return ret
+
+
+def node2dof(dofs):
+    """Mesh::node2dof (Mesh.h:2557-2560): the nodes of every dof, sorted."""
+    return elem2node(dofs)
+
+
+def nodaltyings(dofs):
+    """Mesh::nodaltyings (Mesh.h:2840-2862): for every node the sorted list of nodes that share
+    its dofs (itself included)."""
+    d = np.asarray(dofs)
+    nodemap = node2dof(d)
+    return [sorted(nodemap[int(d[m, 0])]) for m in range(d.shape[0])]
+
+
+def nodal_mass(coor, conn):
+    """Mesh::nodal_mass (Mesh.h:2708-2752): lumped mass of unit density per node and component,
+    through the device path (nodal quadrature, Int_N_scalar_NT_dV, MatrixDiagonal)."""
+    from .element import Hex8 as _H, Quad4 as _Q
+    from .matrix import MatrixDiagonal
+    from .vector import Vector
+
+    coor = np.asarray(coor, dtype=np.float64)
+    conn = np.asarray(conn)
+    d = dofs(coor.shape[0], coor.shape[1])
+    E = {(4, 2): _Q, (8, 3): _H}.get((conn.shape[1], coor.shape[1]))
+    if E is None:
+        raise RuntimeError("Element-type not implemented")
+    vec = Vector(conn, d)
+    quad = E.Quadrature(vec.AsElement(coor), E.Nodal.xi(), E.Nodal.w())
+    M = MatrixDiagonal(conn, d)
+    M.assemble(quad.Int_N_scalar_NT_dV(np.ones(conn.shape)))
+    return vec.AsNode(M.data())
+
+
+def center_of_gravity(coor, conn):
+    """Mesh::center_of_gravity (Mesh.h:2826-2831): the mass-weighted average of the nodal
+    coordinates (unit density)."""
+    coor = np.asarray(coor, dtype=np.float64)
+    w = nodal_mass(coor, conn).cpu().numpy()
+    return (coor * w).sum(axis=0) / w.sum(axis=0)
 
 
 def partition(dofs_, iip):

@@ -1,4 +1,5 @@
-"""Extract the known-answer arrays of GooseFEM's own C++ test-suite into a JSON fixture.
+"""Extract the known-answer arrays of GooseFEM's own test-suite (C++ and Python) into a JSON
+fixture.
 
 Run in a checkout that has the GooseFEM sources (the fixture is committed, so the
 tests never need the sources at run time):
@@ -9,6 +10,7 @@ The script reads the test files as text and copies the brace-initialised literal
 arrays named below; it does not compile or execute anything from the reference.
 """
 
+import ast
 import json
 import os
 import re
@@ -84,6 +86,24 @@ def extract(root):
         e2n[int(k)] = [int(v) for v in vals.split(",")]
     out["quad4_3x3_elem2node"] = {"source": f"{rel}:{text.count(chr(10), 0, s0) + 1}",
                                   "value": e2n}
+
+    # the Python test-suite (tests/test_Mesh.py): the literal expected values of four tests on
+    # Quad4 Regular(4, 4) with periodic dofs and one on Regular(3, 3), read with ast (parsed,
+    # never executed)
+    rel = "tests/test_Mesh.py"
+    with open(os.path.join(root, rel)) as f:
+        tree = ast.parse(f.read())
+    wanted_py = {"test_center_of_gravity": "quad4_3x3_center_of_gravity",
+                 "test_coordination_dofs": "quad4_4x4_coordination_dofsPeriodic",
+                 "test_coordination_node2dof": "quad4_4x4_node2dof",
+                 "test_coordination_nodaltyings": "quad4_4x4_nodaltyings",
+                 "test_elem2node_periodic": "quad4_4x4_elem2node_periodic"}
+    for fn in ast.walk(tree):
+        if isinstance(fn, ast.FunctionDef) and fn.name in wanted_py:
+            lists = [n for n in ast.walk(fn) if isinstance(n, ast.List)]
+            outer = max(lists, key=lambda n: len(ast.dump(n)))  # the largest literal
+            out[wanted_py[fn.name]] = {"source": f"{rel}:{outer.lineno}",
+                                       "value": ast.literal_eval(outer)}
     return out
 
 

@@ -243,3 +243,18 @@ def test_coarse_grid_matches_oracle(lib, nx, ny, hc):
     assert g.rlx == 1.0 / (X[-1] - X[-2]) and g.rly == 1.0 / (Y[-1] - Y[-2])
     with pytest.raises(lib.GFGPUError):
         lib.call("gfgpu_coarse_grid", nx, ny, 0, C.addressof(g))
+
+
+def test_mesh_tyings_utilities_against_reference_kat(lib):
+    """tests/test_Mesh.py of the reference (Quad4 Regular(4, 4), periodic dofs): coordination of
+    the dofs, node2dof, nodaltyings and the periodic elem2node (host set-up)."""
+    import goosefem_gb300 as gf
+
+    mesh = gf.Mesh.Quad4.Regular(4, 4)
+    dofs = mesh.dofsPeriodic()
+    real = np.array(KAT["quad4_4x4_coordination_dofsPeriodic"]["value"]).ravel()
+    assert np.array_equal(gf.Mesh.coordination(dofs), real)
+    assert gf.Mesh.node2dof(dofs) == KAT["quad4_4x4_node2dof"]["value"]
+    assert gf.Mesh.nodaltyings(dofs) == KAT["quad4_4x4_nodaltyings"]["value"]
+    real = np.sort(np.array(KAT["quad4_4x4_elem2node_periodic"]["value"]), axis=1)
+    assert np.array_equal(np.array(gf.Mesh.elem2node(mesh.conn(), dofs)), real)

@@ -268,3 +268,13 @@ def test_vector_assemble_dofs_of_periodic_gradient(gf):
     assert F.numel() == n and np.allclose(to_np(F), 0.0, rtol=0, atol=1e-12)
     F = vec.AssembleDofs(vec.AsElement(F_NODE))
     assert F.numel() == n and np.allclose(to_np(F), 0.0, rtol=0, atol=1e-12)
+
+
+def test_mesh_center_of_gravity(gf):
+    """tests/test_Mesh.py test_center_of_gravity: Quad4 Regular(3, 3) -> [1.5, 1.5] (the nodal
+    masses through the device lumped-mass path); a Hex8 box likewise."""
+    mesh = gf.Mesh.Quad4.Regular(3, 3)
+    assert np.allclose(gf.Mesh.center_of_gravity(mesh.coor(), mesh.conn()),
+                       KAT["quad4_3x3_center_of_gravity"]["value"])
+    h = gf.Mesh.Hex8.Regular(2, 3, 4)
+    assert np.allclose(gf.Mesh.center_of_gravity(h.coor(), h.conn()), [1.0, 1.5, 2.0])
