@@ -258,3 +258,33 @@ def test_mesh_tyings_utilities_against_reference_kat(lib):
     assert gf.Mesh.nodaltyings(dofs) == KAT["quad4_4x4_nodaltyings"]["value"]
     real = np.sort(np.array(KAT["quad4_4x4_elem2node_periodic"]["value"]), axis=1)
     assert np.array_equal(np.array(gf.Mesh.elem2node(mesh.conn(), dofs)), real)
+
+
+def test_quad4_regular_node_sets_reference_python_test(lib):
+    """tests/test_MeshQuad4.py test_Regular of the reference: Regular(3, 3) connectivity from the
+    node grid, the edges, open edges, corners and their aliases."""
+    import goosefem_gb300 as gf
+
+    mesh = gf.Mesh.Quad4.Regular(3, 3)
+    nodes = np.arange(16).reshape(4, 4)
+    conn = np.hstack([nodes[:-1, :-1].reshape(-1, 1), nodes[:-1, 1:].reshape(-1, 1),
+                      nodes[1:, 1:].reshape(-1, 1), nodes[1:, :-1].reshape(-1, 1)])
+    x, y = np.meshgrid(np.arange(4.0), np.arange(4.0))
+    assert np.allclose(mesh.coor(), np.stack([x.ravel(), y.ravel()], axis=1))
+    assert np.array_equal(mesh.conn(), conn)
+    assert np.array_equal(mesh.nodesLeftEdge(), nodes[:, 0])
+    assert np.array_equal(mesh.nodesRightEdge(), nodes[:, -1])
+    assert np.array_equal(mesh.nodesBottomEdge(), nodes[0, :])
+    assert np.array_equal(mesh.nodesTopEdge(), nodes[-1, :])
+    assert np.array_equal(mesh.nodesLeftOpenEdge(), mesh.nodesLeftEdge()[1:-1])
+    assert np.array_equal(mesh.nodesRightOpenEdge(), mesh.nodesRightEdge()[1:-1])
+    assert np.array_equal(mesh.nodesBottomOpenEdge(), mesh.nodesBottomEdge()[1:-1])
+    assert np.array_equal(mesh.nodesTopOpenEdge(), mesh.nodesTopEdge()[1:-1])
+    assert mesh.nodesBottomLeftCorner() == mesh.nodesBottomEdge()[0]
+    assert mesh.nodesBottomRightCorner() == mesh.nodesBottomEdge()[-1]
+    assert mesh.nodesTopLeftCorner() == mesh.nodesTopEdge()[0]
+    assert mesh.nodesTopRightCorner() == mesh.nodesTopEdge()[-1]
+    assert mesh.nodesLeftBottomCorner() == mesh.nodesBottomLeftCorner()
+    assert mesh.nodesRightBottomCorner() == mesh.nodesBottomRightCorner()
+    assert mesh.nodesLeftTopCorner() == mesh.nodesTopLeftCorner()
+    assert mesh.nodesRightTopCorner() == mesh.nodesTopRightCorner()

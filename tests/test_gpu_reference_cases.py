@@ -278,3 +278,22 @@ def test_mesh_center_of_gravity(gf):
                        KAT["quad4_3x3_center_of_gravity"]["value"])
     h = gf.Mesh.Hex8.Regular(2, 3, 4)
     assert np.allclose(gf.Mesh.center_of_gravity(h.coor(), h.conn()), [1.0, 1.5, 2.0])
+
+
+def test_matrix_partitioned_reference_python_test(gf):
+    """tests/test_MeshPartitioned.py of the reference: MatrixPartitioned and Matrix assembled from
+    the same random symmetric element matrices have the same dense form, and
+    MatrixPartitionedSolver recovers x from A.Dot(x) with x's prescribed values."""
+    mesh = gf.Mesh.Quad4.Regular(2, 2)
+    dofs, iip = mesh.dofs(), np.array([0, 5, 7, 13])
+    rng = np.random.default_rng(17)
+    a = rng.random((mesh.nelem(), 8, 8))
+    a = 0.5 * (a + a.transpose(0, 2, 1))
+    x = rng.random(mesh.nnode() * 2)
+    A = gf.MatrixPartitioned(mesh.conn(), dofs, iip)
+    B = gf.Matrix(mesh.conn(), dofs)
+    A.assemble(a)
+    B.assemble(a)
+    assert np.allclose(to_np(A.Todense()), to_np(B.Todense()))
+    xc = gf.MatrixPartitionedSolver(tol=1e-13).Solve(A, A.Dot(x), x)
+    assert allclose(xc, x)
