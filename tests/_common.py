@@ -29,4 +29,4 @@ def seeded_field(shape, seed, amp=1e-3):
 
 
 def to_np(t):
-    return t.detach().cpu().numpy()
+    return t.detach().cpu().numpy() if hasattr(t, "detach") else np.asarray(t)
