@@ -35,7 +35,7 @@ class VerletDesc(C.Structure):
         ("uniform", C.c_int32), ("hx", C.c_double), ("hy", C.c_double), ("hz", C.c_double),
         ("coef", C.c_void_p),
         ("mclass", C.c_void_p), ("mclass_inv", C.c_void_p), ("ncls", C.c_int32),
-        ("reg_nx", C.c_int64), ("reg_ny", C.c_int64),
+        ("reg_nx", C.c_int64), ("reg_ny", C.c_int64), ("reg_nz", C.c_int64),
     ]
 
 

@@ -201,9 +201,9 @@ __global__ void k_probe(gfgpu_coarse_desc g, int a, int b, int comp, double* __r
 __global__ void k_apply_gather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
                                const int32_t* __restrict__ idx, const int32_t* __restrict__ part,
                                int64_t nnu, const double* __restrict__ fe, int64_t n,
-                               double* __restrict__ q, int64_t reg_nx, int64_t reg_ny)
+                               double* __restrict__ q, RegGrid reg)
 {
-    GF_FOR(t, n) q[t] = part[t] < nnu ? gather_dof(t, dofs, ptr, idx, fe, reg_nx, reg_ny) : 0.0;
+    GF_FOR(t, n) q[t] = part[t] < nnu ? gather_dof(t, dofs, ptr, idx, fe, reg) : 0.0;
 }
 
 // column block of A_c from one probe: row i (coarse node jx, jy) gets v[i] in the column of the
@@ -384,7 +384,7 @@ int gfgpu_coarse_setup(const gfgpu_verlet_desc* d, const gfgpu_coarse_desc* g, f
                                                                         p);
                 GF_TRY(gfgpu_internal_element_forces(d, p, fe, s));
                 k_apply_gather<<<grid_for(n), kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part,
-                                                              d->nnu, fe, n, q, d->reg_nx, d->reg_ny);
+                                                              d->nnu, fe, n, q, reg_grid(d));
                 k_restrict<double><<<g->ncx * g->ncy, kRestrictThreads, 0, s>>>(*g, d->part, d->nnu, q, v);
                 k_probe_scatter<<<grid_for(nc), kBlock, 0, s>>>(*g, a, b, comp, v, A);
             }

@@ -455,6 +455,9 @@ __device__ __forceinline__ void fwht8_nomean(double (&v)[8])
     v[4] = v[0] - v[4];
 }
 
+// SOA: fe stored component-major, fe[(m * 3 + j) * nelem + e] (coalesced stores; the static
+// solvers' Regular-mesh gather reads it so); else fe[e * 24 + m * 3 + j].
+template <bool SOA>
 __global__ void __launch_bounds__(128)
 k_elem_force_hex8_cube(const int32_t* __restrict__ conn, const double* __restrict__ u,
                        const double* __restrict__ coef, int64_t nelem, double* __restrict__ fe)
@@ -551,7 +554,12 @@ k_elem_force_hex8_cube(const int32_t* __restrict__ conn, const double* __restric
                         v[i + h] = a - b;
                     }
 #pragma unroll
-            for (int m = 0; m < 8; ++m) out[m * 3 + j] = v[pos[m]];
+            for (int m = 0; m < 8; ++m) {
+                if constexpr (SOA)
+                    fe[(m * 3 + j) * nelem + e] = v[pos[m]];
+                else
+                    out[m * 3 + j] = v[pos[m]];
+            }
         }
     }
 }
@@ -827,6 +835,25 @@ __global__ void k_check_regular(const int32_t* __restrict__ conn, const int32_t*
     }
 }
 
+// MeshHex8.h:104-130 Regular(nx, ny, nz) connectivity and plain dofs, else *flag = 1
+__global__ void k_check_regular_hex8(const int32_t* __restrict__ conn, const int32_t* __restrict__ dofs,
+                                     int64_t nx, int64_t ny, int64_t nz, int* __restrict__ flag)
+{
+    const int64_t W = nx + 1, A = W * (ny + 1);
+    GF_FOR(e, nx * ny * nz)
+    {
+        const int64_t ez = e / (nx * ny), ey = (e - ez * nx * ny) / nx, ex = e - ez * nx * ny - ey * nx;
+        const int64_t n0 = ez * A + ey * W + ex;
+        const int64_t want[8] = {n0, n0 + 1, n0 + W + 1, n0 + W, n0 + A, n0 + A + 1, n0 + A + W + 1, n0 + A + W};
+        for (int m = 0; m < 8; ++m)
+            if (conn[e * 8 + m] != want[m]) *flag = 1;
+    }
+    GF_FOR(t, A * (nz + 1) * 3)
+    {
+        if (dofs[t] != t) *flag = 1;
+    }
+}
+
 template <bool S>
 __global__ void __launch_bounds__(256)
 k_verlet_node(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
@@ -1038,8 +1065,8 @@ static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, 
                                                                       d->nelem, c, fe);
     }
     else if (d->uniform && d->coef) {
-        k_elem_force_hex8_cube<<<grid_for(d->nelem, 128), 128, 0, s>>>(d->conn, u, d->coef, d->nelem,
-                                                                       fe);
+        k_elem_force_hex8_cube<false><<<grid_for(d->nelem, 128), 128, 0, s>>>(d->conn, u, d->coef,
+                                                                              d->nelem, fe);
     }
     else if (d->uniform) {
         Hex8Uniform c = hex8_uniform_constants(d);
@@ -1068,11 +1095,17 @@ static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, 
     return check_launch("verlet element kernel");
 }
 
-// Element-kernel launch shared with the static solver (pcg.cu).
+// Element-kernel launch shared with the static solvers (pcg.cu, learned.cu, coarse.cu), whose
+// gathers read fe in reg_grid(d)'s layout.
 int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                   cudaStream_t s)
 {
     GF_TRY(check_operator(d));
+    if (reg_grid(d).soa && d->nelem > 0) {
+        k_elem_force_hex8_cube<true><<<grid_for(d->nelem, 128), 128, 0, s>>>(d->conn, u, d->coef,
+                                                                             d->nelem, fe);
+        return check_launch("cube element kernel");
+    }
     return launch_elem(d, u, fe, s);
 }
 
@@ -1194,7 +1227,7 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
         if (st)
             k_verlet_node<true><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
                                                       d->inv, fe, d->fext, n, k, adv, u, v, a);
-        else if (d->mclass && d->mclass_inv && d->ncls > 0 && d->reg_nx > 0)
+        else if (d->mclass && d->mclass_inv && d->ncls > 0 && d->reg_nx > 0 && d->reg_nz == 0 && d->nne == 4)
             k_verlet_node_cls_regular<<<grid_for(d->nnode), kBlock, 0, s>>>(
                 d->reg_nx, d->reg_ny, d->mclass, tab, fe, d->fext, k, adv, u, v, a);
         else if (d->mclass && d->mclass_inv && d->ncls > 0)
@@ -1217,8 +1250,9 @@ int gfgpu_verlet_detect_regular(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, gf
     GF_REQUIRE(d && d->conn && d->dofs, "bad argument"); // only the tables it checks are needed
     d->reg_nx = 0;
     d->reg_ny = 0;
+    d->reg_nz = 0;
     if (!(d->nne == 4 && d->ndim == 2 && nx > 0 && ny > 0 && d->nelem == nx * ny &&
-          d->nnode == (nx + 1) * (ny + 1)))
+          d->nnode == (nx + 1) * (ny + 1) && nx * ny * 8 < INT32_MAX))
         return GFGPU_OK;
     GF_REQUIRE((reinterpret_cast<uintptr_t>(d->conn) & 15u) == 0, "conn must be 16-byte aligned");
     cudaStream_t s = S(stream);
@@ -1238,6 +1272,38 @@ int gfgpu_verlet_detect_regular(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, gf
     if (h == 0) {
         d->reg_nx = nx;
         d->reg_ny = ny;
+    }
+    return GFGPU_OK;
+}
+
+int gfgpu_verlet_detect_regular_hex8(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, int64_t nz,
+                                     gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d && d->conn && d->dofs, "bad argument");
+    d->reg_nx = 0;
+    d->reg_ny = 0;
+    d->reg_nz = 0;
+    if (!(d->nne == 8 && d->ndim == 3 && nx > 0 && ny > 0 && nz > 0 && d->nelem == nx * ny * nz &&
+          d->nnode == (nx + 1) * (ny + 1) * (nz + 1) && nx * ny * nz * 24 < INT32_MAX))
+        return GFGPU_OK;
+    cudaStream_t s = S(stream);
+    int* flag = nullptr;
+    GF_TRY(check_cuda(cudaMalloc(&flag, sizeof(int)), "cudaMalloc"));
+    int h = 1;
+    int rc = check_cuda(cudaMemsetAsync(flag, 0, sizeof(int), s), "cudaMemsetAsync");
+    if (rc == GFGPU_OK) {
+        k_check_regular_hex8<<<grid_for(std::max(nx * ny * nz, d->nnode * 3)), kBlock, 0, s>>>(
+            d->conn, d->dofs, nx, ny, nz, flag);
+        rc = check_launch("detect_regular_hex8");
+    }
+    if (rc == GFGPU_OK) rc = check_cuda(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    if (rc == GFGPU_OK) rc = check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    cudaFree(flag);
+    GF_TRY(rc);
+    if (h == 0) {
+        d->reg_nx = nx;
+        d->reg_ny = ny;
+        d->reg_nz = nz;
     }
     return GFGPU_OK;
 }

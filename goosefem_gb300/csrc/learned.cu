@@ -1295,7 +1295,7 @@ __global__ void __launch_bounds__(256)
 k_fres(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
        const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ fe,
        const double* __restrict__ rhs, int64_t n, double* __restrict__ r, double* __restrict__ partial,
-       int64_t reg_nx, int64_t reg_ny)
+       RegGrid reg)
 {
     __shared__ double sh[32];
     double rr = 0.0;
@@ -1303,7 +1303,7 @@ k_fres(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr, const 
     {
         double rv = 0.0;
         if (part[t] < nnu) {
-            const double f = gather_dof(t, dofs, ptr, idx, fe, reg_nx, reg_ny);
+            const double f = gather_dof(t, dofs, ptr, idx, fe, reg);
             rv = (rhs ? rhs[t] : 0.0) - f;
             rr = fma(rv, rv, rr);
         }
@@ -1319,7 +1319,7 @@ k_fgather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr, con
           const int32_t* __restrict__ part, int64_t nnu, const double* __restrict__ fe,
           const double* __restrict__ p, const double* __restrict__ r, int64_t n, double* __restrict__ q,
           double* __restrict__ partial, double* __restrict__ sc, int slot, int dd,
-          unsigned int* __restrict__ counter, int64_t reg_nx, int64_t reg_ny)
+          unsigned int* __restrict__ counter, RegGrid reg)
 {
     __shared__ double sh[32];
     double pq = 0.0, rp = 0.0;
@@ -1327,7 +1327,7 @@ k_fgather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr, con
     {
         double f = 0.0;
         if (part[t] < nnu) {
-            f = gather_dof(t, dofs, ptr, idx, fe, reg_nx, reg_ny);
+            f = gather_dof(t, dofs, ptr, idx, fe, reg);
             pq = fma(p[t], f, pq);
             rp = fma(r[t], p[t], rp);
         }
@@ -1993,8 +1993,7 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
             double* Qn = w.Q + snew * w.ld;
             GF_TRY(gfgpu_internal_element_forces(d, Pn, w.fe, st));
             k_fgather<<<gb, 256, 0, st>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, Pn,
-                                          w.r, n, Qn, w.partial, w.sc, snew, dd, w.cnt + 1, d->reg_nx,
-                                          d->reg_ny);
+                                          w.r, n, Qn, w.partial, w.sc, snew, dd, w.cnt + 1, reg_grid(d));
         }
         k_mupdate<<<gb, 256, 0, st>>>(d->part, d->nnu, w.P, w.Q, w.ld, static_cast<int>(c0 % nslots),
                                       static_cast<int>((c0 + 1) % nslots), ndir, w.sc, n, x, w.r,
@@ -2009,12 +2008,12 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
     k_fkeep<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.P);
     GF_TRY(gfgpu_internal_element_forces(d, w.P, w.fe, s));
     k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, rhs, n, w.z,
-                              w.partial, d->reg_nx, d->reg_ny);
+                              w.partial, reg_grid(d));
     k_fredv<<<1, 1024, 0, s>>>(w.partial, one(F_BB), w.sc);
     // r = -(A x)_u
     GF_TRY(gfgpu_internal_element_forces(d, x, w.fe, s));
     k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, rhs, n, w.r,
-                              w.partial, d->reg_nx, d->reg_ny);
+                              w.partial, reg_grid(d));
     k_fredv<<<1, 1024, 0, s>>>(w.partial, one(F_RR), w.sc);
     GF_TRY(read_sc());
     double bnorm = std::sqrt(h[F_BB]);
@@ -2086,7 +2085,7 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
     // true residual -(A x)_u
     GF_TRY(gfgpu_internal_element_forces(d, x, w.fe, s));
     k_fres<<<gb, 256, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, rhs, n, w.r,
-                              w.partial, d->reg_nx, d->reg_ny);
+                              w.partial, reg_grid(d));
     k_fredv<<<1, 1024, 0, s>>>(w.partial, one(F_RR), w.sc);
     GF_TRY(read_sc());
     *iters = it;

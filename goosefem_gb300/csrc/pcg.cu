@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(kRedThreads)
 k_pcg_gather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
              const int32_t* __restrict__ idx, const int32_t* __restrict__ part, int64_t nnu,
              const double* __restrict__ fe, const double* __restrict__ p, int64_t n,
-             double* __restrict__ q, double* __restrict__ partial, int64_t reg_nx, int64_t reg_ny)
+             double* __restrict__ q, double* __restrict__ partial, RegGrid reg)
 {
     __shared__ double sh[32];
     double acc = 0.0;
@@ -65,7 +65,7 @@ k_pcg_gather(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr,
     {
         double f = 0.0;
         if (__ldg(part + t) < nnu) {
-            f = gather_dof(t, dofs, ptr, idx, fe, reg_nx, reg_ny);
+            f = gather_dof(t, dofs, ptr, idx, fe, reg);
             acc = fma(p[t], f, acc);
         }
         q[t] = f;
@@ -151,7 +151,7 @@ k_pcg_residual(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr
                const double* __restrict__ fe, const double* __restrict__ b,
                const double* __restrict__ minv, int64_t n, double* __restrict__ r,
                double* __restrict__ z, double* __restrict__ p, double* __restrict__ partial,
-               int64_t reg_nx, int64_t reg_ny)
+               RegGrid reg)
 {
     __shared__ double sh[32];
     double rz = 0.0, rr = 0.0;
@@ -159,7 +159,7 @@ k_pcg_residual(const int32_t* __restrict__ dofs, const int32_t* __restrict__ ptr
     {
         double rv = 0.0, zv = 0.0;
         if (__ldg(part + t) < nnu) {
-            const double f = gather_dof(t, dofs, ptr, idx, fe, reg_nx, reg_ny);
+            const double f = gather_dof(t, dofs, ptr, idx, fe, reg);
             rv = (b ? b[t] : 0.0) - f;
             zv = minv[t] * rv;
             rz = fma(rv, zv, rz);
@@ -292,7 +292,7 @@ static int pcg_iteration(const gfgpu_verlet_desc* d, const PcgWs& w, double* x, 
     const unsigned gb = kRedBlocks;
     GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
     k_pcg_gather<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
-                                             w.p, n, w.q, w.partial, d->reg_nx, d->reg_ny);
+                                             w.p, n, w.q, w.partial, reg_grid(d));
     k_reduce_alpha<<<1, 1024, 0, s>>>(w.partial, w.sc);
     k_pcg_update<<<gb, kRedThreads, 0, s>>>(d->part, d->nnu, w.minv, w.p, w.q, n, w.sc, x, w.r, w.z,
                                              w.partial);
@@ -326,12 +326,12 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
     k_keep_prescribed<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.p);
     if ((rc = gfgpu_internal_element_forces(d, w.p, w.fe, s)) != GFGPU_OK) return fail_out(rc);
     k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
-                                               nullptr, w.minv, n, w.bvec, w.z, nullptr, w.partial, d->reg_nx, d->reg_ny);
+                                               nullptr, w.minv, n, w.bvec, w.z, nullptr, w.partial, reg_grid(d));
     k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_BB);
     // r = b - A x, z = M^-1 r, p = z
     if ((rc = gfgpu_internal_element_forces(d, x, w.fe, s)) != GFGPU_OK) return fail_out(rc);
     k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
-                                               nullptr, w.minv, n, w.r, w.z, w.p, w.partial, d->reg_nx, d->reg_ny);
+                                               nullptr, w.minv, n, w.r, w.z, w.p, w.partial, reg_grid(d));
     k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ); // SC_RZ, SC_RZ_NEW(=rr, overwritten)
     if ((rc = check_launch("pcg set-up")) != GFGPU_OK) return fail_out(rc);
     cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -406,7 +406,7 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
     // true residual of the partitioned system: b_u - A_uu x_u = -(A x)_u, x holding x_p as well
     if ((rc = gfgpu_internal_element_forces(d, x, w.fe, s)) != GFGPU_OK) return fail_out(rc);
     k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
-                                               nullptr, w.minv, n, w.r, w.z, nullptr, w.partial, d->reg_nx, d->reg_ny);
+                                               nullptr, w.minv, n, w.r, w.z, nullptr, w.partial, reg_grid(d));
     k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_RR);
     cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
     if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg final residual")) != GFGPU_OK)
@@ -433,12 +433,12 @@ int gfgpu_pcg_begin(const gfgpu_verlet_desc* d, const double* diag, const double
     k_keep_prescribed<<<grid_for(n), kBlock, 0, s>>>(d->part, d->nnu, x, n, w.p);
     GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
     k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
-                                               rhs, w.minv, n, w.bvec, w.z, nullptr, w.partial, d->reg_nx, d->reg_ny);
+                                               rhs, w.minv, n, w.bvec, w.z, nullptr, w.partial, reg_grid(d));
     k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_BB);
     // r = rhs_u - (A x)_u, z = M^-1 r, p = z
     GF_TRY(gfgpu_internal_element_forces(d, x, w.fe, s));
     k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
-                                               rhs, w.minv, n, w.r, w.z, w.p, w.partial, d->reg_nx, d->reg_ny);
+                                               rhs, w.minv, n, w.r, w.z, w.p, w.partial, reg_grid(d));
     k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ); // SC_RZ = r.z, SC_RZ_NEW = r.r
     k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_RR);
     return check_launch("pcg_begin");

@@ -72,8 +72,17 @@ class ElasticStatic:
             _lib.call("gfgpu_verlet_precompute", C.addressof(d), self.coef.data_ptr(),
                       _dev.stream())
             d.coef = self.coef.data_ptr()
-        # Mesh::Quad4::Regular numbering with plain dofs: the operator's gather by index
-        # arithmetic (gfgpu_verlet_detect_regular, checked on the device; same bits as the CSR)
+        # Mesh::Quad4/Hex8::Regular numbering with plain dofs: the operator's gather by index
+        # arithmetic (gfgpu_verlet_detect_regular(_hex8), checked on the device; same bits as the
+        # CSR)
+        if nne == 8 and nd == 3:
+            c = np.asarray(coor)
+            nxg = int(np.argmax(c[:, 1] != c[0, 1])) if np.any(c[:, 1] != c[0, 1]) else c.shape[0]
+            nyg = int(np.argmax(c[:, 2] != c[0, 2])) // max(nxg, 1) if np.any(c[:, 2] != c[0, 2]) else 0
+            nx, ny = nxg - 1, nyg - 1
+            if nx > 0 and ny > 0 and nelem % (nx * ny) == 0:
+                _lib.call("gfgpu_verlet_detect_regular_hex8", C.addressof(d), nx, ny,
+                          nelem // (nx * ny), _dev.stream())
         if nne == 4 and nd == 2:
             y = np.asarray(coor)[:, 1]
             run = int(np.argmax(y != y[0])) if np.any(y != y[0]) else y.size
@@ -91,6 +100,7 @@ class ElasticStatic:
         """Gather the operator's element forces through the dof CSR even on a Regular mesh."""
         self.desc.reg_nx = 0
         self.desc.reg_ny = 0
+        self.desc.reg_nz = 0
 
     @property
     def uniform(self):

@@ -326,6 +326,11 @@ typedef struct {
      * a node by index arithmetic instead of the CSR (same summation order, same bits).
      * 0 = use the CSR. */
     int64_t reg_nx, reg_ny;
+    /* Hex8 Mesh::Hex8::Regular(reg_nx, reg_ny, reg_nz) numbering with dofs = node * 3 + i,
+     * verified by gfgpu_verlet_detect_regular_hex8: the static solvers' operator gathers a node's
+     * <= 8 element forces by index arithmetic (same order and bits as the CSR). 0 = Quad4 or
+     * CSR. */
+    int64_t reg_nz;
 } gfgpu_verlet_desc;
 
 #define GFGPU_MASS_CLASSES 16
@@ -356,6 +361,11 @@ int gfgpu_verlet_classify(gfgpu_verlet_desc* d, uint8_t* mclass, double* mclass_
  * dofs = arange(nnode * 2) (no periodic ties); on success sets d->reg_nx, d->reg_ny, else leaves
  * them 0. Needs only d's sizes, conn and dofs. Returns GFGPU_OK either way. Synchronises. */
 int gfgpu_verlet_detect_regular(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, gfgpu_stream_t stream);
+/* The same for MeshHex8.h:77-130's Regular(nx, ny, nz) connectivity with dofs = arange(nnode * 3):
+ * sets d->reg_nx, reg_ny, reg_nz on success (used by the static solvers' gather; the explicit
+ * step's node kernels are Quad4 only). Returns GFGPU_OK either way. Synchronises. */
+int gfgpu_verlet_detect_regular_hex8(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, int64_t nz,
+                                     gfgpu_stream_t stream);
 /* Advance nsteps increments; u, v, a are nodevec [nnode, ndim] device arrays updated in place.
  * Strict mode (gfgpu_set_strict) with the general path reproduces the reference's operation
  * order bit for bit; fast mode reassociates the lumped solve (a = inv R - (inv eta) v).
