@@ -110,8 +110,10 @@ def cpu_info():
         return "unknown"
 
 
-def cpu_sample(w, seconds, parallel):
-    """Time the oracle's per-operator explicit loop (the reference algorithm) on the host."""
+def cpu_sample(w, seconds, parallel, serial_seconds=0.0):
+    """Time the oracle's per-operator explicit loop (the reference algorithm) on the host.
+    With serial_seconds > 0 a second sample runs the same loop on one thread (the reference as
+    shipped: its OpenMP pragmas are inert) and (n, t, n1, t1) is returned."""
     from oracle import gfref as R
 
     conn, dofs, coor = w["conn"], w["dofs"], w["coor"]
@@ -138,7 +140,13 @@ def cpu_sample(w, seconds, parallel):
     # as many increments as fit in the requested sample length
     t2 = run(2)
     n = max(1, min(1000, int(seconds / max(t2 / 2.0, 1e-9))))
-    return n, run(n)
+    t = run(n)
+    if serial_seconds <= 0.0:
+        return n, t
+    parallel = False
+    t1 = run(1)
+    n1 = max(1, min(1000, int(serial_seconds / max(t1, 1e-9))))
+    return n, t, n1, run(n1)
 
 
 class ClockSampler:
@@ -415,12 +423,15 @@ def run_gpu(args, rank, world):
             from oracle import gfref as R
 
             threads = R.num_threads(True)
-            n, t = cpu_sample(w, args.cpu_seconds, True)
+            n, t, n1, t1 = cpu_sample(w, args.cpu_seconds, True, serial_seconds=args.cpu_seconds / 2)
             cpu_val = nelem * NIP * n / t
             line["cpu_baseline"] = {
                 "value": cpu_val, "unit": "elem-Gauss-pt/s", "cores": threads, "kind": "port",
                 "sample": f"{n} increments of the oracle's per-operator loop ({t:.1f} s, "
-                          f"{threads} OpenMP threads, {cpu_info()})"}
+                          f"{threads} OpenMP threads, {cpu_info()})",
+                "serial": {"value": nelem * NIP * n1 / t1, "cores": 1,
+                           "sample": f"{n1} increments on one thread ({t1:.1f} s): the reference "
+                                     "as shipped runs serially"}}
         except Exception as ex:  # the baseline never blocks the GPU line
             line["cpu_baseline"] = {"value": None, "unit": "elem-Gauss-pt/s", "cores": threads,
                                     "kind": "port", "sample": f"failed: {ex}"}
