@@ -441,10 +441,11 @@ def run_gpu(args, rank, world):
 
 def static_case(n, seed=3):
     """Hex8 Regular n^3 (h = 1), K ~ U[0.5,1.5], G ~ U[0.25,0.75] per element, z = 0 face fixed,
-    z = top face uz = -1e-2 (ux, uy free)."""
-    from oracle import gfref as R
+    z = top face uz = -1e-2 (ux, uy free). The mesh comes from the package's own Mesh.Hex8."""
+    import goosefem_gb300 as gf
 
-    coor, conn = R.hex8_regular(n, n, n)
+    mesh = gf.Mesh.Hex8.Regular(n, n, n)
+    coor, conn = mesh.coor(), mesh.conn()
     rng = np.random.default_rng(seed)
     K = rng.uniform(0.5, 1.5, n ** 3)
     G = rng.uniform(0.25, 0.75, n ** 3)
