@@ -457,6 +457,36 @@ def static_case(n, seed=3):
     return coor, conn, K, G, iip, xp
 
 
+def network_ms(lp, n):
+    """One network application on the n x n nodal grid (gfgpu_nn_infer: the four layers of the
+    preconditioner's correction), CUDA events over 50 applications after 5 warm-ups."""
+    import ctypes as C
+
+    import torch
+
+    from goosefem_gb300 import _lib
+
+    X0 = torch.randn((n, n, 4), dtype=torch.float32, device="cuda")
+    Y = torch.empty((n, n, 2), dtype=torch.float32, device="cuda")
+    wsi = torch.empty(int(_lib_call_bytes(n, n)) // 8 + 1, dtype=torch.float64, device="cuda")
+    nnd = lp.nn_desc()
+    st = torch.cuda.current_stream()
+
+    def call():
+        _lib.call("gfgpu_nn_infer", C.addressof(nnd), X0.data_ptr(), Y.data_ptr(), wsi.data_ptr(),
+                  st.cuda_stream)
+
+    for _ in range(5):
+        call()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(50):
+        call()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 50
+
+
 def run_static(args):
     """3-d static case: Hex8 128^3 matrix-free Jacobi-PCG to 1e-8 relative residual (FP64).
     One bench step = one full solve from a zero initial guess."""
@@ -600,7 +630,9 @@ def run_learned(args):
                     raise
         torch.cuda.synchronize()
         print(json.dumps({"workload": "learned kernel-share probe (untrained network)",
-                          "config": {"nx": nx, "hc": args.hc, "iterations": k}}), flush=True)
+                          "config": {"nx": nx, "hc": args.hc, "iterations": k,
+                                     "nn_path": args.nn_path},
+                          "network_application_ms": network_ms(lp, nx + 1)}), flush=True)
         return 0
     res = {}
     for name, fn in (("jacobi_pcg", lambda x: lp.jacobi_pcg(x)),
@@ -636,26 +668,7 @@ def run_learned(args):
                                   key=lambda v: v["seconds"])
     for v in res.values():
         v["us_per_iteration"] = 1e6 * v["seconds"] / max(v["iterations"] + v.get("fallback_iterations", 0), 1)
-    # one network application (gfgpu_nn_infer: the same four layers), CUDA events
-    H = W = nx + 1
-    X0 = torch.randn((H, W, 4), dtype=torch.float32, device="cuda")
-    Y = torch.empty((H, W, 2), dtype=torch.float32, device="cuda")
-    wsi = torch.empty(int(_lib_call_bytes(H, W)) // 8 + 1, dtype=torch.float64, device="cuda")
-    nnd = lp.nn_desc()
-    import ctypes as C
-    from goosefem_gb300 import _lib
-    st = torch.cuda.current_stream()
-    call = lambda: _lib.call("gfgpu_nn_infer", C.addressof(nnd), X0.data_ptr(), Y.data_ptr(),  # noqa: E731
-                             wsi.data_ptr(), st.cuda_stream)
-    for _ in range(5):
-        call()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    for _ in range(50):
-        call()
-    e1.record(st)
-    torch.cuda.synchronize()
-    nn_ms = e0.elapsed_time(e1) / 50
+    nn_ms = network_ms(lp, nx + 1)
     jac = min(res["jacobi_pcg"]["seconds"], res["jacobi_pcg_graph"]["seconds"])
     learned = res["learned_twolevel"]
     line = {"metric": "time-to-1e-8 resid (learned two-level FCG vs Jacobi PCG)",

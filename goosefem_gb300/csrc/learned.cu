@@ -843,27 +843,45 @@ k_conv32_tc(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict
 //
 // The same implicit GEMM as k_conv32_tc, as a persistent kernel (one CTA per SM) that overlaps
 // the three stages of consecutive tiles of RPC rows x 128 pixels. Activations in and out are
-// channel-planar, [4][H][W][8] BF16 (each plane contiguous), so that a plane of the halo tile is
-// one TMA box of contiguous 16-byte pixels per row. Warp 0 (one lane) loads the halo tile's 4
-// planes with TMA (cp.async.bulk.tensor, 4-d view [4][H][W][8], box [1][R][C][8], zero fill
-// outside the grid) into one of two shared-memory
-// stages; warp 1 (one lane) issues the 18 RPC MMAs of a tile into one of two TMEM accumulators
+// channel-planar, [4][H][W][8] BF16 (each plane contiguous), so that a row of a plane of the halo
+// tile is contiguous in HBM. Warp 0 loads the halo tile's 4 planes with TMA
+// (cp.async.bulk.tensor) one row at a time: a 2 KB box of 128 pixels and a box of the 2 dil
+// remaining pixels (3-d views [4][H][2W] of 8-byte elements, zero fill outside the grid), each
+// landing at a 128-byte aligned row of a shared-memory stage (rows padded to a multiple of 8
+// pixels), the 8 R copies of a tile spread over the warp's lanes; into one of the 2-4 stages that
+// fit in shared memory,
+// warp 1 (one lane) issues the 18 RPC MMAs of a tile into one of two TMEM accumulators
 // and commits them to the stage's "empty" and the accumulator's "full" mbarrier; warps 2-5 drain
 // an accumulator (tcgen05.ld, bias, ReLU, BF16) while the next tile is multiplied. Every wait is
 // bounded; a role that gives up sets the time-out flag and leaves its loop.
 
 constexpr int kTcpThreads = 192;
-constexpr int kTcpStages = 2;
+constexpr int kTcpMaxStages = 4;
+constexpr size_t kTcpSmemBudget = 232448; // maximum dynamic shared memory of a CTA
 constexpr int kTcpRPC = 4;
+
+// pixels per shared-memory row of the halo tile: C padded to a multiple of 8 (128-byte rows)
+__host__ __device__ constexpr int tcp_row_pixels(int dil)
+{
+    return (tc_cols(dil) + 7) / 8 * 8;
+}
 
 __host__ __device__ constexpr uint32_t tcp_plane_bytes(int dil)
 {
-    return static_cast<uint32_t>((tc_rows(kTcpRPC, dil) * tc_cols(dil) * 16 + 127) / 128 * 128);
+    return static_cast<uint32_t>(tc_rows(kTcpRPC, dil) * tcp_row_pixels(dil) * 16);
+}
+
+// halo-tile stages that fit beside the weights (2 .. kTcpMaxStages)
+__host__ __device__ constexpr int tcp_stages(int dil)
+{
+    return static_cast<int>((kTcpSmemBudget - 1024 - kTcWBytes - 128) / (4 * tcp_plane_bytes(dil))) < kTcpMaxStages
+               ? static_cast<int>((kTcpSmemBudget - 1024 - kTcWBytes - 128) / (4 * tcp_plane_bytes(dil)))
+               : kTcpMaxStages;
 }
 
 inline size_t tcp_smem_bytes(int dil)
 {
-    return 1024 + kTcWBytes + static_cast<size_t>(kTcpStages) * 4 * tcp_plane_bytes(dil) + 128;
+    return 1024 + kTcWBytes + static_cast<size_t>(tcp_stages(dil)) * 4 * tcp_plane_bytes(dil) + 128;
 }
 
 __device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count)
@@ -884,24 +902,27 @@ __device__ __forceinline__ void tc_commit(uint32_t a)
 
 template <int RPC>
 __global__ void __launch_bounds__(kTcpThreads, 1)
-k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __restrict__ WB,
-             const float* __restrict__ bias, int dil, int H, int Wd, __nv_bfloat16* __restrict__ Y)
+k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmap_tail,
+             const __nv_bfloat16* __restrict__ WB, const float* __restrict__ bias, int dil, int H, int Wd,
+             __nv_bfloat16* __restrict__ Y)
 {
     constexpr uint32_t kCols = 2 * 32 * RPC; // two accumulators of RPC x 32 columns
     extern __shared__ unsigned char tpsm[];
     unsigned char* wsm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tpsm) + 1023) & ~uintptr_t(1023));
     unsigned char* stages = wsm + kTcWBytes;
-    const int R = tc_rows(RPC, dil), C = tc_cols(dil);
+    const int R = tc_rows(RPC, dil), C = tc_cols(dil), CP = tcp_row_pixels(dil);
     const uint32_t PL = tcp_plane_bytes(dil), SB = 4 * PL;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(stages + kTcpStages * SB); // full[2] empty[2] tfull[2] tempty[2]
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
+    const int NS = tcp_stages(dil);
+    // full[4] empty[4] tfull[2] tempty[2], then the TMEM address slot
+    uint64_t* bars = reinterpret_cast<uint64_t*>(stages + NS * SB);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kTcpMaxStages + 4);
     const uint32_t s_w = static_cast<uint32_t>(__cvta_generic_to_shared(wsm));
     const uint32_t s_st = static_cast<uint32_t>(__cvta_generic_to_shared(stages));
     const uint32_t s_bar = static_cast<uint32_t>(__cvta_generic_to_shared(bars));
     auto full = [&](int i) { return s_bar + 8u * i; };
-    auto empty = [&](int i) { return s_bar + 8u * (2 + i); };
-    auto tfull = [&](int i) { return s_bar + 8u * (4 + i); };
-    auto tempty = [&](int i) { return s_bar + 8u * (6 + i); };
+    auto empty = [&](int i) { return s_bar + 8u * (kTcpMaxStages + i); };
+    auto tfull = [&](int i) { return s_bar + 8u * (2 * kTcpMaxStages + i); };
+    auto tempty = [&](int i) { return s_bar + 8u * (2 * kTcpMaxStages + 2 + i); };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tiles_x = (Wd + kTcM - 1) / kTcM, ntiles = tiles_x * ((H + RPC - 1) / RPC);
 
@@ -912,14 +933,17 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __re
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < NS; ++i) {
             mbar_init(full(i), 1);
             mbar_init(empty(i), 1);
+        }
+        for (int i = 0; i < 2; ++i) {
             mbar_init(tfull(i), 1);
             mbar_init(tempty(i), 128);
         }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap_tail)) : "memory");
     }
     for (int i = threadIdx.x; i < kTcWBytes / 16; i += blockDim.x) cp_async16(wsm + i * 16, WB + i * 8, true);
     cp_async_wait_all();
@@ -929,33 +953,39 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __re
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t taddr = *tslot;
 
-    if (warp == 0) {
-        if (lane == 0) { // TMA producer
-            const uint32_t bytes = 4u * 16u * static_cast<uint32_t>(C * R);
-            for (int k = 0, tile = blockIdx.x; tile < ntiles; ++k, tile += gridDim.x) {
-                const int st = k % kTcpStages;
-                if (k >= kTcpStages && !tc_wait(empty(st), ((k / kTcpStages) - 1) & 1)) {
-                    atomicExch(&g_tc_timeout, 1);
-                    break;
-                }
-                const int y0 = (tile / tiles_x) * RPC, x0 = (tile % tiles_x) * kTcM;
+    if (warp == 0) { // TMA producer: the whole warp waits, lane 0 arms the stage, all lanes copy
+        const uint32_t bytes = 4u * 16u * static_cast<uint32_t>(C * R);
+        for (int k = 0, tile = blockIdx.x; tile < ntiles; ++k, tile += gridDim.x) {
+            const int st = k % NS;
+            if (k >= NS && !__all_sync(0xffffffffu, tc_wait(empty(st), ((k / NS) - 1) & 1))) {
+                if (lane == 0) atomicExch(&g_tc_timeout, 1);
+                break;
+            }
+            const int y0 = (tile / tiles_x) * RPC, x0 = (tile % tiles_x) * kTcM;
+            if (lane == 0)
                 asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(full(st)), "r"(bytes)
                              : "memory");
-                for (int q = 0; q < 4; ++q)
-                    asm volatile(
-                        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                        " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(s_st + st * SB + q * PL),
-                        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(x0 - dil), "r"(y0 - dil), "r"(q),
-                        "r"(full(st))
-                        : "memory");
+            __syncwarp();
+            // copy i: plane q, row r, piece h (0: pixels x0 - dil .. + 127, 1: the 2 dil after);
+            // x in 8-byte units (2 per pixel), always even: 16-byte aligned starts
+            for (int i = lane; i < 8 * R; i += 32) {
+                const int q = i / (2 * R), r = (i >> 1) % R, h = i & 1;
+                const uint32_t dst = s_st + st * SB + q * PL + static_cast<uint32_t>((r * CP + h * kTcM) * 16);
+                const int x = 2 * (x0 - dil + h * kTcM);
+                const uint64_t map = reinterpret_cast<uint64_t>(h ? &tmap_tail : &tmap);
+                asm volatile(
+                    "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                    " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
+                    "l"(map), "r"(x), "r"(y0 - dil + r), "r"(q), "r"(full(st))
+                    : "memory");
             }
         }
     }
     else if (warp == 1) {
         if (lane == 0) { // MMA issuer
             for (int k = 0, tile = blockIdx.x; tile < ntiles; ++k, tile += gridDim.x) {
-                const int st = k % kTcpStages, b = k & 1;
-                if (!tc_wait(full(st), (k / kTcpStages) & 1) || (k >= 2 && !tc_wait(tempty(b), ((k >> 1) - 1) & 1))) {
+                const int st = k % NS, b = k & 1;
+                if (!tc_wait(full(st), (k / NS) & 1) || (k >= 2 && !tc_wait(tempty(b), ((k >> 1) - 1) & 1))) {
                     atomicExch(&g_tc_timeout, 1);
                     break;
                 }
@@ -968,7 +998,7 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __re
 #pragma unroll
                     for (int t = 0; t < 9; ++t) {
                         const int dy = dil * (t / 3 - 1), dx = dil * (t % 3 - 1);
-                        const uint32_t pix0 = static_cast<uint32_t>((m + dil + dy) * C + dil + dx);
+                        const uint32_t pix0 = static_cast<uint32_t>((m + dil + dy) * CP + dil + dx);
 #pragma unroll
                         for (int kc = 0; kc < 2; ++kc) {
                             const uint64_t da = da0 + pix0 + kc * (2 * PL >> 4);
@@ -1643,9 +1673,10 @@ inline void nn_prepare_weights(const gfgpu_nn_desc* nn, __nv_bfloat16* wt1, __nv
     k_nn_wprep_last<<<(9 * 8 * kPadC + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 3), wt3);
 }
 
-// TMA view of a channel-planar BF16 activation [4][H][W][8]; box of one plane of the halo tile of
-// k_conv32_tcp (R rows x C pixels x 8 channels), zero fill outside the grid
-inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W, int dil)
+// TMA view of a channel-planar BF16 activation [4][H][W][8] as [4][H][2W] 8-byte elements; box
+// of box_px pixels of one row of one plane (k_conv32_tcp: 128, and 2 dil for the tail), zero fill
+// outside the grid
+inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W, int box_px)
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
@@ -1657,15 +1688,15 @@ inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
     GF_REQUIRE((reinterpret_cast<uintptr_t>(X) & 15u) == 0, "activation not 16-byte aligned");
-    const cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H), 4};
-    const cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(W) * 16,
+    GF_REQUIRE(box_px >= 1 && box_px <= 128, "box width");
+    const cuuint64_t dims[3] = {2 * static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H), 4};
+    const cuuint64_t strides[2] = {static_cast<cuuint64_t>(W) * 16,
                                    static_cast<cuuint64_t>(H) * static_cast<cuuint64_t>(W) * 16};
-    const cuuint32_t box[4] = {8, static_cast<cuuint32_t>(tc_cols(dil)), static_cast<cuuint32_t>(tc_rows(kTcpRPC, dil)),
-                               1};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult rc = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(X), dims, strides,
-                         box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const cuuint32_t box[3] = {2 * static_cast<cuuint32_t>(box_px), 1, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult rc = encode(map, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<__nv_bfloat16*>(X), dims, strides, box,
+                         estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (rc != CUDA_SUCCESS) return fail(GFGPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(rc)) + ")");
     return GFGPU_OK;
 }
@@ -1688,18 +1719,20 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
         k_first_mma<false><<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
                                                         nn->params_f32 + b_off(0), H, W, a1);
     if (nn_tensor_path() == 2) {
-        CUtensorMap m1, m2;
-        GF_TRY(tcp_tensor_map(&m1, a1, H, W, dil_of(1)));
-        GF_TRY(tcp_tensor_map(&m2, a2, H, W, dil_of(2)));
+        CUtensorMap m1, m1t, m2, m2t;
+        GF_TRY(tcp_tensor_map(&m1, a1, H, W, kTcM));
+        GF_TRY(tcp_tensor_map(&m1t, a1, H, W, 2 * dil_of(1)));
+        GF_TRY(tcp_tensor_map(&m2, a2, H, W, kTcM));
+        GF_TRY(tcp_tensor_map(&m2t, a2, H, W, 2 * dil_of(2)));
         const int ntiles = ((W + kTcM - 1) / kTcM) * ((H + kTcpRPC - 1) / kTcpRPC);
         int sms = 0, dev = 0;
         GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
         GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
         const unsigned g = static_cast<unsigned>(std::max(1, std::min(ntiles, sms)));
         k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(1)), s>>>(
-            m1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
+            m1, m1t, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
         k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(2)), s>>>(
-            m2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
+            m2, m2t, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
     }
     else if (nn_tensor_path() == 1) {
         // layer 2 (dilation 2): 4 rows per CTA; layer 3 (dilation 4): 2 rows, so that two CTAs
