@@ -62,7 +62,8 @@ def parse():
     p.add_argument("--margin", type=int, default=8, help="learned workload: crop margin of the loss")
     p.add_argument("--nn-path", type=int, default=0,
                    help="learned workload: tensor-core form of the network's 32->32 layers "
-                        "(gfgpu_set_nn_tensor_path: 0 mma.sync, 1 tcgen05, 2 tcgen05 + TMA pipeline)")
+                        "(gfgpu_set_nn_tensor_path: 0 mma.sync, 1 tcgen05, 2 tcgen05 + TMA pipeline, "
+                        "3 the same with halo-row reuse)")
     p.add_argument("--profile-iters", type=int, default=0,
                    help="learned workload, kernel-share probe: skip pair generation and training "
                         "and run each solver for this many iterations (untrained network)")

@@ -900,6 +900,23 @@ __device__ __forceinline__ void tc_commit(uint32_t a)
                  : "memory");
 }
 
+// MMA and commit issued by one elected lane of a converged warp (the descriptors stay
+// warp-uniform, so the whole warp runs the issue loop)
+__device__ __forceinline__ void tc_mma_elect(uint32_t tmem, uint64_t da, uint64_t db, uint32_t acc)
+{
+    asm volatile("{\n .reg .pred p, e;\n setp.ne.b32 p, %4, 0;\n elect.sync _|e, 0xffffffff;\n"
+                 " @e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                 "l"(da), "l"(db), "r"(kTcIdesc), "r"(acc)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_commit_elect(uint32_t a)
+{
+    asm volatile("{\n .reg .pred e;\n elect.sync _|e, 0xffffffff;\n"
+                 " @e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}\n" ::"r"(a)
+                 : "memory");
+}
+
 template <int RPC>
 __global__ void __launch_bounds__(kTcpThreads, 1)
 k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmap_tail,
@@ -981,12 +998,14 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
             }
         }
     }
-    else if (warp == 1) {
-        if (lane == 0) { // MMA issuer
+    else if (warp == 1) { // MMA issuer: the whole warp, one elected lane issues
+        {
             for (int k = 0, tile = blockIdx.x; tile < ntiles; ++k, tile += gridDim.x) {
                 const int st = k % NS, b = k & 1;
-                if (!tc_wait(full(st), (k / NS) & 1) || (k >= 2 && !tc_wait(tempty(b), ((k >> 1) - 1) & 1))) {
-                    atomicExch(&g_tc_timeout, 1);
+                const bool ok = __all_sync(0xffffffffu, tc_wait(full(st), (k / NS) & 1)) &&
+                                (k < 2 || __all_sync(0xffffffffu, tc_wait(tempty(b), ((k >> 1) - 1) & 1)));
+                if (!ok) {
+                    if (lane == 0) atomicExch(&g_tc_timeout, 1);
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -1003,17 +1022,12 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
                         for (int kc = 0; kc < 2; ++kc) {
                             const uint64_t da = da0 + pix0 + kc * (2 * PL >> 4);
                             const uint64_t db = db0 + (t * 2 + kc) * 64;
-                            const uint32_t acc = (t | kc) ? 1u : 0u;
-                            asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                                         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-                                             taddr + b * 32 * RPC + m * 32),
-                                         "l"(da), "l"(db), "r"(kTcIdesc), "r"(acc)
-                                         : "memory");
+                            tc_mma_elect(taddr + b * 32 * RPC + m * 32, da, db, (t | kc) ? 1u : 0u);
                         }
                     }
                 }
-                tc_commit(empty(st));
-                tc_commit(tfull(b));
+                tc_commit_elect(empty(st));
+                tc_commit_elect(tfull(b));
             }
         }
     }
@@ -1046,6 +1060,231 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
                 const int yy = y0 + m, xx = x0 + q4 * 32 + lane;
                 if (yy < H && xx < Wd) {
                     // planar output: the lanes of a warp write 32 consecutive 16-byte pixels of a plane
+                    __nv_bfloat16* yp = Y + (static_cast<int64_t>(yy) * Wd + xx) * 8;
+                    const int64_t plane = static_cast<int64_t>(H) * Wd * 8;
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        __nv_bfloat162 h[4];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int co = kk * 8 + 2 * j;
+                            h[j] = __floats2bfloat162_rn(fmaxf(__uint_as_float(v[co]) + bs[co], 0.0f),
+                                                         fmaxf(__uint_as_float(v[co + 1]) + bs[co + 1], 0.0f));
+                        }
+                        *reinterpret_cast<uint4*>(yp + kk * plane) = *reinterpret_cast<uint4*>(h);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            mbar_arrive(tempty(b));
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(kCols) : "memory");
+    }
+}
+
+// The 32 -> 32 layer with row reuse: each persistent CTA takes a contiguous range of tiles
+// (RPC rows x 128 pixels) in column-strip order, so consecutive tiles of a strip share all but
+// RPC of their R = RPC + 2 dil halo rows. Halo rows live in a ring of row slots (4 planes x CP
+// pixels x 16 bytes each); a row is loaded once per run of tiles by TMA (the same two boxes per
+// plane as k_conv32_tcp), each slot with its own "full" (TMA landed) and "empty" (the last MMA
+// reading it completed) mbarrier. Warp 0 streams rows into slots, warp 1 (one lane) waits for a
+// tile's R rows and issues its 18 RPC MMAs (the A operand of output row m and tap (dy, dx) is
+// 128 pixels of the slot of halo row m + dil + dy) into one of two TMEM accumulators, then
+// releases the rows the next tile no longer reads (all of them at the end of a run); warps 2-5
+// drain the accumulators. A slot is reloaded only after its release, and NSLOT >= R keeps the
+// producer from waiting on a tile that needs the row it is about to load. Every wait is bounded.
+constexpr int kTcrThreads = 192;
+constexpr int kTcrMaxSlots = 24;
+
+__host__ __device__ constexpr uint32_t tcr_slot_bytes(int dil)
+{
+    return static_cast<uint32_t>(4 * tcp_row_pixels(dil) * 16);
+}
+
+__host__ __device__ constexpr int tcr_slots(int dil)
+{
+    return static_cast<int>((kTcpSmemBudget - 1024 - kTcWBytes - 512) / tcr_slot_bytes(dil)) < kTcrMaxSlots
+               ? static_cast<int>((kTcpSmemBudget - 1024 - kTcWBytes - 512) / tcr_slot_bytes(dil))
+               : kTcrMaxSlots;
+}
+
+inline size_t tcr_smem_bytes(int dil)
+{
+    return 1024 + kTcWBytes + static_cast<size_t>(tcr_slots(dil)) * tcr_slot_bytes(dil) + 512;
+}
+
+template <int RPC>
+__global__ void __launch_bounds__(kTcrThreads, 1)
+k_conv32_tcr(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmap_tail,
+             const __nv_bfloat16* __restrict__ WB, const float* __restrict__ bias, int dil, int H, int Wd,
+             __nv_bfloat16* __restrict__ Y)
+{
+    constexpr uint32_t kCols = 2 * 32 * RPC;
+    extern __shared__ unsigned char trsm[];
+    unsigned char* wsm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(trsm) + 1023) & ~uintptr_t(1023));
+    unsigned char* ring = wsm + kTcWBytes;
+    const int R = tc_rows(RPC, dil), C = tc_cols(dil), CP = tcp_row_pixels(dil);
+    const int NSLOT = tcr_slots(dil);
+    const uint32_t SL = tcr_slot_bytes(dil), PLR = static_cast<uint32_t>(CP * 16); // slot, plane row
+    // full[NSLOT] empty[NSLOT] tfull[2] tempty[2], then the TMEM address slot
+    uint64_t* bars = reinterpret_cast<uint64_t*>(ring + NSLOT * SL);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kTcrMaxSlots + 4);
+    const uint32_t s_w = static_cast<uint32_t>(__cvta_generic_to_shared(wsm));
+    const uint32_t s_ring = static_cast<uint32_t>(__cvta_generic_to_shared(ring));
+    const uint32_t s_bar = static_cast<uint32_t>(__cvta_generic_to_shared(bars));
+    auto full = [&](int i) { return s_bar + 8u * i; };
+    auto empty = [&](int i) { return s_bar + 8u * (kTcrMaxSlots + i); };
+    auto tfull = [&](int i) { return s_bar + 8u * (2 * kTcrMaxSlots + i); };
+    auto tempty = [&](int i) { return s_bar + 8u * (2 * kTcrMaxSlots + 2 + i); };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_x = (Wd + kTcM - 1) / kTcM, tiles_y = (H + RPC - 1) / RPC;
+    const int ntiles = tiles_x * tiles_y;
+    // this CTA's tiles [t0, t1) in strip order: strip t / tiles_y, row tile t % tiles_y
+    const int t0 = static_cast<int>(static_cast<int64_t>(ntiles) * blockIdx.x / gridDim.x);
+    const int t1 = static_cast<int>(static_cast<int64_t>(ntiles) * (blockIdx.x + 1) / gridDim.x);
+    // a tile continues the previous one's run when it is the next row tile of the same strip
+    auto continues = [&](int t) { return t > t0 && (t % tiles_y) != 0; };
+
+    if (warp == 1) {
+        const uint32_t s_slot = static_cast<uint32_t>(__cvta_generic_to_shared(tslot));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_slot), "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NSLOT; ++i) {
+            mbar_init(full(i), 1);
+            mbar_init(empty(i), 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(tfull(i), 1);
+            mbar_init(tempty(i), 128);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap_tail)) : "memory");
+    }
+    for (int i = threadIdx.x; i < kTcWBytes / 16; i += blockDim.x) cp_async16(wsm + i * 16, WB + i * 8, true);
+    cp_async_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = *tslot;
+
+    if (warp == 0) { // row producer
+        const uint32_t bytes = 4u * 16u * static_cast<uint32_t>(C);
+        int row = 0; // stream index of the next row to load
+        bool ok = true;
+        for (int t = t0; t < t1 && ok; ++t) {
+            const int x0 = (t / tiles_y) * kTcM, y0 = (t % tiles_y) * RPC;
+            // rows of this tile not yet loaded: all R at the start of a run, else the last RPC
+            const int first = continues(t) ? RPC + 2 * dil - RPC : 0;
+            for (int r = first; r < R; ++r, ++row) {
+                const int sl = row % NSLOT;
+                if (row >= NSLOT && !__all_sync(0xffffffffu, tc_wait(empty(sl), ((row / NSLOT) - 1) & 1))) {
+                    if (lane == 0) atomicExch(&g_tc_timeout, 1);
+                    ok = false;
+                    break;
+                }
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(full(sl)),
+                                 "r"(bytes)
+                                 : "memory");
+                __syncwarp();
+                if (lane < 8) { // plane lane >> 1, piece lane & 1
+                    const int q = lane >> 1, h = lane & 1;
+                    const uint32_t dst = s_ring + sl * SL + q * PLR + static_cast<uint32_t>(h * kTcM * 16);
+                    const int x = 2 * (x0 - dil + h * kTcM);
+                    const uint64_t map = reinterpret_cast<uint64_t>(h ? &tmap_tail : &tmap);
+                    asm volatile(
+                        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
+                        "l"(map), "r"(x), "r"(y0 - dil + r), "r"(q), "r"(full(sl))
+                        : "memory");
+                }
+            }
+        }
+    }
+    else if (warp == 1) { // MMA issuer: the whole warp, one elected lane issues
+        {
+            int base = 0; // stream index of the current tile's first halo row
+            int next = 0; // stream index after the rows loaded so far
+            for (int t = t0, k = 0; t < t1; ++t, ++k) {
+                const int b = k & 1;
+                if (continues(t))
+                    base += RPC;
+                else
+                    base = next;
+                next = base + R;
+                bool ok = k < 2 || __all_sync(0xffffffffu, tc_wait(tempty(b), ((k >> 1) - 1) & 1));
+                for (int r = 0; r < R && ok; ++r)
+                    ok = __all_sync(0xffffffffu, tc_wait(full((base + r) % NSLOT), ((base + r) / NSLOT) & 1));
+                if (!ok) {
+                    if (lane == 0) atomicExch(&g_tc_timeout, 1);
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const int b0 = base % NSLOT; // slot of the tile's first halo row
+                const uint64_t db0 = tc_desc(s_w, 512, 128);
+#pragma unroll
+                for (int m = 0; m < RPC; ++m) {
+#pragma unroll
+                    for (int ry = 0; ry < 3; ++ry) { // halo row m + ry dil
+                        int sl = b0 + m + ry * dil;
+                        sl -= sl >= NSLOT ? NSLOT : 0;
+                        const uint64_t dr = tc_desc(s_ring + sl * SL, PLR, 128);
+#pragma unroll
+                        for (int rx = 0; rx < 3; ++rx) { // pixels from rx dil (16-byte units)
+                            const int tp = ry * 3 + rx;
+                            const uint64_t da0 = dr + static_cast<uint64_t>(rx * dil);
+#pragma unroll
+                            for (int kc = 0; kc < 2; ++kc)
+                                tc_mma_elect(taddr + b * 32 * RPC + m * 32, da0 + kc * (2 * PLR >> 4),
+                                             db0 + (tp * 2 + kc) * 64, (tp | kc) ? 1u : 0u);
+                        }
+                    }
+                }
+                tc_commit_elect(tfull(b));
+                // release the rows no later tile of this run reads
+                const int nrel = (t + 1 < t1 && continues(t + 1)) ? RPC : R;
+                for (int r = 0; r < nrel; ++r) tc_commit_elect(empty((base + r) % NSLOT));
+            }
+        }
+    }
+    else { // epilogue, warps 2-5: TMEM lane quarter warp % 4
+        const int q4 = warp & 3;
+        float bs[32];
+#pragma unroll
+        for (int co = 0; co < 32; ++co) bs[co] = bias[co];
+        for (int t = t0, k = 0; t < t1; ++t, ++k) {
+            const int b = k & 1;
+            if (!__all_sync(0xffffffffu, tc_wait(tfull(b), (k >> 1) & 1))) {
+                atomicExch(&g_tc_timeout, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int x0 = (t / tiles_y) * kTcM, y0 = (t % tiles_y) * RPC;
+#pragma unroll 1
+            for (int m = 0; m < RPC; ++m) {
+                uint32_t v[32];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr + (static_cast<uint32_t>(q4 * 32) << 16) + b * 32 * RPC + m * 32));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                const int yy = y0 + m, xx = x0 + q4 * 32 + lane;
+                if (yy < H && xx < Wd) {
                     __nv_bfloat16* yp = Y + (static_cast<int64_t>(yy) * Wd + xx) * 8;
                     const int64_t plane = static_cast<int64_t>(H) * Wd * 8;
 #pragma unroll
@@ -1711,14 +1950,14 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
 {
     const int H = nn->H, W = nn->W;
     dim3 grid((W + kTileX - 1) / kTileX, (H + kTileY - 1) / kTileY);
-    const bool planar = nn_tensor_path() == 2; // path 2: channel-planar activations
+    const bool planar = nn_tensor_path() >= 2; // paths 2, 3: channel-planar activations
     if (planar)
         k_first_mma<true><<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
                                                        nn->params_f32 + b_off(0), H, W, a1);
     else
         k_first_mma<false><<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
                                                         nn->params_f32 + b_off(0), H, W, a1);
-    if (nn_tensor_path() == 2) {
+    if (nn_tensor_path() >= 2) {
         CUtensorMap m1, m1t, m2, m2t;
         GF_TRY(tcp_tensor_map(&m1, a1, H, W, kTcM));
         GF_TRY(tcp_tensor_map(&m1t, a1, H, W, 2 * dil_of(1)));
@@ -1729,10 +1968,18 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
         GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
         GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
         const unsigned g = static_cast<unsigned>(std::max(1, std::min(ntiles, sms)));
-        k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(1)), s>>>(
-            m1, m1t, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
-        k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(2)), s>>>(
-            m2, m2t, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
+        if (nn_tensor_path() == 3) {
+            k_conv32_tcr<kTcpRPC><<<g, kTcrThreads, tcr_smem_bytes(dil_of(1)), s>>>(
+                m1, m1t, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
+            k_conv32_tcr<kTcpRPC><<<g, kTcrThreads, tcr_smem_bytes(dil_of(2)), s>>>(
+                m2, m2t, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
+        }
+        else {
+            k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(1)), s>>>(
+                m1, m1t, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
+            k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(2)), s>>>(
+                m2, m2t, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
+        }
     }
     else if (nn_tensor_path() == 1) {
         // layer 2 (dilation 2): 4 rows per CTA; layer 3 (dilation 4): 2 rows, so that two CTAs
@@ -1786,6 +2033,10 @@ inline int prepare_mma(cudaStream_t)
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_tcp<kTcpRPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(std::max(tcp_smem_bytes(dil_of(1)),
                                                                      tcp_smem_bytes(dil_of(2))))),
+                      "cudaFuncSetAttribute"));
+    GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_tcr<kTcpRPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(std::max(tcr_smem_bytes(dil_of(1)),
+                                                                     tcr_smem_bytes(dil_of(2))))),
                       "cudaFuncSetAttribute"));
     GF_TRY(check_cuda(cudaFuncSetAttribute(k_conv32_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(tc_smem_bytes(4, dil_of(1)))),

@@ -92,7 +92,7 @@ int gfgpu_set_variant(int elem_variant, int node_variant)
 
 int gfgpu_set_nn_tensor_path(int path)
 {
-    if (path < 0 || path > 2) return fail(GFGPU_ERR_ARG, "gfgpu_set_nn_tensor_path: path is 0, 1 or 2");
+    if (path < 0 || path > 3) return fail(GFGPU_ERR_ARG, "gfgpu_set_nn_tensor_path: path is 0, 1, 2 or 3");
     gfgpu::g_nn_path = path;
     return GFGPU_OK;
 }

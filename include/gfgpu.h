@@ -56,8 +56,11 @@ int gfgpu_set_strict(int strict);
 int gfgpu_set_variant(int elem_variant, int node_variant);
 /* Tensor-core instructions of the network's 32 -> 32 layers (process-wide): 0 = mma.sync m16n8k16
  * (default), 1 = tcgen05.mma with TMEM accumulators, one tile per CTA, 2 = tcgen05.mma in a
- * persistent pipeline fed by TMA (cp.async.bulk.tensor) with double-buffered shared memory and
- * TMEM. Same arithmetic (BF16 products, FP32 accumulation); the summation order differs. */
+ * persistent pipeline fed by TMA (cp.async.bulk.tensor) with 2-3 shared-memory stages of whole
+ * halo tiles and double-buffered TMEM, 3 = the same pipeline with a ring of halo rows that
+ * consecutive tiles of a column strip share (each row loaded once per run of tiles). Same
+ * arithmetic (BF16 products, FP32 accumulation); the summation order differs between 0, 1 and
+ * 2/3 (2 and 3 give identical bits). */
 int gfgpu_set_nn_tensor_path(int path);
 /* Error flag of the tcgen05 layers' bounded waits: GFGPU_ERR_TIMEOUT if a wait for the tensor
  * cores gave up since the last call (the layer's output is then invalid), else GFGPU_OK. Clears

@@ -190,7 +190,7 @@ def test_tensor_core_inference_matches_fp32_and_oracle(L, H, W):
     assert rel_err(y32.cpu().numpy(), yref[0]) <= 1e-5
     out = {}
     try:
-        for path in (0, 1, 2):  # mma.sync, tcgen05, tcgen05 + TMA pipeline
+        for path in (0, 1, 2, 3):  # mma.sync, tcgen05, tcgen05 + TMA pipeline, + row reuse
             L.call("gfgpu_set_nn_tensor_path", path)
             ytc = torch.full((H, W, 2), float("nan"), dtype=torch.float32, device="cuda")
             L.call("gfgpu_nn_infer", C.addressof(d), Xd.data_ptr(), ytc.data_ptr(), ws2.data_ptr(), s)
@@ -204,6 +204,8 @@ def test_tensor_core_inference_matches_fp32_and_oracle(L, H, W):
     # same products, different FP32 summation order
     assert rel_err(out[0], out[1]) <= 1e-2
     assert rel_err(out[0], out[2]) <= 1e-2
+    # paths 2 and 3 run the same MMAs on the same rows in the same order
+    assert np.array_equal(out[2], out[3])
 
 
 @pytest.fixture(scope="module")
