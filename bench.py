@@ -317,16 +317,7 @@ def run_gpu(args, rank, world):
     ms_inc = ms / (args.steps * inc)
     ms_node = max(ms_inc - ms_elem, 0.0)
 
-    # FP64 issue-rate probe (for the FP64 roof)
-    probe_out = torch.zeros(2, dtype=torch.float64, device=dev)
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    blocks, iters = sms * 16, 10000
-    _lib.call("gfgpu_probe_fp64", blocks, 1000, probe_out.data_ptr(), stream.cuda_stream)
-    k0.record(stream)
-    _lib.call("gfgpu_probe_fp64", blocks, iters, probe_out.data_ptr(), stream.cuda_stream)
-    k1.record(stream)
-    torch.cuda.synchronize()
-    fp64_peak = 2.0 * 16 * iters * blocks * 256 / (k0.elapsed_time(k1) * 1e-3)
+    fp64_peak = fp64_probe()
 
     # ---------------------------------------------------------------- end-to-end (host buffers)
     hu = torch.zeros((nnode, 2), dtype=torch.float64).pin_memory()
@@ -488,6 +479,28 @@ def network_ms(lp, n):
     return e0.elapsed_time(e1) / 50
 
 
+def fp64_probe():
+    """Measured FP64 FLOP/s of independent DFMA chains on every SM (gfgpu_probe_fp64), the FP64
+    roof the element kernels are held against (2 FLOP per DFMA)."""
+    import torch
+
+    from goosefem_gb300 import _lib
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+    out = torch.zeros(2, dtype=torch.float64, device=dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, iters = sms * 16, 10000
+    _lib.call("gfgpu_probe_fp64", blocks, 1000, out.data_ptr(), stream.cuda_stream)
+    k0 = torch.cuda.Event(enable_timing=True)
+    k1 = torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    _lib.call("gfgpu_probe_fp64", blocks, iters, out.data_ptr(), stream.cuda_stream)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    return 2.0 * 16 * iters * blocks * 256 / (k0.elapsed_time(k1) * 1e-3)
+
+
 def run_static(args):
     """3-d static case: Hex8 128^3 matrix-free Jacobi-PCG to 1e-8 relative residual (FP64).
     One bench step = one full solve from a zero initial guess."""
@@ -529,6 +542,15 @@ def run_static(args):
                        else "general"},
             "iterations": it, "relres_true": rel, "ms_per_iteration": sec * 1e3 / it,
             "elem_updates_per_s": n ** 3 * 8 * it / sec}
+    if st.coef is not None and st.desc.reg_nz > 0:
+        # FP64 instructions of one iteration of the cube / Regular path: element kernel ~171 per
+        # element, gather 8 adds + 1 FMA, update 5 per free dof, direction 1 per dof
+        nfree = nnode * 3 - iip.size
+        instr = 171 * n ** 3 + 14 * nfree + nnode * 3
+        peak = fp64_probe() / 2.0
+        line["fp64"] = {"instr_per_iteration": instr, "achieved_ginstr_s": instr / (sec / it) / 1e9,
+                        "peak_ginstr_s": peak / 1e9, "instr_frac": instr / (sec / it) / peak,
+                        "peak_source": "measured live (gfgpu_probe_fp64: DFMA chains)"}
     print(json.dumps(line), flush=True)
     return 0
 
