@@ -60,7 +60,7 @@ def parse():
                    help="learned workload: degree of the Chebyshev smoother the network is trained to "
                         "reproduce (its support radius in nodes; the network's receptive field radius is 8)")
     p.add_argument("--margin", type=int, default=8, help="learned workload: crop margin of the loss")
-    p.add_argument("--nn-path", type=int, default=0,
+    p.add_argument("--nn-path", type=int, default=2,
                    help="learned workload: tensor-core form of the network's 32->32 layers "
                         "(gfgpu_set_nn_tensor_path: 0 mma.sync, 1 tcgen05, 2 tcgen05 + TMA pipeline, "
                         "3 the same with halo-row reuse)")

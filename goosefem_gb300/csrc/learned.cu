@@ -450,6 +450,17 @@ __global__ void k_nn_wprep_first(const __nv_bfloat16* __restrict__ W, __nv_bfloa
 // LAST = false: Y = relu(conv + b), BF16 [H, W, 32] (NT = 4). LAST = true (NT = 1, the 32 -> 2
 // output layer): z = sigma (conv + b) on the free dofs, 0 on prescribed (FP64 nodevec; sigma =
 // RMS of the residual, sqrt(sc[rr_slot] / nfree)), or Yf [H, W, 2] FP32 when z is null.
+// Channel-planar activations of the tcgen05 layers: [4][H][Wp][8] BF16, pixel (y, x) stored at
+// row position x + kPlanarPad, Wp = planar_row(W) (a multiple of 8 pixels); the pad pixels are
+// zero. Rows of 128-byte groups of 8 pixels make a halo tile one TMA box per plane with
+// 128-byte inner lines.
+constexpr int kPlanarPad = 4;
+
+__host__ __device__ constexpr int planar_row(int W)
+{
+    return (W + kPlanarPad + 7) / 8 * 8;
+}
+
 template <int NT, bool LAST, bool PLANAR_IN = false>
 __global__ void __launch_bounds__(kMmaThreads)
 k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ WT,
@@ -473,7 +484,10 @@ k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict_
         const bool in = yy >= 0 && yy < H && xx >= 0 && xx < Wd;
         const int64_t gp = static_cast<int64_t>(yy) * Wd + xx;
         const __nv_bfloat16* src =
-            !in ? X : (PLANAR_IN ? X + (ch / 8) * (static_cast<int64_t>(H) * Wd * 8) + gp * 8 : X + gp * 32 + ch);
+            !in ? X
+                : (PLANAR_IN ? X + (ch / 8) * (static_cast<int64_t>(H) * planar_row(Wd) * 8) +
+                                   (static_cast<int64_t>(yy) * planar_row(Wd) + xx + kPlanarPad) * 8
+                             : X + gp * 32 + ch);
         cp_async16(halo + pix * kPadC + ch, src, in);
     }
     if (LAST && threadIdx.x == 0) s_sigma = z ? sqrt(sc[rr_slot] / nfree) : 1.0;
@@ -650,9 +664,23 @@ k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_
                 const int co = nt * 8 + tig * 2;
                 float v0 = fmaxf(c[mt][nt][2 * half + 0] + bias[co], 0.0f);
                 float v1 = fmaxf(c[mt][nt][2 * half + 1] + bias[co + 1], 0.0f);
-                __nv_bfloat16* yp = PLANAR_OUT ? Y + nt * (static_cast<int64_t>(H) * Wd * 8) + gp * 8 + tig * 2
-                                               : Y + gp * 32 + co;
-                *reinterpret_cast<__nv_bfloat162*>(yp) = __floats2bfloat162_rn(v0, v1);
+                if (PLANAR_OUT) {
+                    const int Wp = planar_row(Wd);
+                    __nv_bfloat16* row = Y + nt * (static_cast<int64_t>(H) * Wp * 8) + static_cast<int64_t>(yy) * Wp * 8;
+                    *reinterpret_cast<__nv_bfloat162*>(row + (xx + kPlanarPad) * 8 + tig * 2) =
+                        __floats2bfloat162_rn(v0, v1);
+                    // the row's pad pixels (left of x = 0, right of x = W - 1) stay zero
+                    const __nv_bfloat162 z2 = __floats2bfloat162_rn(0.0f, 0.0f);
+                    if (xx == 0)
+                        for (int pp = 0; pp < kPlanarPad; ++pp)
+                            *reinterpret_cast<__nv_bfloat162*>(row + pp * 8 + tig * 2) = z2;
+                    if (xx == Wd - 1)
+                        for (int pp = Wd + kPlanarPad; pp < Wp; ++pp)
+                            *reinterpret_cast<__nv_bfloat162*>(row + pp * 8 + tig * 2) = z2;
+                }
+                else {
+                    *reinterpret_cast<__nv_bfloat162*>(Y + gp * 32 + co) = __floats2bfloat162_rn(v0, v1);
+                }
             }
         }
     }
@@ -843,14 +871,12 @@ k_conv32_tc(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict
 //
 // The same implicit GEMM as k_conv32_tc, as a persistent kernel (one CTA per SM) that overlaps
 // the three stages of consecutive tiles of RPC rows x 128 pixels. Activations in and out are
-// channel-planar, [4][H][W][8] BF16 (each plane contiguous), so that a row of a plane of the halo
-// tile is contiguous in HBM. Warp 0 loads the halo tile's 4 planes with TMA
-// (cp.async.bulk.tensor) one row at a time: a 2 KB box of 128 pixels and a box of the 2 dil
-// remaining pixels (3-d views [4][H][2W] of 8-byte elements, zero fill outside the grid), each
-// landing at a 128-byte aligned row of a shared-memory stage (rows padded to a multiple of 8
-// pixels), the 8 R copies of a tile spread over the warp's lanes; into one of the 2-4 stages that
-// fit in shared memory,
-// warp 1 (one lane) issues the 18 RPC MMAs of a tile into one of two TMEM accumulators
+// channel-planar with padded rows (planar_row), so that the halo tile of a plane is one TMA box
+// (cp.async.bulk.tensor, 4-d view [4][H][Wp/8][16] of 8-byte elements, box R x 17 groups of 128
+// bytes, zero fill outside the grid) into one of the 2-4 shared-memory stages that fit; warp 0
+// (one lane) issues the 4 boxes of a tile. (A TMA instruction costs about the same whatever its
+// size, and 128-byte inner lines are the fast case: 16-byte-wide boxes or one box per row were
+// 1.2-1.3x slower per application.) Warp 1 (one lane) issues the 18 RPC MMAs of a tile into one of two TMEM accumulators
 // and commits them to the stage's "empty" and the accumulator's "full" mbarrier; warps 2-5 drain
 // an accumulator (tcgen05.ld, bias, ReLU, BF16) while the next tile is multiplied. Every wait is
 // bounded; a role that gives up sets the time-out flag and leaves its loop.
@@ -860,10 +886,14 @@ constexpr int kTcpMaxStages = 4;
 constexpr size_t kTcpSmemBudget = 232448; // maximum dynamic shared memory of a CTA
 constexpr int kTcpRPC = 4;
 
-// pixels per shared-memory row of the halo tile: C padded to a multiple of 8 (128-byte rows)
-__host__ __device__ constexpr int tcp_row_pixels(int dil)
+// pixels per shared-memory row of the halo tile: 17 groups of 8 (2176 bytes), the planar
+// positions x0 .. x0 + 135 = image pixels x0 - 4 .. x0 + 131, which hold the 128 + 2 dil pixels of
+// any dilation <= kPlanarPad
+constexpr int kTcpGroups = 17;
+
+__host__ __device__ constexpr int tcp_row_pixels(int)
 {
-    return (tc_cols(dil) + 7) / 8 * 8;
+    return kTcpGroups * 8;
 }
 
 __host__ __device__ constexpr uint32_t tcp_plane_bytes(int dil)
@@ -919,9 +949,8 @@ __device__ __forceinline__ void tc_commit_elect(uint32_t a)
 
 template <int RPC>
 __global__ void __launch_bounds__(kTcpThreads, 1)
-k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmap_tail,
-             const __nv_bfloat16* __restrict__ WB, const float* __restrict__ bias, int dil, int H, int Wd,
-             __nv_bfloat16* __restrict__ Y)
+k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __restrict__ WB,
+             const float* __restrict__ bias, int dil, int H, int Wd, __nv_bfloat16* __restrict__ Y)
 {
     constexpr uint32_t kCols = 2 * 32 * RPC; // two accumulators of RPC x 32 columns
     extern __shared__ unsigned char tpsm[];
@@ -960,7 +989,6 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
         }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
-        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap_tail)) : "memory");
     }
     for (int i = threadIdx.x; i < kTcWBytes / 16; i += blockDim.x) cp_async16(wsm + i * 16, WB + i * 8, true);
     cp_async_wait_all();
@@ -970,8 +998,10 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t taddr = *tslot;
 
-    if (warp == 0) { // TMA producer: the whole warp waits, lane 0 arms the stage, all lanes copy
-        const uint32_t bytes = 4u * 16u * static_cast<uint32_t>(C * R);
+    if (warp == 0) { // TMA producer: the whole warp waits, one lane loads the 4 planes of a tile
+        // box: R rows x 17 groups of 8 pixels (128-byte lines) from planar position x0, i.e. image
+        // pixels x0 - 4 .. x0 + 131; rows and groups outside the grid read as zeros
+        const uint32_t bytes = 4u * static_cast<uint32_t>(R) * kTcpGroups * 128u;
         for (int k = 0, tile = blockIdx.x; tile < ntiles; ++k, tile += gridDim.x) {
             const int st = k % NS;
             if (k >= NS && !__all_sync(0xffffffffu, tc_wait(empty(st), ((k / NS) - 1) & 1))) {
@@ -979,23 +1009,18 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
                 break;
             }
             const int y0 = (tile / tiles_x) * RPC, x0 = (tile % tiles_x) * kTcM;
-            if (lane == 0)
+            if (lane == 0) {
                 asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(full(st)), "r"(bytes)
                              : "memory");
-            __syncwarp();
-            // copy i: plane q, row r, piece h (0: pixels x0 - dil .. + 127, 1: the 2 dil after);
-            // x in 8-byte units (2 per pixel), always even: 16-byte aligned starts
-            for (int i = lane; i < 8 * R; i += 32) {
-                const int q = i / (2 * R), r = (i >> 1) % R, h = i & 1;
-                const uint32_t dst = s_st + st * SB + q * PL + static_cast<uint32_t>((r * CP + h * kTcM) * 16);
-                const int x = 2 * (x0 - dil + h * kTcM);
-                const uint64_t map = reinterpret_cast<uint64_t>(h ? &tmap_tail : &tmap);
-                asm volatile(
-                    "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                    " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
-                    "l"(map), "r"(x), "r"(y0 - dil + r), "r"(q), "r"(full(st))
-                    : "memory");
+                for (int q = 0; q < 4; ++q)
+                    asm volatile(
+                        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(s_st + st * SB + q * PL),
+                        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(x0 / 8), "r"(y0 - dil), "r"(q),
+                        "r"(full(st))
+                        : "memory");
             }
+            __syncwarp();
         }
     }
     else if (warp == 1) { // MMA issuer: the whole warp, one elected lane issues
@@ -1017,7 +1042,7 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
 #pragma unroll
                     for (int t = 0; t < 9; ++t) {
                         const int dy = dil * (t / 3 - 1), dx = dil * (t % 3 - 1);
-                        const uint32_t pix0 = static_cast<uint32_t>((m + dil + dy) * CP + dil + dx);
+                        const uint32_t pix0 = static_cast<uint32_t>((m + dil + dy) * CP + kPlanarPad + dx);
 #pragma unroll
                         for (int kc = 0; kc < 2; ++kc) {
                             const uint64_t da = da0 + pix0 + kc * (2 * PL >> 4);
@@ -1060,8 +1085,17 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
                 const int yy = y0 + m, xx = x0 + q4 * 32 + lane;
                 if (yy < H && xx < Wd) {
                     // planar output: the lanes of a warp write 32 consecutive 16-byte pixels of a plane
-                    __nv_bfloat16* yp = Y + (static_cast<int64_t>(yy) * Wd + xx) * 8;
-                    const int64_t plane = static_cast<int64_t>(H) * Wd * 8;
+                    const int Wp = planar_row(Wd);
+                    __nv_bfloat16* yrow = Y + static_cast<int64_t>(yy) * Wp * 8;
+                    __nv_bfloat16* yp = yrow + (xx + kPlanarPad) * 8;
+                    const int64_t plane = static_cast<int64_t>(H) * Wp * 8;
+                    // the row's pad pixels stay zero
+                    for (int kk = 0; kk < 4 && xx == 0; ++kk)
+                        for (int pp = 0; pp < kPlanarPad; ++pp)
+                            *reinterpret_cast<uint4*>(yrow + kk * plane + pp * 8) = make_uint4(0u, 0u, 0u, 0u);
+                    for (int kk = 0; kk < 4 && xx == Wd - 1; ++kk)
+                        for (int pp = Wd + kPlanarPad; pp < Wp; ++pp)
+                            *reinterpret_cast<uint4*>(yrow + kk * plane + pp * 8) = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk) {
                         __nv_bfloat162 h[4];
@@ -1120,8 +1154,7 @@ inline size_t tcr_smem_bytes(int dil)
 
 template <int RPC>
 __global__ void __launch_bounds__(kTcrThreads, 1)
-k_conv32_tcr(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmap_tail,
-             const __nv_bfloat16* __restrict__ WB, const float* __restrict__ bias, int dil, int H, int Wd,
+k_conv32_tcr(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __restrict__ WB, const float* __restrict__ bias, int dil, int H, int Wd,
              __nv_bfloat16* __restrict__ Y)
 {
     constexpr uint32_t kCols = 2 * 32 * RPC;
@@ -1167,7 +1200,6 @@ k_conv32_tcr(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
         }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
-        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap_tail)) : "memory");
     }
     for (int i = threadIdx.x; i < kTcWBytes / 16; i += blockDim.x) cp_async16(wsm + i * 16, WB + i * 8, true);
     cp_async_wait_all();
@@ -1178,7 +1210,7 @@ k_conv32_tcr(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
     const uint32_t taddr = *tslot;
 
     if (warp == 0) { // row producer
-        const uint32_t bytes = 4u * 16u * static_cast<uint32_t>(C);
+        const uint32_t bytes = 4u * kTcpGroups * 128u; // a row of the 4 planes
         int row = 0; // stream index of the next row to load
         bool ok = true;
         for (int t = t0; t < t1 && ok; ++t) {
@@ -1197,15 +1229,13 @@ k_conv32_tcr(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
                                  "r"(bytes)
                                  : "memory");
                 __syncwarp();
-                if (lane < 8) { // plane lane >> 1, piece lane & 1
-                    const int q = lane >> 1, h = lane & 1;
-                    const uint32_t dst = s_ring + sl * SL + q * PLR + static_cast<uint32_t>(h * kTcM * 16);
-                    const int x = 2 * (x0 - dil + h * kTcM);
-                    const uint64_t map = reinterpret_cast<uint64_t>(h ? &tmap_tail : &tmap);
+                if (lane < 4) { // plane lane: one row of 17 groups from planar position x0
+                    const uint32_t dst = s_ring + sl * SL + lane * PLR;
                     asm volatile(
-                        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                        " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
-                        "l"(map), "r"(x), "r"(y0 - dil + r), "r"(q), "r"(full(sl))
+                        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(dst),
+                        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(x0 / 8), "r"(y0 - dil + r), "r"(lane),
+                        "r"(full(sl))
                         : "memory");
                 }
             }
@@ -1240,9 +1270,9 @@ k_conv32_tcr(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
                         sl -= sl >= NSLOT ? NSLOT : 0;
                         const uint64_t dr = tc_desc(s_ring + sl * SL, PLR, 128);
 #pragma unroll
-                        for (int rx = 0; rx < 3; ++rx) { // pixels from rx dil (16-byte units)
+                        for (int rx = 0; rx < 3; ++rx) { // image pixels from x0 + (rx - 1) dil
                             const int tp = ry * 3 + rx;
-                            const uint64_t da0 = dr + static_cast<uint64_t>(rx * dil);
+                            const uint64_t da0 = dr + static_cast<uint64_t>(kPlanarPad + (rx - 1) * dil);
 #pragma unroll
                             for (int kc = 0; kc < 2; ++kc)
                                 tc_mma_elect(taddr + b * 32 * RPC + m * 32, da0 + kc * (2 * PLR >> 4),
@@ -1285,8 +1315,18 @@ k_conv32_tcr(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
                 const int yy = y0 + m, xx = x0 + q4 * 32 + lane;
                 if (yy < H && xx < Wd) {
-                    __nv_bfloat16* yp = Y + (static_cast<int64_t>(yy) * Wd + xx) * 8;
-                    const int64_t plane = static_cast<int64_t>(H) * Wd * 8;
+                    // planar output: the lanes of a warp write 32 consecutive 16-byte pixels of a plane
+                    const int Wp = planar_row(Wd);
+                    __nv_bfloat16* yrow = Y + static_cast<int64_t>(yy) * Wp * 8;
+                    __nv_bfloat16* yp = yrow + (xx + kPlanarPad) * 8;
+                    const int64_t plane = static_cast<int64_t>(H) * Wp * 8;
+                    // the row's pad pixels stay zero
+                    for (int kk = 0; kk < 4 && xx == 0; ++kk)
+                        for (int pp = 0; pp < kPlanarPad; ++pp)
+                            *reinterpret_cast<uint4*>(yrow + kk * plane + pp * 8) = make_uint4(0u, 0u, 0u, 0u);
+                    for (int kk = 0; kk < 4 && xx == Wd - 1; ++kk)
+                        for (int pp = Wd + kPlanarPad; pp < Wp; ++pp)
+                            *reinterpret_cast<uint4*>(yrow + kk * plane + pp * 8) = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk) {
                         __nv_bfloat162 h[4];
@@ -1836,6 +1876,13 @@ struct FcgWs {
 
 constexpr int64_t kWtBytes = 9 * 32 * kPadC * 2; // prepared weights of one tensor-core layer
 
+// pixels of an activation buffer: H rows of planar_row(W) (the padded planar rows of the tcgen05
+// layers; the other layouts use H x W of them)
+inline int64_t act_pixels(int H, int W)
+{
+    return int64_t(H) * planar_row(W);
+}
+
 // network buffers: three activations [hw][32] BF16 and the four prepared weight sets (layers
 // 2, 3 in kWtBytes each; the first and last layer's smaller sets in the same room)
 inline char* carve_nn(char* c, int64_t hw, __nv_bfloat16** a1, __nv_bfloat16** a2,
@@ -1912,10 +1959,10 @@ inline void nn_prepare_weights(const gfgpu_nn_desc* nn, __nv_bfloat16* wt1, __nv
     k_nn_wprep_last<<<(9 * 8 * kPadC + 255) / 256, 256, 0, s>>>(wb(nn->weights_bf16, 3), wt3);
 }
 
-// TMA view of a channel-planar BF16 activation [4][H][W][8] as [4][H][2W] 8-byte elements; box
-// of box_px pixels of one row of one plane (k_conv32_tcp: 128, and 2 dil for the tail), zero fill
-// outside the grid
-inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W, int box_px)
+// TMA view of a channel-planar BF16 activation with padded rows ([4][H][Wp][8], Wp =
+// planar_row(W)) as [4][H][Wp/8][16] 8-byte elements; box: box_rows rows x 17 groups of 8
+// pixels (128-byte inner lines) of one plane, zero fill outside the grid
+inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W, int box_rows)
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
@@ -1927,13 +1974,13 @@ inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
     GF_REQUIRE((reinterpret_cast<uintptr_t>(X) & 15u) == 0, "activation not 16-byte aligned");
-    GF_REQUIRE(box_px >= 1 && box_px <= 128, "box width");
-    const cuuint64_t dims[3] = {2 * static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H), 4};
-    const cuuint64_t strides[2] = {static_cast<cuuint64_t>(W) * 16,
-                                   static_cast<cuuint64_t>(H) * static_cast<cuuint64_t>(W) * 16};
-    const cuuint32_t box[3] = {2 * static_cast<cuuint32_t>(box_px), 1, 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    CUresult rc = encode(map, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<__nv_bfloat16*>(X), dims, strides, box,
+    GF_REQUIRE(box_rows >= 1 && box_rows <= 256, "box rows");
+    const cuuint64_t Wp = static_cast<cuuint64_t>(planar_row(W));
+    const cuuint64_t dims[4] = {16, Wp / 8, static_cast<cuuint64_t>(H), 4};
+    const cuuint64_t strides[3] = {128, Wp * 16, static_cast<cuuint64_t>(H) * Wp * 16};
+    const cuuint32_t box[4] = {16, kTcpGroups, static_cast<cuuint32_t>(box_rows), 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult rc = encode(map, CU_TENSOR_MAP_DATA_TYPE_INT64, 4, const_cast<__nv_bfloat16*>(X), dims, strides, box,
                          estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (rc != CUDA_SUCCESS) return fail(GFGPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(rc)) + ")");
@@ -1958,27 +2005,30 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
         k_first_mma<false><<<grid, kMmaThreads, 0, s>>>(r, sc, rr_slot, nfree, nn->material, X0, wt0,
                                                         nn->params_f32 + b_off(0), H, W, a1);
     if (nn_tensor_path() >= 2) {
-        CUtensorMap m1, m1t, m2, m2t;
-        GF_TRY(tcp_tensor_map(&m1, a1, H, W, kTcM));
-        GF_TRY(tcp_tensor_map(&m1t, a1, H, W, 2 * dil_of(1)));
-        GF_TRY(tcp_tensor_map(&m2, a2, H, W, kTcM));
-        GF_TRY(tcp_tensor_map(&m2t, a2, H, W, 2 * dil_of(2)));
+        static_assert(kPlanarPad >= 4, "dilations up to 4 fit the 17-group box");
+        // path 2: one box per plane of a whole halo tile; path 3: one box per plane row
+        CUtensorMap m1, m2;
+        const bool ring = nn_tensor_path() == 3;
+        GF_TRY(tcp_tensor_map(&m1, a1, H, W, ring ? 1 : tc_rows(kTcpRPC, dil_of(1))));
+        GF_TRY(tcp_tensor_map(&m2, a2, H, W, ring ? 1 : tc_rows(kTcpRPC, dil_of(2))));
         const int ntiles = ((W + kTcM - 1) / kTcM) * ((H + kTcpRPC - 1) / kTcpRPC);
         int sms = 0, dev = 0;
         GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
         GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
         const unsigned g = static_cast<unsigned>(std::max(1, std::min(ntiles, sms)));
+        GF_REQUIRE(((reinterpret_cast<uintptr_t>(a1) | reinterpret_cast<uintptr_t>(a2)) & 15u) == 0,
+                   "activations not 16-byte aligned");
         if (nn_tensor_path() == 3) {
             k_conv32_tcr<kTcpRPC><<<g, kTcrThreads, tcr_smem_bytes(dil_of(1)), s>>>(
-                m1, m1t, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
+                m1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
             k_conv32_tcr<kTcpRPC><<<g, kTcrThreads, tcr_smem_bytes(dil_of(2)), s>>>(
-                m2, m2t, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
+                m2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
         }
         else {
             k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(1)), s>>>(
-                m1, m1t, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
+                m1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
             k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(2)), s>>>(
-                m2, m2t, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
+                m2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
         }
     }
     else if (nn_tensor_path() == 1) {
@@ -2170,12 +2220,12 @@ int64_t gfgpu_fcg_workspace_bytes(const gfgpu_verlet_desc* d, int32_t H, int32_t
                                   int32_t ndir)
 {
     if (!d || nkeep < 1 || ndir < 1 || ndir > 2 || nkeep + ndir > kMaxSlots) return 0;
-    return fcg_bytes(d, int64_t(H) * W, nkeep + ndir);
+    return fcg_bytes(d, act_pixels(H, W), nkeep + ndir);
 }
 
 int64_t gfgpu_nn_infer_workspace_bytes(int32_t H, int32_t W)
 {
-    return H > 0 && W > 0 ? nn_bytes(int64_t(H) * W) : 0;
+    return H > 0 && W > 0 ? nn_bytes(act_pixels(H, W)) : 0;
 }
 
 int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* workspace,
@@ -2189,7 +2239,7 @@ int gfgpu_nn_infer(const gfgpu_nn_desc* nn, const float* X0, float* Y, void* wor
     GF_TRY(prepare_mma(S(stream)));
     cudaStream_t s = S(stream);
     __nv_bfloat16 *a1, *a2, *a3, *wt1, *wt2, *wt0, *wt3;
-    carve_nn(static_cast<char*>(workspace), int64_t(nn->H) * nn->W, &a1, &a2, &a3, &wt1, &wt2, &wt0, &wt3);
+    carve_nn(static_cast<char*>(workspace), act_pixels(nn->H, nn->W), &a1, &a2, &a3, &wt1, &wt2, &wt0, &wt3);
     nn_prepare_weights(nn, wt1, wt2, wt0, wt3, s);
     return nn_forward(nn, nullptr, X0, nullptr, 0, 1.0, nullptr, 0, a1, a2, a3, wt1, wt2, wt0, wt3,
                       nullptr, Y, s);
@@ -2216,7 +2266,7 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
     cudaStream_t s = S(stream);
     if (nn) GF_TRY(prepare_mma(s));
     const int nslots = nkeep + ndir;
-    int64_t hw = nn ? int64_t(nn->H) * nn->W : 0;
+    int64_t hw = nn ? act_pixels(nn->H, nn->W) : 0;
     FcgWs w = carve_fcg(d, hw, nslots, workspace);
     const int64_t n = d->nnode * d->ndim;
     double *zc = nullptr, *vc = nullptr, *yc = nullptr;

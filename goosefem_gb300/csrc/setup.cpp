@@ -16,7 +16,7 @@ static thread_local std::string g_last_error;
 static int g_strict = 0;
 static int g_variant_elem = 0;
 static int g_variant_node = 0;
-static int g_nn_path = 0;
+static int g_nn_path = 2; // tcgen05 + TMA (the fastest form on GB300)
 
 int nn_tensor_path()
 {

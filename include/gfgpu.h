@@ -54,8 +54,8 @@ int gfgpu_set_strict(int strict);
  * elem_variant 1 = two neighbouring elements per thread in the uniform square Quad4 kernel,
  * node_variant 1 = both dofs of a node per thread in the node kernel. Same results. */
 int gfgpu_set_variant(int elem_variant, int node_variant);
-/* Tensor-core instructions of the network's 32 -> 32 layers (process-wide): 0 = mma.sync m16n8k16
- * (default), 1 = tcgen05.mma with TMEM accumulators, one tile per CTA, 2 = tcgen05.mma in a
+/* Tensor-core instructions of the network's 32 -> 32 layers (process-wide): 0 = mma.sync m16n8k16,
+ * 1 = tcgen05.mma with TMEM accumulators, one tile per CTA, 2 (default) = tcgen05.mma in a
  * persistent pipeline fed by TMA (cp.async.bulk.tensor) with 2-3 shared-memory stages of whole
  * halo tiles and double-buffered TMEM, 3 = the same pipeline with a ring of halo rows that
  * consecutive tiles of a column strip share (each row loaded once per run of tiles). Same
