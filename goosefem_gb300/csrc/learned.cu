@@ -924,12 +924,6 @@ __device__ __forceinline__ void mbar_arrive(uint32_t a)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(a) : "memory");
 }
 
-__device__ __forceinline__ void tc_commit(uint32_t a)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(a)
-                 : "memory");
-}
-
 // MMA and commit issued by one elected lane of a converged warp (the descriptors stay
 // warp-uniform, so the whole warp runs the issue loop)
 __device__ __forceinline__ void tc_mma_elect(uint32_t tmem, uint64_t da, uint64_t db, uint32_t acc)
@@ -956,7 +950,7 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __re
     extern __shared__ unsigned char tpsm[];
     unsigned char* wsm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tpsm) + 1023) & ~uintptr_t(1023));
     unsigned char* stages = wsm + kTcWBytes;
-    const int R = tc_rows(RPC, dil), C = tc_cols(dil), CP = tcp_row_pixels(dil);
+    const int R = tc_rows(RPC, dil), CP = tcp_row_pixels(dil);
     const uint32_t PL = tcp_plane_bytes(dil), SB = 4 * PL;
     const int NS = tcp_stages(dil);
     // full[4] empty[4] tfull[2] tempty[2], then the TMEM address slot
