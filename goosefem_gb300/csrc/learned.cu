@@ -450,6 +450,21 @@ __global__ void k_nn_wprep_first(const __nv_bfloat16* __restrict__ W, __nv_bfloa
 // LAST = false: Y = relu(conv + b), BF16 [H, W, 32] (NT = 4). LAST = true (NT = 1, the 32 -> 2
 // output layer): z = sigma (conv + b) on the free dofs, 0 on prescribed (FP64 nodevec; sigma =
 // RMS of the residual, sqrt(sc[rr_slot] / nfree)), or Yf [H, W, 2] FP32 when z is null.
+// Programmatic dependent launch between the network's layers: a layer lets the next one launch
+// as soon as all of its CTAs are resident (the next one's launch, TMEM allocation, barrier set-up
+// and weight load then overlap this layer's tail) and waits for the previous layer's grid to
+// complete before it touches the previous layer's output or writes anything. Both are no-ops for
+// a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_launch_dependents()
+{
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void pdl_wait()
+{
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+
 // Channel-planar activations of the tcgen05 layers: [4][H][Wp][8] BF16, pixel (y, x) stored at
 // row position x + kPlanarPad, Wp = planar_row(W) (a multiple of 8 pixels); the pad pixels are
 // zero. Rows of 128-byte groups of 8 pixels make a halo tile one TMA box per plane with
@@ -470,6 +485,7 @@ k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict_
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double s_sigma;
+    if (PLANAR_IN) pdl_wait(); // launched as a dependent of the tcgen05 layer
     const int hh = kTileY + 2 * dil, hw = kTileX + 2 * dil;
     __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(smem);          // [hh][hw][40]
     __nv_bfloat16* ws = halo + hh * hw * kPadC;                             // [9][8 NT][40]
@@ -579,6 +595,7 @@ k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_
     __shared__ __align__(16) __nv_bfloat16 halo[hh * hw * 4];
     __shared__ __align__(16) __nv_bfloat16 wf[3 * 32 * kPadF];
     __shared__ float s_inv;
+    if (PLANAR_OUT) pdl_launch_dependents(); // the tcgen05 layer that follows may launch
     const int y0 = blockIdx.y * kTileY, x0 = blockIdx.x * kTileX;
     for (int i = threadIdx.x; i < 3 * 32 * kPadF / 8; i += blockDim.x) cp_async16(wf + i * 8, WF + i * 8, true);
     if (threadIdx.x == 0) {
@@ -965,6 +982,7 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __re
     auto tempty = [&](int i) { return s_bar + 8u * (2 * kTcpMaxStages + 2 + i); };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tiles_x = (Wd + kTcM - 1) / kTcM, ntiles = tiles_x * ((H + RPC - 1) / RPC);
+    pdl_launch_dependents();
 
     if (warp == 1) {
         const uint32_t s_slot = static_cast<uint32_t>(__cvta_generic_to_shared(tslot));
@@ -991,6 +1009,7 @@ k_conv32_tcp(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __re
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t taddr = *tslot;
+    pdl_wait(); // the previous layer's output is complete from here on
 
     if (warp == 0) { // TMA producer: the whole warp waits, one lane loads the 4 planes of a tile
         // box: R rows x 17 groups of 8 pixels (128-byte lines) from planar position x0, i.e. image
@@ -1981,6 +2000,25 @@ inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W
     return GFGPU_OK;
 }
 
+// launch with programmatic stream serialisation (the kernel's pdl_wait orders it after the
+// previous kernel of the stream)
+template <typename... KArgs, typename... Args>
+inline int launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                      Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return check_cuda(cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...), "cudaLaunchKernelEx");
+}
+
 // the four layers on one H x W grid: input from the FP64 residual (r != null) or from X0,
 // output to the FP64 correction z (z != null) or to Y
 inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0, const double* sc,
@@ -2019,10 +2057,10 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
                 m2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
         }
         else {
-            k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(1)), s>>>(
-                m1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2);
-            k_conv32_tcp<kTcpRPC><<<g, kTcpThreads, tcp_smem_bytes(dil_of(2)), s>>>(
-                m2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3);
+            GF_TRY(launch_pdl(k_conv32_tcp<kTcpRPC>, dim3(g), dim3(kTcpThreads), tcp_smem_bytes(dil_of(1)), s,
+                              m1, wt1, nn->params_f32 + b_off(1), dil_of(1), H, W, a2));
+            GF_TRY(launch_pdl(k_conv32_tcp<kTcpRPC>, dim3(g), dim3(kTcpThreads), tcp_smem_bytes(dil_of(2)), s,
+                              m2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3));
         }
     }
     else if (nn_tensor_path() == 1) {
@@ -2042,7 +2080,11 @@ inline int nn_forward(const gfgpu_nn_desc* nn, const double* r, const float* X0,
             a2, wt2, nn->params_f32 + b_off(2), dil_of(2), H, W, a3, nullptr, 0, 0.0, nullptr, 0, nullptr,
             nullptr);
     }
-    if (planar)
+    if (planar && nn_tensor_path() == 2)
+        GF_TRY(launch_pdl(k_conv_mma<1, true, true>, grid, dim3(kMmaThreads), mma_smem_bytes(dil_of(3), 1), s, a3,
+                          static_cast<const __nv_bfloat16*>(wt3), static_cast<const float*>(nn->params_f32 + b_off(3)),
+                          dil_of(3), H, W, static_cast<__nv_bfloat16*>(nullptr), sc, rr_slot, nfree, part, nnu, z, Y));
+    else if (planar)
         k_conv_mma<1, true, true><<<grid, kMmaThreads, mma_smem_bytes(dil_of(3), 1), s>>>(
             a3, wt3, nn->params_f32 + b_off(3), dil_of(3), H, W, nullptr, sc, rr_slot, nfree, part, nnu, z,
             Y);
