@@ -1,14 +1,23 @@
-"""Benchmark: explicit velocity-Verlet dynamics of a 2048 x 2048 Quad4 Regular mesh (FP64).
+"""Benchmark: explicit velocity-Verlet dynamics of a 2048 x 2048 Quad4 Regular mesh (FP64 state),
+plus the static, batched and learned-preconditioner workloads.
 
-Workload (one bench step = 1000 increments of the explicit scheme of GooseFEM's
+Headline (one bench step = 1000 increments of the explicit scheme of GooseFEM's
 docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp): 4,194,304 elements, 4,198,401 nodes,
 plane-strain linear elasticity with per-element K ~ U[0.5,1.5], G ~ U[0.25,0.75] (seeded),
 density 1 (lumped mass from nodal quadrature), nodal viscous damping 0.1, bottom row fixed,
-random initial velocity U[-1e-3, 1e-3], dt = 0.1 x the CFL limit.
+random initial velocity U[-1e-3, 1e-3], dt = 0.1 x the CFL limit. By default the increments run
+in float-float arithmetic (--arith pair: FP64 state in and out, pairs of FP32 numbers inside one
+fused kernel per increment); --arith fp64 runs the FP64 kernels. Metric: element-Gauss-point
+updates per second (nelem x 4 Gauss points x increments / s).
 
-Metric: element-Gauss-point updates per second (nelem x 4 Gauss points x increments / s).
+The default single-GPU run also measures, under "workloads" in the same JSON line:
+  static   Hex8 128^3 matrix-free Jacobi-PCG to 1e-8 (vs the oracle's matvec on the host cores),
+  batch    256 periodic Quad4 instances x 500 increments (vs the instances one at a time),
+  learned  Quad4 512^2 two-phase static solve to 1e-8: learned two-level FCG and the one-level
+           learned FCG (network trained on 4096 Jacobi-PCG pairs) vs Jacobi-PCG on the same GPU.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gfgpu|reference]
+                  [--workload explicit|static|batch|learned] [--no-workloads]
 
 --impl reference times the reference algorithm's CPU implementation on the host cores: the
 reference (header-only C++ on xtensor/Eigen) cannot be built here, so its restatement in
@@ -75,6 +84,14 @@ def parse():
     p.add_argument("--path", default="auto", choices=["auto", "uniform", "general"],
                    help="element kernel: auto (fastest applicable), uniform (closed form with K, G "
                         "read every increment) or general (per Gauss point, stored dNx)")
+    p.add_argument("--arith", default="pair", choices=["pair", "fp64"],
+                   help="explicit workload: float-float fused kernel (pair) or the FP64 kernels")
+    p.add_argument("--no-workloads", action="store_true",
+                   help="headline only (skip the static, batch and learned workloads)")
+    p.add_argument("--train-steps-1level", type=int, default=6000,
+                   help="learned workload: Adam steps of the one-level network")
+    p.add_argument("--pairs-1level", type=int, default=64,
+                   help="learned workload: Jacobi-PCG loads of the one-level pairs (x 64 snapshots)")
     return p.parse_args()
 
 
@@ -253,6 +270,32 @@ def run_reference(args, rank, world):
     return 0
 
 
+def _event_ms(fn, stream):
+    import torch
+
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def _profile_value(kernel, nx, key):
+    """A figure recorded in the ncu summary profiles/<kernel>_<nx>.txt ("key: value" lines)."""
+    prof = os.path.join(ROOT, "profiles", f"{kernel}_{nx}.txt")
+    if os.path.exists(prof):
+        for ln in open(prof):
+            if ln.startswith(key + ":"):
+                v = ln.split(":", 1)[1].strip()
+                try:
+                    return float(v)
+                except ValueError:
+                    return v
+    return None
+
+
 def run_gpu(args, rank, world):
     import torch
 
@@ -266,9 +309,11 @@ def run_gpu(args, rank, world):
     _lib.call("gfgpu_set_variant", ev, nv)
     w = workload(args.nx, gf.Mesh)
     nnode, nelem, inc = w["nnode"], w["nelem"], args.increments
+    pair = args.arith == "pair" and args.path == "auto"
     vv = gf.VelocityVerlet(w["coor"], w["conn"], w["dofs"], w["K"], w["G"], rho=1.0, dt=w["dt"],
                            eta=w["eta"], iip=w["iip"], uniform=(False if args.path == "general"
-                                                                else "auto"))
+                                                                else "auto"),
+                           arithmetic="pair" if pair else "fp64")
     if args.path == "uniform":
         vv.use_uniform_onthefly()
     u = torch.zeros((nnode, 2), dtype=torch.float64, device=dev)
@@ -297,48 +342,52 @@ def run_gpu(args, rank, world):
     ms = e0.elapsed_time(e1)
     clocks = sampler.stop() if sampler else None
     value, ms = job_rate(nelem * NIP * inc * args.steps, ms, world, dev)
+    ms_inc = ms / (args.steps * inc)
 
     # ---------------------------------------------------------------- per-kernel timing
-    # element kernel alone (same launch as inside the step), on the launching stream
     fe = vv.ws
-    reps = 50
-    k0 = torch.cuda.Event(enable_timing=True)
-    k1 = torch.cuda.Event(enable_timing=True)
-    for _ in range(3):
-        _lib.call("gfgpu_verlet_element_forces", C.addressof(vv.desc), u.data_ptr(),
-                  fe.data_ptr(), stream.cuda_stream)
-    k0.record(stream)
-    for _ in range(reps):
-        _lib.call("gfgpu_verlet_element_forces", C.addressof(vv.desc), u.data_ptr(),
-                  fe.data_ptr(), stream.cuda_stream)
-    k1.record(stream)
-    torch.cuda.synchronize()
-    ms_elem = k0.elapsed_time(k1) / reps
-    ms_inc = ms / (args.steps * inc)
-    ms_node = max(ms_inc - ms_elem, 0.0)
+    if pair:
+        # the fused increment kernel alone: two calls of different lengths on the launching
+        # stream; the difference cancels the per-call FP64 <-> pair conversions
+        n1, n2 = 20, 220
+        t1 = min(_event_ms(lambda: vv.step(u, v, a, n1), stream) for _ in range(3))
+        t2 = min(_event_ms(lambda: vv.step(u, v, a, n2), stream) for _ in range(3))
+        ms_kernel = (t2 - t1) / (n2 - n1)
+        ms_elem, ms_node = None, None
+        # the FP64 kernels on the same state, for comparison
+        vv.use_fp64()
+        vv.step(u, v, a, 20)
+        ms_fp64 = min(_event_ms(lambda: vv.step(u, v, a, 200), stream) for _ in range(2)) / 200
+        vv.use_pair()
+    else:
+        reps = 50
+        for _ in range(3):
+            _lib.call("gfgpu_verlet_element_forces", C.addressof(vv.desc), u.data_ptr(),
+                      fe.data_ptr(), stream.cuda_stream)
+        ms_elem = _event_ms(lambda: [_lib.call("gfgpu_verlet_element_forces", C.addressof(vv.desc),
+                                               u.data_ptr(), fe.data_ptr(), stream.cuda_stream)
+                                     for _ in range(reps)], stream) / reps
+        ms_kernel = ms_elem
+        ms_node = max(ms_inc - ms_elem, 0.0)
+        ms_fp64 = None
 
     fp64_peak = fp64_probe()
 
     # ---------------------------------------------------------------- end-to-end (host buffers)
+    # through the public Capital method VelocityVerlet.Step: pinned host state in, the step's
+    # host state out, every bench step
     hu = torch.zeros((nnode, 2), dtype=torch.float64).pin_memory()
     hv = torch.tensor(w["v0"]).pin_memory()
     ha = torch.zeros((nnode, 2), dtype=torch.float64).pin_memory()
-    ou = torch.empty_like(hu).pin_memory()
-    ov = torch.empty_like(hu).pin_memory()
-    oa = torch.empty_like(hu).pin_memory()
+    out = vv.Step(hu, hv, ha, inc)  # warm-up (allocates the pinned outputs)
     barrier()
+    t0 = time.perf_counter()
     e0.record(stream)
     for _ in range(args.steps):
-        u.copy_(hu, non_blocking=True)
-        v.copy_(hv, non_blocking=True)
-        a.copy_(ha, non_blocking=True)
-        vv.step(u, v, a, inc)
-        ou.copy_(u, non_blocking=True)
-        ov.copy_(v, non_blocking=True)
-        oa.copy_(a, non_blocking=True)
+        out = vv.Step(hu, hv, ha, inc, out=out)
     e1.record(stream)
     barrier()
-    ms_e2e = e0.elapsed_time(e1)
+    ms_e2e = 1e3 * (time.perf_counter() - t0)
     e2e_value, ms_e2e = job_rate(nelem * NIP * inc * args.steps, ms_e2e, world, dev)
     state_bytes = 3 * nnode * 2 * 8
 
@@ -352,61 +401,72 @@ def run_gpu(args, rank, world):
         hbm_peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
     path = vv.path
-    kernel = {"uniform-square": "k_elem_force_quad4_square", "uniform": "k_elem_force_quad4_uniform",
+    kernel = {"uniform-square-pair": "k_verlet_pair_quad4",
+              "uniform-square": "k_elem_force_quad4_square", "uniform": "k_elem_force_quad4_uniform",
               "general": "k_elem_force_general"}[path]
-    # algorithmic bytes of one element-kernel launch: u (16 B/node), conn (16 B/elem), material
-    # (K, G: 16 B/elem, or the 4 precomputed coefficients: 32 B/elem), element forces out
-    # (64 B/elem); the general path also streams dNx and vol (72 B/elem)
-    mat = 32 if path == "uniform-square" else 16
-    b_elem = 16 * nnode + (16 + mat + 64) * nelem + (72 * nelem if path == "general" else 0)
-    achieved = b_elem / (ms_elem * 1e-3) / 1e9
-    # FP64 operations of the element kernel per element, DFMA counted as 2 (from the source:
-    # square 34 instructions incl. 2 DFMA; uniform 48 incl. 7; general per Gauss point 8+8+9 FMA
-    # strain, 7 stress, 16 FMA + 8 force)
-    fl_elem = {"uniform-square": 36, "uniform": 55, "general": 4 * (2 * 25 + 7 + 2 * 16 + 8)}[path]
-    # FP64 instructions per element (DADD, DMUL and DFMA issue at the same rate)
-    in_elem = {"uniform-square": 34, "uniform": 48, "general": 4 * (25 + 7 + 16 + 8)}[path]
-    fp64_ach = fl_elem * nelem / (ms_elem * 1e-3)
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", f"{kernel}_{args.nx}.txt")
-    if os.path.exists(prof):
-        for ln in open(prof):
-            if ln.startswith("dram_bytes_per_launch:"):
-                traffic = float(ln.split(":", 1)[1])
-    # fused-step minimum traffic: u, v, a read+write (96 B/node), inverse mass (16 B/node),
-    # K, G (16 B/elem)
+    # fused-step minimum traffic (SURVEY-defined algorithmic bytes of one increment): u, v, a
+    # read+write (96 B/node), inverse mass (16 B/node), K, G (16 B/elem)
     b_step = 112 * nnode + 16 * nelem
+    if pair:
+        # one fused kernel per increment: its algorithmic bytes are the increment's
+        b_launch = b_step
+    else:
+        # element kernel: u (16 B/node), conn (16 B/elem), material (K, G: 16 B/elem, or the 4
+        # precomputed coefficients: 32 B/elem), element forces out (64 B/elem); the general path
+        # also streams dNx and vol (72 B/elem)
+        mat = 32 if path == "uniform-square" else 16
+        b_launch = 16 * nnode + (16 + mat + 64) * nelem + (72 * nelem if path == "general" else 0)
+    achieved = b_launch / (ms_kernel * 1e-3) / 1e9
+    traffic = _profile_value(kernel, args.nx, "dram_bytes_per_launch")
+    binding = _profile_value(kernel, args.nx, "binding_resource")
+    roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm_peak,
+            "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+            "peak_source": peak_src, "ms_per_launch": ms_kernel, "alg_bytes_per_launch": b_launch,
+            "step": {"ms_per_increment": ms_inc, "alg_bytes": b_step,
+                     "achieved_gbs": b_step / (ms_inc * 1e-3) / 1e9,
+                     "frac": b_step / (ms_inc * 1e-3) / 1e9 / hbm_peak}}
+    if binding is not None:
+        roof["binding_resource"] = binding
+    if pair:
+        roof["fp64_kernels"] = {
+            "ms_per_increment": ms_fp64, "value": nelem * NIP / (ms_fp64 * 1e-3),
+            "note": "the FP64 element + node kernels on the same state (34 + 2 x 10 FP64 "
+                    "instructions per node, at GB300's FP64 issue rate)",
+            "fp64_probe_tflops": fp64_peak / 1e12}
+    else:
+        # FP64 operations of the element kernel per element, DFMA counted as 2
+        fl_elem = {"uniform-square": 36, "uniform": 55, "general": 4 * (2 * 25 + 7 + 2 * 16 + 8)}[path]
+        in_elem = {"uniform-square": 34, "uniform": 48, "general": 4 * (25 + 7 + 16 + 8)}[path]
+        roof["bound"] = "fp64"
+        roof["step"]["ms_node_kernel"] = ms_node
+        roof["fp64"] = {"achieved_tflops": fl_elem * nelem / (ms_elem * 1e-3) / 1e12,
+                        "peak_tflops": fp64_peak / 1e12,
+                        "frac": fl_elem * nelem / (ms_elem * 1e-3) / fp64_peak,
+                        "instr_per_elem": in_elem,
+                        "achieved_ginstr_s": in_elem * nelem / (ms_elem * 1e-3) / 1e9,
+                        "peak_ginstr_s": fp64_peak / 2.0 / 1e9,
+                        "instr_frac": in_elem * nelem / (ms_elem * 1e-3) / (fp64_peak / 2.0),
+                        "peak_source": "measured live (gfgpu_probe_fp64: DFMA chains)"}
     line = {
         "metric": "elem-Gauss-pt updates/s", "value": value, "unit": "elem-Gauss-pt/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "vs_baseline": None,
+        "dtype": ("f32x2 (float-float pairs, 48-bit significands; FP64 state in and out)"
+                  if pair else "f64"),
+        "data": "synthetic (seeded)",
         "config": {"workload": f"Quad4 Regular {args.nx}x{args.nx} explicit velocity-Verlet, "
                                "per-element K,G, density 1, damping 0.1, bottom row fixed",
                    "nelem": nelem, "nnode": nnode, "increments_per_step": inc,
-                   "element_path": path, "kernel_variant": args.kernel_variant,
-                   "l2": "inputs larger than L2 (working set > 0.6 GB); no flush",
+                   "element_path": path, "arithmetic": vv.arithmetic,
+                   "kernel_variant": args.kernel_variant,
+                   "l2": "inputs larger than L2 (working set > 0.5 GB); no flush",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "binding_resource": "fp64 issue rate (see fp64)",
-                     "kernel": kernel, "achieved": achieved, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                     "peak_source": peak_src, "ms_per_launch": ms_elem,
-                     "alg_bytes_per_launch": b_elem,
-                     "fp64": {"achieved_tflops": fp64_ach / 1e12,
-                              "peak_tflops": fp64_peak / 1e12,
-                              "frac": fp64_ach / fp64_peak,
-                              "flops_per_elem": fl_elem,
-                              "instr_per_elem": in_elem,
-                              "achieved_ginstr_s": in_elem * nelem / (ms_elem * 1e-3) / 1e9,
-                              "peak_ginstr_s": fp64_peak / 2.0 / 1e9,
-                              "instr_frac": in_elem * nelem / (ms_elem * 1e-3) / (fp64_peak / 2.0),
-                              "peak_source": "measured live (gfgpu_probe_fp64: DFMA chains)"},
-                     "step": {"ms_per_increment": ms_inc, "ms_node_kernel": ms_node,
-                              "alg_bytes": b_step,
-                              "achieved_gbs": b_step / (ms_inc * 1e-3) / 1e9}},
+        "roofline": roof,
         "e2e": {"value": e2e_value, "unit": "elem-Gauss-pt/s", "h2d_bytes_per_step": state_bytes,
-                "d2h_bytes_per_step": state_bytes},
-        "gpu_launches": args.steps * (1 + 2 * inc),
+                "d2h_bytes_per_step": state_bytes,
+                "via": "VelocityVerlet.Step (pinned host u, v, a in and out every step)"},
+        "gpu_launches": args.steps * ((inc + 2) if pair else (1 + 2 * inc)),
         "clocks": clocks,
     }
     if world == 1 and not args.no_cpu:
@@ -427,8 +487,34 @@ def run_gpu(args, rank, world):
         except Exception as ex:  # the baseline never blocks the GPU line
             line["cpu_baseline"] = {"value": None, "unit": "elem-Gauss-pt/s", "cores": threads,
                                     "kind": "port", "sample": f"failed: {ex}"}
+    del vv, u, v, a, hu, hv, ha, out, fe
+    torch.cuda.empty_cache()
+    if world == 1 and not args.no_workloads:
+        line["workloads"] = {}
+        for name, fn in (("static", workload_static), ("batch", workload_batch),
+                         ("learned", workload_learned)):
+            try:
+                line["workloads"][name] = _with_clocks(fn, args)
+            except Exception as ex:  # a failing workload is reported, not fatal to the line
+                line["workloads"][name] = {"error": f"{type(ex).__name__}: {ex}"}
+            torch.cuda.empty_cache()
     print(json.dumps(line), flush=True)
     return 0
+
+
+def _with_clocks(fn, args):
+    import torch
+
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    t0 = time.perf_counter()
+    try:
+        res = fn(args)
+    finally:
+        clocks = sampler.stop()
+    res["clocks"] = clocks
+    res["wall_seconds"] = time.perf_counter() - t0
+    return res
 
 
 def static_case(n, seed=3):
@@ -501,9 +587,10 @@ def fp64_probe():
     return 2.0 * 16 * iters * blocks * 256 / (k0.elapsed_time(k1) * 1e-3)
 
 
-def run_static(args):
-    """3-d static case: Hex8 128^3 matrix-free Jacobi-PCG to 1e-8 relative residual (FP64).
-    One bench step = one full solve from a zero initial guess."""
+def workload_static(args):
+    """3-d static case: Hex8 n3d^3 matrix-free Jacobi-PCG to 1e-8 relative residual (FP64), two
+    timed solves from a zero initial guess (best counts), against the oracle's matrix-free
+    operator (one stiffness action) on the host cores."""
     import torch
 
     import goosefem_gb300 as gf
@@ -523,39 +610,73 @@ def run_static(args):
         x.view(-1)[iip_d] = xp_d
         return st.solve(x, tol=1e-8, check_every=16)
 
-    for _ in range(args.warmup):
-        solve()
+    solve()  # warm-up
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    its = []
-    for _ in range(args.steps):
+    secs, its = [], []
+    for _ in range(2):
+        t0 = time.perf_counter()
         its.append(solve())
-    torch.cuda.synchronize()
-    sec = (time.perf_counter() - t0) / args.steps
+        torch.cuda.synchronize()
+        secs.append(time.perf_counter() - t0)
+    sec = min(secs)
     it, rel = its[-1]
-    line = {"metric": "time-to-1e-8 resid (Jacobi-PCG)", "value": sec, "unit": "s",
-            "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": sec * 1e3, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"Hex8 Regular {n}^3 static, z=0 fixed, top uz=-1e-2, "
-                                   "matrix-free Jacobi-PCG", "element_path":
-                       ("uniform-cube" if st.coef is not None else "uniform") if st.uniform
-                       else "general"},
-            "iterations": it, "relres_true": rel, "ms_per_iteration": sec * 1e3 / it,
-            "elem_updates_per_s": n ** 3 * 8 * it / sec}
+    res = {"metric": "time-to-1e-8 resid (Jacobi-PCG)", "value": sec, "unit": "s",
+           "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded)",
+           "config": {"workload": f"Hex8 Regular {n}^3 static, z=0 fixed, top uz=-1e-2, "
+                                  "matrix-free Jacobi-PCG", "element_path":
+                      ("uniform-cube" if st.coef is not None else "uniform") if st.uniform
+                      else "general", "solves_timed": len(secs)},
+           "iterations": it, "relres_true": rel, "ms_per_iteration": sec * 1e3 / it,
+           "elem_updates_per_s": n ** 3 * 8 * it / sec}
     if st.coef is not None and st.desc.reg_nz > 0:
         # FP64 instructions of one iteration of the cube / Regular path: element kernel ~171 per
         # element, gather 8 adds + 1 FMA, update 5 per free dof, direction 1 per dof
         nfree = nnode * 3 - iip.size
         instr = 171 * n ** 3 + 14 * nfree + nnode * 3
         peak = fp64_probe() / 2.0
-        line["fp64"] = {"instr_per_iteration": instr, "achieved_ginstr_s": instr / (sec / it) / 1e9,
-                        "peak_ginstr_s": peak / 1e9, "instr_frac": instr / (sec / it) / peak,
-                        "peak_source": "measured live (gfgpu_probe_fp64: DFMA chains)"}
-    print(json.dumps(line), flush=True)
+        res["fp64"] = {"instr_per_iteration": instr, "achieved_ginstr_s": instr / (sec / it) / 1e9,
+                       "peak_ginstr_s": peak / 1e9, "instr_frac": instr / (sec / it) / peak,
+                       "peak_source": "measured live (gfgpu_probe_fp64: DFMA chains)"}
+    del st, x
+    if not args.no_cpu:
+        try:
+            res["cpu_baseline"] = static_cpu_matvec(coor, conn, K, G)
+            res["cpu_baseline"]["gpu_ms_per_iteration"] = res["ms_per_iteration"]
+        except Exception as ex:
+            res["cpu_baseline"] = {"error": f"{type(ex).__name__}: {ex}"}
+    return res
+
+
+def static_cpu_matvec(coor, conn, K, G):
+    """One stiffness action of the oracle (the reference's per-operator chain: AsElement,
+    SymGradN_vector, stress, Int_gradN_dot_tensor2_dV, AssembleNode) on all host threads; the set-up
+    (compute_dN) is not timed."""
+    from oracle import gfref as R
+
+    threads = R.num_threads(True)
+    xr = R.as_element(conn, coor)
+    dNx, vol = R.compute_dN(xr, *R.hex8_gauss(), parallel=True)
+    del xr
+    u = np.random.default_rng(11).uniform(-1e-3, 1e-3, coor.shape)
+    t0 = time.perf_counter()
+    ue = R.as_element(conn, u)
+    eps = R.sym_grad_n_vector(dNx, ue, parallel=True)
+    sig = R.elastic_stress(eps, K, G, parallel=True)
+    fe = R.int_grad_n_dot_tensor2_dv(dNx, vol, sig, parallel=True)
+    R.assemble_node(conn, np.arange(coor.shape[0] * 3).reshape(-1, 3), fe)
+    t = time.perf_counter() - t0
+    return {"value": t, "unit": "s per stiffness action", "cores": threads, "kind": "port",
+            "sample": f"one matrix-free stiffness action of the oracle at {conn.shape[0]} Hex8 "
+                      f"elements, {threads} OpenMP threads ({cpu_info()}); the element loops in "
+                      "parallel, the assembly serial as in the reference"}
+
+
+def run_static(args):
+    print(json.dumps(workload_static(args)), flush=True)
     return 0
 
 
-def run_batch(args):
+def workload_batch(args):
     """256 periodic Quad4 instances (nx, ny ~ U{32..512}), 500 increments each, one batched
     launch schedule (autotuned) vs the instances one at a time."""
     import torch
@@ -580,20 +701,26 @@ def run_batch(args):
         bv.check_status()
     sec = e0.elapsed_time(e1) * 1e-3
     seq = B.run_sequential(inst, nsteps, bv.dt)
-    line = {"metric": "elem-Gauss-pt updates/s (batched)", "value": bv.nelem * 4 * nsteps / sec,
-            "unit": "elem-Gauss-pt/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f64",
-            "data": "synthetic (seeded)",
-            "config": {"workload": f"{len(inst)} periodic Quad4 Regular instances, nx,ny~U{{32..512}},"
-                                   f" {nsteps} increments, applied shear 1e-3",
-                       "nelem_total": bv.nelem, "schedule": {"mode": ["graph of 2 kernels",
-                                                                       "persistent"][bv.mode],
-                                                             "block": bv.block,
-                                                             "blocks_per_sm": bv.bps}},
-            "seconds": sec, "sequential_seconds": seq, "speedup_vs_sequential": seq / sec,
-            "autotune": [{"mode": r[0], "block": r[1], "bps": r[2], "ms_per_increment": r[3]}
-                         for r in table]}
-    print(json.dumps(line), flush=True)
+    res = {"metric": "elem-Gauss-pt updates/s (batched)", "value": bv.nelem * 4 * nsteps / sec,
+           "unit": "elem-Gauss-pt/s", "higher_is_better": True, "dtype": "f64",
+           "data": "synthetic (seeded)",
+           "config": {"workload": f"{len(inst)} periodic Quad4 Regular instances, nx,ny~U{{32..512}},"
+                                  f" {nsteps} increments, applied shear 1e-3",
+                      "nelem_total": bv.nelem,
+                      "schedule": {"mode": ["graph of 2 kernels", "persistent"][bv.mode],
+                                   "block": bv.block, "blocks_per_sm": bv.bps},
+                      "colouring": "none: the node kernels gather through the dof CSR "
+                                   "(deterministic, no scatter conflicts to colour)"},
+           "seconds": sec, "ms_per_increment": 1e3 * sec / nsteps, "sequential_seconds": seq,
+           "speedup_vs_sequential": seq / sec,
+           "autotune": [{"mode": r[0], "block": r[1], "bps": r[2], "ms_per_increment": r[3]}
+                        for r in table]}
     bv.release()
+    return res
+
+
+def run_batch(args):
+    print(json.dumps(workload_batch(args)), flush=True)
     return 0
 
 
@@ -603,60 +730,79 @@ def _lib_call_bytes(H, W):
     return _lib.lib().gfgpu_nn_infer_workspace_bytes(H, W)
 
 
-def run_learned(args):
-    """Quad4 512^2 two-phase static case, every solve to 1e-8 relative residual in FP64
-    (time-to-solution on the same GPU; coarse set-up, pair generation and training reported
-    apart): Jacobi-PCG (the baseline; step-by-step session solver and the ring solver with the
-    Jacobi direction alone replayed as a CUDA graph, the faster of the two counts), the two-level
-    flexible CG without the network (the method without it), and the learned two-level solve
-    (the network as the post-smoother of the two-level step)."""
-    import torch
-
+def _learned_problem(args):
     from goosefem_gb300 import learned as LR
     from goosefem_gb300 import mesh as M
 
-    from goosefem_gb300 import _lib as _L
-
-    _L.call("gfgpu_set_nn_tensor_path", int(args.nn_path))
     nx = args.n2d
     K, G, inside = LR.inclusion_material(nx, nx, 512)
     m = M.Quad4.Regular(nx, nx)
     iip, xp = LR.static_bc(m)
-    lp = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0)
+    return LR, nx, K, G, inside, iip, xp
 
-    def timed(fn):
+
+def run_learned(args):
+    """Kernel-share probe of the learned workload (--profile-iters > 0), else the workload line."""
+    import torch
+
+    from goosefem_gb300 import _lib
+
+    if args.profile_iters <= 0:
+        print(json.dumps(workload_learned(args)), flush=True)
+        return 0
+    _lib.call("gfgpu_set_nn_tensor_path", int(args.nn_path))
+    LR, nx, K, G, inside, iip, xp = _learned_problem(args)
+    lp = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0)
+    # the coarse set-up, then each two-level solver for a fixed number of iterations (untrained
+    # network)
+    lp.coarse_setup(args.hc)
+    k = args.profile_iters
+    for name, kw in (("twolevel", dict(use_nn=False, nkeep=1)),
+                     ("learned_twolevel_keep4", dict(use_nn=True, nkeep=4, post=True))):
         x = lp.initial_guess(xp)
+        try:
+            lp.fcg(x, maxiter=k, coarse=True, **kw)
+        except _lib.GFGPUError as e:
+            if e.code != -8:
+                raise
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": "learned kernel-share probe (untrained network)",
+                      "config": {"nx": nx, "hc": args.hc, "iterations": k,
+                                 "nn_path": args.nn_path},
+                      "network_application_ms": network_ms(lp, nx + 1)}), flush=True)
+    return 0
+
+
+def workload_learned(args):
+    """Quad4 512^2 two-phase static case, every solve to 1e-8 relative residual in FP64
+    (time-to-solution on the same GPU; coarse set-up, pair generation and training reported
+    apart): Jacobi-PCG (the baseline; step-by-step session solver and the ring solver with the
+    Jacobi direction alone replayed as a CUDA graph, the faster of the two counts), the two-level
+    flexible CG without the network (the method without it), the learned two-level solve (the
+    network as the post-smoother of the two-level step) and the one-level learned flexible CG
+    (the network trained on 4096 (residual, Jacobi-PCG correction) pairs as the second direction
+    beside Jacobi)."""
+    import torch
+
+    from goosefem_gb300 import _lib as _L
+
+    _L.call("gfgpu_set_nn_tensor_path", int(args.nn_path))
+    LR, nx, K, G, inside, iip, xp = _learned_problem(args)
+    lp = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0)
+    reps = 2
+
+    def timed(fn, l=lp):
+        x = l.initial_guess(xp)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         out = fn(x)
         torch.cuda.synchronize()
         return (time.perf_counter() - t0,) + tuple(out)
 
-    def best_of(fn):
-        timed(fn)  # warm-up
-        return min((timed(fn) for _ in range(args.steps)), key=lambda r: r[0])
+    def best_of(fn, l=lp):
+        timed(fn, l)  # warm-up
+        return min((timed(fn, l) for _ in range(reps)), key=lambda r: r[0])
 
-    if args.profile_iters > 0:
-        # kernel-share probe: the coarse set-up, then each two-level solver for a fixed number of
-        # iterations (untrained network)
-        from goosefem_gb300 import _lib
-
-        lp.coarse_setup(args.hc)
-        k = args.profile_iters
-        for name, kw in (("twolevel", dict(use_nn=False, nkeep=1)),
-                         ("learned_twolevel_keep4", dict(use_nn=True, nkeep=4, post=True))):
-            x = lp.initial_guess(xp)
-            try:
-                lp.fcg(x, maxiter=k, coarse=True, **kw)
-            except _lib.GFGPUError as e:
-                if e.code != -8:
-                    raise
-        torch.cuda.synchronize()
-        print(json.dumps({"workload": "learned kernel-share probe (untrained network)",
-                          "config": {"nx": nx, "hc": args.hc, "iterations": k,
-                                     "nn_path": args.nn_path},
-                          "network_application_ms": network_ms(lp, nx + 1)}), flush=True)
-        return 0
     res = {}
     for name, fn in (("jacobi_pcg", lambda x: lp.jacobi_pcg(x)),
                      ("jacobi_pcg_graph", lambda x: lp.fcg(x, use_nn=False, nkeep=1))):
@@ -673,7 +819,7 @@ def run_learned(args):
     res["twolevel"] = min((v for k, v in res.items() if k.startswith("twolevel_check")),
                           key=lambda v: v["seconds"])
     t0 = time.perf_counter()
-    npairs = lp.make_pairs_twolevel(nloads=args.nloads, snaps=48, every=4, target="cheb",
+    npairs = lp.make_pairs_twolevel(nloads=args.nloads, snaps=64, every=4, target="cheb",
                                     degree=args.cheb_degree, post=True)
     torch.cuda.synchronize()
     t_pairs = time.perf_counter() - t0
@@ -689,35 +835,69 @@ def run_learned(args):
                 "seconds": b[0], "iterations": b[1], "fallback_iterations": b[2], "relres_true": b[3]}
     res["learned_twolevel"] = min((v for k, v in res.items() if k.startswith("learned_twolevel_keep")),
                                   key=lambda v: v["seconds"])
+    nn_ms = network_ms(lp, nx + 1)
+    del lp
+    torch.cuda.empty_cache()
+    # the one-level design: 4096 (residual, Jacobi-PCG correction) pairs from the plain solver
+    # (64 random loads x 64 snapshots every 16 iterations; target PCG_8(r) - D^-1 r), the network
+    # as the second direction of the flexible CG beside Jacobi, no coarse grid
+    lp1 = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0)
+    t0 = time.perf_counter()
+    np1 = lp1.make_pairs(nloads=args.pairs_1level, snaps=64, every=16, inner=8)
+    torch.cuda.synchronize()
+    t_pairs1 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    losses1 = lp1.train(steps=args.train_steps_1level, batch=32, crop=96, margin=args.margin,
+                        lr=2e-3, log_every=max(args.train_steps_1level // 10, 1))
+    torch.cuda.synchronize()
+    t_train1 = time.perf_counter() - t0
+    lp1.R = lp1.T = None
+    # ring of 8 directions (shorter rings needed up to 20x more iterations in trial runs); the
+    # iteration cap bounds the time of a network that does not help
+    cap = 4 * res["jacobi_pcg"]["iterations"]
+    try:
+        b = best_of(lambda x: lp1.fcg(x, use_nn=True, nkeep=8, check_every=16, maxiter=cap), lp1)
+        res["learned_onelevel"] = {"seconds": b[0], "iterations": b[1], "relres_true": b[2],
+                                   "directions_kept": 8}
+    except _L.GFGPUError as e:
+        if e.code != -8:
+            raise
+        res["learned_onelevel"] = {"seconds": float("inf"), "iterations": cap,
+                                   "relres_true": None, "directions_kept": 8,
+                                   "note": f"not converged within {cap} iterations"}
+    del lp1
     for v in res.values():
         v["us_per_iteration"] = 1e6 * v["seconds"] / max(v["iterations"] + v.get("fallback_iterations", 0), 1)
-    nn_ms = network_ms(lp, nx + 1)
     jac = min(res["jacobi_pcg"]["seconds"], res["jacobi_pcg_graph"]["seconds"])
     learned = res["learned_twolevel"]
-    line = {"metric": "time-to-1e-8 resid (learned two-level FCG vs Jacobi PCG)",
+    one = res["learned_onelevel"]
+    return {"metric": "time-to-1e-8 resid (learned FCG vs Jacobi PCG)",
             "value": learned["seconds"], "unit": "s", "higher_is_better": False,
-            "n_gpus": 1, "steps": args.steps,
             "dtype": "f64 solve, bf16-weight/fp32-accumulate network, fp32 coarse correction",
             "data": "synthetic (seeded inclusions)",
             "config": {"workload": f"Quad4 Regular {nx}x{nx}, two-phase (inclusions "
                                    f"{100 * inside.mean():.1f}% area, x10 moduli), bottom fixed, "
-                                   "top uy=-1e-2", "coarse_spacing": args.hc, "pairs": npairs,
-                       "train_steps": args.train_steps, "crop": 96, "margin": args.margin,
-                       "chebyshev_degree": args.cheb_degree,
-                       "residual_check": "best of every 2, 4 (learned) and 4, 8, 16 (two-level) iterations",
-                       "target": "Chebyshev smoother minus Jacobi step, on the residual after "
-                                 "the two-level step", "loss": "energy norm",
-                       "directions_kept": [1, 2, 4], "nn_tensor_path": args.nn_path},
+                                   "top uy=-1e-2", "coarse_spacing": args.hc,
+                       "pairs_twolevel": npairs, "pairs_onelevel": np1,
+                       "train_steps": args.train_steps, "train_steps_onelevel": args.train_steps_1level,
+                       "crop": 96, "margin": args.margin, "chebyshev_degree": args.cheb_degree,
+                       "residual_check": "best of every 2, 4 (learned two-level), 4, 8, 16 "
+                                         "(two-level) and 16 (one-level) iterations",
+                       "target_twolevel": "Chebyshev smoother minus Jacobi step, on the residual "
+                                          "after the two-level step",
+                       "target_onelevel": "8 Jacobi-PCG iterations minus the Jacobi step",
+                       "loss": "energy norm", "nn_tensor_path": args.nn_path},
             "solvers": res,
             "speedup_vs_jacobi_pcg": jac / learned["seconds"],
             "speedup_vs_twolevel_without_network": res["twolevel"]["seconds"] / learned["seconds"],
+            "network_gain_iterations": res["twolevel"]["iterations"] / max(learned["iterations"], 1),
+            "onelevel_speedup_vs_jacobi_pcg": (jac / one["seconds"]) if one["seconds"] > 0 else None,
             "iteration_ratio_vs_jacobi_pcg": res["jacobi_pcg"]["iterations"] / max(learned["iterations"], 1),
-            "iteration_ratio_vs_twolevel": res["twolevel"]["iterations"] / max(learned["iterations"], 1),
             "coarse_setup_seconds": t_coarse, "pair_generation_seconds": t_pairs,
-            "training_seconds": t_train, "network_application_ms": nn_ms,
-            "loss_first_last": [losses[0], losses[-1]]}
-    print(json.dumps(line), flush=True)
-    return 0
+            "training_seconds": t_train, "pair_generation_seconds_onelevel": t_pairs1,
+            "training_seconds_onelevel": t_train1, "network_application_ms": nn_ms,
+            "loss_first_last": [losses[0], losses[-1]],
+            "loss_first_last_onelevel": [losses1[0], losses1[-1]]}
 
 
 def main():

@@ -13,6 +13,8 @@
 // (e, m, i) order (the serial order of Vector.h:724-741, deterministic), then performs the three
 // velocity estimates of docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:129-157 and the
 // displacement predictor of the next increment (main.cpp:119).
+#include <cuda.h>
+
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -1095,6 +1097,11 @@ static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, 
     return check_launch("verlet element kernel");
 }
 
+// float-float path of the Regular square Quad4 mesh (verlet_pair.cu)
+int64_t gfgpu_internal_pair_workspace_bytes(const gfgpu_verlet_desc* d);
+int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                               int64_t nsteps, void* workspace, cudaStream_t s);
+
 // Element-kernel launch shared with the static solvers (pcg.cu, learned.cu, coarse.cu), whose
 // gathers read fe in reg_grid(d)'s layout.
 int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
@@ -1109,17 +1116,86 @@ int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, d
     return launch_elem(d, u, fe, s);
 }
 
+// Coefficients of the closed-form velocity estimates per lumped-mass class (empty table when
+// the descriptor has no classes).
+static int mass_class_tab(const gfgpu_verlet_desc* d, const VerletCoef& k, MassClassTab* tab)
+{
+    *tab = MassClassTab{};
+    if (!(d->mclass && d->mclass_inv)) return GFGPU_OK;
+    GF_REQUIRE(d->ncls > 0 && d->ncls <= GFGPU_MASS_CLASSES, "bad mass-class count");
+    tab->n = d->ncls;
+    for (int c = 0; c < d->ncls; ++c) {
+        double mi = d->mclass_inv[c], be = mi * d->eta, omh = 1.0 - k.h * be;
+        tab->mi[c] = mi;
+        tab->be[c] = be;
+        tab->c1[c] = omh + k.h * k.h * be * be;
+        tab->c2[c] = k.h * omh + k.h * k.h * be * be * k.dt;
+        tab->c3[c] = k.h * omh;
+    }
+    return GFGPU_OK;
+}
+
+// The node kernel of one increment: strict order, Regular-mesh or CSR gather with mass classes,
+// or the per-dof inverse mass.
+static int launch_node(const gfgpu_verlet_desc* d, const MassClassTab& tab, const VerletCoef& k,
+                       const double* fe, int adv, double* u, double* v, double* a, cudaStream_t s)
+{
+    const int64_t n = d->nnode * d->ndim;
+    const unsigned gn = grid_for(n);
+    const bool cls = d->mclass && d->mclass_inv && d->ncls > 0;
+    if (strict_mode())
+        k_verlet_node<true><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
+                                                  d->inv, fe, d->fext, n, k, adv, u, v, a);
+    else if (cls && d->reg_nx > 0 && d->reg_nz == 0 && d->nne == 4)
+        k_verlet_node_cls_regular<<<grid_for(d->nnode), kBlock, 0, s>>>(
+            d->reg_nx, d->reg_ny, d->mclass, tab, fe, d->fext, k, adv, u, v, a);
+    else if (cls)
+        k_verlet_node_cls<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->mclass, tab,
+                                                fe, d->fext, n, k, adv, u, v, a);
+    else if (variant_node() == 1)
+        k_verlet_node_fast_x2<<<grid_for((n + 1) / 2), kBlock, 0, s>>>(
+            d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, d->inv, fe, d->fext, n, k, adv, u, v, a);
+    else
+        k_verlet_node_fast<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
+                                                 d->inv, fe, d->fext, n, k, adv, u, v, a);
+    return check_launch("verlet node kernel");
+}
+
+// nsteps FP64 increments (predictor, then element kernel + node kernel per increment) with the
+// element forces in fe [nelem, nne, ndim]; shared by gfgpu_verlet_step and
+// gfgpu_verlet_step_noalloc, which differ only in where fe lives.
+static int run_increments(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                          int64_t nsteps, double* fe, cudaStream_t s)
+{
+    const VerletCoef k = verlet_coefficients(d);
+    const int64_t n = d->nnode * d->ndim;
+    const unsigned gn = grid_for(n);
+    MassClassTab tab;
+    GF_TRY(mass_class_tab(d, k, &tab));
+    if (strict_mode())
+        k_predict<true><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
+    else
+        k_predict<false><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
+    GF_TRY(check_launch("verlet predict"));
+    for (int64_t it = 0; it < nsteps; ++it) {
+        GF_TRY(launch_elem(d, u, fe, s));
+        GF_TRY(launch_node(d, tab, k, fe, it + 1 < nsteps ? 1 : 0, u, v, a, s));
+    }
+    return GFGPU_OK;
+}
+
 extern "C" {
 
 int64_t gfgpu_verlet_workspace_bytes(const gfgpu_verlet_desc* d)
 {
     if (!d) return 0;
     int64_t b = d->nelem * d->nne * d->ndim * static_cast<int64_t>(sizeof(double));
+    b = std::max(b, gfgpu_internal_pair_workspace_bytes(d));
     return (b + 255) / 256 * 256;
 }
 
 int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
-                                const double* vol_host, double rtol)
+                                const double* vol_host, double rtol, gfgpu_stream_t stream)
 {
     // dNx_host / vol_host: the first element's dNx [nip,nne,ndim] and vol [nip] (host copies);
     // the device arrays d->dNx / d->vol are scanned on the GPU against the box they imply.
@@ -1166,20 +1242,25 @@ int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
         for (int k = 0; k < kk; ++k)
             if (std::fabs(dNx_host[q * kk + k] - ref[q * kk + k]) > rtol * gmax) return GFGPU_OK;
     }
-    double* dref = nullptr;
-    int* bad = nullptr;
-    GF_TRY(check_cuda(cudaMalloc(&dref, sizeof(ref)), "cudaMalloc"));
-    GF_TRY(check_cuda(cudaMalloc(&bad, sizeof(int)), "cudaMalloc"));
-    cudaMemcpy(dref, ref, sizeof(ref), cudaMemcpyHostToDevice);
-    cudaMemset(bad, 0, sizeof(int));
-    k_detect_uniform<<<grid_for(d->nelem * nip), kBlock>>>(d->dNx, d->vol, d->nelem, nip, kk, dref,
-                                                           vref, rtol * gmax, rtol * vref, bad);
+    // one stream-ordered scratch block: the reference dNx, then the flag
+    cudaStream_t s = S(stream);
+    char* mem = nullptr;
+    GF_TRY(check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&mem), sizeof(ref) + 256, s), "cudaMallocAsync"));
+    double* dref = reinterpret_cast<double*>(mem);
+    int* bad = reinterpret_cast<int*>(mem + sizeof(ref));
     int hbad = 1;
-    int rc = check_launch("detect_uniform");
+    int rc = check_cuda(cudaMemcpyAsync(dref, ref, sizeof(ref), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+    if (rc == GFGPU_OK) rc = check_cuda(cudaMemsetAsync(bad, 0, sizeof(int), s), "cudaMemsetAsync");
+    if (rc == GFGPU_OK) {
+        k_detect_uniform<<<grid_for(d->nelem * nip), kBlock, 0, s>>>(d->dNx, d->vol, d->nelem, nip, kk, dref,
+                                                                     vref, rtol * gmax, rtol * vref, bad);
+        rc = check_launch("detect_uniform");
+    }
     if (rc == GFGPU_OK)
-        rc = check_cuda(cudaMemcpy(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
-    cudaFree(dref);
-    cudaFree(bad);
+        rc = check_cuda(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    const int rc_free = check_cuda(cudaFreeAsync(mem, s), "cudaFreeAsync");
+    if (rc == GFGPU_OK) rc = rc_free;
+    if (rc == GFGPU_OK) rc = check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     GF_TRY(rc);
     if (!hbad) {
         d->uniform = 1;
@@ -1197,52 +1278,9 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
     GF_REQUIRE(u && v && a && workspace && nsteps >= 0, "bad argument");
     GF_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 15u) == 0, "workspace must be 16-byte aligned");
     if (nsteps == 0) return GFGPU_OK;
-    cudaStream_t s = S(stream);
-    double* fe = static_cast<double*>(workspace);
-    VerletCoef k = verlet_coefficients(d);
-    int64_t n = d->nnode * d->ndim;
-    unsigned gn = grid_for(n);
-    bool st = strict_mode();
-    MassClassTab tab{};
-    if (d->mclass && d->mclass_inv) {
-        GF_REQUIRE(d->ncls > 0 && d->ncls <= GFGPU_MASS_CLASSES, "bad mass-class count");
-        tab.n = d->ncls;
-        for (int c = 0; c < d->ncls; ++c) {
-            double mi = d->mclass_inv[c], be = mi * d->eta, omh = 1.0 - k.h * be;
-            tab.mi[c] = mi;
-            tab.be[c] = be;
-            tab.c1[c] = omh + k.h * k.h * be * be;
-            tab.c2[c] = k.h * omh + k.h * k.h * be * be * k.dt;
-            tab.c3[c] = k.h * omh;
-        }
-    }
-    if (st)
-        k_predict<true><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
-    else
-        k_predict<false><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
-    GF_TRY(check_launch("verlet predict"));
-    for (int64_t it = 0; it < nsteps; ++it) {
-        GF_TRY(launch_elem(d, u, fe, s));
-        int adv = it + 1 < nsteps ? 1 : 0;
-        if (st)
-            k_verlet_node<true><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
-                                                      d->inv, fe, d->fext, n, k, adv, u, v, a);
-        else if (d->mclass && d->mclass_inv && d->ncls > 0 && d->reg_nx > 0 && d->reg_nz == 0 && d->nne == 4)
-            k_verlet_node_cls_regular<<<grid_for(d->nnode), kBlock, 0, s>>>(
-                d->reg_nx, d->reg_ny, d->mclass, tab, fe, d->fext, k, adv, u, v, a);
-        else if (d->mclass && d->mclass_inv && d->ncls > 0)
-            k_verlet_node_cls<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->mclass, tab,
-                                                    fe, d->fext, n, k, adv, u, v, a);
-        else if (variant_node() == 1)
-            k_verlet_node_fast_x2<<<grid_for((n + 1) / 2), kBlock, 0, s>>>(
-                d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, d->inv, fe, d->fext, n, k, adv, u,
-                v, a);
-        else
-            k_verlet_node_fast<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
-                                                     d->inv, fe, d->fext, n, k, adv, u, v, a);
-        GF_TRY(check_launch("verlet node kernel"));
-    }
-    return GFGPU_OK;
+    if (d->coef_pair && !strict_mode())
+        return gfgpu_internal_verlet_pair(d, u, v, a, nsteps, workspace, S(stream));
+    return run_increments(d, u, v, a, nsteps, static_cast<double*>(workspace), S(stream));
 }
 
 int gfgpu_verlet_detect_regular(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, gfgpu_stream_t stream)
@@ -1257,7 +1295,7 @@ int gfgpu_verlet_detect_regular(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, gf
     GF_REQUIRE((reinterpret_cast<uintptr_t>(d->conn) & 15u) == 0, "conn must be 16-byte aligned");
     cudaStream_t s = S(stream);
     int* flag = nullptr;
-    GF_TRY(check_cuda(cudaMalloc(&flag, sizeof(int)), "cudaMalloc"));
+    GF_TRY(check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&flag), sizeof(int), s), "cudaMallocAsync"));
     int h = 1;
     int rc = check_cuda(cudaMemsetAsync(flag, 0, sizeof(int), s), "cudaMemsetAsync");
     if (rc == GFGPU_OK) {
@@ -1266,8 +1304,9 @@ int gfgpu_verlet_detect_regular(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, gf
         rc = check_launch("detect_regular");
     }
     if (rc == GFGPU_OK) rc = check_cuda(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    const int rc_free = check_cuda(cudaFreeAsync(flag, s), "cudaFreeAsync");
+    if (rc == GFGPU_OK) rc = rc_free;
     if (rc == GFGPU_OK) rc = check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-    cudaFree(flag);
     GF_TRY(rc);
     if (h == 0) {
         d->reg_nx = nx;
@@ -1288,7 +1327,7 @@ int gfgpu_verlet_detect_regular_hex8(gfgpu_verlet_desc* d, int64_t nx, int64_t n
         return GFGPU_OK;
     cudaStream_t s = S(stream);
     int* flag = nullptr;
-    GF_TRY(check_cuda(cudaMalloc(&flag, sizeof(int)), "cudaMalloc"));
+    GF_TRY(check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&flag), sizeof(int), s), "cudaMallocAsync"));
     int h = 1;
     int rc = check_cuda(cudaMemsetAsync(flag, 0, sizeof(int), s), "cudaMemsetAsync");
     if (rc == GFGPU_OK) {
@@ -1297,8 +1336,9 @@ int gfgpu_verlet_detect_regular_hex8(gfgpu_verlet_desc* d, int64_t nx, int64_t n
         rc = check_launch("detect_regular_hex8");
     }
     if (rc == GFGPU_OK) rc = check_cuda(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    const int rc_free = check_cuda(cudaFreeAsync(flag, s), "cudaFreeAsync");
+    if (rc == GFGPU_OK) rc = rc_free;
     if (rc == GFGPU_OK) rc = check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-    cudaFree(flag);
     GF_TRY(rc);
     if (h == 0) {
         d->reg_nx = nx;
@@ -1368,28 +1408,61 @@ int gfgpu_internal_force(const gfgpu_verlet_desc* d, const double* u, double* fi
 // Scratch of gfgpu_verlet_step_noalloc: the element forces of one increment live in this
 // file-scope device array instead of caller- or library-allocated memory. Every GPU that loads
 // the library holds it (32 MiB) until the process exits. In host code the name is only a
-// host-side stand-in: its device address is obtained per device with cudaGetSymbolAddress and
-// passed to the kernels.
+// host-side stand-in: its device address is obtained with cudaGetSymbolAddress, with the device
+// current, and passed to the kernels.
 static __device__ __align__(256) double g_noalloc_fe[GFGPU_NOALLOC_FE_DOUBLES];
 
 namespace {
-constexpr int kMaxDevices = 64;
-double* g_noalloc_ptr[kMaxDevices] = {};
-std::mutex g_noalloc_mutex;
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
 
-// Device address of g_noalloc_fe on the current device (looked up on the first call per device).
+std::mutex g_noalloc_mutex;
+PfnCtxGetCurrent g_ctx_current = nullptr;
+PfnCtxGetId g_ctx_id = nullptr;
+// (context id, device address of g_noalloc_fe in that context); a context made after
+// cudaDeviceReset, or a caller's own driver context, has a new id and gets its own lookup
+std::vector<std::pair<unsigned long long, double*>> g_noalloc_ptr;
+
+int driver_fn(const char* name, void** fn)
+{
+    cudaDriverEntryPointQueryResult q;
+    GF_TRY(check_cuda(cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q),
+                      "cudaGetDriverEntryPointByVersion"));
+    if (q != cudaDriverEntryPointSuccess || !*fn) return fail(GFGPU_ERR_CUDA, std::string(name) + " not found");
+    return GFGPU_OK;
+}
+
+// Device address of g_noalloc_fe in the current CUDA context (looked up on the first call in
+// each context).
 int noalloc_scratch(double** out)
 {
-    int dev = 0;
-    GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
-    if (dev < 0 || dev >= kMaxDevices) return fail(GFGPU_ERR_UNSUPPORTED, "device ordinal >= 64");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
-        GF_TRY(check_cuda(cudaGetSymbolAddress(&p, g_noalloc_fe), "cudaGetSymbolAddress"));
-        g_noalloc_ptr[dev] = static_cast<double*>(p);
+    if (!g_ctx_current || !g_ctx_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        GF_TRY(driver_fn("cuCtxGetCurrent", &f1));
+        GF_TRY(driver_fn("cuCtxGetId", &f2));
+        g_ctx_current = reinterpret_cast<PfnCtxGetCurrent>(f1);
+        g_ctx_id = reinterpret_cast<PfnCtxGetId>(f2);
     }
-    *out = g_noalloc_ptr[dev];
+    CUcontext ctx = nullptr;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS) return fail(GFGPU_ERR_CUDA, "cuCtxGetCurrent failed");
+    void* fresh = nullptr;
+    if (!ctx) {
+        // no context bound to this thread yet: the runtime binds the device's primary context
+        GF_TRY(check_cuda(cudaGetSymbolAddress(&fresh, g_noalloc_fe), "cudaGetSymbolAddress"));
+        if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx) return fail(GFGPU_ERR_CUDA, "no current CUDA context");
+    }
+    unsigned long long id = 0;
+    if (g_ctx_id(ctx, &id) != CUDA_SUCCESS) return fail(GFGPU_ERR_CUDA, "cuCtxGetId failed");
+    for (const auto& e : g_noalloc_ptr)
+        if (e.first == id) {
+            *out = e.second;
+            return GFGPU_OK;
+        }
+    if (!fresh) GF_TRY(check_cuda(cudaGetSymbolAddress(&fresh, g_noalloc_fe), "cudaGetSymbolAddress"));
+    g_noalloc_ptr.emplace_back(id, static_cast<double*>(fresh));
+    *out = static_cast<double*>(fresh);
     return GFGPU_OK;
 }
 } // namespace
@@ -1411,28 +1484,7 @@ int gfgpu_verlet_step_noalloc(const gfgpu_verlet_desc* d, double* u, double* v, 
     double* fe = nullptr;
     GF_TRY(noalloc_scratch(&fe));
     if (nsteps == 0) return GFGPU_OK;
-    cudaStream_t s = S(stream);
-    VerletCoef k = verlet_coefficients(d);
-    int64_t n = d->nnode * d->ndim;
-    unsigned gn = grid_for(n);
-    bool st = strict_mode();
-    if (st)
-        k_predict<true><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
-    else
-        k_predict<false><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
-    GF_TRY(check_launch("noalloc predict"));
-    for (int64_t it = 0; it < nsteps; ++it) {
-        GF_TRY(launch_elem(d, u, fe, s));
-        int adv = it + 1 < nsteps ? 1 : 0;
-        if (st)
-            k_verlet_node<true><<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
-                                                      d->inv, fe, d->fext, n, k, adv, u, v, a);
-        else
-            k_verlet_node_fast<<<gn, kBlock, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu,
-                                                     d->inv, fe, d->fext, n, k, adv, u, v, a);
-        GF_TRY(check_launch("noalloc node kernel"));
-    }
-    return GFGPU_OK;
+    return run_increments(d, u, v, a, nsteps, fe, S(stream));
 }
 
 int gfgpu_verlet_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
@@ -1575,7 +1627,10 @@ int gfgpu_barrier_selftest(int64_t timeout_cycles, int* status)
     GF_REQUIRE(status && timeout_cycles > 0, "bad argument");
     char* mem = nullptr;
     GF_TRY(check_cuda(cudaMalloc(&mem, 256), "cudaMalloc"));
-    cudaMemset(mem, 0, 256);
+    if (int rc0 = check_cuda(cudaMemset(mem, 0, 256), "cudaMemset"); rc0 != GFGPU_OK) {
+        cudaFree(mem);
+        return rc0;
+    }
     GridBar bar;
     bar.count = reinterpret_cast<unsigned*>(mem);
     bar.gen = reinterpret_cast<unsigned*>(mem + 64);

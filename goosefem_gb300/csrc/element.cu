@@ -393,6 +393,40 @@ __global__ void k_int_n_scalar(const double* __restrict__ N, const double* __res
     }
 }
 
+// Diagonal of Int_N_scalar_NT_dV only (the lumped mass of MatrixDiagonal::assemble,
+// MatrixDiagonal.h:151-167): thread per (e, m), out elemvec (e, m, i) = elemmat(e, m*nd+i, m*nd+i)
+// with k_int_n_scalar's operations for that entry (same bits). With offdiag != null the row's
+// off-diagonal entries (m, n != m) are summed too and *offdiag is cleared if one exceeds
+// DBL_EPSILON in magnitude (Element::isDiagonal, Element.h:122-145); nothing of the full
+// [nelem, nne*nd, nne*nd] matrix is stored.
+template <bool S>
+__global__ void k_int_n_scalar_diag(const double* __restrict__ N, const double* __restrict__ vol,
+                                    const double* __restrict__ qscalar, int64_t nelem, int nne,
+                                    int nip, int nd, double* __restrict__ out, int* __restrict__ offdiag)
+{
+    const double eps = 2.220446049250313080847e-16; // DBL_EPSILON
+    GF_FOR(t, nelem * nne)
+    {
+        const int64_t e = t / nne;
+        const int m = static_cast<int>(t - e * nne);
+        double acc = 0.0;
+        for (int q = 0; q < nip; ++q)
+            acc = madd<S>(mul<S>(mul<S>(N[q * nne + m], qscalar[e * nip + q]), N[q * nne + m]),
+                          vol[e * nip + q], acc);
+        for (int i = 0; i < nd; ++i) out[t * nd + i] = acc;
+        if (offdiag) {
+            for (int n = 0; n < nne; ++n) {
+                if (n == m) continue;
+                double o = 0.0;
+                for (int q = 0; q < nip; ++q)
+                    o = madd<S>(mul<S>(mul<S>(N[q * nne + m], qscalar[e * nip + q]), N[q * nne + n]),
+                                vol[e * nip + q], o);
+                if (fabs(o) > eps) *offdiag = 0;
+            }
+        }
+    }
+}
+
 // Int_gradN_dot_tensor4_dot_gradNT_dV: Element.h:1132-1176. Thread per elemmat entry; the
 // entry (m*nd+j, n*nd+k) accumulates over q, then i, then l as in the reference loop nest.
 // td: tensor dimension of C (td = 3 with nd = 2: QuadraturePlanar, the in-plane indices of a
@@ -581,6 +615,39 @@ int gfgpu_int_n_scalar_nt_dv(const double* N, const double* vol, const double* q
     DISPATCH_S(k_int_n_scalar<kS><<<grid_for(nelem * K * K), kBlock, 0, S(stream)>>>(
         N, vol, qscalar, nelem, nne, nip, ndim, elemmat));
     return check_launch("int_n_scalar_nt_dv");
+}
+
+int gfgpu_int_n_scalar_nt_dv_diag(const double* N, const double* vol, const double* qscalar,
+                                  int64_t nelem, int32_t nne, int32_t nip, int32_t ndim,
+                                  double* elemvec, int* is_diag, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(N && vol && qscalar && elemvec && nip > 0, "bad argument");
+    GF_TRY(check_elem(nne, ndim));
+    GF_REQUIRE(!too_big(nelem * nne * ndim), "too many elements");
+    cudaStream_t s = S(stream);
+    int* flag = nullptr;
+    if (is_diag) {
+        GF_TRY(check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&flag), sizeof(int), s), "cudaMallocAsync"));
+        const int one = 1;
+        int rc = check_cuda(cudaMemcpyAsync(flag, &one, sizeof(int), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+        if (rc != GFGPU_OK) {
+            cudaFreeAsync(flag, s);
+            return rc;
+        }
+    }
+    int rc = GFGPU_OK;
+    if (nelem > 0) {
+        DISPATCH_S(k_int_n_scalar_diag<kS><<<grid_for(nelem * nne), kBlock, 0, s>>>(
+            N, vol, qscalar, nelem, nne, nip, ndim, elemvec, flag));
+        rc = check_launch("int_n_scalar_nt_dv_diag");
+    }
+    if (!is_diag) return rc;
+    *is_diag = 0;
+    if (rc == GFGPU_OK) rc = check_cuda(cudaMemcpyAsync(is_diag, flag, sizeof(int), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    const int rc_free = check_cuda(cudaFreeAsync(flag, s), "cudaFreeAsync");
+    if (rc == GFGPU_OK) rc = rc_free;
+    if (rc == GFGPU_OK) rc = check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    return rc;
 }
 
 int gfgpu_int_grad_n_dot_tensor2_dv(const double* dNx, const double* vol, const double* qtensor,

@@ -16,6 +16,29 @@ from . import _dev, _lib
 from . import mesh as _mesh
 from .element import Quad4, Hex8
 
+# Relative tolerance of the uniform-box detection (gfgpu_verlet_detect_uniform): a mesh whose dNx
+# or vol differ from the box model by more than this (relative to the largest |dNx|) takes the
+# general per-Gauss-point kernel. The closed form's error on an almost-uniform mesh is of the
+# order of that deviation, so the floor sits an order of magnitude inside the 1e-12 parity bound.
+UNIFORM_RTOL = 1e-13
+
+
+def uniform_rtol(coor, conn):
+    """Detection tolerance for a mesh: the floor UNIFORM_RTOL, or twice the rounding noise that
+    compute_dN itself leaves on an exact grid of this extent, whichever is larger. The Jacobian
+    sums terms of the size of the coordinates that cancel to the element size, so the reference's
+    own dNx / vol deviate from the exact box by about eps * max|x| / h (measured on Regular unit
+    grids: 1.4e-14 at 64^2, 5.7e-14 at 256^2, 2.3e-13 at 1024^2, 5.1e-13 at 2048^2); twice that
+    (9.1e-13 at 2048^2) separates rounding from geometry. Larger meshes than 2048 elements per
+    edge therefore tolerate more than the parity bound, in proportion to that rounding noise."""
+    x = coor.detach().cpu().numpy() if isinstance(coor, torch.Tensor) else np.asarray(coor)
+    c0 = conn[0].detach().cpu().numpy() if isinstance(conn, torch.Tensor) else np.asarray(conn)[0]
+    e0 = x[c0]
+    h = float(np.min(e0.max(axis=0) - e0.min(axis=0)))
+    if not h > 0.0:
+        return UNIFORM_RTOL
+    return max(UNIFORM_RTOL, 2.0 * np.finfo(np.float64).eps * float(np.abs(x).max()) / h)
+
 
 def elastic_stress(eps, K, G, sig=None):
     """sigma = K tr(eps) I + 2 G dev(eps) per Gauss point, K and G per element [nelem]
@@ -44,10 +67,15 @@ class VelocityVerlet:
     iip : prescribed (fixed) dofs, or None
     fext : external force nodevec, or None
     uniform : "auto" (detect congruent axis-aligned elements), True or False
+    arithmetic : "fp64" (default: FP64 kernels) or "pair": on a Mesh::Quad4::Regular mesh of
+        square elements with lumped-mass classes, the increments run in float-float arithmetic
+        (two FP32 numbers per value, ~48-bit significands) in one fused kernel per increment
+        (gfgpu_verlet_precompute_pair); agreement with the FP64 path ~1e-14 per increment. Other
+        meshes raise with "pair".
     """
 
     def __init__(self, coor, conn, dofs, K, G, rho=1.0, dt=None, eta=0.0, iip=None, fext=None,
-                 uniform="auto"):
+                 uniform="auto", arithmetic="fp64"):
         from .vector import Vector
         from .matrix import MatrixDiagonal, MatrixDiagonalPartitioned
 
@@ -63,20 +91,20 @@ class VelocityVerlet:
         nodal = E.Quadrature(x, E.Nodal.xi(), E.Nodal.w())
         rho_q = torch.full((nelem, nodal.nip()), float(rho), dtype=torch.float64,
                            device=_dev.device())
-        Me = nodal.Int_N_scalar_NT_dV(rho_q)
+        # lumped mass: the element matrices' diagonals only (checked diagonal on the fly), no
+        # [nelem, nne*ndim, nne*ndim] intermediate
+        Md = nodal.Int_N_scalar_NT_dV_diag(rho_q)
         if iip is None or len(iip) == 0:
             self.mass = MatrixDiagonal(conn_h, dofs_h)
-            self.mass.assemble(Me)
             part = dofs_h
             nnu = self.mass.ndof()
-            inv = self.mass.inverse()
         else:
             self.mass = MatrixDiagonalPartitioned(conn_h, dofs_h, iip)
-            self.mass.assemble(Me)
             part = self.mass.part()
             nnu = self.mass.nnu()
-            inv = self.mass.inverse()
-        del Me, nodal
+        self.mass.assemble_diagonal(Md)
+        inv = self.mass.inverse()
+        del Md, nodal, rho_q
         self.part_d = _dev.dev_i32(part)
         self.inv = inv
         self.K = _dev.dev_f64(K)
@@ -106,7 +134,7 @@ class VelocityVerlet:
             g0 = self.quad.GradN()[0].detach().cpu().numpy().copy()
             v0 = self.quad.dV()[0].detach().cpu().numpy().copy()
             _lib.call("gfgpu_verlet_detect_uniform", C.addressof(d), g0.ctypes.data,
-                      v0.ctypes.data, 1e-12)
+                      v0.ctypes.data, uniform_rtol(coor, conn_h), _dev.stream())
             if uniform is True and not d.uniform:
                 raise RuntimeError("mesh is not a uniform axis-aligned Quad4 mesh")
         self.coef = None
@@ -119,11 +147,41 @@ class VelocityVerlet:
             _lib.call("gfgpu_verlet_precompute", C.addressof(d), self.coef.data_ptr(),
                       _dev.stream())
             d.coef = self.coef.data_ptr()
-        self.ws = torch.empty(int(_lib.lib().gfgpu_verlet_workspace_bytes(C.addressof(d))) // 8,
-                              dtype=torch.float64, device=_dev.device())
         self.classify()
         if nne == 4:
-            self._detect_regular(np.asarray(coor))
+            self._detect_regular(coor.detach().cpu().numpy() if isinstance(coor, torch.Tensor)
+                                 else np.asarray(coor))
+        self.coef_pair = None
+        if arithmetic == "pair":
+            self.use_pair()
+        elif arithmetic != "fp64":
+            raise ValueError("arithmetic must be 'fp64' or 'pair'")
+        self._alloc_ws()
+
+    def _alloc_ws(self):
+        self.ws = torch.empty(int(_lib.lib().gfgpu_verlet_workspace_bytes(C.addressof(self.desc))) // 8,
+                              dtype=torch.float64, device=_dev.device())
+
+    def use_pair(self):
+        """Float-float increments (gfgpu_verlet_precompute_pair); raises GFGPUError
+        (GFGPU_ERR_UNSUPPORTED) when the mesh is not a Regular square-element Quad4 mesh with
+        lumped-mass classes."""
+        if self.coef_pair is None:
+            cp = torch.empty(6 * self.nelem + 4, dtype=torch.float32, device=_dev.device())
+            _lib.call("gfgpu_verlet_precompute_pair", C.addressof(self.desc), cp.data_ptr(),
+                      _dev.stream())
+            self.coef_pair = cp
+        self.desc.coef_pair = self.coef_pair.data_ptr()
+        if hasattr(self, "ws"):
+            self._alloc_ws()
+
+    def use_fp64(self):
+        """FP64 kernels (the default)."""
+        self.desc.coef_pair = None
+
+    @property
+    def arithmetic(self):
+        return "pair" if self.desc.coef_pair else "fp64"
 
     @property
     def uniform(self):
@@ -157,12 +215,14 @@ class VelocityVerlet:
         return self.desc.reg_nx > 0
 
     def use_csr_gather(self):
-        """Node kernel through the dof CSR even on a Regular mesh."""
+        """Node kernel through the dof CSR even on a Regular mesh (FP64 kernels)."""
+        self.use_fp64()
         self.desc.reg_nx = 0
         self.desc.reg_ny = 0
 
     def use_per_dof_mass(self):
-        """Node update with the inverse mass read per dof (no mass classes)."""
+        """Node update with the inverse mass read per dof (no mass classes; FP64 kernels)."""
+        self.use_fp64()
         self.desc.mclass = None
         self.desc.mclass_inv = None
         self.desc.ncls = 0
@@ -171,16 +231,20 @@ class VelocityVerlet:
     def path(self):
         if not self.desc.uniform:
             return "general"
+        if self.desc.coef_pair:
+            return "uniform-square-pair"
         if self.desc.coef:
             return "uniform-square" if self.desc.nne == 4 else "uniform-cube"
         return "uniform"
 
     def use_general_path(self):
+        self.use_fp64()
         self.desc.uniform = 0
         self.desc.coef = None
 
     def use_uniform_onthefly(self):
         """Uniform closed form with K, G read every increment (no precomputed coefficients)."""
+        self.use_fp64()
         self.desc.coef = None
 
     def step(self, u, v, a, nsteps=1):
@@ -191,6 +255,27 @@ class VelocityVerlet:
                 raise ValueError("u, v, a must be contiguous float64 CUDA tensors")
         _lib.call("gfgpu_verlet_step", C.addressof(self.desc), u.data_ptr(), v.data_ptr(),
                   a.data_ptr(), int(nsteps), self.ws.data_ptr(), _dev.stream())
+
+    def Step(self, u, v, a, nsteps=1, out=None):
+        """Capital form of step (GooseFEM's allocate-and-return convention): u, v, a are host
+        nodevecs (numpy or torch, pinned torch tensors copy asynchronously); the state is copied
+        to device buffers of this object, advanced nsteps increments, and returned as a tuple of
+        new pinned host tensors (or written into `out`, a previous result). Synchronises."""
+        shape = (self.nnode, self.ndim)
+        if getattr(self, "_dstate", None) is None:
+            self._dstate = [torch.empty(shape, dtype=torch.float64, device=_dev.device())
+                            for _ in range(3)]
+        for d, h in zip(self._dstate, (u, v, a)):
+            h = torch.as_tensor(h, dtype=torch.float64)
+            _dev.check_shape(h, shape, "VelocityVerlet.Step")
+            d.copy_(h, non_blocking=True)
+        self.step(*self._dstate, nsteps)
+        if out is None:
+            out = tuple(torch.empty(shape, dtype=torch.float64).pin_memory() for _ in range(3))
+        for o, d in zip(out, self._dstate):
+            o.copy_(d, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return out
 
     def internal_force(self, u, fint=None):
         u = _dev.dev_f64(u)

@@ -230,6 +230,25 @@ class _QuadratureBase:
     def Int_N_scalar_NT_dV(self, qscalar):
         return self.int_N_scalar_NT_dV(qscalar, self.allocate_elemmat())
 
+    def int_N_scalar_NT_dV_diag(self, qscalar, elemvec, check=True):
+        """Diagonal of Int_N_scalar_NT_dV as an elemvec (elemvec(e,m,i) = elemmat(e, m*ndim+i,
+        m*ndim+i)), without forming the element matrices (gfgpu_int_n_scalar_nt_dv_diag). With
+        check=True the off-diagonal entries are formed on the fly and a non-diagonal result
+        (Element::isDiagonal) raises, as MatrixDiagonal::assemble would."""
+        qs = _dev.dev_f64(qscalar)
+        _dev.check_shape(qs, self.shape_qscalar(), "int_N_scalar_NT_dV_diag")
+        _dev.check_shape(elemvec, self.shape_elemvec(), "int_N_scalar_NT_dV_diag")
+        flag = C.c_int(0)
+        _lib.call("gfgpu_int_n_scalar_nt_dv_diag", self._N.data_ptr(), self._vol.data_ptr(),
+                  qs.data_ptr(), self._nelem, self._nne, self._nip, self._ndim,
+                  elemvec.data_ptr(), C.addressof(flag) if check else None, _dev.stream())
+        if check and not flag.value:
+            raise RuntimeError("Int_N_scalar_NT_dV_diag: the element matrices are not diagonal")
+        return elemvec
+
+    def Int_N_scalar_NT_dV_diag(self, qscalar, check=True):
+        return self.int_N_scalar_NT_dV_diag(qscalar, self.allocate_elemvec(), check)
+
     def int_gradN_dot_tensor2_dV(self, qtensor, elemvec):
         qt = _dev.dev_f64(qtensor)
         _dev.check_shape(qt, self.shape_qtensor(2), "int_gradN_dot_tensor2_dV")

@@ -66,6 +66,19 @@ class MatrixDiagonal:
                   _dev.stream())
         self._changed = True
 
+    def assemble_diagonal(self, elemvec):
+        """MatrixDiagonal::assemble from the element matrices' diagonals only (an elemvec, e.g.
+        Quadrature.Int_N_scalar_NT_dV_diag): the same sums in the same order as assemble()."""
+        ev = _dev.dev_f64(elemvec)
+        _dev.check_shape(ev, (self._nelem, self._nne, self._ndim), "assemble_diagonal")
+        ptr, idx, out = self._assemble_target()
+        _lib.call("gfgpu_assemble_dofs", ptr.data_ptr(), idx.data_ptr(), self._ndof, ev.data_ptr(),
+                  out.data_ptr(), _dev.stream())
+        self._changed = True
+
+    def _assemble_target(self):
+        return self.csr_ptr, self.csr_idx, self._A
+
     def set(self, A):
         A = _dev.dev_f64(A)
         _dev.check_shape(A, (self._ndof,), "set")
@@ -164,6 +177,9 @@ class MatrixDiagonalPartitioned(MatrixDiagonal):
                   self._ndof, self._nne, self._ndim, em.data_ptr(), self._App.data_ptr(),
                   _dev.stream())
         self._changed = True
+
+    def _assemble_target(self):
+        return self.pcsr_ptr, self.pcsr_idx, self._App
 
     def data_uu(self):
         return self._App[: self._nnu]

@@ -91,7 +91,7 @@ def nodal_mass(coor, conn):
     vec = Vector(conn, d)
     quad = E.Quadrature(vec.AsElement(coor), E.Nodal.xi(), E.Nodal.w())
     M = MatrixDiagonal(conn, d)
-    M.assemble(quad.Int_N_scalar_NT_dV(np.ones(conn.shape)))
+    M.assemble_diagonal(quad.Int_N_scalar_NT_dV_diag(np.ones(conn.shape)))
     return vec.AsNode(M.data())
 
 

@@ -14,6 +14,7 @@ import torch
 from . import _dev, _lib
 from . import mesh as _mesh
 from .element import Quad4, Hex8
+from .dynamics import uniform_rtol
 
 
 class ElasticStatic:
@@ -57,7 +58,7 @@ class ElasticStatic:
             g0 = self.quad.GradN()[0].detach().cpu().numpy().copy()
             v0 = self.quad.dV()[0].detach().cpu().numpy().copy()
             _lib.call("gfgpu_verlet_detect_uniform", C.addressof(d), g0.ctypes.data,
-                      v0.ctypes.data, 1e-12)
+                      v0.ctypes.data, uniform_rtol(coor, conn_h), _dev.stream())
             if uniform is True and not d.uniform:
                 raise RuntimeError("mesh is not uniform")
         # square Quad4 / cube Hex8 elements: precomputed per-element coefficients (34 / ~171 FP64

@@ -155,6 +155,18 @@ int gfgpu_int_n_vector_dv(const double* N, const double* vol, const double* qvec
 int gfgpu_int_n_scalar_nt_dv(const double* N, const double* vol, const double* qscalar,
                              int64_t nelem, int32_t nne, int32_t nip, int32_t ndim,
                              double* elemmat, gfgpu_stream_t stream);
+/* Diagonal of Int_N_scalar_NT_dV only, for the lumped mass of MatrixDiagonal::assemble
+ * (ElementQuad4.h:437-464, ElementHex8.h:324-352, MatrixDiagonal.h:151-167): elemvec
+ * [nelem,nne,ndim] with elemvec(e,m,i) = elemmat(e, m*ndim+i, m*ndim+i), the same operations and
+ * bits as gfgpu_int_n_scalar_nt_dv's diagonal, without the [nelem, nne*ndim, nne*ndim] matrix.
+ * Assemble it with gfgpu_assemble_dofs on the dof CSR (gfgpu_host_dof_csr; the CSR on `part` for
+ * MatrixDiagonalPartitioned): the same sums in the same order as gfgpu_diag_assemble. With
+ * is_diag != NULL the off-diagonal entries are formed too (not stored) and *is_diag (host int)
+ * receives Element::isDiagonal's verdict (Element.h:122-145: every |off-diagonal| <= DBL_EPSILON);
+ * the call then synchronises `stream`. */
+int gfgpu_int_n_scalar_nt_dv_diag(const double* N, const double* vol, const double* qscalar,
+                                  int64_t nelem, int32_t nne, int32_t nip, int32_t ndim,
+                                  double* elemvec, int* is_diag, gfgpu_stream_t stream);
 /* Int_gradN_dot_tensor2_dV (ElementQuad4.h:467-491; ElementHex8.h:355-383): -> elemvec. */
 int gfgpu_int_grad_n_dot_tensor2_dv(const double* dNx, const double* vol, const double* qtensor,
                                     int64_t nelem, int32_t nne, int32_t nip, int32_t ndim,
@@ -334,18 +346,26 @@ typedef struct {
      * <= 8 element forces by index arithmetic (same order and bits as the CSR). 0 = Quad4 or
      * CSR. */
     int64_t reg_nz;
+    /* optional float-float ("pair") coefficients of a uniform square Quad4 mesh with the
+     * Regular numbering and lumped-mass classes (gfgpu_verlet_precompute_pair): when set,
+     * gfgpu_verlet_step in fast mode runs its increments in pair arithmetic (two FP32 numbers per
+     * value, ~48-bit significands) in one fused kernel per increment; NULL = FP64 kernels. */
+    const float* coef_pair;
 } gfgpu_verlet_desc;
 
 #define GFGPU_MASS_CLASSES 16
 #define GFGPU_PRESCRIBED_CLASS 255
 
-/* Bytes of scratch the step needs (the element-force buffer), 256-byte aligned size. */
+/* Bytes of scratch the step needs (the element-force buffer, or the pair state when
+ * d->coef_pair is set), 256-byte aligned size. */
 int64_t gfgpu_verlet_workspace_bytes(const gfgpu_verlet_desc* d);
-/* Checks on the host that dNx/vol (copied to the host by the caller: dNx_host, vol_host, nelem
- * entries each) describe congruent axis-aligned boxes with the Gauss rule, within `rtol`; on
+/* Checks that dNx/vol describe congruent axis-aligned boxes with the Gauss rule, within `rtol`
+ * relative to the largest |dNx| (vol: relative to the box volume): first on the host for the first
+ * element (dNx_host [nip,nne,ndim], vol_host [nip], host copies), then for every element of the
+ * device arrays d->dNx / d->vol on `stream` (stream-ordered scratch, one synchronisation). On
  * success sets d->uniform = 1 and d->hx, hy, hz. Returns GFGPU_OK either way (d->uniform tells). */
 int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
-                                const double* vol_host, double rtol);
+                                const double* vol_host, double rtol, gfgpu_stream_t stream);
 /* Uniform square Quad4 meshes: fill coef [nelem, 4] with the element coefficients that depend on
  * K and G only (lam/4, G/2, G/4, g^2 (lam + 3G)/4, lam = K - 2G/3); uniform cube Hex8 meshes:
  * coef [nelem, 8] with the folded mode coefficients (w0 d lam, w0 d G, 2 w0 d G, w1 d lam,
@@ -353,6 +373,18 @@ int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
  * constant, linear and trilinear modes). Set d->coef = coef to use them. Returns
  * GFGPU_ERR_UNSUPPORTED for other meshes. */
 int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stream_t stream);
+/* Pair-arithmetic coefficients of a uniform square Quad4 mesh (same closed form as
+ * gfgpu_verlet_precompute): coef_pair holds 6 floats per element, {L.h, L.l, N.h, N.l} for all
+ * elements (16-byte aligned) then {kH.h, kH.l} (L = lam/4, N = G/4, kH = g^2 (lam + 3G)/4 split
+ * into high and low FP32 parts). Requires d->uniform with hx = hy, the Regular numbering
+ * (gfgpu_verlet_detect_regular) and mass classes (gfgpu_verlet_classify), else returns
+ * GFGPU_ERR_UNSUPPORTED. Set d->coef_pair = coef_pair to run gfgpu_verlet_step on pairs: one
+ * fused kernel per increment (displacement tile + halo in shared memory, element terms of the
+ * tile's elements, four-element gather, velocity estimates, predictor); u, v, a are converted to
+ * pairs at the start of the call and back at its end; each increment agrees with the FP64 kernels
+ * to ~1e-14 relative (48-bit significands, FP32 exponent range: |values| between ~1e-30 and
+ * ~1e38). Strict mode ignores coef_pair. */
+int gfgpu_verlet_precompute_pair(const gfgpu_verlet_desc* d, float* coef_pair, gfgpu_stream_t stream);
 /* Host set-up of the lumped-mass classes: reads part and inv back from the device, and if the
  * free dofs take at most GFGPU_MASS_CLASSES distinct inverse masses (a Regular mesh with uniform
  * density: interior, edge and corner values) writes mclass [nnode*ndim] (device, uint8) and
@@ -386,8 +418,12 @@ int gfgpu_verlet_step(const gfgpu_verlet_desc* d, double* u, double* v, double* 
  * the host); it allocates nothing: the element-force scratch is a file-scope device array of
  * GFGPU_NOALLOC_FE_DOUBLES values that every GPU loading the library keeps until the process
  * exits. Meshes with nelem * nne * ndim above that size are rejected with GFGPU_ERR_ARG.
- * The first call on a device looks up the array's device address (once per device, with that
- * device current); make that first call before any stream capture. All calls share the one
+ * The array's device address is looked up on the first call in each CUDA context (with the
+ * device current; a context created after cudaDeviceReset, or a caller's own driver context, gets
+ * its own lookup); make the first call in a context before any stream capture. This entry point
+ * always runs the FP64 kernels (the pair path of d->coef_pair needs a workspace for its state) and
+ * chooses the node kernel as gfgpu_verlet_step does: the two give the same bits for the same
+ * descriptor without coef_pair. All calls share the one
  * array, which keeps the last call's element forces (every increment overwrites it completely
  * before reading it); calls whose work overlaps on the GPU (for example on two streams) race on
  * it. u, v, a as in gfgpu_verlet_step. */

@@ -3,7 +3,9 @@ size of the throughput measurement, the same kernels): a few increments against 
 per-operator loop (docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:110-157 restated in
 oracle/gfref.cpp), and over 1000 increments two size-independent properties of the linear,
 damped dynamics: scaling the initial velocity by 2 scales every state array by exactly 2 (each
-FP64 operation commutes with a power-of-two scale), and the run is bit-identical run to run."""
+FP64 or FP32 operation commutes with a power-of-two scale), and the run is bit-identical run to
+run. Both arithmetics of the square-element path run: the FP64 kernels and the float-float
+("pair") fused kernel of the throughput measurement."""
 
 import numpy as np
 import pytest
@@ -33,16 +35,20 @@ def case(oracle):
                 v0=v0, dt=dt, vv=vv)
 
 
-def _run(case, v0, nsteps):
+def _run(case, v0, nsteps, arithmetic="fp64"):
+    vv = case["vv"]
+    vv.use_pair() if arithmetic == "pair" else vv.use_fp64()
     u = torch.zeros(v0.shape, dtype=torch.float64, device="cuda")
     v = torch.tensor(v0, device="cuda")
     a = torch.zeros_like(u)
-    case["vv"].step(u, v, a, nsteps)
+    vv.step(u, v, a, nsteps)
     torch.cuda.synchronize()
     return u, v, a
 
 
-def test_full_size_increments_match_oracle(case, oracle):
+@pytest.fixture(scope="module")
+def oracle_4(case, oracle):
+    """The oracle's loop over the first 4 increments (computed once for both arithmetics)."""
     R = oracle
     conn, dofs, coor = case["conn"], case["dofs"], case["coor"]
     nelem, nnode = conn.shape[0], coor.shape[0]
@@ -62,20 +68,28 @@ def test_full_size_increments_match_oracle(case, oracle):
     a = np.zeros_like(u)
     R.verlet_run(conn, dofs, dNx, vol, case["K"], case["G"], A, free, None, case["dt"], 0.1,
                  nsteps, u, v, a, parallel=True)
-    ug, vg, ag = _run(case, case["v0"], nsteps)
+    return nsteps, u, v, a
+
+
+@pytest.mark.parametrize("arithmetic", ["fp64", "pair"])
+def test_full_size_increments_match_oracle(case, oracle_4, arithmetic):
+    nsteps, u, v, a = oracle_4
+    ug, vg, ag = _run(case, case["v0"], nsteps, arithmetic)
     assert case["vv"].uniform  # the square-element kernels of the throughput measurement
+    assert case["vv"].path == ("uniform-square-pair" if arithmetic == "pair" else "uniform-square")
     assert rel_err(to_np(ug), u) <= RTOL
     assert rel_err(to_np(vg), v) <= RTOL
     assert rel_err(to_np(ag), a) <= RTOL
 
 
-def test_full_size_linearity_and_determinism(case):
+@pytest.mark.parametrize("arithmetic", ["fp64", "pair"])
+def test_full_size_linearity_and_determinism(case, arithmetic):
     nsteps = 1000
-    u1, v1, a1 = _run(case, case["v0"], nsteps)
-    u2, v2, a2 = _run(case, 2.0 * case["v0"], nsteps)
+    u1, v1, a1 = _run(case, case["v0"], nsteps, arithmetic)
+    u2, v2, a2 = _run(case, 2.0 * case["v0"], nsteps, arithmetic)
     assert torch.isfinite(u1).all() and u1.abs().max() > 0
     assert torch.equal(u2, 2.0 * u1) and torch.equal(v2, 2.0 * v1) and torch.equal(a2, 2.0 * a1)
-    u3, v3, a3 = _run(case, case["v0"], nsteps)
+    u3, v3, a3 = _run(case, case["v0"], nsteps, arithmetic)
     assert torch.equal(u3, u1) and torch.equal(v3, v1) and torch.equal(a3, a1)
     # the fixed bottom row never moves
     b = torch.as_tensor(case["bottom"], device="cuda").long()

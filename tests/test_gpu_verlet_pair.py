@@ -1,0 +1,129 @@
+"""The float-float ("pair") explicit increments (gfgpu_verlet_precompute_pair + gfgpu_verlet_step,
+one fused tile kernel per increment) against the oracle's loop
+(docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:110-157 restated in oracle/gfref.cpp) and
+against the FP64 kernels, at the suite's 1e-12 relative tolerance; tile edges (meshes that are
+not multiples of the 32 x 8 node tile), external forces, split calls, repeatability, exact
+linearity and the refusal of meshes the path does not cover."""
+
+import numpy as np
+import pytest
+import torch
+
+from _common import RTOL, rel_err, seeded_field, to_np
+from test_gpu_verlet import _run_oracle, _setup
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gf():
+    import goosefem_gb300 as gf
+
+    gf.set_strict(False)
+    yield gf
+    gf.set_strict(False)
+
+
+def _state(v0):
+    u = torch.zeros(v0.shape, dtype=torch.float64, device="cuda")
+    return [u, torch.tensor(v0, device="cuda"), torch.zeros_like(u)]
+
+
+@pytest.mark.parametrize("nx,ny", [(64, 48), (45, 19), (1, 1), (2, 3), (33, 9), (31, 7)])
+def test_pair_matches_oracle(gf, oracle, nx, ny):
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, nx, ny, False, True, 41)
+    vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip, arithmetic="pair")
+    assert vv.path == "uniform-square-pair"
+    s = _state(v0)
+    vv.step(*s, 60)
+    ur, vr, ar = _run_oracle(oracle, ref, v0, dt, 0.1, 60)
+    for g, r in zip(s, (ur, vr, ar)):
+        assert rel_err(to_np(g), r) <= RTOL
+
+
+def test_pair_with_external_force_and_free_edges(gf, oracle):
+    """No fixed dofs (every node free, corner / edge / interior mass classes) and an external
+    force."""
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 50, 37, False, False, 43)
+    fext = seeded_field((mesh.nnode(), 2), 44, amp=1e-4)
+    vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, fext=fext, arithmetic="pair")
+    s = _state(v0)
+    vv.step(*s, 80)
+    ur, vr, ar = _run_oracle(oracle, ref, v0, dt, 0.1, 80, fext)
+    for g, r in zip(s, (ur, vr, ar)):
+        assert rel_err(to_np(g), r) <= RTOL
+
+
+def test_pair_agrees_with_fp64_kernels(gf, oracle):
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 96, 80, False, True, 45)
+    vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip)
+    s64 = _state(v0)
+    vv.step(*s64, 200)
+    vv.use_pair()
+    sp = _state(v0)
+    vv.step(*sp, 200)
+    for g, r in zip(sp, s64):
+        assert rel_err(to_np(g), to_np(r)) <= RTOL
+
+
+@pytest.mark.parametrize("split", [(1, 1), (1, 2), (7, 10), (16, 1)])
+def test_pair_split_calls(gf, oracle, split):
+    """Calls convert the state in and out: step(n1) + step(n2) agrees with step(n1 + n2) to the
+    pair rounding of the state between the calls, and odd and even counts end in the right
+    buffer."""
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 40, 24, False, True, 47)
+    vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip, arithmetic="pair")
+    one, two = _state(v0), _state(v0)
+    vv.step(*one, sum(split))
+    for n in split:
+        vv.step(*two, n)
+    ur, vr, ar = _run_oracle(oracle, ref, v0, dt, 0.1, sum(split))
+    for x, y, r in zip(one, two, (ur, vr, ar)):
+        assert rel_err(to_np(x), to_np(y)) <= 1e-13
+        assert rel_err(to_np(x), r) <= RTOL
+
+
+def test_pair_repeatable_and_exactly_linear(gf, oracle):
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 70, 66, False, True, 49)
+    vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip, arithmetic="pair")
+    s1, s2, s3 = _state(v0), _state(2.0 * v0), _state(v0)
+    for s in (s1, s2, s3):
+        vv.step(*s, 300)
+    for x, y, z in zip(s1, s2, s3):
+        assert torch.equal(y, 2.0 * x)  # every FP32 operation commutes with a power-of-two scale
+        assert torch.equal(z, x)
+
+
+def test_pair_refuses_other_meshes(gf, oracle):
+    # periodic dofs: not the Regular numbering
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 16, 16, True, False, 51)
+    with pytest.raises(gf.GFGPUError) as ei:
+        gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, arithmetic="pair")
+    assert ei.value.code == -7
+    # rectangles (hx != hy)
+    m2 = gf.Mesh.Quad4.Regular(10, 8)
+    with pytest.raises(gf.GFGPUError):
+        gf.VelocityVerlet(m2.coor() * np.array([0.7, 1.3]), m2.conn(), m2.dofs(), K[:80], G[:80],
+                          dt=0.01, arithmetic="pair")
+    # Hex8
+    m3 = gf.Mesh.Hex8.Regular(3, 3, 3)
+    with pytest.raises(gf.GFGPUError):
+        gf.VelocityVerlet(m3.coor(), m3.conn(), m3.dofs(), K[:27], G[:27], dt=0.01,
+                          arithmetic="pair")
+
+
+def test_pair_ignored_in_strict_mode(gf, oracle):
+    """Strict mode runs the FP64 kernels even with coef_pair set: the same bits as without it."""
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 24, 20, False, True, 53)
+    vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip, arithmetic="pair")
+    try:
+        gf.set_strict(True)
+        sp = _state(v0)
+        vv.step(*sp, 20)
+        vv.use_fp64()
+        s64 = _state(v0)
+        vv.step(*s64, 20)
+        for x, y in zip(sp, s64):
+            assert torch.equal(x, y)
+    finally:
+        gf.set_strict(False)

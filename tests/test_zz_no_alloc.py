@@ -21,13 +21,19 @@ from _common import RTOL, rel_err, seeded_field, seeded_material
 pytestmark = pytest.mark.gpu
 
 
-def _problem(gf, nx, ny, uniform):
-    mesh = gf.Mesh.Quad4.Regular(nx, ny)
+def _problem(gf, nx, ny, uniform, hex8=False):
+    if hex8:
+        mesh = gf.Mesh.Hex8.Regular(nx, ny, ny)
+        fixed = mesh.nodesFront()
+    else:
+        mesh = gf.Mesh.Quad4.Regular(nx, ny)
+        fixed = mesh.nodesBottomEdge()
     coor, conn, dofs = mesh.coor(), mesh.conn(), mesh.dofs()
+    nd = coor.shape[1]
     K, G = seeded_material(mesh.nelem(), 71)
-    iip = dofs[mesh.nodesBottomEdge(), :].ravel()
-    v0 = seeded_field((mesh.nnode(), 2), 72)
-    v0[mesh.nodesBottomEdge(), :] = 0.0
+    iip = dofs[fixed, :].ravel()
+    v0 = seeded_field((mesh.nnode(), nd), 72)
+    v0[fixed, :] = 0.0
     dt = 0.1 * gf.critical_dt(K, G)
     vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip,
                            uniform="auto" if uniform else False)
@@ -39,25 +45,34 @@ def _state(v0):
     return [u, torch.tensor(v0, device="cuda"), torch.zeros_like(u)]
 
 
-@pytest.mark.parametrize("uniform", [True, False])
-def test_noalloc_matches_allocating_step(uniform):
+@pytest.mark.parametrize("strict", [False, True])
+@pytest.mark.parametrize("elem,uniform", [("quad4", True), ("quad4", False), ("hex8", True),
+                                          ("hex8", False)])
+def test_noalloc_matches_allocating_step(elem, uniform, strict):
+    """Both entry points run the same kernels (the node kernel is chosen by one shared helper), so
+    the states agree bit for bit; the suite's tolerance is asserted as well."""
     import goosefem_gb300 as gf
     from goosefem_gb300 import _lib
 
-    gf.set_strict(False)
-    mesh, vv, v0 = _problem(gf, 96, 64, uniform)
-    ref = _state(v0)
-    got = _state(v0)
-    stream = torch.cuda.current_stream().cuda_stream
-    for nsteps in (17, 23):  # two calls in a row, continuing the same state
-        _lib.call("gfgpu_verlet_step", C.addressof(vv.desc), ref[0].data_ptr(), ref[1].data_ptr(),
-                  ref[2].data_ptr(), nsteps, vv.ws.data_ptr(), stream)
-        _lib.call("gfgpu_verlet_step_noalloc", C.addressof(vv.desc), got[0].data_ptr(),
-                  got[1].data_ptr(), got[2].data_ptr(), nsteps, stream)
-        torch.cuda.synchronize()
-        for r, g in zip(ref, got):
-            r_np, g_np = r.cpu().numpy(), g.cpu().numpy()
-            assert rel_err(g_np, r_np) <= RTOL
+    gf.set_strict(strict)
+    try:
+        hex8 = elem == "hex8"
+        mesh, vv, v0 = _problem(gf, 12 if hex8 else 96, 10 if hex8 else 64, uniform, hex8)
+        ref = _state(v0)
+        got = _state(v0)
+        stream = torch.cuda.current_stream().cuda_stream
+        for nsteps in (17, 23):  # two calls in a row, continuing the same state
+            _lib.call("gfgpu_verlet_step", C.addressof(vv.desc), ref[0].data_ptr(), ref[1].data_ptr(),
+                      ref[2].data_ptr(), nsteps, vv.ws.data_ptr(), stream)
+            _lib.call("gfgpu_verlet_step_noalloc", C.addressof(vv.desc), got[0].data_ptr(),
+                      got[1].data_ptr(), got[2].data_ptr(), nsteps, stream)
+            torch.cuda.synchronize()
+            for r, g in zip(ref, got):
+                r_np, g_np = r.cpu().numpy(), g.cpu().numpy()
+                assert rel_err(g_np, r_np) <= RTOL
+                assert np.array_equal(g_np, r_np)
+    finally:
+        gf.set_strict(False)
 
 
 def test_noalloc_rejects_meshes_above_its_scratch():
