@@ -401,7 +401,7 @@ def run_gpu(args, rank, world):
         hbm_peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
     path = vv.path
-    kernel = {"uniform-square-pair": "k_verlet_pair_quad4",
+    kernel = {"uniform-square-pair": "k_verlet_pair_tma",
               "uniform-square": "k_elem_force_quad4_square", "uniform": "k_elem_force_quad4_uniform",
               "general": "k_elem_force_general"}[path]
     # fused-step minimum traffic (SURVEY-defined algorithmic bytes of one increment): u, v, a

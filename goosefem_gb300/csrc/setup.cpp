@@ -17,6 +17,12 @@ static int g_strict = 0;
 static int g_variant_elem = 0;
 static int g_variant_node = 0;
 static int g_nn_path = 2; // tcgen05 + TMA (the fastest form on GB300)
+static int g_pair_kernel = 0; // persistent TMA pipeline
+
+int pair_kernel()
+{
+    return g_pair_kernel;
+}
 
 int nn_tensor_path()
 {
@@ -87,6 +93,13 @@ int gfgpu_set_variant(int elem_variant, int node_variant)
         return fail(GFGPU_ERR_ARG, "gfgpu_set_variant: variants are 0 or 1");
     gfgpu::g_variant_elem = elem_variant;
     gfgpu::g_variant_node = node_variant;
+    return GFGPU_OK;
+}
+
+int gfgpu_set_pair_kernel(int kernel)
+{
+    if (kernel < 0 || kernel > 2) return fail(GFGPU_ERR_ARG, "gfgpu_set_pair_kernel: kernel is 0, 1 or 2");
+    gfgpu::g_pair_kernel = kernel;
     return GFGPU_OK;
 }
 

@@ -19,6 +19,10 @@
 // (the halo of one CTA is the tile of another: the increment reads one buffer and writes the
 // other). The caller's FP64 u, v, a are converted in at the start of a call (after the FP64
 // predictor) and out at its end.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -44,9 +48,9 @@ struct PairStep {
     float4* a;           // [nnode] acceleration (in/out)
     const float4* fext;  // [nnode] external force or null
     const float4* cLN;   // [nelem] {L.h, L.l, N.h, N.l}
-    const float2* cH;    // [nelem] {kH.h, kH.l}
+    const float2* cH;    // [ny][nxp] {kH.h, kH.l}
     const uchar2* mcls;  // [nnode] lumped-mass class per component
-    int nx, ny;
+    int nx, ny, nxp;
     int advance;         // write uout
     float2 dt, cc;       // dt and dt^2 / 2 as pairs
 };
@@ -151,7 +155,8 @@ k_verlet_pair_quad4(const PairStep p, const __grid_constant__ PairClassTab tab)
         if (ex >= 0 && ex < nx && ey >= 0 && ey < ny) {
             const int e = ey * nx + ex;
             const int b = ly * UW + lx; // node (ex, ey) in the tile
-            pair_element(su[b], su[b + 1], su[b + UW + 1], su[b + UW], __ldg(p.cLN + e), __ldg(p.cH + e), S, D, H);
+            pair_element(su[b], su[b + 1], su[b + UW + 1], su[b + UW], __ldg(p.cLN + e),
+                         __ldg(p.cH + ey * p.nxp + ex), S, D, H);
         }
         sS[k] = S;
         sD[k] = D;
@@ -182,6 +187,253 @@ k_verlet_pair_quad4(const PairStep p, const __grid_constant__ PairClassTab tab)
         const ffv ux = ff_norm(ff_add(ff_add(lo2(uq), ff_mul(dt, vx)), ff_mul(cc, ax)));
         const ffv uy = ff_norm(ff_add(ff_add(hi2(uq), ff_mul(dt, vy)), ff_mul(cc, ay)));
         p.uout[node] = pack(ux, uy);
+    }
+}
+
+// ------------------------------------------------------------------ persistent TMA form
+//
+// The same increment as k_verlet_pair_quad4, restructured for latency hiding and fewer
+// instructions:
+//  * persistent CTAs walk the node tiles (tile = blockIdx.x + i gridDim.x); the inputs of the
+//    next tile (displacement tile + halo, v, a, the per-element coefficients of the tile's
+//    elements) are fetched by TMA (cp.async.bulk.tensor, one thread, completion on an mbarrier)
+//    into the other of two shared-memory stages while the current tile is computed. Outside the
+//    mesh the copies read zeros, so elements beyond the edges have zero coefficients and
+//    contribute nothing: the element phase needs no bounds checks.
+//  * a tile is 31 x 7 nodes with the 32 x 8 elements around them: the element phase is one
+//    element per thread (lane = element column, warp = element row), and in the node phase warp
+//    w, lane j owns node (x0 + j, y0 + w) (lane 31 and warp 7 only help with the columns).
+//  * the element phase stores only the element terms P0, P1 (= Q0), Q1, H0, H1; the node phase
+//    forms, per column of elements below/above a node row, with A = P0_lo + P0_hi,
+//    B = P1_lo - P1_hi, C = H0_lo - H0_hi (x; y with P1, Q1, H1):
+//      Pcol = (A + C) + B,  Qcol = (A + C) - B,  f_x(ix, iy) = Pcol(ix - 1) - Qcol(ix),
+//    which is the four-element sum (S_a - S_d) + (D_c - D_b) + (H_a - H_b) + (H_d - H_c) of the
+//    tile kernel regrouped (S = P0 + P1, D = P0 - P1): 33 instead of 40 pair additions per node.
+//    Lane j forms the column left of its node, the right column's Qcol comes from lane j + 1.
+//  * every wait is bounded: a CTA whose copies do not arrive sets g_pair_timeout, waits (again
+//    bounded) for the copies it issued and returns.
+__device__ int g_pair_timeout = 0;
+constexpr long kPairSpin = 1L << 22;
+
+// Tile geometry of the persistent kernel: TX x TY owned nodes, the (TX + 1) x (TY + 1) = one
+// per thread elements around them, the displacement tile with its one-node halo.
+template <int TY>
+struct TmaGeom {
+    static constexpr int TX = 31, EW = TX + 1, EH = TY + 1, UW = TX + 2, UH = TY + 2;
+    static constexpr int threads = EW * EH;
+    static constexpr int HW = 68; // kH floats per element row box
+    static constexpr uint32_t UBytes = UW * UH * 16, VBytes = TX * TY * 16, LBytes = EW * EH * 16,
+                              HBytes = HW * EH * 4;
+    static constexpr uint32_t StageTx = UBytes + 2 * VBytes + LBytes + HBytes;
+    static constexpr uint32_t pad(uint32_t b) { return (b + 127u) / 128u * 128u; }
+    // stage layout: u | v | a | cLN | cH, each 128-byte aligned
+    static constexpr uint32_t OffV = pad(UBytes), OffA = OffV + pad(VBytes), OffL = OffA + pad(VBytes),
+                              OffH = OffL + pad(LBytes), StageBytes = OffH + pad(HBytes);
+    static constexpr uint32_t ElemBytes = threads * (16 + 16 + 8); // {P0, P1}, {Q1, H0}, {H1}
+    static constexpr uint32_t Smem = 128 + 2 * StageBytes + pad(ElemBytes) + 64;
+    static constexpr int min_blocks = threads <= 256 ? 4 : 2;
+};
+static_assert(TmaGeom<7>::EW == 32, "one warp per element row");
+constexpr int kTmaTX = 31;
+
+struct PairTmaStep {
+    float4* uout;
+    float4* v;
+    float4* a;
+    const float4* fext;
+    const uchar2* mcls;
+    int nx, ny, ntx, ntiles;
+    int gdx, gdy;        // gridDim.x = gdy ntx + gdx: the tile step in tile columns and rows
+    int advance;
+    float2 dt, cc;
+};
+
+__device__ __forceinline__ bool pair_wait(uint32_t mbar, uint32_t phase)
+{
+    for (long it = 0; it < kPairSpin; ++it) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(mbar), "r"(phase)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                          uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_load2(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3}], [%4];\n" ::"r"(dst),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ ffv shfl_down1(ffv x)
+{
+    return ff_make(__shfl_down_sync(0xffffffffu, x.h, 1), __shfl_down_sync(0xffffffffu, x.l, 1));
+}
+
+// first float of the kH box of a tile starting at node x0: 2 (x0 - 1) rounded down to a multiple
+// of 4 floats (a 16-byte boundary, as a TMA box's innermost coordinate must be)
+__host__ __device__ __forceinline__ int kh_start(int x0)
+{
+    return (2 * (x0 - 1)) & ~3;
+}
+
+template <int TY>
+__global__ void __launch_bounds__(TmaGeom<TY>::threads, TmaGeom<TY>::min_blocks)
+k_verlet_pair_tma(const __grid_constant__ CUtensorMap mu, const __grid_constant__ CUtensorMap mv,
+                  const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap ml,
+                  const __grid_constant__ CUtensorMap mh, const PairTmaStep p,
+                  const __grid_constant__ PairClassTab tab)
+{
+    using Gm = TmaGeom<TY>;
+    constexpr int kTmaTY = TY, kTmaEW = Gm::EW, kTmaUW = Gm::UW, kTmaThreads = Gm::threads, kTmaHW = Gm::HW;
+    constexpr uint32_t kStageBytes = Gm::StageBytes, kOffV = Gm::OffV, kOffA = Gm::OffA, kOffL = Gm::OffL,
+                       kOffH = Gm::OffH, kTmaStageTx = Gm::StageTx;
+    extern __shared__ unsigned char pair_smem[];
+    unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(pair_smem) + 127) & ~uintptr_t(127));
+    unsigned char* elem = base + 2 * kStageBytes;
+    float4* sPP = reinterpret_cast<float4*>(elem);
+    float4* sQH = sPP + kTmaThreads;
+    float2* sH1 = reinterpret_cast<float2*>(sQH + kTmaThreads);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(elem + Gm::pad(Gm::ElemBytes));
+    __shared__ float2 smi[GFGPU_MASS_CLASSES], sbe[GFGPU_MASS_CLASSES], sc1[GFGPU_MASS_CLASSES],
+        sc2[GFGPU_MASS_CLASSES], sc3[GFGPU_MASS_CLASSES];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t s_bar = static_cast<uint32_t>(__cvta_generic_to_shared(bars));
+    if (tid < GFGPU_MASS_CLASSES) {
+        smi[tid] = tab.mi[tid];
+        sbe[tid] = tab.be[tid];
+        sc1[tid] = tab.c1[tid];
+        sc2[tid] = tab.c2[tid];
+        sc3[tid] = tab.c3[tid];
+    }
+    auto issue = [&](int tile, int st) {
+        const int x0 = (tile % p.ntx) * kTmaTX, y0 = (tile / p.ntx) * kTmaTY;
+        const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(base + st * kStageBytes));
+        const uint32_t mb = s_bar + 8u * st;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb), "r"(kTmaStageTx)
+                     : "memory");
+        tma_load3(d, &mu, 0, x0 - 1, y0 - 1, mb);
+        tma_load3(d + kOffV, &mv, 0, x0, y0, mb);
+        tma_load3(d + kOffA, &ma, 0, x0, y0, mb);
+        tma_load3(d + kOffL, &ml, 0, x0 - 1, y0 - 1, mb);
+        tma_load2(d + kOffH, &mh, kh_start(x0), y0 - 1, mb);
+    };
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_bar) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_bar + 8u) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&mu)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&mv)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&ma)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&ml)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&mh)) : "memory");
+        if (static_cast<int>(blockIdx.x) < p.ntiles) issue(blockIdx.x, 0);
+    }
+    const int nx = p.nx, ny = p.ny, W = nx + 1;
+    const ffv dt = pf(p.dt), cc = pf(p.cc);
+    const bool hf = p.fext != nullptr;
+    // element phase: this thread's element (x0 - 1 + lane, y0 - 1 + warp); its nodes in the tile
+    const int b0 = warp * kTmaUW + lane;
+    int i = 0;
+    int tcol = static_cast<int>(blockIdx.x) % p.ntx, trow = static_cast<int>(blockIdx.x) / p.ntx;
+    for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++i) {
+        const int st = i & 1;
+        __syncthreads(); // the other stage and the element terms are free; barriers initialised
+        const int next = tile + gridDim.x;
+        if (tid == 0 && next < p.ntiles) issue(next, st ^ 1);
+        const int x0 = tcol * kTmaTX, y0 = trow * kTmaTY;
+        tcol += p.gdx;
+        trow += p.gdy;
+        if (tcol >= p.ntx) {
+            tcol -= p.ntx;
+            ++trow;
+        }
+        const int ix = x0 + lane, iy = y0 + warp;
+        const bool own = lane < kTmaTX && warp < kTmaTY && ix <= nx && iy <= ny;
+        const int node = iy * W + ix;
+        uchar2 cl = make_uchar2(GFGPU_PRESCRIBED_CLASS, GFGPU_PRESCRIBED_CLASS);
+        float4 fq = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (own) {
+            cl = __ldg(p.mcls + node);
+            if (hf) fq = __ldg(p.fext + node);
+        }
+        const bool ok = pair_wait(s_bar + 8u * st, (i >> 1) & 1);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                // let the copies this CTA issued land (bounded) before its shared memory is released
+                atomicExch(&g_pair_timeout, 1);
+                pair_wait(s_bar + 8u * st, (i >> 1) & 1);
+                if (next < p.ntiles) pair_wait(s_bar + 8u * (st ^ 1), ((i + 1) >> 1) & 1);
+            }
+            return;
+        }
+        const unsigned char* sg = base + st * kStageBytes;
+        const float4* su = reinterpret_cast<const float4*>(sg);
+        {
+            const float4 q0 = su[b0], q1 = su[b0 + 1], q2 = su[b0 + kTmaUW + 1], q3 = su[b0 + kTmaUW];
+            const ffv u0x = lo2(q0), u0y = hi2(q0), u1x = lo2(q1), u1y = hi2(q1);
+            const ffv u2x = lo2(q2), u2y = hi2(q2), u3x = lo2(q3), u3y = hi2(q3);
+            const ffv px = ff_sub(u2x, u0x), qx = ff_sub(u1x, u3x);
+            const ffv py = ff_sub(u2y, u0y), qy = ff_sub(u1y, u3y);
+            const ffv A1x = ff_add(px, qx), A2x = ff_sub(px, qx);
+            const ffv A1y = ff_add(py, qy), A2y = ff_sub(py, qy);
+            const ffv A3x = ff_sub(ff_add(u0x, u2x), ff_add(u1x, u3x));
+            const ffv A3y = ff_sub(ff_add(u0y, u2y), ff_add(u1y, u3y));
+            const float4 cln = reinterpret_cast<const float4*>(sg + kOffL)[tid];
+            const int kr = (2 * (x0 - 1) - kh_start(x0)) >> 1; // 0 or 1 pairs into the box row
+            const ffv kH = pf(reinterpret_cast<const float2*>(sg + kOffH)[warp * (kTmaHW / 2) + kr + lane]);
+            const ffv L = lo2(cln), N = hi2(cln), M = ff_twice(N);
+            const ffv Lt = ff_mul(L, ff_add(A1x, A2y));
+            const ffv P0 = ff_add(ff_mul(M, A1x), Lt);
+            const ffv Q1 = ff_add(ff_mul(M, A2y), Lt);
+            const ffv P1 = ff_mul(N, ff_add(A1y, A2x));
+            sPP[tid] = pack(P0, P1);
+            sQH[tid] = pack(Q1, ff_mul(kH, A3x));
+            const ffv H1 = ff_mul(kH, A3y);
+            sH1[tid] = make_float2(H1.h, H1.l);
+        }
+        __syncthreads();
+        if (warp >= kTmaTY) continue; // the last element row only feeds the node rows below it
+        // node phase: the element column left of node (x0 + lane, y0 + warp): lo = element row
+        // warp (below the node row), hi = warp + 1
+        const int kl = tid, kh = tid + kTmaEW;
+        const float4 ppl = sPP[kl], qhl = sQH[kl], pph = sPP[kh], qhh = sQH[kh];
+        const float2 h1l = sH1[kl], h1h = sH1[kh];
+        const ffv Ex = ff_add(ff_add(lo2(ppl), lo2(pph)), ff_sub(hi2(qhl), hi2(qhh)));
+        const ffv Bx = ff_sub(hi2(ppl), hi2(pph));
+        const ffv Ey = ff_add(ff_add(hi2(ppl), hi2(pph)), ff_sub(pf(h1l), pf(h1h)));
+        const ffv By = ff_sub(lo2(qhl), lo2(qhh));
+        const ffv Qrx = shfl_down1(ff_sub(Ex, Bx)), Qry = shfl_down1(ff_sub(Ey, By));
+        if (!own) continue;
+        const ffv fxn = ff_sub(ff_add(Ex, Bx), Qrx), fyn = ff_sub(ff_add(Ey, By), Qry);
+        const int ln = warp * kTmaTX + lane;
+        const float4 vq = reinterpret_cast<const float4*>(sg + kOffV)[ln];
+        const float4 aq = reinterpret_cast<const float4*>(sg + kOffA)[ln];
+        ffv vx, ax, vy, ay;
+        pair_update(cl.x, fxn, lo2(fq), hf, lo2(vq), lo2(aq), smi, sbe, sc1, sc2, sc3, dt, vx, ax);
+        pair_update(cl.y, fyn, hi2(fq), hf, hi2(vq), hi2(aq), smi, sbe, sc1, sc2, sc3, dt, vy, ay);
+        p.v[node] = pack(vx, vy);
+        p.a[node] = pack(ax, ay);
+        if (p.advance) {
+            const float4 uq = su[(warp + 1) * kTmaUW + lane + 1];
+            const ffv ux = ff_norm(ff_add(ff_add(lo2(uq), ff_mul(dt, vx)), ff_mul(cc, ax)));
+            const ffv uy = ff_norm(ff_add(ff_add(hi2(uq), ff_mul(dt, vy)), ff_mul(cc, ay)));
+            p.uout[node] = pack(ux, uy);
+        }
     }
 }
 
@@ -219,18 +471,25 @@ __global__ void k_pair_end(const float4* __restrict__ pu, const float4* __restri
     }
 }
 
-// per-element pair coefficients: cLN[e] = {L, N}, cH[e] = kH (see pair_element)
-__global__ void k_pair_coef(const double* __restrict__ Km, const double* __restrict__ Gm, int64_t nelem,
-                            double g2, float4* __restrict__ cLN, float2* __restrict__ cH)
+// per-element pair coefficients: cLN[e] = {L, N}, cH[ey * nxp + ex] = kH (see pair_element);
+// one thread per entry of the padded kH rows, the pad entries zero
+__global__ void k_pair_coef(const double* __restrict__ Km, const double* __restrict__ Gm, int nx, int ny,
+                            int nxp, double g2, float4* __restrict__ cLN, float2* __restrict__ cH)
 {
-    GF_FOR(e, nelem)
+    GF_FOR(t, static_cast<int64_t>(ny) * nxp)
     {
+        const int ey = static_cast<int>(t / nxp), ex = static_cast<int>(t - static_cast<int64_t>(ey) * nxp);
+        if (ex >= nx) {
+            cH[t] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const int64_t e = static_cast<int64_t>(ey) * nx + ex;
         const double K = Km[e], G = Gm[e];
         const double lam = K - 2.0 * G / 3.0;
         const ffv L = ff_from_double(0.25 * lam), N = ff_from_double(0.25 * G);
         const ffv kH = ff_from_double(0.25 * g2 * (lam + 3.0 * G));
         cLN[e] = pack(L, N);
-        cH[e] = make_float2(kH.h, kH.l);
+        cH[t] = make_float2(kH.h, kH.l);
     }
 }
 
@@ -267,6 +526,72 @@ int64_t gfgpu_internal_pair_workspace_bytes(const gfgpu_verlet_desc* d)
     return vecs * d->nnode * static_cast<int64_t>(sizeof(float4));
 }
 
+static int encode_map(CUtensorMap* map, const void* ptr, cuuint32_t rank, const cuuint64_t* dims,
+                      const cuuint64_t* strides, const cuuint32_t* box)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        GF_TRY(check_cuda(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q),
+                          "cudaGetDriverEntryPointByVersion"));
+        if (q != cudaDriverEntryPointSuccess || !fn) return fail(GFGPU_ERR_CUDA, "cuTensorMapEncodeTiled not found");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint32_t estr[3] = {1, 1, 1};
+    // zero fill outside the tensor (CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE)
+    CUresult rc = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, const_cast<void*>(ptr), dims, strides, box,
+                         estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (rc != CUDA_SUCCESS) return fail(GFGPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(rc)) + ")");
+    return GFGPU_OK;
+}
+
+// a pair nodevec [H][W] of float4 as a 3-d FP32 tensor {4, W, H}
+static int nodevec_map(CUtensorMap* map, const float4* ptr, int W, int H, int bw, int bh)
+{
+    const cuuint64_t dims[3] = {4, static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H)};
+    const cuuint64_t strides[2] = {16, 16ull * static_cast<cuuint64_t>(W)};
+    const cuuint32_t box[3] = {4, static_cast<cuuint32_t>(bw), static_cast<cuuint32_t>(bh)};
+    return encode_map(map, ptr, 3, dims, strides, box);
+}
+
+static int nxp_of(int64_t nx)
+{
+    return static_cast<int>(nx + (nx & 1));
+}
+
+template <int TY>
+static int launch_tma(PairTmaStep p, const CUtensorMap* mu, const CUtensorMap& mv, const CUtensorMap& ma,
+                      const CUtensorMap& ml, const CUtensorMap& mh, const PairClassTab& tab, int64_t nsteps,
+                      float4* const* ub, int sms, cudaStream_t s)
+{
+    using Gm = TmaGeom<TY>;
+    static bool attr = false;
+    if (!attr) {
+        GF_TRY(check_cuda(cudaFuncSetAttribute(k_verlet_pair_tma<TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(Gm::Smem)),
+                          "cudaFuncSetAttribute"));
+        attr = true;
+    }
+    int per_sm = 0;
+    GF_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_verlet_pair_tma<TY>, Gm::threads,
+                                                                    Gm::Smem),
+                      "occupancy"));
+    GF_REQUIRE(per_sm >= 1, "pair kernel does not fit on an SM");
+    p.ntiles = p.ntx * ((p.ny + TY) / TY);
+    const int grid = std::min(p.ntiles, sms * per_sm);
+    p.gdx = grid % p.ntx;
+    p.gdy = grid / p.ntx;
+    for (int64_t it = 0; it < nsteps; ++it) {
+        p.uout = ub[(it + 1) & 1];
+        p.advance = it + 1 < nsteps ? 1 : 0;
+        k_verlet_pair_tma<TY><<<grid, Gm::threads, Gm::Smem, s>>>(mu[it & 1], mv, ma, ml, mh, p, tab);
+        GF_TRY(check_launch("verlet pair kernel (TMA)"));
+    }
+    return GFGPU_OK;
+}
+
 // gfgpu_verlet_step's pair path (d->coef_pair set, fast arithmetic)
 int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
                                int64_t nsteps, void* workspace, cudaStream_t s)
@@ -299,25 +624,63 @@ int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v,
                                                  reinterpret_cast<const double2*>(d->fext), nn, dt, c, ub[0], pv,
                                                  pa, pfx);
     GF_TRY(check_launch("pair begin"));
-    PairStep p;
-    p.v = pv;
-    p.a = pa;
-    p.fext = pfx;
-    p.cLN = reinterpret_cast<const float4*>(d->coef_pair);
-    p.cH = reinterpret_cast<const float2*>(d->coef_pair + 4 * d->nelem);
-    p.mcls = reinterpret_cast<const uchar2*>(d->mclass);
-    p.nx = static_cast<int>(d->reg_nx);
-    p.ny = static_cast<int>(d->reg_ny);
-    p.dt = split_host(dt);
-    p.cc = split_host(c);
-    const dim3 grid(static_cast<unsigned>((d->reg_nx + kPairTX) / kPairTX),
-                    static_cast<unsigned>((d->reg_ny + kPairTY) / kPairTY));
-    for (int64_t it = 0; it < nsteps; ++it) {
-        p.uin = ub[it & 1];
-        p.uout = ub[(it + 1) & 1];
-        p.advance = it + 1 < nsteps ? 1 : 0;
-        k_verlet_pair_quad4<<<grid, kPairThreads, 0, s>>>(p, tab);
-        GF_TRY(check_launch("verlet pair kernel"));
+    const int nx = static_cast<int>(d->reg_nx), ny = static_cast<int>(d->reg_ny), nxp = nxp_of(nx);
+    const float4* cLN = reinterpret_cast<const float4*>(d->coef_pair);
+    const float2* cH = reinterpret_cast<const float2*>(d->coef_pair + 4 * d->nelem);
+    const uchar2* mcls = reinterpret_cast<const uchar2*>(d->mclass);
+    if (pair_kernel() == 1) {
+        PairStep p;
+        p.v = pv;
+        p.a = pa;
+        p.fext = pfx;
+        p.cLN = cLN;
+        p.cH = cH;
+        p.mcls = mcls;
+        p.nx = nx;
+        p.ny = ny;
+        p.nxp = nxp;
+        p.dt = split_host(dt);
+        p.cc = split_host(c);
+        const dim3 grid(static_cast<unsigned>((nx + kPairTX) / kPairTX), static_cast<unsigned>((ny + kPairTY) / kPairTY));
+        for (int64_t it = 0; it < nsteps; ++it) {
+            p.uin = ub[it & 1];
+            p.uout = ub[(it + 1) & 1];
+            p.advance = it + 1 < nsteps ? 1 : 0;
+            k_verlet_pair_quad4<<<grid, kPairThreads, 0, s>>>(p, tab);
+            GF_TRY(check_launch("verlet pair kernel"));
+        }
+    }
+    else {
+        CUtensorMap mu[2], mv, ma, ml, mh;
+        const int TY = pair_kernel() == 2 ? 15 : 7;
+        GF_TRY(nodevec_map(&mu[0], ub[0], nx + 1, ny + 1, kTmaTX + 2, TY + 2));
+        GF_TRY(nodevec_map(&mu[1], ub[1], nx + 1, ny + 1, kTmaTX + 2, TY + 2));
+        GF_TRY(nodevec_map(&mv, pv, nx + 1, ny + 1, kTmaTX, TY));
+        GF_TRY(nodevec_map(&ma, pa, nx + 1, ny + 1, kTmaTX, TY));
+        GF_TRY(nodevec_map(&ml, cLN, nx, ny, kTmaTX + 1, TY + 1));
+        {
+            const cuuint64_t dims[2] = {2ull * static_cast<cuuint64_t>(nxp), static_cast<cuuint64_t>(ny)};
+            const cuuint64_t strides[1] = {8ull * static_cast<cuuint64_t>(nxp)};
+            const cuuint32_t box[2] = {static_cast<cuuint32_t>(TmaGeom<7>::HW), static_cast<cuuint32_t>(TY + 1)};
+            GF_TRY(encode_map(&mh, cH, 2, dims, strides, box));
+        }
+        int dev = 0, sms = 0;
+        GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+        GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr"));
+        PairTmaStep p;
+        p.v = pv;
+        p.a = pa;
+        p.fext = pfx;
+        p.mcls = mcls;
+        p.nx = nx;
+        p.ny = ny;
+        p.ntx = (nx + kTmaTX) / kTmaTX;
+        p.dt = split_host(dt);
+        p.cc = split_host(c);
+        if (pair_kernel() == 2)
+            GF_TRY(launch_tma<15>(p, mu, mv, ma, ml, mh, tab, nsteps, ub, sms, s));
+        else
+            GF_TRY(launch_tma<7>(p, mu, mv, ma, ml, mh, tab, nsteps, ub, sms, s));
     }
     // the last increment does not advance: its displacement is the one it read
     k_pair_end<<<grid_for(nn), kBlock, 0, s>>>(ub[(nsteps - 1) & 1], pv, pa, nn, reinterpret_cast<double2*>(u),
@@ -326,6 +689,12 @@ int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v,
 }
 
 extern "C" {
+
+int64_t gfgpu_verlet_pair_coef_floats(const gfgpu_verlet_desc* d)
+{
+    if (!d || d->reg_nx <= 0 || d->reg_ny <= 0) return 0;
+    return 4 * d->reg_nx * d->reg_ny + 2 * static_cast<int64_t>(nxp_of(d->reg_nx)) * d->reg_ny;
+}
 
 int gfgpu_verlet_precompute_pair(const gfgpu_verlet_desc* d, float* coef_pair, gfgpu_stream_t stream)
 {
@@ -336,10 +705,25 @@ int gfgpu_verlet_precompute_pair(const gfgpu_verlet_desc* d, float* coef_pair, g
     GF_REQUIRE(d->K && d->G, "null material");
     if (d->nelem == 0) return GFGPU_OK;
     const double g = 1.0 / std::sqrt(3.0);
+    const int nx = static_cast<int>(d->reg_nx), ny = static_cast<int>(d->reg_ny), nxp = nxp_of(nx);
     float4* cLN = reinterpret_cast<float4*>(coef_pair);
     float2* cH = reinterpret_cast<float2*>(coef_pair + 4 * d->nelem);
-    k_pair_coef<<<grid_for(d->nelem), kBlock, 0, S(stream)>>>(d->K, d->G, d->nelem, g * g, cLN, cH);
+    k_pair_coef<<<grid_for(static_cast<int64_t>(ny) * nxp), kBlock, 0, S(stream)>>>(d->K, d->G, nx, ny, nxp, g * g,
+                                                                                   cLN, cH);
     return check_launch("verlet_precompute_pair");
+}
+
+int gfgpu_verlet_pair_status(void)
+{
+    int flag = 0;
+    GF_TRY(check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize"));
+    GF_TRY(check_cuda(cudaMemcpyFromSymbol(&flag, g_pair_timeout, sizeof(int)), "cudaMemcpyFromSymbol"));
+    if (flag) {
+        const int zero = 0;
+        GF_TRY(check_cuda(cudaMemcpyToSymbol(g_pair_timeout, &zero, sizeof(int)), "cudaMemcpyToSymbol"));
+        return fail(GFGPU_ERR_TIMEOUT, "gfgpu_verlet_pair_status: a pair kernel's wait for its TMA copies gave up");
+    }
+    return GFGPU_OK;
 }
 
 } // extern "C"

@@ -167,7 +167,8 @@ class VelocityVerlet:
         (GFGPU_ERR_UNSUPPORTED) when the mesh is not a Regular square-element Quad4 mesh with
         lumped-mass classes."""
         if self.coef_pair is None:
-            cp = torch.empty(6 * self.nelem + 4, dtype=torch.float32, device=_dev.device())
+            n = int(_lib.lib().gfgpu_verlet_pair_coef_floats(C.addressof(self.desc)))
+            cp = torch.empty(max(n, 4), dtype=torch.float32, device=_dev.device())
             _lib.call("gfgpu_verlet_precompute_pair", C.addressof(self.desc), cp.data_ptr(),
                       _dev.stream())
             self.coef_pair = cp

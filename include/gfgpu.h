@@ -54,6 +54,16 @@ int gfgpu_set_strict(int strict);
  * elem_variant 1 = two neighbouring elements per thread in the uniform square Quad4 kernel,
  * node_variant 1 = both dofs of a node per thread in the node kernel. Same results. */
 int gfgpu_set_variant(int elem_variant, int node_variant);
+/* Kernel of the float-float explicit increment (gfgpu_verlet_precompute_pair), process-wide:
+ * 0 (default) = persistent CTAs of 256 threads that prefetch the next 31 x 7 node tile's inputs
+ * by TMA into a second shared-memory stage while computing the current one; 2 = the same with
+ * 31 x 15 node tiles and 512 threads; 1 = one 32 x 8 node tile per CTA with plain loads. Same
+ * arithmetic, the four-element sums grouped differently in 1 (agreement ~1e-14). */
+int gfgpu_set_pair_kernel(int kernel);
+/* Timeout flag of the pair kernels' bounded waits for their TMA copies: GFGPU_ERR_TIMEOUT if a
+ * wait gave up since the last call (the increment's results are then invalid), else GFGPU_OK.
+ * Clears the flag. Synchronises the device. */
+int gfgpu_verlet_pair_status(void);
 /* Tensor-core instructions of the network's 32 -> 32 layers (process-wide): 0 = mma.sync m16n8k16,
  * 1 = tcgen05.mma with TMEM accumulators, one tile per CTA, 2 (default) = tcgen05.mma in a
  * persistent pipeline fed by TMA (cp.async.bulk.tensor) with 2-3 shared-memory stages of whole
@@ -373,10 +383,14 @@ int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
  * constant, linear and trilinear modes). Set d->coef = coef to use them. Returns
  * GFGPU_ERR_UNSUPPORTED for other meshes. */
 int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stream_t stream);
+/* Floats of the pair coefficients of a Regular(nx, ny) mesh: 4 nx ny + 2 nxp ny, nxp = nx rounded
+ * up to even (0 for other descriptors). */
+int64_t gfgpu_verlet_pair_coef_floats(const gfgpu_verlet_desc* d);
 /* Pair-arithmetic coefficients of a uniform square Quad4 mesh (same closed form as
- * gfgpu_verlet_precompute): coef_pair holds 6 floats per element, {L.h, L.l, N.h, N.l} for all
- * elements (16-byte aligned) then {kH.h, kH.l} (L = lam/4, N = G/4, kH = g^2 (lam + 3G)/4 split
- * into high and low FP32 parts). Requires d->uniform with hx = hy, the Regular numbering
+ * gfgpu_verlet_precompute): coef_pair (gfgpu_verlet_pair_coef_floats floats) holds
+ * {L.h, L.l, N.h, N.l} per element in element order (16-byte aligned), then {kH.h, kH.l} per
+ * element in rows of nxp pairs (element (ex, ey) at ey * nxp + ex, the pad pair zero), with
+ * L = lam/4, N = G/4, kH = g^2 (lam + 3G)/4 split into high and low FP32 parts. Requires d->uniform with hx = hy, the Regular numbering
  * (gfgpu_verlet_detect_regular) and mass classes (gfgpu_verlet_classify), else returns
  * GFGPU_ERR_UNSUPPORTED. Set d->coef_pair = coef_pair to run gfgpu_verlet_step on pairs: one
  * fused kernel per increment (displacement tile + halo in shared memory, element terms of the

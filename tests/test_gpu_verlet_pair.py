@@ -22,6 +22,23 @@ def gf():
     gf.set_strict(False)
     yield gf
     gf.set_strict(False)
+    _lib().call("gfgpu_set_pair_kernel", 0)
+
+
+def _lib():
+    from goosefem_gb300 import _lib as L
+
+    return L
+
+
+@pytest.fixture(params=[0, 1, 2], ids=["tma31x7", "tile", "tma31x15"])
+def kernel(request, gf):
+    """The persistent TMA pipeline (0, the default; 2 with taller tiles) and the
+    one-tile-per-CTA kernel (1); every test ends by checking that no bounded wait gave up."""
+    _lib().call("gfgpu_set_pair_kernel", request.param)
+    yield request.param
+    _lib().call("gfgpu_verlet_pair_status")
+    _lib().call("gfgpu_set_pair_kernel", 0)
 
 
 def _state(v0):
@@ -29,8 +46,8 @@ def _state(v0):
     return [u, torch.tensor(v0, device="cuda"), torch.zeros_like(u)]
 
 
-@pytest.mark.parametrize("nx,ny", [(64, 48), (45, 19), (1, 1), (2, 3), (33, 9), (31, 7)])
-def test_pair_matches_oracle(gf, oracle, nx, ny):
+@pytest.mark.parametrize("nx,ny", [(64, 48), (45, 19), (1, 1), (2, 3), (33, 9), (31, 7), (96, 200)])
+def test_pair_matches_oracle(gf, oracle, kernel, nx, ny):
     mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, nx, ny, False, True, 41)
     vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip, arithmetic="pair")
     assert vv.path == "uniform-square-pair"
@@ -41,7 +58,7 @@ def test_pair_matches_oracle(gf, oracle, nx, ny):
         assert rel_err(to_np(g), r) <= RTOL
 
 
-def test_pair_with_external_force_and_free_edges(gf, oracle):
+def test_pair_with_external_force_and_free_edges(gf, oracle, kernel):
     """No fixed dofs (every node free, corner / edge / interior mass classes) and an external
     force."""
     mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 50, 37, False, False, 43)
@@ -54,7 +71,7 @@ def test_pair_with_external_force_and_free_edges(gf, oracle):
         assert rel_err(to_np(g), r) <= RTOL
 
 
-def test_pair_agrees_with_fp64_kernels(gf, oracle):
+def test_pair_agrees_with_fp64_kernels(gf, oracle, kernel):
     mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 96, 80, False, True, 45)
     vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip)
     s64 = _state(v0)
@@ -67,7 +84,7 @@ def test_pair_agrees_with_fp64_kernels(gf, oracle):
 
 
 @pytest.mark.parametrize("split", [(1, 1), (1, 2), (7, 10), (16, 1)])
-def test_pair_split_calls(gf, oracle, split):
+def test_pair_split_calls(gf, oracle, kernel, split):
     """Calls convert the state in and out: step(n1) + step(n2) agrees with step(n1 + n2) to the
     pair rounding of the state between the calls, and odd and even counts end in the right
     buffer."""
@@ -83,7 +100,7 @@ def test_pair_split_calls(gf, oracle, split):
         assert rel_err(to_np(x), r) <= RTOL
 
 
-def test_pair_repeatable_and_exactly_linear(gf, oracle):
+def test_pair_repeatable_and_exactly_linear(gf, oracle, kernel):
     mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 70, 66, False, True, 49)
     vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip, arithmetic="pair")
     s1, s2, s3 = _state(v0), _state(2.0 * v0), _state(v0)
@@ -127,3 +144,26 @@ def test_pair_ignored_in_strict_mode(gf, oracle):
             assert torch.equal(x, y)
     finally:
         gf.set_strict(False)
+
+
+def test_pair_kernels_agree(gf, oracle):
+    """The TMA pipeline and the one-tile-per-CTA kernel group the four-element sums differently:
+    their states agree to a few pair roundings."""
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 130, 75, False, True, 55)
+    vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip, arithmetic="pair")
+    out = []
+    try:
+        for k in (0, 1, 2):
+            _lib().call("gfgpu_set_pair_kernel", k)
+            s = _state(v0)
+            vv.step(*s, 100)
+            out.append(s)
+        _lib().call("gfgpu_verlet_pair_status")
+    finally:
+        _lib().call("gfgpu_set_pair_kernel", 0)
+    for k in (1, 2):
+        for x, y in zip(out[0], out[k]):
+            assert rel_err(to_np(x), to_np(y)) <= 1e-13
+    # the two TMA tile shapes group every sum alike: identical bits
+    for x, y in zip(out[0], out[2]):
+        assert torch.equal(x, y)
