@@ -372,18 +372,9 @@ k_verlet_pair_tma(const __grid_constant__ CUtensorMap mu, const __grid_constant_
             if (hf) fq = __ldg(p.fext + node);
         }
         const bool ok = pair_wait(s_bar + 8u * st, (i >> 1) & 1);
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) {
-                // let the copies this CTA issued land (bounded) before its shared memory is released
-                atomicExch(&g_pair_timeout, 1);
-                pair_wait(s_bar + 8u * st, (i >> 1) & 1);
-                if (next < p.ntiles) pair_wait(s_bar + 8u * (st ^ 1), ((i + 1) >> 1) & 1);
-            }
-            return;
-        }
         const unsigned char* sg = base + st * kStageBytes;
         const float4* su = reinterpret_cast<const float4*>(sg);
-        {
+        if (ok) {
             const float4 q0 = su[b0], q1 = su[b0 + 1], q2 = su[b0 + kTmaUW + 1], q3 = su[b0 + kTmaUW];
             const ffv u0x = lo2(q0), u0y = hi2(q0), u1x = lo2(q1), u1y = hi2(q1);
             const ffv u2x = lo2(q2), u2y = hi2(q2), u3x = lo2(q3), u3y = hi2(q3);
@@ -406,7 +397,16 @@ k_verlet_pair_tma(const __grid_constant__ CUtensorMap mu, const __grid_constant_
             const ffv H1 = ff_mul(kH, A3y);
             sH1[tid] = make_float2(H1.h, H1.l);
         }
-        __syncthreads();
+        // the element terms are complete; a CTA whose copies did not arrive stops here
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                // let the copies this CTA issued land (bounded) before its shared memory is released
+                atomicExch(&g_pair_timeout, 1);
+                pair_wait(s_bar + 8u * st, (i >> 1) & 1);
+                if (next < p.ntiles) pair_wait(s_bar + 8u * (st ^ 1), ((i + 1) >> 1) & 1);
+            }
+            return;
+        }
         if (warp >= kTmaTY) continue; // the last element row only feeds the node rows below it
         // node phase: the element column left of node (x0 + lane, y0 + warp): lo = element row
         // warp (below the node row), hi = warp + 1
