@@ -2000,8 +2000,12 @@ inline int tcp_tensor_map(CUtensorMap* map, const __nv_bfloat16* X, int H, int W
     return GFGPU_OK;
 }
 
+// Dependent launches between the network's layers (gfgpu_set_nn_pdl): on by default.
+int g_nn_pdl = 1;
+
 // launch with programmatic stream serialisation (the kernel's pdl_wait orders it after the
-// previous kernel of the stream)
+// previous kernel of the stream); an ordinary stream-ordered launch when dependent launches are
+// switched off (griddepcontrol.wait / launch_dependents are then no-ops)
 template <typename... KArgs, typename... Args>
 inline int launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                       Args... args)
@@ -2015,7 +2019,7 @@ inline int launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sm
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = g_nn_pdl ? 1 : 0;
     return check_cuda(cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...), "cudaLaunchKernelEx");
 }
 
@@ -2138,6 +2142,12 @@ inline int prepare_mma(cudaStream_t)
 } // namespace gfgpu
 
 extern "C" {
+
+int gfgpu_set_nn_pdl(int on)
+{
+    gfgpu::nn::g_nn_pdl = on ? 1 : 0;
+    return GFGPU_OK;
+}
 
 int gfgpu_nn_tc_status(void)
 {

@@ -563,8 +563,8 @@ static int nxp_of(int64_t nx)
 
 template <int TY>
 static int launch_tma(PairTmaStep p, const CUtensorMap* mu, const CUtensorMap& mv, const CUtensorMap& ma,
-                      const CUtensorMap& ml, const CUtensorMap& mh, const PairClassTab& tab, int64_t nsteps,
-                      float4* const* ub, int sms, cudaStream_t s)
+                      const CUtensorMap& ml, const CUtensorMap& mh, const PairClassTab& tab, int64_t first,
+                      int64_t count, int advance_last, float4* const* ub, int sms, cudaStream_t s)
 {
     using Gm = TmaGeom<TY>;
     static bool attr = false;
@@ -583,31 +583,61 @@ static int launch_tma(PairTmaStep p, const CUtensorMap* mu, const CUtensorMap& m
     const int grid = std::min(p.ntiles, sms * per_sm);
     p.gdx = grid % p.ntx;
     p.gdy = grid / p.ntx;
-    for (int64_t it = 0; it < nsteps; ++it) {
+    for (int64_t it = first; it < first + count; ++it) {
         p.uout = ub[(it + 1) & 1];
-        p.advance = it + 1 < nsteps ? 1 : 0;
+        p.advance = (it + 1 < first + count || advance_last) ? 1 : 0;
         k_verlet_pair_tma<TY><<<grid, Gm::threads, Gm::Smem, s>>>(mu[it & 1], mv, ma, ml, mh, p, tab);
         GF_TRY(check_launch("verlet pair kernel (TMA)"));
     }
     return GFGPU_OK;
 }
 
-// gfgpu_verlet_step's pair path (d->coef_pair set, fast arithmetic)
-int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
-                               int64_t nsteps, void* workspace, cudaStream_t s)
+// The pair state of a descriptor in the workspace: the displacement double-buffered (increment
+// `it` reads ub[it & 1] and writes the next displacement into ub[(it + 1) & 1]), v, a, fext.
+struct PairState {
+    float4 *ub[2], *v, *a, *fext;
+};
+
+static PairState pair_state(const gfgpu_verlet_desc* d, void* workspace)
 {
-    std::string why;
-    if (pair_applicable(d, &why) != GFGPU_OK)
-        return fail(GFGPU_ERR_UNSUPPORTED, "gfgpu_verlet_step (pair arithmetic): " + why);
-    GF_REQUIRE((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(v) | reinterpret_cast<uintptr_t>(a)) % 16 == 0,
-               "u, v, a must be 16-byte aligned");
-    GF_REQUIRE(!d->fext || reinterpret_cast<uintptr_t>(d->fext) % 16 == 0, "fext must be 16-byte aligned");
     const int64_t nn = d->nnode;
     float4* base = static_cast<float4*>(workspace);
-    float4* ub[2] = {base, base + nn};
-    float4* pv = base + 2 * nn;
-    float4* pa = base + 3 * nn;
-    float4* pfx = d->fext ? base + 4 * nn : nullptr;
+    return PairState{{base, base + nn}, base + 2 * nn, base + 3 * nn, d->fext ? base + 4 * nn : nullptr};
+}
+
+static int pair_check(const gfgpu_verlet_desc* d, const void* workspace)
+{
+    std::string why;
+    if (pair_applicable(d, &why) != GFGPU_OK) return fail(GFGPU_ERR_UNSUPPORTED, "pair arithmetic: " + why);
+    GF_REQUIRE(d->coef_pair, "pair arithmetic: d->coef_pair not set (gfgpu_verlet_precompute_pair)");
+    GF_REQUIRE(workspace && (reinterpret_cast<uintptr_t>(workspace) & 15u) == 0,
+               "pair arithmetic: workspace missing or not 16-byte aligned");
+    GF_REQUIRE(!d->fext || reinterpret_cast<uintptr_t>(d->fext) % 16 == 0, "fext must be 16-byte aligned");
+    return GFGPU_OK;
+}
+
+static int pair_begin(const gfgpu_verlet_desc* d, const double* u, const double* v, const double* a,
+                      void* workspace, cudaStream_t s)
+{
+    GF_REQUIRE(u && v && a, "bad argument");
+    GF_REQUIRE((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(v) | reinterpret_cast<uintptr_t>(a)) % 16 == 0,
+               "u, v, a must be 16-byte aligned");
+    const PairState ps = pair_state(d, workspace);
+    const double dt = d->dt, c = 0.5 * std::pow(dt, 2.0);
+    k_pair_begin<<<grid_for(d->nnode), kBlock, 0, s>>>(reinterpret_cast<const double2*>(u), reinterpret_cast<const double2*>(v),
+                                                       reinterpret_cast<const double2*>(a),
+                                                       reinterpret_cast<const double2*>(d->fext), d->nnode, dt, c,
+                                                       ps.ub[0], ps.v, ps.a, ps.fext);
+    return check_launch("pair begin");
+}
+
+static int pair_increments(const gfgpu_verlet_desc* d, int64_t first, int64_t count, int advance_last,
+                           void* workspace, cudaStream_t s)
+{
+    if (count <= 0) return GFGPU_OK;
+    const PairState ps = pair_state(d, workspace);
+    float4* const* ub = ps.ub;
+    float4 *pv = ps.v, *pa = ps.a, *pfx = ps.fext;
     const double dt = d->dt, h = 0.5 * dt, c = 0.5 * std::pow(dt, 2.0);
     PairClassTab tab{};
     for (int k = 0; k < d->ncls; ++k) {
@@ -619,11 +649,6 @@ int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v,
         tab.c2[k] = split_host(h * omh + h * h * be * be * dt);
         tab.c3[k] = split_host(h * omh);
     }
-    k_pair_begin<<<grid_for(nn), kBlock, 0, s>>>(reinterpret_cast<const double2*>(u), reinterpret_cast<const double2*>(v),
-                                                 reinterpret_cast<const double2*>(a),
-                                                 reinterpret_cast<const double2*>(d->fext), nn, dt, c, ub[0], pv,
-                                                 pa, pfx);
-    GF_TRY(check_launch("pair begin"));
     const int nx = static_cast<int>(d->reg_nx), ny = static_cast<int>(d->reg_ny), nxp = nxp_of(nx);
     const float4* cLN = reinterpret_cast<const float4*>(d->coef_pair);
     const float2* cH = reinterpret_cast<const float2*>(d->coef_pair + 4 * d->nelem);
@@ -642,53 +667,99 @@ int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v,
         p.dt = split_host(dt);
         p.cc = split_host(c);
         const dim3 grid(static_cast<unsigned>((nx + kPairTX) / kPairTX), static_cast<unsigned>((ny + kPairTY) / kPairTY));
-        for (int64_t it = 0; it < nsteps; ++it) {
+        for (int64_t it = first; it < first + count; ++it) {
             p.uin = ub[it & 1];
             p.uout = ub[(it + 1) & 1];
-            p.advance = it + 1 < nsteps ? 1 : 0;
+            p.advance = (it + 1 < first + count || advance_last) ? 1 : 0;
             k_verlet_pair_quad4<<<grid, kPairThreads, 0, s>>>(p, tab);
             GF_TRY(check_launch("verlet pair kernel"));
         }
+        return GFGPU_OK;
     }
-    else {
-        CUtensorMap mu[2], mv, ma, ml, mh;
-        const int TY = pair_kernel() == 2 ? 15 : 7;
-        GF_TRY(nodevec_map(&mu[0], ub[0], nx + 1, ny + 1, kTmaTX + 2, TY + 2));
-        GF_TRY(nodevec_map(&mu[1], ub[1], nx + 1, ny + 1, kTmaTX + 2, TY + 2));
-        GF_TRY(nodevec_map(&mv, pv, nx + 1, ny + 1, kTmaTX, TY));
-        GF_TRY(nodevec_map(&ma, pa, nx + 1, ny + 1, kTmaTX, TY));
-        GF_TRY(nodevec_map(&ml, cLN, nx, ny, kTmaTX + 1, TY + 1));
-        {
-            const cuuint64_t dims[2] = {2ull * static_cast<cuuint64_t>(nxp), static_cast<cuuint64_t>(ny)};
-            const cuuint64_t strides[1] = {8ull * static_cast<cuuint64_t>(nxp)};
-            const cuuint32_t box[2] = {static_cast<cuuint32_t>(TmaGeom<7>::HW), static_cast<cuuint32_t>(TY + 1)};
-            GF_TRY(encode_map(&mh, cH, 2, dims, strides, box));
-        }
-        int dev = 0, sms = 0;
-        GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
-        GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr"));
-        PairTmaStep p;
-        p.v = pv;
-        p.a = pa;
-        p.fext = pfx;
-        p.mcls = mcls;
-        p.nx = nx;
-        p.ny = ny;
-        p.ntx = (nx + kTmaTX) / kTmaTX;
-        p.dt = split_host(dt);
-        p.cc = split_host(c);
-        if (pair_kernel() == 2)
-            GF_TRY(launch_tma<15>(p, mu, mv, ma, ml, mh, tab, nsteps, ub, sms, s));
-        else
-            GF_TRY(launch_tma<7>(p, mu, mv, ma, ml, mh, tab, nsteps, ub, sms, s));
+    CUtensorMap mu[2], mv, ma, ml, mh;
+    const int TY = pair_kernel() == 2 ? 15 : 7;
+    GF_TRY(nodevec_map(&mu[0], ub[0], nx + 1, ny + 1, kTmaTX + 2, TY + 2));
+    GF_TRY(nodevec_map(&mu[1], ub[1], nx + 1, ny + 1, kTmaTX + 2, TY + 2));
+    GF_TRY(nodevec_map(&mv, pv, nx + 1, ny + 1, kTmaTX, TY));
+    GF_TRY(nodevec_map(&ma, pa, nx + 1, ny + 1, kTmaTX, TY));
+    GF_TRY(nodevec_map(&ml, cLN, nx, ny, kTmaTX + 1, TY + 1));
+    {
+        const cuuint64_t dims[2] = {2ull * static_cast<cuuint64_t>(nxp), static_cast<cuuint64_t>(ny)};
+        const cuuint64_t strides[1] = {8ull * static_cast<cuuint64_t>(nxp)};
+        const cuuint32_t box[2] = {static_cast<cuuint32_t>(TmaGeom<7>::HW), static_cast<cuuint32_t>(TY + 1)};
+        GF_TRY(encode_map(&mh, cH, 2, dims, strides, box));
     }
-    // the last increment does not advance: its displacement is the one it read
-    k_pair_end<<<grid_for(nn), kBlock, 0, s>>>(ub[(nsteps - 1) & 1], pv, pa, nn, reinterpret_cast<double2*>(u),
-                                               reinterpret_cast<double2*>(v), reinterpret_cast<double2*>(a));
+    int dev = 0, sms = 0;
+    GF_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+    GF_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr"));
+    PairTmaStep p;
+    p.v = pv;
+    p.a = pa;
+    p.fext = pfx;
+    p.mcls = mcls;
+    p.nx = nx;
+    p.ny = ny;
+    p.ntx = (nx + kTmaTX) / kTmaTX;
+    p.dt = split_host(dt);
+    p.cc = split_host(c);
+    if (TY == 15) return launch_tma<15>(p, mu, mv, ma, ml, mh, tab, first, count, advance_last, ub, sms, s);
+    return launch_tma<7>(p, mu, mv, ma, ml, mh, tab, first, count, advance_last, ub, sms, s);
+}
+
+static int pair_end(const gfgpu_verlet_desc* d, int64_t last, double* u, double* v, double* a, void* workspace,
+                    cudaStream_t s)
+{
+    GF_REQUIRE(u && v && a && last >= 0, "bad argument");
+    const PairState ps = pair_state(d, workspace);
+    k_pair_end<<<grid_for(d->nnode), kBlock, 0, s>>>(ps.ub[last & 1], ps.v, ps.a, d->nnode, reinterpret_cast<double2*>(u),
+                                                     reinterpret_cast<double2*>(v), reinterpret_cast<double2*>(a));
     return check_launch("pair end");
 }
 
+// gfgpu_verlet_step's pair path (d->coef_pair set, fast arithmetic)
+int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
+                               int64_t nsteps, void* workspace, cudaStream_t s)
+{
+    GF_TRY(pair_check(d, workspace));
+    GF_TRY(pair_begin(d, u, v, a, workspace, s));
+    GF_TRY(pair_increments(d, 0, nsteps, 0, workspace, s));
+    // the last increment does not advance: its displacement is the one it read
+    return pair_end(d, nsteps - 1, u, v, a, workspace, s);
+}
+
 extern "C" {
+
+int gfgpu_verlet_pair_begin(const gfgpu_verlet_desc* d, const double* u, const double* v, const double* a,
+                            void* workspace, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d, "null descriptor");
+    GF_TRY(pair_check(d, workspace));
+    return pair_begin(d, u, v, a, workspace, S(stream));
+}
+
+int gfgpu_verlet_pair_increments(const gfgpu_verlet_desc* d, int64_t first, int64_t count, int32_t advance_last,
+                                 void* workspace, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d && first >= 0 && count >= 0, "bad argument");
+    GF_TRY(pair_check(d, workspace));
+    return pair_increments(d, first, count, advance_last ? 1 : 0, workspace, S(stream));
+}
+
+int gfgpu_verlet_pair_end(const gfgpu_verlet_desc* d, int64_t last, double* u, double* v, double* a,
+                          void* workspace, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d, "null descriptor");
+    GF_TRY(pair_check(d, workspace));
+    return pair_end(d, last, u, v, a, workspace, S(stream));
+}
+
+int gfgpu_verlet_pair_displacement(const gfgpu_verlet_desc* d, int64_t it, void* workspace, void** ptr)
+{
+    GF_REQUIRE(d && ptr && it >= 0, "bad argument");
+    GF_TRY(pair_check(d, workspace));
+    *ptr = pair_state(d, workspace).ub[it & 1];
+    return GFGPU_OK;
+}
 
 int64_t gfgpu_verlet_pair_coef_floats(const gfgpu_verlet_desc* d)
 {

@@ -72,6 +72,11 @@ int gfgpu_verlet_pair_status(void);
  * arithmetic (BF16 products, FP32 accumulation); the summation order differs between 0, 1 and
  * 2/3 (2 and 3 give identical bits). */
 int gfgpu_set_nn_tensor_path(int path);
+/* Programmatic dependent launch between the network's layers on path 2 (process-wide, default
+ * 1): each layer lets the next one launch once its CTAs are resident; the next one sets up
+ * (TMEM, barriers, weights) and executes griddepcontrol.wait before it reads the previous layer's
+ * output or writes anything. 0 = ordinary stream-ordered launches. Same results bit for bit. */
+int gfgpu_set_nn_pdl(int on);
 /* Error flag of the tcgen05 layers' bounded waits: GFGPU_ERR_TIMEOUT if a wait for the tensor
  * cores gave up since the last call (the layer's output is then invalid), else GFGPU_OK. Clears
  * the flag. Synchronises the device. */
@@ -399,6 +404,26 @@ int64_t gfgpu_verlet_pair_coef_floats(const gfgpu_verlet_desc* d);
  * to ~1e-14 relative (48-bit significands, FP32 exponent range: |values| between ~1e-30 and
  * ~1e38). Strict mode ignores coef_pair. */
 int gfgpu_verlet_precompute_pair(const gfgpu_verlet_desc* d, float* coef_pair, gfgpu_stream_t stream);
+/* The pair path of gfgpu_verlet_step in three parts, for callers that act between increments
+ * (the row-block partition's halo exchange, goosefem_gb300/partition.py). The state lives in
+ * `workspace` (gfgpu_verlet_workspace_bytes with d->coef_pair set). Increments are numbered from 0
+ * after begin; increment `it` reads the displacement buffer of parity it & 1 and, if it advances,
+ * writes the predicted displacement of increment it + 1 into the other one.
+ *  begin: u, v, a (FP64 nodevecs) -> pair state, with the FP64 predictor u + dt v + dt^2/2 a of
+ *         increment 0 (main.cpp:119);
+ *  increments: increments first .. first + count - 1; all advance except the last one unless
+ *         advance_last (the last increment of a run leaves u as it read it, as gfgpu_verlet_step);
+ *  end: the pair state -> u (the displacement increment `last` read), v, a;
+ *  displacement: *ptr = the pair nodevec [nnode] of float4 {x.h, x.l, y.h, y.l} that increment
+ *         `it` reads (host call, no GPU work): where a halo exchange writes rows of neighbours.
+ * gfgpu_verlet_step(n) = begin, increments(0, n, 0), end(n - 1): the same bits. */
+int gfgpu_verlet_pair_begin(const gfgpu_verlet_desc* d, const double* u, const double* v, const double* a,
+                            void* workspace, gfgpu_stream_t stream);
+int gfgpu_verlet_pair_increments(const gfgpu_verlet_desc* d, int64_t first, int64_t count, int32_t advance_last,
+                                 void* workspace, gfgpu_stream_t stream);
+int gfgpu_verlet_pair_end(const gfgpu_verlet_desc* d, int64_t last, double* u, double* v, double* a,
+                          void* workspace, gfgpu_stream_t stream);
+int gfgpu_verlet_pair_displacement(const gfgpu_verlet_desc* d, int64_t it, void* workspace, void** ptr);
 /* Host set-up of the lumped-mass classes: reads part and inv back from the device, and if the
  * free dofs take at most GFGPU_MASS_CLASSES distinct inverse masses (a Regular mesh with uniform
  * density: interior, edge and corner values) writes mclass [nnode*ndim] (device, uint8) and

@@ -208,6 +208,41 @@ def test_tensor_core_inference_matches_fp32_and_oracle(L, H, W):
     assert np.array_equal(out[2], out[3])
 
 
+@pytest.mark.parametrize("H,W", [(37, 45), (513, 513)])
+def test_dependent_launches_give_the_same_bits(L, H, W):
+    """The default network chain (path 2: tcgen05 + TMA layers) launched with programmatic
+    dependent launch and with ordinary stream-ordered launches: identical bits, repeatedly (a layer
+    that read its predecessor's output before griddepcontrol.wait, or wrote before it, would show
+    up as a difference or as run-to-run variation)."""
+    from goosefem_gb300.learned import NNDesc
+    import ctypes as C
+
+    pt, wb = _random_params(L, 5, scale=0.8)
+    X0 = np.random.default_rng(6).normal(size=(H, W, 4)).astype(np.float32)
+    Xd = torch.as_tensor(X0, device="cuda")
+    mat = torch.zeros((H, W, 2), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    d = NNDesc()
+    d.weights_bf16, d.params_f32, d.material, d.H, d.W = wb.data_ptr(), pt.data_ptr(), mat.data_ptr(), H, W
+    ws = torch.empty(int(L.lib().gfgpu_nn_infer_workspace_bytes(H, W)) // 8 + 1, dtype=torch.float64,
+                     device="cuda")
+    out = []
+    try:
+        L.call("gfgpu_set_nn_tensor_path", 2)
+        for pdl in (1, 0, 1, 0):
+            L.call("gfgpu_set_nn_pdl", pdl)
+            y = torch.full((H, W, 2), float("nan"), dtype=torch.float32, device="cuda")
+            for _ in range(3):  # back-to-back applications: each one's first layer follows the last
+                L.call("gfgpu_nn_infer", C.addressof(d), Xd.data_ptr(), y.data_ptr(), ws.data_ptr(), s)
+            L.call("gfgpu_nn_tc_status")
+            out.append(y.cpu().numpy())
+    finally:
+        L.call("gfgpu_set_nn_pdl", 1)
+    assert np.all(np.isfinite(out[0]))
+    for o in out[1:]:
+        assert np.array_equal(o, out[0])
+
+
 @pytest.fixture(scope="module")
 def small_problem():
     from goosefem_gb300 import learned as LR
@@ -340,6 +375,16 @@ def test_trained_network_reduces_twolevel_iterations():
     x_nn = lp.initial_guess(xp)
     it_nn, fb, rel_nn = lp.solve(x_nn, nkeep=4)
     assert fb == 0
+    # the same solve with the network's layers launched without dependent launches: same bits
+    from goosefem_gb300 import _lib as L
+
+    try:
+        L.call("gfgpu_set_nn_pdl", 0)
+        x_np = lp.initial_guess(xp)
+        it_np, fb_np, _ = lp.solve(x_np, nkeep=4)
+    finally:
+        L.call("gfgpu_set_nn_pdl", 1)
+    assert (it_np, fb_np) == (it_nn, fb) and torch.equal(x_np, x_nn)
     A, xr = _direct(nx, ny, K, G, iip, xp)
     xg = x_nn.cpu().numpy()
     assert rel_nn <= 1e-8 and S.residual(A, iip, xg) <= 1e-8
