@@ -309,7 +309,7 @@ def run_gpu(args, rank, world):
     _lib.call("gfgpu_set_variant", ev, nv)
     w = workload(args.nx, gf.Mesh)
     nnode, nelem, inc = w["nnode"], w["nelem"], args.increments
-    pair = args.arith == "pair" and args.path == "auto"
+    pair = args.arith == "pair" and args.path in ("auto", "general")
     vv = gf.VelocityVerlet(w["coor"], w["conn"], w["dofs"], w["K"], w["G"], rho=1.0, dt=w["dt"],
                            eta=w["eta"], iip=w["iip"], uniform=(False if args.path == "general"
                                                                 else "auto"),
@@ -401,7 +401,7 @@ def run_gpu(args, rank, world):
         hbm_peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
     path = vv.path
-    kernel = {"uniform-square-pair": "k_verlet_pair_tma",
+    kernel = {"uniform-square-pair": "k_verlet_pair_tma", "general-pair": "k_pair_elem_stiff",
               "uniform-square": "k_elem_force_quad4_square", "uniform": "k_elem_force_quad4_uniform",
               "general": "k_elem_force_general"}[path]
     # fused-step minimum traffic (SURVEY-defined algorithmic bytes of one increment): u, v, a
@@ -686,6 +686,20 @@ def workload_batch(args):
     inst = B.seeded_instances(args.ninst, 256)
     bv = B.BatchedVerlet(inst)
     table = bv.autotune(nsteps=20, reps=2)
+    # the pair schedule beside it (not a candidate: see BatchedVerlet.autotune), with its deviation
+    mode0 = (bv.mode, bv.block, bv.bps)
+    bv.mode = 2
+    up, vp, ap = bv.state()
+    bv.run_direct(up, vp, ap, 5)
+    torch.cuda.synchronize()
+    up, vp, ap = bv.state()
+    e0p, e1p = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0p.record()
+    bv.run_direct(up, vp, ap, args.batch_steps)
+    e1p.record()
+    torch.cuda.synchronize()
+    pair_ms = e0p.elapsed_time(e1p) / args.batch_steps
+    bv.mode, bv.block, bv.bps = mode0
     nsteps = args.batch_steps
     u, v, a = bv.state()
     bv.run_graph(u, v, a, nsteps)  # warm-up (also builds the graph)
@@ -700,18 +714,27 @@ def workload_batch(args):
     if bv.mode == 1:
         bv.check_status()
     sec = e0.elapsed_time(e1) * 1e-3
-    seq = B.run_sequential(inst, nsteps, bv.dt)
+    pair_dev = {k: float((x - y).abs().max() / y.abs().max()) for k, x, y in (("u", up, u), ("v", vp, v), ("a", ap, a))}
+    seq = B.run_sequential(inst, nsteps, bv.dt, arithmetic=bv.arithmetic)
     res = {"metric": "elem-Gauss-pt updates/s (batched)", "value": bv.nelem * 4 * nsteps / sec,
-           "unit": "elem-Gauss-pt/s", "higher_is_better": True, "dtype": "f64",
+           "unit": "elem-Gauss-pt/s", "higher_is_better": True,
+           "dtype": "f64",
            "data": "synthetic (seeded)",
            "config": {"workload": f"{len(inst)} periodic Quad4 Regular instances, nx,ny~U{{32..512}},"
                                   f" {nsteps} increments, applied shear 1e-3",
                       "nelem_total": bv.nelem,
-                      "schedule": {"mode": ["graph of 2 kernels", "persistent"][bv.mode],
+                      "schedule": {"mode": ["graph of 2 FP64 kernels", "persistent FP64 kernel",
+                                            "graph of 2 pair kernels"][bv.mode],
                                    "block": bv.block, "blocks_per_sm": bv.bps},
                       "colouring": "none: the node kernels gather through the dof CSR "
                                    "(deterministic, no scatter conflicts to colour)"},
-           "seconds": sec, "ms_per_increment": 1e3 * sec / nsteps, "sequential_seconds": seq,
+           "seconds": sec, "ms_per_increment": 1e3 * sec / nsteps,
+           "pair_schedule": {"ms_per_increment": pair_ms, "max_rel_dev_vs_fp64": pair_dev,
+                             "note": "graph of the float-float element + CSR node kernels; not chosen: "
+                                     "the applied shear makes the displacement ~600x its fluctuations, "
+                                     "and the pair rounding of the displacement then exceeds the 1e-12 "
+                                     "agreement"},
+           "sequential_seconds": seq,
            "speedup_vs_sequential": seq / sec,
            "autotune": [{"mode": r[0], "block": r[1], "bps": r[2], "ms_per_increment": r[3]}
                         for r in table]}

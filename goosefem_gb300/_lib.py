@@ -36,7 +36,7 @@ class VerletDesc(C.Structure):
         ("coef", C.c_void_p),
         ("mclass", C.c_void_p), ("mclass_inv", C.c_void_p), ("ncls", C.c_int32),
         ("reg_nx", C.c_int64), ("reg_ny", C.c_int64), ("reg_nz", C.c_int64),
-        ("coef_pair", C.c_void_p),
+        ("coef_pair", C.c_void_p), ("pair_mode", C.c_int32),
     ]
 
 

@@ -437,6 +437,205 @@ k_verlet_pair_tma(const __grid_constant__ CUtensorMap mu, const __grid_constant_
     }
 }
 
+// ------------------------------------------------------------------ element kernel + CSR node kernel
+//
+// The pair path for Quad4 meshes that are not the Regular square-element case: an element kernel
+// writes the element forces as pairs, fe[e * 4 + m] = {fx.h, fx.l, fy.h, fy.l}, and a node kernel
+// gathers them through the dof CSR (ascending flat elemvec index, the order of Vector.h:724-741;
+// periodic ties allowed) and takes the three velocity estimates and the predictor, all on pairs.
+// Element forces: the square closed form (pair_element) on uniform square elements, otherwise the
+// stored element stiffness K_e (8 x 8, symmetric; 36 pairs per element) times u_e. The stiffness
+// is K_e[(m,j),(n,l)] = sum_q vol_q (lam dNx(m,j) dNx(n,l) + G (delta_jl dNx(m,.).dNx(n,.) +
+// dNx(m,l) dNx(n,j))), the linear map of the reference's chain symGradN -> stress ->
+// int_gradN_dot_tensor2_dV (ElementQuad4.h:407-491) for sigma = K tr(eps) I + 2 G dev(eps).
+
+__host__ __device__ constexpr int tri8(int r, int c)
+{
+    // packed upper triangle of an 8 x 8 matrix, r <= c, row by row
+    return r * 8 - r * (r - 1) / 2 + (c - r);
+}
+
+__global__ void k_pair_stiffness(const double* __restrict__ dNx, const double* __restrict__ vol,
+                                 const double* __restrict__ Km, const double* __restrict__ Gm, int64_t nelem,
+                                 int nip, float2* __restrict__ Ke)
+{
+    GF_FOR(e, nelem)
+    {
+        double k[36];
+#pragma unroll
+        for (int i = 0; i < 36; ++i) k[i] = 0.0;
+        const double G = Gm[e], lam = Km[e] - 2.0 * G / 3.0;
+        for (int q = 0; q < nip; ++q) {
+            double g[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) g[i] = dNx[(e * nip + q) * 8 + i];
+            const double v = vol[e * nip + q];
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+#pragma unroll
+                for (int c = r; c < 8; ++c) {
+                    const int m = r / 2, j = r % 2, n = c / 2, l = c % 2;
+                    const double dd = g[m * 2] * g[n * 2] + g[m * 2 + 1] * g[n * 2 + 1];
+                    const double val = lam * g[m * 2 + j] * g[n * 2 + l] + G * ((j == l ? dd : 0.0) + g[m * 2 + l] * g[n * 2 + j]);
+                    k[tri8(r, c)] += v * val;
+                }
+        }
+#pragma unroll
+        for (int i = 0; i < 36; ++i) {
+            const ffv x = ff_from_double(k[i]);
+            Ke[i * nelem + e] = make_float2(x.h, x.l);
+        }
+    }
+}
+
+// element-indexed pair coefficients of the square closed form: cLN[e] = {L, N}, cH[e] = kH
+__global__ void k_pair_coef_elem(const double* __restrict__ Km, const double* __restrict__ Gm, int64_t nelem,
+                                 double g2, float4* __restrict__ cLN, float2* __restrict__ cH)
+{
+    GF_FOR(e, nelem)
+    {
+        const double K = Km[e], G = Gm[e];
+        const double lam = K - 2.0 * G / 3.0;
+        cLN[e] = pack(ff_from_double(0.25 * lam), ff_from_double(0.25 * G));
+        const ffv kH = ff_from_double(0.25 * g2 * (lam + 3.0 * G));
+        cH[e] = make_float2(kH.h, kH.l);
+    }
+}
+
+__global__ void k_pair_split(const double* __restrict__ x, int64_t n, float2* __restrict__ out)
+{
+    GF_FOR(i, n)
+    {
+        const ffv y = ff_from_double(x[i]);
+        out[i] = make_float2(y.h, y.l);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_pair_elem_square(const int32_t* __restrict__ conn, const float4* __restrict__ u, const float4* __restrict__ cLN,
+                   const float2* __restrict__ cH, int64_t nelem, float4* __restrict__ fe)
+{
+    GF_FOR(e, nelem)
+    {
+        const int4 cn = __ldg(reinterpret_cast<const int4*>(conn) + e);
+        float4 S, D, H;
+        pair_element(__ldg(u + cn.x), __ldg(u + cn.y), __ldg(u + cn.z), __ldg(u + cn.w), __ldg(cLN + e), __ldg(cH + e), S,
+                     D, H);
+        const ffv Sx = lo2(S), Sy = hi2(S), Dx = lo2(D), Dy = hi2(D), H0 = lo2(H), H1 = hi2(H);
+        float4* o = fe + e * 4;
+        o[0] = pack(ff_norm(ff_sub(H0, Sx)), ff_norm(ff_sub(H1, Sy)));
+        o[1] = pack(ff_norm(ff_sub(Dx, H0)), ff_norm(ff_sub(Dy, H1)));
+        o[2] = pack(ff_norm(ff_add(Sx, H0)), ff_norm(ff_add(Sy, H1)));
+        o[3] = pack(ff_norm(ff_neg(ff_add(Dx, H0))), ff_norm(ff_neg(ff_add(Dy, H1))));
+    }
+}
+
+__global__ void __launch_bounds__(128)
+k_pair_elem_stiff(const int32_t* __restrict__ conn, const float4* __restrict__ u, const float2* __restrict__ Ke,
+                  int64_t nelem, float4* __restrict__ fe)
+{
+    GF_FOR(e, nelem)
+    {
+        const int4 cn = __ldg(reinterpret_cast<const int4*>(conn) + e);
+        const float4 q[4] = {__ldg(u + cn.x), __ldg(u + cn.y), __ldg(u + cn.z), __ldg(u + cn.w)};
+        ffv uc[8];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            uc[2 * m] = lo2(q[m]);
+            uc[2 * m + 1] = hi2(q[m]);
+        }
+        ffv f[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            ffv acc = ff_make(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const float2 k = __ldg(Ke + static_cast<int64_t>(r <= c ? tri8(r, c) : tri8(c, r)) * nelem + e);
+                const ffv t = ff_mul(pf(k), uc[c]);
+                acc = c == 0 ? t : ff_add(acc, t);
+            }
+            f[r] = ff_norm(acc);
+        }
+        float4* o = fe + e * 4;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) o[m] = pack(f[2 * m], f[2 * m + 1]);
+    }
+}
+
+struct PairCsrStep {
+    const int32_t *dofs, *ptr, *idx, *part;
+    int64_t nnu, n;
+    const uint8_t* mclass;  // per nodevec entry, or null: per-dof inverse mass minv
+    const float2* minv;     // [nnu] pair inverse lumped mass (no classes)
+    const float2* fe;       // [nelem * nne * ndim] element forces
+    const float2* fext;     // per nodevec entry or null
+    float2 *u, *v, *a;      // per nodevec entry
+    float2 dt, h, cc, eta;
+    int advance;
+};
+
+__global__ void __launch_bounds__(256)
+k_pair_node_csr(const PairCsrStep p, const __grid_constant__ PairClassTab tab)
+{
+    __shared__ float2 smi[GFGPU_MASS_CLASSES], sbe[GFGPU_MASS_CLASSES], sc1[GFGPU_MASS_CLASSES],
+        sc2[GFGPU_MASS_CLASSES], sc3[GFGPU_MASS_CLASSES];
+    if (threadIdx.x < GFGPU_MASS_CLASSES) {
+        const int c = threadIdx.x;
+        smi[c] = tab.mi[c];
+        sbe[c] = tab.be[c];
+        sc1[c] = tab.c1[c];
+        sc2[c] = tab.c2[c];
+        sc3[c] = tab.c3[c];
+    }
+    __syncthreads();
+    const ffv dt = pf(p.dt), h = pf(p.h), cc = pf(p.cc);
+    GF_FOR(t, p.n)
+    {
+        const int32_t d = __ldg(p.dofs + t);
+        const int32_t b = __ldg(p.ptr + d), en = __ldg(p.ptr + d + 1);
+        ffv f = ff_make(0.f, 0.f);
+        for (int32_t j = b; j < en; ++j) {
+            const ffv g = pf(__ldg(p.fe + __ldg(p.idx + j)));
+            f = j == b ? g : ff_add(f, g);
+        }
+        f = ff_norm(f);
+        const ffv fx = p.fext ? pf(__ldg(p.fext + t)) : ff_make(0.f, 0.f);
+        const ffv vn = pf(p.v[t]), an = pf(p.a[t]);
+        ffv vv, aa;
+        if (p.mclass) {
+            pair_update(__ldg(p.mclass + t), f, fx, p.fext != nullptr, vn, an, smi, sbe, sc1, sc2, sc3, dt, vv, aa);
+        }
+        else {
+            const int32_t q = __ldg(p.part + t);
+            if (q < p.nnu) {
+                // the closed form of the three estimates with this dof's coefficients (MassClassTab)
+                const ffv mi = pf(__ldg(p.minv + q));
+                const ffv be = ff_mul(mi, pf(p.eta));
+                const ffv x = ff_norm(ff_mul(h, be));
+                const ffv omh = ff_norm(ff_sub(ff_make(1.f, 0.f), x));
+                const ffv x2 = ff_mul(x, x);
+                const ffv c1 = ff_add(omh, x2), c3 = ff_mul(h, omh);
+                const ffv c2 = ff_add(c3, ff_mul(x2, dt));
+                const ffv R = p.fext ? ff_sub(fx, f) : ff_neg(f);
+                const ffv mR = ff_mul(mi, R);
+                vv = ff_norm(ff_add(ff_add(ff_mul(c1, vn), ff_mul(c2, an)), ff_mul(c3, mR)));
+                aa = ff_norm(ff_sub(mR, ff_mul(be, vv)));
+            }
+            else {
+                aa = an;
+                vv = ff_norm(ff_add(vn, ff_mul(dt, an)));
+            }
+        }
+        p.v[t] = make_float2(vv.h, vv.l);
+        p.a[t] = make_float2(aa.h, aa.l);
+        if (p.advance) {
+            const ffv un = pf(p.u[t]);
+            const ffv uu = ff_norm(ff_add(ff_add(un, ff_mul(dt, vv)), ff_mul(cc, aa)));
+            p.u[t] = make_float2(uu.h, uu.l);
+        }
+    }
+}
+
 // FP64 in: the predictor u + dt v + dt^2/2 a of the first increment (FP64, as k_predict), then
 // u, v, a (and fext) as pairs
 __global__ void k_pair_begin(const double2* __restrict__ u, const double2* __restrict__ v,
@@ -515,6 +714,32 @@ static int pair_applicable(const gfgpu_verlet_desc* d, std::string* why)
     return w ? GFGPU_ERR_UNSUPPORTED : GFGPU_OK;
 }
 
+// Which pair path a descriptor can take: 1 = the Regular square-element tile kernel
+// (pair_applicable), 2 = element kernel + dof-CSR node kernel with the square closed form (uniform
+// square Quad4 elements, any numbering, periodic ties allowed), 3 = the same with stored element
+// stiffness matrices (any Quad4 mesh with the Gauss rule); 0 = none (why says why).
+static int pair_mode_for(const gfgpu_verlet_desc* d, std::string* why)
+{
+    if (pair_applicable(d, why) == GFGPU_OK) return 1;
+    if (d->nne != 4 || d->ndim != 2) {
+        if (why) *why = "Quad4 only";
+        return 0;
+    }
+    if (d->nelem * 8 >= INT32_MAX || d->nnode * 2 >= INT32_MAX) {
+        if (why) *why = "mesh too large";
+        return 0;
+    }
+    if (d->uniform && std::fabs(d->hx - d->hy) <= 1e-12 * d->hx) return 2;
+    if (d->dNx && d->vol && d->nip == 4) return 3;
+    if (why) *why = "needs the Gauss-rule dNx and vol of the mesh";
+    return 0;
+}
+
+static bool pair_has_classes(const gfgpu_verlet_desc* d)
+{
+    return d->mclass && d->mclass_inv && d->ncls > 0;
+}
+
 } // namespace gfgpu
 
 using namespace gfgpu;
@@ -522,8 +747,10 @@ using namespace gfgpu;
 int64_t gfgpu_internal_pair_workspace_bytes(const gfgpu_verlet_desc* d)
 {
     if (!d || !d->coef_pair) return 0;
-    const int64_t vecs = d->fext ? 5 : 4;
-    return vecs * d->nnode * static_cast<int64_t>(sizeof(float4));
+    const int64_t f4 = static_cast<int64_t>(sizeof(float4));
+    if (d->pair_mode == 1) return (d->fext ? 5 : 4) * d->nnode * f4;
+    // u, v, a (fext) pair nodevecs and the element forces [nelem * nne] of float4
+    return (d->fext ? 4 : 3) * d->nnode * f4 + d->nelem * 4 * f4;
 }
 
 static int encode_map(CUtensorMap* map, const void* ptr, cuuint32_t rank, const cuuint64_t* dims,
@@ -602,14 +829,24 @@ static PairState pair_state(const gfgpu_verlet_desc* d, void* workspace)
 {
     const int64_t nn = d->nnode;
     float4* base = static_cast<float4*>(workspace);
+    if (d->pair_mode != 1) // one displacement buffer: the element and node phases are two kernels
+        return PairState{{base, base}, base + nn, base + 2 * nn, d->fext ? base + 3 * nn : nullptr};
     return PairState{{base, base + nn}, base + 2 * nn, base + 3 * nn, d->fext ? base + 4 * nn : nullptr};
+}
+
+// element forces of the CSR pair path, after the state vectors
+static float4* pair_fe(const gfgpu_verlet_desc* d, void* workspace)
+{
+    return static_cast<float4*>(workspace) + (d->fext ? 4 : 3) * d->nnode;
 }
 
 static int pair_check(const gfgpu_verlet_desc* d, const void* workspace)
 {
     std::string why;
-    if (pair_applicable(d, &why) != GFGPU_OK) return fail(GFGPU_ERR_UNSUPPORTED, "pair arithmetic: " + why);
+    const int mode = pair_mode_for(d, &why);
+    if (mode == 0) return fail(GFGPU_ERR_UNSUPPORTED, "pair arithmetic: " + why);
     GF_REQUIRE(d->coef_pair, "pair arithmetic: d->coef_pair not set (gfgpu_verlet_precompute_pair)");
+    GF_REQUIRE(d->pair_mode == mode, "pair arithmetic: the descriptor changed since gfgpu_verlet_precompute_pair");
     GF_REQUIRE(workspace && (reinterpret_cast<uintptr_t>(workspace) & 15u) == 0,
                "pair arithmetic: workspace missing or not 16-byte aligned");
     GF_REQUIRE(!d->fext || reinterpret_cast<uintptr_t>(d->fext) % 16 == 0, "fext must be 16-byte aligned");
@@ -648,6 +885,43 @@ static int pair_increments(const gfgpu_verlet_desc* d, int64_t first, int64_t co
         tab.c1[k] = split_host(omh + h * h * be * be);
         tab.c2[k] = split_host(h * omh + h * h * be * be * dt);
         tab.c3[k] = split_host(h * omh);
+    }
+    if (d->pair_mode != 1) {
+        float4* fe = pair_fe(d, workspace);
+        PairCsrStep q;
+        q.dofs = d->dofs;
+        q.ptr = d->csr_ptr;
+        q.idx = d->csr_idx;
+        q.part = d->part;
+        q.nnu = d->nnu;
+        q.n = d->nnode * 2;
+        const bool cls = pair_has_classes(d);
+        q.mclass = cls ? d->mclass : nullptr;
+        const int64_t ncoef = d->pair_mode == 2 ? 6 * d->nelem : 72 * d->nelem;
+        q.minv = cls ? nullptr : reinterpret_cast<const float2*>(d->coef_pair + ncoef);
+        q.fe = reinterpret_cast<const float2*>(fe);
+        q.fext = reinterpret_cast<const float2*>(pfx);
+        q.u = reinterpret_cast<float2*>(ub[0]);
+        q.v = reinterpret_cast<float2*>(pv);
+        q.a = reinterpret_cast<float2*>(pa);
+        q.dt = split_host(dt);
+        q.h = split_host(h);
+        q.cc = split_host(c);
+        q.eta = split_host(d->eta);
+        for (int64_t it = first; it < first + count; ++it) {
+            if (d->pair_mode == 2)
+                k_pair_elem_square<<<grid_for(d->nelem), 256, 0, s>>>(
+                    d->conn, ub[0], reinterpret_cast<const float4*>(d->coef_pair),
+                    reinterpret_cast<const float2*>(d->coef_pair + 4 * d->nelem), d->nelem, fe);
+            else
+                k_pair_elem_stiff<<<grid_for(d->nelem, 128), 128, 0, s>>>(
+                    d->conn, ub[0], reinterpret_cast<const float2*>(d->coef_pair), d->nelem, fe);
+            GF_TRY(check_launch("pair element kernel"));
+            q.advance = (it + 1 < first + count || advance_last) ? 1 : 0;
+            k_pair_node_csr<<<grid_for(q.n), 256, 0, s>>>(q, tab);
+            GF_TRY(check_launch("pair node kernel"));
+        }
+        return GFGPU_OK;
     }
     const int nx = static_cast<int>(d->reg_nx), ny = static_cast<int>(d->reg_ny), nxp = nxp_of(nx);
     const float4* cLN = reinterpret_cast<const float4*>(d->coef_pair);
@@ -763,25 +1037,49 @@ int gfgpu_verlet_pair_displacement(const gfgpu_verlet_desc* d, int64_t it, void*
 
 int64_t gfgpu_verlet_pair_coef_floats(const gfgpu_verlet_desc* d)
 {
-    if (!d || d->reg_nx <= 0 || d->reg_ny <= 0) return 0;
-    return 4 * d->reg_nx * d->reg_ny + 2 * static_cast<int64_t>(nxp_of(d->reg_nx)) * d->reg_ny;
+    if (!d) return 0;
+    const int mode = pair_mode_for(d, nullptr);
+    if (mode == 1) return 4 * d->reg_nx * d->reg_ny + 2 * static_cast<int64_t>(nxp_of(d->reg_nx)) * d->reg_ny;
+    if (mode == 0) return 0;
+    const int64_t minv = pair_has_classes(d) ? 0 : 2 * d->nnu;
+    return (mode == 2 ? 6 : 72) * d->nelem + minv;
 }
 
-int gfgpu_verlet_precompute_pair(const gfgpu_verlet_desc* d, float* coef_pair, gfgpu_stream_t stream)
+int gfgpu_verlet_precompute_pair(gfgpu_verlet_desc* d, float* coef_pair, gfgpu_stream_t stream)
 {
     GF_REQUIRE(d && coef_pair, "bad argument");
     GF_REQUIRE((reinterpret_cast<uintptr_t>(coef_pair) & 15u) == 0, "coef_pair must be 16-byte aligned");
     std::string why;
-    if (pair_applicable(d, &why) != GFGPU_OK) return fail(GFGPU_ERR_UNSUPPORTED, "gfgpu_verlet_precompute_pair: " + why);
+    const int mode = pair_mode_for(d, &why);
+    if (mode == 0) return fail(GFGPU_ERR_UNSUPPORTED, "gfgpu_verlet_precompute_pair: " + why);
     GF_REQUIRE(d->K && d->G, "null material");
+    d->pair_mode = mode;
     if (d->nelem == 0) return GFGPU_OK;
+    cudaStream_t s = S(stream);
     const double g = 1.0 / std::sqrt(3.0);
-    const int nx = static_cast<int>(d->reg_nx), ny = static_cast<int>(d->reg_ny), nxp = nxp_of(nx);
-    float4* cLN = reinterpret_cast<float4*>(coef_pair);
-    float2* cH = reinterpret_cast<float2*>(coef_pair + 4 * d->nelem);
-    k_pair_coef<<<grid_for(static_cast<int64_t>(ny) * nxp), kBlock, 0, S(stream)>>>(d->K, d->G, nx, ny, nxp, g * g,
-                                                                                   cLN, cH);
-    return check_launch("verlet_precompute_pair");
+    if (mode == 1) {
+        const int nx = static_cast<int>(d->reg_nx), ny = static_cast<int>(d->reg_ny), nxp = nxp_of(nx);
+        float4* cLN = reinterpret_cast<float4*>(coef_pair);
+        float2* cH = reinterpret_cast<float2*>(coef_pair + 4 * d->nelem);
+        k_pair_coef<<<grid_for(static_cast<int64_t>(ny) * nxp), kBlock, 0, s>>>(d->K, d->G, nx, ny, nxp, g * g, cLN,
+                                                                              cH);
+        return check_launch("verlet_precompute_pair");
+    }
+    if (mode == 2)
+        k_pair_coef_elem<<<grid_for(d->nelem), kBlock, 0, s>>>(d->K, d->G, d->nelem, g * g,
+                                                               reinterpret_cast<float4*>(coef_pair),
+                                                               reinterpret_cast<float2*>(coef_pair + 4 * d->nelem));
+    else
+        k_pair_stiffness<<<grid_for(d->nelem, 128), 128, 0, s>>>(d->dNx, d->vol, d->K, d->G, d->nelem, d->nip,
+                                                                 reinterpret_cast<float2*>(coef_pair));
+    GF_TRY(check_launch("verlet_precompute_pair"));
+    if (!pair_has_classes(d) && d->nnu > 0) {
+        GF_REQUIRE(d->inv, "null inverse mass");
+        const int64_t ncoef = (mode == 2 ? 6 : 72) * d->nelem;
+        k_pair_split<<<grid_for(d->nnu), kBlock, 0, s>>>(d->inv, d->nnu, reinterpret_cast<float2*>(coef_pair + ncoef));
+        GF_TRY(check_launch("verlet_precompute_pair (inverse mass)"));
+    }
+    return GFGPU_OK;
 }
 
 int gfgpu_verlet_pair_status(void)

@@ -67,11 +67,12 @@ class VelocityVerlet:
     iip : prescribed (fixed) dofs, or None
     fext : external force nodevec, or None
     uniform : "auto" (detect congruent axis-aligned elements), True or False
-    arithmetic : "fp64" (default: FP64 kernels) or "pair": on a Mesh::Quad4::Regular mesh of
-        square elements with lumped-mass classes, the increments run in float-float arithmetic
-        (two FP32 numbers per value, ~48-bit significands) in one fused kernel per increment
-        (gfgpu_verlet_precompute_pair); agreement with the FP64 path ~1e-14 per increment. Other
-        meshes raise with "pair".
+    arithmetic : "fp64" (default: FP64 kernels) or "pair": the increments run in float-float
+        arithmetic (two FP32 numbers per value, ~48-bit significands; gfgpu_verlet_precompute_pair):
+        one fused kernel per increment on a Mesh::Quad4::Regular mesh of square elements with
+        lumped-mass classes, an element kernel (square closed form or stored element stiffness)
+        and a dof-CSR node kernel on any other Quad4 mesh; agreement with the FP64 path ~1e-14 per
+        increment. Hex8 meshes raise with "pair".
     """
 
     def __init__(self, coor, conn, dofs, K, G, rho=1.0, dt=None, eta=0.0, iip=None, fext=None,
@@ -163,15 +164,15 @@ class VelocityVerlet:
                               dtype=torch.float64, device=_dev.device())
 
     def use_pair(self):
-        """Float-float increments (gfgpu_verlet_precompute_pair); raises GFGPUError
-        (GFGPU_ERR_UNSUPPORTED) when the mesh is not a Regular square-element Quad4 mesh with
-        lumped-mass classes."""
-        if self.coef_pair is None:
-            n = int(_lib.lib().gfgpu_verlet_pair_coef_floats(C.addressof(self.desc)))
-            cp = torch.empty(max(n, 4), dtype=torch.float32, device=_dev.device())
-            _lib.call("gfgpu_verlet_precompute_pair", C.addressof(self.desc), cp.data_ptr(),
-                      _dev.stream())
-            self.coef_pair = cp
+        """Float-float increments (gfgpu_verlet_precompute_pair, for the descriptor as it is now:
+        Regular square-element tile kernel, square closed form + CSR, or element stiffness + CSR);
+        raises GFGPUError (GFGPU_ERR_UNSUPPORTED) for Hex8 meshes."""
+        self.desc.coef_pair = None
+        n = int(_lib.lib().gfgpu_verlet_pair_coef_floats(C.addressof(self.desc)))
+        cp = torch.empty(max(n, 4), dtype=torch.float32, device=_dev.device())
+        _lib.call("gfgpu_verlet_precompute_pair", C.addressof(self.desc), cp.data_ptr(),
+                  _dev.stream())
+        self.coef_pair = cp
         self.desc.coef_pair = self.coef_pair.data_ptr()
         if hasattr(self, "ws"):
             self._alloc_ws()
@@ -231,9 +232,9 @@ class VelocityVerlet:
     @property
     def path(self):
         if not self.desc.uniform:
-            return "general"
+            return "general-pair" if self.desc.coef_pair else "general"
         if self.desc.coef_pair:
-            return "uniform-square-pair"
+            return {1: "uniform-square-pair", 2: "uniform-square-pair-csr"}.get(self.desc.pair_mode, "general-pair")
         if self.desc.coef:
             return "uniform-square" if self.desc.nne == 4 else "uniform-cube"
         return "uniform"

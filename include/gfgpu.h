@@ -364,8 +364,12 @@ typedef struct {
     /* optional float-float ("pair") coefficients of a uniform square Quad4 mesh with the
      * Regular numbering and lumped-mass classes (gfgpu_verlet_precompute_pair): when set,
      * gfgpu_verlet_step in fast mode runs its increments in pair arithmetic (two FP32 numbers per
-     * value, ~48-bit significands) in one fused kernel per increment; NULL = FP64 kernels. */
+     * value, ~48-bit significands); NULL = FP64 kernels. */
     const float* coef_pair;
+    /* which pair path coef_pair belongs to (set by gfgpu_verlet_precompute_pair): 1 = the Regular
+     * square-element fused tile kernel, 2 = element kernel + dof-CSR node kernel with the square
+     * closed form, 3 = the same with stored element stiffness matrices */
+    int32_t pair_mode;
 } gfgpu_verlet_desc;
 
 #define GFGPU_MASS_CLASSES 16
@@ -388,22 +392,28 @@ int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
  * constant, linear and trilinear modes). Set d->coef = coef to use them. Returns
  * GFGPU_ERR_UNSUPPORTED for other meshes. */
 int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stream_t stream);
-/* Floats of the pair coefficients of a Regular(nx, ny) mesh: 4 nx ny + 2 nxp ny, nxp = nx rounded
- * up to even (0 for other descriptors). */
+/* Floats of the pair coefficients gfgpu_verlet_precompute_pair writes for this descriptor (0 if no
+ * pair path applies). */
 int64_t gfgpu_verlet_pair_coef_floats(const gfgpu_verlet_desc* d);
-/* Pair-arithmetic coefficients of a uniform square Quad4 mesh (same closed form as
- * gfgpu_verlet_precompute): coef_pair (gfgpu_verlet_pair_coef_floats floats) holds
- * {L.h, L.l, N.h, N.l} per element in element order (16-byte aligned), then {kH.h, kH.l} per
- * element in rows of nxp pairs (element (ex, ey) at ey * nxp + ex, the pad pair zero), with
- * L = lam/4, N = G/4, kH = g^2 (lam + 3G)/4 split into high and low FP32 parts. Requires d->uniform with hx = hy, the Regular numbering
- * (gfgpu_verlet_detect_regular) and mass classes (gfgpu_verlet_classify), else returns
- * GFGPU_ERR_UNSUPPORTED. Set d->coef_pair = coef_pair to run gfgpu_verlet_step on pairs: one
- * fused kernel per increment (displacement tile + halo in shared memory, element terms of the
- * tile's elements, four-element gather, velocity estimates, predictor); u, v, a are converted to
- * pairs at the start of the call and back at its end; each increment agrees with the FP64 kernels
- * to ~1e-14 relative (48-bit significands, FP32 exponent range: |values| between ~1e-30 and
- * ~1e38). Strict mode ignores coef_pair. */
-int gfgpu_verlet_precompute_pair(const gfgpu_verlet_desc* d, float* coef_pair, gfgpu_stream_t stream);
+/* Float-float ("pair") arithmetic for the increments of a Quad4 mesh: values are unevaluated sums
+ * of two FP32 numbers (~48-bit significands, |values| within ~1e-30 .. 1e38), computed on the
+ * FP32 pipes; each increment agrees with the FP64 kernels to ~1e-14 relative. Writes coef_pair
+ * (gfgpu_verlet_pair_coef_floats floats, 16-byte aligned) and sets d->pair_mode; then
+ * d->coef_pair = coef_pair makes gfgpu_verlet_step (fast mode) run on pairs. u, v, a are converted
+ * to pairs at the start of a call (after the FP64 predictor) and back at its end. The path:
+ *  1 = uniform square elements with the Regular numbering (gfgpu_verlet_detect_regular) and
+ *      lumped-mass classes (gfgpu_verlet_classify): one fused tile kernel per increment.
+ *      coef_pair: {L.h, L.l, N.h, N.l} per element (element order), then {kH.h, kH.l} in rows of
+ *      nxp pairs (element (ex, ey) at ey * nxp + ex, nxp = nx rounded up to even, pad pairs 0),
+ *      L = lam/4, N = G/4, kH = g^2 (lam + 3G)/4 split into high and low FP32 parts;
+ *  2 = uniform square elements, any numbering (periodic ties allowed): element kernel (square
+ *      closed form) + dof-CSR node kernel per increment; coef_pair: {L, N} per element, then kH
+ *      per element;
+ *  3 = any Quad4 mesh with the Gauss rule (d->dNx, d->vol): the element stiffness matrices
+ *      (36 pairs per element, [36][nelem]) times u_e + the dof-CSR node kernel.
+ * In paths 2 and 3 without mass classes the pair inverse masses [nnu] follow. Other meshes return
+ * GFGPU_ERR_UNSUPPORTED. Strict mode ignores coef_pair. */
+int gfgpu_verlet_precompute_pair(gfgpu_verlet_desc* d, float* coef_pair, gfgpu_stream_t stream);
 /* The pair path of gfgpu_verlet_step in three parts, for callers that act between increments
  * (the row-block partition's halo exchange, goosefem_gb300/partition.py). The state lives in
  * `workspace` (gfgpu_verlet_workspace_bytes with d->coef_pair set). Increments are numbered from 0

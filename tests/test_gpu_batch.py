@@ -56,6 +56,25 @@ def test_batched_equals_instances_alone(gf, batch, mode, block, bps):
         assert rel_err(us, ur) <= RTOL and rel_err(vs, vr) <= RTOL and rel_err(as_, ar) <= RTOL
 
 
+def test_batched_pair_equals_instances_alone_in_pairs(gf, batch):
+    """The pair schedule (mode 2) of the concatenated batch gives each instance the bits of its
+    own pair run alone (same element terms, same CSR order, same mass-class values)."""
+    B, inst, bv = batch
+    bv.mode = 2
+    u, v, a = bv.state()
+    bv.run_direct(u, v, a, 60)
+    torch.cuda.synchronize()
+    for k, (us, vs, as_) in enumerate(zip(_split(bv, u), _split(bv, v), _split(bv, a))):
+        m = inst[k].mesh
+        vv = gf.VelocityVerlet(m.coor(), m.conn(), m.dofsPeriodic(), inst[k].K, inst[k].G, dt=bv.dt, eta=0.1,
+                               arithmetic="pair")
+        ua = torch.tensor(inst[k].initial_displacement(), device="cuda")
+        va, aa = torch.zeros_like(ua), torch.zeros_like(ua)
+        vv.step(ua, va, aa, 60)
+        assert np.array_equal(us, to_np(ua)) and np.array_equal(vs, to_np(va)) and np.array_equal(as_, to_np(aa))
+    bv.mode = 0
+
+
 def test_batched_matches_oracle(gf, oracle, batch):
     """One instance of the batch against the oracle's loop (periodic dofs, applied shear)."""
     B, inst, bv = batch
@@ -83,7 +102,7 @@ def test_batched_matches_oracle(gf, oracle, batch):
     assert rel_err(_split(bv, a)[k], ar) <= RTOL
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_graph_replay_equals_direct(gf, batch, mode):
     B, inst, bv = batch
     bv.mode, bv.block, bv.bps = mode, 256, 0

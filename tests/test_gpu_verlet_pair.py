@@ -111,22 +111,53 @@ def test_pair_repeatable_and_exactly_linear(gf, oracle, kernel):
         assert torch.equal(z, x)
 
 
-def test_pair_refuses_other_meshes(gf, oracle):
-    # periodic dofs: not the Regular numbering
-    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 16, 16, True, False, 51)
-    with pytest.raises(gf.GFGPUError) as ei:
-        gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, arithmetic="pair")
-    assert ei.value.code == -7
-    # rectangles (hx != hy)
-    m2 = gf.Mesh.Quad4.Regular(10, 8)
-    with pytest.raises(gf.GFGPUError):
-        gf.VelocityVerlet(m2.coor() * np.array([0.7, 1.3]), m2.conn(), m2.dofs(), K[:80], G[:80],
-                          dt=0.01, arithmetic="pair")
-    # Hex8
+@pytest.mark.parametrize("case", ["periodic", "periodic-per-dof", "distorted", "rectangles"])
+def test_pair_csr_paths(gf, oracle, case):
+    """Quad4 meshes outside the Regular square-element case: periodic ties (square closed form +
+    dof-CSR node kernel, pair path 2), distorted and rectangular elements (stored element
+    stiffness, pair path 3), and the node update with per-dof inverse masses (no mass classes)."""
+    R = oracle
+    periodic = case.startswith("periodic")
+    mesh, coor, conn, dofs, K, G, iip, v0, dt, ref = _setup(gf, oracle, 30, 22, periodic, not periodic, 51)
+    if not periodic:
+        coor = coor * np.array([0.7, 1.3]) if case == "rectangles" else coor + seeded_field(coor.shape, 52, amp=0.08)
+        xr = R.as_element(conn, coor)
+        ref["dNx"], ref["vol"] = R.compute_dN(xr, *R.quad4_gauss())
+        xin, win = R.quad4_nodal()
+        _, voln = R.compute_dN(xr, xin, win)
+        Nn, _ = R.shape(xin)
+        ref["A"] = R.diag_assemble(conn, dofs, R.int_n_scalar_nt_dv(Nn, voln, np.ones((mesh.nelem(), 4)), 2))
+        dt = 0.05 * gf.critical_dt(K, G) * 0.7
+    vv = gf.VelocityVerlet(coor, conn, dofs, K, G, dt=dt, eta=0.1, iip=iip)
+    if case == "periodic-per-dof":
+        vv.use_per_dof_mass()
+    if periodic:  # uniform density: one mass class, unless the per-dof update is asked for
+        assert (vv.desc.ncls > 0) == (case == "periodic")
+    vv.use_pair()
+    assert vv.path == ("uniform-square-pair-csr" if periodic else "general-pair"), vv.path
+    s = _state(v0)
+    vv.step(*s, 60)
+    ur, vr, ar = _run_oracle(oracle, ref, v0, dt, 0.1, 60)
+    for g, r in zip(s, (ur, vr, ar)):
+        assert rel_err(to_np(g), r) <= RTOL
+    # the same against the FP64 kernels, and repeatable
+    vv.use_fp64()
+    s64 = _state(v0)
+    vv.step(*s64, 60)
+    vv.use_pair()
+    s2 = _state(v0)
+    vv.step(*s2, 60)
+    for g, r, h in zip(s, s64, s2):
+        assert rel_err(to_np(g), to_np(r)) <= RTOL
+        assert torch.equal(g, h)
+
+
+def test_pair_refuses_hex8(gf):
     m3 = gf.Mesh.Hex8.Regular(3, 3, 3)
-    with pytest.raises(gf.GFGPUError):
-        gf.VelocityVerlet(m3.coor(), m3.conn(), m3.dofs(), K[:27], G[:27], dt=0.01,
-                          arithmetic="pair")
+    K = np.ones(27)
+    with pytest.raises(gf.GFGPUError) as ei:
+        gf.VelocityVerlet(m3.coor(), m3.conn(), m3.dofs(), K, 0.5 * K, dt=0.01, arithmetic="pair")
+    assert ei.value.code == -7
 
 
 def test_pair_ignored_in_strict_mode(gf, oracle):
