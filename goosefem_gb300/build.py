@@ -49,14 +49,18 @@ def build(force=False, verbose=False, extra_flags=()):
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ, src + ".o")
         objs.append(o)
-        if force or _stale(o, [s] + headers):
-            cmd = [nvcc()] + NVCC_FLAGS + list(extra_flags) + ["-c", s, "-o", o]
+        cmd = [nvcc()] + NVCC_FLAGS + list(extra_flags) + ["-c", s, "-o", o]
+        stamp = o + ".cmd"  # the command an object was built with: a flag change rebuilds it
+        same_cmd = os.path.exists(stamp) and open(stamp).read() == " ".join(cmd)
+        if force or not same_cmd or _stale(o, [s] + headers):
             if verbose:
                 print(" ".join(cmd), flush=True)
-            procs.append((cmd, subprocess.Popen(cmd)))
-    for cmd, p in procs:
+            procs.append((cmd, stamp, subprocess.Popen(cmd)))
+    for cmd, stamp, p in procs:
         if p.wait() != 0:
             raise RuntimeError("nvcc failed: " + " ".join(cmd))
+        with open(stamp, "w") as f:
+            f.write(" ".join(cmd))
     if force or procs or _stale(LIB, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs
         if verbose:

@@ -20,7 +20,7 @@ int check_launch(const char* what);
 bool strict_mode();
 int variant_elem();
 int variant_node();
-int pair_kernel();    // float-float explicit increment: 0 / 2 = persistent TMA pipeline (31 x 7 / 31 x 15 tiles), 1 = one tile per CTA
+int pair_kernel();    // float-float explicit increment: 2 (default) / 0 = persistent TMA pipeline (31 x 15 / 31 x 7 tiles), 1 = one tile per CTA
 int nn_tensor_path(); // 32 -> 32 network layers: 0 = mma.sync, 1 = tcgen05, 2 = tcgen05 + TMA pipeline
 
 inline cudaStream_t S(gfgpu_stream_t s)

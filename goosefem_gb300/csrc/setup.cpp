@@ -17,7 +17,7 @@ static int g_strict = 0;
 static int g_variant_elem = 0;
 static int g_variant_node = 0;
 static int g_nn_path = 2; // tcgen05 + TMA (the fastest form on GB300)
-static int g_pair_kernel = 0; // persistent TMA pipeline
+static int g_pair_kernel = 2; // persistent TMA pipeline, 31 x 15 node tiles
 
 int pair_kernel()
 {

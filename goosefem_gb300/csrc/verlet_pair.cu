@@ -27,6 +27,7 @@
 
 #include "common.cuh"
 #include "ffpair.cuh"
+#include "ffpair2.cuh"
 
 namespace gfgpu {
 
@@ -55,27 +56,31 @@ struct PairStep {
     float2 dt, cc;       // dt and dt^2 / 2 as pairs
 };
 
+// Two pair values in a float4. Interleaved {x.h, x.l, y.h, y.l} (lo2, hi2, pack): the element
+// forces and the state of pair paths 2 and 3. Packed {x.h, y.h, x.l, y.l} (px_, py_, ppack): the
+// state and the {L, N} coefficients of pair path 1, so that a float4 is directly the two
+// FP32x2 registers {h, l} of an ff2 (ffpair2.cuh).
 __device__ __forceinline__ ffv lo2(float4 q) { return ff_make(q.x, q.y); }
 __device__ __forceinline__ ffv hi2(float4 q) { return ff_make(q.z, q.w); }
 __device__ __forceinline__ ffv pf(float2 q) { return ff_make(q.x, q.y); }
 __device__ __forceinline__ float4 pack(ffv x, ffv y) { return make_float4(x.h, x.l, y.h, y.l); }
+__device__ __forceinline__ ffv px_(float4 q) { return ff_make(q.x, q.z); }
+__device__ __forceinline__ ffv py_(float4 q) { return ff_make(q.y, q.w); }
+__device__ __forceinline__ float4 ppack(ffv x, ffv y) { return make_float4(x.h, y.h, x.l, y.l); }
 
 // element (ex, ey) of a square-element Regular mesh with per-element L = lam/4, N = G/4 (M = 2N)
 // and kH = g^2 (lam + 3G)/4: the sums S = P0 + P1, D = P0 - P1 (x) and P1 + Q1, P1 - Q1 (y) and
 // the hourglass terms H, from which the element forces are (H - S, D - H, S + H, -(D + H)) at
 // nodes 0..3 (k_elem_force_quad4_square's formulas, every sum and product on pairs)
-__device__ __forceinline__ void pair_element(float4 q0, float4 q1, float4 q2, float4 q3, float4 cln,
-                                             float2 ch, float4& S, float4& D, float4& H)
+__device__ __forceinline__ void pair_element(ffv u0x, ffv u0y, ffv u1x, ffv u1y, ffv u2x, ffv u2y, ffv u3x,
+                                             ffv u3y, ffv L, ffv N, ffv kH, float4& S, float4& D, float4& H)
 {
-    const ffv u0x = lo2(q0), u0y = hi2(q0), u1x = lo2(q1), u1y = hi2(q1);
-    const ffv u2x = lo2(q2), u2y = hi2(q2), u3x = lo2(q3), u3y = hi2(q3);
     const ffv px = ff_sub(u2x, u0x), qx = ff_sub(u1x, u3x);
     const ffv py = ff_sub(u2y, u0y), qy = ff_sub(u1y, u3y);
     const ffv A1x = ff_add(px, qx), A2x = ff_sub(px, qx);
     const ffv A1y = ff_add(py, qy), A2y = ff_sub(py, qy);
     const ffv A3x = ff_sub(ff_add(u0x, u2x), ff_add(u1x, u3x));
     const ffv A3y = ff_sub(ff_add(u0y, u2y), ff_add(u1y, u3y));
-    const ffv L = lo2(cln), N = hi2(cln), kH = pf(ch);
     const ffv Lt = ff_mul(L, ff_add(A1x, A2y));
     const ffv P0 = ff_add(ff_twice(ff_mul(N, A1x)), Lt);
     const ffv Q1 = ff_add(ff_twice(ff_mul(N, A2y)), Lt);
@@ -155,8 +160,10 @@ k_verlet_pair_quad4(const PairStep p, const __grid_constant__ PairClassTab tab)
         if (ex >= 0 && ex < nx && ey >= 0 && ey < ny) {
             const int e = ey * nx + ex;
             const int b = ly * UW + lx; // node (ex, ey) in the tile
-            pair_element(su[b], su[b + 1], su[b + UW + 1], su[b + UW], __ldg(p.cLN + e),
-                         __ldg(p.cH + ey * p.nxp + ex), S, D, H);
+            const float4 q0 = su[b], q1 = su[b + 1], q2 = su[b + UW + 1], q3 = su[b + UW];
+            const float4 cln = __ldg(p.cLN + e);
+            pair_element(px_(q0), py_(q0), px_(q1), py_(q1), px_(q2), py_(q2), px_(q3), py_(q3), px_(cln),
+                         py_(cln), pf(__ldg(p.cH + ey * p.nxp + ex)), S, D, H);
         }
         sS[k] = S;
         sD[k] = D;
@@ -177,16 +184,16 @@ k_verlet_pair_quad4(const PairStep p, const __grid_constant__ PairClassTab tab)
     const ffv dt = pf(p.dt);
     const bool hf = p.fext != nullptr;
     ffv vx, ax, vy, ay;
-    pair_update(cl.x, fxn, lo2(fq), hf, lo2(vq), lo2(aq), smi, sbe, sc1, sc2, sc3, dt, vx, ax);
-    pair_update(cl.y, fyn, hi2(fq), hf, hi2(vq), hi2(aq), smi, sbe, sc1, sc2, sc3, dt, vy, ay);
-    p.v[node] = pack(vx, vy);
-    p.a[node] = pack(ax, ay);
+    pair_update(cl.x, fxn, px_(fq), hf, px_(vq), px_(aq), smi, sbe, sc1, sc2, sc3, dt, vx, ax);
+    pair_update(cl.y, fyn, py_(fq), hf, py_(vq), py_(aq), smi, sbe, sc1, sc2, sc3, dt, vy, ay);
+    p.v[node] = ppack(vx, vy);
+    p.a[node] = ppack(ax, ay);
     if (p.advance) {
         const float4 uq = su[(ty + 1) * UW + tx + 1];
         const ffv cc = pf(p.cc);
-        const ffv ux = ff_norm(ff_add(ff_add(lo2(uq), ff_mul(dt, vx)), ff_mul(cc, ax)));
-        const ffv uy = ff_norm(ff_add(ff_add(hi2(uq), ff_mul(dt, vy)), ff_mul(cc, ay)));
-        p.uout[node] = pack(ux, uy);
+        const ffv ux = ff_norm(ff_add(ff_add(px_(uq), ff_mul(dt, vx)), ff_mul(cc, ax)));
+        const ffv uy = ff_norm(ff_add(ff_add(py_(uq), ff_mul(dt, vy)), ff_mul(cc, ay)));
+        p.uout[node] = ppack(ux, uy);
     }
 }
 
@@ -200,9 +207,13 @@ k_verlet_pair_quad4(const PairStep p, const __grid_constant__ PairClassTab tab)
 //    into the other of two shared-memory stages while the current tile is computed. Outside the
 //    mesh the copies read zeros, so elements beyond the edges have zero coefficients and
 //    contribute nothing: the element phase needs no bounds checks.
-//  * a tile is 31 x 7 nodes with the 32 x 8 elements around them: the element phase is one
-//    element per thread (lane = element column, warp = element row), and in the node phase warp
-//    w, lane j owns node (x0 + j, y0 + w) (lane 31 and warp 7 only help with the columns).
+//  * a tile is 31 x TY nodes (TY = 15 by default, or 7) with the 32 x (TY + 1) elements around
+//    them: the element phase is one element per thread (lane = element column, warp = element
+//    row), and in the node phase warp w, lane j owns node (x0 + j, y0 + w) (lane 31 and the last
+//    warp only help with the columns).
+//  * the x and y components of a node (and the two components of every element term) travel
+//    together as the two lanes of packed FP32x2 float-float values (ffpair2.cuh): the state and
+//    the {L, N} coefficients are stored {x.h, y.h, x.l, y.l}, so a 16-byte load is one ff2.
 //  * the element phase stores only the element terms P0, P1 (= Q0), Q1, H0, H1; the node phase
 //    forms, per column of elements below/above a node row, with A = P0_lo + P0_hi,
 //    B = P1_lo - P1_hi, C = H0_lo - H0_hi (x; y with P1, Q1, H1):
@@ -229,7 +240,7 @@ struct TmaGeom {
     // stage layout: u | v | a | cLN | cH, each 128-byte aligned
     static constexpr uint32_t OffV = pad(UBytes), OffA = OffV + pad(VBytes), OffL = OffA + pad(VBytes),
                               OffH = OffL + pad(LBytes), StageBytes = OffH + pad(HBytes);
-    static constexpr uint32_t ElemBytes = threads * (16 + 16 + 8); // {P0, P1}, {Q1, H0}, {H1}
+    static constexpr uint32_t ElemBytes = threads * 48; // (P0, P1), (P1, Q1), (H0, H1) as ff2
     static constexpr uint32_t Smem = 128 + 2 * StageBytes + pad(ElemBytes) + 64;
     static constexpr int min_blocks = threads <= 256 ? 4 : 2;
 };
@@ -246,6 +257,7 @@ struct PairTmaStep {
     int gdx, gdy;        // gridDim.x = gdy ntx + gdx: the tile step in tile columns and rows
     int advance;
     float2 dt, cc;
+    unsigned long long nz; // kF2NegZero (the addend of the packed products, read at run time)
 };
 
 __device__ __forceinline__ bool pair_wait(uint32_t mbar, uint32_t phase)
@@ -305,20 +317,23 @@ k_verlet_pair_tma(const __grid_constant__ CUtensorMap mu, const __grid_constant_
     extern __shared__ unsigned char pair_smem[];
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(pair_smem) + 127) & ~uintptr_t(127));
     unsigned char* elem = base + 2 * kStageBytes;
-    float4* sPP = reinterpret_cast<float4*>(elem);
-    float4* sQH = sPP + kTmaThreads;
-    float2* sH1 = reinterpret_cast<float2*>(sQH + kTmaThreads);
+    // element terms (two pair lanes each): (P0, P1), (P1, Q1), (H0, H1)
+    ulonglong2* sPP = reinterpret_cast<ulonglong2*>(elem);
+    ulonglong2* sPQ = sPP + kTmaThreads;
+    ulonglong2* sHH = sPQ + kTmaThreads;
     uint64_t* bars = reinterpret_cast<uint64_t*>(elem + Gm::pad(Gm::ElemBytes));
-    __shared__ float2 smi[GFGPU_MASS_CLASSES], sbe[GFGPU_MASS_CLASSES], sc1[GFGPU_MASS_CLASSES],
-        sc2[GFGPU_MASS_CLASSES], sc3[GFGPU_MASS_CLASSES];
+    // class coefficients as separate high / low floats: the two lanes' coefficients of an ff2 are
+    // then two plain loads into the two halves of its registers
+    __shared__ float scf[10][GFGPU_MASS_CLASSES]; // mi, be, c1, c2, c3: high parts, then low parts
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t s_bar = static_cast<uint32_t>(__cvta_generic_to_shared(bars));
     if (tid < GFGPU_MASS_CLASSES) {
-        smi[tid] = tab.mi[tid];
-        sbe[tid] = tab.be[tid];
-        sc1[tid] = tab.c1[tid];
-        sc2[tid] = tab.c2[tid];
-        sc3[tid] = tab.c3[tid];
+        const float2 cf[5] = {tab.mi[tid], tab.be[tid], tab.c1[tid], tab.c2[tid], tab.c3[tid]};
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            scf[k][tid] = cf[k].x;
+            scf[5 + k][tid] = cf[k].y;
+        }
     }
     auto issue = [&](int tile, int st) {
         const int x0 = (tile % p.ntx) * kTmaTX, y0 = (tile / p.ntx) * kTmaTY;
@@ -345,6 +360,8 @@ k_verlet_pair_tma(const __grid_constant__ CUtensorMap mu, const __grid_constant_
     }
     const int nx = p.nx, ny = p.ny, W = nx + 1;
     const ffv dt = pf(p.dt), cc = pf(p.cc);
+    const ff2 DT = ff2_bcast(dt), CC = ff2_bcast(cc);
+    const f2 NZ = p.nz;
     const bool hf = p.fext != nullptr;
     // element phase: this thread's element (x0 - 1 + lane, y0 - 1 + warp); its nodes in the tile
     const int b0 = warp * kTmaUW + lane;
@@ -373,29 +390,35 @@ k_verlet_pair_tma(const __grid_constant__ CUtensorMap mu, const __grid_constant_
         }
         const bool ok = pair_wait(s_bar + 8u * st, (i >> 1) & 1);
         const unsigned char* sg = base + st * kStageBytes;
-        const float4* su = reinterpret_cast<const float4*>(sg);
+        const ulonglong2* su = reinterpret_cast<const ulonglong2*>(sg);
+        auto ldu = [&](int k) {
+            const ulonglong2 q = su[k];
+            return ff2_make(q.x, q.y);
+        };
         if (ok) {
-            const float4 q0 = su[b0], q1 = su[b0 + 1], q2 = su[b0 + kTmaUW + 1], q3 = su[b0 + kTmaUW];
-            const ffv u0x = lo2(q0), u0y = hi2(q0), u1x = lo2(q1), u1y = hi2(q1);
-            const ffv u2x = lo2(q2), u2y = hi2(q2), u3x = lo2(q3), u3y = hi2(q3);
-            const ffv px = ff_sub(u2x, u0x), qx = ff_sub(u1x, u3x);
-            const ffv py = ff_sub(u2y, u0y), qy = ff_sub(u1y, u3y);
-            const ffv A1x = ff_add(px, qx), A2x = ff_sub(px, qx);
-            const ffv A1y = ff_add(py, qy), A2y = ff_sub(py, qy);
-            const ffv A3x = ff_sub(ff_add(u0x, u2x), ff_add(u1x, u3x));
-            const ffv A3y = ff_sub(ff_add(u0y, u2y), ff_add(u1y, u3y));
-            const float4 cln = reinterpret_cast<const float4*>(sg + kOffL)[tid];
+            // both components at once (ff2 lanes x, y)
+            const ff2 U0 = ldu(b0), U1 = ldu(b0 + 1), U2 = ldu(b0 + kTmaUW + 1), U3 = ldu(b0 + kTmaUW);
+            const ff2 P = ff2_sub(U2, U0), Q = ff2_sub(U1, U3);
+            const ff2 A1 = ff2_add(P, Q), A2 = ff2_sub(P, Q);
+            const ff2 A3 = ff2_sub(ff2_add(U0, U2), ff2_add(U1, U3));
+            // (t, s) = (A1x + A2y, A1y + A2x); (Lt, P1) = (L t, N s)
+            const ff2 A2s = ff2_make(f2_make(f2_hi(A2.h), f2_lo(A2.h)), f2_make(f2_hi(A2.l), f2_lo(A2.l)));
+            const ff2 ts = ff2_add(A1, A2s);
+            const ulonglong2 cq = reinterpret_cast<const ulonglong2*>(sg + kOffL)[tid]; // {L, N} packed
+            const ff2 LN = ff2_make(cq.x, cq.y);
+            const ff2 LtP1 = ff2_mul(LN, ts, NZ);
+            // (P0, Q1) = M (A1x, A2y) + (Lt, Lt), M = 2N
+            const ffv N = ff2_lane1(LN), Lt = ff2_lane0(LtP1);
+            const ff2 M2 = ff2_bcast(ff_twice(N));
+            const ff2 dg = ff2_make(f2_make(f2_lo(A1.h), f2_hi(A2.h)), f2_make(f2_lo(A1.l), f2_hi(A2.l)));
+            const ff2 PQ = ff2_add(ff2_mul(M2, dg, NZ), ff2_bcast(Lt));
             const int kr = (2 * (x0 - 1) - kh_start(x0)) >> 1; // 0 or 1 pairs into the box row
             const ffv kH = pf(reinterpret_cast<const float2*>(sg + kOffH)[warp * (kTmaHW / 2) + kr + lane]);
-            const ffv L = lo2(cln), N = hi2(cln), M = ff_twice(N);
-            const ffv Lt = ff_mul(L, ff_add(A1x, A2y));
-            const ffv P0 = ff_add(ff_mul(M, A1x), Lt);
-            const ffv Q1 = ff_add(ff_mul(M, A2y), Lt);
-            const ffv P1 = ff_mul(N, ff_add(A1y, A2x));
-            sPP[tid] = pack(P0, P1);
-            sQH[tid] = pack(Q1, ff_mul(kH, A3x));
-            const ffv H1 = ff_mul(kH, A3y);
-            sH1[tid] = make_float2(H1.h, H1.l);
+            const ff2 H = ff2_mul(ff2_bcast(kH), A3, NZ); // (H0, H1)
+            // element terms (P0, P1), (P1, Q1), (H0, H1)
+            sPP[tid] = make_ulonglong2(f2_make(f2_lo(PQ.h), f2_hi(LtP1.h)), f2_make(f2_lo(PQ.l), f2_hi(LtP1.l)));
+            sPQ[tid] = make_ulonglong2(f2_make(f2_hi(LtP1.h), f2_hi(PQ.h)), f2_make(f2_hi(LtP1.l), f2_hi(PQ.l)));
+            sHH[tid] = make_ulonglong2(H.h, H.l);
         }
         // the element terms are complete; a CTA whose copies did not arrive stops here
         if (__syncthreads_or(!ok)) {
@@ -409,30 +432,67 @@ k_verlet_pair_tma(const __grid_constant__ CUtensorMap mu, const __grid_constant_
         }
         if (warp >= kTmaTY) continue; // the last element row only feeds the node rows below it
         // node phase: the element column left of node (x0 + lane, y0 + warp): lo = element row
-        // warp (below the node row), hi = warp + 1
+        // warp (below the node row), hi = warp + 1; lane x: A = P0lo + P0hi, B = P1lo - P1hi,
+        // C = H0lo - H0hi; lane y: A = P1lo + P1hi, B = Q1lo - Q1hi, C = H1lo - H1hi
         const int kl = tid, kh = tid + kTmaEW;
-        const float4 ppl = sPP[kl], qhl = sQH[kl], pph = sPP[kh], qhh = sQH[kh];
-        const float2 h1l = sH1[kl], h1h = sH1[kh];
-        const ffv Ex = ff_add(ff_add(lo2(ppl), lo2(pph)), ff_sub(hi2(qhl), hi2(qhh)));
-        const ffv Bx = ff_sub(hi2(ppl), hi2(pph));
-        const ffv Ey = ff_add(ff_add(hi2(ppl), hi2(pph)), ff_sub(pf(h1l), pf(h1h)));
-        const ffv By = ff_sub(lo2(qhl), lo2(qhh));
-        const ffv Qrx = shfl_down1(ff_sub(Ex, Bx)), Qry = shfl_down1(ff_sub(Ey, By));
+        auto lde = [](const ulonglong2* t, int k) {
+            const ulonglong2 q = t[k];
+            return ff2_make(q.x, q.y);
+        };
+        const ff2 Ac = ff2_add(lde(sPP, kl), lde(sPP, kh));
+        const ff2 Bc = ff2_sub(lde(sPQ, kl), lde(sPQ, kh));
+        const ff2 Ec = ff2_add(Ac, ff2_sub(lde(sHH, kl), lde(sHH, kh)));
+        const ff2 Qc = ff2_sub(Ec, Bc);
+        const ff2 Qr = ff2_make(__shfl_down_sync(0xffffffffu, Qc.h, 1), __shfl_down_sync(0xffffffffu, Qc.l, 1));
         if (!own) continue;
-        const ffv fxn = ff_sub(ff_add(Ex, Bx), Qrx), fyn = ff_sub(ff_add(Ey, By), Qry);
+        const ff2 F = ff2_sub(ff2_add(Ec, Bc), Qr); // (f_x, f_y)
         const int ln = warp * kTmaTX + lane;
-        const float4 vq = reinterpret_cast<const float4*>(sg + kOffV)[ln];
-        const float4 aq = reinterpret_cast<const float4*>(sg + kOffA)[ln];
-        ffv vx, ax, vy, ay;
-        pair_update(cl.x, fxn, lo2(fq), hf, lo2(vq), lo2(aq), smi, sbe, sc1, sc2, sc3, dt, vx, ax);
-        pair_update(cl.y, fyn, hi2(fq), hf, hi2(vq), hi2(aq), smi, sbe, sc1, sc2, sc3, dt, vy, ay);
-        p.v[node] = pack(vx, vy);
-        p.a[node] = pack(ax, ay);
+        const ulonglong2 vq = reinterpret_cast<const ulonglong2*>(sg + kOffV)[ln];
+        const ulonglong2 aq = reinterpret_cast<const ulonglong2*>(sg + kOffA)[ln];
+        const ff2 VN = ff2_make(vq.x, vq.y), AN = ff2_make(aq.x, aq.y);
+        const ff2 FX = ff2_make(f2_make(fq.x, fq.y), f2_make(fq.z, fq.w));
+        ff2 VV, AA;
+        if (cl.x < GFGPU_MASS_CLASSES && cl.y < GFGPU_MASS_CLASSES) {
+            const int cx = cl.x, cy = cl.y;
+            auto coef = [&](int k) {
+                return ff2_make(f2_make(scf[k][cx], scf[k][cy]), f2_make(scf[5 + k][cx], scf[5 + k][cy]));
+            };
+            const ff2 R = hf ? ff2_sub(FX, F) : ff2_neg(F);
+            const ff2 mR = ff2_mul(coef(0), R, NZ);
+            VV = ff2_norm(ff2_add(ff2_add(ff2_mul(coef(2), VN, NZ), ff2_mul(coef(3), AN, NZ)), ff2_mul(coef(4), mR, NZ)));
+            AA = ff2_norm(ff2_sub(mR, ff2_mul(coef(1), VV, NZ)));
+        }
+        else {
+            // a prescribed component (boundary rows): lane by lane
+            ffv vl[2], al[2];
+            const ffv fl[2] = {ff2_lane0(F), ff2_lane1(F)}, xl[2] = {ff2_lane0(FX), ff2_lane1(FX)};
+            const ffv vn[2] = {ff2_lane0(VN), ff2_lane1(VN)}, an[2] = {ff2_lane0(AN), ff2_lane1(AN)};
+            const int cs[2] = {cl.x, cl.y};
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int c = cs[k];
+                if (c < GFGPU_MASS_CLASSES) {
+                    const ffv R = hf ? ff_sub(xl[k], fl[k]) : ff_neg(fl[k]);
+                    const ffv mR = ff_mul(ff_make(scf[0][c], scf[5][c]), R);
+                    vl[k] = ff_norm(ff_add(ff_add(ff_mul(ff_make(scf[2][c], scf[7][c]), vn[k]),
+                                                  ff_mul(ff_make(scf[3][c], scf[8][c]), an[k])),
+                                           ff_mul(ff_make(scf[4][c], scf[9][c]), mR)));
+                    al[k] = ff_norm(ff_sub(mR, ff_mul(ff_make(scf[1][c], scf[6][c]), vl[k])));
+                }
+                else {
+                    al[k] = an[k];
+                    vl[k] = ff_norm(ff_add(vn[k], ff_mul(dt, an[k])));
+                }
+            }
+            VV = ff2_from(vl[0], vl[1]);
+            AA = ff2_from(al[0], al[1]);
+        }
+        reinterpret_cast<ulonglong2*>(p.v)[node] = make_ulonglong2(VV.h, VV.l);
+        reinterpret_cast<ulonglong2*>(p.a)[node] = make_ulonglong2(AA.h, AA.l);
         if (p.advance) {
-            const float4 uq = su[(warp + 1) * kTmaUW + lane + 1];
-            const ffv ux = ff_norm(ff_add(ff_add(lo2(uq), ff_mul(dt, vx)), ff_mul(cc, ax)));
-            const ffv uy = ff_norm(ff_add(ff_add(hi2(uq), ff_mul(dt, vy)), ff_mul(cc, ay)));
-            p.uout[node] = pack(ux, uy);
+            const ff2 U = ldu((warp + 1) * kTmaUW + lane + 1);
+            const ff2 UN = ff2_norm(ff2_add(ff2_add(U, ff2_mul(DT, VV, NZ)), ff2_mul(CC, AA, NZ)));
+            reinterpret_cast<ulonglong2*>(p.uout)[node] = make_ulonglong2(UN.h, UN.l);
         }
     }
 }
@@ -519,8 +579,10 @@ k_pair_elem_square(const int32_t* __restrict__ conn, const float4* __restrict__ 
     {
         const int4 cn = __ldg(reinterpret_cast<const int4*>(conn) + e);
         float4 S, D, H;
-        pair_element(__ldg(u + cn.x), __ldg(u + cn.y), __ldg(u + cn.z), __ldg(u + cn.w), __ldg(cLN + e), __ldg(cH + e), S,
-                     D, H);
+        const float4 q0 = __ldg(u + cn.x), q1 = __ldg(u + cn.y), q2 = __ldg(u + cn.z), q3 = __ldg(u + cn.w);
+        const float4 cln = __ldg(cLN + e);
+        pair_element(lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), lo2(q3), hi2(q3), lo2(cln), hi2(cln),
+                     pf(__ldg(cH + e)), S, D, H);
         const ffv Sx = lo2(S), Sy = hi2(S), Dx = lo2(D), Dy = hi2(D), H0 = lo2(H), H1 = hi2(H);
         float4* o = fe + e * 4;
         o[0] = pack(ff_norm(ff_sub(H0, Sx)), ff_norm(ff_sub(H1, Sy)));
@@ -638,35 +700,48 @@ k_pair_node_csr(const PairCsrStep p, const __grid_constant__ PairClassTab tab)
 
 // FP64 in: the predictor u + dt v + dt^2/2 a of the first increment (FP64, as k_predict), then
 // u, v, a (and fext) as pairs
+// packed: pair path 1's layout {x.h, y.h, x.l, y.l}, else interleaved {x.h, x.l, y.h, y.l}
+__device__ __forceinline__ float4 lay(ffv x, ffv y, bool packed)
+{
+    return packed ? ppack(x, y) : pack(x, y);
+}
+
 __global__ void k_pair_begin(const double2* __restrict__ u, const double2* __restrict__ v,
                              const double2* __restrict__ a, const double2* __restrict__ fext,
-                             int64_t nnode, double dt, double c, float4* __restrict__ pu,
+                             int64_t nnode, double dt, double c, int packed, float4* __restrict__ pu,
                              float4* __restrict__ pv, float4* __restrict__ pa, float4* __restrict__ pf_)
 {
     GF_FOR(n, nnode)
     {
         const double2 un = u[n], vn = v[n], an = a[n];
         const double ux = fma(c, an.x, fma(dt, vn.x, un.x)), uy = fma(c, an.y, fma(dt, vn.y, un.y));
-        pu[n] = pack(ff_from_double(ux), ff_from_double(uy));
-        pv[n] = pack(ff_from_double(vn.x), ff_from_double(vn.y));
-        pa[n] = pack(ff_from_double(an.x), ff_from_double(an.y));
+        pu[n] = lay(ff_from_double(ux), ff_from_double(uy), packed);
+        pv[n] = lay(ff_from_double(vn.x), ff_from_double(vn.y), packed);
+        pa[n] = lay(ff_from_double(an.x), ff_from_double(an.y), packed);
         if (fext) {
             const double2 fn = fext[n];
-            pf_[n] = pack(ff_from_double(fn.x), ff_from_double(fn.y));
+            pf_[n] = lay(ff_from_double(fn.x), ff_from_double(fn.y), packed);
         }
     }
 }
 
 __global__ void k_pair_end(const float4* __restrict__ pu, const float4* __restrict__ pv,
-                           const float4* __restrict__ pa, int64_t nnode, double2* __restrict__ u,
+                           const float4* __restrict__ pa, int64_t nnode, int packed, double2* __restrict__ u,
                            double2* __restrict__ v, double2* __restrict__ a)
 {
     GF_FOR(n, nnode)
     {
         const float4 qu = pu[n], qv = pv[n], qa = pa[n];
-        u[n] = make_double2(ff_to_double(lo2(qu)), ff_to_double(hi2(qu)));
-        v[n] = make_double2(ff_to_double(lo2(qv)), ff_to_double(hi2(qv)));
-        a[n] = make_double2(ff_to_double(lo2(qa)), ff_to_double(hi2(qa)));
+        if (packed) {
+            u[n] = make_double2(ff_to_double(px_(qu)), ff_to_double(py_(qu)));
+            v[n] = make_double2(ff_to_double(px_(qv)), ff_to_double(py_(qv)));
+            a[n] = make_double2(ff_to_double(px_(qa)), ff_to_double(py_(qa)));
+        }
+        else {
+            u[n] = make_double2(ff_to_double(lo2(qu)), ff_to_double(hi2(qu)));
+            v[n] = make_double2(ff_to_double(lo2(qv)), ff_to_double(hi2(qv)));
+            a[n] = make_double2(ff_to_double(lo2(qa)), ff_to_double(hi2(qa)));
+        }
     }
 }
 
@@ -687,7 +762,7 @@ __global__ void k_pair_coef(const double* __restrict__ Km, const double* __restr
         const double lam = K - 2.0 * G / 3.0;
         const ffv L = ff_from_double(0.25 * lam), N = ff_from_double(0.25 * G);
         const ffv kH = ff_from_double(0.25 * g2 * (lam + 3.0 * G));
-        cLN[e] = pack(L, N);
+        cLN[e] = ppack(L, N);
         cH[t] = make_float2(kH.h, kH.l);
     }
 }
@@ -864,7 +939,7 @@ static int pair_begin(const gfgpu_verlet_desc* d, const double* u, const double*
     k_pair_begin<<<grid_for(d->nnode), kBlock, 0, s>>>(reinterpret_cast<const double2*>(u), reinterpret_cast<const double2*>(v),
                                                        reinterpret_cast<const double2*>(a),
                                                        reinterpret_cast<const double2*>(d->fext), d->nnode, dt, c,
-                                                       ps.ub[0], ps.v, ps.a, ps.fext);
+                                                       d->pair_mode == 1 ? 1 : 0, ps.ub[0], ps.v, ps.a, ps.fext);
     return check_launch("pair begin");
 }
 
@@ -976,6 +1051,7 @@ static int pair_increments(const gfgpu_verlet_desc* d, int64_t first, int64_t co
     p.ntx = (nx + kTmaTX) / kTmaTX;
     p.dt = split_host(dt);
     p.cc = split_host(c);
+    p.nz = kF2NegZero;
     if (TY == 15) return launch_tma<15>(p, mu, mv, ma, ml, mh, tab, first, count, advance_last, ub, sms, s);
     return launch_tma<7>(p, mu, mv, ma, ml, mh, tab, first, count, advance_last, ub, sms, s);
 }
@@ -985,7 +1061,8 @@ static int pair_end(const gfgpu_verlet_desc* d, int64_t last, double* u, double*
 {
     GF_REQUIRE(u && v && a && last >= 0, "bad argument");
     const PairState ps = pair_state(d, workspace);
-    k_pair_end<<<grid_for(d->nnode), kBlock, 0, s>>>(ps.ub[last & 1], ps.v, ps.a, d->nnode, reinterpret_cast<double2*>(u),
+    k_pair_end<<<grid_for(d->nnode), kBlock, 0, s>>>(ps.ub[last & 1], ps.v, ps.a, d->nnode, d->pair_mode == 1 ? 1 : 0,
+                                                     reinterpret_cast<double2*>(u),
                                                      reinterpret_cast<double2*>(v), reinterpret_cast<double2*>(a));
     return check_launch("pair end");
 }

@@ -55,10 +55,11 @@ int gfgpu_set_strict(int strict);
  * node_variant 1 = both dofs of a node per thread in the node kernel. Same results. */
 int gfgpu_set_variant(int elem_variant, int node_variant);
 /* Kernel of the float-float explicit increment (gfgpu_verlet_precompute_pair), process-wide:
- * 0 (default) = persistent CTAs of 256 threads that prefetch the next 31 x 7 node tile's inputs
- * by TMA into a second shared-memory stage while computing the current one; 2 = the same with
- * 31 x 15 node tiles and 512 threads; 1 = one 32 x 8 node tile per CTA with plain loads. Same
- * arithmetic, the four-element sums grouped differently in 1 (agreement ~1e-14). */
+ * 2 (default) = persistent CTAs of 512 threads that prefetch the next 31 x 15 node tile's inputs
+ * by TMA into a second shared-memory stage while computing the current one, x and y of a node in
+ * the packed FP32x2 instructions; 0 = the same with 31 x 7 node tiles and 256 threads; 1 = one
+ * 32 x 8 node tile per CTA with plain loads and scalar FP32. Same arithmetic (0 and 2 bit-identical),
+ * the four-element sums grouped differently in 1 (agreement ~1e-14). */
 int gfgpu_set_pair_kernel(int kernel);
 /* Timeout flag of the pair kernels' bounded waits for their TMA copies: GFGPU_ERR_TIMEOUT if a
  * wait gave up since the last call (the increment's results are then invalid), else GFGPU_OK.

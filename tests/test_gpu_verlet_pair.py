@@ -22,7 +22,7 @@ def gf():
     gf.set_strict(False)
     yield gf
     gf.set_strict(False)
-    _lib().call("gfgpu_set_pair_kernel", 0)
+    _lib().call("gfgpu_set_pair_kernel", DEFAULT_KERNEL)
 
 
 def _lib():
@@ -31,14 +31,17 @@ def _lib():
     return L
 
 
+DEFAULT_KERNEL = 2
+
+
 @pytest.fixture(params=[0, 1, 2], ids=["tma31x7", "tile", "tma31x15"])
 def kernel(request, gf):
-    """The persistent TMA pipeline (0, the default; 2 with taller tiles) and the
+    """The persistent TMA pipeline (2, the default, 31 x 15 tiles; 0 with 31 x 7 tiles) and the
     one-tile-per-CTA kernel (1); every test ends by checking that no bounded wait gave up."""
     _lib().call("gfgpu_set_pair_kernel", request.param)
     yield request.param
     _lib().call("gfgpu_verlet_pair_status")
-    _lib().call("gfgpu_set_pair_kernel", 0)
+    _lib().call("gfgpu_set_pair_kernel", DEFAULT_KERNEL)
 
 
 def _state(v0):
@@ -191,7 +194,7 @@ def test_pair_kernels_agree(gf, oracle):
             out.append(s)
         _lib().call("gfgpu_verlet_pair_status")
     finally:
-        _lib().call("gfgpu_set_pair_kernel", 0)
+        _lib().call("gfgpu_set_pair_kernel", DEFAULT_KERNEL)
     for k in (1, 2):
         for x, y in zip(out[0], out[k]):
             assert rel_err(to_np(x), to_np(y)) <= 1e-13
