@@ -588,9 +588,11 @@ def fp64_probe():
 
 
 def workload_static(args):
-    """3-d static case: Hex8 n3d^3 matrix-free Jacobi-PCG to 1e-8 relative residual (FP64), two
-    timed solves from a zero initial guess (best counts), against the oracle's matrix-free
-    operator (one stiffness action) on the host cores."""
+    """3-d static case: Hex8 n3d^3 matrix-free Jacobi-PCG to 1e-8 relative residual (FP64
+    solution, residuals and dot products), two timed solves from a zero initial guess (best
+    counts), with the stiffness action of the iterations in float-float pairs (the headline of this
+    workload) and in FP64, against the oracle's matrix-free operator (one stiffness action) on the
+    host cores."""
     import torch
 
     import goosefem_gb300 as gf
@@ -599,44 +601,64 @@ def workload_static(args):
     coor, conn, K, G, iip, xp = static_case(n)
     nnode = coor.shape[0]
     dofs = np.arange(nnode * 3).reshape(nnode, 3)
-    st = gf.ElasticStatic(coor, conn, dofs, K, G, iip,
-                          uniform=("auto" if args.path == "auto" else False))
     iip_d = torch.as_tensor(iip, device="cuda").long()
     xp_d = torch.as_tensor(xp, device="cuda")
     x = torch.zeros((nnode, 3), dtype=torch.float64, device="cuda")
 
-    def solve():
-        x.zero_()
-        x.view(-1)[iip_d] = xp_d
-        return st.solve(x, tol=1e-8, check_every=16)
+    def timed(st):
+        def solve():
+            x.zero_()
+            x.view(-1)[iip_d] = xp_d
+            return st.solve(x, tol=1e-8, check_every=16)
 
-    solve()  # warm-up
-    torch.cuda.synchronize()
-    secs, its = [], []
-    for _ in range(2):
-        t0 = time.perf_counter()
-        its.append(solve())
+        solve()  # warm-up
         torch.cuda.synchronize()
-        secs.append(time.perf_counter() - t0)
-    sec = min(secs)
-    it, rel = its[-1]
-    res = {"metric": "time-to-1e-8 resid (Jacobi-PCG)", "value": sec, "unit": "s",
-           "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded)",
-           "config": {"workload": f"Hex8 Regular {n}^3 static, z=0 fixed, top uz=-1e-2, "
-                                  "matrix-free Jacobi-PCG", "element_path":
-                      ("uniform-cube" if st.coef is not None else "uniform") if st.uniform
-                      else "general", "solves_timed": len(secs)},
-           "iterations": it, "relres_true": rel, "ms_per_iteration": sec * 1e3 / it,
-           "elem_updates_per_s": n ** 3 * 8 * it / sec}
+        secs, its = [], []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            its.append(solve())
+            torch.cuda.synchronize()
+            secs.append(time.perf_counter() - t0)
+        sec = min(secs)
+        it, rel = its[-1]
+        return {"seconds": sec, "iterations": it, "relres_true": rel,
+                "ms_per_iteration": sec * 1e3 / it}
+
+    uni = "auto" if args.path == "auto" else False
+    st = gf.ElasticStatic(coor, conn, dofs, K, G, iip, uniform=uni)
+    path = ("uniform-cube" if st.coef is not None else "uniform") if st.uniform else "general"
+    pair_ok = int(gf._lib.lib().gfgpu_pcg_pair_coef_floats(C.addressof(st.desc))) > 0
+    fp64 = timed(st)
     if st.coef is not None and st.desc.reg_nz > 0:
         # FP64 instructions of one iteration of the cube / Regular path: element kernel ~171 per
         # element, gather 8 adds + 1 FMA, update 5 per free dof, direction 1 per dof
         nfree = nnode * 3 - iip.size
         instr = 171 * n ** 3 + 14 * nfree + nnode * 3
         peak = fp64_probe() / 2.0
-        res["fp64"] = {"instr_per_iteration": instr, "achieved_ginstr_s": instr / (sec / it) / 1e9,
-                       "peak_ginstr_s": peak / 1e9, "instr_frac": instr / (sec / it) / peak,
-                       "peak_source": "measured live (gfgpu_probe_fp64: DFMA chains)"}
+        sec_it = fp64["ms_per_iteration"] * 1e-3
+        fp64["fp64"] = {"instr_per_iteration": instr, "achieved_ginstr_s": instr / sec_it / 1e9,
+                        "peak_ginstr_s": peak / 1e9, "instr_frac": instr / sec_it / peak,
+                        "peak_source": "measured live (gfgpu_probe_fp64: DFMA chains)"}
+    pair = None
+    if pair_ok:
+        st.use_pair()
+        pair = timed(st)
+    head = pair if pair is not None else fp64
+    res = {"metric": "time-to-1e-8 resid (Jacobi-PCG)", "value": head["seconds"], "unit": "s",
+           "higher_is_better": False,
+           "dtype": ("f64 solve, float-float (f32 pair) stiffness action in the iterations"
+                     if pair is not None else "f64"),
+           "data": "synthetic (seeded)",
+           "config": {"workload": f"Hex8 Regular {n}^3 static, z=0 fixed, top uz=-1e-2, "
+                                  "matrix-free Jacobi-PCG", "element_path": path,
+                      "operator_arithmetic": "pair" if pair is not None else "fp64",
+                      "solves_timed": 2},
+           "iterations": head["iterations"], "relres_true": head["relres_true"],
+           "ms_per_iteration": head["ms_per_iteration"],
+           "elem_updates_per_s": n ** 3 * 8 * head["iterations"] / head["seconds"],
+           "fp64_operator": fp64}
+    if pair is not None:
+        res["speedup_vs_fp64_operator"] = fp64["seconds"] / pair["seconds"]
     del st, x
     if not args.no_cpu:
         try:

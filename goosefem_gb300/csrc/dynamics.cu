@@ -1102,6 +1102,16 @@ int64_t gfgpu_internal_pair_workspace_bytes(const gfgpu_verlet_desc* d);
 int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
                                int64_t nsteps, void* workspace, cudaStream_t s);
 
+// Factors of the cube Hex8 coefficients in lam and G (k_hex8_cube_coef): L0 = a0 lam, G0 = a0 G,
+// L1 = a1 lam, G1 = a1 G, kH = c2 (lam + 4 G); for the pair operator of the static solvers (pcg.cu).
+void gfgpu_internal_hex8_cube_factors(const gfgpu_verlet_desc* d, double* a0, double* a1, double* c2)
+{
+    const Hex8Uniform c = hex8_uniform_constants(d);
+    *a0 = c.w0x * c.dx;
+    *a1 = c.w1x * c.dx;
+    *c2 = c.w2 * c.dx * c.dx;
+}
+
 // Element-kernel launch shared with the static solvers (pcg.cu, learned.cu, coarse.cu), whose
 // gathers read fe in reg_grid(d)'s layout.
 int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "ffpair.cuh"
 
 namespace gfgpu {
 
@@ -184,6 +185,238 @@ __global__ void k_keep_prescribed(const int32_t* __restrict__ part, int64_t nnu,
     GF_FOR(t, n) o[t] = part[t] < nnu ? 0.0 : x[t];
 }
 
+
+// ---------------------------------------------------------------- float-float operator
+//
+// On a Regular cube Hex8 mesh the iterations can apply A p in pair arithmetic (ffpair.cuh: a value
+// is h + l, two FP32 numbers): the FP64 closed form issues ~171 FP64 instructions per element at
+// GB300's FP64 rate (~1.7 per SM and clock), the pair form ~1500 FP32 instructions at 128 per SM
+// and clock. The direction p stays FP64 (the CG recurrences and dot products need it); the
+// direction update also writes it as pairs (pp), the element kernel reads pp and writes pair
+// element forces into the fe buffer (8 bytes per value, like a double), and the gather sums a
+// dof's forces as pairs and returns the sum to FP64.
+
+// folded coefficient factors as pairs (see gfgpu_internal_hex8_cube_factors) and the grid
+struct CubePair {
+    float2 a0, a1, c2;
+    uint32_t nx, ny, nz;
+};
+
+__device__ __forceinline__ ffv pfl(float2 q)
+{
+    return ff_make(q.x, q.y);
+}
+
+__device__ __forceinline__ float2 split_pair(double x)
+{
+    const float h = __double2float_rn(x);
+    return make_float2(h, __double2float_rn(x - static_cast<double>(h)));
+}
+
+// Walsh-Hadamard transform of 8 pairs without the mean (the operator does not use it)
+__device__ __forceinline__ void fwht8_nomean_pair(ffv (&v)[8])
+{
+#pragma unroll
+    for (int h = 1; h < 4; h <<= 1)
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if ((i & h) == 0) {
+                const ffv a = v[i], b = v[i + h];
+                v[i] = ff_add(a, b);
+                v[i + h] = ff_sub(a, b);
+            }
+#pragma unroll
+    for (int i = 1; i < 4; ++i) {
+        const ffv a = v[i], b = v[i + 4];
+        v[i] = ff_add(a, b);
+        v[i + 4] = ff_sub(a, b);
+    }
+    v[4] = ff_sub(v[0], v[4]);
+}
+
+// Element forces of the cube closed form (k_elem_force_hex8_cube, the same modes and merges) on
+// pairs; element e = (ez ny + ey) nx + ex of Regular(nx, ny, nz), its nodes by index arithmetic;
+// fe component-major (fe[(m * 3 + j) * nelem + e], the layout the Regular gather reads).
+__global__ void __launch_bounds__(128)
+k_elem_force_hex8_cube_pair(const float2* __restrict__ up, const float4* __restrict__ lg, CubePair c,
+                            int64_t nelem, float2* __restrict__ fe)
+{
+    constexpr int pos[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+    const uint32_t W = c.nx + 1u, A = W * (c.ny + 1u);
+    GF_FOR(e, nelem)
+    {
+        const uint32_t ee = static_cast<uint32_t>(e), t = ee / c.nx, ex = ee - t * c.nx;
+        const uint32_t ez = t / c.ny, ey = t - ez * c.ny;
+        const uint32_t n0 = ez * A + ey * W + ex;
+        // binary order b = bx + 2 by + 4 bz
+        ffv H[3][8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const float2* un = up + static_cast<int64_t>(n0 + (b & 1) + ((b >> 1) & 1) * W + (b >> 2) * A) * 3;
+            H[0][b] = pfl(__ldg(un));
+            H[1][b] = pfl(__ldg(un + 1));
+            H[2][b] = pfl(__ldg(un + 2));
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            fwht8_nomean_pair(H[j]);
+#pragma unroll
+            for (int b = 1; b < 8; ++b) H[j][b] = ff_norm(H[j][b]);
+        }
+        const float4 q = __ldg(lg + e);
+        const ffv lam = ff_make(q.x, q.y), G = ff_make(q.z, q.w);
+        const ffv L0 = ff_mul(pfl(c.a0), lam), G0 = ff_mul(pfl(c.a0), G), G0x2 = ff_twice(G0);
+        const ffv L1 = ff_mul(pfl(c.a1), lam), G1 = ff_mul(pfl(c.a1), G), G1x2 = ff_twice(G1);
+        const ffv G1x3 = ff_add(G1x2, G1);
+        const ffv kH = ff_mul(pfl(c.c2), ff_add(lam, ff_twice(ff_twice(G))));
+        // modes (A1 = -H1, A2 = -H2, A3 = -H4, A4 = H3, A5 = H6, A6 = H5, A7 = -H7)
+        ffv A1[3], A2[3], A3[3], A4[3], A5[3], A6[3], A7[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            A1[j] = ff_neg(H[j][1]);
+            A2[j] = ff_neg(H[j][2]);
+            A4[j] = H[j][3];
+            A3[j] = ff_neg(H[j][4]);
+            A6[j] = H[j][5];
+            A5[j] = H[j][6];
+            A7[j] = ff_neg(H[j][7]);
+        }
+        ffv F[8][3];
+        {
+            const ffv Lt = ff_mul(L0, ff_add(ff_add(A1[0], A2[1]), A3[2]));
+            F[1][0] = ff_add(ff_mul(G0x2, A1[0]), Lt);
+            F[2][1] = ff_add(ff_mul(G0x2, A2[1]), Lt);
+            F[3][2] = ff_add(ff_mul(G0x2, A3[2]), Lt);
+            const ffv s01 = ff_mul(G0, ff_add(A1[1], A2[0]));
+            const ffv s02 = ff_mul(G0, ff_add(A1[2], A3[0]));
+            const ffv s12 = ff_mul(G0, ff_add(A2[2], A3[1]));
+            F[1][1] = s01;
+            F[2][0] = s01;
+            F[1][2] = s02;
+            F[3][0] = s02;
+            F[2][2] = s12;
+            F[3][1] = s12;
+        }
+        {
+            const ffv Lxi = ff_mul(L1, ff_add(A4[1], A6[2]));
+            const ffv Let = ff_mul(L1, ff_add(A4[0], A5[2]));
+            const ffv Lze = ff_mul(L1, ff_add(A6[0], A5[1]));
+            F[4][0] = ff_add(ff_mul(G1x3, A4[0]), Let);
+            F[4][1] = ff_add(ff_mul(G1x3, A4[1]), Lxi);
+            F[4][2] = ff_add(ff_mul(G1x2, A4[2]), ff_mul(G1, ff_add(A5[0], A6[1])));
+            F[5][0] = ff_add(ff_mul(G1x2, A5[0]), ff_mul(G1, ff_add(A6[1], A4[2])));
+            F[5][1] = ff_add(ff_mul(G1x3, A5[1]), Lze);
+            F[5][2] = ff_add(ff_mul(G1x3, A5[2]), Let);
+            F[6][0] = ff_add(ff_mul(G1x3, A6[0]), Lze);
+            F[6][1] = ff_add(ff_mul(G1x2, A6[1]), ff_mul(G1, ff_add(A5[0], A4[2])));
+            F[6][2] = ff_add(ff_mul(G1x3, A6[2]), Lxi);
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) F[7][j] = ff_mul(kH, A7[j]);
+        // inverse transform of (0, -F1, -F2, F4, -F3, F6, F5, -F7) in binary order
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const ffv b1 = ff_neg(F[1][j]);
+            ffv v[8] = {b1, F[1][j], ff_sub(F[4][j], F[2][j]), ff_neg(ff_add(F[2][j], F[4][j])),
+                        ff_sub(F[6][j], F[3][j]), ff_neg(ff_add(F[3][j], F[6][j])),
+                        ff_sub(F[5][j], F[7][j]), ff_add(F[5][j], F[7][j])};
+#pragma unroll
+            for (int h = 2; h < 8; h <<= 1)
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if ((i & h) == 0) {
+                        const ffv a = v[i], b = v[i + h];
+                        v[i] = ff_add(a, b);
+                        v[i + h] = ff_sub(a, b);
+                    }
+#pragma unroll
+            for (int m = 0; m < 8; ++m) {
+                const ffv o = v[pos[m]];
+                fe[(m * 3 + j) * nelem + e] = make_float2(o.h, o.l);
+            }
+        }
+    }
+}
+
+// q = A p on free dofs from the pair element forces (the Regular Hex8 gather order of gather_dof,
+// summed as pairs, returned to FP64), 0 on prescribed dofs; partial p.q in FP64.
+__global__ void __launch_bounds__(kRedThreads)
+k_pcg_gather_pair(const int32_t* __restrict__ part, int64_t nnu, const float2* __restrict__ fe,
+                  const double* __restrict__ p, int64_t n, double* __restrict__ q,
+                  double* __restrict__ partial, RegGrid reg)
+{
+    __shared__ double sh[32];
+    double acc = 0.0;
+    const uint32_t nx = static_cast<uint32_t>(reg.nx), ny = static_cast<uint32_t>(reg.ny);
+    const uint32_t nz = static_cast<uint32_t>(reg.nz), cs = nx * ny * nz;
+    const uint32_t W = nx + 1u, A = W * (ny + 1u);
+    GF_FOR(t, n)
+    {
+        double fv = 0.0;
+        if (__ldg(part + t) < nnu) {
+            const uint32_t tt = static_cast<uint32_t>(t), node = tt / 3u, i = tt - node * 3u;
+            const uint32_t iz = node / A, rem = node - iz * A, iy = rem / W, ix = rem - iy * W;
+            ffv f = ff_make(0.0f, 0.0f);
+#pragma unroll
+            for (int dz = 1; dz >= 0; --dz) {
+                if ((dz && iz == 0u) || (!dz && iz >= nz)) continue;
+#pragma unroll
+                for (int dy = 1; dy >= 0; --dy) {
+                    if ((dy && iy == 0u) || (!dy && iy >= ny)) continue;
+#pragma unroll
+                    for (int dx = 1; dx >= 0; --dx) {
+                        if ((dx && ix == 0u) || (!dx && ix >= nx)) continue;
+                        const int m = 4 * dz + (dy ? (dx ? 2 : 3) : (dx ? 1 : 0));
+                        const uint32_t e = ((iz - dz) * ny + (iy - dy)) * nx + (ix - dx);
+                        f = ff_add(f, pfl(__ldg(fe + e + (m * 3u + i) * cs)));
+                    }
+                }
+            }
+            fv = ff_to_double(f);
+            acc = fma(p[t], fv, acc);
+        }
+        q[t] = fv;
+    }
+    double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// p = z + beta p, and p as pairs
+__global__ void k_pcg_direction_pair(const double* __restrict__ z, const double* __restrict__ sc,
+                                     int64_t n, double* __restrict__ p, float2* __restrict__ pp)
+{
+    double beta = sc[SC_BETA];
+    GF_FOR(t, n)
+    {
+        const double v = fma(beta, p[t], z[t]);
+        p[t] = v;
+        pp[t] = split_pair(v);
+    }
+}
+
+__global__ void k_pcg_split(const double* __restrict__ p, int64_t n, float2* __restrict__ pp)
+{
+    GF_FOR(t, n) pp[t] = split_pair(p[t]);
+}
+
+// {lam, G} per element as pairs, lam = K - 2G/3 (the FP64 expression of k_hex8_cube_coef)
+__global__ void k_pcg_pair_coef(const double* __restrict__ Km, const double* __restrict__ Gm,
+                                int64_t nelem, float4* __restrict__ out)
+{
+    GF_FOR(e, nelem)
+    {
+        const double G = Gm[e], lam = Km[e] - 2.0 * G / 3.0;
+        const float2 a = split_pair(lam), b = split_pair(G);
+        out[e] = make_float4(a.x, a.y, b.x, b.y);
+    }
+}
+
+// the pair operator applies: Regular cube Hex8 mesh, index-arithmetic gather (component-major fe)
+inline bool pcg_pair_applies(const gfgpu_verlet_desc* d)
+{
+    return d->nelem > 0 && reg_grid(d).soa && d->reg_nx * d->reg_ny * d->reg_nz == d->nelem;
+}
+
 // Jacobi: diagonal of the element stiffness per (element, node, direction) for isotropic
 // linear elasticity, K_e[(m,j),(m,j)] = sum_q vol (lam dNx(m,j)^2 + G dNx(m,j)^2 + G |dNx(m,:)|^2).
 template <int NNE, int ND>
@@ -221,6 +454,7 @@ __global__ void k_inv_free(const int32_t* __restrict__ part, int64_t nnu,
 
 struct PcgWs {
     double *fe, *p, *r, *z, *q, *minv, *bvec, *partial, *sc;
+    float2* pp; // the direction as pairs (pair operator)
 };
 
 static int64_t align256(int64_t b)
@@ -243,6 +477,8 @@ static PcgWs carve(const gfgpu_verlet_desc* d, void* ws)
     w.partial = reinterpret_cast<double*>(c);
     c += align256(2 * kRedBlocks * 8);
     w.sc = reinterpret_cast<double*>(c);
+    c += align256(SC_COUNT * 8 + 64);
+    w.pp = reinterpret_cast<float2*>(c);
     return w;
 }
 
@@ -250,7 +486,7 @@ static int64_t pcg_bytes(const gfgpu_verlet_desc* d)
 {
     int64_t n = d->nnode * d->ndim;
     return align256(d->nelem * d->nne * d->ndim * 8) + 6 * align256(n * 8) +
-           align256(2 * kRedBlocks * 8) + align256(SC_COUNT * 8 + 64);
+           align256(2 * kRedBlocks * 8) + align256(SC_COUNT * 8 + 64) + align256(n * 8);
 }
 
 } // namespace gfgpu
@@ -260,12 +496,32 @@ using namespace gfgpu;
 // element kernel launch shared with the explicit step (dynamics.cu)
 int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                   cudaStream_t s);
+void gfgpu_internal_hex8_cube_factors(const gfgpu_verlet_desc* d, double* a0, double* a1, double* c2);
 
 extern "C" {
 
 int64_t gfgpu_pcg_workspace_bytes(const gfgpu_verlet_desc* d)
 {
     return d ? pcg_bytes(d) : 0;
+}
+
+int64_t gfgpu_pcg_pair_coef_floats(const gfgpu_verlet_desc* d)
+{
+    return d && pcg_pair_applies(d) ? 4 * d->nelem : 0;
+}
+
+int gfgpu_pcg_precompute_pair(gfgpu_verlet_desc* d, float* coef, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(d && coef && d->K && d->G, "bad argument");
+    GF_REQUIRE(reinterpret_cast<uintptr_t>(coef) % 16 == 0, "coef must be 16-byte aligned");
+    if (!pcg_pair_applies(d))
+        return fail(GFGPU_ERR_UNSUPPORTED, "gfgpu_pcg_precompute_pair: Regular cube Hex8 meshes with the "
+                                           "index-arithmetic gather only");
+    k_pcg_pair_coef<<<grid_for(d->nelem), kBlock, 0, S(stream)>>>(d->K, d->G, d->nelem,
+                                                                  reinterpret_cast<float4*>(coef));
+    GF_TRY(check_launch("pcg_precompute_pair"));
+    d->pcg_pair = coef;
+    return GFGPU_OK;
 }
 
 int gfgpu_elastic_diagonal(const gfgpu_verlet_desc* d, double* diag, void* workspace,
@@ -285,19 +541,61 @@ int gfgpu_elastic_diagonal(const gfgpu_verlet_desc* d, double* diag, void* works
     return gfgpu_assemble_node(d->csr_ptr, d->csr_idx, d->dofs, d->nnode, d->ndim, fe, diag, stream);
 }
 
-// One Jacobi-PCG iteration: 6 launches (element forces, gather, alpha, update, beta, direction).
+static CubePair cube_pair(const gfgpu_verlet_desc* d)
+{
+    double a0, a1, c2;
+    gfgpu_internal_hex8_cube_factors(d, &a0, &a1, &c2);
+    auto sp = [](double x) {
+        const float h = static_cast<float>(x);
+        return make_float2(h, static_cast<float>(x - static_cast<double>(h)));
+    };
+    CubePair c;
+    c.a0 = sp(a0);
+    c.a1 = sp(a1);
+    c.c2 = sp(c2);
+    c.nx = static_cast<uint32_t>(d->reg_nx);
+    c.ny = static_cast<uint32_t>(d->reg_ny);
+    c.nz = static_cast<uint32_t>(d->reg_nz);
+    return c;
+}
+
+// One Jacobi-PCG iteration: 6 launches (element forces, gather, alpha, update, beta, direction);
+// with d->pcg_pair the element forces and the gather run on pairs and the direction update also
+// writes the pair copy of p that the next iteration's element kernel reads.
 static int pcg_iteration(const gfgpu_verlet_desc* d, const PcgWs& w, double* x, int64_t n,
                          cudaStream_t s)
 {
     const unsigned gb = kRedBlocks;
-    GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
-    k_pcg_gather<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
-                                             w.p, n, w.q, w.partial, reg_grid(d));
+    const bool pair = d->pcg_pair != nullptr;
+    if (pair) {
+        k_elem_force_hex8_cube_pair<<<grid_for(d->nelem, 128), 128, 0, s>>>(
+            w.pp, reinterpret_cast<const float4*>(d->pcg_pair), cube_pair(d), d->nelem,
+            reinterpret_cast<float2*>(w.fe));
+        k_pcg_gather_pair<<<gb, kRedThreads, 0, s>>>(d->part, d->nnu, reinterpret_cast<const float2*>(w.fe),
+                                                      w.p, n, w.q, w.partial, reg_grid(d));
+    }
+    else {
+        GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
+        k_pcg_gather<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
+                                                 w.p, n, w.q, w.partial, reg_grid(d));
+    }
     k_reduce_alpha<<<1, 1024, 0, s>>>(w.partial, w.sc);
     k_pcg_update<<<gb, kRedThreads, 0, s>>>(d->part, d->nnu, w.minv, w.p, w.q, n, w.sc, x, w.r, w.z,
                                              w.partial);
     k_reduce_beta<<<1, 1024, 0, s>>>(w.partial, w.sc);
-    k_pcg_direction<<<grid_for(n), kBlock, 0, s>>>(w.z, w.sc, n, w.p);
+    if (pair)
+        k_pcg_direction_pair<<<grid_for(n), kBlock, 0, s>>>(w.z, w.sc, n, w.p, w.pp);
+    else
+        k_pcg_direction<<<grid_for(n), kBlock, 0, s>>>(w.z, w.sc, n, w.p);
+    return GFGPU_OK;
+}
+
+// the pair operator's validity (the caller may have changed the descriptor since the precompute)
+static int pcg_pair_check(const gfgpu_verlet_desc* d)
+{
+    if (d->pcg_pair && !pcg_pair_applies(d))
+        return fail(GFGPU_ERR_UNSUPPORTED, "pcg_pair is set but the mesh is not a Regular cube Hex8 mesh "
+                                           "with the index-arithmetic gather");
     return GFGPU_OK;
 }
 
@@ -309,6 +607,7 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
                "bad argument");
     GF_REQUIRE(d->part && d->conn && d->csr_ptr && d->csr_idx && d->dofs && d->K && d->G,
                "null table");
+    GF_TRY(pcg_pair_check(d));
     if (check_every < 1) check_every = 1;
     cudaStream_t s = S(stream);
     PcgWs w = carve(d, workspace);
@@ -333,6 +632,7 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
     k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
                                                nullptr, w.minv, n, w.r, w.z, w.p, w.partial, reg_grid(d));
     k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ); // SC_RZ, SC_RZ_NEW(=rr, overwritten)
+    if (d->pcg_pair) k_pcg_split<<<grid_for(n), kBlock, 0, s>>>(w.p, n, w.pp);
     if ((rc = check_launch("pcg set-up")) != GFGPU_OK) return fail_out(rc);
     cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
     if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg set-up")) != GFGPU_OK) return fail_out(rc);
@@ -424,6 +724,7 @@ int gfgpu_pcg_begin(const gfgpu_verlet_desc* d, const double* diag, const double
                     const double* x, void* workspace, gfgpu_stream_t stream)
 {
     GF_REQUIRE(d && diag && x && workspace, "bad argument");
+    GF_TRY(pcg_pair_check(d));
     cudaStream_t s = S(stream);
     PcgWs w = carve(d, workspace);
     int64_t n = d->nnode * d->ndim;
@@ -441,6 +742,7 @@ int gfgpu_pcg_begin(const gfgpu_verlet_desc* d, const double* diag, const double
                                                rhs, w.minv, n, w.r, w.z, w.p, w.partial, reg_grid(d));
     k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ); // SC_RZ = r.z, SC_RZ_NEW = r.r
     k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_RR);
+    if (d->pcg_pair) k_pcg_split<<<grid_for(n), kBlock, 0, s>>>(w.p, n, w.pp);
     return check_launch("pcg_begin");
 }
 
@@ -448,6 +750,7 @@ int gfgpu_pcg_iterate(const gfgpu_verlet_desc* d, int64_t niter, double* x, void
                       gfgpu_stream_t stream)
 {
     GF_REQUIRE(d && x && workspace && niter >= 0, "bad argument");
+    GF_TRY(pcg_pair_check(d));
     cudaStream_t s = S(stream);
     PcgWs w = carve(d, workspace);
     int64_t n = d->nnode * d->ndim;
@@ -457,9 +760,10 @@ int gfgpu_pcg_iterate(const gfgpu_verlet_desc* d, int64_t niter, double* x, void
 
 int gfgpu_pcg_vector(const gfgpu_verlet_desc* d, void* workspace, int32_t which, double** ptr)
 {
-    GF_REQUIRE(d && workspace && ptr && which >= 0 && which <= 2, "bad argument");
+    GF_REQUIRE(d && workspace && ptr && which >= 0 && which <= 3, "bad argument");
     PcgWs w = carve(d, workspace);
-    *ptr = which == 0 ? w.r : (which == 1 ? w.z : w.p);
+    double* const v[4] = {w.r, w.z, w.p, w.q};
+    *ptr = v[which];
     return GFGPU_OK;
 }
 

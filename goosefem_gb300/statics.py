@@ -3,7 +3,7 @@
 The reference solves A_uu x_u = b_u - A_up x_p with an assembled sparse matrix and a direct
 factorisation (MatrixPartitioned.h:526-642). Here the stiffness action is the element kernel of the
 explicit step plus the deterministic CSR gather, and the solve is Jacobi-preconditioned CG in FP64
-(gfgpu_pcg_solve).
+(gfgpu_pcg_solve), optionally with the stiffness action in float-float arithmetic.
 """
 
 import ctypes as C
@@ -21,9 +21,12 @@ class ElasticStatic:
     """Matrix-free linear elastic operator of a Quad4/Hex8 mesh with prescribed dofs `iip`.
 
     K, G: per-element bulk and shear moduli. uniform: "auto" | True | False (closed-form element
-    kernel for congruent axis-aligned elements, see gfgpu_verlet_detect_uniform)."""
+    kernel for congruent axis-aligned elements, see gfgpu_verlet_detect_uniform).
+    arithmetic: "fp64" (default) or "pair": the Jacobi-PCG iterations apply the stiffness in
+    float-float arithmetic (gfgpu_pcg_precompute_pair; Regular cube Hex8 meshes only), everything
+    else (solution, residuals, dot products, the true residual check) in FP64."""
 
-    def __init__(self, coor, conn, dofs, K, G, iip, uniform="auto"):
+    def __init__(self, coor, conn, dofs, K, G, iip, uniform="auto", arithmetic="fp64"):
         from .vector import Vector
 
         conn_h = _dev.host_i32(conn)
@@ -91,14 +94,39 @@ class ElasticStatic:
             if nx > 0 and nelem % nx == 0:
                 _lib.call("gfgpu_verlet_detect_regular", C.addressof(d), nx, nelem // nx,
                           _dev.stream())
+        self.coef_pair = None
+        if arithmetic == "pair":
+            self.use_pair()
+        elif arithmetic != "fp64":
+            raise ValueError("arithmetic must be 'fp64' or 'pair'")
         nbytes = int(_lib.lib().gfgpu_pcg_workspace_bytes(C.addressof(d)))
         self.ws = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device=_dev.device())
         self.diag = torch.empty((nnode, nd), dtype=torch.float64, device=_dev.device())
         _lib.call("gfgpu_elastic_diagonal", C.addressof(d), self.diag.data_ptr(),
                   self.ws.data_ptr(), _dev.stream())
 
+    def use_pair(self):
+        """Float-float stiffness action in the PCG iterations (Regular cube Hex8 meshes)."""
+        n = int(_lib.lib().gfgpu_pcg_pair_coef_floats(C.addressof(self.desc)))
+        if n == 0:
+            raise RuntimeError("the pair operator needs a Regular cube Hex8 mesh (uniform, "
+                               "index-arithmetic gather)")
+        self.coef_pair = torch.empty(n, dtype=torch.float32, device=_dev.device())
+        _lib.call("gfgpu_pcg_precompute_pair", C.addressof(self.desc), self.coef_pair.data_ptr(),
+                  _dev.stream())
+
+    def use_fp64(self):
+        """FP64 stiffness action in the PCG iterations."""
+        self.desc.pcg_pair = None
+        self.coef_pair = None
+
+    @property
+    def arithmetic(self):
+        return "pair" if self.desc.pcg_pair else "fp64"
+
     def use_csr_gather(self):
         """Gather the operator's element forces through the dof CSR even on a Regular mesh."""
+        self.use_fp64()
         self.desc.reg_nx = 0
         self.desc.reg_ny = 0
         self.desc.reg_nz = 0
@@ -108,6 +136,7 @@ class ElasticStatic:
         return bool(self.desc.uniform)
 
     def use_general_path(self):
+        self.use_fp64()
         self.desc.uniform = 0
 
     def force(self, u):

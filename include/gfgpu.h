@@ -371,6 +371,13 @@ typedef struct {
      * square-element fused tile kernel, 2 = element kernel + dof-CSR node kernel with the square
      * closed form, 3 = the same with stored element stiffness matrices */
     int32_t pair_mode;
+    /* optional float-float coefficients of the static solvers' operator on a Regular cube Hex8
+     * mesh (gfgpu_pcg_precompute_pair): per element {lam.h, lam.l, G.h, G.l}. When set, the
+     * Jacobi-PCG iterations of gfgpu_pcg_solve / gfgpu_pcg_iterate apply the stiffness in pair
+     * arithmetic (~48-bit significands, ~1e-13 relative to the FP64 action); the solution, the
+     * residual, the preconditioned residual, the direction and every dot product stay FP64, and
+     * the initial and final (true) residuals use the FP64 operator. NULL = FP64 operator. */
+    const float* pcg_pair;
 } gfgpu_verlet_desc;
 
 #define GFGPU_MASS_CLASSES 16
@@ -526,6 +533,19 @@ int gfgpu_barrier_selftest(int64_t timeout_cycles, int* status);
  * The descriptor `d` is the one of the explicit step (dt, eta, inv, fext are ignored); `part`
  * and `nnu` mark the unknown dofs (part < nnu), all other dofs are prescribed. */
 int64_t gfgpu_pcg_workspace_bytes(const gfgpu_verlet_desc* d);
+/* Floats of the pair coefficients gfgpu_pcg_precompute_pair writes (4 per element), or 0 when the
+ * pair operator does not apply: it needs a Regular cube Hex8 mesh with the index-arithmetic gather
+ * (gfgpu_verlet_detect_regular_hex8) and the FP64 cube coefficients (d->coef). */
+int64_t gfgpu_pcg_pair_coef_floats(const gfgpu_verlet_desc* d);
+/* Float-float operator of the Jacobi-PCG iterations: writes {lam.h, lam.l, G.h, G.l} per element
+ * (lam = K - 2G/3) into coef (16-byte aligned, gfgpu_pcg_pair_coef_floats floats) and sets
+ * d->pcg_pair = coef. The iterations then apply the stiffness of the search direction in pair
+ * arithmetic on the FP32 pipes: the direction update also writes the direction as pairs, the
+ * cube closed form runs on pairs (the folded coefficients formed from lam and G in registers),
+ * and the gather sums a dof's element forces as pairs and returns them to FP64. Returns
+ * GFGPU_ERR_UNSUPPORTED where gfgpu_pcg_pair_coef_floats is 0. Set d->pcg_pair = NULL for the
+ * FP64 operator. */
+int gfgpu_pcg_precompute_pair(gfgpu_verlet_desc* d, float* coef, gfgpu_stream_t stream);
 /* Diagonal of the assembled stiffness as a nodevec (Jacobi preconditioner), from dNx/vol.
  * `workspace` needs nelem*nne*ndim doubles. */
 int gfgpu_elastic_diagonal(const gfgpu_verlet_desc* d, double* diag, void* workspace,
@@ -542,8 +562,9 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
 /* Step-by-step Jacobi-PCG on the same workspace as gfgpu_pcg_solve (used to generate the
  * training pairs of the learned preconditioner): begin sets b = rhs_u - (A x_p)_u (rhs may be
  * NULL: no external load), r = b - (A x)_u, z = M^-1 r, p = z; iterate runs niter iterations
- * without convergence checks; vector returns a device pointer to r (which = 0), z (1) or p (2)
- * inside the workspace; norms synchronises and returns r.r and b.b. */
+ * without convergence checks; vector returns a device pointer to r (which = 0), z (1), p (2) or
+ * q = A p of the last iteration's direction (3) inside the workspace; norms synchronises and
+ * returns r.r and b.b. */
 int gfgpu_pcg_begin(const gfgpu_verlet_desc* d, const double* diag, const double* rhs,
                     const double* x, void* workspace, gfgpu_stream_t stream);
 int gfgpu_pcg_iterate(const gfgpu_verlet_desc* d, int64_t niter, double* x, void* workspace,

@@ -249,3 +249,82 @@ def test_hex8_regular_gather_same_bits_as_csr(gf, oracle, uniform):
     perm = np.random.default_rng(3).permutation(nnode * 3)
     st = gf.statics.ElasticStatic(coor, conn, perm.reshape(-1, 3), K, G, iip, uniform=uniform)
     assert st.desc.reg_nz == 0
+
+
+def _pcg_vec(st, which):
+    import ctypes as C
+
+    from goosefem_gb300 import _lib
+
+    p = C.c_void_p(0)
+    _lib.call("gfgpu_pcg_vector", C.addressof(st.desc), st.ws.data_ptr(), which, C.addressof(p))
+    n = st.nnode * st.ndim
+    off = (p.value - st.ws.data_ptr()) // 8
+    return st.ws[off: off + n]
+
+
+def test_pcg_pair_operator_matches_fp64(gf, oracle):
+    """The float-float stiffness action of the Jacobi-PCG iterations (Regular cube Hex8, nx, ny,
+    nz all different) against the FP64 operator on the same direction: q = A p0 with p0 = M^-1 r0
+    after gfgpu_pcg_begin, on the free dofs, within 1e-12 of max |A p0| (pairs carry ~48 bits)."""
+    import ctypes as C
+
+    from goosefem_gb300 import _dev, _lib
+
+    R = oracle
+    nx, ny, nz = 9, 6, 5
+    coor, conn = R.hex8_regular(nx, ny, nz)
+    K, G = seeded_material(conn.shape[0], 47)
+    nxy = (nx + 1) * (ny + 1)
+    front = np.arange(nxy)
+    back = front + nz * nxy
+    iip = np.unique(np.concatenate([(front[:, None] * 3 + np.arange(3)).ravel(), back * 3 + 2]))
+    xp = np.where(np.isin(iip, back * 3 + 2), -1e-2, 0.0)
+    nnode = coor.shape[0]
+    st = gf.statics.ElasticStatic(coor, conn, np.arange(nnode * 3).reshape(-1, 3), K, G, iip,
+                                  arithmetic="pair")
+    assert st.arithmetic == "pair"
+    x = torch.zeros(nnode * 3, dtype=torch.float64, device="cuda")
+    x[torch.as_tensor(iip, device="cuda").long()] = torch.as_tensor(xp, device="cuda")
+    _lib.call("gfgpu_pcg_begin", C.addressof(st.desc), st.diag.data_ptr(), None, x.data_ptr(),
+              st.ws.data_ptr(), _dev.stream())
+    p0 = _pcg_vec(st, 2).clone()
+    _lib.call("gfgpu_pcg_iterate", C.addressof(st.desc), 1, x.data_ptr(), st.ws.data_ptr(),
+              _dev.stream())
+    q = to_np(_pcg_vec(st, 3))
+    f = to_np(st.force(p0.view(-1, 3))).ravel()
+    free = np.setdiff1d(np.arange(nnode * 3), iip)
+    assert np.max(np.abs(q[iip])) == 0.0
+    err = np.max(np.abs(q[free] - f[free])) / np.max(np.abs(f[free]))
+    assert 0 < err <= 1e-12, err
+
+
+def test_pcg_pair_solve(gf, oracle):
+    """Jacobi-PCG with the pair operator reaches the same 1e-8 true residual (checked with the FP64
+    operator and by the oracle), agrees with the FP64 solve and with the direct solve, is
+    deterministic, and refuses meshes it does not cover."""
+    from oracle import statics as S
+
+    coor, conn, K, G, iip, xp = _hex8_case(10, 42)
+    A = S.stiffness(coor, conn, K, G)
+    x_ref = S.solve_partitioned(A, iip, xp)
+    nnode = coor.shape[0]
+    dofs = np.arange(nnode * 3).reshape(-1, 3)
+    out = []
+    for arith in ("pair", "pair", "fp64"):
+        st = gf.statics.ElasticStatic(coor, conn, dofs, K, G, iip, arithmetic=arith)
+        x = torch.zeros((nnode, 3), dtype=torch.float64, device="cuda")
+        x.view(-1)[torch.as_tensor(iip, device="cuda").long()] = torch.as_tensor(xp, device="cuda")
+        it, rel = st.solve(x, tol=1e-8)
+        out.append((it, rel, to_np(x).ravel()))
+    (it_p, rel_p, xp_), (it_p2, rel_p2, xp2), (it_d, rel_d, xd) = out
+    assert rel_p <= 1e-8 and S.residual(A, iip, xp_) <= 1e-8
+    assert it_p == it_p2 and rel_p == rel_p2 and np.array_equal(xp_, xp2)
+    assert abs(it_p - it_d) <= 2
+    assert np.linalg.norm(xp_ - x_ref) / np.linalg.norm(x_ref) <= 1e-6
+    assert np.linalg.norm(xp_ - xd) / np.linalg.norm(xd) <= 1e-7
+    assert np.array_equal(xp_[iip], xp)
+    # not a cube mesh / not Regular: refused
+    st = gf.statics.ElasticStatic(coor * np.array([1.0, 1.0, 1.5]), conn, dofs, K, G, iip)
+    with pytest.raises(RuntimeError):
+        st.use_pair()
