@@ -88,6 +88,9 @@ def parse():
                    help="explicit workload: float-float fused kernel (pair) or the FP64 kernels")
     p.add_argument("--no-workloads", action="store_true",
                    help="headline only (skip the static, batch and learned workloads)")
+    p.add_argument("--static-operator", choices=["both", "pair", "fp64"], default="both",
+                   help="static workload: stiffness action of the PCG iterations in float-float "
+                        "pairs, in FP64, or both (pair is the reported value where it applies)")
     p.add_argument("--train-steps-1level", type=int, default=6000,
                    help="learned workload: Adam steps of the one-level network")
     p.add_argument("--pairs-1level", type=int, default=64,
@@ -628,8 +631,8 @@ def workload_static(args):
     st = gf.ElasticStatic(coor, conn, dofs, K, G, iip, uniform=uni)
     path = ("uniform-cube" if st.coef is not None else "uniform") if st.uniform else "general"
     pair_ok = int(gf._lib.lib().gfgpu_pcg_pair_coef_floats(C.addressof(st.desc))) > 0
-    fp64 = timed(st)
-    if st.coef is not None and st.desc.reg_nz > 0:
+    fp64 = timed(st) if args.static_operator in ("both", "fp64") or not pair_ok else None
+    if fp64 is not None and st.coef is not None and st.desc.reg_nz > 0:
         # FP64 instructions of one iteration of the cube / Regular path: element kernel ~171 per
         # element, gather 8 adds + 1 FMA, update 5 per free dof, direction 1 per dof
         nfree = nnode * 3 - iip.size
@@ -640,7 +643,7 @@ def workload_static(args):
                         "peak_ginstr_s": peak / 1e9, "instr_frac": instr / sec_it / peak,
                         "peak_source": "measured live (gfgpu_probe_fp64: DFMA chains)"}
     pair = None
-    if pair_ok:
+    if pair_ok and args.static_operator in ("both", "pair"):
         st.use_pair()
         pair = timed(st)
     head = pair if pair is not None else fp64
@@ -657,7 +660,7 @@ def workload_static(args):
            "ms_per_iteration": head["ms_per_iteration"],
            "elem_updates_per_s": n ** 3 * 8 * head["iterations"] / head["seconds"],
            "fp64_operator": fp64}
-    if pair is not None:
+    if pair is not None and fp64 is not None:
         res["speedup_vs_fp64_operator"] = fp64["seconds"] / pair["seconds"]
     del st, x
     if not args.no_cpu:

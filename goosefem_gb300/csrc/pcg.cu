@@ -209,8 +209,8 @@ __device__ __forceinline__ ffv pfl(float2 q)
 
 __device__ __forceinline__ float2 split_pair(double x)
 {
-    const float h = __double2float_rn(x);
-    return make_float2(h, __double2float_rn(x - static_cast<double>(h)));
+    const ffv p = ff_from_double(x);
+    return make_float2(p.h, p.l);
 }
 
 // Walsh-Hadamard transform of 8 pairs without the mean (the operator does not use it)

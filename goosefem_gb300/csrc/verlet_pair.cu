@@ -571,6 +571,11 @@ __global__ void k_pair_split(const double* __restrict__ x, int64_t n, float2* __
     }
 }
 
+__global__ void k_pair_join(const float2* __restrict__ in, int64_t n, double* __restrict__ out)
+{
+    GF_FOR(i, n) out[i] = ff_to_double(pf(in[i]));
+}
+
 __global__ void __launch_bounds__(256)
 k_pair_elem_square(const int32_t* __restrict__ conn, const float4* __restrict__ u, const float4* __restrict__ cLN,
                    const float2* __restrict__ cH, int64_t nelem, float4* __restrict__ fe)
@@ -1110,6 +1115,24 @@ int gfgpu_verlet_pair_displacement(const gfgpu_verlet_desc* d, int64_t it, void*
     GF_TRY(pair_check(d, workspace));
     *ptr = pair_state(d, workspace).ub[it & 1];
     return GFGPU_OK;
+}
+
+int gfgpu_pairs_from_f64(const double* x, int64_t n, float* out, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(n >= 0 && (n == 0 || (x && out)), "bad argument");
+    GF_REQUIRE(reinterpret_cast<uintptr_t>(out) % 8 == 0, "out must be 8-byte aligned");
+    if (n == 0) return GFGPU_OK;
+    k_pair_split<<<grid_for(n), kBlock, 0, S(stream)>>>(x, n, reinterpret_cast<float2*>(out));
+    return check_launch("pairs_from_f64");
+}
+
+int gfgpu_pairs_to_f64(const float* in, int64_t n, double* out, gfgpu_stream_t stream)
+{
+    GF_REQUIRE(n >= 0 && (n == 0 || (in && out)), "bad argument");
+    GF_REQUIRE(reinterpret_cast<uintptr_t>(in) % 8 == 0, "in must be 8-byte aligned");
+    if (n == 0) return GFGPU_OK;
+    k_pair_join<<<grid_for(n), kBlock, 0, S(stream)>>>(reinterpret_cast<const float2*>(in), n, out);
+    return check_launch("pairs_to_f64");
 }
 
 int64_t gfgpu_verlet_pair_coef_floats(const gfgpu_verlet_desc* d)

@@ -400,6 +400,12 @@ int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
  * constant, linear and trilinear modes). Set d->coef = coef to use them. Returns
  * GFGPU_ERR_UNSUPPORTED for other meshes. */
 int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stream_t stream);
+/* FP64 <-> float-float ("pair") conversion of n values on `stream` (device pointers; out / in as
+ * n pairs {h, l} of floats, 8-byte aligned): h = rn_f32(x), l = rn_f32(x - h), the bits of the
+ * F64->F32 conversion instruction, computed on the integer pipe for 2^-74 <= |x| < 2^127; and
+ * x = rn_f64(h + l). |x| within the FP32 range. */
+int gfgpu_pairs_from_f64(const double* x, int64_t n, float* out, gfgpu_stream_t stream);
+int gfgpu_pairs_to_f64(const float* in, int64_t n, double* out, gfgpu_stream_t stream);
 /* Floats of the pair coefficients gfgpu_verlet_precompute_pair writes for this descriptor (0 if no
  * pair path applies). */
 int64_t gfgpu_verlet_pair_coef_floats(const gfgpu_verlet_desc* d);
