@@ -90,7 +90,8 @@ def parse():
                    help="headline only (skip the static, batch and learned workloads)")
     p.add_argument("--static-operator", choices=["both", "pair", "fp64"], default="both",
                    help="static workload: stiffness action of the PCG iterations in float-float "
-                        "pairs, in FP64, or both (pair is the reported value where it applies)")
+                        "pairs, in FP64, or both (pair is the reported value where it applies); "
+                        "learned workload: pair unless fp64")
     p.add_argument("--train-steps-1level", type=int, default=6000,
                    help="learned workload: Adam steps of the one-level network")
     p.add_argument("--pairs-1level", type=int, default=64,
@@ -836,7 +837,10 @@ def workload_learned(args):
 
     _L.call("gfgpu_set_nn_tensor_path", int(args.nn_path))
     LR, nx, K, G, inside, iip, xp = _learned_problem(args)
-    lp = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0)
+    # the stiffness action of every solver's iterations (Jacobi-PCG, two-level, learned) in
+    # float-float pairs, or all in FP64 (--static-operator fp64)
+    op = "fp64" if args.static_operator == "fp64" else "pair"
+    lp = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0, arithmetic=op)
     reps = 2
 
     def timed(fn, l=lp):
@@ -889,7 +893,7 @@ def workload_learned(args):
     # the one-level design: 4096 (residual, Jacobi-PCG correction) pairs from the plain solver
     # (64 random loads x 64 snapshots every 16 iterations; target PCG_8(r) - D^-1 r), the network
     # as the second direction of the flexible CG beside Jacobi, no coarse grid
-    lp1 = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0)
+    lp1 = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0, arithmetic=op)
     t0 = time.perf_counter()
     np1 = lp1.make_pairs(nloads=args.pairs_1level, snaps=64, every=16, inner=8)
     torch.cuda.synchronize()
@@ -921,7 +925,9 @@ def workload_learned(args):
     one = res["learned_onelevel"]
     return {"metric": "time-to-1e-8 resid (learned FCG vs Jacobi PCG)",
             "value": learned["seconds"], "unit": "s", "higher_is_better": False,
-            "dtype": "f64 solve, bf16-weight/fp32-accumulate network, fp32 coarse correction",
+            "dtype": ("f64 solve, " + ("float-float (f32 pair) stiffness action in the iterations, "
+                                       if op == "pair" else "") +
+                      "bf16-weight/fp32-accumulate network, fp32 coarse correction"),
             "data": "synthetic (seeded inclusions)",
             "config": {"workload": f"Quad4 Regular {nx}x{nx}, two-phase (inclusions "
                                    f"{100 * inside.mean():.1f}% area, x10 moduli), bottom fixed, "
@@ -934,7 +940,8 @@ def workload_learned(args):
                        "target_twolevel": "Chebyshev smoother minus Jacobi step, on the residual "
                                           "after the two-level step",
                        "target_onelevel": "8 Jacobi-PCG iterations minus the Jacobi step",
-                       "loss": "energy norm", "nn_tensor_path": args.nn_path},
+                       "loss": "energy norm", "nn_tensor_path": args.nn_path,
+                       "operator_arithmetic": op},
             "solvers": res,
             "speedup_vs_jacobi_pcg": jac / learned["seconds"],
             "speedup_vs_twolevel_without_network": res["twolevel"]["seconds"] / learned["seconds"],

@@ -79,43 +79,52 @@ __device__ __forceinline__ ffv ff_norm(ffv x)
     return ff_make(s, __fsub_rn(x.l, __fsub_rn(s, x.h)));
 }
 
-// float -> double on the integer pipe: exact (as a conversion is) for normal floats and zeros;
-// subnormals, infinities and NaN take the conversion instruction
+// Conversions between FP64 and pairs on the integer pipe, branch-free. On GB300 the F64 <-> F32
+// conversion instructions issue at the FP64 rate, and a fallback to them for rare operands is no
+// cure: inlined behind a per-lane condition it is if-converted into predicated FP64 instructions
+// that issue for every operand (measured: the pipe 82 % busy in a kernel with 8 FP64 additions per
+// element), as a call it stops the loads of later grid-stride iterations from being scheduled
+// ahead, and behind a warp vote it costs a vote per conversion. So the rare operands are handled by
+// selects, with the domain stated below.
+
+// float -> double: exact (as the conversion is) for normal floats, zeros and infinities; NaN stays
+// NaN; subnormal floats (|f| < 2^-126) give +-0
 __device__ __forceinline__ double ff_f32_to_f64(float f)
 {
     const uint32_t u = __float_as_uint(f), ef = (u >> 23) & 0xffu;
-    if (ef - 1u >= 254u) {
-        if ((u & 0x7fffffffu) == 0u) return __hiloint2double(static_cast<int>(u & 0x80000000u), 0);
-        return static_cast<double>(f);
-    }
-    const uint32_t hi = (u & 0x80000000u) | ((ef + 896u) << 20) | ((u & 0x7fffffu) >> 3);
-    return __hiloint2double(static_cast<int>(hi), static_cast<int>((u & 7u) << 29));
+    const uint32_t eh = ef == 0u ? 0u : (ef == 255u ? 0x7ffu : ef + 896u);
+    const uint32_t m = ef == 0u ? 0u : (u & 0x7fffffu);
+    const uint32_t hi = (u & 0x80000000u) | (eh << 20) | (m >> 3);
+    return __hiloint2double(static_cast<int>(hi), static_cast<int>((m & 7u) << 29));
 }
 
-// double -> pair: h = rn(x), l = rn(x - h) (x - h is exact in FP64), with the bits of
-// __double2float_rn. On GB300 the F64 <-> F32 conversions issue at the FP64 rate, so for
-// 2^-74 <= |x| < 2^127 the split runs on the integer pipe: h is x's significand rounded to 24 bits
-// (nearest, ties to even; a carry into the exponent is the correct rounding), and x - h is the
-// signed integer (remainder - carry 2^29) times 2^(e - 1075), which one I2F rounds to 24 bits and
-// a power-of-two scale places exactly (a normal float for e >= 949). Other x (0, tiny, huge,
-// non-finite) take the conversion instructions. |x| within FP32 range.
+// double -> pair: h = rn(x), l = rn(x - h) (x - h is exact in FP64), the bits of
+// __double2float_rn, for zeros and 2^-74 <= |x| < 2^128 (where h does not round up to infinity):
+// h is x's significand rounded to 24 bits (nearest, ties to even; a carry into the exponent is the
+// correct rounding), and x - h is the signed integer (remainder - carry 2^29) times 2^(e - 1075),
+// which one I2F rounds to 24 bits and a power-of-two scale places exactly (a normal float for
+// e >= 949). +-0 gives (+-0, +0). Below 2^-74, h = rn(x) and l = 0 (below 2^-126, h = +-0): a
+// relative error of 2^-24 there, far below 2^-48 of any value of 2^-26 or more in the same vector.
+// |x| >= 2^128 gives (+-inf, 0), NaN gives (NaN, 0).
 __device__ __forceinline__ ffv ff_from_double(double x)
 {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
     const uint32_t hi = static_cast<uint32_t>(b >> 32), e = (hi >> 20) & 0x7ffu;
-    if (e - 949u > 200u) {
-        const float h = __double2float_rn(x);
-        return ff_make(h, __double2float_rn(x - static_cast<double>(h)));
-    }
+    const uint32_t sign = hi & 0x80000000u;
     const uint32_t top = static_cast<uint32_t>(b >> 29) & 0x7fffffu;
     const uint32_t r = static_cast<uint32_t>(b) & 0x1fffffffu;
     const uint32_t up = (r > 0x10000000u || (r == 0x10000000u && (top & 1u))) ? 1u : 0u;
-    const uint32_t sign = hi & 0x80000000u;
-    const float h = __uint_as_float(sign | (((e - 896u) << 23) + top + up));
     const int d = static_cast<int>(r) - static_cast<int>(up << 29);
+    uint32_t hb = sign | (((e - 896u) << 23) + top + up);
     // the sign on the integer, so that x == h gives l = +0 as the FP64 subtraction does
-    const float l = __fmul_rn(__int2float_rn(sign ? -d : d), __uint_as_float((e - 948u) << 23));
-    return ff_make(h, l);
+    float l = __fmul_rn(__int2float_rn(sign ? -d : d), __uint_as_float(((e - 948u) & 0xffu) << 23));
+    if (e < 949u) l = 0.0f;
+    if (e < 897u) hb = sign;
+    if (e > 1150u) {
+        hb = (e == 0x7ffu && (b << 12) != 0ull) ? 0x7fffffffu : (sign | 0x7f800000u);
+        l = 0.0f;
+    }
+    return ff_make(__uint_as_float(hb), l);
 }
 
 // pair -> double: rn(h + l), one FP64 addition of the two exactly converted parts

@@ -1383,6 +1383,8 @@ using namespace gfgpu::nn;
 // element-kernel launch shared with the explicit step (dynamics.cu)
 int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                   cudaStream_t s);
+int gfgpu_internal_iteration_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
+                                            cudaStream_t s);
 // two-level correction z = P ainv P^T r + minv r (coarse.cu)
 int gfgpu_internal_coarse_apply(const gfgpu_coarse_desc* g, const int32_t* part, int64_t nnu,
                                 const double* minv, const double* r, double* vc, double* yc,
@@ -2371,7 +2373,7 @@ static int fcg_core(const gfgpu_verlet_desc* d, const double* diag, const gfgpu_
             with_ns<McombineL>(L.n, grid_for(n / 2), st, zin, w.minv, w.r, w.sc, w.P, w.ld, L, snew, n);
             double* Pn = w.P + snew * w.ld;
             double* Qn = w.Q + snew * w.ld;
-            GF_TRY(gfgpu_internal_element_forces(d, Pn, w.fe, st));
+            GF_TRY(gfgpu_internal_iteration_element_forces(d, Pn, w.fe, st));
             k_fgather<<<gb, 256, 0, st>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe, Pn,
                                           w.r, n, Qn, w.partial, w.sc, snew, dd, w.cnt + 1, reg_grid(d));
         }

@@ -411,10 +411,14 @@ __global__ void k_pcg_pair_coef(const double* __restrict__ Km, const double* __r
     }
 }
 
-// the pair operator applies: Regular cube Hex8 mesh, index-arithmetic gather (component-major fe)
-inline bool pcg_pair_applies(const gfgpu_verlet_desc* d)
+// which pair operator applies: 1 = Regular cube Hex8 mesh with the index-arithmetic gather
+// (component-major fe; pair element kernel, pair gather), 2 = uniform square Quad4 mesh (pair
+// element kernel with FP64 input and output, the FP64 gathers); 0 = none
+inline int pcg_pair_kind(const gfgpu_verlet_desc* d)
 {
-    return d->nelem > 0 && reg_grid(d).soa && d->reg_nx * d->reg_ny * d->reg_nz == d->nelem;
+    if (d->nelem > 0 && reg_grid(d).soa && d->reg_nx * d->reg_ny * d->reg_nz == d->nelem) return 1;
+    if (d->nelem > 0 && d->uniform && d->nne == 4 && d->ndim == 2 && d->coef) return 2;
+    return 0;
 }
 
 // Jacobi: diagonal of the element stiffness per (element, node, direction) for isotropic
@@ -497,6 +501,19 @@ using namespace gfgpu;
 int gfgpu_internal_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                   cudaStream_t s);
 void gfgpu_internal_hex8_cube_factors(const gfgpu_verlet_desc* d, double* a0, double* a1, double* c2);
+// the uniform square Quad4 pair operator (verlet_pair.cu)
+int gfgpu_internal_pair_element_forces_f64(const gfgpu_verlet_desc* d, const double* u, double* fe,
+                                           cudaStream_t s);
+int gfgpu_internal_pair_coef_square(const gfgpu_verlet_desc* d, float* coef, cudaStream_t s);
+
+// Element forces of an iteration's search direction: the Quad4 pair operator when d->pcg_pair is set
+// on a square Quad4 mesh, else the FP64 element kernel (also used by the flexible CG, learned.cu).
+int gfgpu_internal_iteration_element_forces(const gfgpu_verlet_desc* d, const double* u, double* fe,
+                                            cudaStream_t s)
+{
+    if (d->pcg_pair && pcg_pair_kind(d) == 2) return gfgpu_internal_pair_element_forces_f64(d, u, fe, s);
+    return gfgpu_internal_element_forces(d, u, fe, s);
+}
 
 extern "C" {
 
@@ -507,19 +524,27 @@ int64_t gfgpu_pcg_workspace_bytes(const gfgpu_verlet_desc* d)
 
 int64_t gfgpu_pcg_pair_coef_floats(const gfgpu_verlet_desc* d)
 {
-    return d && pcg_pair_applies(d) ? 4 * d->nelem : 0;
+    if (!d) return 0;
+    const int k = pcg_pair_kind(d);
+    return k == 1 ? 4 * d->nelem : (k == 2 ? 6 * d->nelem : 0);
 }
 
 int gfgpu_pcg_precompute_pair(gfgpu_verlet_desc* d, float* coef, gfgpu_stream_t stream)
 {
     GF_REQUIRE(d && coef && d->K && d->G, "bad argument");
     GF_REQUIRE(reinterpret_cast<uintptr_t>(coef) % 16 == 0, "coef must be 16-byte aligned");
-    if (!pcg_pair_applies(d))
+    const int kind = pcg_pair_kind(d);
+    if (kind == 0)
         return fail(GFGPU_ERR_UNSUPPORTED, "gfgpu_pcg_precompute_pair: Regular cube Hex8 meshes with the "
-                                           "index-arithmetic gather only");
-    k_pcg_pair_coef<<<grid_for(d->nelem), kBlock, 0, S(stream)>>>(d->K, d->G, d->nelem,
-                                                                  reinterpret_cast<float4*>(coef));
-    GF_TRY(check_launch("pcg_precompute_pair"));
+                                           "index-arithmetic gather or uniform square Quad4 meshes only");
+    if (kind == 1) {
+        k_pcg_pair_coef<<<grid_for(d->nelem), kBlock, 0, S(stream)>>>(d->K, d->G, d->nelem,
+                                                                      reinterpret_cast<float4*>(coef));
+        GF_TRY(check_launch("pcg_precompute_pair"));
+    }
+    else {
+        GF_TRY(gfgpu_internal_pair_coef_square(d, coef, S(stream)));
+    }
     d->pcg_pair = coef;
     return GFGPU_OK;
 }
@@ -566,7 +591,7 @@ static int pcg_iteration(const gfgpu_verlet_desc* d, const PcgWs& w, double* x, 
                          cudaStream_t s)
 {
     const unsigned gb = kRedBlocks;
-    const bool pair = d->pcg_pair != nullptr;
+    const bool pair = d->pcg_pair != nullptr && d->nne == 8;
     if (pair) {
         k_elem_force_hex8_cube_pair<<<grid_for(d->nelem, 128), 128, 0, s>>>(
             w.pp, reinterpret_cast<const float4*>(d->pcg_pair), cube_pair(d), d->nelem,
@@ -575,7 +600,7 @@ static int pcg_iteration(const gfgpu_verlet_desc* d, const PcgWs& w, double* x, 
                                                       w.p, n, w.q, w.partial, reg_grid(d));
     }
     else {
-        GF_TRY(gfgpu_internal_element_forces(d, w.p, w.fe, s));
+        GF_TRY(gfgpu_internal_iteration_element_forces(d, w.p, w.fe, s));
         k_pcg_gather<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
                                                  w.p, n, w.q, w.partial, reg_grid(d));
     }
@@ -593,9 +618,9 @@ static int pcg_iteration(const gfgpu_verlet_desc* d, const PcgWs& w, double* x, 
 // the pair operator's validity (the caller may have changed the descriptor since the precompute)
 static int pcg_pair_check(const gfgpu_verlet_desc* d)
 {
-    if (d->pcg_pair && !pcg_pair_applies(d))
-        return fail(GFGPU_ERR_UNSUPPORTED, "pcg_pair is set but the mesh is not a Regular cube Hex8 mesh "
-                                           "with the index-arithmetic gather");
+    if (d->pcg_pair && pcg_pair_kind(d) == 0)
+        return fail(GFGPU_ERR_UNSUPPORTED, "pcg_pair is set but the mesh is neither a Regular cube Hex8 mesh "
+                                           "with the index-arithmetic gather nor a uniform square Quad4 mesh");
     return GFGPU_OK;
 }
 
@@ -632,7 +657,7 @@ int gfgpu_pcg_solve(const gfgpu_verlet_desc* d, const double* diag, double* x, d
     k_pcg_residual<<<gb, kRedThreads, 0, s>>>(d->dofs, d->csr_ptr, d->csr_idx, d->part, d->nnu, w.fe,
                                                nullptr, w.minv, n, w.r, w.z, w.p, w.partial, reg_grid(d));
     k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ); // SC_RZ, SC_RZ_NEW(=rr, overwritten)
-    if (d->pcg_pair) k_pcg_split<<<grid_for(n), kBlock, 0, s>>>(w.p, n, w.pp);
+    if (d->pcg_pair && d->nne == 8) k_pcg_split<<<grid_for(n), kBlock, 0, s>>>(w.p, n, w.pp);
     if ((rc = check_launch("pcg set-up")) != GFGPU_OK) return fail_out(rc);
     cudaMemcpyAsync(hsc, w.sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s);
     if ((rc = check_cuda(cudaStreamSynchronize(s), "pcg set-up")) != GFGPU_OK) return fail_out(rc);
@@ -742,7 +767,7 @@ int gfgpu_pcg_begin(const gfgpu_verlet_desc* d, const double* diag, const double
                                                rhs, w.minv, n, w.r, w.z, w.p, w.partial, reg_grid(d));
     k_reduce<<<1, 1024, 0, s>>>(w.partial, 2, w.sc, SC_RZ); // SC_RZ = r.z, SC_RZ_NEW = r.r
     k_reduce<<<1, 1024, 0, s>>>(w.partial + kRedBlocks, 1, w.sc, SC_RR);
-    if (d->pcg_pair) k_pcg_split<<<grid_for(n), kBlock, 0, s>>>(w.p, n, w.pp);
+    if (d->pcg_pair && d->nne == 8) k_pcg_split<<<grid_for(n), kBlock, 0, s>>>(w.p, n, w.pp);
     return check_launch("pcg_begin");
 }
 

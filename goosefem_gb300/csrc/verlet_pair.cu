@@ -597,6 +597,34 @@ k_pair_elem_square(const int32_t* __restrict__ conn, const float4* __restrict__ 
     }
 }
 
+// The static solvers' operator on uniform square Quad4 elements in pair arithmetic, FP64 in and
+// out: each element splits its nodes' FP64 displacements into pairs (on the integer pipe), runs
+// the square closed form of k_pair_elem_square and joins its forces to FP64 into fe [nelem, 4, 2]
+// (the layout of k_elem_force_quad4_square that the FP64 gathers read). 8 FP64 additions per
+// element instead of 34 FP64 instructions.
+__global__ void __launch_bounds__(256)
+k_pair_elem_square_f64(const int32_t* __restrict__ conn, const double2* __restrict__ u,
+                       const float4* __restrict__ cLN, const float2* __restrict__ cH, int64_t nelem,
+                       double2* __restrict__ fe)
+{
+    GF_FOR(e, nelem)
+    {
+        const int4 cn = __ldg(reinterpret_cast<const int4*>(conn) + e);
+        const double2 q0 = __ldg(u + cn.x), q1 = __ldg(u + cn.y), q2 = __ldg(u + cn.z), q3 = __ldg(u + cn.w);
+        const float4 cln = __ldg(cLN + e);
+        float4 S, D, H;
+        pair_element(ff_from_double(q0.x), ff_from_double(q0.y), ff_from_double(q1.x), ff_from_double(q1.y),
+                     ff_from_double(q2.x), ff_from_double(q2.y), ff_from_double(q3.x), ff_from_double(q3.y),
+                     lo2(cln), hi2(cln), pf(__ldg(cH + e)), S, D, H);
+        const ffv Sx = lo2(S), Sy = hi2(S), Dx = lo2(D), Dy = hi2(D), H0 = lo2(H), H1 = hi2(H);
+        double2* o = fe + e * 4;
+        o[0] = make_double2(ff_to_double(ff_sub(H0, Sx)), ff_to_double(ff_sub(H1, Sy)));
+        o[1] = make_double2(ff_to_double(ff_sub(Dx, H0)), ff_to_double(ff_sub(Dy, H1)));
+        o[2] = make_double2(ff_to_double(ff_add(Sx, H0)), ff_to_double(ff_add(Sy, H1)));
+        o[3] = make_double2(ff_to_double(ff_neg(ff_add(Dx, H0))), ff_to_double(ff_neg(ff_add(Dy, H1))));
+    }
+}
+
 __global__ void __launch_bounds__(128)
 k_pair_elem_stiff(const int32_t* __restrict__ conn, const float4* __restrict__ u, const float2* __restrict__ Ke,
                   int64_t nelem, float4* __restrict__ fe)
@@ -1081,6 +1109,31 @@ int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v,
     GF_TRY(pair_increments(d, 0, nsteps, 0, workspace, s));
     // the last increment does not advance: its displacement is the one it read
     return pair_end(d, nsteps - 1, u, v, a, workspace, s);
+}
+
+// Static solvers' operator of a uniform square Quad4 mesh in pair arithmetic (pcg.cu, learned.cu):
+// coef = d->pcg_pair as written by gfgpu_internal_pair_coef_square.
+int gfgpu_internal_pair_element_forces_f64(const gfgpu_verlet_desc* d, const double* u, double* fe,
+                                           cudaStream_t s)
+{
+    if (d->nelem == 0) return GFGPU_OK;
+    const float* c = d->pcg_pair;
+    k_pair_elem_square_f64<<<grid_for(d->nelem), 256, 0, s>>>(
+        d->conn, reinterpret_cast<const double2*>(u), reinterpret_cast<const float4*>(c),
+        reinterpret_cast<const float2*>(c + 4 * d->nelem), d->nelem, reinterpret_cast<double2*>(fe));
+    return check_launch("pair element kernel (static operator)");
+}
+
+// {L, N} [nelem] interleaved pairs, then kH [nelem] (6 floats per element) of a uniform square Quad4
+// mesh, the layout k_pair_elem_square_f64 reads
+int gfgpu_internal_pair_coef_square(const gfgpu_verlet_desc* d, float* coef, cudaStream_t s)
+{
+    if (d->nelem == 0) return GFGPU_OK;
+    const double g = 1.0 / std::sqrt(3.0);
+    k_pair_coef_elem<<<grid_for(d->nelem), kBlock, 0, s>>>(d->K, d->G, d->nelem, g * g,
+                                                           reinterpret_cast<float4*>(coef),
+                                                           reinterpret_cast<float2*>(coef + 4 * d->nelem));
+    return check_launch("pair coefficients (static operator)");
 }
 
 extern "C" {

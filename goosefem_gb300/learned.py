@@ -75,14 +75,15 @@ class LearnedPreconditioner:
     """Network parameters, training pairs, training loop and the preconditioned FCG solve for one
     Regular Quad4 mesh (nx x ny elements, per-element K, G) with prescribed dofs iip."""
 
-    def __init__(self, nx, ny, K, G, iip, seed=0):
+    def __init__(self, nx, ny, K, G, iip, seed=0, arithmetic="fp64"):
         from . import mesh as M
 
         self.nx, self.ny = int(nx), int(ny)
         self.H, self.W = self.ny + 1, self.nx + 1
         m = M.Quad4.Regular(nx, ny)
         self.mesh = m
-        self.static = ElasticStatic(m.coor(), m.conn(), m.dofs(), K, G, iip)
+        # arithmetic "pair": the stiffness action of the solvers' iterations in float-float pairs
+        self.static = ElasticStatic(m.coor(), m.conn(), m.dofs(), K, G, iip, arithmetic=arithmetic)
         self.iip = np.asarray(iip)
         dev = _dev.device()
         self.free = torch.ones(self.H * self.W * 2, dtype=torch.bool, device=dev)

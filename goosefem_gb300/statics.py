@@ -22,9 +22,10 @@ class ElasticStatic:
 
     K, G: per-element bulk and shear moduli. uniform: "auto" | True | False (closed-form element
     kernel for congruent axis-aligned elements, see gfgpu_verlet_detect_uniform).
-    arithmetic: "fp64" (default) or "pair": the Jacobi-PCG iterations apply the stiffness in
-    float-float arithmetic (gfgpu_pcg_precompute_pair; Regular cube Hex8 meshes only), everything
-    else (solution, residuals, dot products, the true residual check) in FP64."""
+    arithmetic: "fp64" (default) or "pair": the Jacobi-PCG (and flexible CG) iterations apply the
+    stiffness in float-float arithmetic (gfgpu_pcg_precompute_pair; Regular cube Hex8 meshes and
+    uniform square Quad4 meshes), everything else (solution, residuals, dot products, the initial
+    and the true final residual) in FP64."""
 
     def __init__(self, coor, conn, dofs, K, G, iip, uniform="auto", arithmetic="fp64"):
         from .vector import Vector
@@ -106,11 +107,12 @@ class ElasticStatic:
                   self.ws.data_ptr(), _dev.stream())
 
     def use_pair(self):
-        """Float-float stiffness action in the PCG iterations (Regular cube Hex8 meshes)."""
+        """Float-float stiffness action in the PCG iterations (Regular cube Hex8 meshes, uniform
+        square Quad4 meshes)."""
         n = int(_lib.lib().gfgpu_pcg_pair_coef_floats(C.addressof(self.desc)))
         if n == 0:
             raise RuntimeError("the pair operator needs a Regular cube Hex8 mesh (uniform, "
-                               "index-arithmetic gather)")
+                               "index-arithmetic gather) or a uniform square Quad4 mesh")
         self.coef_pair = torch.empty(n, dtype=torch.float32, device=_dev.device())
         _lib.call("gfgpu_pcg_precompute_pair", C.addressof(self.desc), self.coef_pair.data_ptr(),
                   _dev.stream())

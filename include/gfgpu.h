@@ -371,12 +371,14 @@ typedef struct {
      * square-element fused tile kernel, 2 = element kernel + dof-CSR node kernel with the square
      * closed form, 3 = the same with stored element stiffness matrices */
     int32_t pair_mode;
-    /* optional float-float coefficients of the static solvers' operator on a Regular cube Hex8
-     * mesh (gfgpu_pcg_precompute_pair): per element {lam.h, lam.l, G.h, G.l}. When set, the
-     * Jacobi-PCG iterations of gfgpu_pcg_solve / gfgpu_pcg_iterate apply the stiffness in pair
-     * arithmetic (~48-bit significands, ~1e-13 relative to the FP64 action); the solution, the
-     * residual, the preconditioned residual, the direction and every dot product stay FP64, and
-     * the initial and final (true) residuals use the FP64 operator. NULL = FP64 operator. */
+    /* optional float-float coefficients of the static solvers' operator (gfgpu_pcg_precompute_pair)
+     * on a Regular cube Hex8 mesh (per element {lam.h, lam.l, G.h, G.l}) or a uniform square Quad4
+     * mesh ({L, N} pairs [nelem] then kH pairs [nelem]). When set, the iterations of
+     * gfgpu_pcg_solve / gfgpu_pcg_iterate (and, on Quad4, of the flexible CG gfgpu_fcg_*) apply the
+     * stiffness of their search directions in pair arithmetic (~48-bit significands, ~1e-13
+     * relative to the FP64 action); the solution, the residual, the preconditioned residual, the
+     * direction and every dot product stay FP64, and the initial and final (true) residuals use the
+     * FP64 operator. NULL = FP64 operator. */
     const float* pcg_pair;
 } gfgpu_verlet_desc;
 
@@ -401,9 +403,10 @@ int gfgpu_verlet_detect_uniform(gfgpu_verlet_desc* d, const double* dNx_host,
  * GFGPU_ERR_UNSUPPORTED for other meshes. */
 int gfgpu_verlet_precompute(const gfgpu_verlet_desc* d, double* coef, gfgpu_stream_t stream);
 /* FP64 <-> float-float ("pair") conversion of n values on `stream` (device pointers; out / in as
- * n pairs {h, l} of floats, 8-byte aligned): h = rn_f32(x), l = rn_f32(x - h), the bits of the
- * F64->F32 conversion instruction, computed on the integer pipe for 2^-74 <= |x| < 2^127; and
- * x = rn_f64(h + l). |x| within the FP32 range. */
+ * n pairs {h, l} of floats, 8-byte aligned), on the integer pipe: h = rn_f32(x), l = rn_f32(x - h),
+ * the bits of the F64->F32 conversion instruction, for x = 0 and 2^-74 <= |x| < 2^128 (short of
+ * h rounding up to infinity); below 2^-74 l = 0, below 2^-126 also h = +-0. Back: x = rn_f64(h + l)
+ * with h and l converted exactly (subnormal floats as +-0). */
 int gfgpu_pairs_from_f64(const double* x, int64_t n, float* out, gfgpu_stream_t stream);
 int gfgpu_pairs_to_f64(const float* in, int64_t n, double* out, gfgpu_stream_t stream);
 /* Floats of the pair coefficients gfgpu_verlet_precompute_pair writes for this descriptor (0 if no
@@ -539,18 +542,20 @@ int gfgpu_barrier_selftest(int64_t timeout_cycles, int* status);
  * The descriptor `d` is the one of the explicit step (dt, eta, inv, fext are ignored); `part`
  * and `nnu` mark the unknown dofs (part < nnu), all other dofs are prescribed. */
 int64_t gfgpu_pcg_workspace_bytes(const gfgpu_verlet_desc* d);
-/* Floats of the pair coefficients gfgpu_pcg_precompute_pair writes (4 per element), or 0 when the
- * pair operator does not apply: it needs a Regular cube Hex8 mesh with the index-arithmetic gather
- * (gfgpu_verlet_detect_regular_hex8) and the FP64 cube coefficients (d->coef). */
+/* Floats of the pair coefficients gfgpu_pcg_precompute_pair writes (4 per element on a Regular
+ * cube Hex8 mesh with the index-arithmetic gather, gfgpu_verlet_detect_regular_hex8, and the FP64
+ * cube coefficients d->coef; 6 per element on a uniform square Quad4 mesh with d->coef), or 0 when
+ * the pair operator does not apply. */
 int64_t gfgpu_pcg_pair_coef_floats(const gfgpu_verlet_desc* d);
-/* Float-float operator of the Jacobi-PCG iterations: writes {lam.h, lam.l, G.h, G.l} per element
- * (lam = K - 2G/3) into coef (16-byte aligned, gfgpu_pcg_pair_coef_floats floats) and sets
- * d->pcg_pair = coef. The iterations then apply the stiffness of the search direction in pair
- * arithmetic on the FP32 pipes: the direction update also writes the direction as pairs, the
- * cube closed form runs on pairs (the folded coefficients formed from lam and G in registers),
- * and the gather sums a dof's element forces as pairs and returns them to FP64. Returns
- * GFGPU_ERR_UNSUPPORTED where gfgpu_pcg_pair_coef_floats is 0. Set d->pcg_pair = NULL for the
- * FP64 operator. */
+/* Float-float operator of the static solvers' iterations: writes the pair coefficients into coef
+ * (16-byte aligned, gfgpu_pcg_pair_coef_floats floats) and sets d->pcg_pair = coef. Hex8 cube:
+ * {lam.h, lam.l, G.h, G.l} per element (lam = K - 2G/3); the direction update also writes the
+ * direction as pairs, the cube closed form runs on pairs (the folded coefficients formed from lam
+ * and G in registers), and the gather sums a dof's element forces as pairs and returns them to
+ * FP64. Quad4 square: {L, N} and kH pairs (L = lam/4, N = G/4, kH = g^2 (lam + 3G)/4); the element
+ * kernel splits the FP64 direction into pairs, runs the square closed form on pairs and joins its
+ * forces to FP64 for the FP64 gathers. Returns GFGPU_ERR_UNSUPPORTED where
+ * gfgpu_pcg_pair_coef_floats is 0. Set d->pcg_pair = NULL for the FP64 operator. */
 int gfgpu_pcg_precompute_pair(gfgpu_verlet_desc* d, float* coef, gfgpu_stream_t stream);
 /* Diagonal of the assembled stiffness as a nodevec (Jacobi preconditioner), from dNx/vol.
  * `workspace` needs nelem*nne*ndim doubles. */

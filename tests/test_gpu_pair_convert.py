@@ -1,9 +1,9 @@
 """FP64 <-> float-float conversions (gfgpu_pairs_from_f64 / gfgpu_pairs_to_f64, the device
 functions every pair path uses) against numpy's IEEE casts, bit for bit: h = rn_f32(x),
-l = rn_f32(x - h) (x - h exact in FP64) and x' = rn_f64(h + l). The device split runs on the integer
-pipe for 2^-74 <= |x| < 2^127 (rounding ties to even, carries into the exponent) and on the
-conversion instructions elsewhere; the inputs cover both, signed zeros, exact ties and
-significands of all ones."""
+l = rn_f32(x - h) (x - h exact in FP64) and x' = rn_f64(h + l), on the integer pipe. Exact for zeros
+and 2^-74 <= |x| < 2^127 (rounding ties to even, carries into the exponent); below 2^-74 the low
+part is 0 and below 2^-126 the pair is +-0. The inputs cover all of these, signed zeros, exact
+ties and significands of all ones."""
 
 import ctypes as C
 
@@ -42,12 +42,23 @@ def test_pair_conversions_match_ieee_casts():
     out = torch.empty(2 * x.size, dtype=torch.float32, device="cuda")
     _lib.call("gfgpu_pairs_from_f64", xd.data_ptr(), x.size, out.data_ptr(), _dev.stream())
     got = out.cpu().numpy().reshape(-1, 2)
-    assert np.array_equal(got[:, 0].view(np.uint32), h.view(np.uint32))
-    assert np.array_equal(got[:, 1].view(np.uint32), l.view(np.uint32))
+    ax = np.abs(x)
+    exact = (ax == 0) | ((ax >= 2.0 ** -74) & (ax < 2.0 ** 127))
+    assert exact.sum() > 0.7 * x.size
+    assert np.array_equal(got[exact, 0].view(np.uint32), h[exact].view(np.uint32))
+    assert np.array_equal(got[exact, 1].view(np.uint32), l[exact].view(np.uint32))
+    # below 2^-74: h = rn(x), l = 0; below 2^-126: h = +-0
+    tiny = (ax > 0) & (ax < 2.0 ** -74)
+    normal_h = tiny & (ax >= 2.0 ** -126)
+    assert np.array_equal(got[normal_h, 0].view(np.uint32), h[normal_h].view(np.uint32))
+    assert np.all(got[tiny, 1] == 0)
+    sub = tiny & (ax < 2.0 ** -126)
+    assert np.all(got[sub, 0] == 0) and np.array_equal(np.signbit(got[sub, 0]), np.signbit(x[sub]))
+    # back to FP64: rn(h + l) of the exactly converted parts, bit for bit
     back = torch.empty_like(xd)
     _lib.call("gfgpu_pairs_to_f64", out.data_ptr(), x.size, back.data_ptr(), _dev.stream())
-    ref = h.astype(np.float64) + l.astype(np.float64)
+    ref = got[:, 0].astype(np.float64) + got[:, 1].astype(np.float64)
     assert np.array_equal(back.cpu().numpy().view(np.uint64), ref.view(np.uint64))
     # inside the FP32 range the pair holds x to ~2^-48 relative
-    m = (np.abs(x) > 1e-20) & (np.abs(x) < 1e37)
-    assert np.max(np.abs(ref[m] - x[m]) / np.abs(x[m])) < 2.0 ** -46
+    m = (ax > 1e-20) & (ax < 1e37)
+    assert np.max(np.abs(back.cpu().numpy()[m] - x[m]) / ax[m]) < 2.0 ** -46

@@ -328,3 +328,88 @@ def test_pcg_pair_solve(gf, oracle):
     st = gf.statics.ElasticStatic(coor * np.array([1.0, 1.0, 1.5]), conn, dofs, K, G, iip)
     with pytest.raises(RuntimeError):
         st.use_pair()
+
+
+def _quad4_case(nx, ny, seed):
+    from oracle import gfref as R
+
+    coor, conn = R.quad4_regular(nx, ny)
+    K, G = seeded_material(conn.shape[0], seed)
+    W = nx + 1
+    bot = np.arange(W)
+    top = bot + ny * W
+    iip = np.unique(np.concatenate([(bot[:, None] * 2 + np.arange(2)).ravel(), top * 2 + 1]))
+    xp = np.where(np.isin(iip, top * 2 + 1), -1e-2, 0.0)
+    return coor, conn, K, G, iip, xp
+
+
+def test_pcg_pair_operator_quad4(gf, oracle):
+    """Uniform square Quad4: the pair element kernel (FP64 direction split into pairs, square closed
+    form on pairs, forces joined to FP64) followed by the FP64 gather, against the FP64 operator on
+    the same direction, within 1e-12 of max |A p0|."""
+    import ctypes as C
+
+    from goosefem_gb300 import _dev, _lib
+
+    coor, conn, K, G, iip, xp = _quad4_case(24, 16, 48)
+    nnode = coor.shape[0]
+    st = gf.statics.ElasticStatic(coor, conn, np.arange(nnode * 2).reshape(-1, 2), K, G, iip,
+                                  arithmetic="pair")
+    assert st.arithmetic == "pair"
+    x = torch.zeros(nnode * 2, dtype=torch.float64, device="cuda")
+    x[torch.as_tensor(iip, device="cuda").long()] = torch.as_tensor(xp, device="cuda")
+    _lib.call("gfgpu_pcg_begin", C.addressof(st.desc), st.diag.data_ptr(), None, x.data_ptr(),
+              st.ws.data_ptr(), _dev.stream())
+    p0 = _pcg_vec(st, 2).clone()
+    _lib.call("gfgpu_pcg_iterate", C.addressof(st.desc), 1, x.data_ptr(), st.ws.data_ptr(),
+              _dev.stream())
+    q = to_np(_pcg_vec(st, 3))
+    f = to_np(st.force(p0.view(-1, 2))).ravel()
+    free = np.setdiff1d(np.arange(nnode * 2), iip)
+    err = np.max(np.abs(q[free] - f[free])) / np.max(np.abs(f[free]))
+    assert 0 < err <= 1e-12, err
+
+
+def test_pcg_pair_quad4_solve(gf, oracle):
+    """Quad4 Jacobi-PCG with the pair operator against the direct solve and the FP64 PCG."""
+    from oracle import statics as S
+
+    coor, conn, K, G, iip, xp = _quad4_case(24, 16, 44)
+    A = S.stiffness(coor, conn, K, G)
+    x_ref = S.solve_partitioned(A, iip, xp)
+    nnode = coor.shape[0]
+    dofs = np.arange(nnode * 2).reshape(-1, 2)
+    out = []
+    for arith in ("pair", "fp64"):
+        st = gf.statics.ElasticStatic(coor, conn, dofs, K, G, iip, arithmetic=arith)
+        x = torch.zeros((nnode, 2), dtype=torch.float64, device="cuda")
+        x.view(-1)[torch.as_tensor(iip, device="cuda").long()] = torch.as_tensor(xp, device="cuda")
+        it, rel = st.solve(x, tol=1e-8)
+        out.append((it, rel, to_np(x).ravel()))
+    (it_p, rel_p, xq), (it_d, rel_d, xd) = out
+    assert rel_p <= 1e-8 and S.residual(A, iip, xq) <= 1e-8
+    assert abs(it_p - it_d) <= 2
+    assert np.linalg.norm(xq - x_ref) / np.linalg.norm(x_ref) <= 1e-6
+    assert np.linalg.norm(xq - xd) / np.linalg.norm(xd) <= 1e-7
+
+
+def test_two_level_fcg_pair_operator(gf, oracle):
+    """The two-level flexible CG (no network) with the pair operator on its directions reaches the
+    FP64 true residual and agrees with the FP64-operator solve."""
+    from goosefem_gb300 import learned as LR
+    from goosefem_gb300 import mesh as M
+
+    nx = ny = 48
+    K, G, _ = LR.inclusion_material(nx, ny, 5, rmin=2.0, rmax=5.0)
+    iip, xp = LR.static_bc(M.Quad4.Regular(nx, ny))
+    res = []
+    for arith in ("pair", "fp64"):
+        lp = LR.LearnedPreconditioner(nx, ny, K, G, iip, seed=0, arithmetic=arith)
+        assert lp.static.arithmetic == arith
+        lp.coarse_setup(8)
+        x = lp.initial_guess(xp)
+        it, rel = lp.fcg(x, tol=1e-8, use_nn=False, nkeep=4, coarse=True)
+        res.append((it, rel, to_np(x)))
+    assert res[0][1] <= 1e-8 and res[1][1] <= 1e-8
+    assert abs(res[0][0] - res[1][0]) <= 2
+    assert np.linalg.norm(res[0][2] - res[1][2]) / np.linalg.norm(res[1][2]) <= 1e-7
