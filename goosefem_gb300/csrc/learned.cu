@@ -23,6 +23,7 @@
 #include <numeric>
 
 #include "common.cuh"
+#include "ffpair.cuh"
 
 namespace gfgpu {
 namespace nn {
@@ -559,8 +560,9 @@ k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict_
                 const float v1 = c[mt][0][2 * half + 1] + bias[1];
                 if (z) {
                     const double sg = s_sigma;
-                    z[2 * p] = part[2 * p] < nnu ? sg * static_cast<double>(v0) : 0.0;
-                    z[2 * p + 1] = part[2 * p + 1] < nnu ? sg * static_cast<double>(v1) : 0.0;
+                    // exact float -> double on the integer pipe (ffpair.cuh)
+                    z[2 * p] = part[2 * p] < nnu ? sg * ff_f32_to_f64(v0) : 0.0;
+                    z[2 * p + 1] = part[2 * p + 1] < nnu ? sg * ff_f32_to_f64(v1) : 0.0;
                 }
                 else {
                     *reinterpret_cast<float2*>(Yf + 2 * p) = make_float2(v0, v1);
@@ -585,7 +587,7 @@ k_conv_mma(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict_
 // BF16 into a shared halo tile [18][18][4]; K = 3 steps of 4 taps x 4 channels. Output BF16
 // [H, W, 32]. Same tile and warp layout as k_conv_mma.
 template <bool PLANAR_OUT = false>
-__global__ void __launch_bounds__(kMmaThreads)
+__global__ void __launch_bounds__(kMmaThreads, 4)
 k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_slot, double nfree,
             const float* __restrict__ mat, const float* __restrict__ X0,
             const __nv_bfloat16* __restrict__ WF, const float* __restrict__ bias, int H, int Wd,
@@ -612,8 +614,10 @@ k_first_mma(const double* __restrict__ r, const double* __restrict__ sc, int rr_
             if (r) {
                 double2 rv = *reinterpret_cast<const double2*>(r + 2 * q);
                 float2 mv = *reinterpret_cast<const float2*>(mat + 2 * q);
-                v[0] = static_cast<float>(rv.x) * inv;
-                v[1] = static_cast<float>(rv.y) * inv;
+                // rn_f32 of the FP64 residual on the integer pipe (ffpair.cuh; the conversion
+                // instruction issues at the FP64 rate)
+                v[0] = ff_from_double(rv.x).h * inv;
+                v[1] = ff_from_double(rv.y).h * inv;
                 v[2] = mv.x;
                 v[3] = mv.y;
             }
