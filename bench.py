@@ -870,6 +870,9 @@ def workload_learned(args):
         res[f"twolevel_check{ce}"] = {"seconds": b[0], "iterations": b[1], "relres_true": b[2]}
     res["twolevel"] = min((v for k, v in res.items() if k.startswith("twolevel_check")),
                           key=lambda v: v["seconds"])
+    # the training pairs come from solves with the FP64 stiffness action (the network learns the
+    # solver of the reference's arithmetic); the timed solves use `op`
+    lp.static.use_fp64()
     t0 = time.perf_counter()
     npairs = lp.make_pairs_twolevel(nloads=args.nloads, snaps=64, every=4, target="cheb",
                                     degree=args.cheb_degree, post=True)
@@ -880,6 +883,8 @@ def workload_learned(args):
                       log_every=max(args.train_steps // 10, 1))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
+    if op == "pair":
+        lp.static.use_pair()
     for nkeep in (1, 2, 4):
         for ce in (2, 4):
             b = best_of(lambda x: lp.solve(x, nkeep=nkeep, check_every=ce))
@@ -893,7 +898,7 @@ def workload_learned(args):
     # the one-level design: 4096 (residual, Jacobi-PCG correction) pairs from the plain solver
     # (64 random loads x 64 snapshots every 16 iterations; target PCG_8(r) - D^-1 r), the network
     # as the second direction of the flexible CG beside Jacobi, no coarse grid
-    lp1 = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0, arithmetic=op)
+    lp1 = LR.LearnedPreconditioner(nx, nx, K, G, iip, seed=0)  # FP64 action for the pairs
     t0 = time.perf_counter()
     np1 = lp1.make_pairs(nloads=args.pairs_1level, snaps=64, every=16, inner=8)
     torch.cuda.synchronize()
@@ -904,6 +909,8 @@ def workload_learned(args):
     torch.cuda.synchronize()
     t_train1 = time.perf_counter() - t0
     lp1.R = lp1.T = None
+    if op == "pair":
+        lp1.static.use_pair()
     # ring of 8 directions (shorter rings needed up to 20x more iterations in trial runs); the
     # iteration cap bounds the time of a network that does not help
     cap = 4 * res["jacobi_pcg"]["iterations"]
