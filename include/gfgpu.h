@@ -427,7 +427,9 @@ int64_t gfgpu_verlet_pair_coef_floats(const gfgpu_verlet_desc* d);
  *      closed form) + dof-CSR node kernel per increment; coef_pair: {L, N} per element, then kH
  *      per element;
  *  3 = any Quad4 mesh with the Gauss rule (d->dNx, d->vol): the element stiffness matrices
- *      (36 pairs per element, [36][nelem]) times u_e + the dof-CSR node kernel.
+ *      times u_e + the dof-CSR node kernel; coef_pair: the 6 off-diagonal 2 x 2 node blocks of
+ *      each K_e (24 pairs per element, [24][nelem]; the diagonal blocks follow from translation
+ *      invariance, f_m = sum_{n != m} K_mn (u_n - u_m)).
  * In paths 2 and 3 without mass classes the pair inverse masses [nnu] follow. Other meshes return
  * GFGPU_ERR_UNSUPPORTED. Strict mode ignores coef_pair. */
 int gfgpu_verlet_precompute_pair(gfgpu_verlet_desc* d, float* coef_pair, gfgpu_stream_t stream);
