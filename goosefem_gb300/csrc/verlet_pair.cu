@@ -689,6 +689,9 @@ struct PairCsrStep {
     float2 *u, *v, *a;      // per nodevec entry
     float2 dt, h, cc, eta;
     int advance;
+    // Mesh::Quad4::Regular(reg_nx, reg_ny) numbering with plain dofs (gfgpu_verlet_detect_regular):
+    // a dof's element forces found by index arithmetic in the CSR's order (same bits, no tables)
+    int64_t reg_nx, reg_ny;
 };
 
 __global__ void __launch_bounds__(256)
@@ -708,12 +711,31 @@ k_pair_node_csr(const PairCsrStep p, const __grid_constant__ PairClassTab tab)
     const ffv dt = pf(p.dt), h = pf(p.h), cc = pf(p.cc);
     GF_FOR(t, p.n)
     {
-        const int32_t d = __ldg(p.dofs + t);
-        const int32_t b = __ldg(p.ptr + d), en = __ldg(p.ptr + d + 1);
         ffv f = ff_make(0.f, 0.f);
-        for (int32_t j = b; j < en; ++j) {
-            const ffv g = pf(__ldg(p.fe + __ldg(p.idx + j)));
-            f = j == b ? g : ff_add(f, g);
+        if (p.reg_nx > 0) {
+            // node (ix, iy): elements (ix-1, iy-1) node 2, (ix, iy-1) node 3, (ix-1, iy) node 1,
+            // (ix, iy) node 0, i.e. ascending flat elemvec index as in the CSR
+            const uint32_t nx = static_cast<uint32_t>(p.reg_nx), ny = static_cast<uint32_t>(p.reg_ny);
+            const uint32_t tt = static_cast<uint32_t>(t), node = tt >> 1, i = tt & 1u, W = nx + 1u;
+            const uint32_t iy = node / W, ix = node - iy * W;
+            bool first = true;
+            auto add = [&](uint32_t e, uint32_t m) {
+                const ffv g = pf(__ldg(p.fe + (e * 4u + m) * 2u + i));
+                f = first ? g : ff_add(f, g);
+                first = false;
+            };
+            if (iy > 0u && ix > 0u) add((iy - 1u) * nx + ix - 1u, 2u);
+            if (iy > 0u && ix < nx) add((iy - 1u) * nx + ix, 3u);
+            if (iy < ny && ix > 0u) add(iy * nx + ix - 1u, 1u);
+            if (iy < ny && ix < nx) add(iy * nx + ix, 0u);
+        }
+        else {
+            const int32_t d = __ldg(p.dofs + t);
+            const int32_t b = __ldg(p.ptr + d), en = __ldg(p.ptr + d + 1);
+            for (int32_t j = b; j < en; ++j) {
+                const ffv g = pf(__ldg(p.fe + __ldg(p.idx + j)));
+                f = j == b ? g : ff_add(f, g);
+            }
         }
         f = ff_norm(f);
         const ffv fx = p.fext ? pf(__ldg(p.fext + t)) : ff_make(0.f, 0.f);
@@ -1019,6 +1041,8 @@ static int pair_increments(const gfgpu_verlet_desc* d, int64_t first, int64_t co
     if (d->pair_mode != 1) {
         float4* fe = pair_fe(d, workspace);
         PairCsrStep q;
+        q.reg_nx = (d->reg_nz == 0 && d->nne == 4) ? d->reg_nx : 0;
+        q.reg_ny = d->reg_ny;
         q.dofs = d->dofs;
         q.ptr = d->csr_ptr;
         q.idx = d->csr_idx;

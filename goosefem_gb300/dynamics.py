@@ -150,8 +150,7 @@ class VelocityVerlet:
             d.coef = self.coef.data_ptr()
         self.classify()
         if nne == 4:
-            self._detect_regular(coor.detach().cpu().numpy() if isinstance(coor, torch.Tensor)
-                                 else np.asarray(coor))
+            self._detect_regular(conn_h)
         self.coef_pair = None
         if arithmetic == "pair":
             self.use_pair()
@@ -205,13 +204,14 @@ class VelocityVerlet:
             self._mclass = None
             return False
 
-    def _detect_regular(self, coor):
+    def _detect_regular(self, conn):
         """Mesh::Quad4::Regular numbering (gfgpu_verlet_detect_regular, checked on the device):
-        nx + 1 = the leading run of nodes at the first node's y."""
-        y = coor[:, 1]
-        run = int(np.argmax(y != y[0])) if np.any(y != y[0]) else y.size
-        nx = run - 1
-        if nx > 0 and self.desc.nelem % nx == 0:
+        the first element (0, 1, nx + 2, nx + 1) gives nx; the coordinates play no part, so a
+        distorted Regular mesh is found too."""
+        c0 = conn[0]
+        nx = int(c0[3]) - 1
+        if (nx > 0 and int(c0[0]) == 0 and int(c0[1]) == 1 and int(c0[2]) == nx + 2
+                and self.desc.nelem % nx == 0):
             _lib.call("gfgpu_verlet_detect_regular", C.addressof(self.desc), nx,
                       self.desc.nelem // nx, _dev.stream())
         return self.desc.reg_nx > 0

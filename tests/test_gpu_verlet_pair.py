@@ -153,6 +153,15 @@ def test_pair_csr_paths(gf, oracle, case):
     for g, r, h in zip(s, s64, s2):
         assert rel_err(to_np(g), to_np(r)) <= RTOL
         assert torch.equal(g, h)
+    if not periodic:
+        # a Regular numbering (distorted or not): the node kernel gathers by index arithmetic in
+        # the CSR's order; through the CSR tables it gives the same bits
+        assert vv.desc.reg_nx == 30
+        vv.desc.reg_nx = 0
+        s3 = _state(v0)
+        vv.step(*s3, 60)
+        for g, h in zip(s, s3):
+            assert torch.equal(g, h)
 
 
 def test_pair_refuses_hex8(gf):
