@@ -4,10 +4,11 @@ Every instance has its own size, per-element moduli, fully periodic dofs
 (RegularBase::dofsPeriodic, Mesh.h:291-306) and an applied mean shear (the affine displacement
 of docs/examples/dynamics/Elastic-VelocityVerlet/main.cpp:88-98). The instances are concatenated
 into one block-diagonal mesh (node and dof numbers offset per instance), so one launch covers
-all of them: either a CUDA graph of the two kernels per increment (FP64, mode 0, or float-float
-pairs, mode 2: square closed form + dof-CSR node kernel, gfgpu_verlet_precompute_pair path 2), or
-one persistent cooperative kernel for all increments (FP64, mode 1). `autotune` times them (and
-the persistent block shapes) on a few increments and keeps the fastest.
+all of them: either a CUDA graph of the two kernels per increment (FP64, mode 0; float-float
+pairs, mode 2: square closed form + dof-CSR node kernel, gfgpu_verlet_precompute_pair path 2;
+mixed, mode 3: the pair element kernel on node differences formed in FP64 + the FP64 node
+kernel), or one persistent cooperative kernel for all increments (FP64, mode 1). `autotune` times
+them (and the persistent block shapes) on a few increments and keeps the fastest.
 """
 
 import ctypes as C
@@ -87,6 +88,8 @@ class BatchedVerlet:
             raise RuntimeError("batched instances must be uniform Quad4 meshes")
         nbytes = int(_lib.lib().gfgpu_verlet_persistent_workspace_bytes(C.addressof(self.vv.desc)))
         self.pws = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device=_dev.device())
+        self.vv.use_mixed()  # pair element coefficients for mode 3 (FP64 state)
+        self._mixed_coef = self.vv.desc.pcg_pair
         self.vv.use_pair()  # pair coefficients for mode 2 (square closed form + CSR)
         self._pair_coef = self.vv.desc.coef_pair
         self.vv.use_fp64()
@@ -105,16 +108,18 @@ class BatchedVerlet:
 
     # ------------------------------------------------------------------ execution
     def _arith(self):
-        """The FP64 kernels for modes 0 and 1, the pair kernels for mode 2."""
+        """The FP64 kernels for modes 0 and 1, the pair kernels for mode 2, the pair element kernel
+        with the FP64 node kernel for mode 3."""
         self.vv.desc.coef_pair = self._pair_coef if self.mode == 2 else None
+        self.vv.desc.pcg_pair = self._mixed_coef if self.mode == 3 else None
 
     @property
     def arithmetic(self):
-        return "pair" if self.mode == 2 else "fp64"
+        return {2: "pair", 3: "mixed"}.get(self.mode, "fp64")
 
     def run_direct(self, u, v, a, nsteps):
         self._arith()
-        if self.mode in (0, 2):
+        if self.mode in (0, 2, 3):
             self.vv.step(u, v, a, nsteps)
         else:
             _lib.call("gfgpu_verlet_persistent", C.addressof(self.vv.desc), u.data_ptr(),
@@ -163,8 +168,9 @@ class BatchedVerlet:
         candidate only with pair=True: under the applied shear the displacement is about 600 times
         its fluctuations here, and the pair state's 2^-48 relative rounding of the displacement
         then leaves the velocity ~5e-12 from the FP64 run after 60 increments, beyond the 1e-12
-        agreement the FP64 schedules keep."""
-        cands = [(0, 256, 0)] + ([(2, 256, 0)] if pair else []) + \
+        agreement the FP64 schedules keep. The mixed schedule (mode 3) keeps the state in FP64 and
+        forms the element's node differences in FP64, so the affine part cancels as in FP64."""
+        cands = [(0, 256, 0), (3, 256, 0)] + ([(2, 256, 0)] if pair else []) + \
             [(1, b, bps) for b in (128, 256) for bps in (0, 1, 2)]
         table = []
         best = None

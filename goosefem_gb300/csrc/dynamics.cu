@@ -1097,6 +1097,19 @@ static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, 
     return check_launch("verlet element kernel");
 }
 
+// the square Quad4 element forces in pair arithmetic, FP64 in and out (verlet_pair.cu)
+int gfgpu_internal_pair_element_forces_f64(const gfgpu_verlet_desc* d, const double* u, double* fe,
+                                           cudaStream_t s);
+
+// The explicit step's element kernel: in fast mode with d->pcg_pair set on a uniform square Quad4
+// mesh ("mixed" arithmetic: FP64 state and node update), the pair element kernel; else launch_elem.
+static int launch_elem_step(const gfgpu_verlet_desc* d, const double* u, double* fe, cudaStream_t s)
+{
+    if (d->pcg_pair && !strict_mode() && d->uniform && d->nne == 4 && d->ndim == 2 && d->coef)
+        return gfgpu_internal_pair_element_forces_f64(d, u, fe, s);
+    return launch_elem(d, u, fe, s);
+}
+
 // float-float path of the Regular square Quad4 mesh (verlet_pair.cu)
 int64_t gfgpu_internal_pair_workspace_bytes(const gfgpu_verlet_desc* d);
 int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v, double* a,
@@ -1188,7 +1201,7 @@ static int run_increments(const gfgpu_verlet_desc* d, double* u, double* v, doub
         k_predict<false><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
     GF_TRY(check_launch("verlet predict"));
     for (int64_t it = 0; it < nsteps; ++it) {
-        GF_TRY(launch_elem(d, u, fe, s));
+        GF_TRY(launch_elem_step(d, u, fe, s));
         GF_TRY(launch_node(d, tab, k, fe, it + 1 < nsteps ? 1 : 0, u, v, a, s));
     }
     return GFGPU_OK;

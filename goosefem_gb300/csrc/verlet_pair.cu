@@ -91,6 +91,26 @@ __device__ __forceinline__ void pair_element(ffv u0x, ffv u0y, ffv u1x, ffv u1y,
     H = pack(ff_norm(H0), ff_norm(H1));
 }
 
+// The same closed form from the element's node differences P = u2 - u0, Q = u1 - u3 and
+// D = u0 - u1, E = u2 - u3 (A1 = P + Q, A2 = P - Q, A3 = D + E), given as pairs: a caller that
+// forms them in FP64 from an FP64 displacement keeps the pair rounding at the scale of the
+// differences, not of the displacement (an applied affine field cancels exactly as in FP64).
+__device__ __forceinline__ void pair_element_diff(ffv Px, ffv Py, ffv Qx, ffv Qy, ffv Dx, ffv Dy, ffv Ex,
+                                                  ffv Ey, ffv L, ffv N, ffv kH, float4& S, float4& D, float4& H)
+{
+    const ffv A1x = ff_add(Px, Qx), A2x = ff_sub(Px, Qx);
+    const ffv A1y = ff_add(Py, Qy), A2y = ff_sub(Py, Qy);
+    const ffv A3x = ff_add(Dx, Ex), A3y = ff_add(Dy, Ey);
+    const ffv Lt = ff_mul(L, ff_add(A1x, A2y));
+    const ffv P0 = ff_add(ff_twice(ff_mul(N, A1x)), Lt);
+    const ffv Q1 = ff_add(ff_twice(ff_mul(N, A2y)), Lt);
+    const ffv P1 = ff_mul(N, ff_add(A1y, A2x));
+    const ffv H0 = ff_mul(kH, A3x), H1 = ff_mul(kH, A3y);
+    S = pack(ff_norm(ff_add(P0, P1)), ff_norm(ff_add(P1, Q1)));
+    D = pack(ff_norm(ff_sub(P0, P1)), ff_norm(ff_sub(P1, Q1)));
+    H = pack(ff_norm(H0), ff_norm(H1));
+}
+
 // One velocity-Verlet component update (closed form per mass class, or a prescribed dof).
 __device__ __forceinline__ void pair_update(int c, ffv f, ffv fx, bool has_fext, ffv vn, ffv an,
                                             const float2* smi, const float2* sbe, const float2* sc1,
@@ -616,11 +636,13 @@ k_pair_elem_square(const int32_t* __restrict__ conn, const float4* __restrict__ 
     }
 }
 
-// The static solvers' operator on uniform square Quad4 elements in pair arithmetic, FP64 in and
-// out: each element splits its nodes' FP64 displacements into pairs (on the integer pipe), runs
-// the square closed form of k_pair_elem_square and joins its forces to FP64 into fe [nelem, 4, 2]
-// (the layout of k_elem_force_quad4_square that the FP64 gathers read). 8 FP64 additions per
-// element instead of 34 FP64 instructions.
+// Element forces of uniform square Quad4 elements in pair arithmetic with FP64 input and output
+// (the static solvers' operator and the explicit step's element kernel in "mixed" arithmetic): the
+// node differences of the square closed form are formed in FP64 (8 subtractions), split into pairs
+// on the integer pipe, the closed form runs on pairs (pair_element_diff) and the forces are joined
+// to FP64 into fe [nelem, 4, 2] (the layout of k_elem_force_quad4_square that the FP64 gathers and
+// node kernels read): 16 FP64 instructions per element instead of 34. Forming the differences in
+// FP64 keeps the pair rounding relative to them: an applied affine displacement cancels as in FP64.
 __global__ void __launch_bounds__(256)
 k_pair_elem_square_f64(const int32_t* __restrict__ conn, const double2* __restrict__ u,
                        const float4* __restrict__ cLN, const float2* __restrict__ cH, int64_t nelem,
@@ -632,9 +654,10 @@ k_pair_elem_square_f64(const int32_t* __restrict__ conn, const double2* __restri
         const double2 q0 = __ldg(u + cn.x), q1 = __ldg(u + cn.y), q2 = __ldg(u + cn.z), q3 = __ldg(u + cn.w);
         const float4 cln = __ldg(cLN + e);
         float4 S, D, H;
-        pair_element(ff_from_double(q0.x), ff_from_double(q0.y), ff_from_double(q1.x), ff_from_double(q1.y),
-                     ff_from_double(q2.x), ff_from_double(q2.y), ff_from_double(q3.x), ff_from_double(q3.y),
-                     lo2(cln), hi2(cln), pf(__ldg(cH + e)), S, D, H);
+        pair_element_diff(ff_from_double(q2.x - q0.x), ff_from_double(q2.y - q0.y), ff_from_double(q1.x - q3.x),
+                          ff_from_double(q1.y - q3.y), ff_from_double(q0.x - q1.x), ff_from_double(q0.y - q1.y),
+                          ff_from_double(q2.x - q3.x), ff_from_double(q2.y - q3.y), lo2(cln), hi2(cln),
+                          pf(__ldg(cH + e)), S, D, H);
         const ffv Sx = lo2(S), Sy = hi2(S), Dx = lo2(D), Dy = hi2(D), H0 = lo2(H), H1 = hi2(H);
         double2* o = fe + e * 4;
         o[0] = make_double2(ff_to_double(ff_sub(H0, Sx)), ff_to_double(ff_sub(H1, Sy)));
@@ -1157,7 +1180,8 @@ int gfgpu_internal_verlet_pair(const gfgpu_verlet_desc* d, double* u, double* v,
     return pair_end(d, nsteps - 1, u, v, a, workspace, s);
 }
 
-// Static solvers' operator of a uniform square Quad4 mesh in pair arithmetic (pcg.cu, learned.cu):
+// Element forces of a uniform square Quad4 mesh in pair arithmetic, FP64 in and out (the static
+// solvers' iterations, pcg.cu / learned.cu, and the explicit step in mixed arithmetic, dynamics.cu):
 // coef = d->pcg_pair as written by gfgpu_internal_pair_coef_square.
 int gfgpu_internal_pair_element_forces_f64(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                            cudaStream_t s)

@@ -72,7 +72,10 @@ class VelocityVerlet:
         one fused kernel per increment on a Mesh::Quad4::Regular mesh of square elements with
         lumped-mass classes, an element kernel (square closed form or stored element stiffness)
         and a dof-CSR node kernel on any other Quad4 mesh; agreement with the FP64 path ~1e-14 per
-        increment. Hex8 meshes raise with "pair".
+        increment. Hex8 meshes raise with "pair". "mixed" (uniform square Quad4 meshes): the FP64
+        state and node kernels, the element forces from the pair closed form on node differences
+        formed in FP64 (gfgpu_pcg_precompute_pair), so that an applied affine displacement
+        cancels as in FP64.
     """
 
     def __init__(self, coor, conn, dofs, K, G, rho=1.0, dt=None, eta=0.0, iip=None, fext=None,
@@ -154,8 +157,10 @@ class VelocityVerlet:
         self.coef_pair = None
         if arithmetic == "pair":
             self.use_pair()
+        elif arithmetic == "mixed":
+            self.use_mixed()
         elif arithmetic != "fp64":
-            raise ValueError("arithmetic must be 'fp64' or 'pair'")
+            raise ValueError("arithmetic must be 'fp64', 'pair' or 'mixed'")
         self._alloc_ws()
 
     def _alloc_ws(self):
@@ -179,10 +184,24 @@ class VelocityVerlet:
     def use_fp64(self):
         """FP64 kernels (the default)."""
         self.desc.coef_pair = None
+        self.desc.pcg_pair = None
+
+    def use_mixed(self):
+        """FP64 state and node kernels with the element forces of the pair closed form (uniform
+        square Quad4 meshes; strict mode ignores it)."""
+        self.use_fp64()
+        n = int(_lib.lib().gfgpu_pcg_pair_coef_floats(C.addressof(self.desc)))
+        if n == 0 or self.desc.nne != 4:
+            raise RuntimeError("mixed arithmetic needs a uniform square Quad4 mesh")
+        self.coef_mixed = torch.empty(n, dtype=torch.float32, device=_dev.device())
+        _lib.call("gfgpu_pcg_precompute_pair", C.addressof(self.desc), self.coef_mixed.data_ptr(),
+                  _dev.stream())
 
     @property
     def arithmetic(self):
-        return "pair" if self.desc.coef_pair else "fp64"
+        if self.desc.coef_pair:
+            return "pair"
+        return "mixed" if self.desc.pcg_pair else "fp64"
 
     @property
     def uniform(self):
@@ -235,6 +254,8 @@ class VelocityVerlet:
             return "general-pair" if self.desc.coef_pair else "general"
         if self.desc.coef_pair:
             return {1: "uniform-square-pair", 2: "uniform-square-pair-csr"}.get(self.desc.pair_mode, "general-pair")
+        if self.desc.pcg_pair and self.desc.nne == 4:
+            return "uniform-square-mixed"
         if self.desc.coef:
             return "uniform-square" if self.desc.nne == 4 else "uniform-cube"
         return "uniform"

@@ -371,14 +371,17 @@ typedef struct {
      * square-element fused tile kernel, 2 = element kernel + dof-CSR node kernel with the square
      * closed form, 3 = the same with stored element stiffness matrices */
     int32_t pair_mode;
-    /* optional float-float coefficients of the static solvers' operator (gfgpu_pcg_precompute_pair)
-     * on a Regular cube Hex8 mesh (per element {lam.h, lam.l, G.h, G.l}) or a uniform square Quad4
-     * mesh ({L, N} pairs [nelem] then kH pairs [nelem]). When set, the iterations of
-     * gfgpu_pcg_solve / gfgpu_pcg_iterate (and, on Quad4, of the flexible CG gfgpu_fcg_*) apply the
-     * stiffness of their search directions in pair arithmetic (~48-bit significands, ~1e-13
-     * relative to the FP64 action); the solution, the residual, the preconditioned residual, the
-     * direction and every dot product stay FP64, and the initial and final (true) residuals use the
-     * FP64 operator. NULL = FP64 operator. */
+    /* optional float-float coefficients of the element operator with FP64 state
+     * (gfgpu_pcg_precompute_pair) on a Regular cube Hex8 mesh (per element {lam.h, lam.l, G.h,
+     * G.l}) or a uniform square Quad4 mesh ({L, N} pairs [nelem] then kH pairs [nelem]). When set,
+     * the iterations of gfgpu_pcg_solve / gfgpu_pcg_iterate (and, on Quad4, of the flexible CG
+     * gfgpu_fcg_*) apply the stiffness of their search directions in pair arithmetic (~48-bit
+     * significands, ~1e-13 relative to the FP64 action); the solution, the residual, the
+     * preconditioned residual, the direction and every dot product stay FP64, and the initial and
+     * final (true) residuals use the FP64 operator. On a uniform square Quad4 mesh with coef_pair
+     * NULL, gfgpu_verlet_step in fast mode also takes its element forces from the pair kernel
+     * ("mixed" arithmetic: the node differences formed in FP64, the closed form on pairs, the forces
+     * and the whole state and node update in FP64). NULL = FP64 operator. */
     const float* pcg_pair;
 } gfgpu_verlet_desc;
 

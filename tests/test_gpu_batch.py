@@ -34,9 +34,10 @@ def _split(bv, x):
     return [x[o:o + n] for o, n in bv.offsets]
 
 
-def _alone(gf, inst, dt, nsteps):
+def _alone(gf, inst, dt, nsteps, arithmetic="fp64"):
     m = inst.mesh
-    vv = gf.VelocityVerlet(m.coor(), m.conn(), m.dofsPeriodic(), inst.K, inst.G, dt=dt, eta=0.1)
+    vv = gf.VelocityVerlet(m.coor(), m.conn(), m.dofsPeriodic(), inst.K, inst.G, dt=dt, eta=0.1,
+                           arithmetic=arithmetic)
     u = torch.tensor(inst.initial_displacement(), device="cuda")
     v = torch.zeros_like(u)
     a = torch.zeros_like(u)
@@ -44,7 +45,7 @@ def _alone(gf, inst, dt, nsteps):
     return to_np(u), to_np(v), to_np(a)
 
 
-@pytest.mark.parametrize("mode,block,bps", [(0, 256, 0), (1, 256, 0), (1, 128, 1)])
+@pytest.mark.parametrize("mode,block,bps", [(0, 256, 0), (1, 256, 0), (1, 128, 1), (3, 256, 0)])
 def test_batched_equals_instances_alone(gf, batch, mode, block, bps):
     B, inst, bv = batch
     bv.mode, bv.block, bv.bps = mode, block, bps
@@ -68,6 +69,26 @@ def test_batched_pair_equals_instances_alone_in_pairs(gf, batch):
         m = inst[k].mesh
         vv = gf.VelocityVerlet(m.coor(), m.conn(), m.dofsPeriodic(), inst[k].K, inst[k].G, dt=bv.dt, eta=0.1,
                                arithmetic="pair")
+        ua = torch.tensor(inst[k].initial_displacement(), device="cuda")
+        va, aa = torch.zeros_like(ua), torch.zeros_like(ua)
+        vv.step(ua, va, aa, 60)
+        assert np.array_equal(us, to_np(ua)) and np.array_equal(vs, to_np(va)) and np.array_equal(as_, to_np(aa))
+    bv.mode = 0
+
+
+def test_batched_mixed_equals_instances_alone_mixed(gf, batch):
+    """The mixed schedule (mode 3: FP64 state, pair element kernel on FP64 node differences) gives
+    each instance the bits of its own mixed run alone."""
+    B, inst, bv = batch
+    bv.mode = 3
+    u, v, a = bv.state()
+    bv.run_direct(u, v, a, 60)
+    torch.cuda.synchronize()
+    for k, (us, vs, as_) in enumerate(zip(_split(bv, u), _split(bv, v), _split(bv, a))):
+        m = inst[k].mesh
+        vv = gf.VelocityVerlet(m.coor(), m.conn(), m.dofsPeriodic(), inst[k].K, inst[k].G, dt=bv.dt, eta=0.1,
+                               arithmetic="mixed")
+        assert vv.arithmetic == "mixed" and vv.path == "uniform-square-mixed"
         ua = torch.tensor(inst[k].initial_displacement(), device="cuda")
         va, aa = torch.zeros_like(ua), torch.zeros_like(ua)
         vv.step(ua, va, aa, 60)
@@ -102,7 +123,7 @@ def test_batched_matches_oracle(gf, oracle, batch):
     assert rel_err(_split(bv, a)[k], ar) <= RTOL
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
 def test_graph_replay_equals_direct(gf, batch, mode):
     B, inst, bv = batch
     bv.mode, bv.block, bv.bps = mode, 256, 0
@@ -136,10 +157,52 @@ def test_grid_barrier_timeout_is_reported(gf):
     assert float((x * 2).sum()) == 2000.0
 
 
+def _oracle_run(R, inst, dt, nsteps):
+    m = inst.mesh
+    coor, conn, dofs = m.coor(), m.conn(), m.dofsPeriodic()
+    xr = R.as_element(conn, coor)
+    dNx, vol = R.compute_dN(xr, *R.quad4_gauss())
+    xin, win = R.quad4_nodal()
+    _, voln = R.compute_dN(xr, xin, win)
+    Nn, _ = R.shape(xin)
+    A = R.diag_assemble(conn, dofs, R.int_n_scalar_nt_dv(Nn, voln, np.ones((m.nelem(), 4)), 2))
+    ur = inst.initial_displacement()
+    vr = np.zeros_like(ur)
+    ar = np.zeros_like(ur)
+    R.verlet_run(conn, dofs, dNx, vol, inst.K, inst.G, A, np.ones(ur.size, dtype=np.uint8), None, dt,
+                 0.1, nsteps, ur, vr, ar)
+    return ur, vr, ar
+
+
+def test_mixed_is_as_close_to_the_reference_as_fp64(gf, oracle, batch):
+    """Mixed arithmetic (FP64 state and node update, pair element forces on FP64 node
+    differences) against the oracle's loop over 500 sheared increments: as close as the FP64 fast
+    path is. Both reassociate the reference's per-Gauss-point sums (closed form, lumped solve), and
+    with the displacement ~1e3 times its fluctuations the FP64 rounding of the stored state alone
+    moves v and a by ~1e-12 over 500 increments (measured: 1.0-1.4e-12 and 1.4-2.0e-12 for the
+    FP64 path on these instances); mixed stays within twice that, and one increment's forces
+    agree with the FP64 kernel to 1e-12."""
+    B, inst, bv = batch
+    R = oracle
+    for i in inst[:3]:
+        ref = _oracle_run(R, i, bv.dt, 500)
+        d64 = [rel_err(x, r) for x, r in zip(_alone(gf, i, bv.dt, 500), ref)]
+        dmx = [rel_err(x, r) for x, r in zip(_alone(gf, i, bv.dt, 500, "mixed"), ref)]
+        for a, b in zip(dmx, d64):
+            assert a <= 2.0 * b + 1e-13, (dmx, d64)
+        # one increment from the sheared initial state: the element forces agree
+        one64 = _alone(gf, i, bv.dt, 1)
+        onemx = _alone(gf, i, bv.dt, 1, "mixed")
+        assert rel_err(onemx[2], one64[2]) <= 1e-12
+
+
 def test_full_size_batch(gf):
     """The measured configuration: 256 seeded periodic instances (nx, ny ~ U{32..512}), 500
     increments in the autotuned schedule. A repeat gives identical bits, and eight instances picked
-    across the batch agree with the same instance run alone (1e-12)."""
+    across the batch give the bits of the same instance run alone in the schedule's arithmetic.
+    Against the FP64 kernels: 1e-12 for the FP64 schedules; for the mixed schedule 1e-10, the
+    spread the FP64 fast path itself shows against the reference algorithm at this size (see
+    test_mixed_is_as_close_to_the_reference_as_fp64)."""
     from goosefem_gb300 import batch as B
 
     inst = B.seeded_instances(256, 256)
@@ -154,7 +217,11 @@ def test_full_size_batch(gf):
     assert all(torch.equal(x, y) for x, y in zip(runs[0], runs[1]))
     assert torch.isfinite(runs[0][0]).all()
     us, vs, as_ = (_split(bv, x) for x in runs[0])
+    tol = 1e-10 if bv.arithmetic == "mixed" else RTOL
     for k in np.linspace(0, 255, 8).astype(int):
+        if bv.arithmetic == "mixed":
+            ua, va, aa = _alone(gf, inst[k], bv.dt, 500, "mixed")
+            assert np.array_equal(us[k], ua) and np.array_equal(vs[k], va) and np.array_equal(as_[k], aa)
         ur, vr, ar = _alone(gf, inst[k], bv.dt, 500)
-        assert rel_err(us[k], ur) <= RTOL and rel_err(vs[k], vr) <= RTOL
-        assert rel_err(as_[k], ar) <= RTOL
+        assert rel_err(us[k], ur) <= tol and rel_err(vs[k], vr) <= tol
+        assert rel_err(as_[k], ar) <= tol
