@@ -1101,12 +1101,22 @@ static int launch_elem(const gfgpu_verlet_desc* d, const double* u, double* fe, 
 int gfgpu_internal_pair_element_forces_f64(const gfgpu_verlet_desc* d, const double* u, double* fe,
                                            cudaStream_t s);
 
-// The explicit step's element kernel: in fast mode with d->pcg_pair set on a uniform square Quad4
-// mesh ("mixed" arithmetic: FP64 state and node update), the pair element kernel; else launch_elem.
+// one increment of mixed arithmetic with lumped-mass classes (verlet_pair.cu)
+int gfgpu_internal_mixed_increment(const gfgpu_verlet_desc* d, double* fe, int advance, double* u, double* v,
+                                   double* a, cudaStream_t s);
+
+// "Mixed" arithmetic: in fast mode with d->pcg_pair set on a uniform square Quad4 mesh, the FP64
+// state with the element forces of the pair closed form (on node differences formed in FP64).
+static bool mixed_arithmetic(const gfgpu_verlet_desc* d)
+{
+    return d->pcg_pair && !strict_mode() && d->uniform && d->nne == 4 && d->ndim == 2 && d->coef;
+}
+
+// The explicit step's element kernel: the pair element kernel (FP64 forces) in mixed arithmetic,
+// else launch_elem.
 static int launch_elem_step(const gfgpu_verlet_desc* d, const double* u, double* fe, cudaStream_t s)
 {
-    if (d->pcg_pair && !strict_mode() && d->uniform && d->nne == 4 && d->ndim == 2 && d->coef)
-        return gfgpu_internal_pair_element_forces_f64(d, u, fe, s);
+    if (mixed_arithmetic(d)) return gfgpu_internal_pair_element_forces_f64(d, u, fe, s);
     return launch_elem(d, u, fe, s);
 }
 
@@ -1200,9 +1210,17 @@ static int run_increments(const gfgpu_verlet_desc* d, double* u, double* v, doub
     else
         k_predict<false><<<gn, kBlock, 0, s>>>(u, v, a, n, k);
     GF_TRY(check_launch("verlet predict"));
+    // mixed arithmetic with lumped-mass classes: the element forces stay pairs and the node kernel
+    // takes the velocity estimates on pairs (4 FP64 instructions per free dof instead of 10)
+    const bool mixed_cls = mixed_arithmetic(d) && d->mclass && d->mclass_inv && d->ncls > 0;
     for (int64_t it = 0; it < nsteps; ++it) {
+        const int adv = it + 1 < nsteps ? 1 : 0;
+        if (mixed_cls) {
+            GF_TRY(gfgpu_internal_mixed_increment(d, fe, adv, u, v, a, s));
+            continue;
+        }
         GF_TRY(launch_elem_step(d, u, fe, s));
-        GF_TRY(launch_node(d, tab, k, fe, it + 1 < nsteps ? 1 : 0, u, v, a, s));
+        GF_TRY(launch_node(d, tab, k, fe, adv, u, v, a, s));
     }
     return GFGPU_OK;
 }

@@ -643,6 +643,9 @@ k_pair_elem_square(const int32_t* __restrict__ conn, const float4* __restrict__ 
 // to FP64 into fe [nelem, 4, 2] (the layout of k_elem_force_quad4_square that the FP64 gathers and
 // node kernels read): 16 FP64 instructions per element instead of 34. Forming the differences in
 // FP64 keeps the pair rounding relative to them: an applied affine displacement cancels as in FP64.
+// PAIR_OUT: the forces stay pairs, normalised, fe [nelem, 4] of float4 {x.h, x.l, y.h, y.l} (8 bytes
+// per value like the FP64 layout; the mixed node kernel gathers them).
+template <bool PAIR_OUT>
 __global__ void __launch_bounds__(256)
 k_pair_elem_square_f64(const int32_t* __restrict__ conn, const double2* __restrict__ u,
                        const float4* __restrict__ cLN, const float2* __restrict__ cH, int64_t nelem,
@@ -659,11 +662,98 @@ k_pair_elem_square_f64(const int32_t* __restrict__ conn, const double2* __restri
                           ff_from_double(q2.x - q3.x), ff_from_double(q2.y - q3.y), lo2(cln), hi2(cln),
                           pf(__ldg(cH + e)), S, D, H);
         const ffv Sx = lo2(S), Sy = hi2(S), Dx = lo2(D), Dy = hi2(D), H0 = lo2(H), H1 = hi2(H);
-        double2* o = fe + e * 4;
-        o[0] = make_double2(ff_to_double(ff_sub(H0, Sx)), ff_to_double(ff_sub(H1, Sy)));
-        o[1] = make_double2(ff_to_double(ff_sub(Dx, H0)), ff_to_double(ff_sub(Dy, H1)));
-        o[2] = make_double2(ff_to_double(ff_add(Sx, H0)), ff_to_double(ff_add(Sy, H1)));
-        o[3] = make_double2(ff_to_double(ff_neg(ff_add(Dx, H0))), ff_to_double(ff_neg(ff_add(Dy, H1))));
+        const ffv f[8] = {ff_sub(H0, Sx), ff_sub(H1, Sy), ff_sub(Dx, H0), ff_sub(Dy, H1),
+                          ff_add(Sx, H0), ff_add(Sy, H1), ff_neg(ff_add(Dx, H0)), ff_neg(ff_add(Dy, H1))};
+        if constexpr (PAIR_OUT) {
+            float4* o = reinterpret_cast<float4*>(fe) + e * 4;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) o[m] = pack(ff_norm(f[2 * m]), ff_norm(f[2 * m + 1]));
+        }
+        else {
+            double2* o = fe + e * 4;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) o[m] = make_double2(ff_to_double(f[2 * m]), ff_to_double(f[2 * m + 1]));
+        }
+    }
+}
+
+// The node update of mixed arithmetic (FP64 state, pair element forces from
+// k_pair_elem_square_f64<true>): a dof's pair forces gathered in the CSR's order (or by index
+// arithmetic on a Regular numbering, the same order), the closed form of the three velocity
+// estimates with the lumped-mass class's coefficients on pairs (v and a split from FP64 on the
+// integer pipe), v' and a' returned to FP64, and the predictor u + dt v' + c a' in FP64 as in
+// k_verlet_node_cls. 4 FP64 instructions per free dof instead of 10; prescribed dofs as there.
+struct MixedNodeStep {
+    const int32_t *dofs, *ptr, *idx;
+    const uint8_t* mclass;
+    const float2* fe; // [nelem * nne * ndim] pair element forces
+    const double* fext;
+    double *u, *v, *a;
+    int64_t n, reg_nx, reg_ny;
+    double dt, h, c;
+    int advance;
+};
+
+__global__ void __launch_bounds__(256)
+k_mixed_node(const MixedNodeStep p, const __grid_constant__ PairClassTab tab)
+{
+    __shared__ float2 smi[GFGPU_MASS_CLASSES], sbe[GFGPU_MASS_CLASSES], sc1[GFGPU_MASS_CLASSES],
+        sc2[GFGPU_MASS_CLASSES], sc3[GFGPU_MASS_CLASSES];
+    if (threadIdx.x < GFGPU_MASS_CLASSES) {
+        const int c = threadIdx.x;
+        smi[c] = tab.mi[c];
+        sbe[c] = tab.be[c];
+        sc1[c] = tab.c1[c];
+        sc2[c] = tab.c2[c];
+        sc3[c] = tab.c3[c];
+    }
+    __syncthreads();
+    GF_FOR(t, p.n)
+    {
+        ffv f = ff_make(0.f, 0.f);
+        if (p.reg_nx > 0) {
+            const uint32_t nx = static_cast<uint32_t>(p.reg_nx), ny = static_cast<uint32_t>(p.reg_ny);
+            const uint32_t tt = static_cast<uint32_t>(t), node = tt >> 1, i = tt & 1u, W = nx + 1u;
+            const uint32_t iy = node / W, ix = node - iy * W;
+            bool first = true;
+            auto add = [&](uint32_t e, uint32_t m) {
+                const ffv g = pf(__ldg(p.fe + (e * 4u + m) * 2u + i));
+                f = first ? g : ff_add(f, g);
+                first = false;
+            };
+            if (iy > 0u && ix > 0u) add((iy - 1u) * nx + ix - 1u, 2u);
+            if (iy > 0u && ix < nx) add((iy - 1u) * nx + ix, 3u);
+            if (iy < ny && ix > 0u) add(iy * nx + ix - 1u, 1u);
+            if (iy < ny && ix < nx) add(iy * nx + ix, 0u);
+        }
+        else {
+            const int32_t d = __ldg(p.dofs + t);
+            const int32_t b = __ldg(p.ptr + d), en = __ldg(p.ptr + d + 1);
+            for (int32_t j = b; j < en; ++j) {
+                const ffv g = pf(__ldg(p.fe + __ldg(p.idx + j)));
+                f = j == b ? g : ff_add(f, g);
+            }
+        }
+        const int c = __ldg(p.mclass + t);
+        const double vn = p.v[t], an = p.a[t];
+        double vv, aa;
+        if (c < GFGPU_MASS_CLASSES) {
+            const ffv R = p.fext ? ff_sub(ff_from_double(__ldg(p.fext + t)), f) : ff_neg(f);
+            const ffv mR = ff_mul(pf(smi[c]), R);
+            const ffv V = ff_add(ff_add(ff_mul(pf(sc1[c]), ff_from_double(vn)), ff_mul(pf(sc2[c]), ff_from_double(an))),
+                                 ff_mul(pf(sc3[c]), mR));
+            const ffv Vn = ff_norm(V);
+            const ffv Ac = ff_sub(mR, ff_mul(pf(sbe[c]), Vn));
+            vv = ff_to_double(Vn);
+            aa = ff_to_double(Ac);
+        }
+        else {
+            aa = an;
+            vv = fma(p.h, an + an, vn);
+        }
+        p.v[t] = vv;
+        p.a[t] = aa;
+        if (p.advance) p.u[t] = fma(p.c, aa, fma(p.dt, vv, p.u[t]));
     }
 }
 
@@ -678,7 +768,10 @@ k_pair_elem_stiff(const int32_t* __restrict__ conn, const float4* __restrict__ u
         ffv f[8];
         bool first[8];
 #pragma unroll
-        for (int r = 0; r < 8; ++r) first[r] = true;
+        for (int r = 0; r < 8; ++r) {
+            f[r] = ff_make(0.f, 0.f);
+            first[r] = true;
+        }
         auto acc = [&](int r, ffv t) {
             f[r] = first[r] ? t : ff_add(f[r], t);
             first[r] = false;
@@ -873,6 +966,23 @@ static float2 split_host(double x)
     return make_float2(h, static_cast<float>(x - static_cast<double>(h)));
 }
 
+// the pair class coefficients of a descriptor's lumped-mass classes (those of k_verlet_node_cls)
+static PairClassTab pair_class_tab(const gfgpu_verlet_desc* d)
+{
+    const double dt = d->dt, h = 0.5 * dt;
+    PairClassTab tab{};
+    for (int k = 0; k < d->ncls; ++k) {
+        const double mi = d->mclass_inv[k], be = mi * d->eta, omh = 1.0 - h * be;
+        tab.mi[k] = split_host(mi);
+        tab.be[k] = split_host(be);
+        tab.c1[k] = split_host(omh + h * h * be * be);
+        tab.c2[k] = split_host(h * omh + h * h * be * be * dt);
+        tab.c3[k] = split_host(h * omh);
+    }
+    return tab;
+}
+
+
 // The pair path applies to: uniform square Quad4 elements (coefficients), Mesh::Quad4::Regular
 // numbering with plain dofs (verified on the device), lumped-mass classes.
 static int pair_applicable(const gfgpu_verlet_desc* d, std::string* why)
@@ -1051,16 +1161,7 @@ static int pair_increments(const gfgpu_verlet_desc* d, int64_t first, int64_t co
     float4* const* ub = ps.ub;
     float4 *pv = ps.v, *pa = ps.a, *pfx = ps.fext;
     const double dt = d->dt, h = 0.5 * dt, c = 0.5 * std::pow(dt, 2.0);
-    PairClassTab tab{};
-    for (int k = 0; k < d->ncls; ++k) {
-        // the coefficients of k_verlet_node_cls (MassClassTab), as pairs
-        const double mi = d->mclass_inv[k], be = mi * d->eta, omh = 1.0 - h * be;
-        tab.mi[k] = split_host(mi);
-        tab.be[k] = split_host(be);
-        tab.c1[k] = split_host(omh + h * h * be * be);
-        tab.c2[k] = split_host(h * omh + h * h * be * be * dt);
-        tab.c3[k] = split_host(h * omh);
-    }
+    const PairClassTab tab = pair_class_tab(d);
     if (d->pair_mode != 1) {
         float4* fe = pair_fe(d, workspace);
         PairCsrStep q;
@@ -1188,10 +1289,41 @@ int gfgpu_internal_pair_element_forces_f64(const gfgpu_verlet_desc* d, const dou
 {
     if (d->nelem == 0) return GFGPU_OK;
     const float* c = d->pcg_pair;
-    k_pair_elem_square_f64<<<grid_for(d->nelem), 256, 0, s>>>(
+    k_pair_elem_square_f64<false><<<grid_for(d->nelem), 256, 0, s>>>(
         d->conn, reinterpret_cast<const double2*>(u), reinterpret_cast<const float4*>(c),
         reinterpret_cast<const float2*>(c + 4 * d->nelem), d->nelem, reinterpret_cast<double2*>(fe));
     return check_launch("pair element kernel (static operator)");
+}
+
+// One increment of mixed arithmetic after the FP64 predictor (dynamics.cu): the pair element
+// forces into fe (8 bytes per value) and the mixed node kernel; needs lumped-mass classes.
+int gfgpu_internal_mixed_increment(const gfgpu_verlet_desc* d, double* fe, int advance, double* u, double* v,
+                                   double* a, cudaStream_t s)
+{
+    const float* c = d->pcg_pair;
+    k_pair_elem_square_f64<true><<<grid_for(d->nelem), 256, 0, s>>>(
+        d->conn, reinterpret_cast<const double2*>(u), reinterpret_cast<const float4*>(c),
+        reinterpret_cast<const float2*>(c + 4 * d->nelem), d->nelem, reinterpret_cast<double2*>(fe));
+    GF_TRY(check_launch("pair element kernel (mixed)"));
+    MixedNodeStep q;
+    q.dofs = d->dofs;
+    q.ptr = d->csr_ptr;
+    q.idx = d->csr_idx;
+    q.mclass = d->mclass;
+    q.fe = reinterpret_cast<const float2*>(fe);
+    q.fext = d->fext;
+    q.u = u;
+    q.v = v;
+    q.a = a;
+    q.n = d->nnode * d->ndim;
+    q.reg_nx = (d->reg_nz == 0 && d->nne == 4) ? d->reg_nx : 0;
+    q.reg_ny = d->reg_ny;
+    q.dt = d->dt;
+    q.h = 0.5 * d->dt;
+    q.c = 0.5 * std::pow(d->dt, 2.0);
+    q.advance = advance;
+    k_mixed_node<<<grid_for(q.n), 256, 0, s>>>(q, pair_class_tab(d));
+    return check_launch("mixed node kernel");
 }
 
 // {L, N} [nelem] interleaved pairs, then kH [nelem] (6 floats per element) of a uniform square Quad4

@@ -379,9 +379,10 @@ typedef struct {
      * significands, ~1e-13 relative to the FP64 action); the solution, the residual, the
      * preconditioned residual, the direction and every dot product stay FP64, and the initial and
      * final (true) residuals use the FP64 operator. On a uniform square Quad4 mesh with coef_pair
-     * NULL, gfgpu_verlet_step in fast mode also takes its element forces from the pair kernel
-     * ("mixed" arithmetic: the node differences formed in FP64, the closed form on pairs, the forces
-     * and the whole state and node update in FP64). NULL = FP64 operator. */
+     * NULL, gfgpu_verlet_step in fast mode also runs in "mixed" arithmetic: FP64 state, the element
+     * forces from the pair closed form on node differences formed in FP64 and, with lumped-mass
+     * classes, the three velocity estimates on pairs (v and a split from FP64, v' and a' returned to
+     * FP64) and the predictor in FP64; without classes the FP64 node kernel. NULL = FP64 operator. */
     const float* pcg_pair;
 } gfgpu_verlet_desc;
 
