@@ -755,8 +755,8 @@ def workload_batch(args):
     seq = B.run_sequential(inst, nsteps, bv.dt, arithmetic=bv.arithmetic)
     res = {"metric": "elem-Gauss-pt updates/s (batched)", "value": bv.nelem * 4 * nsteps / sec,
            "unit": "elem-Gauss-pt/s", "higher_is_better": True,
-           "dtype": ("f64 state and node update, float-float (f32 pair) element forces"
-                     if bv.mode == 3 else "f64"),
+           "dtype": ("f64 state and predictor, float-float (f32 pair) element forces and "
+                     "velocity estimates" if bv.mode == 3 else "f64"),
            "data": "synthetic (seeded)",
            "config": {"workload": f"{len(inst)} periodic Quad4 Regular instances, nx,ny~U{{32..512}},"
                                   f" {nsteps} increments, applied shear 1e-3",
@@ -764,14 +764,15 @@ def workload_batch(args):
                       "schedule": {"mode": ["graph of 2 FP64 kernels", "persistent FP64 kernel",
                                             "graph of 2 pair kernels",
                                             "graph of the mixed element kernel (pair closed form on "
-                                            "FP64 node differences) + the FP64 node kernel"][bv.mode],
+                                            "FP64 node differences) + the mixed node kernel"][bv.mode],
                                    "block": bv.block, "blocks_per_sm": bv.bps},
                       "colouring": "none: the node kernels gather through the dof CSR "
                                    "(deterministic, no scatter conflicts to colour)"},
            "seconds": sec, "ms_per_increment": 1e3 * sec / nsteps,
            "max_rel_dev_vs_fp64": dev,
-           "accuracy_note": ("mixed: FP64 state and node update, pair element forces on FP64 node "
-                             "differences; over 500 sheared increments it is as close to the reference "
+           "accuracy_note": ("mixed: FP64 state and predictor, pair element forces on FP64 node "
+                             "differences and pair velocity estimates; over 500 sheared increments it "
+                             "is as close to the reference "
                              "algorithm as the FP64 fast path is (both ~1e-12 on 24-40^2 instances; "
                              "tests/test_gpu_batch.py), the deviation above is the two arithmetics' "
                              "shared spread" if bv.mode == 3 else None),
