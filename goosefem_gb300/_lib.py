@@ -37,7 +37,7 @@ class VerletDesc(C.Structure):
         ("mclass", C.c_void_p), ("mclass_inv", C.c_void_p), ("ncls", C.c_int32),
         ("reg_nx", C.c_int64), ("reg_ny", C.c_int64), ("reg_nz", C.c_int64),
         ("coef_pair", C.c_void_p), ("pair_mode", C.c_int32),
-        ("pcg_pair", C.c_void_p),
+        ("pcg_pair", C.c_void_p), ("ell", C.c_void_p),
     ]
 
 

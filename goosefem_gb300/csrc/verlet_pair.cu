@@ -68,6 +68,19 @@ __device__ __forceinline__ ffv px_(float4 q) { return ff_make(q.x, q.z); }
 __device__ __forceinline__ ffv py_(float4 q) { return ff_make(q.y, q.w); }
 __device__ __forceinline__ float4 ppack(ffv x, ffv y) { return make_float4(x.h, y.h, x.l, y.l); }
 
+// pair sum of a nodevec entry's element forces through the gather table (the CSR's entries and
+// order; -1 pads): the first term assigned, the others added, as the CSR loop does
+__device__ __forceinline__ ffv gather_ell_pair(const int4* __restrict__ ell, const float2* __restrict__ fe,
+                                               int64_t t)
+{
+    const int4 q = __ldg(ell + t);
+    ffv f = q.x >= 0 ? pf(__ldg(fe + q.x)) : ff_make(0.f, 0.f);
+    if (q.y >= 0) f = ff_add(f, pf(__ldg(fe + q.y)));
+    if (q.z >= 0) f = ff_add(f, pf(__ldg(fe + q.z)));
+    if (q.w >= 0) f = ff_add(f, pf(__ldg(fe + q.w)));
+    return f;
+}
+
 // element (ex, ey) of a square-element Regular mesh with per-element L = lam/4, N = G/4 (M = 2N)
 // and kH = g^2 (lam + 3G)/4: the sums S = P0 + P1, D = P0 - P1 (x) and P1 + Q1, P1 - Q1 (y) and
 // the hourglass terms H, from which the element forces are (H - S, D - H, S + H, -(D + H)) at
@@ -690,6 +703,7 @@ struct MixedNodeStep {
     const double* fext;
     double *u, *v, *a;
     int64_t n, reg_nx, reg_ny;
+    const int4* ell;
     double dt, h, c;
     int advance;
 };
@@ -725,6 +739,9 @@ k_mixed_node(const MixedNodeStep p, const __grid_constant__ PairClassTab tab)
             if (iy > 0u && ix < nx) add((iy - 1u) * nx + ix, 3u);
             if (iy < ny && ix > 0u) add(iy * nx + ix - 1u, 1u);
             if (iy < ny && ix < nx) add(iy * nx + ix, 0u);
+        }
+        else if (p.ell) {
+            f = gather_ell_pair(p.ell, p.fe, t);
         }
         else {
             const int32_t d = __ldg(p.dofs + t);
@@ -808,7 +825,9 @@ struct PairCsrStep {
     // Mesh::Quad4::Regular(reg_nx, reg_ny) numbering with plain dofs (gfgpu_verlet_detect_regular):
     // a dof's element forces found by index arithmetic in the CSR's order (same bits, no tables)
     int64_t reg_nx, reg_ny;
+    const int4* ell; // else, when set: the CSR entries per nodevec entry (gfgpu_verlet_build_ell)
 };
+
 
 __global__ void __launch_bounds__(256)
 k_pair_node_csr(const PairCsrStep p, const __grid_constant__ PairClassTab tab)
@@ -844,6 +863,9 @@ k_pair_node_csr(const PairCsrStep p, const __grid_constant__ PairClassTab tab)
             if (iy > 0u && ix < nx) add((iy - 1u) * nx + ix, 3u);
             if (iy < ny && ix > 0u) add(iy * nx + ix - 1u, 1u);
             if (iy < ny && ix < nx) add(iy * nx + ix, 0u);
+        }
+        else if (p.ell) {
+            f = gather_ell_pair(p.ell, p.fe, t);
         }
         else {
             const int32_t d = __ldg(p.dofs + t);
@@ -1167,6 +1189,7 @@ static int pair_increments(const gfgpu_verlet_desc* d, int64_t first, int64_t co
         PairCsrStep q;
         q.reg_nx = (d->reg_nz == 0 && d->nne == 4) ? d->reg_nx : 0;
         q.reg_ny = d->reg_ny;
+        q.ell = reinterpret_cast<const int4*>(d->ell);
         q.dofs = d->dofs;
         q.ptr = d->csr_ptr;
         q.idx = d->csr_idx;
@@ -1318,6 +1341,7 @@ int gfgpu_internal_mixed_increment(const gfgpu_verlet_desc* d, double* fe, int a
     q.n = d->nnode * d->ndim;
     q.reg_nx = (d->reg_nz == 0 && d->nne == 4) ? d->reg_nx : 0;
     q.reg_ny = d->reg_ny;
+    q.ell = reinterpret_cast<const int4*>(d->ell);
     q.dt = d->dt;
     q.h = 0.5 * d->dt;
     q.c = 0.5 * std::pow(d->dt, 2.0);

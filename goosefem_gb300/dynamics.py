@@ -152,8 +152,10 @@ class VelocityVerlet:
                       _dev.stream())
             d.coef = self.coef.data_ptr()
         self.classify()
+        self._ell = None
         if nne == 4:
-            self._detect_regular(conn_h)
+            if not self._detect_regular(conn_h):
+                self._build_ell()
         self.coef_pair = None
         if arithmetic == "pair":
             self.use_pair()
@@ -235,11 +237,24 @@ class VelocityVerlet:
                       self.desc.nelem // nx, _dev.stream())
         return self.desc.reg_nx > 0
 
+    def _build_ell(self):
+        """The node kernels' gather table (gfgpu_verlet_build_ell): at most 4 element
+        contributions per dof; same entries and order as the dof CSR, one 16-byte load."""
+        n = self.desc.nnode * self.desc.ndim
+        t = torch.empty(max(n, 1) * 4, dtype=torch.int32, device=_dev.device())
+        try:
+            _lib.call("gfgpu_verlet_build_ell", C.addressof(self.desc), t.data_ptr(), _dev.stream())
+            self._ell = t
+        except _lib.GFGPUError:
+            self.desc.ell = None
+
     def use_csr_gather(self):
-        """Node kernel through the dof CSR even on a Regular mesh (FP64 kernels)."""
+        """Node kernel through the dof CSR even on a Regular mesh, without the gather table (FP64
+        kernels)."""
         self.use_fp64()
         self.desc.reg_nx = 0
         self.desc.reg_ny = 0
+        self.desc.ell = None
 
     def use_per_dof_mass(self):
         """Node update with the inverse mass read per dof (no mass classes; FP64 kernels)."""

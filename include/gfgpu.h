@@ -384,6 +384,13 @@ typedef struct {
      * classes, the three velocity estimates on pairs (v and a split from FP64, v' and a' returned to
      * FP64) and the predictor in FP64; without classes the FP64 node kernel. NULL = FP64 operator. */
     const float* pcg_pair;
+    /* optional gather table of the node kernels (gfgpu_verlet_build_ell): for nodevec entry t the
+     * flat elemvec indices of its dof's element contributions in the dof CSR's order,
+     * ell[4 t + k], padded with -1 (at most 4 per dof: Quad4 meshes, periodic ties included).
+     * When set and no Regular numbering applies, the class, pair and mixed node kernels read it
+     * instead of dofs / csr_ptr / csr_idx: one dependent load of 16 bytes instead of three
+     * levels (same order, same bits). NULL = the CSR. */
+    const int32_t* ell;
 } gfgpu_verlet_desc;
 
 #define GFGPU_MASS_CLASSES 16
@@ -468,6 +475,10 @@ int gfgpu_verlet_classify(gfgpu_verlet_desc* d, uint8_t* mclass, double* mclass_
  * dofs = arange(nnode * 2) (no periodic ties); on success sets d->reg_nx, d->reg_ny, else leaves
  * them 0. Needs only d's sizes, conn and dofs. Returns GFGPU_OK either way. Synchronises. */
 int gfgpu_verlet_detect_regular(gfgpu_verlet_desc* d, int64_t nx, int64_t ny, gfgpu_stream_t stream);
+/* Fill ell [nnode * ndim * 4] (16-byte aligned) from d->dofs, csr_ptr, csr_idx and set d->ell = ell
+ * when every dof has at most 4 element contributions; else leave d->ell unchanged and return
+ * GFGPU_ERR_UNSUPPORTED. Synchronises. */
+int gfgpu_verlet_build_ell(gfgpu_verlet_desc* d, int32_t* ell, gfgpu_stream_t stream);
 /* The same for MeshHex8.h:77-130's Regular(nx, ny, nz) connectivity with dofs = arange(nnode * 3):
  * sets d->reg_nx, reg_ny, reg_nz on success (used by the static solvers' gather; the explicit
  * step's node kernels are Quad4 only). Returns GFGPU_OK either way. Synchronises. */

@@ -96,6 +96,26 @@ def test_batched_mixed_equals_instances_alone_mixed(gf, batch):
     bv.mode = 0
 
 
+@pytest.mark.parametrize("mode", [0, 2, 3])
+def test_gather_table_same_bits_as_csr(gf, batch, mode):
+    """The node kernels' gather table (periodic ties: 4 contributions per dof) gives the bits of
+    the dof CSR in the FP64, pair and mixed schedules."""
+    B, inst, bv = batch
+    assert bv.vv.desc.ell and bv.vv.desc.reg_nx == 0
+    bv.mode = mode
+    out = []
+    for ell in (bv.vv.desc.ell, None):
+        bv.vv.desc.ell = ell
+        u, v, a = bv.state()
+        bv.run_direct(u, v, a, 30)
+        torch.cuda.synchronize()
+        out.append((u, v, a))
+    bv.vv.desc.ell = bv.vv._ell.data_ptr()
+    for x, y in zip(*out):
+        assert torch.equal(x, y)
+    bv.mode = 0
+
+
 def test_batched_matches_oracle(gf, oracle, batch):
     """One instance of the batch against the oracle's loop (periodic dofs, applied shear)."""
     B, inst, bv = batch
