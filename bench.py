@@ -12,9 +12,12 @@ updates per second (nelem x 4 Gauss points x increments / s).
 
 The default single-GPU run also measures, under "workloads" in the same JSON line:
   static   Hex8 128^3 matrix-free Jacobi-PCG to 1e-8 (vs the oracle's matvec on the host cores),
-  batch    256 periodic Quad4 instances x 500 increments (vs the instances one at a time),
+           the iterations' stiffness action in float-float pairs and in FP64 (--static-operator),
+  batch    256 periodic Quad4 instances x 500 increments in the autotuned schedule (FP64 graph,
+           persistent kernel or mixed arithmetic) vs the instances one at a time,
   learned  Quad4 512^2 two-phase static solve to 1e-8: learned two-level FCG and the one-level
-           learned FCG (network trained on 4096 Jacobi-PCG pairs) vs Jacobi-PCG on the same GPU.
+           learned FCG (network trained on 4096 Jacobi-PCG pairs) vs Jacobi-PCG on the same GPU,
+           every solver with the pair stiffness action (FP64 with --static-operator fp64).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gfgpu|reference]
                   [--workload explicit|static|batch|learned] [--no-workloads]
