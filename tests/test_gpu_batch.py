@@ -245,3 +245,19 @@ def test_full_size_batch(gf):
         ur, vr, ar = _alone(gf, inst[k], bv.dt, 500)
         assert rel_err(us[k], ur) <= tol and rel_err(vs[k], vr) <= tol
         assert rel_err(as_[k], ar) <= tol
+
+
+def test_gather_table_refuses_more_than_four(gf):
+    """A Hex8 mesh (8 element contributions per interior dof) gets no gather table: the builder
+    refuses and leaves the descriptor on the CSR."""
+    import ctypes as C
+
+    from goosefem_gb300 import _dev, _lib
+
+    m = gf.Mesh.Hex8.Regular(3, 3, 3)
+    K = np.ones(27)
+    vv = gf.VelocityVerlet(m.coor(), m.conn(), m.dofs(), K, 0.5 * K, dt=0.01)
+    t = torch.empty(m.nnode() * 3 * 4, dtype=torch.int32, device="cuda")
+    with pytest.raises(gf.GFGPUError) as ei:
+        _lib.call("gfgpu_verlet_build_ell", C.addressof(vv.desc), t.data_ptr(), _dev.stream())
+    assert ei.value.code == -7 and not vv.desc.ell
